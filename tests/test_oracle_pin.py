@@ -1,0 +1,156 @@
+"""Pin the CPU oracle against golden vectors produced by the upstream library.
+
+The fixtures under tests/golden/ were written by tests/golden/make_golden.py,
+which drives the upstream C library itself.  The oracle follows the upstream
+loop order, so agreement is expected to the last few ulps (1e-13 relative).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, name + ".npz")))
+
+
+def rel(a, b, floor=1.0):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if a.size else 0.0
+
+
+@pytest.mark.parametrize("name", ["mf", "rbm", "rbm_big", "crbm", "crbm_big"])
+def test_ansatz_init_logamp_gradients(name):
+    d = load("ansatz_" + name)
+    kind, N, M = int(d["kind"]), int(d["N"]), int(d["M"])
+    p = O.init_params(kind, N, M, float(d["scale"]), int(d["seed"]))
+    assert np.array_equal(p, d["params"])                       # bit-exact initialisation
+    amp = O.Amp(kind, N, M, p)
+    la, ar = O.log_amp(amp, d["spins"])
+    assert rel(la, d["la"]) < 1e-13
+    assert rel(ar, d["arg"]) < 1e-13
+    assert rel(O.gradient(amp, d["spins"]), d["grad"]) < 1e-13
+    gr, gi = O.gradient_complex(amp, d["spins"])
+    assert rel(gr, d["grad_re"]) < 1e-13 and rel(gi, d["grad_im"]) < 1e-13
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "eloc_*.npz"))))
+def test_local_energy(path):
+    d = dict(np.load(path))
+    layers = [("marshall", int(d["Lx"]), int(d["Ly"]))] if int(d["marshall"]) else []
+    amp = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params"], layers)
+    h = O.ham(int(d["ham"]), int(d["Lx"]), int(d["Ly"]), 0, int(d["kagome_pbc"]),
+              float(d["J"]), float(d["J2"]), float(d["Jz"]), float(d["Gamma"]))
+    re, im = O.local_energy(h, amp, d["spins"], complex_out=True)
+    assert rel(re, d["E"]) < 1e-12
+    assert rel(re, d["E_re"]) < 1e-12
+    assert rel(im, d["E_im"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["rbm16", "crbm16_marshall"])
+def test_xorshift_sampler_sequence(name):
+    d = load("sampler_" + name)
+    layers = [("marshall", 4, 4)] if int(d["marshall"]) else []
+    amp = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params"], layers)
+    out, acc = O.xorshift_sampler(amp, int(d["seed"]), int(d["therm"]), int(d["decor"]),
+                                  d["batch"].shape[0])
+    assert np.array_equal(out, d["batch"])                        # identical Markov chain
+    assert acc == pytest.approx(float(d["acceptance"]), abs=0)
+
+
+@pytest.mark.parametrize("name", ["minsr_tfim_rbm", "minsr_heis_crbm_marshall", "cg_tfim_rbm",
+                                  "cg_j1j2_crbm"])
+def test_sr_step_on_reference_batch(name):
+    d = load("sr_" + name)
+    layers = [("marshall", int(d["Lx"]), int(d["Ly"]))] if int(d["marshall"]) else []
+    amp = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params0"].copy(), layers)
+    h = O.ham(int(d["ham"]), int(d["Lx"]), int(d["Ly"]), 0, 1, float(d["J"]), float(d["J2"]),
+              1.0, float(d["Gamma"]))
+    if str(d["solver"]) == "minsr":
+        E, delta, info = O.minsr_step(h, amp, d["batch"], float(d["shift"]), float(d["lr"]))
+    else:
+        E, delta, info = O.cgsr_step(h, amp, d["batch"], float(d["shift"]), float(d["lr"]),
+                                     int(d["cg_max"]), float(d["cg_tol"]))
+    ref = d["info"]
+    assert info.mean_energy == pytest.approx(ref[0], rel=1e-12)
+    assert info.variance_energy == pytest.approx(ref[1], rel=1e-9)
+    assert info.update_norm == pytest.approx(ref[2], rel=1e-10)
+    assert info.cg_iterations == int(ref[4]) and info.converged == int(ref[5])
+    step = d["params1"] - d["params0"]
+    assert np.linalg.norm((amp.params - d["params0"]) - step) <= 1e-10 * np.linalg.norm(step)
+
+
+@pytest.mark.parametrize("name", ["p2", "trans"])
+def test_symproj(name):
+    d = load("symproj_" + name)
+    amp = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params"],
+                [("symproj", d["perm"], d["chars"])])
+    la, ar = O.log_amp(amp, d["spins"])
+    assert rel(la, d["la"]) < 1e-13
+    assert np.array_equal(ar, d["arg"])
+    assert rel(O.symproj_gradient(amp, d["spins"]), d["grad"]) < 1e-12
+
+
+def test_exact_energies_obc():
+    d = load("exact_obc")
+    for kind, Lx, Ly, J, X, e0 in d["rows"]:
+        if int(kind) == 0:
+            h = O.ham(O.OR_TFIM, int(Lx), int(Ly), 0, 1, J, 0.0, 1.0, X)
+            e = O.exact_energy(h, -1)
+        else:
+            h = O.ham(O.OR_XXZ, int(Lx), int(Ly), 0, 1, J, 0.0, X, 0.0)
+            e = min(O.exact_energy(h, nd) for nd in range(int(Lx * Ly) + 1))
+        assert e == pytest.approx(e0, abs=1e-8)
+
+
+def test_known_answers():
+    """Closed-form values from the upstream unit tests (test_nqs.c:110-156,
+    test_nqs_kagome.c:52-141, test_nqs_lanczos.c:163,259, test_nqs_kspace_ed.c:47,61)."""
+    mf0 = O.Amp(O.OR_MF, 9, 0, np.zeros(9))
+    allup = np.ones((1, 9), np.int32)
+    neel = np.array([[1, -1, 1, -1, 1, -1, 1, -1, 1]], np.int32)
+    assert O.local_energy(O.ham(O.OR_TFIM, 3, 3, Gamma=0.0), mf0, allup)[0] == pytest.approx(-12.0, abs=1e-12)
+    assert O.local_energy(O.ham(O.OR_HEIS, 3, 3), mf0, neel)[0] == pytest.approx(3.0, abs=1e-12)
+    assert O.local_energy(O.ham(O.OR_J1J2, 3, 3, J2=0.0), mf0, neel)[0] == pytest.approx(3.0, abs=1e-12)
+    mf12 = O.Amp(O.OR_MF, 12, 0, np.zeros(12))
+    k_all = np.ones((1, 12), np.int32)
+    assert O.local_energy(O.ham(O.OR_KAGOME, 2, 2, kagome_pbc=1), mf12, k_all)[0] == pytest.approx(6.0)
+    assert O.local_energy(O.ham(O.OR_KAGOME, 2, 2, kagome_pbc=0), mf12, k_all)[0] == pytest.approx(3.75)
+    mf3 = O.Amp(O.OR_MF, 3, 0, np.array([0.1, 0.2, 0.3]))
+    e = O.local_energy(O.ham(O.OR_KAGOME, 1, 1, kagome_pbc=1), mf3, np.array([[1, -1, 1]], np.int32))
+    assert e[0] == pytest.approx(-0.5 + 2 * np.cosh(0.2), abs=1e-12)
+    # Heisenberg chains (OBC N=4, N=8) and rings (PBC N=4, N=6)
+    assert O.exact_energy(O.ham(O.OR_HEIS, 4, 1), 2) == pytest.approx(-1.616025, abs=1e-6)
+    assert O.exact_energy(O.ham(O.OR_HEIS, 8, 1), 4) == pytest.approx(-3.37493260, abs=1e-7)
+    assert O.exact_energy(O.ham(O.OR_HEIS, 4, 1, pbc=1), 2) == pytest.approx(-2.0, abs=1e-10)
+    assert O.exact_energy(O.ham(O.OR_HEIS, 6, 1, pbc=1), 3) == pytest.approx(-2.802775637732, abs=1e-9)
+    # kagome 2x2 PBC, Sz=0 sector (upstream spin_gap_L2_Sz0.json:2-3)
+    assert O.exact_energy(O.ham(O.OR_KAGOME, 2, 2, kagome_pbc=1), 6) == pytest.approx(
+        -5.444875216941, abs=1e-9)
+    assert O.exact_energy(O.ham(O.OR_KAGOME, 2, 2, kagome_pbc=1), 5) == pytest.approx(
+        -5.062206850707, abs=1e-9)
+
+
+def test_marshall_parity_tables():
+    """upstream tests/test_nqs_marshall.c:25-55"""
+    P = lambda s, x, y: O.lib().oracle_marshall_parity(O.ip(np.array(s, np.int32)), x, y)
+    assert [P(s, 2, 1) for s in ([1, 1], [-1, 1], [1, -1], [-1, -1])] == [0, 1, 0, 1]
+    assert P([1, -1, -1, 1], 2, 2) == 0 and P([-1, 1, 1, -1], 2, 2) == 0
+    assert P([-1, -1, -1, 1], 2, 2) == 1
+
+
+def test_philox_known_answer():
+    """Philox4x32-10 known-answer vectors published with Random123 (kat_vectors):
+    counter=0,key=0 and counter=all-ones,key=all-ones."""
+    import ctypes as C
+    out = (C.c_uint32 * 4)()
+    O.lib().oracle_philox4x32((C.c_uint32 * 4)(0, 0, 0, 0), (C.c_uint32 * 2)(0, 0), out)
+    assert list(out) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    m = 0xFFFFFFFF
+    O.lib().oracle_philox4x32((C.c_uint32 * 4)(m, m, m, m), (C.c_uint32 * 2)(m, m), out)
+    assert list(out) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
