@@ -1,0 +1,343 @@
+"""MinSR steps/s of the NQS VMC step on one GB300 (and N independent replicas).
+
+Workload (the reference's 2-D Heisenberg configuration): 4x4 Heisenberg
+antiferromagnet with periodic boundaries and the Marshall sign, complex RBM
+alpha = 2 (M = 32, 1120 real parameters, each real/imag part N(0, 0.01^2) from
+a seed), Sz = 0 start with nearest-neighbour exchange moves on 1024 Philox
+chains x 4 samples = N_s = 4096 samples/step (one lattice sweep of 16
+proposals between samples), MinSR with shift 1e-4 and lr 0.005.  A step is
+one nqs_sr_step_minsr_full call: sampling -> local energies + Jacobian ->
+Gram -> Cholesky -> solve -> update.  Synthetic data: the configurations are
+generated by the sampler itself; nothing is read from disk.
+
+Arms:
+  default            the CUDA library (value: CUDA events on the library stream,
+                     e2e: wall clock through the C ABI with host buffers)
+  --impl reference   the upstream algorithm on the host cores (the upstream
+                     library where it was built, else the oracle restatement):
+                     K independent MinSR steps spread over all host cores.
+Multi-GPU: the step does not shard (one Gram per Markov-chain ensemble), so N
+GPUs run N independent replicas ("scaling": "weak").
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+LX = LY = 4
+N_SITES = 16
+M_HIDDEN = 32
+NS = 4096
+CHAINS = 1024
+DECOR = 16
+THERM = 512
+SHIFT = 1e-4
+LR = 0.005
+SEED = 2026
+METRIC = "MinSR steps/s (4x4 Heisenberg PBC, complex RBM alpha=2, N_s=4096)"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ workload
+
+def workload_cfg(abi):
+    return abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M_HIDDEN,
+                               hamiltonian=abi.HAM_HEISENBERG, j_coupling=1.0, rng_seed=SEED,
+                               num_samples=NS, num_thermalize=THERM, num_decorrelate=DECOR,
+                               sr_diag_shift=SHIFT, learning_rate=LR, num_iterations=1)
+
+
+def init_params(P, seed=SEED):
+    import numpy as np
+    return np.random.default_rng(seed).normal(0.0, 0.01, size=P)
+
+
+def algorithmic_work(Ns, P):
+    """Per-kernel algorithmic FLOPs of one MinSR step (2 flops per FMA)."""
+    gram = Ns * (Ns + 1) * P                        # lower triangle incl. diagonal
+    syrk = 0
+    nb = 32
+    for k0 in range(0, Ns, nb):
+        kb = min(nb, Ns - k0)
+        rest = Ns - k0 - kb
+        syrk += rest * (rest + 1) * kb              # 2 * rest(rest+1)/2 * kb
+    return {"gram_fp64": gram, "chol_syrk": syrk, "gram_tc": gram}
+
+
+# ------------------------------------------------------------------ clocks
+
+class Clocks:
+    def __init__(self):
+        self.p = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self, gpu_index=0):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+
+def cpu_step(task):
+    """One upstream MinSR step on the host: the upstream single-chain xorshift
+    sampler followed by nqs_sr_step_minsr_full's algorithm, through the
+    upstream library when it is loadable here, else the oracle restatement."""
+    kind, seed = task
+    import numpy as np
+    import oracle_lib as O
+    P = O.num_params(O.OR_CRBM, N_SITES, M_HIDDEN)
+    params = init_params(P, seed)
+    amp = O.Amp(O.OR_CRBM, N_SITES, M_HIDDEN, params, [("marshall", LX, LY)])
+    h = O.ham(O.OR_HEIS, LX, LY, pbc=1)
+    t0 = time.perf_counter()
+    batch, _ = O.xorshift_sampler(amp, seed, THERM, DECOR, NS)
+    O.minsr_step(h, amp, batch, SHIFT, LR)
+    return time.perf_counter() - t0
+
+
+def reference_kind():
+    return "port"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    import oracle_lib
+    oracle_lib.build_oracle()
+    cores = os.cpu_count() or 1
+    workers = max(1, min(cores, max(args.steps, 1)))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        if args.warmup > 0:
+            pool.map(cpu_step, [("port", SEED + i) for i in range(min(args.warmup, workers))])
+        t0 = time.perf_counter()
+        pool.map(cpu_step, [("port", SEED + 100 + i) for i in range(args.steps)])
+        wall = time.perf_counter() - t0
+    value = args.steps / wall
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES,
+                       "hidden": M_HIDDEN, "num_samples": NS, "num_params": 1120, "shift": SHIFT, "lr": LR},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": workers, "kind": reference_kind(),
+                             "sample": "%d independent MinSR steps (N_s=4096, N_p=1120, FP64, upstream "
+                                       "single-chain sampler) run concurrently on %d host processes"
+                                       % (args.steps, workers)},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = dist_init(ws)
+    import numpy as np
+    import spin_based_neural_network_gb300 as pkg
+    pkg.lib()
+    from spin_based_neural_network_gb300 import abi, nqs
+    L = nqs.lib()
+
+    prec = abi.PREC_FP64 if args.precision == "fp64" else abi.PREC_MIXED
+    nqs.set_options(square_pbc=1, precision=prec)
+    cfg = workload_cfg(abi)
+    a = nqs.Ansatz(cfg, N_SITES)
+    a.params[:] = init_params(a.P)
+    m = nqs.Marshall(a.log_amp_fn, a.user, LX, LY)
+    opts = nqs.options(num_chains=CHAINS, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=N_SITES // 2,
+                       lattice_x=LX, lattice_y=LY, square_pbc=1, precision=prec)
+    s = nqs.Sampler(N_SITES, cfg, m.log_amp_fn, m.user, opts)
+    s.thermalize()
+
+    def step():
+        return nqs.sr_step_minsr(cfg, LX, LY, a, s, m.log_amp_fn, m.user)
+
+    for _ in range(args.warmup):
+        step()
+
+    # value: device time of K steps, CUDA events on the library stream
+    dist_barrier(dist)
+    nqs.lib().nqs_gpu_synchronize()
+    clocks = Clocks()
+    clocks.start()
+    n0 = nqs.launch_count()
+    e0 = L.nqs_gpu_event_record()
+    energies = []
+    for _ in range(args.steps):
+        energies.append(step().mean_energy)
+    e1 = L.nqs_gpu_event_record()
+    dev_ms = L.nqs_gpu_event_elapsed_ms(e0, e1)
+    launches = nqs.launch_count() - n0
+    L.nqs_gpu_event_destroy(e0)
+    L.nqs_gpu_event_destroy(e1)
+    nqs.lib().nqs_gpu_synchronize()
+    clk = clocks.stop(0)
+    dist_barrier(dist)
+    dev_ms = dist_max(dist, dev_ms)
+    value = ws * args.steps / (dev_ms / 1000.0)
+
+    # e2e: wall clock through the C ABI; each step uploads the host parameter
+    # mirror (pinned) and reads back the step info and the updated parameters
+    P = a.P
+    dist_barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a.params[:] = a.params            # the step's input, written by the host
+        step()
+    wall = time.perf_counter() - t0
+    wall = dist_max(dist, wall)
+    e2e = ws * args.steps / wall
+
+    # roofline: per-kernel CUDA events over a few extra steps
+    nqs.profile_reset()
+    nqs.profile(True)
+    for _ in range(3):
+        step()
+    nqs.profile(False)
+    prof = nqs.profile_read()
+    total = sum(v[1] for v in prof.values())
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    work = algorithmic_work(NS, P)
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        peaks = json.load(f)
+    roof = None
+    name, (cnt, ms) = top
+    if name in work:
+        launches_per_step = cnt / 3.0
+        flops_per_launch = work[name] / launches_per_step
+        avg_ms = ms / cnt
+        achieved = flops_per_launch / (avg_ms / 1000.0) / 1e12
+        peak = peaks["bf16_tflops"]
+        roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_source": "bf16_tflops of measured",
+                "pipe": "fp64" if name.endswith("fp64") or name.startswith("chol") else "tensor",
+                "frac_of_fp64_nominal": achieved / 1.25 if "fp64" in name or name.startswith("chol") else None,
+                "traffic": None, "share_of_step": ms / total}
+    kernels = {k: {"launches_per_step": v[0] / 3.0, "ms_per_step": v[1] / 3.0} for k, v in
+               sorted(prof.items(), key=lambda kv: -kv[1][1])}
+
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == abi.PREC_FP64 else "mixed(tf32/bf16 gram, f64 solve)",
+            "data": "synthetic (sampled configurations; parameters N(0,0.01^2) from a seed)",
+            "config": {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES,
+                       "hidden": M_HIDDEN, "num_params": P, "num_samples": NS, "chains": CHAINS,
+                       "decorrelate": DECOR, "moves": "nn-exchange, Sz=0", "shift": SHIFT, "lr": LR,
+                       "precision": args.precision,
+                       "l2": "working set > L2 (Gram 4096^2 FP64 = 134 MB)",
+                       "parallelism": "replicas x%d" % ws},
+            "gpu_launches": launches,
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * P,
+                    "d2h_bytes_per_step": 8 * P + 16 * 8},
+            "roofline": roof, "clocks": clk, "kernels": kernels,
+            "final_energy_per_site": energies[-1] / N_SITES if energies else None}
+    if rank == 0 and not args.no_cpu_baseline:
+        secs = cpu_step(("port", SEED))
+        line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": "one MinSR step of the same workload (N_s=4096, N_p=1120) by the "
+                                          "oracle restatement of the upstream algorithm, 1 host core"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,139 @@
+/*
+ * include/nqs/nqs_gpu.h -- GPU-only extensions of the NQS C API.
+ *
+ * None of these entry points exists upstream; they add what the upstream
+ * nqs_config_t (whose layout is frozen) cannot express: many-chain Philox
+ * sampling with exchange moves and a fixed-magnetisation start, periodic
+ * square lattices, the precision mode of the SR solve, batched device entry
+ * points on caller-supplied configurations ("replay" of identical batches),
+ * the deep MLP ansatz, and per-kernel timing.
+ */
+#ifndef NQS_GPU_H
+#define NQS_GPU_H
+
+#include "nqs_config.h"
+#include "nqs_ansatz.h"
+#include "nqs_sampler.h"
+#include "nqs_optimizer.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 2-hidden-layer tanh MLP, N -> width -> width -> (Re, Im) head.  Parameter
+ * layout: W1[width][N], b1[width], W2[width][width], b2[width], w_re[width],
+ * w_im[width], c_re, c_im.  Selected through nqs_config_t.ansatz. */
+#define NQS_GPU_ANSATZ_MLP 100
+
+typedef enum {
+    NQS_GPU_RNG_XORSHIFT_COMPAT = 0,  /* upstream single chain, same sequence */
+    NQS_GPU_RNG_PHILOX          = 1   /* num_chains chains, Philox4x32-10 */
+} nqs_gpu_rng_t;
+
+typedef enum {
+    NQS_GPU_MOVE_SINGLE_FLIP = 0,
+    NQS_GPU_MOVE_EXCHANGE    = 1      /* swap the spins of a random bond */
+} nqs_gpu_move_t;
+
+typedef enum {
+    NQS_GPU_PREC_FP64  = 0,           /* every stage in FP64 (parity path) */
+    NQS_GPU_PREC_MIXED = 1            /* tensor-core Gram, FP64 refinement */
+} nqs_gpu_precision_t;
+
+typedef struct {
+    int num_chains;      /* Philox chains (one warp each); compat mode uses 1 */
+    int rng;             /* nqs_gpu_rng_t */
+    int move;            /* nqs_gpu_move_t (exchange needs rng = PHILOX) */
+    int n_down;          /* >= 0: start each chain with this many down spins */
+    int square_pbc;      /* 1: periodic chain / square lattices */
+    int precision;       /* nqs_gpu_precision_t for MinSR */
+    int refine_sweeps;   /* MIXED: FP64 iterative-refinement sweeps */
+    int gram_passes;     /* MIXED: 1 = single TF32 pass, 3 = split (hi/lo) passes */
+    int chol_fp32;       /* MIXED: 1 = FP32 Cholesky factor, 0 = FP64 */
+    int lattice_x;       /* exchange moves: lattice whose nearest-neighbour bonds */
+    int lattice_y;       /*   are swapped (0 x 0 = periodic ring of N sites)      */
+    int lattice_kagome;  /*   1: kagome cells, bonds of kagome_pbc = 1          */
+    int reserved[4];
+} nqs_gpu_options_t;
+
+/* Defaults: compat sampler, single flips, open lattices, FP64. */
+nqs_gpu_options_t nqs_gpu_options_default(void);
+/* Process-wide options read by nqs_sampler_create and every step call. */
+int nqs_gpu_set_options(const nqs_gpu_options_t *opts);
+int nqs_gpu_get_options(nqs_gpu_options_t *opts);
+
+/* Sampler with explicit options (upstream nqs_sampler_create + options). */
+nqs_sampler_t *nqs_sampler_create_gpu(int num_sites, const nqs_config_t *cfg,
+                                      const nqs_gpu_options_t *opts,
+                                      nqs_log_amp_fn_t log_amp, void *log_amp_user);
+/* Number of chains the sampler runs. */
+int nqs_sampler_num_chains(const nqs_sampler_t *s);
+
+/* Human-readable reason of the last failure on this thread ("" if none). */
+const char *nqs_gpu_last_error(void);
+/* Device name and SM count of the device in use; 0 on success. */
+int nqs_gpu_device_info(char *name, int name_len, int *sm_count);
+/* The cudaStream_t every kernel of this library is launched on. */
+void *nqs_gpu_stream(void);
+int nqs_gpu_synchronize(void);
+
+/* Batched entry points on caller-supplied configurations (host int +-1,
+ * row-major [B][N]).  0 on success, -1 on failure. */
+int nqs_gpu_log_amp_batch(nqs_log_amp_fn_t log_amp, void *user,
+                          const int *spins, int batch, int num_sites,
+                          double *out_log_abs, double *out_arg);
+int nqs_gpu_local_energy_batch(const nqs_config_t *cfg, int size_x, int size_y,
+                               const int *spins, int batch,
+                               nqs_log_amp_fn_t log_amp, void *user,
+                               double *out_re, double *out_im);
+/* O[b][k] = d log|psi| / d theta_k (complex_out = 0) or the holomorphic pair
+ * (complex_out = 1, out_im used) for the base ansatz, or the symmetry-
+ * projected gradient when gradient_fn = nqs_symproj_gradient. */
+int nqs_gpu_gradient_batch(nqs_ansatz_t *a, nqs_gradient_fn_t gradient_fn,
+                           void *grad_user, const int *spins, int batch,
+                           int complex_out, double *out_re, double *out_im);
+
+/* One SR step on a caller-supplied batch (no sampling): the parity entry
+ * points.  `minsr` = 1 runs MinSR, 0 runs CG-SR.  Optional outputs:
+ * out_energies[batch], out_delta[num_params]. */
+int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int size_x, int size_y,
+                          nqs_ansatz_t *ansatz,
+                          nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,
+                          nqs_gradient_fn_t gradient_fn, void *grad_user,
+                          const int *batch, int num_samples, int minsr,
+                          nqs_sr_step_info_t *out_info,
+                          double *out_energies, double *out_delta);
+
+/* Statistics of the last SR step on this thread. */
+typedef struct {
+    double tau_int;          /* integrated autocorrelation time of E_loc (Sokal, c = 5) */
+    double ess;              /* effective sample size = sum_c n_c / tau_c */
+    double refine_residual;  /* MIXED: relative residual after refinement */
+    int    refine_sweeps;    /* sweeps used */
+    int    chol_retry;       /* 1 if the +1e-6 retry ran */
+    int    chol_fail_col;    /* first failing column or -1 */
+    int    gpu_launches;     /* kernels launched by the step */
+} nqs_gpu_step_stats_t;
+int nqs_gpu_last_step_stats(nqs_gpu_step_stats_t *out);
+
+/* Per-kernel CUDA-event timing.  While enabled every launch is bracketed by
+ * events on the library stream; nqs_gpu_profile_read() returns, for up to
+ * `cap` kernels, their name, launch count and summed milliseconds. */
+int nqs_gpu_profile_enable(int on);
+int nqs_gpu_profile_reset(void);
+int nqs_gpu_profile_read(int cap, char names[][48], int *counts, double *ms);
+/* Kernels launched by this library since the last nqs_gpu_profile_reset(). */
+long nqs_gpu_launch_count(void);
+
+/* CUDA events on the library stream, for timing from the host:
+ * nqs_gpu_event_record() creates and records one; nqs_gpu_event_elapsed_ms()
+ * waits for `end` and returns the milliseconds between the two. */
+void *nqs_gpu_event_record(void);
+double nqs_gpu_event_elapsed_ms(void *start, void *end);
+void nqs_gpu_event_destroy(void *event);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NQS_GPU_H */

@@ -1,0 +1,121 @@
+/*
+ * include/nqs/nqs_optimizer.h -- stochastic reconfiguration (CG-SR, MinSR).
+ *
+ * Drop-in for upstream include/nqs/nqs_optimizer.h:35-323 (real-projected SR
+ * and MinSR).  One step = sample -> local energies -> Jacobian O_k -> solve
+ * -> parameter update, all on the GPU; only the step info and the parameter
+ * mirror come back to the host.  The upstream semantics are kept: real-
+ * projected gradients for complex ansatze, the real local energy, variance
+ * <E^2> - <E>^2, update_norm = ||delta|| * lr, the one-shot +1e-6 Cholesky
+ * retry and delta = 0 on a second failure.
+ */
+#ifndef NQS_OPTIMIZER_H
+#define NQS_OPTIMIZER_H
+
+#include "nqs_config.h"
+#include "nqs_ansatz.h"
+#include "nqs_sampler.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-step diagnostics, upstream include/nqs/nqs_optimizer.h:35-42. */
+typedef struct {
+    double mean_energy;
+    double variance_energy;
+    double update_norm;
+    double acceptance_ratio;
+    int    cg_iterations;
+    int    converged;
+} nqs_sr_step_info_t;
+
+/* Replaces upstream nqs_sr_step (include/nqs/nqs_optimizer.h:47). */
+int nqs_sr_step(const nqs_config_t *cfg,
+                int size_x, int size_y,
+                nqs_ansatz_t *ansatz,
+                nqs_sampler_t *sampler,
+                nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run (include/nqs/nqs_optimizer.h:58). */
+int nqs_sr_run(const nqs_config_t *cfg,
+               int size_x, int size_y,
+               nqs_ansatz_t *ansatz,
+               nqs_sampler_t *sampler,
+               double *out_energy_trace);
+
+/* Upstream gradient callback (include/nqs/nqs_optimizer.h:69-72).  Accepted
+ * values: NULL (base ansatz gradient) or nqs_symproj_gradient with its
+ * nqs_symproj_wrapper_t; anything else fails the step. */
+typedef int (*nqs_gradient_fn_t)(void *grad_user,
+                                  nqs_ansatz_t *ansatz,
+                                  const int *spins, int num_sites,
+                                  double *out_grad);
+
+/* Replaces upstream nqs_sr_step_custom (include/nqs/nqs_optimizer.h:78). */
+int nqs_sr_step_custom(const nqs_config_t *cfg,
+                       int size_x, int size_y,
+                       nqs_ansatz_t *ansatz,
+                       nqs_sampler_t *sampler,
+                       nqs_log_amp_fn_t log_amp_fn,
+                       void *log_amp_user,
+                       nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run_custom (include/nqs/nqs_optimizer.h:86). */
+int nqs_sr_run_custom(const nqs_config_t *cfg,
+                      int size_x, int size_y,
+                      nqs_ansatz_t *ansatz,
+                      nqs_sampler_t *sampler,
+                      nqs_log_amp_fn_t log_amp_fn,
+                      void *log_amp_user,
+                      double *out_energy_trace);
+
+/* Replaces upstream nqs_sr_step_custom_full (include/nqs/nqs_optimizer.h:97):
+ * CG-SR with the matrix-free QGT product. */
+int nqs_sr_step_custom_full(const nqs_config_t *cfg,
+                             int size_x, int size_y,
+                             nqs_ansatz_t *ansatz,
+                             nqs_sampler_t *sampler,
+                             nqs_log_amp_fn_t log_amp_fn,
+                             void *log_amp_user,
+                             nqs_gradient_fn_t gradient_fn,
+                             void *grad_user,
+                             nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run_custom_full (include/nqs/nqs_optimizer.h:107). */
+int nqs_sr_run_custom_full(const nqs_config_t *cfg,
+                            int size_x, int size_y,
+                            nqs_ansatz_t *ansatz,
+                            nqs_sampler_t *sampler,
+                            nqs_log_amp_fn_t log_amp_fn,
+                            void *log_amp_user,
+                            nqs_gradient_fn_t gradient_fn,
+                            void *grad_user,
+                            double *out_energy_trace);
+
+/* Replaces upstream nqs_sr_step_minsr_full (include/nqs/nqs_optimizer.h:307):
+ * MinSR through the N_s x N_s sample-space Gram matrix. */
+int nqs_sr_step_minsr_full(const nqs_config_t *cfg,
+                            int size_x, int size_y,
+                            nqs_ansatz_t *ansatz,
+                            nqs_sampler_t *sampler,
+                            nqs_log_amp_fn_t log_amp_fn,
+                            void *log_amp_user,
+                            nqs_gradient_fn_t gradient_fn,
+                            void *grad_user,
+                            nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run_minsr (include/nqs/nqs_optimizer.h:317). */
+int nqs_sr_run_minsr(const nqs_config_t *cfg,
+                      int size_x, int size_y,
+                      nqs_ansatz_t *ansatz,
+                      nqs_sampler_t *sampler,
+                      nqs_log_amp_fn_t log_amp_fn,
+                      void *log_amp_user,
+                      double *out_energy_trace);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NQS_OPTIMIZER_H */

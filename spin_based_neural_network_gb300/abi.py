@@ -127,5 +127,8 @@ class GpuOptions(C.Structure):
         ("refine_sweeps", C.c_int),
         ("gram_passes", C.c_int),
         ("chol_fp32", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("lattice_x", C.c_int),
+        ("lattice_y", C.c_int),
+        ("lattice_kagome", C.c_int),
+        ("reserved", C.c_int * 4),
     ]

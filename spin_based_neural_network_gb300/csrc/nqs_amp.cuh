@@ -1,0 +1,162 @@
+// Warp-cooperative evaluation of the device amplitude program.
+//
+// One warp evaluates one configuration: lanes own hidden units (h = lane +
+// 32 j), so a hidden pre-activation theta_h = b_h + sum_i W_hi s_i is summed
+// by one lane in the upstream order (ascending i; s_i = +-1 makes every
+// product exact, so theta is bit-identical to upstream), the weight column of
+// site i is one coalesced load across the warp, and the sum over hidden units
+// is a 5-step XOR butterfly that leaves the same value in every lane.
+#pragma once
+#include "nqs_internal.cuh"
+
+namespace nqs {
+
+__device__ __forceinline__ long crbm_pr(const DevAnsatz &a) {
+    return (long)a.N + a.M + (long)a.M * a.N;
+}
+
+// Visible-bias term sum_i a_i s_i (real and imaginary parts).
+__device__ __forceinline__ void warp_visible(const DevAnsatz &a, uint64_t bits, double &vr, double &vi) {
+    int lane = threadIdx.x & 31;
+    double r = 0.0, im = 0.0;
+    if (a.kind != KIND_MLP) {
+        long Pr = a.kind == KIND_CRBM ? crbm_pr(a) : 0;
+        for (int i = lane; i < a.N; i += 32) {
+            double s = (double)spin_of(bits, i);
+            r += a.p[i] * s;
+            if (a.kind == KIND_CRBM) im += a.p[Pr + i] * s;
+        }
+    }
+    vr = warp_sum(r);
+    vi = warp_sum(im);
+}
+
+// theta_h of the RBM / complex RBM, summed in the upstream order.
+__device__ __forceinline__ void rbm_theta(const DevAnsatz &a, uint64_t bits, int h, double &xr,
+                                          double &xi) {
+    long Pr = crbm_pr(a);
+    xr = a.p[a.N + h];
+    xi = a.kind == KIND_CRBM ? a.p[Pr + a.N + h] : 0.0;
+    for (int i = 0; i < a.N; i++) {
+        double s = (double)spin_of(bits, i);
+        xr += a.wtr[(long)i * a.M + h] * s;
+        if (a.kind == KIND_CRBM) xi += a.wti[(long)i * a.M + h] * s;
+    }
+}
+
+// Deep MLP forward pass; `h1` is a per-warp scratch of M doubles.
+__device__ __forceinline__ void warp_mlp_eval(const DevAnsatz &a, uint64_t bits, double &la, double &ar,
+                                              double *h1) {
+    int lane = threadIdx.x & 31;
+    const int N = a.N, M = a.M;
+    const double *b1 = a.p + (long)M * N;
+    const double *b2 = b1 + M + (long)M * M;
+    const double *wr = b2 + M, *wi = wr + M;
+    for (int k = lane; k < M; k += 32) {
+        double z = b1[k];
+        for (int i = 0; i < N; i++) z += a.wtr[(long)i * M + k] * (double)spin_of(bits, i);
+        h1[k] = tanh(z);
+    }
+    __syncwarp();
+    double r = 0.0, im = 0.0;
+    for (int j = lane; j < M; j += 32) {
+        double z = b2[j];
+        for (int k = 0; k < M; k++) z += a.wti[(long)k * M + j] * h1[k];
+        double h2 = tanh(z);
+        r += wr[j] * h2;
+        im += wi[j] * h2;
+    }
+    __syncwarp();
+    la = warp_sum(r) + wi[M];
+    ar = warp_sum(im) + wi[M + 1];
+}
+
+// log psi of the base ansatz (all lanes return the same value).
+__device__ __forceinline__ void warp_base_eval(const DevAnsatz &a, uint64_t bits, double &la, double &ar,
+                                               double *scratch) {
+    int lane = threadIdx.x & 31;
+    if (a.kind == KIND_MLP) {
+        warp_mlp_eval(a, bits, la, ar, scratch);
+        return;
+    }
+    double vr, vi;
+    warp_visible(a, bits, vr, vi);
+    double hr = 0.0, hi = 0.0;
+    if (a.kind == KIND_RBM || a.kind == KIND_CRBM) {
+        for (int h = lane; h < a.M; h += 32) {
+            double xr, xi;
+            rbm_theta(a, bits, h, xr, xi);
+            if (a.kind == KIND_RBM) {
+                hr += logcosh_r(xr);
+            } else {
+                double t1, t2;
+                clogcosh(xr, xi, t1, t2);
+                hr += t1;
+                hi += t2;
+            }
+        }
+    }
+    la = vr + warp_sum(hr);
+    ar = vi + warp_sum(hi);
+}
+
+// (g.s)_i = s_{perm_g[i]} as a bit permutation (two ballots for N <= 64).
+__device__ __forceinline__ uint64_t permute_bits(uint64_t bits, const int *perm_g, int N) {
+    int lane = threadIdx.x & 31;
+    int i0 = lane, i1 = lane + 32;
+    bool b0 = i0 < N && ((bits >> perm_g[i0]) & 1ull);
+    bool b1 = i1 < N && ((bits >> perm_g[i1]) & 1ull);
+    uint32_t lo = __ballot_sync(0xffffffffu, b0);
+    uint32_t hi = __ballot_sync(0xffffffffu, b1);
+    return (uint64_t)lo | ((uint64_t)hi << 32);
+}
+
+// Marshall layers (src/nqs/nqs_marshall.c:29-40): arg += pi for odd parity,
+// innermost layer first.
+__device__ __forceinline__ double apply_marshall(double ar, uint64_t bits, int n, const uint64_t *masks) {
+    for (int m = n - 1; m >= 0; m--) ar = ar + ((__popcll(bits & masks[m]) & 1) ? kPi : 0.0);
+    return ar;
+}
+
+// Full program: outer Marshall o symproj o inner Marshall o base.
+__device__ __forceinline__ void warp_amp_eval(const DevAmp &A, uint64_t bits, double &la, double &ar,
+                                              double *scratch) {
+    if (A.G == 0) {
+        warp_base_eval(A.a, bits, la, ar, scratch);
+    } else {
+        // src/nqs/nqs_symproj.c:31-80 with an online log-sum-exp over g
+        const int N = A.a.N;
+        double mx = -1e300, sum = 0.0;
+        for (int g = 0; g < A.G; g++) {
+            uint64_t pb = permute_bits(bits, A.perm + (long)g * N, N);
+            double l, a;
+            warp_base_eval(A.a, pb, l, a, scratch);
+            a = apply_marshall(a, pb, A.n_inner, A.inner_mask);
+            double c = A.chars[g] * cos(a);
+            if (l > mx) {
+                sum = sum * exp(mx - l) + c;
+                mx = l;
+            } else {
+                sum += c * exp(l - mx);
+            }
+        }
+        double as = fabs(sum);
+        if (as > 0.0) {
+            la = log(as) + mx - 0.5 * log((double)A.G);
+            ar = sum < 0.0 ? kPi : 0.0;
+        } else {
+            la = -1e300;
+            ar = 0.0;
+        }
+    }
+    ar = apply_marshall(ar, bits, A.n_outer, A.outer_mask);
+}
+
+// Parity count of all Marshall layers of a projection-free program.
+__device__ __forceinline__ int marshall_count(const DevAmp &A, uint64_t bits) {
+    int c = 0;
+    for (int m = 0; m < A.n_outer; m++) c += __popcll(bits & A.outer_mask[m]) & 1;
+    return c;
+}
+
+}  // namespace nqs

@@ -1,0 +1,789 @@
+// Ansatz handle, amplitude-program builder, log-amplitude and Jacobian kernels.
+#include <math.h>
+#include <stdlib.h>
+
+#include "nqs_amp.cuh"
+
+namespace nqs {
+
+// ---------------------------------------------------------------- parameters
+
+static long num_params_of(int kind, int N, int M) {
+    long n = N, m = M;
+    switch (kind) {
+        case KIND_MF: return n;                                   // src/nqs/nqs_ansatz.c:77-87
+        case KIND_RBM: return n + m + m * n;                      // :88
+        case KIND_CRBM: return 2 * (n + m + m * n);               // :223
+        case KIND_MLP: return m * n + m + m * m + m + 2 * m + 2;  // GPU extension
+        default: return -1;
+    }
+}
+
+// Initial parameters: the upstream xorshift64 stream and Box-Muller draws
+// (src/nqs/nqs_ansatz.c:47-61, :65-252), so a given config yields the same
+// starting point as upstream.  Host-side set-up, run once per handle.
+static double xs_uniform(uint64_t *s) {
+    uint64_t x = *s;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    *s = x;
+    return (double)(x >> 11) / 9007199254740992.0;
+}
+
+static double xs_gauss(uint64_t *s) {
+    double u1 = xs_uniform(s), u2 = xs_uniform(s);
+    if (u1 < 1e-15) u1 = 1e-15;
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * kPi * u2);
+}
+
+static void init_params(const nqs_config_t *cfg, int kind, int N, int M, double *p) {
+    uint64_t st = cfg->rng_seed ? (uint64_t)cfg->rng_seed : 0xDEADBEEFCAFEBABEull;
+    double scale = cfg->rbm_init_scale > 0.0 ? cfg->rbm_init_scale : 0.01;
+    if (kind == KIND_MF) {
+        for (int i = 0; i < N; i++) p[i] = 0.01 * (xs_uniform(&st) - 0.5);
+        return;
+    }
+    if (kind == KIND_RBM || kind == KIND_CRBM) {
+        long Pr = (long)N + M + (long)M * N;
+        double wstd = scale / sqrt((double)N);
+        for (int i = 0; i < N; i++) p[i] = scale * (xs_uniform(&st) - 0.5);
+        for (int h = 0; h < M; h++) p[N + h] = scale * (xs_uniform(&st) - 0.5);
+        for (long k = 0; k < (long)M * N; k++) p[N + M + k] = wstd * xs_gauss(&st);
+        if (kind == KIND_CRBM) {
+            double is = 0.1 * scale, iw = is / sqrt((double)N);
+            for (int i = 0; i < N; i++) p[Pr + i] = is * (xs_uniform(&st) - 0.5);
+            for (int h = 0; h < M; h++) p[Pr + N + h] = is * (xs_uniform(&st) - 0.5);
+            for (long k = 0; k < (long)M * N; k++) p[Pr + N + M + k] = iw * xs_gauss(&st);
+        }
+        return;
+    }
+    // deep MLP: Xavier-normal weights in layout order, zero biases
+    long P = num_params_of(kind, N, M);
+    memset(p, 0, sizeof(double) * (size_t)P);
+    long o = 0;
+    double s1 = sqrt(2.0 / (double)(N + M));
+    for (long k = 0; k < (long)M * N; k++) p[o + k] = s1 * xs_gauss(&st);
+    o += (long)M * N + M;
+    double s2 = sqrt(2.0 / (double)(M + M));
+    for (long k = 0; k < (long)M * M; k++) p[o + k] = s2 * xs_gauss(&st);
+    o += (long)M * M + M;
+    double s3 = sqrt(2.0 / (double)(M + 1));
+    for (long k = 0; k < 2L * M; k++) p[o + k] = s3 * xs_gauss(&st);
+}
+
+// Transposed weight copies: RBM/cRBM W[h][i] -> wt[i][h]; MLP W1 -> W1^T, W2 -> W2^T.
+__global__ void k_derive(DevAnsatz a, double *wtr, double *wti) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = a.N, M = a.M;
+    if (a.kind == KIND_RBM || a.kind == KIND_CRBM) {
+        if (t >= (long)M * N) return;
+        int h = (int)(t / N), i = (int)(t % N);
+        wtr[(long)i * M + h] = a.p[N + M + t];
+        if (a.kind == KIND_CRBM) wti[(long)i * M + h] = a.p[crbm_pr(a) + N + M + t];
+    } else if (a.kind == KIND_MLP) {
+        long nW1 = (long)M * N;
+        if (t < nW1) {
+            int k = (int)(t / N), i = (int)(t % N);
+            wtr[(long)i * M + k] = a.p[t];
+        } else if (t < nW1 + (long)M * M) {
+            long u = t - nW1;
+            int j = (int)(u / M), k = (int)(u % M);
+            wti[(long)k * M + j] = a.p[nW1 + M + u];
+        }
+    }
+}
+
+DevAnsatz ansatz_dev(const Ansatz *a) {
+    DevAnsatz d;
+    d.kind = a->kind;
+    d.N = a->N;
+    d.M = a->M;
+    d.P = a->P;
+    d.p = a->d_params.p;
+    d.wtr = a->d_wtr.p;
+    d.wti = a->d_wti.p;
+    return d;
+}
+
+bool ansatz_refresh_derived(Ansatz *a) {
+    if (a->kind == KIND_MF) return true;
+    long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * a->M : (long)a->M * a->N;
+    NQS_LAUNCH("derive_weights");
+    k_derive<<<(unsigned)((work + 255) / 256), 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
+                                                                        a->d_wti.p);
+    return NQS_CUDA(cudaGetLastError());
+}
+
+bool ansatz_sync(Ansatz *a, bool force) {
+    size_t bytes = sizeof(double) * (size_t)a->P;
+    bool same = a->dev_valid && memcmp(a->h_params, a->h_shadow, bytes) == 0;
+    if (same && !force) return true;
+    if (!NQS_CUDA(cudaMemcpyAsync(a->d_params.p, a->h_params, bytes, cudaMemcpyHostToDevice,
+                                  ctx().stream)))
+        return false;
+    if (same) return true;
+    memcpy(a->h_shadow, a->h_params, bytes);
+    a->dev_valid = true;
+    return ansatz_refresh_derived(a);
+}
+
+bool ansatz_pull(Ansatz *a) {
+    size_t bytes = sizeof(double) * (size_t)a->P;
+    if (!NQS_CUDA(cudaMemcpyAsync(a->h_params, a->d_params.p, bytes, cudaMemcpyDeviceToHost,
+                                  ctx().stream)))
+        return false;
+    if (!NQS_CUDA(cudaStreamSynchronize(ctx().stream))) return false;
+    memcpy(a->h_shadow, a->h_params, bytes);
+    return true;
+}
+
+// ---------------------------------------------------------------- program builder
+
+struct PermEntry {
+    std::vector<int> perm;
+    std::vector<double> chars;
+    DevBuf<int> d_perm;
+    DevBuf<double> d_chars;
+};
+static std::map<const void *, PermEntry *> g_perm_cache;
+
+static bool stage_perm(const nqs_symproj_wrapper_t *w, const int **dp, const double **dc) {
+    size_t np = (size_t)w->num_group_elements * w->num_sites;
+    PermEntry *&e = g_perm_cache[(const void *)w->perm];
+    if (!e) e = new PermEntry();
+    bool same = e->perm.size() == np && e->chars.size() == (size_t)w->num_group_elements &&
+                memcmp(e->perm.data(), w->perm, np * sizeof(int)) == 0 &&
+                memcmp(e->chars.data(), w->characters, sizeof(double) * w->num_group_elements) == 0;
+    if (!same) {
+        for (size_t k = 0; k < np; k++)
+            if (w->perm[k] < 0 || w->perm[k] >= w->num_sites) {
+                set_error("symproj permutation entry %d out of range", w->perm[k]);
+                return false;
+            }
+        e->perm.assign(w->perm, w->perm + np);
+        e->chars.assign(w->characters, w->characters + w->num_group_elements);
+        if (!e->d_perm.ensure(np) || !e->d_chars.ensure((size_t)w->num_group_elements)) return false;
+        if (!NQS_CUDA(cudaMemcpy(e->d_perm.p, w->perm, np * sizeof(int), cudaMemcpyHostToDevice)))
+            return false;
+        if (!NQS_CUDA(cudaMemcpy(e->d_chars.p, w->characters, sizeof(double) * w->num_group_elements,
+                                 cudaMemcpyHostToDevice)))
+            return false;
+    }
+    *dp = e->d_perm.p;
+    *dc = e->d_chars.p;
+    return true;
+}
+
+static uint64_t marshall_mask(int sx, int sy, int N) {
+    uint64_t m = 0;
+    for (int x = 0; x < sx; x++)
+        for (int y = 0; y < sy; y++)
+            if (((x + y) & 1) == 0) {
+                int idx = x * sy + y;
+                if (idx < N && idx < 64) m |= 1ull << idx;
+            }
+    return m;
+}
+
+bool build_amp(nqs_log_amp_fn_t fn, void *user, int num_sites, DevAmp *out, Ansatz **base) {
+    memset(out, 0, sizeof(*out));
+    // Walk the wrapper chain from the outside in.
+    int layers_type[8];
+    const void *layers_user[8];
+    int nl = 0;
+    while (true) {
+        if (fn == nqs_ansatz_log_amp) break;
+        if (nl >= 8) {
+            set_error("amplitude wrapper chain too deep");
+            return false;
+        }
+        if (fn == nqs_marshall_log_amp) {
+            auto *w = (const nqs_marshall_wrapper_t *)user;
+            if (!w) { set_error("NULL Marshall wrapper"); return false; }
+            layers_type[nl] = 1;
+            layers_user[nl++] = w;
+            fn = w->base_log_amp;
+            user = w->base_user;
+        } else if (fn == nqs_symproj_log_amp) {
+            auto *w = (const nqs_symproj_wrapper_t *)user;
+            if (!w || !w->perm || !w->characters || w->num_group_elements <= 0) {
+                set_error("invalid symproj wrapper");
+                return false;
+            }
+            layers_type[nl] = 2;
+            layers_user[nl++] = w;
+            fn = w->base_log_amp;
+            user = w->base_user;
+        } else {
+            set_error("log_amp callback %p is not one of this library's amplitude programs "
+                      "(nqs_ansatz_log_amp, nqs_marshall_log_amp, nqs_symproj_log_amp); "
+                      "host callbacks are not evaluated",
+                      (void *)fn);
+            return false;
+        }
+    }
+    Ansatz *a = (Ansatz *)user;
+    if (!a) { set_error("NULL ansatz"); return false; }
+    if (a->N != num_sites) {
+        set_error("num_sites %d does not match the ansatz (%d)", num_sites, a->N);
+        return false;
+    }
+    if (!ansatz_sync(a)) return false;
+    out->a = ansatz_dev(a);
+    int seen_sym = 0;
+    int outer_tmp = 0, inner_tmp = 0;
+    uint64_t outer_m[8], inner_m[8];
+    for (int k = 0; k < nl; k++) {
+        if (layers_type[k] == 1) {
+            auto *w = (const nqs_marshall_wrapper_t *)layers_user[k];
+            uint64_t m = marshall_mask(w->size_x, w->size_y, num_sites);
+            if (seen_sym) inner_m[inner_tmp++] = m;
+            else outer_m[outer_tmp++] = m;
+        } else {
+            if (seen_sym) {
+                set_error("nested symmetry projections are not supported");
+                return false;
+            }
+            seen_sym = 1;
+            auto *w = (const nqs_symproj_wrapper_t *)layers_user[k];
+            if (w->num_sites != num_sites) {
+                set_error("symproj num_sites %d != %d", w->num_sites, num_sites);
+                return false;
+            }
+            out->G = w->num_group_elements;
+            if (!stage_perm(w, &out->perm, &out->chars)) return false;
+        }
+    }
+    if (outer_tmp > 3 || inner_tmp > 3) {
+        set_error("more than three Marshall layers");
+        return false;
+    }
+    out->n_outer = outer_tmp;
+    out->n_inner = inner_tmp;
+    for (int k = 0; k < outer_tmp; k++) out->outer_mask[k] = outer_m[k];
+    for (int k = 0; k < inner_tmp; k++) out->inner_mask[k] = inner_m[k];
+    if (base) *base = a;
+    return true;
+}
+
+// ---------------------------------------------------------------- kernels
+
+constexpr int kWarpsPerBlock = 4;
+
+static int scratch_per_warp(const DevAnsatz &a) {
+    return a.kind == KIND_MLP ? 4 * a.M : 2 * a.M;   // doubles
+}
+
+__global__ void k_log_amp(DevAmp A, const uint64_t *__restrict__ bits, int B, double *la,
+                          double *ar) {
+    extern __shared__ double sm[];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int b = blockIdx.x * kWarpsPerBlock + warp;
+    double *scr = sm + warp * (A.a.kind == KIND_MLP ? 4 * A.a.M : 2 * A.a.M);
+    if (b >= B) return;
+    double l, a;
+    warp_amp_eval(A, bits[b], l, a, scr);
+    if (lane == 0) {
+        if (la) la[b] = l;
+        if (ar) ar[b] = a;
+    }
+}
+
+bool launch_log_amp(const DevAmp &A, const uint64_t *bits, int B, double *la, double *ar) {
+    size_t smem = sizeof(double) * (size_t)scratch_per_warp(A.a) * kWarpsPerBlock;
+    NQS_LAUNCH("log_amp");
+    k_log_amp<<<(B + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, smem, ctx().stream>>>(
+        A, bits, B, la, ar);
+    return NQS_CUDA(cudaGetLastError());
+}
+
+// Writes alpha * d log psi / d theta of configuration `bits` into row `o`
+// (accumulating when acc).  mode 1: real projection (src/nqs/nqs_ansatz.c:885-995);
+// mode 2: holomorphic pair (o = Re, oi = Im; :1025-1091).  `t` is a per-warp
+// scratch of 2*M doubles (4*M for the MLP).
+__device__ void warp_grad_row(const DevAnsatz &a, uint64_t bits, int mode, double *o, double *oi,
+                              double alpha, bool acc, double *t) {
+    int lane = threadIdx.x & 31;
+    const int N = a.N, M = a.M;
+    auto put = [&](double *row, long k, double v) {
+        if (acc) row[k] += alpha * v;
+        else row[k] = alpha * v;
+    };
+    if (a.kind == KIND_MF) {
+        for (int i = lane; i < N; i += 32) {
+            put(o, i, (double)spin_of(bits, i));
+            if (mode == 2) put(oi, i, 0.0);
+        }
+        return;
+    }
+    if (a.kind == KIND_MLP) {
+        // back-propagation through the two tanh layers (extension)
+        double *h1 = t, *h2 = t + M, *d2 = t + 2 * M, *d1 = t + 3 * M;
+        const double *b1 = a.p + (long)M * N, *W2 = b1 + M, *b2 = W2 + (long)M * M;
+        const double *wr = b2 + M, *wi = wr + M;
+        for (int k = lane; k < M; k += 32) {
+            double z = b1[k];
+            for (int i = 0; i < N; i++) z += a.wtr[(long)i * M + k] * (double)spin_of(bits, i);
+            h1[k] = tanh(z);
+        }
+        __syncwarp();
+        for (int j = lane; j < M; j += 32) {
+            double z = b2[j];
+            for (int k = 0; k < M; k++) z += a.wti[(long)k * M + j] * h1[k];
+            h2[j] = tanh(z);
+        }
+        __syncwarp();
+        long o_b1 = (long)M * N, o_W2 = o_b1 + M, o_b2 = o_W2 + (long)M * M, o_wr = o_b2 + M;
+        for (int pass = 0; pass < (mode == 2 ? 2 : 1); pass++) {
+            double *row = pass ? oi : o;
+            const double *head = pass ? wi : wr;
+            for (int j = lane; j < M; j += 32) d2[j] = head[j] * (1.0 - h2[j] * h2[j]);
+            __syncwarp();
+            for (int k = lane; k < M; k += 32) {
+                double s = 0.0;
+                for (int j = 0; j < M; j++) s += W2[(long)j * M + k] * d2[j];
+                d1[k] = s * (1.0 - h1[k] * h1[k]);
+            }
+            __syncwarp();
+            for (long q = lane; q < (long)M * N; q += 32) {
+                int k = (int)(q / N), i = (int)(q % N);
+                put(row, q, d1[k] * (double)spin_of(bits, i));
+            }
+            for (int k = lane; k < M; k += 32) put(row, o_b1 + k, d1[k]);
+            for (long q = lane; q < (long)M * M; q += 32) {
+                int j = (int)(q / M), k = (int)(q % M);
+                put(row, o_W2 + q, d2[j] * h1[k]);
+            }
+            for (int j = lane; j < M; j += 32) {
+                put(row, o_b2 + j, d2[j]);
+                put(row, o_wr + j, pass == 0 ? h2[j] : 0.0);
+                put(row, o_wr + M + j, pass == 0 ? 0.0 : h2[j]);
+            }
+            if (lane == 0) {
+                put(row, o_wr + 2 * M, pass == 0 ? 1.0 : 0.0);
+                put(row, o_wr + 2 * M + 1, pass == 0 ? 0.0 : 1.0);
+            }
+            __syncwarp();
+        }
+        return;
+    }
+    // RBM / complex RBM: tanh of every hidden pre-activation into t[]
+    double *tr = t, *ti = t + M;
+    for (int h = lane; h < M; h += 32) {
+        double xr, xi;
+        rbm_theta(a, bits, h, xr, xi);
+        if (a.kind == KIND_RBM) {
+            tr[h] = tanh(xr);
+            ti[h] = 0.0;
+        } else {
+            double r, i;
+            ctanh_d(xr, xi, r, i);
+            tr[h] = r;
+            ti[h] = i;
+        }
+    }
+    __syncwarp();
+    if (a.kind == KIND_RBM) {
+        for (long k = lane; k < a.P; k += 32) {
+            double v;
+            if (k < N) v = (double)spin_of(bits, (int)k);
+            else if (k < N + M) v = tr[k - N];
+            else {
+                long q = k - N - M;
+                v = tr[q / N] * (double)spin_of(bits, (int)(q % N));
+            }
+            put(o, k, v);
+            if (mode == 2) put(oi, k, 0.0);
+        }
+        __syncwarp();
+        return;
+    }
+    long Pr = crbm_pr(a);
+    for (long k = lane; k < Pr; k += 32) {
+        double sr, si;   // (re, im) of d log psi / d theta_R; d/d theta_I = i * that
+        if (k < N) {
+            sr = (double)spin_of(bits, (int)k);
+            si = 0.0;
+        } else if (k < N + M) {
+            sr = tr[k - N];
+            si = ti[k - N];
+        } else {
+            long q = k - N - M;
+            double s = (double)spin_of(bits, (int)(q % N));
+            sr = tr[q / N] * s;
+            si = ti[q / N] * s;
+        }
+        if (mode == 2) {
+            put(o, k, sr);
+            put(oi, k, si);
+            put(o, Pr + k, -si);
+            put(oi, Pr + k, sr);
+        } else {
+            put(o, k, sr);
+            // real projection: d log|psi| / d theta_I = -Im(...), and 0 for the visible block
+            put(o, Pr + k, k < N ? 0.0 : -si);
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void k_gradient(DevAnsatz a, const uint64_t *__restrict__ bits, int B, int mode, double *O,
+                           double *Oi) {
+    extern __shared__ double sm[];
+    int warp = threadIdx.x >> 5;
+    int b = blockIdx.x * kWarpsPerBlock + warp;
+    double *scr = sm + warp * (a.kind == KIND_MLP ? 4 * a.M : 2 * a.M);
+    if (b >= B) return;
+    warp_grad_row(a, bits[b], mode, O + (size_t)b * a.P, Oi ? Oi + (size_t)b * a.P : nullptr, 1.0,
+                  false, scr);
+}
+
+// Symmetry-projected gradient, src/nqs/nqs_symproj.c:82-155: the weights
+// w_g = chi_g cos(arg_g) e^{lp_g - max} / sum_g' (...) are formed first, then
+// the G base gradients are accumulated into the row in ascending g.
+__global__ void k_symproj_gradient(DevAmp A, const uint64_t *__restrict__ bits, int B, double *O,
+                                   double *wbuf) {
+    extern __shared__ double sm[];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int b = blockIdx.x * kWarpsPerBlock + warp;
+    double *scr = sm + warp * (A.a.kind == KIND_MLP ? 4 * A.a.M : 2 * A.a.M);
+    if (b >= B) return;
+    const int N = A.a.N, G = A.G;
+    uint64_t s = bits[b];
+    double *lp = wbuf + (size_t)b * 2 * G, *cs = lp + G;
+    double mx = -1e300;
+    for (int g = 0; g < G; g++) {
+        uint64_t pb = permute_bits(s, A.perm + (long)g * N, N);
+        double l, a;
+        warp_base_eval(A.a, pb, l, a, scr);
+        a = apply_marshall(a, pb, A.n_inner, A.inner_mask);
+        if (lane == 0) {
+            lp[g] = l;
+            cs[g] = A.chars[g] * cos(a);
+        }
+        mx = fmax(mx, l);
+    }
+    __syncwarp();
+    double den = 0.0;
+    for (int g = 0; g < G; g++) den += cs[g] * exp(lp[g] - mx);
+    double *row = O + (size_t)b * A.a.P;
+    for (long k = lane; k < A.a.P; k += 32) row[k] = 0.0;
+    __syncwarp();
+    if (den == 0.0) return;
+    for (int g = 0; g < G; g++) {
+        double w = cs[g] * exp(lp[g] - mx) / den;
+        if (w == 0.0) continue;
+        uint64_t pb = permute_bits(s, A.perm + (long)g * N, N);
+        warp_grad_row(A.a, pb, 1, row, nullptr, w, true, scr);
+    }
+}
+
+static DevBuf<double> g_symw;
+
+bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O) {
+    if (!g_symw.ensure((size_t)B * 2 * A.G)) return false;
+    size_t smem = sizeof(double) * (size_t)scratch_per_warp(A.a) * kWarpsPerBlock;
+    NQS_LAUNCH("symproj_gradient");
+    k_symproj_gradient<<<(B + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, smem,
+                         ctx().stream>>>(A, bits, B, O, g_symw.p);
+    return NQS_CUDA(cudaGetLastError());
+}
+
+bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, double *O,
+                            double *Oi) {
+    size_t smem = sizeof(double) * (size_t)scratch_per_warp(a) * kWarpsPerBlock;
+    NQS_LAUNCH("gradient");
+    k_gradient<<<(B + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, smem, ctx().stream>>>(
+        a, bits, B, mode, O, Oi);
+    return NQS_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- apply update
+__global__ void k_axpy(double *p, const double *__restrict__ d, double step, long n) {
+    long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) p[k] += step * d[k];
+}
+
+static DevBuf<double> g_delta_stage;
+
+}  // namespace nqs
+
+using namespace nqs;
+
+// ---------------------------------------------------------------- C ABI
+
+extern "C" {
+
+nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
+    clear_error();
+    if (!cfg || num_sites <= 0) return nullptr;
+    int kind = (int)cfg->ansatz;
+    if (kind != KIND_MF && kind != KIND_RBM && kind != KIND_CRBM && kind != KIND_MLP) {
+        set_error("ansatz kind %d is not available in this build", kind);
+        return nullptr;
+    }
+    if (num_sites > kMaxSites) {
+        set_error("num_sites %d > %d", num_sites, kMaxSites);
+        return nullptr;
+    }
+    if (!ensure_context()) return nullptr;
+    int M = 0;
+    if (kind == KIND_RBM || kind == KIND_CRBM)
+        M = cfg->rbm_hidden_units > 0 ? cfg->rbm_hidden_units : 2 * num_sites;
+    if (kind == KIND_MLP) {
+        M = cfg->width > 0 ? cfg->width : 4 * num_sites;
+        if (cfg->depth != 2) {
+            set_error("deep MLP supports depth = 2 hidden layers (got %d)", cfg->depth);
+            return nullptr;
+        }
+    }
+    if (M > 32 * kMaxJ) {
+        set_error("hidden width %d > %d", M, 32 * kMaxJ);
+        return nullptr;
+    }
+    Ansatz *a = new Ansatz();
+    a->kind = kind;
+    a->N = num_sites;
+    a->M = M;
+    a->P = num_params_of(kind, num_sites, M);
+    size_t bytes = sizeof(double) * (size_t)a->P;
+    if (!NQS_CUDA(cudaMallocHost(&a->h_params, bytes)) || !(a->h_shadow = (double *)malloc(bytes)) ||
+        !a->d_params.ensure((size_t)a->P) ||
+        !a->d_wtr.ensure((size_t)num_sites * (M ? M : 1) + (kind == KIND_MLP ? 0 : 0)) ||
+        !a->d_wti.ensure(kind == KIND_MLP ? (size_t)M * M : (size_t)num_sites * (M ? M : 1))) {
+        nqs_ansatz_free((nqs_ansatz_t *)a);
+        return nullptr;
+    }
+    init_params(cfg, kind, num_sites, M, a->h_params);
+    if (!ansatz_sync(a) || !NQS_CUDA(cudaStreamSynchronize(ctx().stream))) {
+        nqs_ansatz_free((nqs_ansatz_t *)a);
+        return nullptr;
+    }
+    return (nqs_ansatz_t *)a;
+}
+
+void nqs_ansatz_free(nqs_ansatz_t *h) {
+    Ansatz *a = (Ansatz *)h;
+    if (!a) return;
+    if (a->h_params) cudaFreeHost(a->h_params);
+    free(a->h_shadow);
+    delete a;
+}
+
+long nqs_ansatz_num_params(const nqs_ansatz_t *h) { return h ? ((const Ansatz *)h)->P : 0; }
+
+int nqs_ansatz_is_complex(const nqs_ansatz_t *h) {
+    if (!h) return 0;
+    int k = ((const Ansatz *)h)->kind;
+    return (k == KIND_CRBM || k == KIND_MLP) ? 1 : 0;
+}
+
+double *nqs_ansatz_params_raw(nqs_ansatz_t *h) { return h ? ((Ansatz *)h)->h_params : nullptr; }
+
+int nqs_ansatz_apply_update(nqs_ansatz_t *h, const double *delta, double step) {
+    Ansatz *a = (Ansatz *)h;
+    if (!a || !delta) return -1;
+    if (!ensure_context() || !ansatz_sync(a)) return -1;
+    if (!g_delta_stage.ensure((size_t)a->P)) return -1;
+    Context &c = ctx();
+    if (!NQS_CUDA(cudaMemcpyAsync(g_delta_stage.p, delta, sizeof(double) * a->P,
+                                  cudaMemcpyHostToDevice, c.stream)))
+        return -1;
+    {
+        NQS_LAUNCH("apply_update");
+        k_axpy<<<(unsigned)((a->P + 255) / 256), 256, 0, c.stream>>>(a->d_params.p, g_delta_stage.p,
+                                                                   step, a->P);
+    }
+    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a) || !ansatz_pull(a)) return -1;
+    return 0;
+}
+
+static int scalar_log_amp(nqs_log_amp_fn_t fn, const int *spins, int N, void *user, double *la,
+                          double *ar) {
+    if (!ensure_context()) return -1;
+    DevAmp A;
+    if (!build_amp(fn, user, N, &A, nullptr)) return -1;
+    uint64_t *bits;
+    if (!upload_spins(spins, 1, N, &bits)) return -1;
+    static DevBuf<double> out;
+    if (!out.ensure(2)) return -1;
+    if (!launch_log_amp(A, bits, 1, out.p, out.p + 1)) return -1;
+    double h[2];
+    if (!NQS_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, ctx().stream)) ||
+        !NQS_CUDA(cudaStreamSynchronize(ctx().stream)))
+        return -1;
+    *la = h[0];
+    *ar = h[1];
+    return 0;
+}
+
+void nqs_ansatz_log_amp(const int *spins, int num_sites, void *user, double *out_log_abs,
+                        double *out_arg) {
+    double la = 0.0, ar = 0.0;
+    Ansatz *a = (Ansatz *)user;
+    if (a && spins && num_sites == a->N) {                 // src/nqs/nqs_ansatz.c:851-872
+        if (scalar_log_amp(nqs_ansatz_log_amp, spins, num_sites, user, &la, &ar) != 0) la = ar = 0.0;
+    }
+    if (out_log_abs) *out_log_abs = la;
+    if (out_arg) *out_arg = ar;
+}
+
+void nqs_marshall_log_amp(const int *spins, int num_sites, void *user, double *out_log_abs,
+                          double *out_arg) {
+    double la = 0.0, ar = 0.0;
+    if (user && spins) scalar_log_amp(nqs_marshall_log_amp, spins, num_sites, user, &la, &ar);
+    if (out_log_abs) *out_log_abs = la;
+    if (out_arg) *out_arg = ar;
+}
+
+void nqs_symproj_log_amp(const int *spins, int num_sites, void *user, double *out_log_abs,
+                         double *out_arg) {
+    double la = 0.0, ar = 0.0;
+    auto *w = (nqs_symproj_wrapper_t *)user;
+    if (w && spins && num_sites == w->num_sites)
+        if (scalar_log_amp(nqs_symproj_log_amp, spins, num_sites, user, &la, &ar) != 0) la = ar = 0.0;
+    if (out_log_abs) *out_log_abs = la;
+    if (out_arg) *out_arg = ar;
+}
+
+int nqs_marshall_parity(const int *spins, int size_x, int size_y) {
+    // src/nqs/nqs_marshall.c:16-27 (host utility; the device program uses a popcount)
+    int n = 0;
+    for (int x = 0; x < size_x; x++)
+        for (int y = 0; y < size_y; y++)
+            if (((x + y) & 1) == 0 && spins[x * size_y + y] < 0) n++;
+    return n & 1;
+}
+
+int nqs_gpu_log_amp_batch(nqs_log_amp_fn_t fn, void *user, const int *spins, int B, int N,
+                          double *out_la, double *out_ar) {
+    clear_error();
+    if (!spins || B <= 0 || !ensure_context()) return -1;
+    DevAmp A;
+    if (!build_amp(fn, user, N, &A, nullptr)) return -1;
+    uint64_t *bits;
+    if (!upload_spins(spins, B, N, &bits)) return -1;
+    static DevBuf<double> out;
+    if (!out.ensure(2 * (size_t)B)) return -1;
+    if (!launch_log_amp(A, bits, B, out.p, out.p + B)) return -1;
+    Context &c = ctx();
+    if (out_la && !NQS_CUDA(cudaMemcpyAsync(out_la, out.p, sizeof(double) * B, cudaMemcpyDeviceToHost,
+                                            c.stream)))
+        return -1;
+    if (out_ar && !NQS_CUDA(cudaMemcpyAsync(out_ar, out.p + B, sizeof(double) * B,
+                                            cudaMemcpyDeviceToHost, c.stream)))
+        return -1;
+    return NQS_CUDA(cudaStreamSynchronize(c.stream)) ? 0 : -1;
+}
+
+int nqs_gpu_gradient_batch(nqs_ansatz_t *h, nqs_gradient_fn_t gfn, void *guser, const int *spins,
+                           int B, int complex_out, double *out_re, double *out_im) {
+    clear_error();
+    Ansatz *a = (Ansatz *)h;
+    if (!a || !spins || B <= 0 || !out_re || (complex_out && !out_im)) return -1;
+    if (!ensure_context() || !ansatz_sync(a)) return -1;
+    uint64_t *bits;
+    if (!upload_spins(spins, B, a->N, &bits)) return -1;
+    static DevBuf<double> O;
+    if (!O.ensure((size_t)B * a->P * (complex_out ? 2 : 1))) return -1;
+    if (gfn == nullptr) {
+        if (!launch_gradient(ansatz_dev(a), bits, B, complex_out ? 2 : 1, O.p,
+                             complex_out ? O.p + (size_t)B * a->P : nullptr))
+            return -1;
+    } else if (gfn == nqs_symproj_gradient && !complex_out) {
+        DevAmp A;
+        if (!build_amp(nqs_symproj_log_amp, guser, a->N, &A, nullptr)) return -1;
+        if (!launch_symproj_gradient(A, bits, B, O.p)) return -1;
+    } else {
+        set_error("gradient callback is not supported on the GPU");
+        return -1;
+    }
+    Context &c = ctx();
+    size_t bytes = sizeof(double) * (size_t)B * a->P;
+    if (!NQS_CUDA(cudaMemcpyAsync(out_re, O.p, bytes, cudaMemcpyDeviceToHost, c.stream))) return -1;
+    if (complex_out &&
+        !NQS_CUDA(cudaMemcpyAsync(out_im, O.p + (size_t)B * a->P, bytes, cudaMemcpyDeviceToHost, c.stream)))
+        return -1;
+    return NQS_CUDA(cudaStreamSynchronize(c.stream)) ? 0 : -1;
+}
+
+int nqs_ansatz_logpsi_gradient(nqs_ansatz_t *h, const int *spins, int num_sites, double *out) {
+    Ansatz *a = (Ansatz *)h;
+    if (!a || !spins || !out || num_sites != a->N) return -1;
+    return nqs_gpu_gradient_batch(h, nullptr, nullptr, spins, 1, 0, out, nullptr);
+}
+
+int nqs_ansatz_logpsi_gradient_complex(nqs_ansatz_t *h, const int *spins, int num_sites, double *re,
+                                       double *im) {
+    Ansatz *a = (Ansatz *)h;
+    if (!a || !spins || !re || !im || num_sites != a->N) return -1;
+    return nqs_gpu_gradient_batch(h, nullptr, nullptr, spins, 1, 1, re, im);
+}
+
+int nqs_symproj_gradient(void *grad_user, nqs_ansatz_t *h, const int *spins, int num_sites,
+                         double *out) {
+    auto *w = (nqs_symproj_wrapper_t *)grad_user;
+    if (!w || !h || !spins || !out || num_sites != w->num_sites) return -1;
+    return nqs_gpu_gradient_batch(h, nqs_symproj_gradient, grad_user, spins, 1, 0, out, nullptr);
+}
+
+// Kagome permutation tables: host-side set-up restating
+// src/nqs/nqs_symproj.c:269-371 (translations, and translations x C2).
+#define KG_SITE(cx, cy, sub, Ly) (3 * ((cx) * (Ly) + (cy)) + (sub))
+
+int nqs_kagome_translation_perm(int Lx, int Ly, int **out_perm, int *out_G) {
+    if (Lx <= 0 || Ly <= 0 || !out_perm || !out_G) return -1;
+    int N = 3 * Lx * Ly, G = Lx * Ly;
+    int *perm = (int *)malloc(sizeof(int) * (size_t)G * N);
+    if (!perm) return -1;
+    int g = 0;
+    for (int tx = 0; tx < Lx; tx++)
+        for (int ty = 0; ty < Ly; ty++, g++)
+            for (int cx = 0; cx < Lx; cx++)
+                for (int cy = 0; cy < Ly; cy++)
+                    for (int sub = 0; sub < 3; sub++)
+                        perm[(size_t)g * N + KG_SITE(cx, cy, sub, Ly)] =
+                            KG_SITE((cx + tx) % Lx, (cy + ty) % Ly, sub, Ly);
+    *out_perm = perm;
+    *out_G = G;
+    return 0;
+}
+
+int nqs_kagome_p2_perm(int Lx, int Ly, int **out_perm, double **out_chars, int *out_G) {
+    if (Lx <= 0 || Ly <= 0 || !out_perm || !out_chars || !out_G) return -1;
+    int N = 3 * Lx * Ly, G = 2 * Lx * Ly;
+    int *perm = (int *)malloc(sizeof(int) * (size_t)G * N);
+    double *chars = (double *)malloc(sizeof(double) * (size_t)G);
+    if (!perm || !chars) {
+        free(perm);
+        free(chars);
+        return -1;
+    }
+    int g = 0;
+    for (int half = 0; half < 2; half++)
+        for (int tx = 0; tx < Lx; tx++)
+            for (int ty = 0; ty < Ly; ty++, g++) {
+                for (int cx = 0; cx < Lx; cx++)
+                    for (int cy = 0; cy < Ly; cy++)
+                        for (int sub = 0; sub < 3; sub++) {
+                            int xs, ys;
+                            if (!half) {
+                                xs = (cx + tx) % Lx;
+                                ys = (cy + ty) % Ly;
+                            } else {   // C2 through the A site: B -> -a1, C -> -a2
+                                int dx = sub == 1 ? -1 : 0, dy = sub == 2 ? -1 : 0;
+                                xs = ((-cx + dx + tx) % Lx + Lx) % Lx;
+                                ys = ((-cy + dy + ty) % Ly + Ly) % Ly;
+                            }
+                            perm[(size_t)g * N + KG_SITE(cx, cy, sub, Ly)] = KG_SITE(xs, ys, sub, Ly);
+                        }
+                chars[g] = 1.0;
+            }
+    *out_perm = perm;
+    *out_chars = chars;
+    *out_G = G;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,251 @@
+// Internal declarations shared by the translation units of libnqs_gb300.so.
+//
+// Data layout in HBM (one GPU, one stream):
+//   * parameters: FP64 in the upstream layout (src/nqs/nqs_ansatz.c:39-41,
+//     :219-247) plus derived copies transposed to [site][hidden] so that a warp
+//     whose lanes own hidden units reads one weight column with one coalesced
+//     256-byte load per flipped site;
+//   * configurations: one uint64 per configuration, bit i = 1 <-> spin -1
+//     (the basis convention of src/nqs/nqs_lanczos.c:16-20), N <= 64;
+//   * Jacobian O: FP64 row-major [N_s][N_p] exactly as the upstream optimiser
+//     (src/nqs/nqs_optimizer.c:164), so that the row and column sweeps of the
+//     solvers are unit-stride.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+extern "C" {
+#include "nqs/nqs_config.h"
+#include "nqs/nqs_ansatz.h"
+#include "nqs/nqs_sampler.h"
+#include "nqs/nqs_gradient.h"
+#include "nqs/nqs_optimizer.h"
+#include "nqs/nqs_marshall.h"
+#include "nqs/nqs_symproj.h"
+#include "nqs/nqs_gpu.h"
+}
+
+namespace nqs {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kMaxSites = 64;
+constexpr int kMaxJ = 8;           // hidden units per lane -> M <= 256
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+void clear_error();
+bool cuda_ok(cudaError_t e, const char *what);
+#define NQS_CUDA(call) ::nqs::cuda_ok((call), #call)
+
+// ---------------------------------------------------------------- context
+struct ProfEvent {
+    const char *name;
+    cudaEvent_t a, b;
+};
+
+struct Context {
+    bool initialised = false;
+    bool usable = false;
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    nqs_gpu_options_t opts{};
+    std::mutex mu;
+    bool profiling = false;
+    std::vector<ProfEvent> prof_pending;
+    std::map<std::string, std::pair<long, double>> prof_done;
+    long launches = 0;
+};
+Context &ctx();
+bool ensure_context();              // false (and error set) when no usable device
+
+// Bracket a launch with profiling events when enabled and count it.
+struct LaunchScope {
+    ProfEvent ev{};
+    bool on;
+    explicit LaunchScope(const char *name);
+    ~LaunchScope();
+};
+#define NQS_LAUNCH(name) ::nqs::LaunchScope _nqs_ls_##__LINE__(name)
+
+// ---------------------------------------------------------------- device buffers
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    bool ensure(size_t count) {
+        if (count <= n && p) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        if (count == 0) count = 1;
+        if (!NQS_CUDA(cudaMalloc(&p, count * sizeof(T)))) return false;
+        n = count;
+        return true;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+};
+
+// ---------------------------------------------------------------- device program
+enum : int { KIND_MF = 0, KIND_RBM = 5, KIND_CRBM = 6, KIND_MLP = NQS_GPU_ANSATZ_MLP };
+
+struct DevAnsatz {
+    int kind, N, M;
+    long P;
+    const double *p;     // device params, upstream layout
+    const double *wtr;   // [N][M] real weights transposed (RBM, cRBM); MLP: W1^T
+    const double *wti;   // [N][M] imaginary weights transposed (cRBM); MLP: W2^T [M][M]
+};
+
+struct DevAmp {
+    DevAnsatz a;
+    int n_outer;                 // Marshall layers outside the projection
+    uint64_t outer_mask[3];
+    int G;                       // symmetry projection group size, 0 = none
+    const int *perm;             // [G][N] device
+    const double *chars;         // [G] device
+    int n_inner;                 // Marshall layers inside the projection
+    uint64_t inner_mask[3];
+};
+
+// Hamiltonian as bond groups (built on the host from the lattice, in the
+// upstream enumeration order; see hamiltonian_build()).
+struct DevHam {
+    int kind;           // NQS_HAM_*
+    int N;
+    int nb1, nb2;       // bond counts: group 1 (NN / kagome), group 2 (J1-J2 diagonals)
+    const int *b1;      // [nb1][2] device
+    const int *b2;      // [nb2][2] device
+    double J, J2, Jz, Jxy, Gamma;
+};
+
+// ---------------------------------------------------------------- host objects
+struct Ansatz {
+    int kind, N, M;
+    long P;
+    double *h_params = nullptr;     // pinned host mirror (returned by params_raw)
+    double *h_shadow = nullptr;     // last value known to be on the device
+    DevBuf<double> d_params, d_wtr, d_wti;
+    bool dev_valid = false;
+};
+
+// Upload the host mirror when it changed (or always with force: the SR steps
+// take the mirror as the step's input).
+bool ansatz_sync(Ansatz *a, bool force = false);
+bool ansatz_refresh_derived(Ansatz *a);      // rebuild transposed copies (device)
+bool ansatz_pull(Ansatz *a);                 // device -> host mirror
+DevAnsatz ansatz_dev(const Ansatz *a);
+
+// Resolve a (log_amp, user) callback pair into a device program.
+bool build_amp(nqs_log_amp_fn_t fn, void *user, int num_sites, DevAmp *out, Ansatz **base);
+bool hamiltonian_build(const nqs_config_t *cfg, int size_x, int size_y, DevHam *out);
+
+// configurations: host int +-1 [B][N] <-> device bits
+bool upload_spins(const int *spins, int B, int N, uint64_t **d_bits);
+uint64_t pack_spins(const int *s, int N);
+
+// kernels exported across translation units
+bool launch_log_amp(const DevAmp &A, const uint64_t *bits, int B, double *la, double *ar);
+bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B,
+                            double *E_re, double *E_im, double *O, double *O_im, int grad_mode);
+bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, double *O, double *Oi);
+bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
+bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
+
+// thread-local statistics of the last SR step
+nqs_gpu_step_stats_t &step_stats();
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;   // XOR butterfly: every lane ends with the bitwise-identical sum
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ int spin_of(uint64_t bits, int i) {
+    return 1 - 2 * (int)((bits >> i) & 1ull);
+}
+
+// log(2 cosh z) for z = x + i y in the overflow-safe form used upstream
+// (src/nqs/nqs_ansatz.c:309-318): with e = exp(-2|x|),
+//   2 cosh z = e^{|x|} ((1 + e) cos y + i sgn(x) (1 - e) sin y).
+__device__ __forceinline__ void clogcosh(double x, double y, double &la, double &ar) {
+    double ax = fabs(x);
+    double e = exp(-2.0 * ax);
+    double sy, cy;
+    sincos(y, &sy, &cy);
+    double re = (1.0 + e) * cy;
+    double im = (x >= 0.0 ? 1.0 : -1.0) * (1.0 - e) * sy;
+    double mag = hypot(re, im);
+    la = ax + (mag > 0.0 ? log(mag) : -1e300);
+    ar = atan2(im, re);
+}
+
+// Re log(2 cosh z) only: |x| + 0.5 log(1 + 2 e cos 2y + e^2), e = exp(-2|x|).
+__device__ __forceinline__ double rlogcosh(double x, double y) {
+    double ax = fabs(x);
+    double e = exp(-2.0 * ax);
+    return ax + 0.5 * log1p(e * (2.0 * cos(2.0 * y) + e));
+}
+
+// Real log(2 cosh x), src/nqs/nqs_ansatz.c:291.
+__device__ __forceinline__ double logcosh_r(double x) {
+    double ax = fabs(x);
+    return ax + log1p(exp(-2.0 * ax));
+}
+
+// tanh(x + i y) through sinh / cosh, the formula of src/nqs/nqs_ansatz.c:961-972.
+__device__ __forceinline__ void ctanh_d(double x, double y, double &tr, double &ti) {
+    double cxr = cosh(x), sxr = sinh(x);
+    double sy, cy;
+    sincos(y, &sy, &cy);
+    double nr = sxr * cy, ni = cxr * sy;
+    double dr = cxr * cy, di = sxr * sy;
+    double den = dr * dr + di * di;
+    if (den < 1e-300) den = 1e-300;
+    tr = (nr * dr + ni * di) / den;
+    ti = (ni * dr - nr * di) / den;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), computed redundantly by
+// every lane of a warp so that a chain's random numbers need no shuffles.
+__device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        uint4 n;
+        n.x = hi1 ^ c.y ^ k.x;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k.y;
+        n.w = lo0;
+        c = n;
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+}  // namespace nqs

@@ -1,0 +1,527 @@
+// Local energies: bond tables, the fused local-estimator kernel and the
+// nqs_local_energy* entry points.
+//
+// Fused estimator (RBM / complex RBM, any Marshall layers): one warp per
+// sample.  Each lane computes theta_h for its hidden units once, caches
+// log(2 cosh theta_h), and every connected configuration s' (single flip at u
+// or pair flip (u, v)) costs one O(M) update
+//     theta'_h = theta_h - 2 s_u W_hu [- 2 s_v W_hv]
+// plus M complex log-cosh evaluations and one warp butterfly, instead of the
+// upstream O(N M) recomputation per connected configuration
+// (src/nqs/nqs_gradient.c:24-30).  The same theta feeds the Jacobian row.
+#include <math.h>
+
+#include "nqs_amp.cuh"
+
+namespace nqs {
+
+// ---------------------------------------------------------------- bond tables
+
+// Square / chain nearest-neighbour bonds in the upstream enumeration order
+// (src/nqs/nqs_gradient.c:60-67, :98-107): for x, for y, the +x bond then the
+// +y bond.  Periodic mode wraps a neighbour whenever the extent exceeds 1.
+static void square_bonds(int Lx, int Ly, int pbc, std::vector<int> &b) {
+    for (int x = 0; x < Lx; x++)
+        for (int y = 0; y < Ly; y++) {
+            int a = x * Ly + y;
+            if (x + 1 < Lx) { b.push_back(a); b.push_back((x + 1) * Ly + y); }
+            else if (pbc && Lx > 1) { b.push_back(a); b.push_back(y); }
+            if (y + 1 < Ly) { b.push_back(a); b.push_back(x * Ly + y + 1); }
+            else if (pbc && Ly > 1) { b.push_back(a); b.push_back(x * Ly); }
+        }
+}
+
+// J1-J2 next-nearest bonds, src/nqs/nqs_gradient.c:146-159: for each
+// plaquette the (x,y)-(x+1,y+1) diagonal then the (x,y+1)-(x+1,y) one.
+static void diagonal_bonds(int Lx, int Ly, int pbc, std::vector<int> &b) {
+    int xe = (pbc && Lx > 1) ? Lx : Lx - 1, ye = (pbc && Ly > 1) ? Ly : Ly - 1;
+    for (int x = 0; x < xe; x++)
+        for (int y = 0; y < ye; y++) {
+            int x1 = (x + 1) % Lx, y1 = (y + 1) % Ly;
+            b.push_back(x * Ly + y); b.push_back(x1 * Ly + y1);
+            b.push_back(x * Ly + y1); b.push_back(x1 * Ly + y);
+        }
+}
+
+// Kagome bonds, src/nqs/nqs_gradient.c:374-445: per unit cell the up-triangle
+// (A-B, A-C, B-C) then the down-triangle {A(cx,cy), B(cx-1,cy), C(cx,cy-1)},
+// site 3*(cx*Ly+cy)+sub; open boundaries drop down-triangles at cx=0 or cy=0.
+static void kagome_bonds(int Lx, int Ly, int pbc, std::vector<int> &b) {
+    auto S = [&](int cx, int cy, int sub) { return 3 * (cx * Ly + cy) + sub; };
+    for (int cx = 0; cx < Lx; cx++)
+        for (int cy = 0; cy < Ly; cy++) {
+            int A = S(cx, cy, 0), B = S(cx, cy, 1), C = S(cx, cy, 2);
+            int up[6] = {A, B, A, C, B, C};
+            b.insert(b.end(), up, up + 6);
+            int cxm, cym;
+            if (pbc) { cxm = (cx - 1 + Lx) % Lx; cym = (cy - 1 + Ly) % Ly; }
+            else {
+                if (cx == 0 || cy == 0) continue;
+                cxm = cx - 1;
+                cym = cy - 1;
+            }
+            int Bm = S(cxm, cy, 1), Cm = S(cx, cym, 2);
+            int dn[6] = {A, Bm, A, Cm, Bm, Cm};
+            b.insert(b.end(), dn, dn + 6);
+        }
+}
+
+struct BondEntry {
+    DevBuf<int> d;
+    int n1 = 0, n2 = 0;
+};
+static std::map<std::string, BondEntry *> g_bonds;
+
+bool hamiltonian_build(const nqs_config_t *cfg, int size_x, int size_y, DevHam *H) {
+    memset(H, 0, sizeof(*H));
+    int kind = (int)cfg->hamiltonian;
+    int pbc = ctx().opts.square_pbc;
+    if (size_x <= 0 || size_y <= 0) {
+        set_error("invalid lattice %d x %d", size_x, size_y);
+        return false;
+    }
+    std::vector<int> b1, b2;
+    switch (kind) {
+        case NQS_HAM_TFIM:
+        case NQS_HAM_HEISENBERG:
+        case NQS_HAM_XXZ:
+            square_bonds(size_x, size_y, pbc, b1);
+            break;
+        case NQS_HAM_J1_J2:
+            square_bonds(size_x, size_y, pbc, b1);
+            diagonal_bonds(size_x, size_y, pbc, b2);
+            break;
+        case NQS_HAM_KAGOME_HEISENBERG:
+            kagome_bonds(size_x, size_y, cfg->kagome_pbc, b1);
+            pbc = cfg->kagome_pbc;
+            break;
+        default:
+            set_error("Hamiltonian kind %d is not implemented on the GPU", kind);
+            return false;
+    }
+    H->kind = kind;
+    H->N = kind == NQS_HAM_KAGOME_HEISENBERG ? 3 * size_x * size_y : size_x * size_y;
+    if (H->N > kMaxSites) {
+        set_error("lattice has %d sites > %d", H->N, kMaxSites);
+        return false;
+    }
+    char key[96];
+    snprintf(key, sizeof(key), "%d:%d:%d:%d", kind, size_x, size_y, pbc);
+    BondEntry *&e = g_bonds[key];
+    if (!e) {
+        e = new BondEntry();
+        e->n1 = (int)b1.size() / 2;
+        e->n2 = (int)b2.size() / 2;
+        std::vector<int> all(b1);
+        all.insert(all.end(), b2.begin(), b2.end());
+        if (!e->d.ensure(all.size() + 2)) return false;
+        if (!all.empty() &&
+            !NQS_CUDA(cudaMemcpy(e->d.p, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice)))
+            return false;
+    }
+    H->nb1 = e->n1;
+    H->nb2 = e->n2;
+    H->b1 = e->d.p;
+    H->b2 = e->d.p + 2 * e->n1;
+    H->J = cfg->j_coupling;
+    H->J2 = cfg->j2_coupling;
+    H->Jz = kind == NQS_HAM_XXZ ? cfg->j_z_coupling : cfg->j_coupling;
+    H->Jxy = cfg->j_coupling;
+    H->Gamma = cfg->transverse_field;
+    return true;
+}
+
+// ---------------------------------------------------------------- kernels
+
+constexpr int kWarps = 4;
+
+// Jacobian row from precomputed tanh(theta) (tr, ti in shared memory);
+// same layouts as warp_grad_row in nqs_ansatz.cu.
+__device__ void rbm_row_from_t(const DevAnsatz &a, uint64_t bits, int mode, double *o, double *oi,
+                               const double *tr, const double *ti) {
+    int lane = threadIdx.x & 31;
+    const int N = a.N, M = a.M;
+    if (a.kind == KIND_RBM) {
+        for (long k = lane; k < a.P; k += 32) {
+            double v;
+            if (k < N) v = (double)spin_of(bits, (int)k);
+            else if (k < N + M) v = tr[k - N];
+            else {
+                long q = k - N - M;
+                v = tr[q / N] * (double)spin_of(bits, (int)(q % N));
+            }
+            o[k] = v;
+            if (mode == 2) oi[k] = 0.0;
+        }
+        return;
+    }
+    long Pr = crbm_pr(a);
+    for (long k = lane; k < Pr; k += 32) {
+        double sr, si;
+        if (k < N) {
+            sr = (double)spin_of(bits, (int)k);
+            si = 0.0;
+        } else if (k < N + M) {
+            sr = tr[k - N];
+            si = ti[k - N];
+        } else {
+            long q = k - N - M;
+            double s = (double)spin_of(bits, (int)(q % N));
+            sr = tr[q / N] * s;
+            si = ti[q / N] * s;
+        }
+        o[k] = sr;
+        if (mode == 2) {
+            oi[k] = si;
+            o[Pr + k] = -si;
+            oi[Pr + k] = sr;
+        } else {
+            o[Pr + k] = k < N ? 0.0 : -si;
+        }
+    }
+}
+
+template <int J, bool CPLX>
+__global__ void __launch_bounds__(32 * kWarps)
+k_local_rbm(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, double *__restrict__ Er,
+            double *__restrict__ Ei, double *__restrict__ O, double *__restrict__ Oi, int grad_mode,
+            double *__restrict__ la_out) {
+    extern __shared__ double sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarps + warp;
+    if (b >= B) return;
+    const DevAnsatz &a = A.a;
+    const int N = a.N, M = a.M;
+    const double *aR = a.p;
+    const double *aI = a.p + crbm_pr(a);
+    const uint64_t s = bits[b];
+
+    double thr[J], thi[J], lr[J], li[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        int h = lane + 32 * j;
+        thr[j] = thi[j] = lr[j] = li[j] = 0.0;
+        if (h < M) {
+            rbm_theta(a, s, h, thr[j], thi[j]);
+            if (CPLX) clogcosh(thr[j], thi[j], lr[j], li[j]);
+            else lr[j] = logcosh_r(thr[j]);
+        }
+    }
+    const int par0 = marshall_count(A, s);
+
+    // psi(s') / psi(s) for s' = s with sites u (and v >= 0) flipped
+    auto ratio = [&](int u, int v, double &rre, double &rim) {
+        const double su = (double)spin_of(s, u);
+        const double sv = v >= 0 ? (double)spin_of(s, v) : 0.0;
+        double dla = 0.0, dar = 0.0;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            int h = lane + 32 * j;
+            if (h < M) {
+                double xr = thr[j] - 2.0 * su * a.wtr[(long)u * M + h];
+                double xi = thi[j];
+                if (CPLX) xi -= 2.0 * su * a.wti[(long)u * M + h];
+                if (v >= 0) {
+                    xr -= 2.0 * sv * a.wtr[(long)v * M + h];
+                    if (CPLX) xi -= 2.0 * sv * a.wti[(long)v * M + h];
+                }
+                if (CPLX) {
+                    double l2, a2;
+                    clogcosh(xr, xi, l2, a2);
+                    dla += l2 - lr[j];
+                    dar += a2 - li[j];
+                } else {
+                    dla += logcosh_r(xr) - lr[j];
+                }
+            }
+        }
+        dla = warp_sum(dla);
+        if (CPLX) dar = warp_sum(dar);
+        dla += -2.0 * su * aR[u];
+        if (CPLX) dar += -2.0 * su * aI[u];
+        uint64_t s2 = s ^ (1ull << u);
+        if (v >= 0) {
+            dla += -2.0 * sv * aR[v];
+            if (CPLX) dar += -2.0 * sv * aI[v];
+            s2 ^= 1ull << v;
+        }
+        dar += kPi * (double)(marshall_count(A, s2) - par0);
+        double mag = exp(dla);
+        double sn, cs;
+        sincos(dar, &sn, &cs);
+        rre = mag * cs;
+        rim = mag * sn;
+    };
+
+    double e_re, e_im;
+    if (H.kind == NQS_HAM_TFIM) {                        // src/nqs/nqs_gradient.c:50-82
+        double diag = 0.0;
+        for (int k = 0; k < H.nb1; k++)
+            diag += -H.J * (double)(spin_of(s, H.b1[2 * k]) * spin_of(s, H.b1[2 * k + 1]));
+        double ore = 0.0, oim = 0.0;
+        for (int i = 0; i < N; i++) {
+            double r, q;
+            ratio(i, -1, r, q);
+            ore += -H.Gamma * r;
+            oim += -H.Gamma * q;
+        }
+        e_re = diag + ore;
+        e_im = oim;
+    } else {                                             // :87-139, :146-205, :374-445
+        double diag = 0.0, ore = 0.0, oim = 0.0;
+        for (int k = 0; k < H.nb1; k++) {
+            int u = H.b1[2 * k], v = H.b1[2 * k + 1];
+            int su = spin_of(s, u), sv = spin_of(s, v);
+            diag += 0.25 * H.Jz * (double)(su * sv);
+            if (su != sv) {
+                double r, q;
+                ratio(u, v, r, q);
+                ore += 0.5 * H.Jxy * r;
+                oim += 0.5 * H.Jxy * q;
+            }
+        }
+        e_re = diag + ore;
+        e_im = oim;
+        if (H.nb2 > 0) {
+            double d2 = 0.0, r2 = 0.0, i2 = 0.0;
+            for (int k = 0; k < H.nb2; k++) {
+                int u = H.b2[2 * k], v = H.b2[2 * k + 1];
+                int su = spin_of(s, u), sv = spin_of(s, v);
+                d2 += 0.25 * H.J2 * (double)(su * sv);
+                if (su != sv) {
+                    double r, q;
+                    ratio(u, v, r, q);
+                    r2 += 0.5 * H.J2 * r;
+                    i2 += 0.5 * H.J2 * q;
+                }
+            }
+            e_re = e_re + d2 + r2;
+            e_im = e_im + i2;
+        }
+    }
+    if (lane == 0) {
+        if (Er) Er[b] = e_re;
+        if (Ei) Ei[b] = e_im;
+    }
+    if (la_out) {
+        double sr = 0.0;
+#pragma unroll
+        for (int j = 0; j < J; j++) sr += lr[j];
+        double vr, vi;
+        warp_visible(a, s, vr, vi);
+        sr = vr + warp_sum(sr);
+        if (lane == 0) la_out[b] = sr;
+    }
+    if (grad_mode) {
+        double *tr = sm + warp * 2 * M, *ti = tr + M;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            int h = lane + 32 * j;
+            if (h < M) {
+                if (CPLX) ctanh_d(thr[j], thi[j], tr[h], ti[h]);
+                else {
+                    tr[h] = tanh(thr[j]);
+                    ti[h] = 0.0;
+                }
+            }
+        }
+        __syncwarp();
+        rbm_row_from_t(a, s, grad_mode, O + (size_t)b * a.P, Oi ? Oi + (size_t)b * a.P : nullptr, tr, ti);
+    }
+}
+
+// Generic estimator: any program (symmetry projection, MLP).  Every connected
+// configuration is evaluated from scratch, as upstream does.
+__global__ void __launch_bounds__(32 * kWarps)
+k_local_generic(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, double *Er, double *Ei,
+                double *la_out) {
+    extern __shared__ double sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarps + warp;
+    if (b >= B) return;
+    double *scr = sm + warp * 4 * A.a.M;
+    const uint64_t s = bits[b];
+    const int N = A.a.N;
+    double la0, ar0;
+    warp_amp_eval(A, s, la0, ar0, scr);
+    auto ratio = [&](uint64_t s2, double &r, double &q) {
+        double l, g;
+        warp_amp_eval(A, s2, l, g, scr);
+        double mag = exp(l - la0), sn, cs;
+        sincos(g - ar0, &sn, &cs);
+        r = mag * cs;
+        q = mag * sn;
+    };
+    double e_re, e_im;
+    if (H.kind == NQS_HAM_TFIM) {
+        double diag = 0.0;
+        for (int k = 0; k < H.nb1; k++)
+            diag += -H.J * (double)(spin_of(s, H.b1[2 * k]) * spin_of(s, H.b1[2 * k + 1]));
+        double ore = 0.0, oim = 0.0;
+        for (int i = 0; i < N; i++) {
+            double r, q;
+            ratio(s ^ (1ull << i), r, q);
+            ore += -H.Gamma * r;
+            oim += -H.Gamma * q;
+        }
+        e_re = diag + ore;
+        e_im = oim;
+    } else {
+        double diag = 0.0, ore = 0.0, oim = 0.0;
+        for (int k = 0; k < H.nb1; k++) {
+            int u = H.b1[2 * k], v = H.b1[2 * k + 1];
+            int su = spin_of(s, u), sv = spin_of(s, v);
+            diag += 0.25 * H.Jz * (double)(su * sv);
+            if (su != sv) {
+                double r, q;
+                ratio(s ^ (1ull << u) ^ (1ull << v), r, q);
+                ore += 0.5 * H.Jxy * r;
+                oim += 0.5 * H.Jxy * q;
+            }
+        }
+        e_re = diag + ore;
+        e_im = oim;
+        if (H.nb2 > 0) {
+            double d2 = 0.0, r2 = 0.0, i2 = 0.0;
+            for (int k = 0; k < H.nb2; k++) {
+                int u = H.b2[2 * k], v = H.b2[2 * k + 1];
+                int su = spin_of(s, u), sv = spin_of(s, v);
+                d2 += 0.25 * H.J2 * (double)(su * sv);
+                if (su != sv) {
+                    double r, q;
+                    ratio(s ^ (1ull << u) ^ (1ull << v), r, q);
+                    r2 += 0.5 * H.J2 * r;
+                    i2 += 0.5 * H.J2 * q;
+                }
+            }
+            e_re = e_re + d2 + r2;
+            e_im = e_im + i2;
+        }
+    }
+    if (lane == 0) {
+        if (Er) Er[b] = e_re;
+        if (Ei) Ei[b] = e_im;
+        if (la_out) la_out[b] = la0;
+    }
+}
+
+template <int J, bool C>
+static void launch_rbm(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er,
+                       double *Ei, double *O, double *Oi, int gm) {
+    size_t smem = gm ? sizeof(double) * 2 * A.a.M * kWarps : 0;
+    k_local_rbm<J, C><<<(B + kWarps - 1) / kWarps, 32 * kWarps, smem, ctx().stream>>>(A, H, bits, B, Er,
+                                                                                    Ei, O, Oi, gm,
+                                                                                    nullptr);
+}
+
+bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er,
+                            double *Ei, double *O, double *Oi, int grad_mode) {
+    if (A.a.N != H.N) {
+        set_error("ansatz has %d sites, lattice has %d", A.a.N, H.N);
+        return false;
+    }
+    const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
+    if (fused) {
+        int J = (A.a.M + 31) / 32;
+        bool c = A.a.kind == KIND_CRBM;
+        NQS_LAUNCH("local_estimator");
+#define NQS_CASE(JJ)                                                                   \
+    case JJ:                                                                           \
+        if (c) launch_rbm<JJ, true>(A, H, bits, B, Er, Ei, O, Oi, grad_mode);          \
+        else launch_rbm<JJ, false>(A, H, bits, B, Er, Ei, O, Oi, grad_mode);           \
+        break;
+        switch (J) {
+            NQS_CASE(1) NQS_CASE(2) NQS_CASE(3) NQS_CASE(4) NQS_CASE(5) NQS_CASE(6) NQS_CASE(7) NQS_CASE(8)
+            default:
+                set_error("hidden width %d unsupported", A.a.M);
+                return false;
+        }
+#undef NQS_CASE
+        return NQS_CUDA(cudaGetLastError());
+    }
+    {
+        size_t smem = sizeof(double) * 4 * (A.a.M ? A.a.M : 1) * kWarps;
+        NQS_LAUNCH("local_generic");
+        k_local_generic<<<(B + kWarps - 1) / kWarps, 32 * kWarps, smem, ctx().stream>>>(A, H, bits, B, Er,
+                                                                                      Ei, nullptr);
+        if (!NQS_CUDA(cudaGetLastError())) return false;
+    }
+    if (grad_mode) {
+        if (A.G > 0) {
+            if (grad_mode != 1) {
+                set_error("holomorphic gradient through a symmetry projection is not implemented");
+                return false;
+            }
+            return launch_symproj_gradient(A, bits, B, O);
+        }
+        return launch_gradient(A.a, bits, B, grad_mode, O, Oi);
+    }
+    return true;
+}
+
+}  // namespace nqs
+
+using namespace nqs;
+
+extern "C" {
+
+int nqs_gpu_local_energy_batch(const nqs_config_t *cfg, int size_x, int size_y, const int *spins,
+                               int B, nqs_log_amp_fn_t fn, void *user, double *out_re, double *out_im) {
+    clear_error();
+    if (!cfg || !spins || B <= 0 || !fn) {
+        set_error("invalid arguments");
+        return -1;
+    }
+    if (!ensure_context()) return -1;
+    DevHam H;
+    if (!hamiltonian_build(cfg, size_x, size_y, &H)) return -1;
+    DevAmp A;
+    if (!build_amp(fn, user, H.N, &A, nullptr)) return -1;
+    uint64_t *bits;
+    if (!upload_spins(spins, B, H.N, &bits)) return -1;
+    static DevBuf<double> E;
+    if (!E.ensure(2 * (size_t)B)) return -1;
+    if (!launch_local_estimator(A, H, bits, B, E.p, E.p + B, nullptr, nullptr, 0)) return -1;
+    Context &c = ctx();
+    if (out_re && !NQS_CUDA(cudaMemcpyAsync(out_re, E.p, sizeof(double) * B, cudaMemcpyDeviceToHost,
+                                            c.stream)))
+        return -1;
+    if (out_im && !NQS_CUDA(cudaMemcpyAsync(out_im, E.p + B, sizeof(double) * B, cudaMemcpyDeviceToHost,
+                                            c.stream)))
+        return -1;
+    return NQS_CUDA(cudaStreamSynchronize(c.stream)) ? 0 : -1;
+}
+
+double nqs_local_energy(const nqs_config_t *cfg, int size_x, int size_y, const int *spins,
+                        nqs_log_amp_fn_t fn, void *user) {
+    if (!cfg || !spins || !fn) return 0.0;               // src/nqs/nqs_gradient.c:453
+    double e = 0.0;
+    if (nqs_gpu_local_energy_batch(cfg, size_x, size_y, spins, 1, fn, user, &e, nullptr) != 0) return NAN;
+    return e;
+}
+
+void nqs_local_energy_batch(const nqs_config_t *cfg, int size_x, int size_y, const int *spins, int B,
+                            nqs_log_amp_fn_t fn, void *user, double *out) {
+    if (!cfg || !spins || !out || B <= 0) return;        // :900
+    if (nqs_gpu_local_energy_batch(cfg, size_x, size_y, spins, B, fn, user, out, nullptr) != 0)
+        for (int i = 0; i < B; i++) out[i] = NAN;
+}
+
+void nqs_local_energy_complex(const nqs_config_t *cfg, int size_x, int size_y, const int *spins,
+                              nqs_log_amp_fn_t fn, void *user, double *re, double *im) {
+    if (!cfg || !spins || !fn || !re || !im) {           // :800-804
+        if (re) *re = 0;
+        if (im) *im = 0;
+        return;
+    }
+    if (nqs_gpu_local_energy_batch(cfg, size_x, size_y, spins, 1, fn, user, re, im) != 0) *re = *im = NAN;
+}
+
+void nqs_local_energy_batch_complex(const nqs_config_t *cfg, int size_x, int size_y, const int *spins,
+                                    int B, nqs_log_amp_fn_t fn, void *user, double *re, double *im) {
+    if (!cfg || !spins || !re || !im || B <= 0) return;
+    if (nqs_gpu_local_energy_batch(cfg, size_x, size_y, spins, B, fn, user, re, im) != 0)
+        for (int i = 0; i < B; i++) re[i] = im[i] = NAN;
+}
+
+}  // extern "C"

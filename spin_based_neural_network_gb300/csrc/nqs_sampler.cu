@@ -1,0 +1,480 @@
+// Metropolis sampler: one warp per Markov chain.
+//
+// A chain's state is its configuration (one uint64 in HBM); at the start of a
+// launch the warp rebuilds theta_h = b_h + sum_i W_hi s_i in registers (lane =
+// hidden unit) and then runs its proposals with O(M) incremental updates:
+// a single flip at u or an exchange on bond (u, v) changes theta by one or two
+// weight columns, the acceptance needs only Re log(2 cosh theta') (3 FP64
+// transcendentals per hidden unit) and one warp butterfly.  Random numbers are
+// computed redundantly by all lanes (xorshift64 state replicated in registers,
+// or counter-based Philox4x32-10 keyed by (seed, chain) with counter = move
+// index), so no lane ever waits on another for them.
+//
+// Compat mode (one chain, xorshift64) replays the upstream chain of
+// src/nqs/nqs_sampler.c:86-117 proposal for proposal: same site choice
+// (next % N), same draw order (a uniform is drawn only when the log-ratio is
+// negative), same test log(u) < 2 (log|psi'| - log|psi|).
+#include <math.h>
+
+#include "nqs_amp.cuh"
+
+namespace nqs {
+
+struct Sampler {
+    int N = 0, C = 1;
+    nqs_config_t cfg{};
+    nqs_gpu_options_t opts{};
+    nqs_log_amp_fn_t fn = nullptr;
+    void *user = nullptr;
+    uint64_t move_counter = 0;
+    DevBuf<uint64_t> d_bits, d_rng, d_samples;
+    DevBuf<unsigned long long> d_counts;
+    DevBuf<int> d_bonds, d_spins;
+    int nb = 0;
+    int *h_current = nullptr;        // pinned, N ints (next/current)
+};
+
+struct SampleArgs {
+    int C, N;
+    uint64_t *bits;
+    uint64_t *rng;
+    uint64_t seed;
+    uint64_t move0;
+    int skip, decor, total;          // proposals: skip, then `total - skip` recorded in groups of decor
+    uint64_t *out;
+    int n_out;
+    const int *bonds;
+    int nb;
+    unsigned long long *counts;
+};
+
+__device__ __forceinline__ uint64_t xs_next(uint64_t &s) {   // src/nqs/nqs_sampler.c:31-38
+    uint64_t x = s;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    s = x;
+    return x;
+}
+
+// Shared proposal driver.  `delta(u, v, accept_fn)` evaluates the proposal.
+template <int RNG, int MOVE, typename Eval, typename Commit>
+__device__ __forceinline__ void run_chain(const SampleArgs &S, int c, uint64_t &s, Eval eval,
+                                          Commit commit, unsigned long long &acc,
+                                          unsigned long long &pro) {
+    const int lane = threadIdx.x & 31;
+    uint64_t st = RNG == NQS_GPU_RNG_XORSHIFT_COMPAT ? S.rng[c] : 0;
+    const int per = S.decor > 0 ? S.decor : 1;
+    for (int t = 0; t < S.total; t++) {
+        int u, v = -1;
+        uint4 r = make_uint4(0, 0, 0, 0);
+        if (RNG == NQS_GPU_RNG_XORSHIFT_COMPAT) {
+            u = (int)(xs_next(st) % (uint64_t)S.N);
+        } else {
+            uint64_t m = S.move0 + (uint64_t)t;
+            r = philox4x32(make_uint4((uint32_t)c, (uint32_t)m, (uint32_t)(m >> 32), 0u),
+                           make_uint2((uint32_t)S.seed, (uint32_t)(S.seed >> 32)));
+            if (MOVE == NQS_GPU_MOVE_EXCHANGE) {
+                int k = (int)(((uint64_t)r.x * (uint64_t)S.nb) >> 32);
+                u = S.bonds[2 * k];
+                v = S.bonds[2 * k + 1];
+            } else {
+                u = (int)(((uint64_t)r.x * (uint64_t)S.N) >> 32);
+            }
+        }
+        pro++;
+        bool parallel = v >= 0 && (((s >> u) ^ (s >> v)) & 1ull) == 0;
+        if (!parallel) {
+            double lr = 2.0 * eval(u, v);
+            bool accept;
+            if (lr >= 0.0) {
+                accept = true;
+            } else {
+                double uni;
+                if (RNG == NQS_GPU_RNG_XORSHIFT_COMPAT) {
+                    uni = (double)(xs_next(st) >> 11) * (1.0 / 9007199254740992.0);
+                } else {
+                    uint64_t u53 = ((((uint64_t)r.z) << 32) | r.w) >> 11;
+                    uni = (double)u53 * (1.0 / 9007199254740992.0);
+                }
+                accept = log(uni) < lr;
+            }
+            if (accept) {
+                acc++;
+                commit(u, v);
+                s ^= 1ull << u;
+                if (v >= 0) s ^= 1ull << v;
+            }
+        }
+        if (t >= S.skip && ((t - S.skip + 1) % per) == 0) {
+            long idx = (long)((t - S.skip + 1) / per - 1) * S.C + c;
+            if (idx < S.n_out && lane == 0) S.out[idx] = s;
+        }
+    }
+    if (RNG == NQS_GPU_RNG_XORSHIFT_COMPAT && lane == 0) S.rng[c] = st;
+}
+
+constexpr int kSW = 4;   // warps (chains) per block
+
+template <int J, bool CPLX, int RNG, int MOVE>
+__global__ void __launch_bounds__(32 * kSW) k_sample_rbm(SampleArgs S, DevAmp A) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kSW + (threadIdx.x >> 5);
+    if (c >= S.C) return;
+    const DevAnsatz &a = A.a;
+    const int M = a.M;
+    const double *aR = a.p;
+    uint64_t s = S.bits[c];
+    double thr[J], thi[J], lr[J], nr[J], ni[J], nl[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        int h = lane + 32 * j;
+        thr[j] = thi[j] = lr[j] = 0.0;
+        if (h < M) {
+            rbm_theta(a, s, h, thr[j], thi[j]);
+            lr[j] = CPLX ? rlogcosh(thr[j], thi[j]) : logcosh_r(thr[j]);
+        }
+    }
+    auto eval = [&](int u, int v) -> double {
+        const double su = (double)spin_of(s, u);
+        const double sv = v >= 0 ? (double)spin_of(s, v) : 0.0;
+        double d = 0.0;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            int h = lane + 32 * j;
+            nr[j] = thr[j];
+            ni[j] = thi[j];
+            nl[j] = lr[j];
+            if (h < M) {
+                nr[j] -= 2.0 * su * a.wtr[(long)u * M + h];
+                if (CPLX) ni[j] -= 2.0 * su * a.wti[(long)u * M + h];
+                if (v >= 0) {
+                    nr[j] -= 2.0 * sv * a.wtr[(long)v * M + h];
+                    if (CPLX) ni[j] -= 2.0 * sv * a.wti[(long)v * M + h];
+                }
+                nl[j] = CPLX ? rlogcosh(nr[j], ni[j]) : logcosh_r(nr[j]);
+                d += nl[j] - lr[j];
+            }
+        }
+        d = warp_sum(d) - 2.0 * su * aR[u];
+        if (v >= 0) d -= 2.0 * sv * aR[v];
+        return d;
+    };
+    auto commit = [&](int, int) {
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            thr[j] = nr[j];
+            thi[j] = ni[j];
+            lr[j] = nl[j];
+        }
+    };
+    unsigned long long acc = 0, pro = 0;
+    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro);
+    if (lane == 0) {
+        S.bits[c] = s;
+        atomicAdd(&S.counts[0], acc);
+        atomicAdd(&S.counts[1], pro);
+    }
+}
+
+// Any other program (symmetry projection, mean field, MLP): full evaluation of
+// every proposal, as upstream.
+template <int RNG, int MOVE>
+__global__ void __launch_bounds__(32 * kSW) k_sample_generic(SampleArgs S, DevAmp A) {
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * kSW + warp;
+    if (c >= S.C) return;
+    double *scr = sm + warp * 4 * (A.a.M ? A.a.M : 1);
+    uint64_t s = S.bits[c];
+    double la, ar, nla = 0.0;
+    warp_amp_eval(A, s, la, ar, scr);
+    auto eval = [&](int u, int v) -> double {
+        uint64_t s2 = s ^ (1ull << u);
+        if (v >= 0) s2 ^= 1ull << v;
+        double g;
+        warp_amp_eval(A, s2, nla, g, scr);
+        return nla - la;
+    };
+    auto commit = [&](int, int) { la = nla; };
+    unsigned long long acc = 0, pro = 0;
+    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro);
+    if (lane == 0) {
+        S.bits[c] = s;
+        atomicAdd(&S.counts[0], acc);
+        atomicAdd(&S.counts[1], pro);
+    }
+}
+
+// Philox chain start: uniform bits, or a Fisher-Yates shuffle of n_down down
+// spins (fixed-magnetisation sector).  One thread per chain.
+__global__ void k_chain_init(int C, int N, uint64_t seed, int n_down, uint64_t *bits) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    if (n_down < 0) {
+        uint4 r = philox4x32(make_uint4((uint32_t)c, 0u, 0u, 1u), key);
+        uint64_t b = (uint64_t)r.x | ((uint64_t)r.y << 32);
+        bits[c] = N == 64 ? b : (b & ((1ull << N) - 1));
+        return;
+    }
+    unsigned char arr[64];
+    for (int i = 0; i < N; i++) arr[i] = i < n_down ? 1 : 0;
+    for (int i = N - 1; i >= 1; i--) {
+        uint4 r = philox4x32(make_uint4((uint32_t)c, (uint32_t)i, 0u, 1u), key);
+        int j = (int)(((uint64_t)r.x * (uint64_t)(i + 1)) >> 32);
+        unsigned char t = arr[i];
+        arr[i] = arr[j];
+        arr[j] = t;
+    }
+    uint64_t b = 0;
+    for (int i = 0; i < N; i++)
+        if (arr[i]) b |= 1ull << i;
+    bits[c] = b;
+}
+
+template <int RNG, int MOVE>
+static bool dispatch(const SampleArgs &S, const DevAmp &A) {
+    dim3 grid((S.C + kSW - 1) / kSW), block(32 * kSW);
+    cudaStream_t st = ctx().stream;
+    const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
+    if (fused) {
+        int J = (A.a.M + 31) / 32;
+        bool cx = A.a.kind == KIND_CRBM;
+        NQS_LAUNCH("sampler");
+#define NQS_SCASE(JJ)                                                             \
+    case JJ:                                                                      \
+        if (cx) k_sample_rbm<JJ, true, RNG, MOVE><<<grid, block, 0, st>>>(S, A);  \
+        else k_sample_rbm<JJ, false, RNG, MOVE><<<grid, block, 0, st>>>(S, A);    \
+        break;
+        switch (J) {
+            NQS_SCASE(1) NQS_SCASE(2) NQS_SCASE(3) NQS_SCASE(4) NQS_SCASE(5) NQS_SCASE(6) NQS_SCASE(7)
+            NQS_SCASE(8)
+            default:
+                set_error("hidden width %d unsupported", A.a.M);
+                return false;
+        }
+#undef NQS_SCASE
+    } else {
+        size_t smem = sizeof(double) * 4 * (A.a.M ? A.a.M : 1) * kSW;
+        NQS_LAUNCH("sampler_generic");
+        k_sample_generic<RNG, MOVE><<<grid, block, smem, st>>>(S, A);
+    }
+    return NQS_CUDA(cudaGetLastError());
+}
+
+// Advance all chains: `skip` proposals, then record `n_out` samples
+// (sample k of chain c at row k*C + c), `decor` proposals apart.
+bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
+    DevAmp A;
+    if (!build_amp(sm->fn, sm->user, sm->N, &A, nullptr)) return false;
+    int per = sm->cfg.num_decorrelate > 0 ? sm->cfg.num_decorrelate : 1;
+    int n_spc = n_out > 0 ? (n_out + sm->C - 1) / sm->C : 0;
+    SampleArgs S;
+    S.C = sm->C;
+    S.N = sm->N;
+    S.bits = sm->d_bits.p;
+    S.rng = sm->d_rng.p;
+    S.seed = sm->cfg.rng_seed;
+    S.move0 = sm->move_counter;
+    S.skip = skip;
+    S.decor = per;
+    S.total = skip + n_spc * per;
+    S.out = out;
+    S.n_out = n_out;
+    S.bonds = sm->d_bonds.p;
+    S.nb = sm->nb;
+    S.counts = sm->d_counts.p;
+    if (S.total <= 0) return true;
+    bool ok;
+    if (sm->opts.rng == NQS_GPU_RNG_XORSHIFT_COMPAT)
+        ok = dispatch<NQS_GPU_RNG_XORSHIFT_COMPAT, NQS_GPU_MOVE_SINGLE_FLIP>(S, A);
+    else if (sm->opts.move == NQS_GPU_MOVE_EXCHANGE)
+        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_EXCHANGE>(S, A);
+    else
+        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_SINGLE_FLIP>(S, A);
+    sm->move_counter += (uint64_t)S.total;
+    return ok;
+}
+
+bool sampler_produce(Sampler *sm, int n, uint64_t **d_out) {
+    if (!sm->d_samples.ensure((size_t)n)) return false;
+    if (!sampler_run(sm, 0, n, sm->d_samples.p)) return false;
+    *d_out = sm->d_samples.p;
+    return true;
+}
+
+static void exchange_bonds(const nqs_gpu_options_t &o, int N, std::vector<int> &b) {
+    if (o.lattice_kagome) {
+        int Lx = o.lattice_x, Ly = o.lattice_y;
+        auto S = [&](int cx, int cy, int sub) { return 3 * (cx * Ly + cy) + sub; };
+        for (int cx = 0; cx < Lx; cx++)
+            for (int cy = 0; cy < Ly; cy++) {
+                int A = S(cx, cy, 0), B = S(cx, cy, 1), Cc = S(cx, cy, 2);
+                int Bm = S((cx - 1 + Lx) % Lx, cy, 1), Cm = S(cx, (cy - 1 + Ly) % Ly, 2);
+                int e[12] = {A, B, A, Cc, B, Cc, A, Bm, A, Cm, Bm, Cm};
+                b.insert(b.end(), e, e + 12);
+            }
+        return;
+    }
+    int Lx = o.lattice_x > 0 ? o.lattice_x : N, Ly = o.lattice_x > 0 ? o.lattice_y : 1;
+    int pbc = o.lattice_x > 0 ? o.square_pbc : 1;
+    for (int x = 0; x < Lx; x++)
+        for (int y = 0; y < Ly; y++) {
+            int a = x * Ly + y;
+            if (x + 1 < Lx) { b.push_back(a); b.push_back((x + 1) * Ly + y); }
+            else if (pbc && Lx > 1) { b.push_back(a); b.push_back(y); }
+            if (y + 1 < Ly) { b.push_back(a); b.push_back(x * Ly + y + 1); }
+            else if (pbc && Ly > 1) { b.push_back(a); b.push_back(x * Ly); }
+        }
+}
+
+}  // namespace nqs
+
+using namespace nqs;
+
+extern "C" {
+
+nqs_sampler_t *nqs_sampler_create_gpu(int num_sites, const nqs_config_t *cfg,
+                                      const nqs_gpu_options_t *opts, nqs_log_amp_fn_t fn,
+                                      void *user) {
+    clear_error();
+    if (num_sites <= 0 || !cfg || !fn || !opts) return nullptr;   // src/nqs/nqs_sampler.c:54
+    if (num_sites > kMaxSites) {
+        set_error("num_sites %d > %d", num_sites, kMaxSites);
+        return nullptr;
+    }
+    if (!ensure_context()) return nullptr;
+    DevAmp A;
+    if (!build_amp(fn, user, num_sites, &A, nullptr)) return nullptr;
+    Sampler *s = new Sampler();
+    s->N = num_sites;
+    s->cfg = *cfg;
+    s->opts = *opts;
+    s->fn = fn;
+    s->user = user;
+    bool compat = opts->rng == NQS_GPU_RNG_XORSHIFT_COMPAT;
+    s->C = compat ? 1 : (opts->num_chains > 0 ? opts->num_chains : 1);
+    if (!compat && opts->move == NQS_GPU_MOVE_EXCHANGE) {
+        std::vector<int> b;
+        exchange_bonds(*opts, num_sites, b);
+        for (int x : b)
+            if (x < 0 || x >= num_sites) {
+                set_error("exchange lattice does not match num_sites %d", num_sites);
+                delete s;
+                return nullptr;
+            }
+        s->nb = (int)b.size() / 2;
+        if (s->nb == 0 || !s->d_bonds.ensure(b.size()) ||
+            !NQS_CUDA(cudaMemcpy(s->d_bonds.p, b.data(), sizeof(int) * b.size(), cudaMemcpyHostToDevice))) {
+            if (s->nb == 0) set_error("exchange moves need at least one bond");
+            delete s;
+            return nullptr;
+        }
+    }
+    if (!s->d_bits.ensure((size_t)s->C) || !s->d_rng.ensure((size_t)s->C) || !s->d_counts.ensure(2) ||
+        !NQS_CUDA(cudaMallocHost(&s->h_current, sizeof(int) * num_sites))) {
+        delete s;
+        return nullptr;
+    }
+    cudaStream_t st = ctx().stream;
+    NQS_CUDA(cudaMemsetAsync(s->d_counts.p, 0, 2 * sizeof(unsigned long long), st));
+    if (compat) {
+        // upstream start: rng = seed (or a fixed constant), then one draw per site
+        // (src/nqs/nqs_sampler.c:62-72); host-side set-up of the single chain
+        uint64_t rng = cfg->rng_seed ? (uint64_t)cfg->rng_seed : 0x9E3779B97F4A7C15ull;
+        uint64_t bits = 0;
+        for (int i = 0; i < num_sites; i++) {
+            uint64_t x = rng;
+            x ^= x << 13;
+            x ^= x >> 7;
+            x ^= x << 17;
+            rng = x;
+            if (!(x & 1)) bits |= 1ull << i;     // odd draw -> +1, even -> -1 (bit set)
+        }
+        uint64_t h[2] = {bits, rng};
+        NQS_CUDA(cudaMemcpyAsync(s->d_bits.p, &h[0], 8, cudaMemcpyHostToDevice, st));
+        NQS_CUDA(cudaMemcpyAsync(s->d_rng.p, &h[1], 8, cudaMemcpyHostToDevice, st));
+    } else {
+        NQS_LAUNCH("chain_init");
+        k_chain_init<<<(s->C + 127) / 128, 128, 0, st>>>(s->C, num_sites, cfg->rng_seed,
+                                                          opts->n_down, s->d_bits.p);
+    }
+    if (!NQS_CUDA(cudaStreamSynchronize(st))) {
+        delete s;
+        return nullptr;
+    }
+    return (nqs_sampler_t *)s;
+}
+
+nqs_sampler_t *nqs_sampler_create(int num_sites, const nqs_config_t *cfg, nqs_log_amp_fn_t fn,
+                                  void *user) {
+    if (!ensure_context()) return nullptr;
+    nqs_gpu_options_t o = ctx().opts;
+    return nqs_sampler_create_gpu(num_sites, cfg, &o, fn, user);
+}
+
+void nqs_sampler_free(nqs_sampler_t *h) {
+    Sampler *s = (Sampler *)h;
+    if (!s) return;
+    if (s->h_current) cudaFreeHost(s->h_current);
+    delete s;
+}
+
+void nqs_sampler_thermalize(nqs_sampler_t *h) {
+    Sampler *s = (Sampler *)h;
+    if (!s) return;
+    if (!sampler_run(s, s->cfg.num_thermalize, 0, nullptr)) return;
+    NQS_CUDA(cudaStreamSynchronize(ctx().stream));
+}
+
+static const int *fetch_chain0(Sampler *s) {
+    if (!s->d_spins.ensure((size_t)s->N)) return nullptr;
+    if (!launch_bits_to_spins(s->d_bits.p, 1, s->N, s->d_spins.p)) return nullptr;
+    if (!NQS_CUDA(cudaMemcpyAsync(s->h_current, s->d_spins.p, sizeof(int) * s->N, cudaMemcpyDeviceToHost,
+                                  ctx().stream)) ||
+        !NQS_CUDA(cudaStreamSynchronize(ctx().stream)))
+        return nullptr;
+    return s->h_current;
+}
+
+const int *nqs_sampler_next(nqs_sampler_t *h) {
+    Sampler *s = (Sampler *)h;
+    if (!s) return nullptr;
+    int per = s->cfg.num_decorrelate > 0 ? s->cfg.num_decorrelate : 1;
+    if (!sampler_run(s, per, 0, nullptr)) return nullptr;
+    return fetch_chain0(s);
+}
+
+int nqs_sampler_batch(nqs_sampler_t *h, int n, int *out) {
+    Sampler *s = (Sampler *)h;
+    if (!s || !out || n <= 0) return -1;                 // src/nqs/nqs_sampler.c:136
+    uint64_t *d;
+    if (!sampler_produce(s, n, &d)) return -1;
+    if (!s->d_spins.ensure((size_t)n * s->N)) return -1;
+    if (!launch_bits_to_spins(d, n, s->N, s->d_spins.p)) return -1;
+    if (!NQS_CUDA(cudaMemcpyAsync(out, s->d_spins.p, sizeof(int) * (size_t)n * s->N,
+                                  cudaMemcpyDeviceToHost, ctx().stream)))
+        return -1;
+    return NQS_CUDA(cudaStreamSynchronize(ctx().stream)) ? 0 : -1;
+}
+
+double nqs_sampler_acceptance_ratio(const nqs_sampler_t *h) {
+    const Sampler *s = (const Sampler *)h;
+    if (!s) return 0.0;
+    unsigned long long c[2] = {0, 0};
+    if (!NQS_CUDA(cudaMemcpyAsync(c, s->d_counts.p, sizeof(c), cudaMemcpyDeviceToHost, ctx().stream)) ||
+        !NQS_CUDA(cudaStreamSynchronize(ctx().stream)))
+        return 0.0;
+    return c[1] ? (double)c[0] / (double)c[1] : 0.0;
+}
+
+const int *nqs_sampler_current(const nqs_sampler_t *h) {
+    return h ? fetch_chain0((Sampler *)h) : nullptr;
+}
+
+int nqs_sampler_num_sites(const nqs_sampler_t *h) { return h ? ((const Sampler *)h)->N : 0; }
+
+int nqs_sampler_num_chains(const nqs_sampler_t *h) { return h ? ((const Sampler *)h)->C : 0; }
+
+}  // extern "C"

@@ -1,0 +1,809 @@
+// Stochastic reconfiguration on the GPU: MinSR (sample-space Gram + Cholesky)
+// and CG-SR (matrix-free QGT), FP64.
+//
+// Pipeline of one MinSR step (src/nqs/nqs_optimizer.c:1063-1194), every stage
+// a kernel on the library stream, no host round trip until the step info:
+//   sampler -> fused local estimator (E_loc + Jacobian row O_i)
+//   -> energy statistics (compensated) and eps_i = E_i - <E>
+//   -> column means <O_k>, centring O_c = O - <O>
+//   -> T = O_c O_c^T / N_s + shift I (lower triangle, 64x64 tiles)
+//   -> blocked right-looking Cholesky (32-wide panels: diagonal-block factor,
+//      panel triangular solve, trailing SYRK update), status word on device
+//   -> forward / backward blocked triangular solves
+//   -> delta = O_c^T y / N_s, theta -= lr delta, ||delta||.
+#include <math.h>
+
+#include "nqs_amp.cuh"
+
+namespace nqs {
+
+struct Sampler;
+bool sampler_produce(Sampler *s, int n, uint64_t **d_out);
+
+// ---------------------------------------------------------------- workspace
+struct Workspace {
+    DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part;
+    DevBuf<int> status;
+    DevBuf<uint64_t> batch_bits;
+};
+static Workspace g_ws;
+
+// device scalars (doubles): [0] e_mean [1] e_sq_mean [2] ||delta||^2 [3] rs
+// [4] rs0 [5] pAp [6] alpha  ; status ints: [0] chol fail column (-1 ok)
+// [1] cg done flag [2] cg iterations [3] cg converged [4] retry ran
+enum { S_EMEAN = 0, S_ESQ = 1, S_NORM2 = 2, S_RS = 3, S_RS0 = 4, S_PAP = 5, S_ALPHA = 6, S_UMEAN = 7 };
+enum { I_FAIL = 0, I_DONE = 1, I_ITERS = 2, I_CONV = 3, I_RETRY = 4, I_FAIL2 = 5 };
+
+// ---------------------------------------------------------------- statistics
+// Neumaier-compensated sums of E and E^2 (one block), then eps_i = E_i - <E>.
+__global__ void k_energy_stats(const double *__restrict__ E, int n, double *scal, double *eps) {
+    __shared__ double ss[1024], sc[1024], qs[1024], qc[1024];
+    int t = threadIdx.x;
+    double s = 0.0, c = 0.0, q = 0.0, qcc = 0.0;
+    for (int i = t; i < n; i += blockDim.x) {
+        double x = E[i], tt = s + x;
+        c += fabs(s) >= fabs(x) ? (s - tt) + x : (x - tt) + s;
+        s = tt;
+        double x2 = x * x, t2 = q + x2;
+        qcc += fabs(q) >= fabs(x2) ? (q - t2) + x2 : (x2 - t2) + q;
+        q = t2;
+    }
+    ss[t] = s; sc[t] = c; qs[t] = q; qc[t] = qcc;
+    __syncthreads();
+    __shared__ double mean;
+    if (t == 0) {
+        double S = 0.0, Cc = 0.0, Q = 0.0, QC = 0.0;
+        for (int k = 0; k < (int)blockDim.x; k++) {
+            double x = ss[k], tt = S + x;
+            Cc += fabs(S) >= fabs(x) ? (S - tt) + x : (x - tt) + S;
+            S = tt;
+            Cc += sc[k];
+            double x2 = qs[k], t2 = Q + x2;
+            QC += fabs(Q) >= fabs(x2) ? (Q - t2) + x2 : (x2 - t2) + Q;
+            Q = t2;
+            QC += qc[k];
+        }
+        mean = (S + Cc) / (double)n;
+        scal[S_EMEAN] = mean;
+        scal[S_ESQ] = (Q + QC) / (double)n;
+    }
+    __syncthreads();
+    if (eps)
+        for (int i = t; i < n; i += blockDim.x) eps[i] = E[i] - mean;
+}
+
+// Column sums of O (and of O_ik E_i for CG-SR): 32 columns x 8 row groups per
+// block, coalesced along the row.
+__global__ void k_col_stats(const double *__restrict__ O, int Ns, long P, const double *__restrict__ E,
+                            const double *__restrict__ scal, double *gm, double *F) {
+    __shared__ double a[8][33], b[8][33];
+    long k = (long)blockIdx.x * 32 + threadIdx.x;
+    double s = 0.0, se = 0.0;
+    if (k < P)
+        for (int i = threadIdx.y; i < Ns; i += 8) {
+            double g = O[(size_t)i * P + k];
+            s += g;
+            if (F) se += g * E[i];
+        }
+    a[threadIdx.y][threadIdx.x] = s;
+    b[threadIdx.y][threadIdx.x] = se;
+    __syncthreads();
+    if (threadIdx.y == 0 && k < P) {
+        double S = 0.0, SE = 0.0;
+        for (int y = 0; y < 8; y++) {
+            S += a[y][threadIdx.x];
+            SE += b[y][threadIdx.x];
+        }
+        double m = S / (double)Ns;
+        gm[k] = m;
+        if (F) F[k] = SE / (double)Ns - m * scal[S_EMEAN];     // src/nqs/nqs_optimizer.c:213-215
+    }
+}
+
+__global__ void k_center(double *O, int Ns, long P, const double *__restrict__ gm) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, tot = (size_t)Ns * P;
+    for (; t < tot; t += (size_t)gridDim.x * blockDim.x) O[t] -= gm[t % P];
+}
+
+// ---------------------------------------------------------------- FP64 Gram
+// T[i][j] = scale * sum_k A[i][k] A[j][k] (+ shift on the diagonal) for the
+// lower-triangular 64x64 tiles; 256 threads, 4x4 register blocking.
+constexpr int TG = 64, KC = 16;
+
+__device__ __forceinline__ void tri_tile(int t, int &bi, int &bj) {
+    int r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((r + 1) * (r + 2) / 2 <= t) r++;
+    while (r * (r + 1) / 2 > t) r--;
+    bi = r;
+    bj = t - r * (r + 1) / 2;
+}
+
+// Shared tile product: acc[m][n] += sum_k A[r0+ty+16m][k] * B[c0+tx+16n][k] over k in [k0,k1).
+__device__ __forceinline__ void tile_mma_fp64(const double *__restrict__ A, long lda,
+                                              const double *__restrict__ Bm, long ldb, int rows_a,
+                                              int rows_b, int r0, int c0, int k0, int k1,
+                                              double (*As)[TG + 1], double (*Bs)[TG + 1],
+                                              double acc[4][4]) {
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int kk = k0; kk < k1; kk += KC) {
+        for (int e = tid; e < TG * KC; e += 256) {
+            int rr = e / KC, cc = e % KC;
+            int k = kk + cc;
+            int ra = r0 + rr, rb = c0 + rr;
+            As[cc][rr] = (ra < rows_a && k < k1) ? A[(size_t)ra * lda + k] : 0.0;
+            Bs[cc][rr] = (rb < rows_b && k < k1) ? Bm[(size_t)rb * ldb + k] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < KC; c++) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) av[m] = As[c][ty + 16 * m];
+#pragma unroll
+            for (int n = 0; n < 4; n++) bv[n] = Bs[c][tx + 16 * n];
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+#pragma unroll
+                for (int n = 0; n < 4; n++) acc[m][n] = fma(av[m], bv[n], acc[m][n]);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_gram_fp64(const double *__restrict__ O, int Ns, long P,
+                                                   double scale, double shift, double *T) {
+    __shared__ double As[KC][TG + 1], Bs[KC][TG + 1];
+    int bi, bj;
+    tri_tile(blockIdx.x, bi, bj);
+    double acc[4][4] = {};
+    tile_mma_fp64(O, P, O, P, Ns, Ns, bi * TG, bj * TG, 0, (int)P, As, Bs, acc);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            int i = bi * TG + ty + 16 * m, j = bj * TG + tx + 16 * n;
+            if (i < Ns && j <= i) T[(size_t)i * Ns + j] = acc[m][n] * scale + (i == j ? shift : 0.0);
+        }
+}
+
+// ---------------------------------------------------------------- Cholesky
+constexpr int NB = 32;
+
+// Factor the kb x kb diagonal block at k0 in shared memory (column by column,
+// the pivot test of src/nqs/nqs_optimizer.c:1029-1031); first failing column
+// goes to status[I_FAIL].
+__global__ void k_potrf_diag(double *A, int n, int k0, int kb, int *status) {
+    if (status[I_FAIL] >= 0) return;
+    __shared__ double L[NB][NB + 1];
+    __shared__ int fail;
+    int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 32
+    if (tx < kb && ty < kb && tx <= ty) L[ty][tx] = A[(size_t)(k0 + ty) * n + k0 + tx];
+    if (tx == 0 && ty == 0) fail = -1;
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        if (tx == 0 && ty == 0) {
+            double d = L[j][j];
+            if (!(d > 0.0)) fail = j;
+            else L[j][j] = sqrt(d);
+        }
+        __syncthreads();
+        if (fail >= 0) break;
+        if (tx == 0 && ty > j && ty < kb) L[ty][j] = L[ty][j] * (1.0 / L[j][j]);
+        __syncthreads();
+        if (ty > j && ty < kb && tx > j && tx <= ty) L[ty][tx] -= L[ty][j] * L[tx][j];
+        __syncthreads();
+    }
+    if (fail >= 0) {
+        // keep the columns finished before the failing one (they define the
+        // state the upstream retry works on)
+        if (tx < fail && ty < kb && tx <= ty) A[(size_t)(k0 + ty) * n + k0 + tx] = L[ty][tx];
+        if (tx == 0 && ty == 0) status[I_FAIL] = k0 + fail;
+        return;
+    }
+    if (tx < kb && ty < kb && tx <= ty) A[(size_t)(k0 + ty) * n + k0 + tx] = L[ty][tx];
+}
+
+// Rows below the block: L[i][k0:k0+ncol] = A[i][k0:k0+ncol] L_kk^{-T}, one
+// thread per row (forward substitution with the reciprocal pivot, as upstream).
+__global__ void k_trsm_panel(double *A, int n, int k0, int kb, int ncol, int row0, const int *status,
+                             int ignore_status) {
+    if (!ignore_status && status[I_FAIL] >= 0) return;
+    __shared__ double L[NB][NB + 1];
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        int r = e / kb, c = e % kb;
+        L[r][c] = c <= r ? A[(size_t)(k0 + r) * n + k0 + c] : 0.0;
+    }
+    __syncthreads();
+    int i = row0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x[NB];
+    double *row = A + (size_t)i * n + k0;
+#pragma unroll
+    for (int j = 0; j < NB; j++) x[j] = j < ncol ? row[j] : 0.0;
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+        if (j < ncol) {
+            double s = x[j];
+            for (int m = 0; m < j; m++) s -= x[m] * L[j][m];
+            x[j] = s * (1.0 / L[j][j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NB; j++)
+        if (j < ncol) row[j] = x[j];
+}
+
+// Trailing update A[i][j] -= sum_m L[i][k0+m] L[j][k0+m] for k1 <= j <= i < n.
+__global__ void __launch_bounds__(256) k_syrk_update(double *A, int n, int k0, int kb, int k1,
+                                                     const int *status) {
+    if (status[I_FAIL] >= 0) return;
+    __shared__ double As[KC][TG + 1], Bs[KC][TG + 1];
+    int bi, bj;
+    tri_tile(blockIdx.x, bi, bj);
+    int r0 = k1 + bi * TG, c0 = k1 + bj * TG;
+    double acc[4][4] = {};
+    tile_mma_fp64(A + k0, n, A + k0, n, n, n, r0, c0, 0, kb, As, Bs, acc);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int i = r0 + ty + 16 * m, j = c0 + tx + 16 * q;
+            if (i < n && j <= i) A[(size_t)i * n + j] -= acc[m][q];
+        }
+}
+
+static bool cholesky_fp64(double *T, int n, int *status) {
+    cudaStream_t st = ctx().stream;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        int kb = n - k0 < NB ? n - k0 : NB;
+        {
+            NQS_LAUNCH("chol_diag");
+            k_potrf_diag<<<1, dim3(32, 32), 0, st>>>(T, n, k0, kb, status);
+        }
+        int k1 = k0 + kb, rest = n - k1;
+        if (rest <= 0) break;
+        {
+            NQS_LAUNCH("chol_panel");
+            k_trsm_panel<<<(rest + 127) / 128, 128, 0, st>>>(T, n, k0, kb, kb, k1, status, 0);
+        }
+        int nt = (rest + TG - 1) / TG;
+        {
+            NQS_LAUNCH("chol_syrk");
+            k_syrk_update<<<nt * (nt + 1) / 2, 256, 0, st>>>(T, n, k0, kb, k1, status);
+        }
+    }
+    return NQS_CUDA(cudaGetLastError());
+}
+
+// The upstream retry (src/nqs/nqs_optimizer.c:1156-1160) re-factors the matrix
+// as the failed column-by-column factorisation left it: columns c < j hold L
+// (every row), columns >= j hold the original T.  Rebuild exactly that state
+// from the partially factored T and a pristine copy T0, then add 1e-6.
+__global__ void k_quirk_restore(double *T, const double *__restrict__ T0, int n, int j) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, tot = (size_t)n * n;
+    for (; t < tot; t += (size_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / n), c = (int)(t % n);
+        if (c > r) continue;
+        if (c >= j) T[t] = T0[t];
+        if (r == c) T[t] += 1e-6;
+    }
+}
+
+// ---------------------------------------------------------------- triangular solves
+// Forward L z = b, block by block.  Every CTA re-solves the 32x32 diagonal
+// block with a warp (lane = row) and then updates its rows of the right-hand
+// side; CTA 0 stores the block of the solution.
+__global__ void k_trsv_fwd(const double *__restrict__ L, int n, int k0, int kb, double *rhs, double *x) {
+    __shared__ double xs[NB];
+    int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        double v = lane < kb ? rhs[k0 + lane] : 0.0;
+        for (int j = 0; j < kb; j++) {
+            double xj = __shfl_sync(0xffffffffu, v, j) / L[(size_t)(k0 + j) * n + k0 + j];
+            if (lane == j) v = xj;
+            if (lane > j && lane < kb) v -= L[(size_t)(k0 + lane) * n + k0 + j] * xj;
+        }
+        if (lane < kb) xs[lane] = v;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x < kb) x[k0 + threadIdx.x] = xs[threadIdx.x];
+    int i = k0 + kb + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        double s = 0.0;
+        const double *row = L + (size_t)i * n + k0;
+        for (int m = 0; m < kb; m++) s += row[m] * xs[m];
+        rhs[i] -= s;
+    }
+}
+
+// Backward L^T y = z, last block first; the update reads row-block k of L.
+__global__ void k_trsv_bwd(const double *__restrict__ L, int n, int k0, int kb, double *rhs, double *x) {
+    __shared__ double xs[NB];
+    int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        double v = lane < kb ? rhs[k0 + lane] : 0.0;
+        for (int j = kb - 1; j >= 0; j--) {
+            double xj = __shfl_sync(0xffffffffu, v, j) / L[(size_t)(k0 + j) * n + k0 + j];
+            if (lane == j) v = xj;
+            if (lane < j) v -= L[(size_t)(k0 + j) * n + k0 + lane] * xj;
+        }
+        if (lane < kb) xs[lane] = v;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x < kb) x[k0 + threadIdx.x] = xs[threadIdx.x];
+    int jcol = blockIdx.x * blockDim.x + threadIdx.x;
+    if (jcol < k0) {
+        double s = 0.0;
+        for (int m = 0; m < kb; m++) s += L[(size_t)(k0 + m) * n + jcol] * xs[m];
+        rhs[jcol] -= s;
+    }
+}
+
+static bool cholesky_solve(const double *L, int n, const double *b, double *z, double *y) {
+    cudaStream_t st = ctx().stream;
+    if (!NQS_CUDA(cudaMemcpyAsync(z, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st))) return false;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        int kb = n - k0 < NB ? n - k0 : NB;
+        int rest = n - k0 - kb;
+        NQS_LAUNCH("trsv_fwd");
+        k_trsv_fwd<<<rest > 0 ? (rest + 127) / 128 : 1, 128, 0, st>>>(L, n, k0, kb, z, y);
+    }
+    // y now holds the forward solution; reuse it as the right-hand side
+    if (!NQS_CUDA(cudaMemcpyAsync(z, y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st))) return false;
+    int last = ((n - 1) / NB) * NB;
+    for (int k0 = last; k0 >= 0; k0 -= NB) {
+        int kb = n - k0 < NB ? n - k0 : NB;
+        NQS_LAUNCH("trsv_bwd");
+        k_trsv_bwd<<<k0 > 0 ? (k0 + 127) / 128 : 1, 128, 0, st>>>(L, n, k0, kb, z, y);
+    }
+    return NQS_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- update
+// delta_k = scale * sum_i O[i][k] y_i (same blocking as k_col_stats).
+__global__ void k_col_dot(const double *__restrict__ O, int Ns, long P, const double *__restrict__ y,
+                          double scale, double *out) {
+    __shared__ double a[8][33];
+    long k = (long)blockIdx.x * 32 + threadIdx.x;
+    double s = 0.0;
+    if (k < P)
+        for (int i = threadIdx.y; i < Ns; i += 8) s += O[(size_t)i * P + k] * y[i];
+    a[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && k < P) {
+        double S = 0.0;
+        for (int q = 0; q < 8; q++) S += a[q][threadIdx.x];
+        out[k] = S * scale;
+    }
+}
+
+// theta -= lr * delta and ||delta||^2 (one block, deterministic order).
+__global__ void k_apply(double *params, const double *__restrict__ delta, long P, double lr, double *scal,
+                        const int *status, int zero_on_fail) {
+    __shared__ double red[1024];
+    bool zero = zero_on_fail && status[I_FAIL2] >= 0;
+    double s = 0.0;
+    for (long k = threadIdx.x; k < P; k += blockDim.x) {
+        double d = zero ? 0.0 : delta[k];
+        params[k] += -lr * d;
+        s += d * d;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) scal[S_NORM2] = red[0];
+}
+
+// ---------------------------------------------------------------- CG-SR
+// u_i = sum_k O_ik p_k (warp per row) and per-block partial sums of u.
+__global__ void k_qgt_rows(const double *__restrict__ O, int Ns, long P, const double *__restrict__ p,
+                           double *u, const int *status) {
+    if (status[I_DONE]) return;
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= Ns) return;
+    double s = 0.0;
+    for (long k = lane; k < P; k += 32) s += O[(size_t)w * P + k] * p[k];
+    s = warp_sum(s);
+    if (lane == 0) u[w] = s;
+}
+
+// (S + eps) p = O^T u / Ns - <O> mean(u) + eps p  (src/nqs/nqs_optimizer.c:44-80)
+__global__ void k_qgt_cols(const double *__restrict__ O, int Ns, long P, const double *__restrict__ u,
+                           const double *__restrict__ gm, const double *__restrict__ p, double eps,
+                           double *Ap, const int *status) {
+    if (status[I_DONE]) return;
+    __shared__ double a[8][33];
+    __shared__ double um;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double s = 0.0;
+        for (int i = 0; i < Ns; i++) s += u[i];
+        um = s / (double)Ns;
+    }
+    long k = (long)blockIdx.x * 32 + threadIdx.x;
+    double s = 0.0;
+    if (k < P)
+        for (int i = threadIdx.y; i < Ns; i += 8) s += O[(size_t)i * P + k] * u[i];
+    a[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && k < P) {
+        double S = 0.0;
+        for (int q = 0; q < 8; q++) S += a[q][threadIdx.x];
+        Ap[k] = (S / (double)Ns) - gm[k] * um + eps * p[k];
+    }
+}
+
+__device__ double block_dot(const double *a, const double *b, long n, double *red) {
+    double s = 0.0;
+    for (long k = threadIdx.x; k < n; k += blockDim.x) s += a[k] * b[k];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+// One CG update (src/nqs/nqs_optimizer.c:105-135), single block of 1024.
+__global__ void k_cg_update(double *d, double *r, double *p, const double *__restrict__ Ap, long P,
+                            double *scal, int *status, int it, double tol) {
+    if (status[I_DONE]) return;
+    __shared__ double red[1024];
+    double pAp = block_dot(p, Ap, P, red);
+    if (!(fabs(pAp) >= 1e-30)) {                 // Krylov breakdown: stop, unconverged
+        if (threadIdx.x == 0) {
+            status[I_DONE] = 1;
+            status[I_ITERS] = it;
+            scal[S_PAP] = pAp;
+        }
+        return;
+    }
+    double alpha = scal[S_RS] / pAp;
+    for (long k = threadIdx.x; k < P; k += blockDim.x) {
+        d[k] += alpha * p[k];
+        r[k] += -alpha * Ap[k];
+    }
+    __syncthreads();
+    double rs_new = block_dot(r, r, P, red);
+    if (rs_new <= tol * tol * scal[S_RS0]) {
+        if (threadIdx.x == 0) {
+            status[I_DONE] = 1;
+            status[I_CONV] = 1;
+            status[I_ITERS] = it + 1;
+        }
+        return;
+    }
+    double beta = rs_new / scal[S_RS];
+    for (long k = threadIdx.x; k < P; k += blockDim.x) p[k] = r[k] + beta * p[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        scal[S_RS] = rs_new;
+        status[I_ITERS] = it + 1;
+    }
+}
+
+__global__ void k_cg_init(const double *__restrict__ F, double *d, double *r, double *p, long P,
+                          double *scal, int *status) {
+    __shared__ double red[1024];
+    for (long k = threadIdx.x; k < P; k += blockDim.x) {
+        d[k] = 0.0;
+        r[k] = F[k];
+        p[k] = F[k];
+    }
+    __syncthreads();
+    double rs = block_dot(r, r, P, red);
+    if (threadIdx.x == 0) {
+        scal[S_RS] = rs;
+        scal[S_RS0] = rs;
+        status[I_DONE] = 0;
+        status[I_ITERS] = 0;
+        status[I_CONV] = 0;
+    }
+}
+
+// ---------------------------------------------------------------- the step
+
+struct StepIn {
+    const nqs_config_t *cfg;
+    int size_x, size_y;
+    Ansatz *ansatz;
+    Sampler *sampler;                  // or NULL with a host batch
+    const int *host_batch;
+    int Ns;
+    nqs_log_amp_fn_t fn;
+    void *user;
+    nqs_gradient_fn_t gfn;
+    void *guser;
+    int minsr;
+};
+
+static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
+    clear_error();
+    const nqs_config_t *cfg = in.cfg;
+    Ansatz *a = in.ansatz;
+    if (!ensure_context()) return -1;
+    if (!ansatz_sync(a, true)) return -1;
+    Context &c = ctx();
+    cudaStream_t st = c.stream;
+    long launches0 = c.launches;
+    const int Ns = in.Ns;
+    const long P = a->P;
+    if (Ns <= 0 || P <= 0) {
+        set_error("num_samples and num_params must be positive");
+        return -1;
+    }
+    DevHam H;
+    if (!hamiltonian_build(cfg, in.size_x, in.size_y, &H)) return -1;
+    nqs_log_amp_fn_t fn = in.fn ? in.fn : nqs_ansatz_log_amp;   // src/nqs/nqs_optimizer.c:159
+    void *user = in.fn ? in.user : (void *)a;
+    DevAmp A;
+    Ansatz *base = nullptr;
+    if (!build_amp(fn, user, H.N, &A, &base)) return -1;
+    if (base != a) {
+        set_error("the log_amp program does not wrap the ansatz being optimised");
+        return -1;
+    }
+    DevAmp Ag;   // program whose gradient fills O
+    int grad_sym = 0;
+    if (in.gfn == nullptr) {
+        Ag = A;
+        Ag.G = 0;
+        Ag.n_outer = Ag.n_inner = 0;
+    } else if (in.gfn == nqs_symproj_gradient) {
+        if (!build_amp(nqs_symproj_log_amp, in.guser, H.N, &Ag, nullptr)) return -1;
+        grad_sym = 1;
+    } else {
+        set_error("gradient callback is not supported on the GPU (NULL or nqs_symproj_gradient)");
+        return -1;
+    }
+    Workspace &w = g_ws;
+    if (!w.E.ensure(Ns) || !w.Ei.ensure(Ns) || !w.eps.ensure(Ns) || !w.O.ensure((size_t)Ns * P) ||
+        !w.gm.ensure(P) || !w.delta.ensure(P) || !w.scal.ensure(16) || !w.status.ensure(16))
+        return -1;
+    // 1. samples
+    uint64_t *bits = nullptr;
+    if (in.sampler) {
+        if (!sampler_produce(in.sampler, Ns, &bits)) return -1;
+    } else {
+        if (!upload_spins(in.host_batch, Ns, H.N, &bits)) return -1;
+    }
+    // 2. local energies + Jacobian rows (fused when the program allows)
+    bool fused_grad = !grad_sym && A.G == 0;
+    if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
+                                fused_grad ? 1 : 0))
+        return -1;
+    if (!fused_grad) {
+        if (grad_sym) {
+            if (!launch_symproj_gradient(Ag, bits, Ns, w.O.p)) return -1;
+        } else if (!launch_gradient(Ag.a, bits, Ns, 1, w.O.p, nullptr)) {
+            return -1;
+        }
+    }
+    // 3. statistics
+    {
+        NQS_LAUNCH("energy_stats");
+        k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
+    }
+    NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
+    dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
+    int converged = 0, cg_iters = 0;
+    if (in.minsr) {
+        if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns)) return -1;
+        {
+            NQS_LAUNCH("col_mean");
+            k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
+        }
+        {
+            NQS_LAUNCH("center");
+            k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+        }
+        int nt = (Ns + TG - 1) / TG;
+        {
+            NQS_LAUNCH("gram_fp64");
+            k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(w.O.p, Ns, P, 1.0 / (double)Ns,
+                                                            cfg->sr_diag_shift, w.T.p);
+        }
+        if (!cholesky_fp64(w.T.p, Ns, w.status.p)) return -1;
+        int fail = -1;
+        if (!NQS_CUDA(cudaMemcpyAsync(&fail, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaStreamSynchronize(st)))
+            return -1;
+        step_stats().chol_fail_col = fail;
+        step_stats().chol_retry = 0;
+        int fail2 = -1;
+        if (fail >= 0) {
+            // upstream retry on the partially overwritten matrix (+1e-6)
+            step_stats().chol_retry = 1;
+            if (!w.T0.ensure((size_t)Ns * Ns)) return -1;
+            {
+                NQS_LAUNCH("gram_fp64");
+                k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(w.O.p, Ns, P, 1.0 / (double)Ns,
+                                                                cfg->sr_diag_shift, w.T0.p);
+            }
+            int k0 = (fail / NB) * NB, kb = Ns - k0 < NB ? Ns - k0 : NB;
+            if (fail > k0 && k0 + kb < Ns) {
+                NQS_LAUNCH("chol_panel");
+                k_trsm_panel<<<(Ns - k0 - kb + 127) / 128, 128, 0, st>>>(w.T.p, Ns, k0, kb, fail - k0,
+                                                                        k0 + kb, w.status.p, 1);
+            }
+            {
+                NQS_LAUNCH("chol_restore");
+                k_quirk_restore<<<c.sm_count * 8, 256, 0, st>>>(w.T.p, w.T0.p, Ns, fail);
+            }
+            NQS_CUDA(cudaMemsetAsync(w.status.p + I_FAIL, 0xff, sizeof(int), st));
+            if (!cholesky_fp64(w.T.p, Ns, w.status.p)) return -1;
+            if (!NQS_CUDA(cudaMemcpyAsync(&fail2, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+                !NQS_CUDA(cudaStreamSynchronize(st)))
+                return -1;
+        }
+        if (fail2 < 0) {
+            if (!cholesky_solve(w.T.p, Ns, w.eps.p, w.z.p, w.y.p)) return -1;
+            converged = 1;
+        } else {
+            fprintf(stderr, "nqs_sr_step_minsr: Cholesky breakdown after retry; increase "
+                            "sr_diag_shift or num_samples. Update set to 0.\n");
+            NQS_CUDA(cudaMemsetAsync(w.y.p, 0, sizeof(double) * Ns, st));
+        }
+        {
+            NQS_LAUNCH("delta");
+            k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y.p, 1.0 / (double)Ns, w.delta.p);
+        }
+    } else {
+        if (!w.F.ensure(P) || !w.r.ensure(P) || !w.p.ensure(P) || !w.Ap.ensure(P) || !w.u.ensure(Ns))
+            return -1;
+        {
+            NQS_LAUNCH("col_stats");
+            k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.E.p, w.scal.p, w.gm.p, w.F.p);
+        }
+        {
+            NQS_LAUNCH("cg_init");
+            k_cg_init<<<1, 1024, 0, st>>>(w.F.p, w.delta.p, w.r.p, w.p.p, P, w.scal.p, w.status.p);
+        }
+        int maxit = cfg->sr_cg_max_iters;
+        for (int it = 0; it < maxit; it++) {
+            {
+                NQS_LAUNCH("qgt_rows");
+                k_qgt_rows<<<(Ns * 32 + 255) / 256, 256, 0, st>>>(w.O.p, Ns, P, w.p.p, w.u.p, w.status.p);
+            }
+            {
+                NQS_LAUNCH("qgt_cols");
+                k_qgt_cols<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.u.p, w.gm.p, w.p.p, cfg->sr_diag_shift,
+                                              w.Ap.p, w.status.p);
+            }
+            {
+                NQS_LAUNCH("cg_update");
+                k_cg_update<<<1, 1024, 0, st>>>(w.delta.p, w.r.p, w.p.p, w.Ap.p, P, w.scal.p, w.status.p,
+                                                it, cfg->sr_cg_tol);
+            }
+        }
+        int h[16];
+        double hs[16];
+        if (!NQS_CUDA(cudaMemcpyAsync(h, w.status.p, sizeof(h), cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaStreamSynchronize(st)))
+            return -1;
+        converged = h[I_CONV] == 1;
+        cg_iters = h[I_DONE] == 1 ? h[I_ITERS] : maxit;
+        if (h[I_DONE] == 1 && !converged)
+            fprintf(stderr, "nqs_sr cg_solve: Krylov breakdown at iter=%d, pAp=%.3e. Returning "
+                            "unconverged partial step.\n", h[I_ITERS], hs[S_PAP]);
+    }
+    // 4. update
+    {
+        NQS_LAUNCH("apply_update");
+        k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.delta.p, P, cfg->learning_rate, w.scal.p, w.status.p, 0);
+    }
+    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a)) return -1;
+    double hs[16];
+    if (out_E && !NQS_CUDA(cudaMemcpyAsync(out_E, w.E.p, sizeof(double) * Ns, cudaMemcpyDeviceToHost, st)))
+        return -1;
+    if (out_delta && !NQS_CUDA(cudaMemcpyAsync(out_delta, w.delta.p, sizeof(double) * P,
+                                               cudaMemcpyDeviceToHost, st)))
+        return -1;
+    if (!NQS_CUDA(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st)) || !ansatz_pull(a))
+        return -1;
+    step_stats().gpu_launches = (int)(c.launches - launches0);
+    if (info) {
+        info->mean_energy = hs[S_EMEAN];
+        info->variance_energy = hs[S_ESQ] - hs[S_EMEAN] * hs[S_EMEAN];
+        info->update_norm = sqrt(hs[S_NORM2]) * cfg->learning_rate;
+        info->acceptance_ratio = in.sampler ? nqs_sampler_acceptance_ratio((nqs_sampler_t *)in.sampler) : 0.0;
+        info->cg_iterations = in.minsr ? 0 : cg_iters;
+        info->converged = converged;
+    }
+    return 0;
+}
+
+}  // namespace nqs
+
+using namespace nqs;
+
+extern "C" {
+
+static int step_common(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *ansatz, nqs_sampler_t *sampler,
+                       nqs_log_amp_fn_t fn, void *user, nqs_gradient_fn_t gfn, void *guser, int minsr,
+                       nqs_sr_step_info_t *info) {
+    if (!cfg || !ansatz || !sampler) return -1;          // src/nqs/nqs_optimizer.c:150
+    StepIn in{cfg, sx, sy, (Ansatz *)ansatz, (Sampler *)sampler, nullptr, cfg->num_samples,
+              fn, user, gfn, guser, minsr};
+    if (nqs_sampler_num_sites(sampler) != ((Ansatz *)ansatz)->N) {
+        set_error("sampler and ansatz disagree on num_sites");
+        return -1;
+    }
+    return sr_step_impl(in, info, nullptr, nullptr);
+}
+
+int nqs_sr_step_custom_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                            nqs_log_amp_fn_t fn, void *user, nqs_gradient_fn_t gfn, void *guser,
+                            nqs_sr_step_info_t *info) {
+    return step_common(cfg, sx, sy, a, s, fn, user, gfn, guser, 0, info);
+}
+
+int nqs_sr_step_custom(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                       nqs_log_amp_fn_t fn, void *user, nqs_sr_step_info_t *info) {
+    return nqs_sr_step_custom_full(cfg, sx, sy, a, s, fn, user, nullptr, nullptr, info);
+}
+
+int nqs_sr_step(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                nqs_sr_step_info_t *info) {
+    return nqs_sr_step_custom_full(cfg, sx, sy, a, s, nullptr, nullptr, nullptr, nullptr, info);
+}
+
+int nqs_sr_run_custom_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                           nqs_log_amp_fn_t fn, void *user, nqs_gradient_fn_t gfn, void *guser,
+                           double *trace) {
+    if (!cfg || !a || !s) return -1;                     // src/nqs/nqs_optimizer.c:264-284
+    nqs_sampler_thermalize(s);
+    for (int it = 0; it < cfg->num_iterations; it++) {
+        nqs_sr_step_info_t info;
+        int rc = nqs_sr_step_custom_full(cfg, sx, sy, a, s, fn, user, gfn, guser, &info);
+        if (rc != 0) return rc;
+        if (trace) trace[it] = info.mean_energy;
+    }
+    return 0;
+}
+
+int nqs_sr_run_custom(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                      nqs_log_amp_fn_t fn, void *user, double *trace) {
+    return nqs_sr_run_custom_full(cfg, sx, sy, a, s, fn, user, nullptr, nullptr, trace);
+}
+
+int nqs_sr_run(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s, double *trace) {
+    return nqs_sr_run_custom(cfg, sx, sy, a, s, nullptr, nullptr, trace);
+}
+
+int nqs_sr_step_minsr_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                           nqs_log_amp_fn_t fn, void *user, nqs_gradient_fn_t gfn, void *guser,
+                           nqs_sr_step_info_t *info) {
+    return step_common(cfg, sx, sy, a, s, fn, user, gfn, guser, 1, info);
+}
+
+int nqs_sr_run_minsr(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                     nqs_log_amp_fn_t fn, void *user, double *trace) {
+    if (!cfg || !a || !s) return -1;                     // src/nqs/nqs_optimizer.c:1196-1214
+    nqs_sampler_thermalize(s);
+    for (int it = 0; it < cfg->num_iterations; it++) {
+        nqs_sr_step_info_t info;
+        int rc = nqs_sr_step_minsr_full(cfg, sx, sy, a, s, fn, user, nullptr, nullptr, &info);
+        if (rc != 0) return rc;
+        if (trace) trace[it] = info.mean_energy;
+    }
+    return 0;
+}
+
+int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_log_amp_fn_t fn,
+                          void *user, nqs_gradient_fn_t gfn, void *guser, const int *batch, int Ns, int minsr,
+                          nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
+    if (!cfg || !a || !batch || Ns <= 0) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, nullptr, batch, Ns, fn, user, gfn, guser, minsr};
+    return sr_step_impl(in, info, out_E, out_delta);
+}
+
+}  // extern "C"

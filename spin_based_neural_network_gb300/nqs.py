@@ -1,0 +1,371 @@
+"""Thin Python mirror of the C API in include/nqs/*.h.
+
+Names, argument meaning and error behaviour follow the upstream C entry points
+(upstream include/nqs/nqs_ansatz.h, nqs_sampler.h, nqs_gradient.h,
+nqs_optimizer.h, nqs_marshall.h, nqs_symproj.h); every call goes straight to
+libnqs_gb300.so.  Failures raise NqsError carrying nqs_gpu_last_error().
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi, lib
+
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int)
+VP = C.c_void_p
+
+
+class NqsError(RuntimeError):
+    pass
+
+
+def _declare(L):
+    cfgp = C.POINTER(abi.NqsConfig)
+    optp = C.POINTER(abi.GpuOptions)
+    infop = C.POINTER(abi.StepInfo)
+    sig = {
+        "nqs_ansatz_create": (VP, [cfgp, C.c_int]),
+        "nqs_ansatz_free": (None, [VP]),
+        "nqs_ansatz_num_params": (C.c_long, [VP]),
+        "nqs_ansatz_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
+        "nqs_ansatz_logpsi_gradient": (C.c_int, [VP, IP, C.c_int, DP]),
+        "nqs_ansatz_logpsi_gradient_complex": (C.c_int, [VP, IP, C.c_int, DP, DP]),
+        "nqs_ansatz_is_complex": (C.c_int, [VP]),
+        "nqs_ansatz_apply_update": (C.c_int, [VP, DP, C.c_double]),
+        "nqs_ansatz_params_raw": (DP, [VP]),
+        "nqs_sampler_create": (VP, [C.c_int, cfgp, VP, VP]),
+        "nqs_sampler_create_gpu": (VP, [C.c_int, cfgp, optp, VP, VP]),
+        "nqs_sampler_free": (None, [VP]),
+        "nqs_sampler_thermalize": (None, [VP]),
+        "nqs_sampler_next": (IP, [VP]),
+        "nqs_sampler_batch": (C.c_int, [VP, C.c_int, IP]),
+        "nqs_sampler_acceptance_ratio": (C.c_double, [VP]),
+        "nqs_sampler_current": (IP, [VP]),
+        "nqs_sampler_num_sites": (C.c_int, [VP]),
+        "nqs_sampler_num_chains": (C.c_int, [VP]),
+        "nqs_local_energy": (C.c_double, [cfgp, C.c_int, C.c_int, IP, VP, VP]),
+        "nqs_local_energy_batch": (None, [cfgp, C.c_int, C.c_int, IP, C.c_int, VP, VP, DP]),
+        "nqs_local_energy_complex": (None, [cfgp, C.c_int, C.c_int, IP, VP, VP, DP, DP]),
+        "nqs_local_energy_batch_complex": (None, [cfgp, C.c_int, C.c_int, IP, C.c_int, VP, VP, DP, DP]),
+        "nqs_sr_step": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, infop]),
+        "nqs_sr_run": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, DP]),
+        "nqs_sr_step_custom": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, infop]),
+        "nqs_sr_run_custom": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
+        "nqs_sr_step_custom_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
+        "nqs_sr_run_custom_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, DP]),
+        "nqs_sr_step_minsr_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
+        "nqs_sr_run_minsr": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
+        "nqs_marshall_parity": (C.c_int, [IP, C.c_int, C.c_int]),
+        "nqs_marshall_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
+        "nqs_symproj_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
+        "nqs_symproj_gradient": (C.c_int, [VP, VP, IP, C.c_int, DP]),
+        "nqs_kagome_translation_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), IP]),
+        "nqs_kagome_p2_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
+        "nqs_gpu_options_default": (abi.GpuOptions, []),
+        "nqs_gpu_set_options": (C.c_int, [optp]),
+        "nqs_gpu_get_options": (C.c_int, [optp]),
+        "nqs_gpu_last_error": (C.c_char_p, []),
+        "nqs_gpu_device_info": (C.c_int, [C.c_char_p, C.c_int, IP]),
+        "nqs_gpu_stream": (VP, []),
+        "nqs_gpu_synchronize": (C.c_int, []),
+        "nqs_gpu_log_amp_batch": (C.c_int, [VP, VP, IP, C.c_int, C.c_int, DP, DP]),
+        "nqs_gpu_local_energy_batch": (C.c_int, [cfgp, C.c_int, C.c_int, IP, C.c_int, VP, VP, DP, DP]),
+        "nqs_gpu_gradient_batch": (C.c_int, [VP, VP, VP, IP, C.c_int, C.c_int, DP, DP]),
+        "nqs_gpu_sr_step_batch": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, IP, C.c_int,
+                                            C.c_int, infop, DP, DP]),
+        "nqs_gpu_last_step_stats": (C.c_int, [VP]),
+        "nqs_gpu_profile_enable": (C.c_int, [C.c_int]),
+        "nqs_gpu_profile_reset": (C.c_int, []),
+        "nqs_gpu_profile_read": (C.c_int, [C.c_int, VP, IP, DP]),
+        "nqs_gpu_launch_count": (C.c_long, []),
+        "nqs_gpu_event_record": (VP, []),
+        "nqs_gpu_event_elapsed_ms": (C.c_double, [VP, VP]),
+        "nqs_gpu_event_destroy": (None, [VP]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def fn(name):
+    """Address of an exported amplitude / gradient callback (e.g.
+    'nqs_ansatz_log_amp'), usable as an nqs_log_amp_fn_t argument."""
+    return C.cast(getattr(lib(), name), C.c_void_p).value
+
+
+def last_error():
+    return lib().nqs_gpu_last_error().decode()
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise NqsError("%s failed: %s" % (what, last_error()))
+
+
+def _ip(a):
+    return a.ctypes.data_as(IP)
+
+
+def _dp(a):
+    return a.ctypes.data_as(DP)
+
+
+def spins_array(spins, N=None):
+    s = np.ascontiguousarray(spins, dtype=np.int32)
+    if s.ndim == 1:
+        s = s.reshape(1, -1)
+    if N is not None and s.shape[1] != N:
+        raise ValueError("expected %d sites, got %d" % (N, s.shape[1]))
+    return s
+
+
+def set_options(**kw):
+    o = lib().nqs_gpu_options_default()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    _check(lib().nqs_gpu_set_options(C.byref(o)), "nqs_gpu_set_options")
+    return o
+
+
+def options(**kw):
+    o = lib().nqs_gpu_options_default()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Ansatz:
+    """nqs_ansatz_t (upstream include/nqs/nqs_ansatz.h:28-82)."""
+
+    def __init__(self, cfg, num_sites):
+        self.cfg = cfg
+        self.h = lib().nqs_ansatz_create(C.byref(cfg), num_sites)
+        if not self.h:
+            raise NqsError("nqs_ansatz_create failed: " + last_error())
+        self.N = num_sites
+        self.P = lib().nqs_ansatz_num_params(self.h)
+
+    def free(self):
+        if self.h:
+            lib().nqs_ansatz_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        """numpy view of the host mirror (nqs_ansatz_params_raw); writes are
+        picked up by the next library call."""
+        return np.ctypeslib.as_array(lib().nqs_ansatz_params_raw(self.h), shape=(self.P,))
+
+    @property
+    def user(self):
+        return self.h
+
+    log_amp_fn = property(lambda self: fn("nqs_ansatz_log_amp"))
+
+    def is_complex(self):
+        return bool(lib().nqs_ansatz_is_complex(self.h))
+
+    def log_amp(self, spins):
+        s = spins_array(spins, self.N)[0]
+        la, ar = C.c_double(), C.c_double()
+        lib().nqs_ansatz_log_amp(_ip(s), self.N, self.h, C.byref(la), C.byref(ar))
+        return la.value, ar.value
+
+    def gradient(self, spins, complex_out=False):
+        s = spins_array(spins, self.N)
+        B = s.shape[0]
+        re = np.zeros((B, self.P))
+        im = np.zeros((B, self.P)) if complex_out else None
+        _check(lib().nqs_gpu_gradient_batch(self.h, None, None, _ip(s), B, int(complex_out), _dp(re),
+                                            _dp(im) if complex_out else None), "gradient")
+        return (re, im) if complex_out else re
+
+    def apply_update(self, delta, step):
+        d = np.ascontiguousarray(delta, dtype=np.float64)
+        _check(lib().nqs_ansatz_apply_update(self.h, _dp(d), step), "nqs_ansatz_apply_update")
+
+
+class Marshall:
+    """nqs_marshall_wrapper_t around another program."""
+
+    def __init__(self, base_fn, base_user, size_x, size_y):
+        self.s = abi.MarshallWrapper(base_fn, base_user, size_x, size_y)
+        self.log_amp_fn = fn("nqs_marshall_log_amp")
+
+    @property
+    def user(self):
+        return C.addressof(self.s)
+
+
+class Symproj:
+    """nqs_symproj_wrapper_t; keeps the permutation and character arrays alive."""
+
+    def __init__(self, base_fn, base_user, num_sites, perm, chars):
+        self.perm = np.ascontiguousarray(perm, dtype=np.int32).ravel()
+        self.chars = np.ascontiguousarray(chars, dtype=np.float64)
+        self.s = abi.SymprojWrapper(base_fn, base_user, num_sites, len(self.chars), _ip(self.perm),
+                                    _dp(self.chars))
+        self.log_amp_fn = fn("nqs_symproj_log_amp")
+        self.gradient_fn = fn("nqs_symproj_gradient")
+
+    @property
+    def user(self):
+        return C.addressof(self.s)
+
+
+def kagome_perm(Lx, Ly, group="p2"):
+    p = IP()
+    G = C.c_int()
+    if group == "p2":
+        ch = DP()
+        _check(lib().nqs_kagome_p2_perm(Lx, Ly, C.byref(p), C.byref(ch), C.byref(G)), "p2 perm")
+        chars = np.ctypeslib.as_array(ch, shape=(G.value,)).copy()
+    else:
+        _check(lib().nqs_kagome_translation_perm(Lx, Ly, C.byref(p), C.byref(G)), "translation perm")
+        chars = np.ones(G.value)
+    N = 3 * Lx * Ly
+    perm = np.ctypeslib.as_array(p, shape=(G.value * N,)).copy().reshape(G.value, N)
+    return perm, chars
+
+
+def log_amp_batch(log_amp_fn, user, spins):
+    s = spins_array(spins)
+    B, N = s.shape
+    la, ar = np.zeros(B), np.zeros(B)
+    _check(lib().nqs_gpu_log_amp_batch(log_amp_fn, user, _ip(s), B, N, _dp(la), _dp(ar)), "log_amp_batch")
+    return la, ar
+
+
+def local_energy_batch(cfg, size_x, size_y, spins, log_amp_fn, user, complex_out=False):
+    s = spins_array(spins)
+    B = s.shape[0]
+    re, im = np.zeros(B), np.zeros(B)
+    _check(lib().nqs_gpu_local_energy_batch(C.byref(cfg), size_x, size_y, _ip(s), B, log_amp_fn, user,
+                                            _dp(re), _dp(im)), "local_energy_batch")
+    return (re, im) if complex_out else re
+
+
+def symproj_gradient_batch(ansatz, sym, spins):
+    s = spins_array(spins, ansatz.N)
+    B = s.shape[0]
+    out = np.zeros((B, ansatz.P))
+    _check(lib().nqs_gpu_gradient_batch(ansatz.h, sym.gradient_fn, sym.user, _ip(s), B, 0, _dp(out), None),
+           "symproj gradient")
+    return out
+
+
+class Sampler:
+    """nqs_sampler_t (upstream include/nqs/nqs_sampler.h:20-75)."""
+
+    def __init__(self, num_sites, cfg, log_amp_fn, user, opts=None):
+        self.cfg = cfg
+        if opts is None:
+            self.h = lib().nqs_sampler_create(num_sites, C.byref(cfg), log_amp_fn, user)
+        else:
+            self.h = lib().nqs_sampler_create_gpu(num_sites, C.byref(cfg), C.byref(opts), log_amp_fn, user)
+        if not self.h:
+            raise NqsError("nqs_sampler_create failed: " + last_error())
+        self.N = num_sites
+
+    def free(self):
+        if self.h:
+            lib().nqs_sampler_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def thermalize(self):
+        lib().nqs_sampler_thermalize(self.h)
+
+    def batch(self, n):
+        out = np.zeros((n, self.N), dtype=np.int32)
+        _check(lib().nqs_sampler_batch(self.h, n, _ip(out)), "nqs_sampler_batch")
+        return out
+
+    def next(self):
+        p = lib().nqs_sampler_next(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.N,)).copy()
+
+    def current(self):
+        p = lib().nqs_sampler_current(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.N,)).copy()
+
+    def acceptance_ratio(self):
+        return lib().nqs_sampler_acceptance_ratio(self.h)
+
+    @property
+    def num_chains(self):
+        return lib().nqs_sampler_num_chains(self.h)
+
+
+def sr_step_minsr(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, grad_fn=None,
+                  grad_user=None):
+    info = abi.StepInfo()
+    _check(lib().nqs_sr_step_minsr_full(C.byref(cfg), size_x, size_y, ansatz.h, sampler.h, log_amp_fn, user,
+                                        grad_fn, grad_user, C.byref(info)), "nqs_sr_step_minsr_full")
+    return info
+
+
+def sr_step_cg(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, grad_fn=None,
+               grad_user=None):
+    info = abi.StepInfo()
+    _check(lib().nqs_sr_step_custom_full(C.byref(cfg), size_x, size_y, ansatz.h, sampler.h, log_amp_fn, user,
+                                         grad_fn, grad_user, C.byref(info)), "nqs_sr_step_custom_full")
+    return info
+
+
+def sr_step_batch(cfg, size_x, size_y, ansatz, batch, minsr=True, log_amp_fn=None, user=None, grad_fn=None,
+                  grad_user=None):
+    """One SR step on a caller-supplied batch; returns (info, energies, delta)."""
+    s = spins_array(batch, ansatz.N)
+    Ns = s.shape[0]
+    E, d = np.zeros(Ns), np.zeros(ansatz.P)
+    info = abi.StepInfo()
+    _check(lib().nqs_gpu_sr_step_batch(C.byref(cfg), size_x, size_y, ansatz.h, log_amp_fn, user, grad_fn,
+                                       grad_user, _ip(s), Ns, int(minsr), C.byref(info), _dp(E), _dp(d)),
+           "nqs_gpu_sr_step_batch")
+    return info, E, d
+
+
+class StepStats(C.Structure):
+    _fields_ = [("tau_int", C.c_double), ("ess", C.c_double), ("refine_residual", C.c_double),
+                ("refine_sweeps", C.c_int), ("chol_retry", C.c_int), ("chol_fail_col", C.c_int),
+                ("gpu_launches", C.c_int)]
+
+
+def last_step_stats():
+    s = StepStats()
+    lib().nqs_gpu_last_step_stats(C.byref(s))
+    return s
+
+
+def profile(on):
+    lib().nqs_gpu_profile_enable(int(on))
+
+
+def profile_reset():
+    lib().nqs_gpu_profile_reset()
+
+
+def profile_read(cap=64):
+    names = (C.c_char * 48 * cap)()
+    counts = (C.c_int * cap)()
+    ms = (C.c_double * cap)()
+    n = lib().nqs_gpu_profile_read(cap, C.cast(names, VP), counts, ms)
+    return {bytes(names[i]).split(b"\0")[0].decode(): (counts[i], ms[i]) for i in range(n)}
+
+
+def launch_count():
+    return lib().nqs_gpu_launch_count()
