@@ -278,11 +278,13 @@ def test_sr_step_on_reference_batch(nqs, name):
         assert info.cg_iterations == int(ref[4])
 
 
-@pytest.mark.parametrize("Ns,iters,shift", [(256, 10, 1e-3), (2048, 100, 1e-2)])
-def test_cg_sr_against_oracle(nqs, Ns, iters, shift):
+@pytest.mark.parametrize("Ns,iters,shift,tol", [(256, 10, 1e-3, 1e-6), (2048, 400, 1e-2, 1e-13)])
+def test_cg_sr_against_oracle(nqs, Ns, iters, shift, tol):
     """CG-SR parity at the 1e-10 bar: an iteration-capped solve on the upstream
-    fixture's singular system, and a well-conditioned (N_s > N_p) solve that
-    converges before the cap."""
+    fixture's singular system, and a well-conditioned (N_s > N_p, cond ~ 1e2)
+    solve driven to a 1e-13 residual, where both solvers must reach the exact
+    solution.  (With the default 1e-6 tolerance two correct CG runs stop at
+    different points inside that tolerance, ~1e-7 apart.)"""
     from spin_based_neural_network_gb300 import abi
     N, M = 16, 16
     a = make_ansatz(nqs, O.OR_RBM, N, M, None, 0.3, 31337)
@@ -290,15 +292,17 @@ def test_cg_sr_against_oracle(nqs, Ns, iters, shift):
     rng = np.random.default_rng(Ns)
     batch = np.where(rng.random((Ns, N)) < 0.5, 1, -1).astype(np.int32)
     cfg = abi.config_defaults(hamiltonian=0, transverse_field=0.9, sr_diag_shift=shift, learning_rate=0.01,
-                              sr_cg_max_iters=iters)
+                              sr_cg_max_iters=iters, sr_cg_tol=tol)
     info, E, delta = nqs.sr_step_batch(cfg, 4, 4, a, batch, minsr=False)
     amp = O.Amp(O.OR_RBM, N, M, p0.copy())
-    Eo, do, io = O.cgsr_step(O.ham(O.OR_TFIM, 4, 4, Gamma=0.9), amp, batch, shift, 0.01, iters, 1e-6)
+    Eo, do, io = O.cgsr_step(O.ham(O.OR_TFIM, 4, 4, Gamma=0.9), amp, batch, shift, 0.01, iters, tol)
     assert rel(E, Eo) < TOL
     assert np.linalg.norm(delta - do) <= TOL_DELTA * np.linalg.norm(do)
-    assert info.cg_iterations == io.cg_iterations and info.converged == io.converged
+    assert info.converged == io.converged
     if Ns == 2048:
-        assert io.converged == 1 and io.cg_iterations < iters
+        assert io.converged == 1 and abs(info.cg_iterations - io.cg_iterations) <= 3
+    else:
+        assert info.cg_iterations == io.cg_iterations == iters
 
 
 @pytest.mark.parametrize("name", ["minsr_tfim_rbm", "minsr_heis_crbm_marshall", "cg_tfim_rbm"])
