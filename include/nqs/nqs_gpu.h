@@ -104,6 +104,38 @@ int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int size_x, int size_y,
                           nqs_sr_step_info_t *out_info,
                           double *out_energies, double *out_delta);
 
+/* MinSR solve that allocates no device memory.  It has no counterpart in the
+ * upstream library.
+ *
+ * For callers that cannot call cudaMalloc: a host framework that has reserved
+ * (pre-allocated) the device memory for its own pool, so that an allocation
+ * made by a plug-in fails or fragments that pool, or a latency-critical loop
+ * that must stay out of the driver's allocator.  The caller passes device
+ * buffers: the Jacobian d_O [num_samples][num_params] (FP64, row-major, not
+ * centred, only read), the local energies d_E [num_samples] and the output
+ * d_delta [num_params].  The routine centres O, forms T = O_c O_c^T / N_s +
+ * diag_shift I, factors it (FP64 Cholesky), solves (T) y = E - <E> and writes
+ * delta = O_c^T y / N_s, the same arithmetic as the MinSR step.  A failed
+ * factorisation gives delta = 0 and out_info->converged = 0 (the upstream
+ * +1e-6 retry would need a second N_s x N_s copy and is not run here).
+ * out_info (host, optional) receives <E>, Var(E), ||delta|| (update_norm,
+ * without a learning rate) and converged.  Runs on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream) and returns after the result is ready.
+ *
+ * Limits: num_samples <= 1024 and num_params <= 16384; larger sizes are
+ * rejected with -1 and a message in nqs_gpu_last_error().  All scratch
+ * (the 1024 x 1024 Gram matrix, vectors, status words: about 8.5 MB) is one
+ * statically sized device array that every GPU which loads this library keeps
+ * until the process exits.  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress) with the device current; make that
+ * first call before any stream capture.  Every call reuses the same array and
+ * it keeps the last call's contents, so calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller. */
+int nqs_gpu_minsr_solve_noalloc(const double *d_O, const double *d_E,
+                                int num_samples, long num_params, double diag_shift,
+                                double *d_delta, nqs_sr_step_info_t *out_info,
+                                void *stream);
+
 /* Statistics of the last SR step on this thread. */
 typedef struct {
     double tau_int;          /* integrated autocorrelation time of E_loc (Sokal, c = 5) */

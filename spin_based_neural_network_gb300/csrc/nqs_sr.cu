@@ -807,3 +807,207 @@ int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t 
 }
 
 }  // extern "C"
+
+// ====================================================================== no-allocation MinSR solve
+//
+// nqs_gpu_minsr_solve_noalloc solves the MinSR system for a Jacobian and local
+// energies that the caller already holds in device memory, without allocating
+// any device memory.  It is for callers that cannot call cudaMalloc: a host
+// framework that owns (and has pre-reserved) all device memory, so that a
+// stray cudaMalloc from a plug-in can fail or fragment its pool, or a
+// latency-critical loop that must not enter the driver's allocator.  All of
+// its scratch lives in one statically sized device array below, which every
+// GPU that loads this library holds until the process exits.
+namespace nqs {
+
+constexpr int kNoAllocMaxSamples = 1024;     // T is N_s x N_s doubles (8 MiB at the limit)
+constexpr long kNoAllocMaxParams = 16384;
+constexpr size_t kNoAllocScratchDoubles = (size_t)kNoAllocMaxSamples * kNoAllocMaxSamples  // T
+                                          + (size_t)kNoAllocMaxParams                       // <O_k>
+                                          + 3 * (size_t)kNoAllocMaxSamples                  // eps, y, z
+                                          + 16                                              // scalars
+                                          + 16;                                             // status words
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+// Gram of the centred Jacobian with the centring done while staging tiles:
+// T[i][j] = scale * sum_k (O[i][k] - m_k)(O[j][k] - m_k) (+ shift on the
+// diagonal), lower triangle.  The caller's O is only read.
+__global__ void __launch_bounds__(256) k_gram_fp64_centred(const double *__restrict__ O, int Ns, long P,
+                                                           const double *__restrict__ m, double scale,
+                                                           double shift, double *T) {
+    __shared__ double As[KC][TG + 1], Bs[KC][TG + 1];
+    int bi, bj;
+    tri_tile(blockIdx.x, bi, bj);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int r0 = bi * TG, c0 = bj * TG;
+    double acc[4][4] = {};
+    for (long kk = 0; kk < P; kk += KC) {
+        for (int e = tid; e < TG * KC; e += 256) {
+            int rr = e / KC, cc = e % KC;
+            long k = kk + cc;
+            int ra = r0 + rr, rb = c0 + rr;
+            As[cc][rr] = (ra < Ns && k < P) ? O[(size_t)ra * P + k] - m[k] : 0.0;
+            Bs[cc][rr] = (rb < Ns && k < P) ? O[(size_t)rb * P + k] - m[k] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < KC; c++) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) av[q] = As[c][ty + 16 * q];
+#pragma unroll
+            for (int q = 0; q < 4; q++) bv[q] = Bs[c][tx + 16 * q];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            int i = r0 + ty + 16 * a, j = c0 + tx + 16 * b;
+            if (i < Ns && j <= i) T[(size_t)i * Ns + j] = acc[a][b] * scale + (i == j ? shift : 0.0);
+        }
+}
+
+// delta_k = scale * sum_i (O[i][k] - m_k) y_i  (status[I_FAIL] >= 0 -> 0).
+__global__ void k_col_dot_centred(const double *__restrict__ O, int Ns, long P, const double *__restrict__ m,
+                                  const double *__restrict__ y, double scale, const int *status,
+                                  double *out) {
+    __shared__ double a[8][33];
+    long k = (long)blockIdx.x * 32 + threadIdx.x;
+    double s = 0.0;
+    if (k < P)
+        for (int i = threadIdx.y; i < Ns; i += 8) s += (O[(size_t)i * P + k] - m[k]) * y[i];
+    a[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && k < P) {
+        double S = 0.0;
+        for (int q = 0; q < 8; q++) S += a[q][threadIdx.x];
+        out[k] = status[I_FAIL] >= 0 ? 0.0 : S * scale;
+    }
+}
+
+// ||delta||^2 into scal[S_NORM2] (one block).
+__global__ void k_norm2(const double *__restrict__ d, long P, double *scal) {
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (long k = threadIdx.x; k < P; k += blockDim.x) s += d[k] * d[k];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) scal[S_NORM2] = red[0];
+}
+
+// Device address of the scratch array, looked up once per device.
+static double *g_noalloc_ptr[64];
+static std::mutex g_noalloc_mu;
+
+static double *noalloc_scratch(int dev) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return nullptr;
+    }
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed: %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        g_noalloc_ptr[dev] = (double *)p;
+    }
+    return g_noalloc_ptr[dev];
+}
+
+}  // namespace nqs
+
+extern "C" {
+
+// See nqs_gpu.h.  Same factorisation and solve as the MinSR step (blocked FP64
+// Cholesky, blocked triangular solves); the upstream +1e-6 retry is not run
+// here (it needs a second N_s x N_s copy): a failed factorisation returns
+// delta = 0 with out_info->converged = 0.
+int nqs_gpu_minsr_solve_noalloc(const double *d_O, const double *d_E, int Ns, long P, double shift,
+                                double *d_delta, nqs_sr_step_info_t *out_info, void *stream_ptr) {
+    clear_error();
+    if (!d_O || !d_E || !d_delta || Ns <= 0 || P <= 0) {
+        set_error("nqs_gpu_minsr_solve_noalloc: NULL buffer or non-positive size");
+        return -1;
+    }
+    if (Ns > kNoAllocMaxSamples || P > kNoAllocMaxParams) {
+        set_error("nqs_gpu_minsr_solve_noalloc: N_s = %d, N_p = %ld exceed the static scratch limits "
+                  "(N_s <= %d, N_p <= %ld)", Ns, P, kNoAllocMaxSamples, kNoAllocMaxParams);
+        return -1;
+    }
+    int dev = 0;
+    if (!NQS_CUDA(cudaGetDevice(&dev))) return -1;
+    double *base = noalloc_scratch(dev);
+    if (!base) return -1;
+    cudaStream_t st = (cudaStream_t)stream_ptr;
+    double *T = base;
+    double *gm = T + (size_t)kNoAllocMaxSamples * kNoAllocMaxSamples;
+    double *eps = gm + kNoAllocMaxParams;
+    double *y = eps + kNoAllocMaxSamples;
+    double *z = y + kNoAllocMaxSamples;
+    double *scal = z + kNoAllocMaxSamples;
+    int *status = (int *)(scal + 16);
+    // the array keeps the previous call's contents: reset what must start fresh
+    if (!NQS_CUDA(cudaMemsetAsync(scal, 0, 16 * sizeof(double), st)) ||
+        !NQS_CUDA(cudaMemsetAsync(status, 0xff, 16 * sizeof(int), st)))
+        return -1;
+    k_energy_stats<<<1, 1024, 0, st>>>(d_E, Ns, scal, eps);
+    dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
+    k_col_stats<<<cg, cb, 0, st>>>(d_O, Ns, P, nullptr, scal, gm, nullptr);
+    int nt = (Ns + TG - 1) / TG;
+    k_gram_fp64_centred<<<nt * (nt + 1) / 2, 256, 0, st>>>(d_O, Ns, P, gm, 1.0 / (double)Ns, shift, T);
+    for (int k0 = 0; k0 < Ns; k0 += NB) {
+        int kb = Ns - k0 < NB ? Ns - k0 : NB;
+        k_potrf_diag<<<1, dim3(32, 32), 0, st>>>(T, Ns, k0, kb, status);
+        int k1 = k0 + kb, rest = Ns - k1;
+        if (rest <= 0) break;
+        k_trsm_panel<<<(rest + 127) / 128, 128, 0, st>>>(T, Ns, k0, kb, kb, k1, status, 0);
+        int ntt = (rest + TG - 1) / TG;
+        k_syrk_update<<<ntt * (ntt + 1) / 2, 256, 0, st>>>(T, Ns, k0, kb, k1, status);
+    }
+    // forward and backward substitution (skipped work is harmless: delta is
+    // zeroed below when the factorisation failed)
+    if (!NQS_CUDA(cudaMemcpyAsync(z, eps, sizeof(double) * Ns, cudaMemcpyDeviceToDevice, st))) return -1;
+    for (int k0 = 0; k0 < Ns; k0 += NB) {
+        int kb = Ns - k0 < NB ? Ns - k0 : NB, rest = Ns - k0 - kb;
+        k_trsv_fwd<<<rest > 0 ? (rest + 127) / 128 : 1, 128, 0, st>>>(T, Ns, k0, kb, z, y);
+    }
+    if (!NQS_CUDA(cudaMemcpyAsync(z, y, sizeof(double) * Ns, cudaMemcpyDeviceToDevice, st))) return -1;
+    for (int k0 = ((Ns - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
+        int kb = Ns - k0 < NB ? Ns - k0 : NB;
+        k_trsv_bwd<<<k0 > 0 ? (k0 + 127) / 128 : 1, 128, 0, st>>>(T, Ns, k0, kb, z, y);
+    }
+    k_col_dot_centred<<<cg, cb, 0, st>>>(d_O, Ns, P, gm, y, 1.0 / (double)Ns, status, d_delta);
+    k_norm2<<<1, 1024, 0, st>>>(d_delta, P, scal);
+    if (!NQS_CUDA(cudaGetLastError())) return -1;
+    double hs[16];
+    int hst[16];
+    if (!NQS_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaMemcpyAsync(hst, status, sizeof(hst), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaStreamSynchronize(st)))
+        return -1;
+    if (out_info) {
+        out_info->mean_energy = hs[S_EMEAN];
+        out_info->variance_energy = hs[S_ESQ] - hs[S_EMEAN] * hs[S_EMEAN];
+        out_info->update_norm = sqrt(hs[S_NORM2]);
+        out_info->acceptance_ratio = 0.0;
+        out_info->cg_iterations = 0;
+        out_info->converged = hst[I_FAIL] < 0 ? 1 : 0;
+    }
+    return 0;
+}
+
+}  // extern "C"

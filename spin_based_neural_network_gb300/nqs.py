@@ -82,6 +82,7 @@ def _declare(L):
         "nqs_gpu_event_record": (VP, []),
         "nqs_gpu_event_elapsed_ms": (C.c_double, [VP, VP]),
         "nqs_gpu_event_destroy": (None, [VP]),
+        "nqs_gpu_minsr_solve_noalloc": (C.c_int, [VP, VP, C.c_int, C.c_long, C.c_double, VP, infop, VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
