@@ -53,7 +53,9 @@ typedef struct {
     int lattice_x;       /* exchange moves: lattice whose nearest-neighbour bonds */
     int lattice_y;       /*   are swapped (0 x 0 = periodic ring of N sites)      */
     int lattice_kagome;  /*   1: kagome cells, bonds of kagome_pbc = 1          */
-    int reserved[4];
+    int mixed_check;     /* MIXED: also solve in FP64 on the same samples and
+                          * report the delta-theta error (step stats) */
+    int reserved[3];
 } nqs_gpu_options_t;
 
 /* Defaults: compat sampler, single flips, open lattices, FP64. */
@@ -136,6 +138,14 @@ int nqs_gpu_minsr_solve_noalloc(const double *d_O, const double *d_E,
                                 double *d_delta, nqs_sr_step_info_t *out_info,
                                 void *stream);
 
+/* Diagnostic: the tensor-core (tcgen05, TF32) Gram used by the MIXED MinSR
+ * path, alone.  O_host [num_samples][num_params] FP64 is taken as already
+ * centred; T_out [num_samples][num_samples] receives the lower triangle of
+ * scale * (hi hi^T) (passes = 1) or scale * (hi hi^T + hi lo^T + lo hi^T)
+ * (passes = 3) where O = hi + lo is split into two TF32 words. */
+int nqs_gpu_gram_tc(const double *O_host, int num_samples, long num_params, int passes,
+                    double scale, float *T_out);
+
 /* Statistics of the last SR step on this thread. */
 typedef struct {
     double tau_int;          /* integrated autocorrelation time of E_loc (Sokal, c = 5) */
@@ -145,6 +155,9 @@ typedef struct {
     int    chol_retry;       /* 1 if the +1e-6 retry ran */
     int    chol_fail_col;    /* first failing column or -1 */
     int    gpu_launches;     /* kernels launched by the step */
+    double delta_rel_err;    /* MIXED with mixed_check: ||d - d_fp64|| / ||d_fp64|| */
+    int    mixed_fallback;   /* 1 if the FP32 factor failed and FP64 solved the step */
+    int    pad_;
 } nqs_gpu_step_stats_t;
 int nqs_gpu_last_step_stats(nqs_gpu_step_stats_t *out);
 

@@ -16,7 +16,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnqs_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["nqs_context.cu", "nqs_ansatz.cu", "nqs_local_energy.cu", "nqs_sampler.cu", "nqs_sr.cu"]
+SOURCES = ["nqs_context.cu", "nqs_ansatz.cu", "nqs_local_energy.cu", "nqs_sampler.cu", "nqs_sr.cu",
+           "nqs_mixed.cu"]
 
 
 def nvcc():

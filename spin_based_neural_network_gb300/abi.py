@@ -130,5 +130,6 @@ class GpuOptions(C.Structure):
         ("lattice_x", C.c_int),
         ("lattice_y", C.c_int),
         ("lattice_kagome", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("mixed_check", C.c_int),
+        ("reserved", C.c_int * 3),
     ]

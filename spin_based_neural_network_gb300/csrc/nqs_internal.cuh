@@ -168,6 +168,11 @@ bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, 
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
 
+// Mixed-precision MinSR solve (nqs_mixed.cu): centres O in place, writes y with
+// (T + shift I) y = eps; *out_fail >= 0 when the FP32 factor broke down.
+bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
+                       int passes, double *y, double *out_resid, int *out_fail);
+
 // thread-local statistics of the last SR step
 nqs_gpu_step_stats_t &step_stats();
 

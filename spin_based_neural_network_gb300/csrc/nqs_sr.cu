@@ -22,7 +22,7 @@ bool sampler_produce(Sampler *s, int n, uint64_t **d_out);
 
 // ---------------------------------------------------------------- workspace
 struct Workspace {
-    DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part;
+    DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part, y64, d64;
     DevBuf<int> status;
     DevBuf<uint64_t> batch_bits;
 };
@@ -600,11 +600,17 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             NQS_LAUNCH("col_mean");
             k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
         }
-        {
-            NQS_LAUNCH("center");
-            k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
-        }
+        const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
+        nqs_gpu_step_stats_t &ss = step_stats();
+        ss.refine_residual = 0.0;
+        ss.refine_sweeps = 0;
+        ss.mixed_fallback = 0;
+        ss.delta_rel_err = -1.0;
+        // FP64 factorisation and solve of (T + shift I) y = eps on the centred O,
+        // with the upstream retry semantics; writes y_out.
+        auto fp64_solve = [&](double *y_out, int *conv) -> int {
         int nt = (Ns + TG - 1) / TG;
+        NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));
         {
             NQS_LAUNCH("gram_fp64");
             k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(w.O.p, Ns, P, 1.0 / (double)Ns,
@@ -644,16 +650,59 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
                 return -1;
         }
         if (fail2 < 0) {
-            if (!cholesky_solve(w.T.p, Ns, w.eps.p, w.z.p, w.y.p)) return -1;
-            converged = 1;
+            if (!cholesky_solve(w.T.p, Ns, w.eps.p, w.z.p, y_out)) return -1;
+            *conv = 1;
         } else {
             fprintf(stderr, "nqs_sr_step_minsr: Cholesky breakdown after retry; increase "
                             "sr_diag_shift or num_samples. Update set to 0.\n");
-            NQS_CUDA(cudaMemsetAsync(w.y.p, 0, sizeof(double) * Ns, st));
+            NQS_CUDA(cudaMemsetAsync(y_out, 0, sizeof(double) * Ns, st));
         }
+        return 0;
+        };
+        bool solved = false;
+        if (mixed) {
+            // centring happens inside the split kernel of the mixed solve
+            double resid = 0.0;
+            int f32 = -1;
+            if (!minsr_mixed_solve(w.O.p, w.gm.p, w.eps.p, Ns, P, cfg->sr_diag_shift, c.opts.refine_sweeps,
+                                   c.opts.gram_passes, w.y.p, &resid, &f32))
+                return -1;
+            ss.refine_residual = resid;
+            ss.refine_sweeps = c.opts.refine_sweeps;
+            if (f32 < 0) {
+                solved = true;
+                converged = 1;
+                ss.chol_fail_col = -1;
+                ss.chol_retry = 0;
+            } else {
+                ss.mixed_fallback = 1;          // FP32 factor failed: solve this step in FP64
+            }
+        } else {
+            NQS_LAUNCH("center");
+            k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+        }
+        if (!solved && fp64_solve(w.y.p, &converged) != 0) return -1;
         {
             NQS_LAUNCH("delta");
             k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y.p, 1.0 / (double)Ns, w.delta.p);
+        }
+        if (mixed && solved && c.opts.mixed_check) {
+            // the FP64 solve on the same centred Jacobian, for the delta-theta error
+            if (!w.y64.ensure(Ns) || !w.d64.ensure(P)) return -1;
+            int conv64 = 0;
+            if (fp64_solve(w.y64.p, &conv64) != 0) return -1;
+            k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y64.p, 1.0 / (double)Ns, w.d64.p);
+            std::vector<double> a((size_t)P), b((size_t)P);
+            if (!NQS_CUDA(cudaMemcpyAsync(a.data(), w.delta.p, sizeof(double) * P, cudaMemcpyDeviceToHost, st)) ||
+                !NQS_CUDA(cudaMemcpyAsync(b.data(), w.d64.p, sizeof(double) * P, cudaMemcpyDeviceToHost, st)) ||
+                !NQS_CUDA(cudaStreamSynchronize(st)))
+                return -1;
+            double num = 0.0, den = 0.0;
+            for (long k = 0; k < P; k++) {
+                num += (a[k] - b[k]) * (a[k] - b[k]);
+                den += b[k] * b[k];
+            }
+            ss.delta_rel_err = den > 0 ? sqrt(num / den) : 0.0;
         }
     } else {
         if (!w.F.ensure(P) || !w.r.ensure(P) || !w.p.ensure(P) || !w.Ap.ensure(P) || !w.u.ensure(Ns))

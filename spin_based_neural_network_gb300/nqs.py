@@ -83,6 +83,7 @@ def _declare(L):
         "nqs_gpu_event_elapsed_ms": (C.c_double, [VP, VP]),
         "nqs_gpu_event_destroy": (None, [VP]),
         "nqs_gpu_minsr_solve_noalloc": (C.c_int, [VP, VP, C.c_int, C.c_long, C.c_double, VP, infop, VP]),
+        "nqs_gpu_gram_tc": (C.c_int, [DP, C.c_int, C.c_long, C.c_int, C.c_double, C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -343,7 +344,8 @@ def sr_step_batch(cfg, size_x, size_y, ansatz, batch, minsr=True, log_amp_fn=Non
 class StepStats(C.Structure):
     _fields_ = [("tau_int", C.c_double), ("ess", C.c_double), ("refine_residual", C.c_double),
                 ("refine_sweeps", C.c_int), ("chol_retry", C.c_int), ("chol_fail_col", C.c_int),
-                ("gpu_launches", C.c_int)]
+                ("gpu_launches", C.c_int), ("delta_rel_err", C.c_double), ("mixed_fallback", C.c_int),
+                ("pad_", C.c_int)]
 
 
 def last_step_stats():

@@ -1,0 +1,87 @@
+"""Mixed-precision MinSR: tensor-core (tcgen05, TF32) Gram and FP32 factor with
+FP64 iterative refinement, checked against FP64 references.
+
+Bars: the 3-pass split Gram (hi hi^T + hi lo^T + lo hi^T) reproduces the FP64
+Gram to 2e-6 of its largest entry (single pass TF32: 5e-3); after refinement the
+MinSR update matches the FP64 oracle's on the same samples to 1e-8 relative
+(the refinement residual is reported by the step)."""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nqs():
+    import spin_based_neural_network_gb300 as pkg
+    pkg.build()
+    from spin_based_neural_network_gb300 import nqs as N
+    N.set_options()
+    return N
+
+
+def gram_tc(nqs, Om, passes, scale):
+    import ctypes as C
+    Om = np.ascontiguousarray(Om, dtype=np.float64)
+    Ns, P = Om.shape
+    T = np.zeros((Ns, Ns), dtype=np.float32)
+    rc = nqs.lib().nqs_gpu_gram_tc(Om.ctypes.data_as(nqs.DP), Ns, P, passes, scale,
+                                   T.ctypes.data_as(C.POINTER(C.c_float)))
+    assert rc == 0, nqs.last_error()
+    return T
+
+
+@pytest.mark.parametrize("Ns,P", [(128, 32), (500, 300), (4096, 1120)])
+def test_gram_tc_against_fp64(nqs, Ns, P):
+    rng = np.random.default_rng(Ns + P)
+    Om = rng.normal(size=(Ns, P))
+    Om[:, : P // 4] = np.sign(Om[:, : P // 4])          # +-1 columns like the visible block
+    ref = np.tril(Om @ Om.T) / Ns
+    scale = np.max(np.abs(ref))
+    T3 = np.tril(gram_tc(nqs, Om, 3, 1.0 / Ns).astype(np.float64))
+    assert np.max(np.abs(T3 - ref)) <= 2e-6 * scale
+    T1 = np.tril(gram_tc(nqs, Om, 1, 1.0 / Ns).astype(np.float64))
+    err1 = np.max(np.abs(T1 - ref))
+    assert err1 <= 5e-3 * scale and err1 > np.max(np.abs(T3 - ref))
+
+
+def minsr_mixed(nqs, sweeps, check=0):
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    N, M, Ns = 16, 32, 4096
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, rbm_init_scale=0.3,
+                              hamiltonian=1, rng_seed=4242, sr_diag_shift=1e-4, learning_rate=0.005)
+    a = nqs.Ansatz(cfg, N)
+    p0 = a.params.copy()
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    rng = np.random.default_rng(11)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(Ns)])
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=sweeps, gram_passes=3,
+                    mixed_check=check)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True, log_amp_fn=m.log_amp_fn,
+                                           user=m.user)
+        stats = nqs.last_step_stats()
+    finally:
+        nqs.set_options()
+    amp = O.Amp(O.OR_CRBM, N, M, p0.copy(), [("marshall", Lx, Ly)])
+    Eo, do, io = O.minsr_step(O.ham(O.OR_HEIS, Lx, Ly, pbc=1), amp, batch, 1e-4, 0.005)
+    return info, E, delta, stats, Eo, do, io
+
+
+def test_mixed_minsr_against_fp64_oracle(nqs):
+    info, E, delta, stats, Eo, do, io = minsr_mixed(nqs, sweeps=3, check=1)
+    assert info.converged == 1 and stats.mixed_fallback == 0
+    assert np.max(np.abs(E - Eo) / np.maximum(np.abs(Eo), 1.0)) < 1e-12
+    err = np.linalg.norm(delta - do) / np.linalg.norm(do)
+    assert stats.refine_residual < 1e-8
+    assert err < 1e-8
+    assert 0 <= stats.delta_rel_err < 1e-8          # the step's own FP64 cross-check
+
+
+def test_refinement_contracts(nqs):
+    """More sweeps, smaller residual: the refinement converges."""
+    r = [minsr_mixed(nqs, sweeps=s)[3].refine_residual for s in (0, 1, 2)]
+    assert r[1] < r[0] and r[2] < r[1]
