@@ -90,15 +90,34 @@ def init_params(P, seed=SEED):
 
 
 def algorithmic_work(Ns, P):
-    """Per-kernel algorithmic FLOPs of one MinSR step (2 flops per FMA)."""
-    gram = Ns * (Ns + 1) * P                        # lower triangle incl. diagonal
+    """Per-kernel FLOPs of one MinSR step (2 flops per FMA) and the pipe that
+    executes them.  gram: lower triangle incl. diagonal, N_s (N_s + 1) N_p;
+    the tensor-core Gram runs it three times (hi hi^T + hi lo^T + lo hi^T).
+    syrk: the trailing updates of the 32-wide panels, sum 2 * rest(rest+1)/2 * 32."""
+    gram = Ns * (Ns + 1) * P
     syrk = 0
     nb = 32
     for k0 in range(0, Ns, nb):
         kb = min(nb, Ns - k0)
         rest = Ns - k0 - kb
-        syrk += rest * (rest + 1) * kb              # 2 * rest(rest+1)/2 * kb
-    return {"gram_fp64": gram, "chol_syrk": syrk, "gram_tc": gram}
+        syrk += rest * (rest + 1) * kb
+    return {"gram_fp64": (gram, "fp64"), "chol_syrk": (syrk, "fp64"), "gram_tc": (3 * gram, "tensor"),
+            "chol32_syrk": (syrk, "fp32")}
+
+
+def device_shape(nqs):
+    import ctypes as C
+    name = C.create_string_buffer(128)
+    sms = C.c_int()
+    nqs.lib().nqs_gpu_device_info(name, 128, C.byref(sms))
+    clk = 2070.0
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=10).stdout.split()
+        clk = float(out[0])
+    except Exception:
+        pass
+    return sms.value, clk
 
 
 # ------------------------------------------------------------------ clocks
@@ -220,7 +239,8 @@ def run_gpu(args):
     L = nqs.lib()
 
     prec = abi.PREC_FP64 if args.precision == "fp64" else abi.PREC_MIXED
-    nqs.set_options(square_pbc=1, precision=prec)
+    base_opts = dict(square_pbc=1, precision=prec, refine_sweeps=3, gram_passes=3)
+    nqs.set_options(**base_opts)
     cfg = workload_cfg(abi)
     a = nqs.Ansatz(cfg, N_SITES)
     a.params[:] = init_params(a.P)
@@ -281,37 +301,75 @@ def run_gpu(args):
     work = algorithmic_work(NS, P)
     with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
         peaks = json.load(f)
-    roof = None
-    name, (cnt, ms) = top
-    if name in work:
-        launches_per_step = cnt / 3.0
-        flops_per_launch = work[name] / launches_per_step
-        avg_ms = ms / cnt
-        achieved = flops_per_launch / (avg_ms / 1000.0) / 1e12
+    sm_count, max_mhz = device_shape(nqs)
+    nominal = {"fp64": 1.25, "fp32": sm_count * 128 * 2 * max_mhz / 1e6, "tensor": peaks["bf16_tflops"]}
+
+    def roofline_of(name):
+        if name not in prof or name not in work:
+            return None
+        cnt, ms = prof[name]
+        flops, pipe = work[name]
+        achieved = (flops / (cnt / 3.0)) / (ms / cnt / 1000.0) / 1e12
         peak = peaks["bf16_tflops"]
-        roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "peak_source": "bf16_tflops of measured",
-                "pipe": "fp64" if name.endswith("fp64") or name.startswith("chol") else "tensor",
-                "frac_of_fp64_nominal": achieved / 1.25 if "fp64" in name or name.startswith("chol") else None,
-                "traffic": None, "share_of_step": ms / total}
+        return {"bound": "tensor", "kernel": name, "pipe": pipe, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": "bf16_tflops of measured",
+                "frac_of_pipe_nominal": achieved / nominal[pipe], "pipe_nominal_tflops": nominal[pipe],
+                "traffic": None, "share_of_step": ms / total, "avg_launch_us": 1000.0 * ms / cnt}
+
+    top_name = max(prof.items(), key=lambda kv: kv[1][1])[0]
+    roof = roofline_of(top_name)
     kernels = {k: {"launches_per_step": v[0] / 3.0, "ms_per_step": v[1] / 3.0} for k, v in
                sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    extra_roofs = {k: roofline_of(k) for k in ("gram_tc", "gram_fp64", "chol32_syrk", "chol_syrk")
+                   if k in prof and k != top_name}
+
+    # delta-theta error of the mixed step against the FP64 solve on the same samples
+    delta_err = None
+    if prec == abi.PREC_MIXED:
+        nqs.set_options(**dict(base_opts, mixed_check=1))
+        errs = []
+        for _ in range(2):
+            step()
+            errs.append(nqs.last_step_stats().delta_rel_err)
+        delta_err = {"max_rel": max(errs), "refine_residual": nqs.last_step_stats().refine_residual,
+                     "refine_sweeps": nqs.last_step_stats().refine_sweeps}
+        nqs.set_options(**base_opts)
+
+    # the plain FP64 path on the same state, for the mixed / plain ratio
+    plain = None
+    if prec == abi.PREC_MIXED and not args.no_plain:
+        nqs.set_options(**dict(base_opts, precision=abi.PREC_FP64))
+        step()
+        k_plain = max(2, args.steps // 4)
+        p0 = L.nqs_gpu_event_record()
+        for _ in range(k_plain):
+            step()
+        p1 = L.nqs_gpu_event_record()
+        pms = L.nqs_gpu_event_elapsed_ms(p0, p1)
+        L.nqs_gpu_event_destroy(p0)
+        L.nqs_gpu_event_destroy(p1)
+        plain = {"value": k_plain / (pms / 1000.0), "unit": "steps/s", "steps": k_plain}
+        nqs.set_options(**base_opts)
 
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == abi.PREC_FP64 else "mixed(tf32/bf16 gram, f64 solve)",
+            "dtype": "f64" if prec == abi.PREC_FP64 else
+            "mixed: tf32x3 tensor-core gram (fp32 accumulate), fp32 factor, f64 refinement; f64 sampling/E_loc/O",
             "data": "synthetic (sampled configurations; parameters N(0,0.01^2) from a seed)",
             "config": {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES,
                        "hidden": M_HIDDEN, "num_params": P, "num_samples": NS, "chains": CHAINS,
                        "decorrelate": DECOR, "moves": "nn-exchange, Sz=0", "shift": SHIFT, "lr": LR,
                        "precision": args.precision,
-                       "l2": "working set > L2 (Gram 4096^2 FP64 = 134 MB)",
+                       "l2": "working set > L2 every step (O 37 MB FP64 + split 37 MB + Gram 67 MB FP32 "
+                             "+ factor; FP64 path: Gram 134 MB)",
+                       "refine_sweeps": 3,
                        "parallelism": "replicas x%d" % ws},
             "gpu_launches": launches,
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * P,
                     "d2h_bytes_per_step": 8 * P + 16 * 8},
-            "roofline": roof, "clocks": clk, "kernels": kernels,
+            "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
+            "delta_theta_vs_fp64": delta_err, "plain_fp64": plain,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
@@ -331,7 +389,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

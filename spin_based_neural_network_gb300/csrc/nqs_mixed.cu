@@ -7,12 +7,13 @@
 //      staged by TMA (cp.async.bulk.tensor, 128-byte swizzle) in a 3-stage
 //      mbarrier ring, FP32 accumulator in TMEM read back with tcgen05.ld;
 //      only the lower-triangular 128 x 128 tiles are computed;
-//   3. FP32 blocked Cholesky T = L L^T and the explicit inverse X = L^{-1}, so
-//      every solve with the factor is two GEMVs (X and X^T, 33.5 MB at
-//      N_s = 4096, resident in the 129 MB L2);
+//   3. FP32 blocked Cholesky T = L L^T (32-wide panels: warp-register diagonal
+//      factor, panel solve, trailing SYRK) and the inverses of its 128 x 128
+//      diagonal blocks, so a triangular solve is 2 N_s / 128 block steps of two
+//      parallel GEMVs each;
 //   4. iterative refinement in FP64 against the exact operator
 //      A y = O_c (O_c^T y) / N_s + shift y (two FP64 passes over O_c):
-//      y <- y + X^T X (eps - A y).
+//      y <- y + (L L^T)^{-1} (eps - A y), the correction solved in FP32.
 // The FP32 factor of the TF32x3 Gram keeps the refinement contraction well
 // below 1 for cond(A) up to ~1e6; the achieved relative residual is returned.
 #include <cuda.h>
@@ -287,43 +288,60 @@ static bool make_map(CUtensorMap *m, const float *ptr, long rows, long cols_pad)
 }
 
 // ---------------------------------------------------------------- FP32 Cholesky
-constexpr int NB32 = 32, TG32 = 64, KC32 = 16;
+constexpr int NB32 = 32, TG32 = 64;
 
+// Diagonal block (kb <= 32) factorised in registers by one warp: lane r holds
+// row r; column j is finished with one square root and broadcast by shuffles.
 __global__ void k_potrf_diag32(float *A, int n, int k0, int kb, int *status) {
     if (status[0] >= 0) return;
-    __shared__ float L[NB32][NB32 + 1];
-    __shared__ int fail;
-    int tx = threadIdx.x, ty = threadIdx.y;
-    if (tx < kb && ty < kb && tx <= ty) L[ty][tx] = A[(size_t)(k0 + ty) * n + k0 + tx];
-    if (tx == 0 && ty == 0) fail = -1;
-    __syncthreads();
-    for (int j = 0; j < kb; j++) {
-        if (tx == 0 && ty == 0) {
-            float d = L[j][j];
-            if (!(d > 0.f)) fail = j;
-            else L[j][j] = sqrtf(d);
+    const int lane = threadIdx.x;
+    float row[NB32];
+#pragma unroll
+    for (int c = 0; c < NB32; c++)
+        row[c] = (lane < kb && c < kb && c <= lane) ? A[(size_t)(k0 + lane) * n + k0 + c] : 0.f;
+    int fail = -1;
+#pragma unroll
+    for (int j = 0; j < NB32; j++) {
+        if (j < kb && fail < 0) {
+            float d = __shfl_sync(0xffffffffu, row[j], j);
+            if (!(d > 0.f)) {
+                fail = j;
+            } else {
+                float ljj = sqrtf(d), inv = 1.f / ljj;
+                if (lane == j) row[j] = ljj;
+                if (lane > j) row[j] *= inv;
+                const float lrj = row[j];
+#pragma unroll
+                for (int c = j + 1; c < NB32; c++) {
+                    float lcj = __shfl_sync(0xffffffffu, row[j], c);
+                    if (lane > j && c <= lane) row[c] -= lrj * lcj;
+                }
+            }
         }
-        __syncthreads();
-        if (fail >= 0) break;
-        if (tx == 0 && ty > j && ty < kb) L[ty][j] = L[ty][j] / L[j][j];
-        __syncthreads();
-        if (ty > j && ty < kb && tx > j && tx <= ty) L[ty][tx] -= L[ty][j] * L[tx][j];
-        __syncthreads();
     }
     if (fail >= 0) {
-        if (tx == 0 && ty == 0) status[0] = k0 + fail;
+        if (lane == 0) status[0] = k0 + fail;
         return;
     }
-    if (tx < kb && ty < kb && tx <= ty) A[(size_t)(k0 + ty) * n + k0 + tx] = L[ty][tx];
+    if (lane < kb) {
+#pragma unroll
+        for (int c = 0; c < NB32; c++)
+            if (c <= lane && c < kb) A[(size_t)(k0 + lane) * n + k0 + c] = row[c];
+    }
 }
 
+// Rows below the block: L[i][k0:k0+kb] = A[i][k0:k0+kb] L_kk^{-T}, one thread
+// per row, reciprocal pivots staged in shared memory.
 __global__ void k_trsm_panel32(float *A, int n, int k0, int kb, int row0, const int *status) {
     if (status[0] >= 0) return;
     __shared__ float L[NB32][NB32 + 1];
+    __shared__ float rinv[NB32];
     for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
         int r = e / kb, c = e % kb;
         L[r][c] = c <= r ? A[(size_t)(k0 + r) * n + k0 + c] : 0.f;
     }
+    __syncthreads();
+    if (threadIdx.x < kb) rinv[threadIdx.x] = 1.f / L[threadIdx.x][threadIdx.x];
     __syncthreads();
     int i = row0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -337,7 +355,7 @@ __global__ void k_trsm_panel32(float *A, int n, int k0, int kb, int row0, const 
             float s = x[j];
 #pragma unroll
             for (int m = 0; m < j; m++) s -= x[m] * L[j][m];
-            x[j] = s / L[j][j];
+            x[j] = s * rinv[j];
         }
     }
 #pragma unroll
@@ -390,117 +408,106 @@ __global__ void __launch_bounds__(256) k_syrk_update32(float *A, int n, int k0, 
         }
 }
 
-// ---------------------------------------------------------------- FP32 triangular inverse
-// X = L^{-1} by block columns from the last to the first (blocked TRTRI):
-//   X_jj = inv(L_jj);  X[j+b:, j:j+b] = -(X[j+b:, j+b:] L[j+b:, j:j+b]) X_jj.
-__global__ void k_trtri_diag32(const float *L, float *X, int n, int k0, int kb) {
-    // one warp: lane c inverts column c of the kb x kb lower block by forward substitution
-    __shared__ float Ls[NB32][NB32 + 1];
-    int lane = threadIdx.x;
-    for (int e = lane; e < kb * kb; e += 32) {
-        int r = e / kb, c = e % kb;
-        Ls[r][c] = c <= r ? L[(size_t)(k0 + r) * n + k0 + c] : 0.f;
+// ---------------------------------------------------------------- block triangular solves
+// The factor is solved with in blocks of BT = 128 rows; the inverses of the
+// diagonal blocks are formed once per factorisation (all blocks in one launch,
+// thread c computes column c by forward substitution), so a block step of a
+// triangular solve is two independent GEMVs instead of a 128-long dependency
+// chain.
+constexpr int BT = 128;
+constexpr int BINV_SMEM = 2 * BT * (BT + 1) * 4;
+
+__global__ void __launch_bounds__(BT) k_block_inverse(const float *__restrict__ L, int n, float *Xd) {
+    extern __shared__ float sh[];
+    float (*Ls)[BT + 1] = (float (*)[BT + 1])sh;
+    float (*Xs)[BT + 1] = (float (*)[BT + 1])(sh + BT * (BT + 1));
+    const int b = blockIdx.x, j0 = b * BT, bs = min(BT, n - j0), c = threadIdx.x;
+    for (int e = c; e < BT * BT; e += BT) {
+        int r = e / BT, q = e % BT;
+        Ls[r][q] = (r < bs && q < bs && q <= r) ? L[(size_t)(j0 + r) * n + j0 + q] : 0.f;
     }
-    __syncwarp();
-    if (lane < kb) {
-        float x[NB32];
-#pragma unroll
-        for (int r = 0; r < NB32; r++) {
-            if (r < kb) {
-                float s = (r == lane) ? 1.f : 0.f;
-#pragma unroll
-                for (int m = 0; m < r; m++) s -= Ls[r][m] * x[m];
-                x[r] = r < lane ? 0.f : s / Ls[r][r];
-            }
+    __syncthreads();
+    for (int r = 0; r < BT; r++) {
+        float x = 0.f;
+        if (c < bs && r < bs && r >= c) {
+            float s = (r == c) ? 1.f : 0.f;
+            for (int m = c; m < r; m++) s -= Ls[r][m] * Xs[m][c];
+            x = s / Ls[r][r];
         }
-#pragma unroll
-        for (int r = 0; r < NB32; r++)
-            if (r < kb) X[(size_t)(k0 + r) * n + k0 + lane] = x[r];
+        Xs[r][c] = x;
     }
+    __syncthreads();
+    float *out = Xd + (size_t)b * BT * BT;
+    for (int e = c; e < BT * BT; e += BT) out[e] = Xs[e / BT][e % BT];
 }
 
-// W[i][c] = sum_{k=k1}^{i} X[i][k] L[k][k0+c] for rows i in [k1, n), then
-// X[i][k0+c] = -sum_m W[i][m] X_jj[m][c].  One block per 64 rows.
-__global__ void __launch_bounds__(256) k_trtri_panel32(const float *L, float *X, int n, int k0, int kb, int k1) {
-    __shared__ float Xs[KC32][TG32 + 1];
-    __shared__ float Ls[KC32][NB32 + 1];
-    __shared__ float Xd[NB32][NB32 + 1];
-    __shared__ float W[TG32][NB32 + 1];
-    const int tid = threadIdx.x;
-    const int r0 = k1 + blockIdx.x * TG32;
-    const int tr = tid >> 2;            // row within the tile (64 rows, 4 threads each)
-    const int tc = (tid & 3) * 8;       // 8 columns per thread
-    float acc[8] = {};
-    int rmax = min(r0 + TG32, n);
-    for (int kk = k1; kk < rmax; kk += KC32) {
-        for (int e = tid; e < TG32 * KC32; e += 256) {
-            int rr = e / KC32, cc = e % KC32;
-            int i = r0 + rr, k = kk + cc;
-            Xs[cc][rr] = (i < n && k <= i && k < n) ? X[(size_t)i * n + k] : 0.f;
-        }
-        for (int e = tid; e < KC32 * NB32; e += 256) {
-            int rr = e / NB32, cc = e % NB32;
-            int k = kk + rr;
-            Ls[rr][cc] = (k < n && cc < kb) ? L[(size_t)k * n + k0 + cc] : 0.f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int c = 0; c < KC32; c++) {
-            float xv = Xs[c][tr];
-#pragma unroll
-            for (int q = 0; q < 8; q++) acc[q] = fmaf(xv, Ls[c][tc + q], acc[q]);
-        }
-        __syncthreads();
+// Forward block step j: z = X_jj rhs_j (every CTA), x_j = z (CTA 0), then
+// rhs_i -= L[i][j0:j0+bs] z for the rows below (one warp per row).
+__global__ void __launch_bounds__(256) k_trsv_fwd_blk(const float *__restrict__ L, const float *__restrict__ Xd,
+                                                     int n, int j, float *rhs, float *x) {
+    __shared__ float z[BT];
+    __shared__ float part[2][BT];
+    const int j0 = j * BT, bs = min(BT, n - j0), t = threadIdx.x;
+    const float *X = Xd + (size_t)j * BT * BT;
+    {
+        int r = t & (BT - 1), h = t >> 7;                 // two threads per row, half the columns each
+        float s = 0.f;
+        if (r < bs)
+            for (int m = h; m <= r; m += 2) s += X[r * BT + m] * rhs[j0 + m];
+        part[h][r] = s;
     }
-    for (int e = tid; e < NB32 * NB32; e += 256) {
-        int r = e / NB32, c = e % NB32;
-        Xd[r][c] = (r < kb && c < kb && c <= r) ? X[(size_t)(k0 + r) * n + k0 + c] : 0.f;
-    }
-#pragma unroll
-    for (int q = 0; q < 8; q++) W[tr][tc + q] = acc[q];
     __syncthreads();
-    int i = r0 + tr;
+    if (t < BT) z[t] = t < bs ? part[0][t] + part[1][t] : 0.f;
+    __syncthreads();
+    if (blockIdx.x == 0 && t < bs) x[j0 + t] = z[t];
+    const int warp = t >> 5, lane = t & 31;
+    const int i = j0 + bs + blockIdx.x * 8 + warp;
     if (i < n) {
+        const float *row = L + (size_t)i * n + j0;
+        float s = 0.f;
+        for (int m = lane; m < bs; m += 32) s += row[m] * z[m];
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            int c = tc + q;
-            if (c < kb) {
-                float s = 0.f;
-                for (int m = c; m < kb; m++) s += W[tr][m] * Xd[m][c];
-                X[(size_t)i * n + k0 + c] = -s;
-            }
-        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) rhs[i] -= s;
     }
 }
 
-// ---------------------------------------------------------------- GEMVs
-// w = X v (X lower triangular FP32, v FP64): warp per row.
-__global__ void k_trmv_lower(const float *__restrict__ X, int n, const double *__restrict__ v, double *w) {
-    int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (row >= n) return;
-    const float *xr = X + (size_t)row * n;
-    double s = 0.0;
-    for (int k = lane; k <= row; k += 32) s += (double)xr[k] * v[k];
-    s = warp_sum(s);
-    if (lane == 0) w[row] = s;
-}
-
-// y = X^T w: y_k = sum_{i >= k} X[i][k] w_i, 32 columns x 8 row groups per block.
-__global__ void k_trmv_lower_t(const float *__restrict__ X, int n, const double *__restrict__ w, double *y,
-                               double *add_to) {
-    __shared__ double a[8][33];
-    int k = blockIdx.x * 32 + threadIdx.x;
-    double s = 0.0;
-    if (k < n)
-        for (int i = k + threadIdx.y; i < n; i += 8) s += (double)X[(size_t)i * n + k] * w[i];
-    a[threadIdx.y][threadIdx.x] = s;
+// Backward block step j (last block first): y_j = X_jj^T rhs_j, then
+// rhs_c -= sum_m L[j0+m][c] y_m for the columns before the block.
+__global__ void __launch_bounds__(256) k_trsv_bwd_blk(const float *__restrict__ L, const float *__restrict__ Xd,
+                                                     int n, int j, float *rhs, float *x) {
+    __shared__ float z[BT];
+    __shared__ float part[2][BT];
+    const int j0 = j * BT, bs = min(BT, n - j0), t = threadIdx.x;
+    const float *X = Xd + (size_t)j * BT * BT;
+    {
+        int c = t & (BT - 1), h = t >> 7;
+        float s = 0.f;
+        if (c < bs)
+            for (int r = c + h; r < bs; r += 2) s += X[r * BT + c] * rhs[j0 + r];
+        part[h][c] = s;
+    }
     __syncthreads();
-    if (threadIdx.y == 0 && k < n) {
-        double S = 0.0;
-        for (int q = 0; q < 8; q++) S += a[q][threadIdx.x];
-        if (add_to) add_to[k] += S;
-        else y[k] = S;
+    if (t < BT) z[t] = t < bs ? part[0][t] + part[1][t] : 0.f;
+    __syncthreads();
+    if (blockIdx.x == 0 && t < bs) x[j0 + t] = z[t];
+    const int col = blockIdx.x * 256 + t;
+    if (col < j0) {
+        float s = 0.f;
+        for (int m = 0; m < bs; m++) s += L[(size_t)(j0 + m) * n + col] * z[m];
+        rhs[col] -= s;
     }
+}
+
+// ---------------------------------------------------------------- refinement helpers
+__global__ void k_d2f(const double *__restrict__ a, float *b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+__global__ void k_add_f2d(double *y, const float *__restrict__ d, int n, int first) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = first ? (double)d[i] : y[i] + (double)d[i];
 }
 
 // u = O_c^T y (FP64, 32 columns x 8 row groups per block)
@@ -519,7 +526,7 @@ __global__ void k_ct_dot(const double *__restrict__ O, int Ns, long P, const dou
     }
 }
 
-// r_i = eps_i - (O_c u)_i / Ns - shift y_i  (warp per row), |r|^2 and |eps|^2 partials
+// r_i = eps_i - (O_c u)_i / Ns - shift y_i  (warp per row)
 __global__ void k_residual(const double *__restrict__ O, int Ns, long P, const double *__restrict__ u,
                            const double *__restrict__ y, const double *__restrict__ eps, double shift,
                            double *r) {
@@ -557,42 +564,46 @@ __global__ void k_norms(const double *__restrict__ r, const double *__restrict__
 
 // ---------------------------------------------------------------- driver
 struct MixedWs {
-    DevBuf<float> hi, lo, T, X;
-    DevBuf<double> w, u, r, nrm;
+    DevBuf<float> hi, lo, T, Xd, rf, zf, xf;
+    DevBuf<double> u, r, nrm;
     DevBuf<int> status;
     int ns_pad = 0;
     long p_pad = 0;
 };
 static MixedWs g_mx;
 
-bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
-                       int passes, double *y, double *out_resid, int *out_fail) {
-    cudaStream_t st = ctx().stream;
-    MixedWs &w = g_mx;
-    const int ns_pad = (Ns + TC_M - 1) / TC_M * TC_M;
-    const long p_pad = (P + TC_K - 1) / TC_K * TC_K;
-    if (ns_pad != w.ns_pad || p_pad != w.p_pad) {
-        if (!w.hi.ensure((size_t)ns_pad * p_pad) || !w.lo.ensure((size_t)ns_pad * p_pad)) return false;
-        if (!NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ns_pad * p_pad, st)) ||
-            !NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ns_pad * p_pad, st)))
-            return false;
-        w.ns_pad = ns_pad;
-        w.p_pad = p_pad;
+// Two block triangular solves: xf = (L L^T)^{-1} rf (rf is consumed).
+static void factor_solve(MixedWs &w, int n, cudaStream_t st) {
+    const int nb = (n + BT - 1) / BT;
+    for (int j = 0; j < nb; j++) {
+        int below = n - (j * BT + min(BT, n - j * BT));
+        NQS_LAUNCH("trsv32_fwd");
+        k_trsv_fwd_blk<<<below > 0 ? (below + 7) / 8 : 1, 256, 0, st>>>(w.T.p, w.Xd.p, n, j, w.rf.p, w.zf.p);
     }
-    if (!w.T.ensure((size_t)Ns * Ns) || !w.X.ensure((size_t)Ns * Ns) || !w.w.ensure(Ns) || !w.u.ensure(P) ||
-        !w.r.ensure(Ns) || !w.nrm.ensure(2) || !w.status.ensure(2))
-        return false;
-    NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, 2 * sizeof(int), st));
+    for (int j = nb - 1; j >= 0; j--) {
+        int before = j * BT;
+        NQS_LAUNCH("trsv32_bwd");
+        k_trsv_bwd_blk<<<before > 0 ? (before + 255) / 256 : 1, 256, 0, st>>>(w.T.p, w.Xd.p, n, j, w.zf.p,
+                                                                               w.xf.p);
+    }
+}
+
+// Enqueue the whole mixed solve with no host synchronisation: split, tensor-core
+// Gram, factor, block inverses, refinement sweeps and the final norms.  Kernels
+// after the factor run unconditionally; a broken factor is reported through
+// status[0] and the caller discards the result.
+static void enqueue_mixed(double *O, const double *gm, const double *eps, int Ns, long P, double shift,
+                          int sweeps, int passes, double *y, const CUtensorMap &mh, const CUtensorMap &ml,
+                          int *err, cudaStream_t st) {
+    MixedWs &w = g_mx;
+    const long p_pad = w.p_pad;
+    const int nb = (Ns + BT - 1) / BT;
+    cudaMemsetAsync(w.status.p, 0xff, 2 * sizeof(int), st);
+    cudaMemsetAsync(err, 0, sizeof(int), st);
     {
         NQS_LAUNCH("center_split");
         k_center_split<<<ctx().sm_count * 8, 256, 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, p_pad);
     }
-    // tensor-core Gram
-    CUtensorMap mh, ml;
-    if (!make_map(&mh, w.hi.p, ns_pad, p_pad) || !make_map(&ml, w.lo.p, ns_pad, p_pad)) return false;
-    static DevBuf<int> err;
-    if (!err.ensure(1)) return false;
-    NQS_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
     GramTcArgs g;
     g.kt_per_seg = (int)(p_pad / TC_K);
     g.nseg = passes >= 3 ? 3 : 1;
@@ -600,32 +611,23 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
     g.shift = (float)shift;
     g.C = w.T.p;
     g.n = Ns;
-    g.err = err.p;
-    int nt = ns_pad / TC_M;
+    g.err = err;
+    int nt = w.ns_pad / TC_M;
     {
-        static bool attr = false;
-        if (!attr) {
-            if (!NQS_CUDA(cudaFuncSetAttribute(k_gram_tf32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               TC_SMEM)))
-                return false;
-            attr = true;
-        }
         NQS_LAUNCH("gram_tc");
         k_gram_tf32_tc<<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(mh, ml, g);
     }
-    if (!NQS_CUDA(cudaGetLastError())) return false;
-    // FP32 Cholesky
     for (int k0 = 0; k0 < Ns; k0 += NB32) {
         int kb = Ns - k0 < NB32 ? Ns - k0 : NB32;
         {
             NQS_LAUNCH("chol32_diag");
-            k_potrf_diag32<<<1, dim3(32, 32), 0, st>>>(w.T.p, Ns, k0, kb, w.status.p);
+            k_potrf_diag32<<<1, 32, 0, st>>>(w.T.p, Ns, k0, kb, w.status.p);
         }
         int k1 = k0 + kb, rest = Ns - k1;
         if (rest <= 0) break;
         {
             NQS_LAUNCH("chol32_panel");
-            k_trsm_panel32<<<(rest + 127) / 128, 128, 0, st>>>(w.T.p, Ns, k0, kb, k1, w.status.p);
+            k_trsm_panel32<<<(rest + 63) / 64, 64, 0, st>>>(w.T.p, Ns, k0, kb, k1, w.status.p);
         }
         int ntt = (rest + TG32 - 1) / TG32;
         {
@@ -633,61 +635,136 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
             k_syrk_update32<<<ntt * (ntt + 1) / 2, 256, 0, st>>>(w.T.p, Ns, k0, kb, k1, w.status.p);
         }
     }
-    int fail = -1, ierr = 0;
-    if (!NQS_CUDA(cudaMemcpyAsync(&fail, w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
-        !NQS_CUDA(cudaMemcpyAsync(&ierr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
-        !NQS_CUDA(cudaStreamSynchronize(st)))
-        return false;
-    if (ierr) {
-        set_error("tensor-core Gram timed out waiting on its pipeline");
-        return false;
-    }
-    *out_fail = fail;
-    if (fail >= 0) return true;
-    // X = L^{-1}
-    for (int k0 = ((Ns - 1) / NB32) * NB32; k0 >= 0; k0 -= NB32) {
-        int kb = Ns - k0 < NB32 ? Ns - k0 : NB32;
-        {
-            NQS_LAUNCH("trtri32_diag");
-            k_trtri_diag32<<<1, 32, 0, st>>>(w.T.p, w.X.p, Ns, k0, kb);
-        }
-        int k1 = k0 + kb;
-        if (k1 < Ns) {
-            NQS_LAUNCH("trtri32_panel");
-            k_trtri_panel32<<<(Ns - k1 + TG32 - 1) / TG32, 256, 0, st>>>(w.T.p, w.X.p, Ns, k0, kb, k1);
-        }
-    }
-    // y = X^T X eps, then refinement sweeps against the FP64 operator
-    dim3 cb(32, 8);
-    unsigned gridN = (unsigned)((Ns + 31) / 32), gridP = (unsigned)((P + 31) / 32);
-    unsigned rowsN = (unsigned)((Ns * 32 + 255) / 256);
     {
-        NQS_LAUNCH("solve_gemv");
-        k_trmv_lower<<<rowsN, 256, 0, st>>>(w.X.p, Ns, eps, w.w.p);
-        k_trmv_lower_t<<<gridN, cb, 0, st>>>(w.X.p, Ns, w.w.p, y, nullptr);
+        NQS_LAUNCH("block_inverse");
+        k_block_inverse<<<nb, BT, BINV_SMEM, st>>>(w.T.p, Ns, w.Xd.p);
     }
-    for (int s = 0; s < sweeps; s++) {
+    // refinement: y = S eps; y += S (eps - A y) per sweep, S = (L L^T)^{-1} in FP32
+    dim3 cb(32, 8);
+    unsigned gridP = (unsigned)((P + 31) / 32), rowsN = (unsigned)((Ns * 32 + 255) / 256);
+    unsigned vN = (unsigned)((Ns + 255) / 256);
+    for (int s = 0; s <= sweeps; s++) {
+        {
+            NQS_LAUNCH("refine_vec");
+            k_d2f<<<vN, 256, 0, st>>>(s == 0 ? eps : w.r.p, w.rf.p, Ns);
+        }
+        factor_solve(w, Ns, st);
+        {
+            NQS_LAUNCH("refine_vec");
+            k_add_f2d<<<vN, 256, 0, st>>>(y, w.xf.p, Ns, s == 0);
+        }
         {
             NQS_LAUNCH("refine_residual");
             k_ct_dot<<<gridP, cb, 0, st>>>(O, Ns, P, y, w.u.p);
-            k_residual<<<rowsN, 256, 0, st>>>(O, Ns, P, w.u.p, y, eps, shift, w.r.p);
         }
         {
-            NQS_LAUNCH("solve_gemv");
-            k_trmv_lower<<<rowsN, 256, 0, st>>>(w.X.p, Ns, w.r.p, w.w.p);
-            k_trmv_lower_t<<<gridN, cb, 0, st>>>(w.X.p, Ns, w.w.p, nullptr, y);
+            NQS_LAUNCH("refine_residual");
+            k_residual<<<rowsN, 256, 0, st>>>(O, Ns, P, w.u.p, y, eps, shift, w.r.p);
         }
     }
     {
         NQS_LAUNCH("refine_residual");
-        k_ct_dot<<<gridP, cb, 0, st>>>(O, Ns, P, y, w.u.p);
-        k_residual<<<rowsN, 256, 0, st>>>(O, Ns, P, w.u.p, y, eps, shift, w.r.p);
         k_norms<<<1, 1024, 0, st>>>(w.r.p, eps, Ns, w.nrm.p);
     }
-    double h[2];
-    if (!NQS_CUDA(cudaMemcpyAsync(h, w.nrm.p, sizeof(h), cudaMemcpyDeviceToHost, st)) ||
+}
+
+// The launch sequence above is fixed for given buffers and sizes: it is
+// captured once into a CUDA graph and replayed every step (one launch instead
+// of ~600).  Per-kernel profiling runs the sequence uncaptured.
+struct MixedGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void *key[5] = {};
+    int Ns = 0, sweeps = -1, passes = -1;
+    long P = 0;
+    double shift = 0.0;
+    long kernels = 0;
+};
+static MixedGraph g_mgraph;
+
+bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
+                       int passes, double *y, double *out_resid, int *out_fail) {
+    Context &c = ctx();
+    cudaStream_t st = c.stream;
+    MixedWs &w = g_mx;
+    const int ns_pad = (Ns + TC_M - 1) / TC_M * TC_M;
+    const long p_pad = (P + TC_K - 1) / TC_K * TC_K;
+    bool moved = false;
+    if (ns_pad != w.ns_pad || p_pad != w.p_pad) {
+        if (!w.hi.ensure((size_t)ns_pad * p_pad) || !w.lo.ensure((size_t)ns_pad * p_pad)) return false;
+        if (!NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ns_pad * p_pad, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ns_pad * p_pad, st)))
+            return false;
+        w.ns_pad = ns_pad;
+        w.p_pad = p_pad;
+        moved = true;
+    }
+    const int nb = (Ns + BT - 1) / BT;
+    const void *before[8] = {w.T.p, w.Xd.p, w.rf.p, w.zf.p, w.xf.p, w.u.p, w.r.p, w.nrm.p};
+    if (!w.T.ensure((size_t)Ns * Ns) || !w.Xd.ensure((size_t)nb * BT * BT) || !w.rf.ensure(Ns) ||
+        !w.zf.ensure(Ns) || !w.xf.ensure(Ns) || !w.u.ensure(P) || !w.r.ensure(Ns) || !w.nrm.ensure(2) ||
+        !w.status.ensure(2))
+        return false;
+    const void *after[8] = {w.T.p, w.Xd.p, w.rf.p, w.zf.p, w.xf.p, w.u.p, w.r.p, w.nrm.p};
+    for (int i = 0; i < 8; i++) moved |= before[i] != after[i];
+    static DevBuf<int> err;
+    if (!err.ensure(1)) return false;
+    static bool attr = false;
+    if (!attr) {
+        if (!NQS_CUDA(cudaFuncSetAttribute(k_gram_tf32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM)) ||
+            !NQS_CUDA(cudaFuncSetAttribute(k_block_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           BINV_SMEM)))
+            return false;
+        attr = true;
+    }
+    CUtensorMap mh, ml;
+    if (!make_map(&mh, w.hi.p, ns_pad, p_pad) || !make_map(&ml, w.lo.p, ns_pad, p_pad)) return false;
+
+    if (c.profiling) {
+        enqueue_mixed(O, gm, eps, Ns, P, shift, sweeps, passes, y, mh, ml, err.p, st);
+    } else {
+        MixedGraph &G = g_mgraph;
+        const void *key[5] = {O, gm, eps, y, w.hi.p};
+        bool same = G.exec && !moved && G.Ns == Ns && G.P == P && G.sweeps == sweeps && G.passes == passes &&
+                    G.shift == shift;
+        for (int i = 0; i < 5 && same; i++) same = G.key[i] == key[i];
+        if (!same) {
+            if (G.exec) cudaGraphExecDestroy(G.exec);
+            G.exec = nullptr;
+            cudaGraph_t graph;
+            long l0 = c.launches;
+            if (!NQS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal))) return false;
+            enqueue_mixed(O, gm, eps, Ns, P, shift, sweeps, passes, y, mh, ml, err.p, st);
+            if (!NQS_CUDA(cudaStreamEndCapture(st, &graph))) return false;
+            G.kernels = c.launches - l0;
+            c.launches = l0;
+            bool ok = NQS_CUDA(cudaGraphInstantiate(&G.exec, graph, 0));
+            cudaGraphDestroy(graph);
+            if (!ok) {
+                G.exec = nullptr;
+                return false;
+            }
+            for (int i = 0; i < 5; i++) G.key[i] = key[i];
+            G.Ns = Ns;
+            G.P = P;
+            G.sweeps = sweeps;
+            G.passes = passes;
+            G.shift = shift;
+        }
+        if (!NQS_CUDA(cudaGraphLaunch(G.exec, st))) return false;
+        c.launches += G.kernels;
+    }
+    int hs[2] = {-1, 0};
+    double h[2] = {0.0, 0.0};
+    if (!NQS_CUDA(cudaMemcpyAsync(&hs[0], w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaMemcpyAsync(&hs[1], err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaMemcpyAsync(h, w.nrm.p, sizeof(h), cudaMemcpyDeviceToHost, st)) ||
         !NQS_CUDA(cudaStreamSynchronize(st)))
         return false;
+    if (hs[1]) {
+        set_error("tensor-core Gram timed out waiting on its pipeline");
+        return false;
+    }
+    *out_fail = hs[0];
     *out_resid = h[1] > 0 ? sqrt(h[0] / h[1]) : 0.0;
     return NQS_CUDA(cudaGetLastError());
 }

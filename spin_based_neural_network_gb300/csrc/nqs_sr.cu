@@ -50,22 +50,26 @@ __global__ void k_energy_stats(const double *__restrict__ E, int n, double *scal
     }
     ss[t] = s; sc[t] = c; qs[t] = q; qc[t] = qcc;
     __syncthreads();
+    // pairwise tree over the (sum, compensation) pairs: each merge is an exact
+    // TwoSum of the sums plus the two compensations
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (t < o) {
+            double a = ss[t], b = ss[t + o], tt = a + b, bb = tt - a;
+            double e = (a - (tt - bb)) + (b - bb);
+            ss[t] = tt;
+            sc[t] = sc[t] + sc[t + o] + e;
+            double a2 = qs[t], b2 = qs[t + o], t2 = a2 + b2, b3 = t2 - a2;
+            double e2 = (a2 - (t2 - b3)) + (b2 - b3);
+            qs[t] = t2;
+            qc[t] = qc[t] + qc[t + o] + e2;
+        }
+        __syncthreads();
+    }
     __shared__ double mean;
     if (t == 0) {
-        double S = 0.0, Cc = 0.0, Q = 0.0, QC = 0.0;
-        for (int k = 0; k < (int)blockDim.x; k++) {
-            double x = ss[k], tt = S + x;
-            Cc += fabs(S) >= fabs(x) ? (S - tt) + x : (x - tt) + S;
-            S = tt;
-            Cc += sc[k];
-            double x2 = qs[k], t2 = Q + x2;
-            QC += fabs(Q) >= fabs(x2) ? (Q - t2) + x2 : (x2 - t2) + Q;
-            Q = t2;
-            QC += qc[k];
-        }
-        mean = (S + Cc) / (double)n;
+        mean = (ss[0] + sc[0]) / (double)n;
         scal[S_EMEAN] = mean;
-        scal[S_ESQ] = (Q + QC) / (double)n;
+        scal[S_ESQ] = (qs[0] + qc[0]) / (double)n;
     }
     __syncthreads();
     if (eps)
