@@ -383,8 +383,43 @@ def run_gpu(args):
     return 0
 
 
+def run_gram_only(args):
+    """The tensor-core Gram alone (nqs_gpu_gram_tc, 3-pass TF32 split) on a
+    seeded Jacobian-shaped matrix, for profiling and for its own roofline:
+    prints achieved TFLOP/s over `--steps` launches (CUDA events)."""
+    import ctypes as C
+    import numpy as np
+    import spin_based_neural_network_gb300 as pkg
+    pkg.lib()
+    from spin_based_neural_network_gb300 import nqs
+    Ns, P = args.gram_ns, args.gram_np
+    O = np.random.default_rng(SEED).normal(size=(Ns, P))
+    T = np.zeros((Ns, Ns), dtype=np.float32)
+    L = nqs.lib()
+    run = lambda: L.nqs_gpu_gram_tc(O.ctypes.data_as(nqs.DP), Ns, P, 3, 1.0 / Ns,
+                                    T.ctypes.data_as(C.POINTER(C.c_float)))
+    for _ in range(max(args.warmup, 1)):
+        assert run() == 0, nqs.last_error()
+    nqs.profile_reset()
+    nqs.profile(True)
+    for _ in range(args.steps):
+        assert run() == 0, nqs.last_error()
+    nqs.profile(False)
+    cnt, ms = nqs.profile_read()["gram_tc"]
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        peak = json.load(f)["bf16_tflops"]
+    flops = 3.0 * Ns * (Ns + 1) * P
+    tf = flops / (ms / cnt / 1e3) / 1e12
+    print(json.dumps({"kernel": "gram_tc", "ns": Ns, "np": P, "launches": cnt, "avg_ms": ms / cnt,
+                      "tflops": tf, "frac_of_bf16_measured": tf / peak}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--gram-only", action="store_true", help="time / profile the tensor-core Gram alone")
+    ap.add_argument("--gram-ns", type=int, default=8192)
+    ap.add_argument("--gram-np", type=int, default=10728)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -393,6 +428,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.gram_only:
+        return run_gram_only(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
