@@ -269,6 +269,11 @@ def run_gpu(args):
     e1 = L.nqs_gpu_event_record()
     dev_ms = L.nqs_gpu_event_elapsed_ms(e0, e1)
     launches = nqs.launch_count() - n0
+    phases = None
+    if prec == abi.PREC_MIXED:
+        ph = nqs.last_step_stats().phase_us
+        phases = dict(zip(("diag_blocks", "panels", "trailing", "fwd_solves", "bwd_solves", "residuals",
+                           "total"), [round(ph[i], 1) for i in range(7)]))
     L.nqs_gpu_event_destroy(e0)
     L.nqs_gpu_event_destroy(e1)
     nqs.lib().nqs_gpu_synchronize()
@@ -369,7 +374,7 @@ def run_gpu(args):
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * P,
                     "d2h_bytes_per_step": 8 * P + 16 * 8},
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
-            "delta_theta_vs_fp64": delta_err, "plain_fp64": plain,
+            "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))

@@ -25,6 +25,10 @@ extern "C" {
  * w_im[width], c_re, c_im.  Selected through nqs_config_t.ansatz. */
 #define NQS_GPU_ANSATZ_MLP 100
 
+#define NQS_GPU_SPACE_AUTO       0
+#define NQS_GPU_SPACE_SAMPLES    1
+#define NQS_GPU_SPACE_PARAMETERS 2
+
 typedef enum {
     NQS_GPU_RNG_XORSHIFT_COMPAT = 0,  /* upstream single chain, same sequence */
     NQS_GPU_RNG_PHILOX          = 1   /* num_chains chains, Philox4x32-10 */
@@ -49,7 +53,9 @@ typedef struct {
     int precision;       /* nqs_gpu_precision_t for MinSR */
     int refine_sweeps;   /* MIXED: FP64 iterative-refinement sweeps */
     int gram_passes;     /* MIXED: 1 = single TF32 pass, 3 = split (hi/lo) passes */
-    int chol_fp32;       /* MIXED: 1 = FP32 Cholesky factor, 0 = FP64 */
+    int mixed_space;     /* MIXED: system solved, 0 = the smaller one, 1 = sample space
+                          * (N_s x N_s, O O^T), 2 = parameter space (N_p x N_p, O^T O);
+                          * both give the same delta (push-through identity) */
     int lattice_x;       /* exchange moves: lattice whose nearest-neighbour bonds */
     int lattice_y;       /*   are swapped (0 x 0 = periodic ring of N sites)      */
     int lattice_kagome;  /*   1: kagome cells, bonds of kagome_pbc = 1          */
@@ -158,6 +164,12 @@ typedef struct {
     double delta_rel_err;    /* MIXED with mixed_check: ||d - d_fp64|| / ||d_fp64|| */
     int    mixed_fallback;   /* 1 if the FP32 factor failed and FP64 solved the step */
     int    pad_;
+    /* MIXED: microseconds spent in the phases of the cooperative factor /
+     * inverse / refinement kernel: [0] diagonal blocks, [1] panels, [2] trailing
+     * updates, [3] triangular inverse, [4] triangular solves, [5] right-hand
+     * side and FP64 residuals, [6] total; [7] the part of [0] spent by the
+     * owning CTAs on factoring and inverting the diagonal blocks */
+    double phase_us[8];
 } nqs_gpu_step_stats_t;
 int nqs_gpu_last_step_stats(nqs_gpu_step_stats_t *out);
 

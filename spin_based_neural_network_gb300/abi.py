@@ -113,6 +113,9 @@ RNG_XORSHIFT_COMPAT = 0      # upstream single chain, bit-identical sequence
 RNG_PHILOX = 1               # many chains, counter-based Philox4x32-10
 PREC_FP64 = 0                # plain FP64 path
 PREC_MIXED = 1               # tensor-core Gram + FP64 iterative refinement
+SPACE_AUTO = 0               # mixed MinSR: solve the smaller of the two systems
+SPACE_SAMPLES = 1            # N_s x N_s (O O^T)
+SPACE_PARAMETERS = 2         # N_p x N_p (O^T O)
 
 
 class GpuOptions(C.Structure):
@@ -126,7 +129,7 @@ class GpuOptions(C.Structure):
         ("precision", C.c_int),
         ("refine_sweeps", C.c_int),
         ("gram_passes", C.c_int),
-        ("chol_fp32", C.c_int),
+        ("mixed_space", C.c_int),
         ("lattice_x", C.c_int),
         ("lattice_y", C.c_int),
         ("lattice_kagome", C.c_int),

@@ -36,7 +36,7 @@ static nqs_gpu_options_t default_options() {
     o.precision = NQS_GPU_PREC_FP64;
     o.refine_sweeps = 2;
     o.gram_passes = 3;
-    o.chol_fp32 = 1;
+    o.mixed_space = NQS_GPU_SPACE_AUTO;
     return o;
 }
 
@@ -177,7 +177,10 @@ int nqs_gpu_set_options(const nqs_gpu_options_t *o) {
     if (!ensure_context()) return -1;
     if (o->num_chains <= 0 || (o->rng != NQS_GPU_RNG_XORSHIFT_COMPAT && o->rng != NQS_GPU_RNG_PHILOX) ||
         (o->move != NQS_GPU_MOVE_SINGLE_FLIP && o->move != NQS_GPU_MOVE_EXCHANGE) ||
-        (o->move == NQS_GPU_MOVE_EXCHANGE && o->rng != NQS_GPU_RNG_PHILOX)) {
+        (o->move == NQS_GPU_MOVE_EXCHANGE && o->rng != NQS_GPU_RNG_PHILOX) ||
+        (o->precision != NQS_GPU_PREC_FP64 && o->precision != NQS_GPU_PREC_MIXED) || o->refine_sweeps < 0 ||
+        (o->gram_passes != 1 && o->gram_passes != 3) || o->mixed_space < NQS_GPU_SPACE_AUTO ||
+        o->mixed_space > NQS_GPU_SPACE_PARAMETERS) {
         set_error("invalid nqs_gpu_options_t");
         return -1;
     }

@@ -168,10 +168,14 @@ bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, 
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
 
-// Mixed-precision MinSR solve (nqs_mixed.cu): centres O in place, writes y with
-// (T + shift I) y = eps; *out_fail >= 0 when the FP32 factor broke down.
+// Mixed-precision MinSR solve (nqs_mixed.cu): centres O in place and solves in
+// sample space, (O_c O_c^T / N_s + shift I) y = eps (writes y), or in parameter
+// space, (O_c^T O_c / N_s + shift I) delta = O_c^T eps / N_s (writes delta and
+// sets *param_space); space_opt 0 picks the smaller system, 1 samples, 2
+// parameters.  *out_fail >= 0 when the FP32 factor broke down.
 bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
-                       int passes, double *y, double *out_resid, int *out_fail);
+                       int passes, int space_opt, double *y, double *delta, bool *param_space, double *out_resid,
+                       int *out_fail);
 
 // thread-local statistics of the last SR step
 nqs_gpu_step_stats_t &step_stats();

@@ -7,15 +7,16 @@
 //      staged by TMA (cp.async.bulk.tensor, 128-byte swizzle) in a 3-stage
 //      mbarrier ring, FP32 accumulator in TMEM read back with tcgen05.ld;
 //      only the lower-triangular 128 x 128 tiles are computed;
-//   3. FP32 blocked Cholesky T = L L^T (32-wide panels: warp-register diagonal
-//      factor, panel solve, trailing SYRK) and the inverses of its 128 x 128
-//      diagonal blocks, so a triangular solve is 2 N_s / 128 block steps of two
-//      parallel GEMVs each;
+//   3. FP32 blocked Cholesky T = L L^T with 128-wide panels and the explicit
+//      inverse L^{-1}, so each triangular solve is one parallel GEMV;
 //   4. iterative refinement in FP64 against the exact operator
 //      A y = O_c (O_c^T y) / N_s + shift y (two FP64 passes over O_c):
 //      y <- y + (L L^T)^{-1} (eps - A y), the correction solved in FP32.
-// The FP32 factor of the TF32x3 Gram keeps the refinement contraction well
-// below 1 for cond(A) up to ~1e6; the achieved relative residual is returned.
+// When N_p < N_s the same update is solved in parameter space instead (the
+// push-through identity O^T (O O^T / N_s + s)^{-1} = (O^T O / N_s + s)^{-1} O^T):
+// the Gram is O_c^T O_c / N_s (N_p x N_p), the right-hand side O_c^T eps / N_s,
+// and the refinement operator A d = O_c^T (O_c d) / N_s + shift d.
+// The achieved relative residual is returned.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <math.h>
@@ -287,394 +288,834 @@ static bool make_map(CUtensorMap *m, const float *ptr, long rows, long cols_pad)
     return true;
 }
 
-// ---------------------------------------------------------------- FP32 Cholesky
-constexpr int NB32 = 32, TG32 = 64;
+// ---------------------------------------------------------------- FP32 factor, inverse and refinement
+// One cooperative launch (one CTA per SM, all co-resident) runs everything
+// after the Gram:
+//   factor   for each 128-column block k: the owner CTA factors the diagonal
+//            block in shared memory and inverts it (X_kk = L_kk^{-1}); every CTA
+//            forms 64 x 64 tiles of the panel U_k = X_kk A_k^T (stored as L^T in
+//            the unused upper triangle of T) and of the trailing update
+//            A -= U_k^T U_k (lower triangle);
+//   inverse  L^{-1} by recursive doubling over the 128-blocks: halves of h
+//            blocks are joined as [X11 0; -X22 L21 X11  X22], two GEMM phases
+//            per level, log2(n / 128) levels; L^{-1} is kept row-major (Li) and
+//            transposed (LiT) so both triangular solves are row GEMVs;
+//   refine   sweeps of y <- y + L^{-T} L^{-1} r with the residual r formed in
+//            FP64 against the exact operator (two passes over O_c).
+// Phases are separated by a grid barrier on a generation word with a bounded
+// spin budget; on timeout it raises *err and every CTA leaves at its next
+// barrier.  Data written by other CTAs is read with L1-bypassing loads.
+constexpr int BT = 128;                              // diagonal block
+constexpr int PS_THREADS = 256;
+constexpr int PS_SMEM = 2 * BT * (BT + 1) * 4;       // two 128 x 129 float tiles
+constexpr int GT = 64, GKC = 32;                     // GEMM tile and K chunk
+constexpr int RCH = 64;                              // rows per partial column sum
 
-// Diagonal block (kb <= 32) factorised in registers by one warp: lane r holds
-// row r; column j is finished with one square root and broadcast by shuffles.
-__global__ void k_potrf_diag32(float *A, int n, int k0, int kb, int *status) {
-    if (status[0] >= 0) return;
-    const int lane = threadIdx.x;
-    float row[NB32];
-#pragma unroll
-    for (int c = 0; c < NB32; c++)
-        row[c] = (lane < kb && c < kb && c <= lane) ? A[(size_t)(k0 + lane) * n + k0 + c] : 0.f;
-    int fail = -1;
-#pragma unroll
-    for (int j = 0; j < NB32; j++) {
-        if (j < kb && fail < 0) {
-            float d = __shfl_sync(0xffffffffu, row[j], j);
-            if (!(d > 0.f)) {
-                fail = j;
-            } else {
-                float ljj = sqrtf(d), inv = 1.f / ljj;
-                if (lane == j) row[j] = ljj;
-                if (lane > j) row[j] *= inv;
-                const float lrj = row[j];
-#pragma unroll
-                for (int c = j + 1; c < NB32; c++) {
-                    float lcj = __shfl_sync(0xffffffffu, row[j], c);
-                    if (lane > j && c <= lane) row[c] -= lrj * lcj;
+struct TileSmem {
+    float a[GKC][GT + 1];
+    float b[GKC][GT + 1];
+};
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = bar + 1;
+        const unsigned g0 = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            bar[0] = 0;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            uint32_t it = 0;
+            while (*gen == g0) {
+                if (*((volatile int *)err)) break;
+                if (++it > (1u << 24)) {
+                    atomicExch(err, 2);
+                    break;
                 }
+                if (it > 64) __nanosleep(32);
             }
         }
+        __threadfence();
     }
-    if (fail >= 0) {
-        if (lane == 0) status[0] = k0 + fail;
-        return;
-    }
-    if (lane < kb) {
+    __syncthreads();
+    return *((volatile int *)err) == 0;
+}
+
+// Factor the 128 x 128 block in S (rows >= bs padded with the identity) in four
+// 32-column sub-panels and leave the inverses of the four diagonal 32 x 32
+// factors in the matching diagonal blocks of X.  The 32 x 32 factor and its
+// inverse run in one warp's registers; the panel below it and the update of the
+// rest of the block use the whole CTA.  Returns the first failing column or -1.
+__device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s_flag, float *tmp) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int e = tid; e < BT * BT; e += PS_THREADS) X[e / BT][e % BT] = 0.f;
+    for (int sb = 0; sb < 4; sb++) {
+        const int c0 = sb * 32;
+        if (warp == 0) {
+            // right-looking, lane = row in registers; the scaled column j is
+            // broadcast through shared memory (a shuffle per entry is ~3x slower)
+            float row[32];
 #pragma unroll
-        for (int c = 0; c < NB32; c++)
-            if (c <= lane && c < kb) A[(size_t)(k0 + lane) * n + k0 + c] = row[c];
+            for (int c = 0; c < 32; c++) row[c] = (c <= lane) ? S[c0 + lane][c0 + c] : 0.f;
+            float *colj = tmp;                                 // 32 floats
+            int fail = -1;
+            float dinv = 0.f;                                  // lane j keeps 1 / L_jj
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                if (fail < 0) {
+                    const float d = __shfl_sync(0xffffffffu, row[j], j);
+                    if (!(d > 0.f)) {
+                        fail = j;
+                    } else {
+                        const float inv = rsqrtf(d);
+                        row[j] = lane == j ? d * inv : row[j] * inv;
+                        if (lane == j) dinv = inv;
+                        colj[lane] = row[j];
+                        __syncwarp();
+                        const float lrj = row[j];
+#pragma unroll
+                        for (int c = j + 1; c < 32; c++)
+                            if (c <= lane) row[c] -= lrj * colj[c];
+                        __syncwarp();
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 32; c++)
+                if (c <= lane) S[c0 + lane][c0 + c] = row[c];
+            if (lane == 0) *s_flag = (fail >= 0 && c0 + fail < bs) ? c0 + fail : -1;
+            __syncwarp();
+            if (fail < 0) {
+                // X_s = L_s^{-1} by forward substitution, lane = column
+                float x[32];
+#pragma unroll
+                for (int rr = 0; rr < 32; rr++) {
+                    const float di = __shfl_sync(0xffffffffu, dinv, rr);
+                    float s0 = (rr == lane) ? 1.f : 0.f, s1 = 0.f;
+#pragma unroll
+                    for (int m = 0; m < rr; m += 2) {
+                        s0 -= S[c0 + rr][c0 + m] * x[m];
+                        if (m + 1 < rr) s1 -= S[c0 + rr][c0 + m + 1] * x[m + 1];
+                    }
+                    x[rr] = rr < lane ? 0.f : (s0 + s1) * di;
+                }
+#pragma unroll
+                for (int rr = 0; rr < 32; rr++) X[c0 + rr][c0 + lane] = x[rr];
+            }
+        }
+        __syncthreads();
+        if (*s_flag >= 0) return *s_flag;
+        const int t0 = c0 + 32, nr = BT - t0;
+        if (nr == 0) break;
+        // rows below the sub-panel: L[r][c0+j] = sum_m A[r][c0+m] X_s[j][m]
+        for (int w = tid; w < nr * 8; w += PS_THREADS) {
+            const int r = t0 + w / 8, j0 = (w % 8) * 4;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll 8
+            for (int m = 0; m < 32; m++) {
+                float av = S[r][c0 + m];
+                a0 += av * X[c0 + j0][c0 + m];
+                a1 += av * X[c0 + j0 + 1][c0 + m];
+                a2 += av * X[c0 + j0 + 2][c0 + m];
+                a3 += av * X[c0 + j0 + 3][c0 + m];
+            }
+            tmp[w * 4 + 0] = a0;
+            tmp[w * 4 + 1] = a1;
+            tmp[w * 4 + 2] = a2;
+            tmp[w * 4 + 3] = a3;
+        }
+        __syncthreads();
+        for (int w = tid; w < nr * 8; w += PS_THREADS) {
+            const int r = t0 + w / 8, j0 = (w % 8) * 4;
+#pragma unroll
+            for (int q = 0; q < 4; q++) S[r][c0 + j0 + q] = tmp[w * 4 + q];
+        }
+        __syncthreads();
+        // rest of the block: S[i][j] -= sum_m L[i][c0+m] L[j][c0+m], 4 x 4 outputs
+        // per thread on rows / columns strided by nr / 4
+        const int q = nr / 4;
+        for (int e = tid; e < q * q; e += PS_THREADS) {
+            const int ti = e / q, tj = e % q;
+            float acc[4][4] = {};
+#pragma unroll 4
+            for (int m = 0; m < 32; m++) {
+                float av[4], bv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    av[u] = S[t0 + ti + q * u][c0 + m];
+                    bv[u] = S[t0 + tj + q * u][c0 + m];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int i = t0 + ti + q * u, j = t0 + tj + q * v;
+                    if (j <= i) S[i][j] -= acc[u][v];
+                }
+        }
+        __syncthreads();
+    }
+    return -1;
+}
+
+// Off-diagonal 32-blocks of X = L^{-1} inside the 128-block (the diagonal
+// 32-blocks are already in X): for d = 1..3, X_ba = -X_bb (sum_{m=a}^{b-1}
+// L_bm X_ma), b = a + d, all pairs of one block diagonal computed by the CTA,
+// 4 x 4 outputs per thread (rows and columns strided by 8).
+__device__ void block_inv128(float (*S)[BT + 1], float (*X)[BT + 1], float *tmp) {
+    const int tid = threadIdx.x, r8 = (tid >> 3) & 7, c8 = tid & 7;
+    for (int d = 1; d < 4; d++) {
+        const int pairs = 4 - d;
+        for (int w = tid; w < pairs * 64; w += PS_THREADS) {
+            const int pa = w >> 6, ob = (pa + d) * 32, oa = pa * 32;
+            float acc[4][4] = {};
+#pragma unroll 4
+            for (int m = oa; m < ob; m++) {
+                float sv[4], xv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    sv[u] = S[ob + r8 + 8 * u][m];
+                    xv[u] = X[m][oa + c8 + 8 * u];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] = fmaf(sv[u], xv[v], acc[u][v]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) tmp[pa * 1024 + (r8 + 8 * u) * 32 + c8 + 8 * v] = acc[u][v];
+        }
+        __syncthreads();
+        for (int w = tid; w < pairs * 64; w += PS_THREADS) {
+            const int pa = w >> 6, ob = (pa + d) * 32, oa = pa * 32;
+            float acc[4][4] = {};
+#pragma unroll 4
+            for (int m = 0; m < 32; m++) {              // X_bb is lower triangular (zeros above)
+                float xv[4], tv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    xv[u] = X[ob + r8 + 8 * u][ob + m];
+                    tv[u] = tmp[pa * 1024 + m * 32 + c8 + 8 * u];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] = fmaf(xv[u], tv[v], acc[u][v]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) X[ob + r8 + 8 * u][oa + c8 + 8 * v] = -acc[u][v];
+        }
+        __syncthreads();
     }
 }
 
-// Rows below the block: L[i][k0:k0+kb] = A[i][k0:k0+kb] L_kk^{-T}, one thread
-// per row, reciprocal pivots staged in shared memory.
-__global__ void k_trsm_panel32(float *A, int n, int k0, int kb, int row0, const int *status) {
-    if (status[0] >= 0) return;
-    __shared__ float L[NB32][NB32 + 1];
-    __shared__ float rinv[NB32];
-    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-        int r = e / kb, c = e % kb;
-        L[r][c] = c <= r ? A[(size_t)(k0 + r) * n + k0 + c] : 0.f;
+// GEMM tile: acc[u][v] += sum_{m in [kb, ke)} A(r0 + ty + 16u, m) B(c0 + tx + 16v, m)
+// (tx = tid % 16, ty = tid / 16).  An operand is row-major in its row index
+// (RM: X(x, m) at p[x * ld + m]) or in the K index (KM: X(x, m) at p[m * ld + x]);
+// rows at or beyond xlim read as zero.  K chunks of 32 go through shared memory
+// with the next chunk prefetched in registers.
+template <bool KM>
+__device__ __forceinline__ void tile_fetch(float (&v)[8], const float *p, long ld, int x0, int xlim, int m0, int ke) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int e = threadIdx.x + PS_THREADS * q;
+        const int m = KM ? (e >> 6) : (e & 31), x = KM ? (e & 63) : (e >> 5);
+        const int gm = m0 + m, gx = x0 + x;
+        v[q] = (gm < ke && gx < xlim) ? __ldcg(p + (KM ? (size_t)gm * ld + gx : (size_t)gx * ld + gm)) : 0.f;
     }
-    __syncthreads();
-    if (threadIdx.x < kb) rinv[threadIdx.x] = 1.f / L[threadIdx.x][threadIdx.x];
-    __syncthreads();
-    int i = row0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float x[NB32];
-    float *row = A + (size_t)i * n + k0;
+}
+
+template <bool KM>
+__device__ __forceinline__ void tile_put(float (*s)[GT + 1], const float (&v)[8]) {
 #pragma unroll
-    for (int j = 0; j < NB32; j++) x[j] = j < kb ? row[j] : 0.f;
+    for (int q = 0; q < 8; q++) {
+        const int e = threadIdx.x + PS_THREADS * q;
+        const int m = KM ? (e >> 6) : (e & 31), x = KM ? (e & 63) : (e >> 5);
+        s[m][x] = v[q];
+    }
+}
+
+template <bool AKM, bool BKM>
+__device__ void gemm64(float (&acc)[4][4], const float *A, long lda, int r0, int rlim, const float *B, long ldb,
+                       int c0, int clim, int kb, int ke, TileSmem &S) {
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    if (kb >= ke) return;
+    float va[8], vb[8];
+    tile_fetch<AKM>(va, A, lda, r0, rlim, kb, ke);
+    tile_fetch<BKM>(vb, B, ldb, c0, clim, kb, ke);
+    for (int k = kb; k < ke; k += GKC) {
+        __syncthreads();
+        tile_put<AKM>(S.a, va);
+        tile_put<BKM>(S.b, vb);
+        __syncthreads();
+        if (k + GKC < ke) {
+            tile_fetch<AKM>(va, A, lda, r0, rlim, k + GKC, ke);
+            tile_fetch<BKM>(vb, B, ldb, c0, clim, k + GKC, ke);
+        }
+#pragma unroll 8
+        for (int m = 0; m < GKC; m++) {
+            float a[4], b[4];
 #pragma unroll
-    for (int j = 0; j < NB32; j++) {
-        if (j < kb) {
-            float s = x[j];
+            for (int u = 0; u < 4; u++) {
+                a[u] = S.a[m][ty + 16 * u];
+                b[u] = S.b[m][tx + 16 * u];
+            }
 #pragma unroll
-            for (int m = 0; m < j; m++) s -= x[m] * L[j][m];
-            x[j] = s * rinv[j];
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
         }
     }
-#pragma unroll
-    for (int j = 0; j < NB32; j++)
-        if (j < kb) row[j] = x[j];
+    __syncthreads();
 }
 
-__device__ __forceinline__ void tri_tile32(int t, int &bi, int &bj) {
-    int r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+__device__ __forceinline__ void tri_tile(int t, int &bi, int &bj) {
+    int r = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
     while ((r + 1) * (r + 2) / 2 <= t) r++;
     while (r * (r + 1) / 2 > t) r--;
     bi = r;
     bj = t - r * (r + 1) / 2;
 }
 
-// A[i][j] -= sum_m L[i][k0+m] L[j][k0+m] over the lower trailing tiles.
-__global__ void __launch_bounds__(256) k_syrk_update32(float *A, int n, int k0, int kb, int k1, const int *status) {
-    if (status[0] >= 0) return;
-    __shared__ float As[NB32][TG32 + 1], Bs[NB32][TG32 + 1];
-    int bi, bj;
-    tri_tile32(blockIdx.x, bi, bj);
-    int r0 = k1 + bi * TG32, c0 = k1 + bj * TG32;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    for (int e = tid; e < TG32 * NB32; e += 256) {
-        int rr = e / NB32, cc = e % NB32;
-        int ra = r0 + rr, rb = c0 + rr;
-        As[cc][rr] = (ra < n && cc < kb) ? A[(size_t)ra * n + k0 + cc] : 0.f;
-        Bs[cc][rr] = (rb < n && cc < kb) ? A[(size_t)rb * n + k0 + cc] : 0.f;
-    }
-    __syncthreads();
-    float acc[4][4] = {};
-#pragma unroll 8
-    for (int c = 0; c < NB32; c++) {
-        float av[4], bv[4];
+// Partial column sums upart[ch][k] = sum_{i in chunk ch} O[i][k] v[i] (RCH rows
+// per chunk, one warp per (chunk, 32 columns)), then out[k] = scale * sum_ch.
+__device__ __forceinline__ void colsum_partial(const double *O, int Ns, long P, const double *v, double *upart,
+                                               int gwarp, int gwarps, int lane) {
+    const int nch = (Ns + RCH - 1) / RCH;
+    const long ncg = (P + 31) / 32;
+    for (long w = gwarp; w < (long)nch * ncg; w += gwarps) {
+        const int ch = (int)(w / ncg);
+        const long k = (w % ncg) * 32 + lane;
+        const int i0 = ch * RCH, i1 = min(Ns, i0 + RCH);
+        double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (k < P) {
+            int i = i0;
+            for (; i + 7 < i1; i += 8) {
 #pragma unroll
-        for (int m = 0; m < 4; m++) av[m] = As[c][ty + 16 * m];
-#pragma unroll
-        for (int q = 0; q < 4; q++) bv[q] = Bs[c][tx + 16 * q];
-#pragma unroll
-        for (int m = 0; m < 4; m++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[m][q] = fmaf(av[m], bv[q], acc[m][q]);
-    }
-#pragma unroll
-    for (int m = 0; m < 4; m++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            int i = r0 + ty + 16 * m, j = c0 + tx + 16 * q;
-            if (i < n && j <= i) A[(size_t)i * n + j] -= acc[m][q];
+                for (int q = 0; q < 8; q++) acc[q] += O[(size_t)(i + q) * P + k] * __ldcg(v + i + q);
+            }
+            for (; i < i1; i++) acc[0] += O[(size_t)i * P + k] * __ldcg(v + i);
+            upart[(size_t)ch * P + k] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
         }
+    }
 }
 
-// ---------------------------------------------------------------- block triangular solves
-// The factor is solved with in blocks of BT = 128 rows; the inverses of the
-// diagonal blocks are formed once per factorisation (all blocks in one launch,
-// thread c computes column c by forward substitution), so a block step of a
-// triangular solve is two independent GEMVs instead of a 128-long dependency
-// chain.
-constexpr int BT = 128;
-constexpr int BINV_SMEM = 2 * BT * (BT + 1) * 4;
+__device__ __forceinline__ double colsum_reduce(const double *upart, int Ns, long P, long k, int lane) {
+    const int nch = (Ns + RCH - 1) / RCH;
+    double acc = 0.0;
+    for (int ch = lane; ch < nch; ch += 32) acc += __ldcg(upart + (size_t)ch * P + k);
+    return warp_sum(acc);
+}
 
-__global__ void __launch_bounds__(BT) k_block_inverse(const float *__restrict__ L, int n, float *Xd) {
-    extern __shared__ float sh[];
-    float (*Ls)[BT + 1] = (float (*)[BT + 1])sh;
-    float (*Xs)[BT + 1] = (float (*)[BT + 1])(sh + BT * (BT + 1));
-    const int b = blockIdx.x, j0 = b * BT, bs = min(BT, n - j0), c = threadIdx.x;
-    for (int e = c; e < BT * BT; e += BT) {
-        int r = e / BT, q = e % BT;
-        Ls[r][q] = (r < bs && q < bs && q <= r) ? L[(size_t)(j0 + r) * n + j0 + q] : 0.f;
-    }
-    __syncthreads();
-    for (int r = 0; r < BT; r++) {
-        float x = 0.f;
-        if (c < bs && r < bs && r >= c) {
-            float s = (r == c) ? 1.f : 0.f;
-            for (int m = c; m < r; m++) s -= Ls[r][m] * Xs[m][c];
-            x = s / Ls[r][r];
+__device__ __forceinline__ double rowdot(const double *o, long P, const double *v, int lane) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if ((P & 1) == 0) {                                  // rows 16-byte aligned: double2 loads
+        const double2 *o2 = (const double2 *)o, *v2 = (const double2 *)v;
+        const long P2 = P >> 1;
+        long k = lane;
+        for (; k + 96 < P2; k += 128) {
+            const double2 x0 = o2[k], x1 = o2[k + 32], x2 = o2[k + 64], x3 = o2[k + 96];
+            const double2 y0 = __ldcg(v2 + k), y1 = __ldcg(v2 + k + 32), y2 = __ldcg(v2 + k + 64),
+                          y3 = __ldcg(v2 + k + 96);
+            a0 += x0.x * y0.x + x0.y * y0.y;
+            a1 += x1.x * y1.x + x1.y * y1.y;
+            a2 += x2.x * y2.x + x2.y * y2.y;
+            a3 += x3.x * y3.x + x3.y * y3.y;
         }
-        Xs[r][c] = x;
+        for (; k < P2; k += 32) {
+            const double2 x0 = o2[k], y0 = __ldcg(v2 + k);
+            a0 += x0.x * y0.x + x0.y * y0.y;
+        }
+    } else {
+        long k = lane;
+        for (; k + 96 < P; k += 128) {
+            a0 += o[k] * __ldcg(v + k);
+            a1 += o[k + 32] * __ldcg(v + k + 32);
+            a2 += o[k + 64] * __ldcg(v + k + 64);
+            a3 += o[k + 96] * __ldcg(v + k + 96);
+        }
+        for (; k < P; k += 32) a0 += o[k] * __ldcg(v + k);
     }
-    __syncthreads();
-    float *out = Xd + (size_t)b * BT * BT;
-    for (int e = c; e < BT * BT; e += BT) out[e] = Xs[e / BT][e % BT];
+    return warp_sum((a0 + a1) + (a2 + a3));
 }
 
-// Forward block step j: z = X_jj rhs_j (every CTA), x_j = z (CTA 0), then
-// rhs_i -= L[i][j0:j0+bs] z for the rows below (one warp per row).
-__global__ void __launch_bounds__(256) k_trsv_fwd_blk(const float *__restrict__ L, const float *__restrict__ Xd,
-                                                     int n, int j, float *rhs, float *x) {
-    __shared__ float z[BT];
-    __shared__ float part[2][BT];
-    const int j0 = j * BT, bs = min(BT, n - j0), t = threadIdx.x;
-    const float *X = Xd + (size_t)j * BT * BT;
-    {
-        int r = t & (BT - 1), h = t >> 7;                 // two threads per row, half the columns each
-        float s = 0.f;
-        if (r < bs)
-            for (int m = h; m <= r; m += 2) s += X[r * BT + m] * rhs[j0 + m];
-        part[h][r] = s;
+// sum over the float4 groups [g0, g1) of row . v, one warp, result in every lane
+__device__ __forceinline__ float dot4_range(const float *row, const float *v, int g0, int g1, int lane) {
+    const float4 *r4 = (const float4 *)row, *v4 = (const float4 *)v;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int g = g0 + lane;
+    for (; g + 96 < g1; g += 128) {
+        const float4 x0 = __ldcg(r4 + g), x1 = __ldcg(r4 + g + 32), x2 = __ldcg(r4 + g + 64),
+                     x3 = __ldcg(r4 + g + 96);
+        const float4 y0 = __ldcg(v4 + g), y1 = __ldcg(v4 + g + 32), y2 = __ldcg(v4 + g + 64),
+                     y3 = __ldcg(v4 + g + 96);
+        s0 += (x0.x * y0.x + x0.y * y0.y) + (x0.z * y0.z + x0.w * y0.w);
+        s1 += (x1.x * y1.x + x1.y * y1.y) + (x1.z * y1.z + x1.w * y1.w);
+        s2 += (x2.x * y2.x + x2.y * y2.y) + (x2.z * y2.z + x2.w * y2.w);
+        s3 += (x3.x * y3.x + x3.y * y3.y) + (x3.z * y3.z + x3.w * y3.w);
     }
-    __syncthreads();
-    if (t < BT) z[t] = t < bs ? part[0][t] + part[1][t] : 0.f;
-    __syncthreads();
-    if (blockIdx.x == 0 && t < bs) x[j0 + t] = z[t];
-    const int warp = t >> 5, lane = t & 31;
-    const int i = j0 + bs + blockIdx.x * 8 + warp;
-    if (i < n) {
-        const float *row = L + (size_t)i * n + j0;
-        float s = 0.f;
-        for (int m = lane; m < bs; m += 32) s += row[m] * z[m];
+    for (; g < g1; g += 32) {
+        const float4 x0 = __ldcg(r4 + g), y0 = __ldcg(v4 + g);
+        s0 += (x0.x * y0.x + x0.y * y0.y) + (x0.z * y0.z + x0.w * y0.w);
+    }
+    float t = (s0 + s1) + (s2 + s3);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) rhs[i] -= s;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+struct FrArgs {
+    float *T;           // [n][n] Gram + shift (lower) on entry; U = L^T in the upper triangle after
+    float *Li, *LiT;    // [n][ldl] L^{-1} (lower) and its transpose; pad columns are zero
+    int n;              // order of the system
+    int ldl;            // row pitch of Li / LiT (n rounded up to 32)
+    int space;          // 0: samples (n = N_s, unknown y), 1: parameters (n = N_p, unknown delta)
+    const double *O;    // centred Jacobian [N_s][N_p]
+    int Ns;
+    long P;
+    const double *eps;  // [N_s] centred local energies
+    double shift;
+    double *x;          // [n] solution
+    double *rhs, *r;    // [n] right-hand side and residual
+    double *u, *upart;  // intermediate vector, partial column sums
+    float *rf, *zf;     // [n] FP32 right-hand side and half-solve
+    double *nrm;        // [2] |r|^2, |rhs|^2
+    int sweeps;
+    int *status;        // [0] first failing column or -1
+    unsigned *bar;      // [0] arrivals, [1] generation
+    int *err;
+    unsigned long long *tm;   // [8] phase nanoseconds: [0..6] CTA 0's view, [7] owners' block work
+};
+
+__global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
+    extern __shared__ float psm[];
+    float (*S0)[BT + 1] = (float (*)[BT + 1])psm;
+    float (*S1)[BT + 1] = (float (*)[BT + 1])(psm + BT * (BT + 1));
+    TileSmem &TS = *(TileSmem *)psm;
+    float (*ST)[GT + 1] = (float (*)[GT + 1])psm;           // 64 x 65 staging tile
+    const int n = a.n, ldl = a.ldl, tid = threadIdx.x, G = gridDim.x;
+    const int lane = tid & 31, tx = tid & 15, ty = tid >> 4;
+    const int gtid = blockIdx.x * PS_THREADS + tid, gthreads = G * PS_THREADS;
+    const int gwarp = blockIdx.x * (PS_THREADS / 32) + (tid >> 5), gwarps = G * (PS_THREADS / 32);
+    const int nb = (n + BT - 1) / BT;
+    __shared__ int s_flag;
+    __shared__ float tmpb[3 * 1024];
+    unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const bool timing = blockIdx.x == 0 && tid == 0;
+    unsigned long long tstart = timing ? gtimer() : 0, tprev = tstart;
+#define NQS_PHASE(k)                                  \
+    if (timing) {                                     \
+        unsigned long long now_ = gtimer();           \
+        tacc[k] += now_ - tprev;                      \
+        tprev = now_;                                 \
     }
-}
 
-// Backward block step j (last block first): y_j = X_jj^T rhs_j, then
-// rhs_c -= sum_m L[j0+m][c] y_m for the columns before the block.
-__global__ void __launch_bounds__(256) k_trsv_bwd_blk(const float *__restrict__ L, const float *__restrict__ Xd,
-                                                     int n, int j, float *rhs, float *x) {
-    __shared__ float z[BT];
-    __shared__ float part[2][BT];
-    const int j0 = j * BT, bs = min(BT, n - j0), t = threadIdx.x;
-    const float *X = Xd + (size_t)j * BT * BT;
-    {
-        int c = t & (BT - 1), h = t >> 7;
-        float s = 0.f;
-        if (c < bs)
-            for (int r = c + h; r < bs; r += 2) s += X[r * BT + c] * rhs[j0 + r];
-        part[h][c] = s;
+    // ---------------- factor
+    for (int kb = 0; kb < nb; kb++) {
+        const int k0 = kb * BT, bs = min(BT, n - k0), k1 = k0 + bs, rest = n - k1;
+        if (blockIdx.x == kb % G) {
+            const unsigned long long t_own = tid == 0 ? gtimer() : 0;
+            for (int e0 = 0; e0 < BT * BT; e0 += 8 * PS_THREADS) {
+                float v[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int e = e0 + tid + q * PS_THREADS, rr = e / BT, cc = e % BT;
+                    const bool in = rr < bs && cc <= rr;
+                    v[q] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) : (rr == cc ? 1.f : 0.f);
+                }
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int e = e0 + tid + q * PS_THREADS;
+                    S0[e / BT][e % BT] = v[q];
+                }
+            }
+            __syncthreads();
+            const int f = block_chol128(S0, S1, bs, &s_flag, tmpb);
+            if (f >= 0) {
+                if (tid == 0) {
+                    a.status[0] = k0 + f;
+                    __threadfence();
+                }
+            } else {
+                block_inv128(S0, S1, tmpb);
+                for (int e = tid; e < BT * BT; e += PS_THREADS) {
+                    const int rr = e >> 7, q = e & (BT - 1);
+                    if (rr < bs && q < bs) {
+                        a.Li[(size_t)(k0 + rr) * ldl + k0 + q] = S1[rr][q];
+                        a.LiT[(size_t)(k0 + rr) * ldl + k0 + q] = S1[q][rr];
+                    }
+                }
+            }
+            if (tid == 0) atomicAdd(a.tm + 7, gtimer() - t_own);
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
+        NQS_PHASE(0);
+        if (rest <= 0) break;
+        // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1
+        {
+            const int ntr = (rest + GT - 1) / GT;
+            for (int t = blockIdx.x; t < 2 * ntr; t += G) {
+                const int c0 = (t & 1) * GT, r0 = k1 + (t >> 1) * GT;
+                if (c0 >= bs) continue;
+                float acc[4][4] = {};
+                gemm64<false, false>(acc, a.Li + (size_t)k0 * ldl + k0, ldl, c0, bs, a.T + k0, n, r0, n, 0,
+                                     min(bs, c0 + GT), TS);
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int c = c0 + ty + 16 * u, r = r0 + tx + 16 * v;
+                        if (c < bs && r < n) a.T[(size_t)(k0 + c) * n + r] = acc[u][v];
+                    }
+            }
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        NQS_PHASE(1);
+        // trailing update: A[i][j] -= sum_m U[k0 + m][i] U[k0 + m][j], k1 <= j <= i
+        {
+            const int ntt = (rest + GT - 1) / GT, ntiles = ntt * (ntt + 1) / 2;
+            for (int t = blockIdx.x; t < ntiles; t += G) {
+                int bi, bj;
+                tri_tile(t, bi, bj);
+                const int r0 = k1 + bi * GT, c0 = k1 + bj * GT;
+                float acc[4][4] = {};
+                const float *U = a.T + (size_t)k0 * n;
+                gemm64<true, true>(acc, U, n, r0, n, U, n, c0, n, 0, bs, TS);
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
+                        if (i < n && j <= i) {
+                            const size_t idx = (size_t)i * n + j;
+                            a.T[idx] = __ldcg(&a.T[idx]) - acc[u][v];
+                        }
+                    }
+            }
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        NQS_PHASE(2);
     }
-    __syncthreads();
-    if (t < BT) z[t] = t < bs ? part[0][t] + part[1][t] : 0.f;
-    __syncthreads();
-    if (blockIdx.x == 0 && t < bs) x[j0 + t] = z[t];
-    const int col = blockIdx.x * 256 + t;
-    if (col < j0) {
-        float s = 0.f;
-        for (int m = 0; m < bs; m++) s += L[(size_t)(j0 + m) * n + col] * z[m];
-        rhs[col] -= s;
+
+    // ---------------- L^{-1}: join halves of h blocks, h = 1, 2, 4, ...
+    for (int h = 1; h < nb; h *= 2) {
+        const int span = 2 * h * BT, ngrp = (n + span - 1) / span, per = 4 * h * h;
+        // W = L21 X11 (into the dead lower triangle of T)
+        for (int t = blockIdx.x; t < ngrp * per; t += G) {
+            const int g = t / per, rt = (t % per) / (2 * h), ct = t % (2 * h);
+            const int a0 = g * span, a1 = a0 + h * BT, a2 = min(n, a0 + span);
+            const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
+            if (a1 >= a2 || r0 >= a2) continue;
+            float acc[4][4] = {};
+            gemm64<true, true>(acc, a.T, n, r0, a2, a.Li, ldl, c0, a1, c0, a1, TS);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
+                    if (i < a2) a.T[(size_t)i * n + j] = acc[u][v];
+                }
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        // X21 = -X22 W
+        for (int t = blockIdx.x; t < ngrp * per; t += G) {
+            const int g = t / per, rt = (t % per) / (2 * h), ct = t % (2 * h);
+            const int a0 = g * span, a1 = a0 + h * BT, a2 = min(n, a0 + span);
+            const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
+            if (a1 >= a2 || r0 >= a2) continue;
+            float acc[4][4] = {};
+            gemm64<false, true>(acc, a.Li, ldl, r0, a2, a.T, n, c0, a1, a1, min(a2, r0 + GT), TS);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
+                    if (i < a2) a.Li[(size_t)i * ldl + j] = -acc[u][v];
+                    ST[ty + 16 * u][tx + 16 * v] = -acc[u][v];
+                }
+            __syncthreads();
+            for (int e = tid; e < GT * GT; e += PS_THREADS) {
+                const int cc = e / GT, rr = e % GT;
+                if (r0 + rr < a2) a.LiT[(size_t)(c0 + cc) * ldl + r0 + rr] = ST[rr][cc];
+            }
+            __syncthreads();
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
     }
-}
+    NQS_PHASE(3);
 
-// ---------------------------------------------------------------- refinement helpers
-__global__ void k_d2f(const double *__restrict__ a, float *b, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
-
-__global__ void k_add_f2d(double *y, const float *__restrict__ d, int n, int first) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = first ? (double)d[i] : y[i] + (double)d[i];
-}
-
-// u = O_c^T y (FP64, 32 columns x 8 row groups per block)
-__global__ void k_ct_dot(const double *__restrict__ O, int Ns, long P, const double *__restrict__ y, double *u) {
-    __shared__ double a[8][33];
-    long k = (long)blockIdx.x * 32 + threadIdx.x;
-    double s = 0.0;
-    if (k < P)
-        for (int i = threadIdx.y; i < Ns; i += 8) s += O[(size_t)i * P + k] * y[i];
-    a[threadIdx.y][threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.y == 0 && k < P) {
-        double S = 0.0;
-        for (int q = 0; q < 8; q++) S += a[q][threadIdx.x];
-        u[k] = S;
+    // ---------------- right-hand side
+    const int Ns = a.Ns;
+    const long P = a.P;
+    if (a.space == 1) {
+        colsum_partial(a.O, Ns, P, a.eps, a.upart, gwarp, gwarps, lane);
+        if (!grid_barrier(a.bar, a.err)) return;
+        for (long k = gwarp; k < P; k += gwarps) {
+            const double s = colsum_reduce(a.upart, Ns, P, k, lane) / (double)Ns;
+            if (lane == 0) {
+                a.rhs[k] = s;
+                a.rf[k] = (float)s;
+            }
+        }
+    } else {
+        for (int i = gtid; i < n; i += gthreads) {
+            a.rhs[i] = a.eps[i];
+            a.rf[i] = (float)a.eps[i];
+        }
     }
-}
+    if (!grid_barrier(a.bar, a.err)) return;
+    NQS_PHASE(5);
 
-// r_i = eps_i - (O_c u)_i / Ns - shift y_i  (warp per row)
-__global__ void k_residual(const double *__restrict__ O, int Ns, long P, const double *__restrict__ u,
-                           const double *__restrict__ y, const double *__restrict__ eps, double shift,
-                           double *r) {
-    int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (row >= Ns) return;
-    const double *o = O + (size_t)row * P;
-    double s = 0.0;
-    for (long k = lane; k < P; k += 32) s += o[k] * u[k];
-    s = warp_sum(s);
-    if (lane == 0) r[row] = eps[row] - s / (double)Ns - shift * y[row];
-}
-
-__global__ void k_norms(const double *__restrict__ r, const double *__restrict__ e, int n, double *out) {
-    __shared__ double a[1024], b[1024];
-    double s = 0.0, t = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        s += r[i] * r[i];
-        t += e[i] * e[i];
+    // ---------------- refinement sweeps
+    for (int s = 0; s <= a.sweeps; s++) {
+        // z = L^{-1} rf (row i reads the 4-aligned groups up to i; the entries
+        // right of the diagonal inside a group are the zeros of the diagonal block)
+        for (int i = gwarp; i < n; i += gwarps) {
+            const float t = dot4_range(a.Li + (size_t)i * ldl, a.rf, 0, (i >> 2) + 1, lane);
+            if (lane == 0) a.zf[i] = t;
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        // x += L^{-T} z (zf and the pad columns are zero beyond n)
+        for (int j = gwarp; j < n; j += gwarps) {
+            const float t = dot4_range(a.LiT + (size_t)j * ldl, a.zf, j >> 2, ldl >> 2, lane);
+            if (lane == 0) a.x[j] = (s == 0 ? 0.0 : __ldcg(a.x + j)) + (double)t;
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        NQS_PHASE(4);
+        // FP64 residual r = rhs - A x
+        if (a.space == 0) {
+            // A y = O_c (O_c^T y) / N_s + shift y
+            colsum_partial(a.O, Ns, P, a.x, a.upart, gwarp, gwarps, lane);
+            if (!grid_barrier(a.bar, a.err)) return;
+            for (long k = gwarp; k < P; k += gwarps) {
+                const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
+                if (lane == 0) a.u[k] = sk;
+            }
+            if (!grid_barrier(a.bar, a.err)) return;
+            for (int i = gwarp; i < Ns; i += gwarps) {
+                const double d = rowdot(a.O + (size_t)i * P, P, a.u, lane);
+                if (lane == 0) {
+                    const double ri = a.rhs[i] - d / (double)Ns - a.shift * __ldcg(a.x + i);
+                    a.r[i] = ri;
+                    a.rf[i] = (float)ri;
+                }
+            }
+        } else {
+            // A delta = O_c^T (O_c delta) / N_s + shift delta
+            for (int i = gwarp; i < Ns; i += gwarps) {
+                const double d = rowdot(a.O + (size_t)i * P, P, a.x, lane);
+                if (lane == 0) a.u[i] = d;
+            }
+            if (!grid_barrier(a.bar, a.err)) return;
+            colsum_partial(a.O, Ns, P, a.u, a.upart, gwarp, gwarps, lane);
+            if (!grid_barrier(a.bar, a.err)) return;
+            for (long k = gwarp; k < P; k += gwarps) {
+                const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
+                if (lane == 0) {
+                    const double rk = __ldcg(a.rhs + k) - sk / (double)Ns - a.shift * __ldcg(a.x + k);
+                    a.r[k] = rk;
+                    a.rf[k] = (float)rk;
+                }
+            }
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        NQS_PHASE(5);
     }
-    a[threadIdx.x] = s;
-    b[threadIdx.x] = t;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            a[threadIdx.x] += a[threadIdx.x + o];
-            b[threadIdx.x] += b[threadIdx.x + o];
+    // ---------------- |r|^2 and |rhs|^2
+    if (blockIdx.x == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int i = tid; i < n; i += PS_THREADS) {
+            const double ri = __ldcg(a.r + i), bi = __ldcg(a.rhs + i);
+            s1 += ri * ri;
+            s2 += bi * bi;
+        }
+        s1 = warp_sum(s1);
+        s2 = warp_sum(s2);
+        __shared__ double red[2][PS_THREADS / 32];
+        if (lane == 0) {
+            red[0][tid >> 5] = s1;
+            red[1][tid >> 5] = s2;
         }
         __syncthreads();
+        if (tid == 0) {
+            double t1 = 0.0, t2 = 0.0;
+            for (int q = 0; q < PS_THREADS / 32; q++) {
+                t1 += red[0][q];
+                t2 += red[1][q];
+            }
+            a.nrm[0] = t1;
+            a.nrm[1] = t2;
+        }
     }
-    if (threadIdx.x == 0) {
-        out[0] = a[0];
-        out[1] = b[0];
+    if (timing) {
+        tacc[6] = gtimer() - tstart;
+        for (int k = 0; k < 7; k++) a.tm[k] = tacc[k];     // [7]: summed by the block owners
     }
+#undef NQS_PHASE
 }
 
 // ---------------------------------------------------------------- driver
 struct MixedWs {
-    DevBuf<float> hi, lo, T, Xd, rf, zf, xf;
-    DevBuf<double> u, r, nrm;
+    DevBuf<float> hi, lo, T, Li, LiT, rf, zf;
+    DevBuf<double> rhs, r, u, upart, nrm;
+    DevBuf<unsigned> bar;
     DevBuf<int> status;
-    int ns_pad = 0;
-    long p_pad = 0;
+    DevBuf<unsigned long long> tm;
+    long rows_pad = 0, k_pad = 0;     // operand layout of hi / lo
+    int space = -1;
+    int n = 0;                        // order of the last system (pad columns of Li zeroed for it)
 };
 static MixedWs g_mx;
 
-// Two block triangular solves: xf = (L L^T)^{-1} rf (rf is consumed).
-static void factor_solve(MixedWs &w, int n, cudaStream_t st) {
-    const int nb = (n + BT - 1) / BT;
-    for (int j = 0; j < nb; j++) {
-        int below = n - (j * BT + min(BT, n - j * BT));
-        NQS_LAUNCH("trsv32_fwd");
-        k_trsv_fwd_blk<<<below > 0 ? (below + 7) / 8 : 1, 256, 0, st>>>(w.T.p, w.Xd.p, n, j, w.rf.p, w.zf.p);
-    }
-    for (int j = nb - 1; j >= 0; j--) {
-        int before = j * BT;
-        NQS_LAUNCH("trsv32_bwd");
-        k_trsv_bwd_blk<<<before > 0 ? (before + 255) / 256 : 1, 256, 0, st>>>(w.T.p, w.Xd.p, n, j, w.zf.p,
-                                                                               w.xf.p);
+struct MixedPlan {
+    int space;        // 0 samples, 1 parameters
+    int n;            // order of the solved system
+    long rows_pad;    // Gram operand rows (n padded to TC_M)
+    long k_pad;       // Gram operand K (the other dimension padded to TC_K)
+};
+
+static MixedPlan plan_mixed(int Ns, long P, int space_opt) {
+    MixedPlan p;
+    p.space = space_opt == 1 ? 0 : space_opt == 2 ? 1 : ((long)Ns > P ? 1 : 0);
+    const long rows = p.space ? P : Ns, k = p.space ? Ns : P;
+    p.n = (int)rows;
+    p.rows_pad = (rows + TC_M - 1) / TC_M * TC_M;
+    p.k_pad = (k + TC_K - 1) / TC_K * TC_K;
+    return p;
+}
+
+// Param-space operand: hi[k][i] = tf32(O_c[i][k]) (row pitch ldn), via 32 x 32
+// shared-memory transposes; O is centred in place as in k_center_split.
+__global__ void k_center_split_t(double *O, int Ns, long P, const double *__restrict__ gm, float *hi, float *lo,
+                                 long ldn) {
+    __shared__ float th[32][33], tl[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+    const long tk = (P + 31) / 32, ti = (Ns + 31) / 32;
+    for (long t = blockIdx.x; t < tk * ti; t += gridDim.x) {
+        const long i0 = (t / tk) * 32, k0 = (t % tk) * 32;
+        for (int r = ty; r < 32; r += 8) {
+            const long i = i0 + r, k = k0 + tx;
+            float h = 0.f, l = 0.f;
+            if (i < Ns && k < P) {
+                const double x = O[i * P + k] - gm[k];
+                O[i * P + k] = x;
+                h = tf32_rna((float)x);
+                l = tf32_rna((float)(x - (double)h));
+            }
+            th[r][tx] = h;
+            tl[r][tx] = l;
+        }
+        __syncthreads();
+        for (int r = ty; r < 32; r += 8) {
+            const long k = k0 + r, i = i0 + tx;
+            if (k < P && i < Ns) {
+                hi[k * ldn + i] = th[tx][r];
+                lo[k * ldn + i] = tl[tx][r];
+            }
+        }
+        __syncthreads();
     }
 }
 
-// Enqueue the whole mixed solve with no host synchronisation: split, tensor-core
-// Gram, factor, block inverses, refinement sweeps and the final norms.  Kernels
-// after the factor run unconditionally; a broken factor is reported through
-// status[0] and the caller discards the result.
-static void enqueue_mixed(double *O, const double *gm, const double *eps, int Ns, long P, double shift,
-                          int sweeps, int passes, double *y, const CUtensorMap &mh, const CUtensorMap &ml,
-                          int *err, cudaStream_t st) {
+// Enqueue the whole mixed solve with no host synchronisation: centring and
+// split, tensor-core Gram, then the cooperative factor / inverse / refinement
+// kernel.  A broken factor is reported through status[0].
+static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, const double *eps, int Ns, long P,
+                          double shift, int sweeps, int passes, double *x, const CUtensorMap &mh,
+                          const CUtensorMap &ml, int *err, cudaStream_t st) {
     MixedWs &w = g_mx;
-    const long p_pad = w.p_pad;
-    const int nb = (Ns + BT - 1) / BT;
     cudaMemsetAsync(w.status.p, 0xff, 2 * sizeof(int), st);
     cudaMemsetAsync(err, 0, sizeof(int), st);
-    {
+    if (pl.space == 0) {
         NQS_LAUNCH("center_split");
-        k_center_split<<<ctx().sm_count * 8, 256, 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, p_pad);
+        k_center_split<<<ctx().sm_count * 8, 256, 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, pl.k_pad);
+    } else {
+        NQS_LAUNCH("center_split_t");
+        k_center_split_t<<<ctx().sm_count * 8, dim3(32, 8), 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, pl.k_pad);
     }
     GramTcArgs g;
-    g.kt_per_seg = (int)(p_pad / TC_K);
+    g.kt_per_seg = (int)(pl.k_pad / TC_K);
     g.nseg = passes >= 3 ? 3 : 1;
     g.scale = (float)(1.0 / (double)Ns);
     g.shift = (float)shift;
     g.C = w.T.p;
-    g.n = Ns;
+    g.n = pl.n;
     g.err = err;
-    int nt = w.ns_pad / TC_M;
+    const int nt = (int)(pl.rows_pad / TC_M);
     {
         NQS_LAUNCH("gram_tc");
         k_gram_tf32_tc<<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(mh, ml, g);
     }
-    for (int k0 = 0; k0 < Ns; k0 += NB32) {
-        int kb = Ns - k0 < NB32 ? Ns - k0 : NB32;
-        {
-            NQS_LAUNCH("chol32_diag");
-            k_potrf_diag32<<<1, 32, 0, st>>>(w.T.p, Ns, k0, kb, w.status.p);
-        }
-        int k1 = k0 + kb, rest = Ns - k1;
-        if (rest <= 0) break;
-        {
-            NQS_LAUNCH("chol32_panel");
-            k_trsm_panel32<<<(rest + 63) / 64, 64, 0, st>>>(w.T.p, Ns, k0, kb, k1, w.status.p);
-        }
-        int ntt = (rest + TG32 - 1) / TG32;
-        {
-            NQS_LAUNCH("chol32_syrk");
-            k_syrk_update32<<<ntt * (ntt + 1) / 2, 256, 0, st>>>(w.T.p, Ns, k0, kb, k1, w.status.p);
-        }
-    }
+    FrArgs fa;
+    fa.T = w.T.p;
+    fa.Li = w.Li.p;
+    fa.LiT = w.LiT.p;
+    fa.n = pl.n;
+    fa.ldl = (pl.n + 31) / 32 * 32;
+    fa.space = pl.space;
+    fa.O = O;
+    fa.Ns = Ns;
+    fa.P = P;
+    fa.eps = eps;
+    fa.shift = shift;
+    fa.x = x;
+    fa.rhs = w.rhs.p;
+    fa.r = w.r.p;
+    fa.u = w.u.p;
+    fa.upart = w.upart.p;
+    fa.rf = w.rf.p;
+    fa.zf = w.zf.p;
+    fa.nrm = w.nrm.p;
+    fa.sweeps = sweeps;
+    fa.status = w.status.p;
+    fa.bar = w.bar.p;
+    fa.err = err;
+    fa.tm = w.tm.p;
+    cudaMemsetAsync(w.bar.p, 0, 2 * sizeof(unsigned), st);
+    cudaMemsetAsync(w.tm.p, 0, 8 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(w.rf.p, 0, sizeof(float) * fa.ldl, st);
+    cudaMemsetAsync(w.zf.p, 0, sizeof(float) * fa.ldl, st);
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)ctx().sm_count);
+    lc.blockDim = dim3(PS_THREADS);
+    lc.dynamicSmemBytes = PS_SMEM;
+    lc.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
     {
-        NQS_LAUNCH("block_inverse");
-        k_block_inverse<<<nb, BT, BINV_SMEM, st>>>(w.T.p, Ns, w.Xd.p);
-    }
-    // refinement: y = S eps; y += S (eps - A y) per sweep, S = (L L^T)^{-1} in FP32
-    dim3 cb(32, 8);
-    unsigned gridP = (unsigned)((P + 31) / 32), rowsN = (unsigned)((Ns * 32 + 255) / 256);
-    unsigned vN = (unsigned)((Ns + 255) / 256);
-    for (int s = 0; s <= sweeps; s++) {
-        {
-            NQS_LAUNCH("refine_vec");
-            k_d2f<<<vN, 256, 0, st>>>(s == 0 ? eps : w.r.p, w.rf.p, Ns);
-        }
-        factor_solve(w, Ns, st);
-        {
-            NQS_LAUNCH("refine_vec");
-            k_add_f2d<<<vN, 256, 0, st>>>(y, w.xf.p, Ns, s == 0);
-        }
-        {
-            NQS_LAUNCH("refine_residual");
-            k_ct_dot<<<gridP, cb, 0, st>>>(O, Ns, P, y, w.u.p);
-        }
-        {
-            NQS_LAUNCH("refine_residual");
-            k_residual<<<rowsN, 256, 0, st>>>(O, Ns, P, w.u.p, y, eps, shift, w.r.p);
-        }
-    }
-    {
-        NQS_LAUNCH("refine_residual");
-        k_norms<<<1, 1024, 0, st>>>(w.r.p, eps, Ns, w.nrm.p);
+        NQS_LAUNCH("factor_refine");
+        cudaLaunchKernelEx(&lc, k_factor_refine, fa);
     }
 }
 
 // The launch sequence above is fixed for given buffers and sizes: it is
-// captured once into a CUDA graph and replayed every step (one launch instead
-// of ~600).  Per-kernel profiling runs the sequence uncaptured.
+// captured once into a CUDA graph and replayed every step.  Per-kernel
+// profiling runs the sequence uncaptured.
 struct MixedGraph {
     cudaGraphExec_t exec = nullptr;
     const void *key[5] = {};
-    int Ns = 0, sweeps = -1, passes = -1;
+    int Ns = 0, sweeps = -1, passes = -1, space = -1;
     long P = 0;
     double shift = 0.0;
     long kernels = 0;
@@ -682,90 +1123,119 @@ struct MixedGraph {
 static MixedGraph g_mgraph;
 
 bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
-                       int passes, double *y, double *out_resid, int *out_fail) {
+                       int passes, int space_opt, double *y, double *delta, bool *param_space, double *out_resid,
+                       int *out_fail) {
     Context &c = ctx();
     cudaStream_t st = c.stream;
     MixedWs &w = g_mx;
-    const int ns_pad = (Ns + TC_M - 1) / TC_M * TC_M;
-    const long p_pad = (P + TC_K - 1) / TC_K * TC_K;
+    const MixedPlan pl = plan_mixed(Ns, P, space_opt);
+    const int n = pl.n;
     bool moved = false;
-    if (ns_pad != w.ns_pad || p_pad != w.p_pad) {
-        if (!w.hi.ensure((size_t)ns_pad * p_pad) || !w.lo.ensure((size_t)ns_pad * p_pad)) return false;
-        if (!NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ns_pad * p_pad, st)) ||
-            !NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ns_pad * p_pad, st)))
+    if (pl.rows_pad != w.rows_pad || pl.k_pad != w.k_pad || pl.space != w.space) {
+        const size_t ne = (size_t)pl.rows_pad * pl.k_pad;
+        if (!w.hi.ensure(ne) || !w.lo.ensure(ne)) return false;
+        if (!NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ne, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ne, st)))
             return false;
-        w.ns_pad = ns_pad;
-        w.p_pad = p_pad;
+        w.rows_pad = pl.rows_pad;
+        w.k_pad = pl.k_pad;
+        w.space = pl.space;
         moved = true;
     }
-    const int nb = (Ns + BT - 1) / BT;
-    const void *before[8] = {w.T.p, w.Xd.p, w.rf.p, w.zf.p, w.xf.p, w.u.p, w.r.p, w.nrm.p};
-    if (!w.T.ensure((size_t)Ns * Ns) || !w.Xd.ensure((size_t)nb * BT * BT) || !w.rf.ensure(Ns) ||
-        !w.zf.ensure(Ns) || !w.xf.ensure(Ns) || !w.u.ensure(P) || !w.r.ensure(Ns) || !w.nrm.ensure(2) ||
-        !w.status.ensure(2))
+    const long big = (long)Ns > P ? (long)Ns : P;
+    const void *before[12] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p};
+    const int ldl = (n + 31) / 32 * 32;
+    if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
+        !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
+        !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(2) || !w.status.ensure(2) ||
+        !w.bar.ensure(2) || !w.tm.ensure(8))
         return false;
-    const void *after[8] = {w.T.p, w.Xd.p, w.rf.p, w.zf.p, w.xf.p, w.u.p, w.r.p, w.nrm.p};
-    for (int i = 0; i < 8; i++) moved |= before[i] != after[i];
+    const void *after[12] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p};
+    for (int i = 0; i < 12; i++) moved |= before[i] != after[i];
+    if (moved || w.n != n) {
+        // the pad columns of L^{-1} are read (as zeros) by the vectorised solves
+        if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.LiT.p, 0, sizeof(float) * (size_t)n * ldl, st)))
+            return false;
+        w.n = n;
+        moved = true;
+    }
     static DevBuf<int> err;
     if (!err.ensure(1)) return false;
     static bool attr = false;
     if (!attr) {
         if (!NQS_CUDA(cudaFuncSetAttribute(k_gram_tf32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM)) ||
-            !NQS_CUDA(cudaFuncSetAttribute(k_block_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           BINV_SMEM)))
+            !NQS_CUDA(cudaFuncSetAttribute(k_factor_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, PS_SMEM)))
             return false;
+        int per_sm = 0;
+        if (!NQS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_refine, PS_THREADS, PS_SMEM)))
+            return false;
+        if (per_sm < 1) {
+            set_error("factor / refinement kernel does not fit on an SM");
+            return false;
+        }
         attr = true;
     }
     CUtensorMap mh, ml;
-    if (!make_map(&mh, w.hi.p, ns_pad, p_pad) || !make_map(&ml, w.lo.p, ns_pad, p_pad)) return false;
+    if (!make_map(&mh, w.hi.p, pl.rows_pad, pl.k_pad) || !make_map(&ml, w.lo.p, pl.rows_pad, pl.k_pad))
+        return false;
+    double *x = pl.space ? delta : y;
 
     if (c.profiling) {
-        enqueue_mixed(O, gm, eps, Ns, P, shift, sweeps, passes, y, mh, ml, err.p, st);
+        enqueue_mixed(pl, O, gm, eps, Ns, P, shift, sweeps, passes, x, mh, ml, err.p, st);
     } else {
-        MixedGraph &G = g_mgraph;
-        const void *key[5] = {O, gm, eps, y, w.hi.p};
-        bool same = G.exec && !moved && G.Ns == Ns && G.P == P && G.sweeps == sweeps && G.passes == passes &&
-                    G.shift == shift;
-        for (int i = 0; i < 5 && same; i++) same = G.key[i] == key[i];
+        MixedGraph &Gr = g_mgraph;
+        const void *key[5] = {O, gm, eps, x, w.hi.p};
+        bool same = Gr.exec && !moved && Gr.Ns == Ns && Gr.P == P && Gr.sweeps == sweeps &&
+                    Gr.passes == passes && Gr.shift == shift && Gr.space == pl.space;
+        for (int i = 0; i < 5 && same; i++) same = Gr.key[i] == key[i];
         if (!same) {
-            if (G.exec) cudaGraphExecDestroy(G.exec);
-            G.exec = nullptr;
+            if (Gr.exec) cudaGraphExecDestroy(Gr.exec);
+            Gr.exec = nullptr;
             cudaGraph_t graph;
-            long l0 = c.launches;
+            const long l0 = c.launches;
             if (!NQS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal))) return false;
-            enqueue_mixed(O, gm, eps, Ns, P, shift, sweeps, passes, y, mh, ml, err.p, st);
+            enqueue_mixed(pl, O, gm, eps, Ns, P, shift, sweeps, passes, x, mh, ml, err.p, st);
             if (!NQS_CUDA(cudaStreamEndCapture(st, &graph))) return false;
-            G.kernels = c.launches - l0;
+            Gr.kernels = c.launches - l0;
             c.launches = l0;
-            bool ok = NQS_CUDA(cudaGraphInstantiate(&G.exec, graph, 0));
+            const bool ok = NQS_CUDA(cudaGraphInstantiate(&Gr.exec, graph, 0));
             cudaGraphDestroy(graph);
             if (!ok) {
-                G.exec = nullptr;
+                Gr.exec = nullptr;
                 return false;
             }
-            for (int i = 0; i < 5; i++) G.key[i] = key[i];
-            G.Ns = Ns;
-            G.P = P;
-            G.sweeps = sweeps;
-            G.passes = passes;
-            G.shift = shift;
+            for (int i = 0; i < 5; i++) Gr.key[i] = key[i];
+            Gr.Ns = Ns;
+            Gr.P = P;
+            Gr.sweeps = sweeps;
+            Gr.passes = passes;
+            Gr.shift = shift;
+            Gr.space = pl.space;
         }
-        if (!NQS_CUDA(cudaGraphLaunch(G.exec, st))) return false;
-        c.launches += G.kernels;
+        if (!NQS_CUDA(cudaGraphLaunch(Gr.exec, st))) return false;
+        c.launches += Gr.kernels;
     }
     int hs[2] = {-1, 0};
     double h[2] = {0.0, 0.0};
+    unsigned long long tns[8] = {};
     if (!NQS_CUDA(cudaMemcpyAsync(&hs[0], w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaMemcpyAsync(tns, w.tm.p, sizeof(tns), cudaMemcpyDeviceToHost, st)) ||
         !NQS_CUDA(cudaMemcpyAsync(&hs[1], err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
         !NQS_CUDA(cudaMemcpyAsync(h, w.nrm.p, sizeof(h), cudaMemcpyDeviceToHost, st)) ||
         !NQS_CUDA(cudaStreamSynchronize(st)))
         return false;
     if (hs[1]) {
-        set_error("tensor-core Gram timed out waiting on its pipeline");
+        set_error(hs[1] == 2 ? "mixed solve: grid barrier timed out"
+                             : "tensor-core Gram timed out waiting on its pipeline");
         return false;
     }
+    *param_space = pl.space == 1;
     *out_fail = hs[0];
     *out_resid = h[1] > 0 ? sqrt(h[0] / h[1]) : 0.0;
+    for (int k = 0; k < 8; k++) step_stats().phase_us[k] = 1e-3 * (double)tns[k];
     return NQS_CUDA(cudaGetLastError());
 }
 
@@ -791,12 +1261,13 @@ int nqs_gpu_gram_tc(const double *O_host, int Ns, long P, int passes, double sca
     MixedWs &w = g_mx;
     const int ns_pad = (Ns + TC_M - 1) / TC_M * TC_M;
     const long p_pad = (P + TC_K - 1) / TC_K * TC_K;
-    if (ns_pad != w.ns_pad || p_pad != w.p_pad) {
+    if (ns_pad != w.rows_pad || p_pad != w.k_pad || w.space != 0) {
         if (!w.hi.ensure((size_t)ns_pad * p_pad) || !w.lo.ensure((size_t)ns_pad * p_pad)) return -1;
         NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ns_pad * p_pad, st));
         NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ns_pad * p_pad, st));
-        w.ns_pad = ns_pad;
-        w.p_pad = p_pad;
+        w.rows_pad = ns_pad;
+        w.k_pad = p_pad;
+        w.space = 0;
     }
     if (!w.T.ensure((size_t)Ns * Ns)) return -1;
     k_center_split<<<ctx().sm_count * 8, 256, 0, st>>>(dO.p, Ns, P, dz.p, w.hi.p, w.lo.p, p_pad);

@@ -663,13 +663,14 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         }
         return 0;
         };
-        bool solved = false;
+        bool solved = false, have_delta = false;
         if (mixed) {
             // centring happens inside the split kernel of the mixed solve
             double resid = 0.0;
             int f32 = -1;
             if (!minsr_mixed_solve(w.O.p, w.gm.p, w.eps.p, Ns, P, cfg->sr_diag_shift, c.opts.refine_sweeps,
-                                   c.opts.gram_passes, w.y.p, &resid, &f32))
+                                   c.opts.gram_passes, c.opts.mixed_space, w.y.p, w.delta.p, &have_delta,
+                                   &resid, &f32))
                 return -1;
             ss.refine_residual = resid;
             ss.refine_sweeps = c.opts.refine_sweeps;
@@ -680,13 +681,14 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
                 ss.chol_retry = 0;
             } else {
                 ss.mixed_fallback = 1;          // FP32 factor failed: solve this step in FP64
+                have_delta = false;
             }
         } else {
             NQS_LAUNCH("center");
             k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
         }
         if (!solved && fp64_solve(w.y.p, &converged) != 0) return -1;
-        {
+        if (!have_delta) {
             NQS_LAUNCH("delta");
             k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y.p, 1.0 / (double)Ns, w.delta.p);
         }

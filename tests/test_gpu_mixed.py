@@ -2,9 +2,11 @@
 FP64 iterative refinement, checked against FP64 references.
 
 Bars: the 3-pass split Gram (hi hi^T + hi lo^T + lo hi^T) reproduces the FP64
-Gram to 1e-5 of its largest entry (single pass TF32: 5e-3); after refinement the
+Gram to 4e-5 of its largest entry (single pass TF32: 5e-3); after refinement the
 MinSR update matches the FP64 oracle's on the same samples to 1e-8 relative
-(the refinement residual is reported by the step)."""
+(the refinement residual is reported by the step), whether the solve runs in
+sample space (N_s x N_s) or in parameter space (N_p x N_p, the push-through
+form of the same update)."""
 import numpy as np
 import pytest
 
@@ -50,10 +52,10 @@ def test_gram_tc_against_fp64(nqs, Ns, P):
     assert err1 <= 5e-3 * scale and err1 > np.max(np.abs(T3 - ref))
 
 
-def minsr_mixed(nqs, sweeps, check=0):
+def minsr_mixed(nqs, sweeps, check=0, space=0, Ns=4096):
     from spin_based_neural_network_gb300 import abi
     Lx = Ly = 4
-    N, M, Ns = 16, 32, 4096
+    N, M = 16, 32
     cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, rbm_init_scale=0.3,
                               hamiltonian=1, rng_seed=4242, sr_diag_shift=1e-4, learning_rate=0.005)
     a = nqs.Ansatz(cfg, N)
@@ -62,7 +64,7 @@ def minsr_mixed(nqs, sweeps, check=0):
     rng = np.random.default_rng(11)
     batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(Ns)])
     nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=sweeps, gram_passes=3,
-                    mixed_check=check)
+                    mixed_check=check, mixed_space=space)
     try:
         info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True, log_amp_fn=m.log_amp_fn,
                                            user=m.user)
@@ -74,8 +76,13 @@ def minsr_mixed(nqs, sweeps, check=0):
     return info, E, delta, stats, Eo, do, io
 
 
-def test_mixed_minsr_against_fp64_oracle(nqs):
-    info, E, delta, stats, Eo, do, io = minsr_mixed(nqs, sweeps=3, check=1)
+# (N_s, space, sweeps): 4096 > N_p = 1120 picks parameter space, 512 < N_p picks
+# samples.  The N_p x N_p system keeps the small-eigenvalue directions that the
+# sample-space update projects out through O_c^T, so its refinement contracts
+# ~7x per sweep here against ~200x in sample space and needs more sweeps.
+@pytest.mark.parametrize("Ns,space,sweeps", [(4096, 0, 8), (4096, 1, 3), (512, 0, 3), (512, 2, 3)])
+def test_mixed_minsr_against_fp64_oracle(nqs, Ns, space, sweeps):
+    info, E, delta, stats, Eo, do, io = minsr_mixed(nqs, sweeps=sweeps, check=1, space=space, Ns=Ns)
     assert info.converged == 1 and stats.mixed_fallback == 0
     assert np.max(np.abs(E - Eo) / np.maximum(np.abs(Eo), 1.0)) < 1e-12
     err = np.linalg.norm(delta - do) / np.linalg.norm(do)
@@ -84,7 +91,14 @@ def test_mixed_minsr_against_fp64_oracle(nqs):
     assert 0 <= stats.delta_rel_err < 1e-8          # the step's own FP64 cross-check
 
 
-def test_refinement_contracts(nqs):
+@pytest.mark.parametrize("space", [1, 2])
+def test_refinement_contracts(nqs, space):
     """More sweeps, smaller residual: the refinement converges."""
-    r = [minsr_mixed(nqs, sweeps=s)[3].refine_residual for s in (0, 1, 2)]
+    r = [minsr_mixed(nqs, sweeps=s, space=space)[3].refine_residual for s in (0, 1, 2)]
     assert r[1] < r[0] and r[2] < r[1]
+
+
+def test_phase_times_reported(nqs):
+    stats = minsr_mixed(nqs, sweeps=2)[3]
+    ph = list(stats.phase_us)
+    assert ph[6] > 0 and all(p >= 0 for p in ph[:6]) and sum(ph[:6]) <= ph[6] * 1.01
