@@ -42,6 +42,8 @@ THERM = 512
 SHIFT = 1e-4
 LR = 0.005
 SEED = 2026
+SWEEPS = 5           # FP64 refinement sweeps: the parameter-space refinement error (~2e-7 after 5)
+                     # is below the FP32 estimator's own delta-theta error (~3e-6)
 METRIC = "MinSR steps/s (4x4 Heisenberg PBC, complex RBM alpha=2, N_s=4096)"
 
 
@@ -89,11 +91,14 @@ def init_params(P, seed=SEED):
     return np.random.default_rng(seed).normal(0.0, 0.01, size=P)
 
 
-def algorithmic_work(Ns, P):
+def algorithmic_work(Ns, P, sweeps=SWEEPS):
     """Per-kernel FLOPs of one MinSR step (2 flops per FMA) and the pipe that
     executes them.  gram: lower triangle incl. diagonal, N_s (N_s + 1) N_p;
-    the tensor-core Gram runs it three times (hi hi^T + hi lo^T + lo hi^T).
-    syrk: the trailing updates of the 32-wide panels, sum 2 * rest(rest+1)/2 * 32."""
+    the tensor-core Gram runs it three times (hi hi^T + hi lo^T + lo hi^T) on
+    the smaller system (n = min(N_s, N_p), K = the other dimension).
+    syrk: the trailing updates of the 32-wide FP64 panels, sum 2 * rest(rest+1)/2 * 32.
+    factor_refine: FP32 Cholesky n^3/3 + triangular inverse n^3/3 + per sweep
+    two triangular GEMVs (2 n^2) and the FP64 residual (4 N_s N_p)."""
     gram = Ns * (Ns + 1) * P
     syrk = 0
     nb = 32
@@ -101,8 +106,10 @@ def algorithmic_work(Ns, P):
         kb = min(nb, Ns - k0)
         rest = Ns - k0 - kb
         syrk += rest * (rest + 1) * kb
-    return {"gram_fp64": (gram, "fp64"), "chol_syrk": (syrk, "fp64"), "gram_tc": (3 * gram, "tensor"),
-            "chol32_syrk": (syrk, "fp32")}
+    n, k = min(Ns, P), max(Ns, P)
+    fr = 2 * n ** 3 / 3 + (sweeps + 1) * (2 * n * n + 4 * Ns * P)
+    return {"gram_fp64": (gram, "fp64"), "chol_syrk": (syrk, "fp64"), "gram_tc": (3 * n * (n + 1) * k, "tensor"),
+            "factor_refine": (fr, "fp32")}
 
 
 def device_shape(nqs):
@@ -239,14 +246,17 @@ def run_gpu(args):
     L = nqs.lib()
 
     prec = abi.PREC_FP64 if args.precision == "fp64" else abi.PREC_MIXED
-    base_opts = dict(square_pbc=1, precision=prec, refine_sweeps=3, gram_passes=3)
+    mixed = prec == abi.PREC_MIXED
+    base_opts = dict(square_pbc=1, precision=prec, refine_sweeps=SWEEPS, gram_passes=3,
+                     fp32_estimator=1 if mixed else 0)
     nqs.set_options(**base_opts)
     cfg = workload_cfg(abi)
     a = nqs.Ansatz(cfg, N_SITES)
     a.params[:] = init_params(a.P)
     m = nqs.Marshall(a.log_amp_fn, a.user, LX, LY)
     opts = nqs.options(num_chains=CHAINS, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=N_SITES // 2,
-                       lattice_x=LX, lattice_y=LY, square_pbc=1, precision=prec)
+                       lattice_x=LX, lattice_y=LY, square_pbc=1, precision=prec,
+                       fp32_estimator=1 if mixed else 0)
     s = nqs.Sampler(N_SITES, cfg, m.log_amp_fn, m.user, opts)
     s.thermalize()
 
@@ -272,8 +282,9 @@ def run_gpu(args):
     phases = None
     if prec == abi.PREC_MIXED:
         ph = nqs.last_step_stats().phase_us
-        phases = dict(zip(("diag_blocks", "panels", "trailing", "fwd_solves", "bwd_solves", "residuals",
-                           "total"), [round(ph[i], 1) for i in range(7)]))
+        phases = dict(zip(("diag_blocks", "panels", "trailing", "triangular_inverse", "triangular_solves",
+                           "rhs_and_residuals", "total", "diag_block_owner_work"),
+                          [round(ph[i], 1) for i in range(8)]))
     L.nqs_gpu_event_destroy(e0)
     L.nqs_gpu_event_destroy(e1)
     nqs.lib().nqs_gpu_synchronize()
@@ -325,7 +336,7 @@ def run_gpu(args):
     roof = roofline_of(top_name)
     kernels = {k: {"launches_per_step": v[0] / 3.0, "ms_per_step": v[1] / 3.0} for k, v in
                sorted(prof.items(), key=lambda kv: -kv[1][1])}
-    extra_roofs = {k: roofline_of(k) for k in ("gram_tc", "gram_fp64", "chol32_syrk", "chol_syrk")
+    extra_roofs = {k: roofline_of(k) for k in ("gram_tc", "gram_fp64", "factor_refine", "chol_syrk")
                    if k in prof and k != top_name}
 
     # delta-theta error of the mixed step against the FP64 solve on the same samples
@@ -336,8 +347,10 @@ def run_gpu(args):
         for _ in range(2):
             step()
             errs.append(nqs.last_step_stats().delta_rel_err)
-        delta_err = {"max_rel": max(errs), "refine_residual": nqs.last_step_stats().refine_residual,
-                     "refine_sweeps": nqs.last_step_stats().refine_sweeps}
+        st = nqs.last_step_stats()
+        delta_err = {"max_rel": max(errs), "refine_residual": st.refine_residual,
+                     "refine_sweeps": st.refine_sweeps, "energy_rel_err": st.energy_rel_err,
+                     "reference": "FP64 estimator + FP64 MinSR (sample space) on the same samples"}
         nqs.set_options(**base_opts)
 
     # the plain FP64 path on the same state, for the mixed / plain ratio
@@ -360,7 +373,8 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == abi.PREC_FP64 else
-            "mixed: tf32x3 tensor-core gram (fp32 accumulate), fp32 factor, f64 refinement; f64 sampling/E_loc/O",
+            "mixed: fp32 sampling/E_loc/O (product-form ratios), f64 centring and energy sums, "
+            "tf32x3 tensor-core gram (fp32 accumulate), fp32 factor + inverse, f64 refinement",
             "data": "synthetic (sampled configurations; parameters N(0,0.01^2) from a seed)",
             "config": {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES,
                        "hidden": M_HIDDEN, "num_params": P, "num_samples": NS, "chains": CHAINS,
@@ -368,7 +382,7 @@ def run_gpu(args):
                        "precision": args.precision,
                        "l2": "working set > L2 every step (O 37 MB FP64 + split 37 MB + Gram 67 MB FP32 "
                              "+ factor; FP64 path: Gram 134 MB)",
-                       "refine_sweeps": 3,
+                       "refine_sweeps": SWEEPS, "solve_space": "parameters (N_p < N_s)" if mixed else "samples",
                        "parallelism": "replicas x%d" % ws},
             "gpu_launches": launches,
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * P,

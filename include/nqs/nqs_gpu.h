@@ -61,7 +61,11 @@ typedef struct {
     int lattice_kagome;  /*   1: kagome cells, bonds of kagome_pbc = 1          */
     int mixed_check;     /* MIXED: also solve in FP64 on the same samples and
                           * report the delta-theta error (step stats) */
-    int reserved[3];
+    int fp32_estimator;  /* MIXED: RBM / cRBM local energies, Jacobian rows and
+                          * Metropolis acceptance in FP32 (product form of the
+                          * amplitude ratios); with mixed_check the FP64
+                          * estimator is rerun on the same samples */
+    int reserved[2];
 } nqs_gpu_options_t;
 
 /* Defaults: compat sampler, single flips, open lattices, FP64. */
@@ -170,6 +174,9 @@ typedef struct {
      * side and FP64 residuals, [6] total; [7] the part of [0] spent by the
      * owning CTAs on factoring and inverting the diagonal blocks */
     double phase_us[8];
+    /* MIXED with mixed_check and fp32_estimator: |<E> - <E>_fp64| / |<E>_fp64|
+     * on the same samples (-1 when not measured) */
+    double energy_rel_err;
 } nqs_gpu_step_stats_t;
 int nqs_gpu_last_step_stats(nqs_gpu_step_stats_t *out);
 

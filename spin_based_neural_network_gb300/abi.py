@@ -134,5 +134,6 @@ class GpuOptions(C.Structure):
         ("lattice_y", C.c_int),
         ("lattice_kagome", C.c_int),
         ("mixed_check", C.c_int),
-        ("reserved", C.c_int * 3),
+        ("fp32_estimator", C.c_int),
+        ("reserved", C.c_int * 2),
     ]

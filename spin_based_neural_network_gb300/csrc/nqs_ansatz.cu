@@ -73,14 +73,27 @@ static void init_params(const nqs_config_t *cfg, int kind, int N, int M, double 
 }
 
 // Transposed weight copies: RBM/cRBM W[h][i] -> wt[i][h]; MLP W1 -> W1^T, W2 -> W2^T.
-__global__ void k_derive(DevAnsatz a, double *wtr, double *wti) {
+// RBM / cRBM also get the FP32 tables of the mixed-precision estimator:
+// f32 = [W^T | cosh(2 W^T) | sinh(2 W^T)] ([N][M] each), a [N], b [M], complex.
+__global__ void k_derive(DevAnsatz a, double *wtr, double *wti, float2 *f32) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int N = a.N, M = a.M;
     if (a.kind == KIND_RBM || a.kind == KIND_CRBM) {
         if (t >= (long)M * N) return;
+        const bool cx = a.kind == KIND_CRBM;
+        const long Pr = crbm_pr(a), NM = (long)N * M;
         int h = (int)(t / N), i = (int)(t % N);
-        wtr[(long)i * M + h] = a.p[N + M + t];
-        if (a.kind == KIND_CRBM) wti[(long)i * M + h] = a.p[crbm_pr(a) + N + M + t];
+        const double x = a.p[N + M + t], y = cx ? a.p[Pr + N + M + t] : 0.0;
+        wtr[(long)i * M + h] = x;
+        if (cx) wti[(long)i * M + h] = y;
+        double s2y, c2y;
+        sincos(2.0 * y, &s2y, &c2y);
+        const double c2x = cosh(2.0 * x), s2x = sinh(2.0 * x);
+        f32[(long)i * M + h] = make_float2((float)x, (float)y);
+        f32[NM + (long)i * M + h] = make_float2((float)(c2x * c2y), (float)(s2x * s2y));
+        f32[2 * NM + (long)i * M + h] = make_float2((float)(s2x * c2y), (float)(c2x * s2y));
+        if (t < N) f32[3 * NM + t] = make_float2((float)a.p[t], cx ? (float)a.p[Pr + t] : 0.f);
+        if (t < M) f32[3 * NM + N + t] = make_float2((float)a.p[N + t], cx ? (float)a.p[Pr + N + t] : 0.f);
     } else if (a.kind == KIND_MLP) {
         long nW1 = (long)M * N;
         if (t < nW1) {
@@ -103,6 +116,13 @@ DevAnsatz ansatz_dev(const Ansatz *a) {
     d.p = a->d_params.p;
     d.wtr = a->d_wtr.p;
     d.wti = a->d_wti.p;
+    const bool rbm = a->kind == KIND_RBM || a->kind == KIND_CRBM;
+    const long NM = (long)a->N * a->M;
+    d.w32 = rbm ? a->d_f32.p : nullptr;
+    d.ch32 = rbm ? a->d_f32.p + NM : nullptr;
+    d.sh32 = rbm ? a->d_f32.p + 2 * NM : nullptr;
+    d.a32 = rbm ? a->d_f32.p + 3 * NM : nullptr;
+    d.b32 = rbm ? a->d_f32.p + 3 * NM + a->N : nullptr;
     return d;
 }
 
@@ -111,7 +131,7 @@ bool ansatz_refresh_derived(Ansatz *a) {
     long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * a->M : (long)a->M * a->N;
     NQS_LAUNCH("derive_weights");
     k_derive<<<(unsigned)((work + 255) / 256), 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
-                                                                        a->d_wti.p);
+                                                                        a->d_wti.p, a->d_f32.p);
     return NQS_CUDA(cudaGetLastError());
 }
 
@@ -551,7 +571,8 @@ nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
     if (!NQS_CUDA(cudaMallocHost(&a->h_params, bytes)) || !(a->h_shadow = (double *)malloc(bytes)) ||
         !a->d_params.ensure((size_t)a->P) ||
         !a->d_wtr.ensure((size_t)num_sites * (M ? M : 1) + (kind == KIND_MLP ? 0 : 0)) ||
-        !a->d_wti.ensure(kind == KIND_MLP ? (size_t)M * M : (size_t)num_sites * (M ? M : 1))) {
+        !a->d_wti.ensure(kind == KIND_MLP ? (size_t)M * M : (size_t)num_sites * (M ? M : 1)) ||
+        !a->d_f32.ensure(3 * (size_t)num_sites * (M ? M : 1) + num_sites + (M ? M : 1))) {
         nqs_ansatz_free((nqs_ansatz_t *)a);
         return nullptr;
     }

@@ -111,6 +111,10 @@ struct DevAnsatz {
     const double *p;     // device params, upstream layout
     const double *wtr;   // [N][M] real weights transposed (RBM, cRBM); MLP: W1^T
     const double *wti;   // [N][M] imaginary weights transposed (cRBM); MLP: W2^T [M][M]
+    // FP32 tables of the RBM / cRBM (complex, imaginary part 0 for the RBM),
+    // rebuilt with the transposed copies: W^T [N][M], cosh(2 W^T), sinh(2 W^T)
+    // [N][M], visible bias [N], hidden bias [M]
+    const float2 *w32, *ch32, *sh32, *a32, *b32;
 };
 
 struct DevAmp {
@@ -142,6 +146,7 @@ struct Ansatz {
     double *h_params = nullptr;     // pinned host mirror (returned by params_raw)
     double *h_shadow = nullptr;     // last value known to be on the device
     DevBuf<double> d_params, d_wtr, d_wti;
+    DevBuf<float2> d_f32;           // RBM / cRBM FP32 tables (see DevAnsatz)
     bool dev_valid = false;
 };
 
@@ -163,7 +168,11 @@ uint64_t pack_spins(const int *s, int N);
 // kernels exported across translation units
 bool launch_log_amp(const DevAmp &A, const uint64_t *bits, int B, double *la, double *ar);
 bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B,
-                            double *E_re, double *E_im, double *O, double *O_im, int grad_mode);
+                            double *E_re, double *E_im, double *O, double *O_im, int grad_mode,
+                            bool fp32 = false);
+// True when the FP32 estimator / sampler can run this program (RBM or cRBM
+// with Marshall layers, no symmetry projection).
+bool fp32_capable(const DevAmp &A);
 bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, double *O, double *Oi);
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);

@@ -330,6 +330,185 @@ k_local_rbm(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, double
     }
 }
 
+// ---------------------------------------------------------------- FP32 estimator
+// Mixed-precision variant of k_local_rbm for the RBM / cRBM.  A flip of site u
+// (and v) moves theta_h by delta_h = 2 s_u W_hu (+ 2 s_v W_hv), and
+//   cosh(theta_h - delta_h) / cosh(theta_h) = cosh(delta_h) - tanh(theta_h) sinh(delta_h),
+// so with t_h = tanh(theta_h) once per sample and cosh / sinh(2 W) tabulated
+// once per step, the amplitude ratio of a connected configuration is a
+// product of M complex factors (a few FP32 multiply-adds each) times the
+// visible-bias exponential and the Marshall sign; no transcendental per
+// hidden unit.  For a pair flip cosh / sinh(delta_u + delta_v) follow from the
+// addition theorems.  Local energies are accumulated in FP32 and stored in FP64;
+// the Jacobian row is written from the FP32 tanh values.
+
+// tanh(x + i y) = (sinh 2x + i sin 2y) / (cosh 2x + cos 2y), with
+// sinh / cosh from expm1 so that small |x| keeps its relative accuracy.
+__device__ __forceinline__ float2 ctanh32(float x, float y) {
+    if (fabsf(x) > 9.f) return make_float2(x > 0.f ? 1.f : -1.f, 0.f);   // |error| < 1e-7
+    const float e = expm1f(2.f * x);
+    const float ch = 1.f + e * e / (2.f * (1.f + e)), sh = 0.5f * (e + e / (1.f + e));
+    float s2, c2;
+    sincosf(2.f * y, &s2, &c2);
+    const float den = ch + c2;
+    return make_float2(sh / den, s2 / den);
+}
+
+__device__ __forceinline__ float2 cmul32(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// theta_h (FP32, ascending i) and t_h = tanh(theta_h) of hidden unit h.
+template <bool CPLX>
+__device__ __forceinline__ void rbm_theta32(const DevAnsatz &a, uint64_t s, int h, float2 &th, float2 &t) {
+    float xr = a.b32[h].x, xi = a.b32[h].y;
+    for (int i = 0; i < a.N; i++) {
+        const float sp = (float)spin_of(s, i);
+        const float2 w = a.w32[(long)i * a.M + h];
+        xr = fmaf(sp, w.x, xr);
+        if (CPLX) xi = fmaf(sp, w.y, xi);
+    }
+    th = make_float2(xr, CPLX ? xi : 0.f);
+    t = CPLX ? ctanh32(xr, xi) : make_float2(tanhf(xr), 0.f);
+}
+
+// cosh(delta_h) - t_h sinh(delta_h) for the flip of u (and v >= 0).
+template <bool CPLX>
+__device__ __forceinline__ float2 flip_factor32(const DevAnsatz &a, int h, int u, float su, int v, float sv,
+                                                float2 t) {
+    const long M = a.M;
+    float2 C = a.ch32[u * M + h], S = a.sh32[u * M + h];
+    S.x *= su;
+    S.y *= su;
+    if (v >= 0) {
+        const float2 Cv = a.ch32[v * M + h];
+        float2 Sv = a.sh32[v * M + h];
+        Sv.x *= sv;
+        Sv.y *= sv;
+        const float2 c1 = cmul32(C, Cv), c2 = cmul32(S, Sv), s1 = cmul32(S, Cv), s2 = cmul32(C, Sv);
+        C = make_float2(c1.x + c2.x, c1.y + c2.y);
+        S = make_float2(s1.x + s2.x, s1.y + s2.y);
+    }
+    if (!CPLX) return make_float2(C.x - t.x * S.x, 0.f);
+    const float2 tS = cmul32(t, S);
+    return make_float2(C.x - tS.x, C.y - tS.y);
+}
+
+template <int J, bool CPLX>
+__global__ void __launch_bounds__(32 * kWarps)
+k_local_rbm32(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, double *__restrict__ Er,
+              double *__restrict__ Ei, double *__restrict__ O, double *__restrict__ Oi, int grad_mode) {
+    extern __shared__ double sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarps + warp;
+    if (b >= B) return;
+    const DevAnsatz &a = A.a;
+    const int N = a.N, M = a.M;
+    const uint64_t s = bits[b];
+    float2 th[J], tt[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const int h = lane + 32 * j;
+        th[j] = tt[j] = make_float2(0.f, 0.f);
+        if (h < M) rbm_theta32<CPLX>(a, s, h, th[j], tt[j]);
+    }
+    const int par0 = marshall_count(A, s);
+
+    // psi(s') / psi(s) for s' = s with sites u (and v >= 0) flipped
+    auto ratio = [&](int u, int v, float &rre, float &rim) {
+        const float su = (float)spin_of(s, u), sv = v >= 0 ? (float)spin_of(s, v) : 0.f;
+        float2 p = make_float2(1.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int h = lane + 32 * j;
+            if (h < M) p = cmul32(p, flip_factor32<CPLX>(a, h, u, su, v, sv, tt[j]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float2 q = make_float2(__shfl_xor_sync(0xffffffffu, p.x, o), __shfl_xor_sync(0xffffffffu, p.y, o));
+            p = cmul32(p, q);
+        }
+        float dvr = -2.f * su * a.a32[u].x, dvi = -2.f * su * a.a32[u].y;
+        uint64_t s2 = s ^ (1ull << u);
+        if (v >= 0) {
+            dvr -= 2.f * sv * a.a32[v].x;
+            dvi -= 2.f * sv * a.a32[v].y;
+            s2 ^= 1ull << v;
+        }
+        const float mag = expf(dvr);
+        float sn = 0.f, cs = 1.f;
+        if (CPLX) sincosf(dvi, &sn, &cs);
+        float2 e = make_float2(mag * cs, mag * sn);
+        if ((marshall_count(A, s2) - par0) & 1) e = make_float2(-e.x, -e.y);
+        const float2 r = cmul32(p, e);
+        rre = r.x;
+        rim = r.y;
+    };
+
+    float e_re, e_im;
+    if (H.kind == NQS_HAM_TFIM) {
+        float diag = 0.f, ore = 0.f, oim = 0.f;
+        for (int k = 0; k < H.nb1; k++)
+            diag += -(float)H.J * (float)(spin_of(s, H.b1[2 * k]) * spin_of(s, H.b1[2 * k + 1]));
+        for (int i = 0; i < N; i++) {
+            float r, q;
+            ratio(i, -1, r, q);
+            ore += -(float)H.Gamma * r;
+            oim += -(float)H.Gamma * q;
+        }
+        e_re = diag + ore;
+        e_im = oim;
+    } else {
+        float diag = 0.f, ore = 0.f, oim = 0.f;
+        for (int k = 0; k < H.nb1; k++) {
+            const int u = H.b1[2 * k], v = H.b1[2 * k + 1];
+            const int su = spin_of(s, u), sv = spin_of(s, v);
+            diag += 0.25f * (float)H.Jz * (float)(su * sv);
+            if (su != sv) {
+                float r, q;
+                ratio(u, v, r, q);
+                ore += 0.5f * (float)H.Jxy * r;
+                oim += 0.5f * (float)H.Jxy * q;
+            }
+        }
+        e_re = diag + ore;
+        e_im = oim;
+        if (H.nb2 > 0) {
+            float d2 = 0.f, r2 = 0.f, i2 = 0.f;
+            for (int k = 0; k < H.nb2; k++) {
+                const int u = H.b2[2 * k], v = H.b2[2 * k + 1];
+                const int su = spin_of(s, u), sv = spin_of(s, v);
+                d2 += 0.25f * (float)H.J2 * (float)(su * sv);
+                if (su != sv) {
+                    float r, q;
+                    ratio(u, v, r, q);
+                    r2 += 0.5f * (float)H.J2 * r;
+                    i2 += 0.5f * (float)H.J2 * q;
+                }
+            }
+            e_re = e_re + d2 + r2;
+            e_im = e_im + i2;
+        }
+    }
+    if (lane == 0) {
+        if (Er) Er[b] = (double)e_re;
+        if (Ei) Ei[b] = (double)e_im;
+    }
+    if (grad_mode) {
+        double *tr = sm + warp * 2 * M, *ti = tr + M;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int h = lane + 32 * j;
+            if (h < M) {
+                tr[h] = (double)tt[j].x;
+                ti[h] = (double)tt[j].y;
+            }
+        }
+        __syncwarp();
+        rbm_row_from_t(a, s, grad_mode, O + (size_t)b * a.P, Oi ? Oi + (size_t)b * a.P : nullptr, tr, ti);
+    }
+}
+
 // Generic estimator: any program (symmetry projection, MLP).  Every connected
 // configuration is evaluated from scratch, as upstream does.
 __global__ void __launch_bounds__(32 * kWarps)
@@ -407,15 +586,23 @@ k_local_generic(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, do
 
 template <int J, bool C>
 static void launch_rbm(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er,
-                       double *Ei, double *O, double *Oi, int gm) {
+                       double *Ei, double *O, double *Oi, int gm, bool f32) {
     size_t smem = gm ? sizeof(double) * 2 * A.a.M * kWarps : 0;
-    k_local_rbm<J, C><<<(B + kWarps - 1) / kWarps, 32 * kWarps, smem, ctx().stream>>>(A, H, bits, B, Er,
-                                                                                    Ei, O, Oi, gm,
-                                                                                    nullptr);
+    if (f32)
+        k_local_rbm32<J, C><<<(B + kWarps - 1) / kWarps, 32 * kWarps, smem, ctx().stream>>>(A, H, bits, B, Er,
+                                                                                          Ei, O, Oi, gm);
+    else
+        k_local_rbm<J, C><<<(B + kWarps - 1) / kWarps, 32 * kWarps, smem, ctx().stream>>>(A, H, bits, B, Er,
+                                                                                        Ei, O, Oi, gm,
+                                                                                        nullptr);
+}
+
+bool fp32_capable(const DevAmp &A) {
+    return A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM) && A.a.w32 != nullptr;
 }
 
 bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er,
-                            double *Ei, double *O, double *Oi, int grad_mode) {
+                            double *Ei, double *O, double *Oi, int grad_mode, bool fp32) {
     if (A.a.N != H.N) {
         set_error("ansatz has %d sites, lattice has %d", A.a.N, H.N);
         return false;
@@ -424,11 +611,12 @@ bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bi
     if (fused) {
         int J = (A.a.M + 31) / 32;
         bool c = A.a.kind == KIND_CRBM;
-        NQS_LAUNCH("local_estimator");
+        const bool f32 = fp32 && fp32_capable(A);
+        NQS_LAUNCH(f32 ? "local_estimator_fp32" : "local_estimator");
 #define NQS_CASE(JJ)                                                                   \
     case JJ:                                                                           \
-        if (c) launch_rbm<JJ, true>(A, H, bits, B, Er, Ei, O, Oi, grad_mode);          \
-        else launch_rbm<JJ, false>(A, H, bits, B, Er, Ei, O, Oi, grad_mode);           \
+        if (c) launch_rbm<JJ, true>(A, H, bits, B, Er, Ei, O, Oi, grad_mode, f32);     \
+        else launch_rbm<JJ, false>(A, H, bits, B, Er, Ei, O, Oi, grad_mode, f32);      \
         break;
         switch (J) {
             NQS_CASE(1) NQS_CASE(2) NQS_CASE(3) NQS_CASE(4) NQS_CASE(5) NQS_CASE(6) NQS_CASE(7) NQS_CASE(8)

@@ -177,6 +177,162 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm(SampleArgs S, DevAmp A)
     }
 }
 
+// ---------------------------------------------------------------- FP32 chains
+// Mixed-precision variant (Philox chains only).  The acceptance needs
+// log|psi'/psi| = sum_h log|cosh(delta_h) - t_h sinh(delta_h)| + Re(visible
+// change), with t_h = tanh(theta_h) kept per chain in FP32 and cosh / sinh of
+// the weights tabulated once per step (one fast log per hidden unit and
+// proposal instead of three FP64 transcendentals); an accepted move updates
+// theta additively and recomputes t.  The uniform is drawn from the same
+// Philox word as in the FP64 chain, as a 24-bit float.
+template <int MOVE, typename Eval, typename Commit>
+__device__ __forceinline__ void run_chain32(const SampleArgs &S, int c, uint64_t &s, Eval eval, Commit commit,
+                                            unsigned long long &acc, unsigned long long &pro) {
+    const int lane = threadIdx.x & 31;
+    const int per = S.decor > 0 ? S.decor : 1;
+    for (int t = 0; t < S.total; t++) {
+        int u, v = -1;
+        const uint64_t m = S.move0 + (uint64_t)t;
+        const uint4 r = philox4x32(make_uint4((uint32_t)c, (uint32_t)m, (uint32_t)(m >> 32), 0u),
+                                   make_uint2((uint32_t)S.seed, (uint32_t)(S.seed >> 32)));
+        if (MOVE == NQS_GPU_MOVE_EXCHANGE) {
+            const int k = (int)(((uint64_t)r.x * (uint64_t)S.nb) >> 32);
+            u = S.bonds[2 * k];
+            v = S.bonds[2 * k + 1];
+        } else {
+            u = (int)(((uint64_t)r.x * (uint64_t)S.N) >> 32);
+        }
+        pro++;
+        const bool parallel = v >= 0 && (((s >> u) ^ (s >> v)) & 1ull) == 0;
+        if (!parallel) {
+            const float lr = 2.f * eval(u, v);
+            bool accept = lr >= 0.f;
+            if (!accept) {
+                const float uni = ((float)(r.z >> 8) + 0.5f) * (1.f / 16777216.f);
+                accept = __logf(uni) < lr;
+            }
+            if (accept) {
+                acc++;
+                commit(u, v);
+                s ^= 1ull << u;
+                if (v >= 0) s ^= 1ull << v;
+            }
+        }
+        if (t >= S.skip && ((t - S.skip + 1) % per) == 0) {
+            const long idx = (long)((t - S.skip + 1) / per - 1) * S.C + c;
+            if (idx < S.n_out && lane == 0) S.out[idx] = s;
+        }
+    }
+}
+
+__device__ __forceinline__ float2 ctanh32s(float x, float y) {
+    if (fabsf(x) > 9.f) return make_float2(x > 0.f ? 1.f : -1.f, 0.f);
+    const float e = expm1f(2.f * x);
+    const float ch = 1.f + e * e / (2.f * (1.f + e)), sh = 0.5f * (e + e / (1.f + e));
+    float s2, c2;
+    sincosf(2.f * y, &s2, &c2);
+    const float den = ch + c2;
+    return make_float2(sh / den, s2 / den);
+}
+
+template <int J, bool CPLX, int MOVE>
+__global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp A) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kSW + (threadIdx.x >> 5);
+    if (c >= S.C) return;
+    const DevAnsatz &a = A.a;
+    const int M = a.M;
+    const long Ml = M;
+    uint64_t s = S.bits[c];
+    float thr[J], thi[J], tr[J], ti[J], nr[J], ni[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const int h = lane + 32 * j;
+        thr[j] = thi[j] = tr[j] = ti[j] = 0.f;
+        if (h < M) {
+            float xr = a.b32[h].x, xi = a.b32[h].y;
+            for (int i = 0; i < a.N; i++) {
+                const float sp = (float)spin_of(s, i);
+                const float2 w = a.w32[(long)i * Ml + h];
+                xr = fmaf(sp, w.x, xr);
+                if (CPLX) xi = fmaf(sp, w.y, xi);
+            }
+            thr[j] = xr;
+            thi[j] = CPLX ? xi : 0.f;
+            if (CPLX) {
+                const float2 t = ctanh32s(xr, xi);
+                tr[j] = t.x;
+                ti[j] = t.y;
+            } else {
+                tr[j] = tanhf(xr);
+            }
+        }
+    }
+    auto eval = [&](int u, int v) -> float {
+        const float su = (float)spin_of(s, u), sv = v >= 0 ? (float)spin_of(s, v) : 0.f;
+        float lg = 0.f;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int h = lane + 32 * j;
+            nr[j] = thr[j];
+            ni[j] = thi[j];
+            if (h < M) {
+                const float2 wu = a.w32[u * Ml + h];
+                float2 C = a.ch32[u * Ml + h], Sh = a.sh32[u * Ml + h];
+                Sh.x *= su;
+                Sh.y *= su;
+                nr[j] -= 2.f * su * wu.x;
+                if (CPLX) ni[j] -= 2.f * su * wu.y;
+                if (v >= 0) {
+                    const float2 wv = a.w32[v * Ml + h], Cv = a.ch32[v * Ml + h];
+                    float2 Sv = a.sh32[v * Ml + h];
+                    Sv.x *= sv;
+                    Sv.y *= sv;
+                    nr[j] -= 2.f * sv * wv.x;
+                    if (CPLX) ni[j] -= 2.f * sv * wv.y;
+                    const float cr = C.x * Cv.x - C.y * Cv.y + Sh.x * Sv.x - Sh.y * Sv.y;
+                    const float ci = C.x * Cv.y + C.y * Cv.x + Sh.x * Sv.y + Sh.y * Sv.x;
+                    const float sr = Sh.x * Cv.x - Sh.y * Cv.y + C.x * Sv.x - C.y * Sv.y;
+                    const float si = Sh.x * Cv.y + Sh.y * Cv.x + C.x * Sv.y + C.y * Sv.x;
+                    C = make_float2(cr, ci);
+                    Sh = make_float2(sr, si);
+                }
+                const float fr = C.x - (tr[j] * Sh.x - ti[j] * Sh.y);
+                const float fi = CPLX ? C.y - (tr[j] * Sh.y + ti[j] * Sh.x) : 0.f;
+                lg += 0.5f * __logf(fr * fr + fi * fi);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) lg += __shfl_xor_sync(0xffffffffu, lg, o);
+        lg -= 2.f * su * a.a32[u].x;
+        if (v >= 0) lg -= 2.f * sv * a.a32[v].x;
+        return lg;
+    };
+    auto commit = [&](int, int) {
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            thr[j] = nr[j];
+            thi[j] = ni[j];
+            if (lane + 32 * j < M) {
+                if (CPLX) {
+                    const float2 t = ctanh32s(nr[j], ni[j]);
+                    tr[j] = t.x;
+                    ti[j] = t.y;
+                } else {
+                    tr[j] = tanhf(nr[j]);
+                }
+            }
+        }
+    };
+    unsigned long long acc = 0, pro = 0;
+    run_chain32<MOVE>(S, c, s, eval, commit, acc, pro);
+    if (lane == 0) {
+        S.bits[c] = s;
+        atomicAdd(&S.counts[0], acc);
+        atomicAdd(&S.counts[1], pro);
+    }
+}
+
 // Any other program (symmetry projection, mean field, MLP): full evaluation of
 // every proposal, as upstream.
 template <int RNG, int MOVE>
@@ -234,10 +390,29 @@ __global__ void k_chain_init(int C, int N, uint64_t seed, int n_down, uint64_t *
 }
 
 template <int RNG, int MOVE>
-static bool dispatch(const SampleArgs &S, const DevAmp &A) {
+static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32) {
     dim3 grid((S.C + kSW - 1) / kSW), block(32 * kSW);
     cudaStream_t st = ctx().stream;
     const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
+    if (f32 && RNG == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
+        const int J = (A.a.M + 31) / 32;
+        const bool cx = A.a.kind == KIND_CRBM;
+        NQS_LAUNCH("sampler_fp32");
+#define NQS_FCASE(JJ)                                                             \
+    case JJ:                                                                      \
+        if (cx) k_sample_rbm32<JJ, true, MOVE><<<grid, block, 0, st>>>(S, A);     \
+        else k_sample_rbm32<JJ, false, MOVE><<<grid, block, 0, st>>>(S, A);       \
+        break;
+        switch (J) {
+            NQS_FCASE(1) NQS_FCASE(2) NQS_FCASE(3) NQS_FCASE(4) NQS_FCASE(5) NQS_FCASE(6) NQS_FCASE(7)
+            NQS_FCASE(8)
+            default:
+                set_error("hidden width %d unsupported", A.a.M);
+                return false;
+        }
+#undef NQS_FCASE
+        return NQS_CUDA(cudaGetLastError());
+    }
     if (fused) {
         int J = (A.a.M + 31) / 32;
         bool cx = A.a.kind == KIND_CRBM;
@@ -287,12 +462,13 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
     S.counts = sm->d_counts.p;
     if (S.total <= 0) return true;
     bool ok;
+    const bool f32 = sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator;
     if (sm->opts.rng == NQS_GPU_RNG_XORSHIFT_COMPAT)
-        ok = dispatch<NQS_GPU_RNG_XORSHIFT_COMPAT, NQS_GPU_MOVE_SINGLE_FLIP>(S, A);
+        ok = dispatch<NQS_GPU_RNG_XORSHIFT_COMPAT, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, false);
     else if (sm->opts.move == NQS_GPU_MOVE_EXCHANGE)
-        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_EXCHANGE>(S, A);
+        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_EXCHANGE>(S, A, f32);
     else
-        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_SINGLE_FLIP>(S, A);
+        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, f32);
     sm->move_counter += (uint64_t)S.total;
     return ok;
 }

@@ -578,38 +578,6 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     } else {
         if (!upload_spins(in.host_batch, Ns, H.N, &bits)) return -1;
     }
-    // 2. local energies + Jacobian rows (fused when the program allows)
-    bool fused_grad = !grad_sym && A.G == 0;
-    if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
-                                fused_grad ? 1 : 0))
-        return -1;
-    if (!fused_grad) {
-        if (grad_sym) {
-            if (!launch_symproj_gradient(Ag, bits, Ns, w.O.p)) return -1;
-        } else if (!launch_gradient(Ag.a, bits, Ns, 1, w.O.p, nullptr)) {
-            return -1;
-        }
-    }
-    // 3. statistics
-    {
-        NQS_LAUNCH("energy_stats");
-        k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
-    }
-    NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
-    dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
-    int converged = 0, cg_iters = 0;
-    if (in.minsr) {
-        if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns)) return -1;
-        {
-            NQS_LAUNCH("col_mean");
-            k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
-        }
-        const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
-        nqs_gpu_step_stats_t &ss = step_stats();
-        ss.refine_residual = 0.0;
-        ss.refine_sweeps = 0;
-        ss.mixed_fallback = 0;
-        ss.delta_rel_err = -1.0;
         // FP64 factorisation and solve of (T + shift I) y = eps on the centred O,
         // with the upstream retry semantics; writes y_out.
         auto fp64_solve = [&](double *y_out, int *conv) -> int {
@@ -663,6 +631,61 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         }
         return 0;
         };
+    const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
+    const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && fp32_capable(A);
+    nqs_gpu_step_stats_t &ss = step_stats();
+    ss.energy_rel_err = -1.0;
+    double e64 = 0.0;
+    bool have64 = false;
+    if (in.minsr && fp32est && c.opts.mixed_check) {
+        // reference for the check: the FP64 estimator, statistics and FP64
+        // MinSR solve on the same samples
+        if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns) || !w.y64.ensure(Ns) ||
+            !w.d64.ensure(P))
+            return -1;
+        if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, w.O.p, nullptr, 1, false)) return -1;
+        dim3 cb0(32, 8), cg0((unsigned)((P + 31) / 32));
+        k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
+        k_col_stats<<<cg0, cb0, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
+        k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+        int conv64 = 0;
+        if (fp64_solve(w.y64.p, &conv64) != 0) return -1;
+        k_col_dot<<<cg0, cb0, 0, st>>>(w.O.p, Ns, P, w.y64.p, 1.0 / (double)Ns, w.d64.p);
+        if (!NQS_CUDA(cudaMemcpyAsync(&e64, w.scal.p + S_EMEAN, sizeof(double), cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaStreamSynchronize(st)))
+            return -1;
+        have64 = true;
+    }
+    // 2. local energies + Jacobian rows (fused when the program allows)
+    bool fused_grad = !grad_sym && A.G == 0;
+    if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
+                                fused_grad ? 1 : 0, fp32est))
+        return -1;
+    if (!fused_grad) {
+        if (grad_sym) {
+            if (!launch_symproj_gradient(Ag, bits, Ns, w.O.p)) return -1;
+        } else if (!launch_gradient(Ag.a, bits, Ns, 1, w.O.p, nullptr)) {
+            return -1;
+        }
+    }
+    // 3. statistics
+    {
+        NQS_LAUNCH("energy_stats");
+        k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
+    }
+    NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
+    dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
+    int converged = 0, cg_iters = 0;
+    if (in.minsr) {
+        if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns)) return -1;
+        {
+            NQS_LAUNCH("col_mean");
+            k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
+        }
+        ss.refine_residual = 0.0;
+        ss.refine_sweeps = 0;
+        ss.mixed_fallback = 0;
+        ss.delta_rel_err = -1.0;
         bool solved = false, have_delta = false;
         if (mixed) {
             // centring happens inside the split kernel of the mixed solve
@@ -693,11 +716,21 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y.p, 1.0 / (double)Ns, w.delta.p);
         }
         if (mixed && solved && c.opts.mixed_check) {
-            // the FP64 solve on the same centred Jacobian, for the delta-theta error
-            if (!w.y64.ensure(Ns) || !w.d64.ensure(P)) return -1;
-            int conv64 = 0;
-            if (fp64_solve(w.y64.p, &conv64) != 0) return -1;
-            k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y64.p, 1.0 / (double)Ns, w.d64.p);
+            // the FP64 solve on the same centred Jacobian (or, with the FP32
+            // estimator, the whole FP64 step computed above), for the
+            // delta-theta error
+            if (!have64) {
+                if (!w.y64.ensure(Ns) || !w.d64.ensure(P)) return -1;
+                int conv64 = 0;
+                if (fp64_solve(w.y64.p, &conv64) != 0) return -1;
+                k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y64.p, 1.0 / (double)Ns, w.d64.p);
+            } else {
+                double em = 0.0;
+                if (!NQS_CUDA(cudaMemcpyAsync(&em, w.scal.p + S_EMEAN, sizeof(double), cudaMemcpyDeviceToHost, st)) ||
+                    !NQS_CUDA(cudaStreamSynchronize(st)))
+                    return -1;
+                ss.energy_rel_err = fabs(em - e64) / fmax(fabs(e64), 1e-300);
+            }
             std::vector<double> a((size_t)P), b((size_t)P);
             if (!NQS_CUDA(cudaMemcpyAsync(a.data(), w.delta.p, sizeof(double) * P, cudaMemcpyDeviceToHost, st)) ||
                 !NQS_CUDA(cudaMemcpyAsync(b.data(), w.d64.p, sizeof(double) * P, cudaMemcpyDeviceToHost, st)) ||

@@ -345,7 +345,7 @@ class StepStats(C.Structure):
     _fields_ = [("tau_int", C.c_double), ("ess", C.c_double), ("refine_residual", C.c_double),
                 ("refine_sweeps", C.c_int), ("chol_retry", C.c_int), ("chol_fail_col", C.c_int),
                 ("gpu_launches", C.c_int), ("delta_rel_err", C.c_double), ("mixed_fallback", C.c_int),
-                ("pad_", C.c_int), ("phase_us", C.c_double * 8)]
+                ("pad_", C.c_int), ("phase_us", C.c_double * 8), ("energy_rel_err", C.c_double)]
 
 
 def last_step_stats():

@@ -1,0 +1,113 @@
+"""Mixed-precision estimator and sampler: the FP32 product form of the RBM /
+cRBM amplitude ratios (cosh(theta - d) / cosh(theta) = cosh d - tanh(theta)
+sinh d) against the FP64 oracle and the FP64 GPU path.
+
+Bars: local energies within 2e-5 of the largest |E_loc| (FP32 rounding of a
+sum of ~16 ratios); the step's own end-to-end check (the FP64 estimator and
+FP64 MinSR rerun on the same samples) reports the energy and delta-theta
+errors; FP32 and FP64 chains draw the same Philox words, so they take the same
+decisions except where |log u - 2 log|psi'/psi|| falls below the FP32
+rounding, and nearly all chains end in the same configuration."""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nqs():
+    import spin_based_neural_network_gb300 as pkg
+    pkg.build()
+    from spin_based_neural_network_gb300 import nqs as N
+    N.set_options()
+    return N
+
+
+def heis_case(abi, Ns, seed=11):
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=32, rbm_init_scale=0.3,
+                              hamiltonian=1, rng_seed=4242, sr_diag_shift=1e-4, learning_rate=0.005)
+    rng = np.random.default_rng(seed)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(Ns)])
+    return cfg, batch
+
+
+def test_fp32_step_against_fp64(nqs):
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    cfg, batch = heis_case(abi, 2048)
+    a = nqs.Ansatz(cfg, 16)
+    p0 = a.params.copy()
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=8, gram_passes=3, mixed_check=1,
+                    fp32_estimator=1)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True, log_amp_fn=m.log_amp_fn,
+                                           user=m.user)
+        st = nqs.last_step_stats()
+    finally:
+        nqs.set_options()
+    amp = O.Amp(O.OR_CRBM, 16, 32, p0.copy(), [("marshall", Lx, Ly)])
+    Eo, do, io = O.minsr_step(O.ham(O.OR_HEIS, Lx, Ly, pbc=1), amp, batch, 1e-4, 0.005)
+    assert info.converged == 1
+    assert np.max(np.abs(E - Eo)) <= 2e-5 * np.max(np.abs(Eo))
+    assert abs(info.mean_energy - io.mean_energy) <= 1e-6 * abs(io.mean_energy)
+    assert 0 <= st.energy_rel_err <= 1e-6
+    err = np.linalg.norm(delta - do) / np.linalg.norm(do)
+    print("fp32 estimator: energy rel err %.2e, delta err vs oracle %.2e (step's own check %.2e)"
+          % (st.energy_rel_err, err, st.delta_rel_err))
+    assert err < 1e-3 and 0 <= st.delta_rel_err < 1e-3
+    # the step's own check and the oracle see the same error
+    assert st.delta_rel_err == pytest.approx(err, rel=0.05, abs=1e-9)
+
+
+def test_fp32_real_rbm_tfim_energies(nqs):
+    from spin_based_neural_network_gb300 import abi
+    N = 16
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=16, rbm_init_scale=0.2, hamiltonian=0,
+                              j_coupling=1.0, transverse_field=1.0, rng_seed=7, sr_diag_shift=1e-3,
+                              learning_rate=0.01)
+    rng = np.random.default_rng(3)
+    batch = rng.choice(np.array([-1, 1], np.int32), size=(512, N))
+    a = nqs.Ansatz(cfg, N)
+    p0 = a.params.copy()
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=8, fp32_estimator=1)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, N, 1, a, batch, minsr=True)
+    finally:
+        nqs.set_options()
+    amp = O.Amp(O.OR_RBM, N, 16, p0.copy(), [])
+    Eo, do, io = O.minsr_step(O.ham(O.OR_TFIM, N, 1, pbc=1, J=1.0, Gamma=1.0), amp, batch, 1e-3, 0.01)
+    assert np.max(np.abs(E - Eo)) <= 2e-5 * np.max(np.abs(Eo))
+
+
+@pytest.mark.parametrize("kind", ["crbm_exchange", "rbm_flip"])
+def test_fp32_chains_follow_fp64_chains(nqs, kind):
+    from spin_based_neural_network_gb300 import abi
+    if kind == "crbm_exchange":
+        N, Lx, Ly = 16, 4, 4
+        cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=32, rbm_init_scale=0.3,
+                                  hamiltonian=1, rng_seed=99)
+        move, n_down = abi.MOVE_EXCHANGE, 8
+    else:
+        N, Lx, Ly = 16, 16, 1
+        cfg = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=16, rbm_init_scale=0.3,
+                                  hamiltonian=0, rng_seed=99)
+        move, n_down = abi.MOVE_SINGLE_FLIP, -1
+    a = nqs.Ansatz(cfg, N)
+    chains = 128
+
+    def run(prec, f32):
+        o = nqs.options(num_chains=chains, rng=abi.RNG_PHILOX, move=move, n_down=n_down, lattice_x=Lx,
+                        lattice_y=Ly, square_pbc=1, precision=prec, fp32_estimator=f32)
+        s = nqs.Sampler(N, cfg, a.log_amp_fn, a.user, o)
+        s.thermalize()
+        out = s.batch(chains * 8)
+        return out, s.acceptance_ratio()
+
+    b64, acc64 = run(abi.PREC_FP64, 0)
+    b32, acc32 = run(abi.PREC_MIXED, 1)
+    same = np.mean(np.all(b64 == b32, axis=1))
+    assert same >= 0.9, same
+    assert abs(acc64 - acc32) <= 0.02
