@@ -595,10 +595,46 @@ __device__ __forceinline__ void tri_tile(int t, int &bi, int &bj) {
 }
 
 // Partial column sums upart[ch][k] = sum_{i in chunk ch} O[i][k] v[i] (RCH rows
-// per chunk, one warp per (chunk, 32 columns)), then out[k] = scale * sum_ch.
+// per chunk).  Even N_p: one warp per (chunk, 64 columns), double2 loads, 16
+// rows in flight per lane; odd N_p: one warp per (chunk, 32 columns).
 __device__ __forceinline__ void colsum_partial(const double *O, int Ns, long P, const double *v, double *upart,
                                                int gwarp, int gwarps, int lane) {
     const int nch = (Ns + RCH - 1) / RCH;
+    if ((P & 1) == 0) {
+        const long P2 = P >> 1, ncg = (P2 + 31) / 32;
+        const double2 *O2 = (const double2 *)O;
+        for (long w = gwarp; w < (long)nch * ncg; w += gwarps) {
+            const int ch = (int)(w / ncg);
+            const long k2 = (w % ncg) * 32 + lane;
+            const int i0 = ch * RCH, i1 = min(Ns, i0 + RCH);
+            double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
+            if (k2 < P2) {
+                int i = i0;
+                for (; i + 15 < i1; i += 16) {
+                    double2 o[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++) o[q] = O2[(size_t)(i + q) * P2 + k2];
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const double v0 = __ldcg(v + i + q), v1 = __ldcg(v + i + q + 1);
+                        ax += o[q].x * v0;
+                        ay += o[q].y * v0;
+                        bx += o[q + 1].x * v1;
+                        by += o[q + 1].y * v1;
+                    }
+                }
+                for (; i < i1; i++) {
+                    const double2 o = O2[(size_t)i * P2 + k2];
+                    const double vi = __ldcg(v + i);
+                    ax += o.x * vi;
+                    ay += o.y * vi;
+                }
+                upart[(size_t)ch * P + 2 * k2] = ax + bx;
+                upart[(size_t)ch * P + 2 * k2 + 1] = ay + by;
+            }
+        }
+        return;
+    }
     const long ncg = (P + 31) / 32;
     for (long w = gwarp; w < (long)nch * ncg; w += gwarps) {
         const int ch = (int)(w / ncg);
@@ -624,36 +660,59 @@ __device__ __forceinline__ double colsum_reduce(const double *upart, int Ns, lon
     return warp_sum(acc);
 }
 
+// o . v for one row of O (N_p doubles), one warp.  v is either in shared
+// memory or (GV) in global memory written by other CTAs (L1-bypassing loads).
+template <bool GV>
+__device__ __forceinline__ double ldv(const double *p) { return GV ? __ldcg(p) : *p; }
+template <bool GV>
+__device__ __forceinline__ double2 ldv2(const double2 *p) { return GV ? __ldcg(p) : *p; }
+
+template <bool GV>
 __device__ __forceinline__ double rowdot(const double *o, long P, const double *v, int lane) {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     if ((P & 1) == 0) {                                  // rows 16-byte aligned: double2 loads
         const double2 *o2 = (const double2 *)o, *v2 = (const double2 *)v;
         const long P2 = P >> 1;
         long k = lane;
-        for (; k + 96 < P2; k += 128) {
-            const double2 x0 = o2[k], x1 = o2[k + 32], x2 = o2[k + 64], x3 = o2[k + 96];
-            const double2 y0 = __ldcg(v2 + k), y1 = __ldcg(v2 + k + 32), y2 = __ldcg(v2 + k + 64),
-                          y3 = __ldcg(v2 + k + 96);
-            a0 += x0.x * y0.x + x0.y * y0.y;
-            a1 += x1.x * y1.x + x1.y * y1.y;
-            a2 += x2.x * y2.x + x2.y * y2.y;
-            a3 += x3.x * y3.x + x3.y * y3.y;
+        for (; k + 224 < P2; k += 256) {
+            double2 x[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) x[q] = o2[k + 32 * q];
+#pragma unroll
+            for (int q = 0; q < 8; q += 2) {
+                const double2 y0 = ldv2<GV>(v2 + k + 32 * q), y1 = ldv2<GV>(v2 + k + 32 * q + 32);
+                a0 += x[q].x * y0.x;
+                a1 += x[q].y * y0.y;
+                a2 += x[q + 1].x * y1.x;
+                a3 += x[q + 1].y * y1.y;
+            }
         }
         for (; k < P2; k += 32) {
-            const double2 x0 = o2[k], y0 = __ldcg(v2 + k);
-            a0 += x0.x * y0.x + x0.y * y0.y;
+            const double2 x0 = o2[k], y0 = ldv2<GV>(v2 + k);
+            a0 += x0.x * y0.x;
+            a1 += x0.y * y0.y;
         }
     } else {
         long k = lane;
         for (; k + 96 < P; k += 128) {
-            a0 += o[k] * __ldcg(v + k);
-            a1 += o[k + 32] * __ldcg(v + k + 32);
-            a2 += o[k + 64] * __ldcg(v + k + 64);
-            a3 += o[k + 96] * __ldcg(v + k + 96);
+            a0 += o[k] * ldv<GV>(v + k);
+            a1 += o[k + 32] * ldv<GV>(v + k + 32);
+            a2 += o[k + 64] * ldv<GV>(v + k + 64);
+            a3 += o[k + 96] * ldv<GV>(v + k + 96);
         }
-        for (; k < P; k += 32) a0 += o[k] * __ldcg(v + k);
+        for (; k < P; k += 32) a0 += o[k] * ldv<GV>(v + k);
     }
     return warp_sum((a0 + a1) + (a2 + a3));
+}
+
+// Stage the N_p-vector v (written by other CTAs) in shared memory when it fits
+// (the caller has passed a barrier since the last use of psm); returns where to
+// read it.
+__device__ __forceinline__ const double *stage_vec(const double *v, long P, double *smem, long cap) {
+    if (P > cap) return v;
+    for (long k = threadIdx.x; k < P; k += PS_THREADS) smem[k] = __ldcg(v + k);
+    __syncthreads();
+    return smem;
 }
 
 // sum over the float4 groups [g0, g1) of row . v, one warp, result in every lane
@@ -910,8 +969,10 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                 if (lane == 0) a.u[k] = sk;
             }
             if (!grid_barrier(a.bar, a.err)) return;
+            const double *us = stage_vec(a.u, P, (double *)psm, PS_SMEM / 8);
             for (int i = gwarp; i < Ns; i += gwarps) {
-                const double d = rowdot(a.O + (size_t)i * P, P, a.u, lane);
+                const double d = us == a.u ? rowdot<true>(a.O + (size_t)i * P, P, us, lane)
+                                           : rowdot<false>(a.O + (size_t)i * P, P, us, lane);
                 if (lane == 0) {
                     const double ri = a.rhs[i] - d / (double)Ns - a.shift * __ldcg(a.x + i);
                     a.r[i] = ri;
@@ -920,8 +981,10 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
             }
         } else {
             // A delta = O_c^T (O_c delta) / N_s + shift delta
+            const double *xs = stage_vec(a.x, P, (double *)psm, PS_SMEM / 8);
             for (int i = gwarp; i < Ns; i += gwarps) {
-                const double d = rowdot(a.O + (size_t)i * P, P, a.x, lane);
+                const double d = xs == a.x ? rowdot<true>(a.O + (size_t)i * P, P, xs, lane)
+                                           : rowdot<false>(a.O + (size_t)i * P, P, xs, lane);
                 if (lane == 0) a.u[i] = d;
             }
             if (!grid_barrier(a.bar, a.err)) return;
