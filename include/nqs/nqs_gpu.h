@@ -156,10 +156,18 @@ int nqs_gpu_minsr_solve_noalloc(const double *d_O, const double *d_E,
 int nqs_gpu_gram_tc(const double *O_host, int num_samples, long num_params, int passes,
                     double scale, float *T_out);
 
+/* Diagnostic: the SR step's effective-sample-size estimator on a host series
+ * `energies` laid out as the sampler writes a batch (sample k of chain c at
+ * row k * num_chains + c).  tau = 1 + 2 sum_{t=1}^{M} rho(t), rho pooled over
+ * the chains, M the smallest window with M >= 5 tau(M) (Sokal); ESS =
+ * (complete rows x num_chains) / tau.  Fewer than two samples per chain give
+ * tau = 1. */
+int nqs_gpu_ess(const double *energies, int num_samples, int num_chains, double *out_tau, double *out_ess);
+
 /* Statistics of the last SR step on this thread. */
 typedef struct {
-    double tau_int;          /* integrated autocorrelation time of E_loc (Sokal, c = 5) */
-    double ess;              /* effective sample size = sum_c n_c / tau_c */
+    double tau_int;          /* integrated autocorrelation time of E_loc (see nqs_gpu_ess) */
+    double ess;              /* effective sample size of the step's batch */
     double refine_residual;  /* MIXED: relative residual after refinement */
     int    refine_sweeps;    /* sweeps used */
     int    chol_retry;       /* 1 if the +1e-6 retry ran */

@@ -31,7 +31,8 @@ static Workspace g_ws;
 // device scalars (doubles): [0] e_mean [1] e_sq_mean [2] ||delta||^2 [3] rs
 // [4] rs0 [5] pAp [6] alpha  ; status ints: [0] chol fail column (-1 ok)
 // [1] cg done flag [2] cg iterations [3] cg converged [4] retry ran
-enum { S_EMEAN = 0, S_ESQ = 1, S_NORM2 = 2, S_RS = 3, S_RS0 = 4, S_PAP = 5, S_ALPHA = 6, S_UMEAN = 7 };
+enum { S_EMEAN = 0, S_ESQ = 1, S_NORM2 = 2, S_RS = 3, S_RS0 = 4, S_PAP = 5, S_ALPHA = 6, S_UMEAN = 7,
+       S_TAU = 8, S_ESS = 9 };
 enum { I_FAIL = 0, I_DONE = 1, I_ITERS = 2, I_CONV = 3, I_RETRY = 4, I_FAIL2 = 5 };
 
 // ---------------------------------------------------------------- statistics
@@ -74,6 +75,54 @@ __global__ void k_energy_stats(const double *__restrict__ E, int n, double *scal
     __syncthreads();
     if (eps)
         for (int i = t; i < n; i += blockDim.x) eps[i] = E[i] - mean;
+}
+
+// Integrated autocorrelation time of E_loc over C chains whose samples sit at
+// rows k * C + c (k = 0 .. K-1): gamma(t) pooled over chains, rho = gamma /
+// gamma(0), tau(M) = 1 + 2 sum_{t=1}^{M} rho(t) with the self-consistent
+// window, the smallest M >= 5 tau(M) (Sokal; the automatic window of emcee),
+// and ESS = K C / tau.  One block; eps holds E - <E>.
+__global__ void k_ess(const double *__restrict__ eps, int Ns, int C, double *scal) {
+    __shared__ double red[256];
+    __shared__ int stop;
+    const int K = C > 0 ? Ns / C : 0, n = K * C, t0 = threadIdx.x;
+    if (K < 2) {
+        if (t0 == 0) {
+            scal[S_TAU] = 1.0;
+            scal[S_ESS] = (double)Ns;
+        }
+        return;
+    }
+    double g0 = 0.0, tau = 1.0;
+    const int maxlag = K - 1 < 512 ? K - 1 : 512;
+    if (t0 == 0) stop = 0;
+    for (int t = 0; t <= maxlag; t++) {
+        double s = 0.0;
+        const int m = (K - t) * C;
+        for (int e = t0; e < m; e += blockDim.x) s += eps[e] * eps[e + t * C];
+        red[t0] = s;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (t0 < o) red[t0] += red[t0 + o];
+            __syncthreads();
+        }
+        const double g = red[0] / (double)m;
+        __syncthreads();
+        if (t == 0) {
+            g0 = g;
+            if (!(g0 > 0.0)) break;
+            continue;
+        }
+        tau += 2.0 * g / g0;
+        if (t0 == 0 && (double)t >= 5.0 * tau) stop = 1;
+        __syncthreads();
+        if (stop) break;
+    }
+    if (t0 == 0) {
+        if (!(tau > 0.0)) tau = 1.0;
+        scal[S_TAU] = tau;
+        scal[S_ESS] = (double)n / tau;
+    }
 }
 
 // Column sums of O (and of O_ik E_i for CG-SR): 32 columns x 8 row groups per
@@ -673,6 +722,11 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         NQS_LAUNCH("energy_stats");
         k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
     }
+    {
+        const int chains = in.sampler ? nqs_sampler_num_chains((nqs_sampler_t *)in.sampler) : 0;
+        NQS_LAUNCH("ess");
+        k_ess<<<1, 256, 0, st>>>(w.eps.p, Ns, chains, w.scal.p);
+    }
     NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
     dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
     int converged = 0, cg_iters = 0;
@@ -798,6 +852,8 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     if (!NQS_CUDA(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st)) || !ansatz_pull(a))
         return -1;
     step_stats().gpu_launches = (int)(c.launches - launches0);
+    step_stats().tau_int = hs[S_TAU];
+    step_stats().ess = hs[S_ESS];
     if (info) {
         info->mean_energy = hs[S_EMEAN];
         info->variance_energy = hs[S_ESQ] - hs[S_EMEAN] * hs[S_EMEAN];
@@ -814,6 +870,38 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
 using namespace nqs;
 
 extern "C" {
+
+// Diagnostic: the step's ESS estimator on a host series (energies in the
+// sampler's layout, sample k of chain c at row k * num_chains + c).
+int nqs_gpu_ess(const double *energies, int num_samples, int num_chains, double *out_tau, double *out_ess) {
+    clear_error();
+    if (!energies || num_samples <= 0 || num_chains <= 0) {
+        set_error("invalid arguments");
+        return -1;
+    }
+    if (!ensure_context()) return -1;
+    cudaStream_t st = ctx().stream;
+    static DevBuf<double> dE, deps, dscal;
+    if (!dE.ensure(num_samples) || !deps.ensure(num_samples) || !dscal.ensure(16)) return -1;
+    double hs[16];
+    if (!NQS_CUDA(cudaMemcpyAsync(dE.p, energies, sizeof(double) * num_samples, cudaMemcpyHostToDevice, st)))
+        return -1;
+    {
+        NQS_LAUNCH("energy_stats");
+        k_energy_stats<<<1, 1024, 0, st>>>(dE.p, num_samples, dscal.p, deps.p);
+    }
+    {
+        NQS_LAUNCH("ess");
+        k_ess<<<1, 256, 0, st>>>(deps.p, num_samples, num_chains, dscal.p);
+    }
+    if (!NQS_CUDA(cudaGetLastError()) ||
+        !NQS_CUDA(cudaMemcpyAsync(hs, dscal.p, sizeof(hs), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaStreamSynchronize(st)))
+        return -1;
+    if (out_tau) *out_tau = hs[S_TAU];
+    if (out_ess) *out_ess = hs[S_ESS];
+    return 0;
+}
 
 static int step_common(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *ansatz, nqs_sampler_t *sampler,
                        nqs_log_amp_fn_t fn, void *user, nqs_gradient_fn_t gfn, void *guser, int minsr,

@@ -84,6 +84,7 @@ def _declare(L):
         "nqs_gpu_event_destroy": (None, [VP]),
         "nqs_gpu_minsr_solve_noalloc": (C.c_int, [VP, VP, C.c_int, C.c_long, C.c_double, VP, infop, VP]),
         "nqs_gpu_gram_tc": (C.c_int, [DP, C.c_int, C.c_long, C.c_int, C.c_double, C.POINTER(C.c_float)]),
+        "nqs_gpu_ess": (C.c_int, [DP, C.c_int, C.c_int, DP, DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -372,3 +373,11 @@ def profile_read(cap=64):
 
 def launch_count():
     return lib().nqs_gpu_launch_count()
+
+
+def ess(energies, num_chains):
+    """(tau_int, ESS) of a batch laid out as the sampler writes it."""
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    tau, n = C.c_double(), C.c_double()
+    _check(lib().nqs_gpu_ess(_dp(e), len(e), num_chains, C.byref(tau), C.byref(n)), "nqs_gpu_ess")
+    return tau.value, n.value

@@ -154,3 +154,16 @@ def test_philox_known_answer():
     m = 0xFFFFFFFF
     O.lib().oracle_philox4x32((C.c_uint32 * 4)(m, m, m, m), (C.c_uint32 * 2)(m, m), out)
     assert list(out) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+
+
+def test_exact_energy_fixture():
+    """tests/golden/exact_energies.json (bench's |dE/N| target) against closed
+    forms: the critical TFIM ring, E0 = -2 / sin(pi / 2N) (even-parity sector of
+    the free-fermion solution), and the 4x4 Heisenberg torus, -11.2284832084."""
+    import json
+    import math
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "exact_energies.json")) as f:
+        ex = json.load(f)
+    assert ex["tfim_chain16_pbc_h1"]["E0"] == pytest.approx(-2.0 / math.sin(math.pi / 32), abs=1e-9)
+    assert ex["heisenberg_4x4_pbc_sz0"]["E0"] == pytest.approx(-11.2284832084, abs=1e-9)
