@@ -81,6 +81,49 @@ nqs_sampler_t *nqs_sampler_create_gpu(int num_sites, const nqs_config_t *cfg,
 /* Number of chains the sampler runs. */
 int nqs_sampler_num_chains(const nqs_sampler_t *s);
 
+/* ---- learned proposal ---------------------------------------------------
+ * A masked autoregressive MLP q(s) (MADE: 2 hidden layers, BF16 weights, FP32
+ * accumulation) trained online by Adam on every batch the sampler produces
+ * (maximum likelihood of the chains' own samples).  A move is a draw from q
+ * with probability `mix` (an independent proposal accepted with
+ * min(1, |psi(s')|^2 q(s) / (|psi(s)|^2 q(s')))), else the sampler's local move;
+ * the mixture keeps |psi|^2 invariant.  When the learned proposals' acceptance
+ * on a batch falls below `min_acceptance` the next batches use local moves only,
+ * with a probe every 8 batches.  With a fixed magnetisation (n_down >= 0 and
+ * exchange moves) q is normalised over that sector.  Needs Philox chains, the
+ * MIXED precision mode with fp32_estimator = 1 and an RBM / cRBM program. */
+typedef struct {
+    int hidden;               /* width of both hidden layers: multiple of 32, <= 128 (64) */
+    int train_iters;          /* Adam iterations per produced batch (2) */
+    double mix;               /* probability that a move is a learned proposal (0.5) */
+    double learning_rate;     /* Adam step (3e-3) */
+    double min_acceptance;    /* fallback threshold (0.01) */
+    unsigned long long seed;  /* weight initialisation and proposal streams */
+} nqs_gpu_made_options_t;
+
+typedef struct {
+    double proposals;         /* learned proposals made so far */
+    double accepted;          /* of which accepted */
+    double nll;               /* mean negative log-likelihood of the last trained batch */
+    int active;               /* 0 while the fallback (local moves only) is in force */
+    int train_steps;          /* Adam steps taken */
+} nqs_gpu_made_stats_t;
+
+nqs_gpu_made_options_t nqs_gpu_made_options_default(void);
+/* Attach (opts != NULL) or remove (NULL) the learned proposal of a sampler. */
+int nqs_sampler_set_learned_proposal(nqs_sampler_t *s, const nqs_gpu_made_options_t *opts);
+int nqs_sampler_learned_stats(const nqs_sampler_t *s, nqs_gpu_made_stats_t *out);
+/* Diagnostics of the attached model: parameter count, FP32 master weights in
+ * the layout W1t[N][H], b1[H], W2t[H][H], b2[H], W3t[H][N], b3[N] (transposed
+ * weights; masked entries read 0 and are forced to 0 on set), log q of
+ * configurations, the mean NLL gradient of a batch (masked), and draws from q. */
+long nqs_gpu_made_num_params(const nqs_sampler_t *s);
+int nqs_gpu_made_get_weights(const nqs_sampler_t *s, float *out);
+int nqs_gpu_made_set_weights(nqs_sampler_t *s, const float *in);
+int nqs_gpu_made_log_prob(const nqs_sampler_t *s, const int *spins, int batch, double *out_logq);
+int nqs_gpu_made_nll_grad(nqs_sampler_t *s, const int *spins, int batch, float *out_grad, double *out_nll);
+int nqs_gpu_made_sample(nqs_sampler_t *s, int count, int *out_spins, double *out_logq);
+
 /* Human-readable reason of the last failure on this thread ("" if none). */
 const char *nqs_gpu_last_error(void);
 /* Device name and SM count of the device in use; 0 on success. */

@@ -137,3 +137,15 @@ class GpuOptions(C.Structure):
         ("fp32_estimator", C.c_int),
         ("reserved", C.c_int * 2),
     ]
+
+
+class MadeOptions(C.Structure):
+    """nqs_gpu_made_options_t (include/nqs/nqs_gpu.h)."""
+    _fields_ = [("hidden", C.c_int), ("train_iters", C.c_int), ("mix", C.c_double),
+                ("learning_rate", C.c_double), ("min_acceptance", C.c_double), ("seed", C.c_ulonglong)]
+
+
+class MadeStats(C.Structure):
+    """nqs_gpu_made_stats_t (include/nqs/nqs_gpu.h)."""
+    _fields_ = [("proposals", C.c_double), ("accepted", C.c_double), ("nll", C.c_double),
+                ("active", C.c_int), ("train_steps", C.c_int)]

@@ -17,6 +17,7 @@
 #include <math.h>
 
 #include "nqs_amp.cuh"
+#include "nqs_made.cuh"
 
 namespace nqs {
 
@@ -32,6 +33,7 @@ struct Sampler {
     DevBuf<int> d_bonds, d_spins;
     int nb = 0;
     int *h_current = nullptr;        // pinned, N ints (next/current)
+    Made *made = nullptr;            // learned proposal (optional)
 };
 
 struct SampleArgs {
@@ -185,9 +187,11 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm(SampleArgs S, DevAmp A)
 // proposal instead of three FP64 transcendentals); an accepted move updates
 // theta additively and recomputes t.  The uniform is drawn from the same
 // Philox word as in the FP64 chain, as a 24-bit float.
-template <int MOVE, typename Eval, typename Commit>
+template <int MOVE, bool LEARNED, typename Eval, typename Commit, typename Learned>
 __device__ __forceinline__ void run_chain32(const SampleArgs &S, int c, uint64_t &s, Eval eval, Commit commit,
-                                            unsigned long long &acc, unsigned long long &pro) {
+                                            Learned learned, uint32_t mix_thr, unsigned long long &acc,
+                                            unsigned long long &pro, unsigned long long &lacc,
+                                            unsigned long long &lpro) {
     const int lane = threadIdx.x & 31;
     const int per = S.decor > 0 ? S.decor : 1;
     for (int t = 0; t < S.total; t++) {
@@ -195,27 +199,37 @@ __device__ __forceinline__ void run_chain32(const SampleArgs &S, int c, uint64_t
         const uint64_t m = S.move0 + (uint64_t)t;
         const uint4 r = philox4x32(make_uint4((uint32_t)c, (uint32_t)m, (uint32_t)(m >> 32), 0u),
                                    make_uint2((uint32_t)S.seed, (uint32_t)(S.seed >> 32)));
-        if (MOVE == NQS_GPU_MOVE_EXCHANGE) {
-            const int k = (int)(((uint64_t)r.x * (uint64_t)S.nb) >> 32);
-            u = S.bonds[2 * k];
-            v = S.bonds[2 * k + 1];
-        } else {
-            u = (int)(((uint64_t)r.x * (uint64_t)S.N) >> 32);
-        }
         pro++;
-        const bool parallel = v >= 0 && (((s >> u) ^ (s >> v)) & 1ull) == 0;
-        if (!parallel) {
-            const float lr = 2.f * eval(u, v);
-            bool accept = lr >= 0.f;
-            if (!accept) {
-                const float uni = ((float)(r.z >> 8) + 0.5f) * (1.f / 16777216.f);
-                accept = __logf(uni) < lr;
-            }
-            if (accept) {
+        if (LEARNED && r.y < mix_thr) {
+            // learned proposal slot: the move kind depends on the random word
+            // only, never on the state, so the mixture stays |psi|^2-invariant
+            lpro++;
+            if (learned(r)) {
                 acc++;
-                commit(u, v);
-                s ^= 1ull << u;
-                if (v >= 0) s ^= 1ull << v;
+                lacc++;
+            }
+        } else {
+            if (MOVE == NQS_GPU_MOVE_EXCHANGE) {
+                const int k = (int)(((uint64_t)r.x * (uint64_t)S.nb) >> 32);
+                u = S.bonds[2 * k];
+                v = S.bonds[2 * k + 1];
+            } else {
+                u = (int)(((uint64_t)r.x * (uint64_t)S.N) >> 32);
+            }
+            const bool parallel = v >= 0 && (((s >> u) ^ (s >> v)) & 1ull) == 0;
+            if (!parallel) {
+                const float lr = 2.f * eval(u, v);
+                bool accept = lr >= 0.f;
+                if (!accept) {
+                    const float uni = ((float)(r.z >> 8) + 0.5f) * (1.f / 16777216.f);
+                    accept = __logf(uni) < lr;
+                }
+                if (accept) {
+                    acc++;
+                    commit(u, v);
+                    s ^= 1ull << u;
+                    if (v >= 0) s ^= 1ull << v;
+                }
             }
         }
         if (t >= S.skip && ((t - S.skip + 1) % per) == 0) {
@@ -235,39 +249,58 @@ __device__ __forceinline__ float2 ctanh32s(float x, float y) {
     return make_float2(sh / den, s2 / den);
 }
 
-template <int J, bool CPLX, int MOVE>
-__global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp A) {
-    const int lane = threadIdx.x & 31;
-    const int c = blockIdx.x * kSW + (threadIdx.x >> 5);
+template <int J, bool CPLX, int MOVE, bool LEARNED>
+__global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp A, DevMade md) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * kSW + warp;
+    const __nv_bfloat16 *Wsm = nullptr;
+    float *h1 = nullptr, *h2 = nullptr;
+    uint32_t mix_thr = 0;
+    if (LEARNED) {
+        // BF16 weights of the proposal model in shared memory for the log q of
+        // the current configuration
+        const long PM = made_off(md.N, md.H).total, wbytes = (PM * 2 + 15) / 16 * 16;
+        __nv_bfloat16 *W = (__nv_bfloat16 *)smraw;
+        for (long p = threadIdx.x; p < PM; p += blockDim.x) W[p] = md.w[p];
+        __syncthreads();
+        Wsm = W;
+        h1 = (float *)(smraw + wbytes) + (size_t)warp * 2 * md.H;
+        h2 = h1 + md.H;
+        mix_thr = *md.active ? md.mix_thr : 0u;
+    }
     if (c >= S.C) return;
     const DevAnsatz &a = A.a;
     const int M = a.M;
     const long Ml = M;
     uint64_t s = S.bits[c];
     float thr[J], thi[J], tr[J], ti[J], nr[J], ni[J];
+    auto rebuild = [&]() {
 #pragma unroll
-    for (int j = 0; j < J; j++) {
-        const int h = lane + 32 * j;
-        thr[j] = thi[j] = tr[j] = ti[j] = 0.f;
-        if (h < M) {
-            float xr = a.b32[h].x, xi = a.b32[h].y;
-            for (int i = 0; i < a.N; i++) {
-                const float sp = (float)spin_of(s, i);
-                const float2 w = a.w32[(long)i * Ml + h];
-                xr = fmaf(sp, w.x, xr);
-                if (CPLX) xi = fmaf(sp, w.y, xi);
-            }
-            thr[j] = xr;
-            thi[j] = CPLX ? xi : 0.f;
-            if (CPLX) {
-                const float2 t = ctanh32s(xr, xi);
-                tr[j] = t.x;
-                ti[j] = t.y;
-            } else {
-                tr[j] = tanhf(xr);
+        for (int j = 0; j < J; j++) {
+            const int h = lane + 32 * j;
+            thr[j] = thi[j] = tr[j] = ti[j] = 0.f;
+            if (h < M) {
+                float xr = a.b32[h].x, xi = a.b32[h].y;
+                for (int i = 0; i < a.N; i++) {
+                    const float sp = (float)spin_of(s, i);
+                    const float2 w = a.w32[(long)i * Ml + h];
+                    xr = fmaf(sp, w.x, xr);
+                    if (CPLX) xi = fmaf(sp, w.y, xi);
+                }
+                thr[j] = xr;
+                thi[j] = CPLX ? xi : 0.f;
+                if (CPLX) {
+                    const float2 t = ctanh32s(xr, xi);
+                    tr[j] = t.x;
+                    ti[j] = t.y;
+                } else {
+                    tr[j] = tanhf(xr);
+                }
             }
         }
-    }
+    };
+    rebuild();
     auto eval = [&](int u, int v) -> float {
         const float su = (float)spin_of(s, u), sv = v >= 0 ? (float)spin_of(s, v) : 0.f;
         float lg = 0.f;
@@ -308,6 +341,9 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp 
         if (v >= 0) lg -= 2.f * sv * a.a32[v].x;
         return lg;
     };
+    bool dirty = true;          // log q of the current configuration not known
+    float lq = 0.f;
+    int used = 0;
     auto commit = [&](int, int) {
 #pragma unroll
         for (int j = 0; j < J; j++) {
@@ -323,13 +359,46 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp 
                 }
             }
         }
+        dirty = true;
     };
-    unsigned long long acc = 0, pro = 0;
-    run_chain32<MOVE>(S, c, s, eval, commit, acc, pro);
+    // independent proposal s' ~ q from this chain's next pool entry, accepted
+    // with min(1, |psi(s')|^2 q(s) / (|psi(s)|^2 q(s'))); an exhausted pool
+    // leaves the state unchanged (a rejected move)
+    auto learned = [&](const uint4 &r) -> bool {
+        if (!LEARNED || used >= md.per_chain) return false;
+        const long e = (long)c * md.per_chain + used;
+        used++;
+        const uint64_t x2 = md.pbits[e];
+        if (x2 == s) return false;
+        const float lq2 = md.plq[e], lp2 = md.plpsi[e];
+        const float lp = rbm_logabs32<CPLX>(a, s);
+        if (dirty) {
+            lq = made_logq_warp(md, Wsm, s, h1, h2);
+            dirty = false;
+        }
+        const float la = 2.f * (lp2 - lp) + lq - lq2;
+        bool accept = la >= 0.f;
+        if (!accept) {
+            const float uni = ((float)(r.z >> 8) + 0.5f) * (1.f / 16777216.f);
+            accept = __logf(uni) < la;
+        }
+        if (accept) {
+            s = x2;
+            lq = lq2;
+            rebuild();
+        }
+        return accept;
+    };
+    unsigned long long acc = 0, pro = 0, lacc = 0, lpro = 0;
+    run_chain32<MOVE, LEARNED>(S, c, s, eval, commit, learned, mix_thr, acc, pro, lacc, lpro);
     if (lane == 0) {
         S.bits[c] = s;
         atomicAdd(&S.counts[0], acc);
         atomicAdd(&S.counts[1], pro);
+        if (LEARNED) {
+            atomicAdd(&S.counts[2], lpro);
+            atomicAdd(&S.counts[3], lacc);
+        }
     }
 }
 
@@ -389,19 +458,35 @@ __global__ void k_chain_init(int C, int N, uint64_t seed, int n_down, uint64_t *
     bits[c] = b;
 }
 
+template <int J, bool CX, int MOVE>
+static void launch_rbm32(dim3 grid, dim3 block, cudaStream_t st, const SampleArgs &S, const DevAmp &A,
+                         const DevMade &md, size_t smem) {
+    if (md.per_chain > 0) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_sample_rbm32<J, CX, MOVE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024);
+            attr = true;
+        }
+        k_sample_rbm32<J, CX, MOVE, true><<<grid, block, smem, st>>>(S, A, md);
+    } else {
+        k_sample_rbm32<J, CX, MOVE, false><<<grid, block, 0, st>>>(S, A, md);
+    }
+}
+
 template <int RNG, int MOVE>
-static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32) {
+static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32, const DevMade &md, size_t smem) {
     dim3 grid((S.C + kSW - 1) / kSW), block(32 * kSW);
     cudaStream_t st = ctx().stream;
     const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
     if (f32 && RNG == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
         const int J = (A.a.M + 31) / 32;
         const bool cx = A.a.kind == KIND_CRBM;
-        NQS_LAUNCH("sampler_fp32");
+        NQS_LAUNCH(md.per_chain > 0 ? "sampler_fp32_learned" : "sampler_fp32");
 #define NQS_FCASE(JJ)                                                             \
     case JJ:                                                                      \
-        if (cx) k_sample_rbm32<JJ, true, MOVE><<<grid, block, 0, st>>>(S, A);     \
-        else k_sample_rbm32<JJ, false, MOVE><<<grid, block, 0, st>>>(S, A);       \
+        if (cx) launch_rbm32<JJ, true, MOVE>(grid, block, st, S, A, md, smem);    \
+        else launch_rbm32<JJ, false, MOVE>(grid, block, st, S, A, md, smem);      \
         break;
         switch (J) {
             NQS_FCASE(1) NQS_FCASE(2) NQS_FCASE(3) NQS_FCASE(4) NQS_FCASE(5) NQS_FCASE(6) NQS_FCASE(7)
@@ -463,12 +548,18 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
     if (S.total <= 0) return true;
     bool ok;
     const bool f32 = sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator;
+    DevMade md{};
+    size_t smem = 0;
+    if (sm->made && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
+        if (!made_prepare(sm->made, A, sm->C, S.total, sm->cfg.rng_seed ^ 0x9E3779B97F4A7C15ull, &md)) return false;
+        smem = made_chain_smem(sm->made, kSW);
+    }
     if (sm->opts.rng == NQS_GPU_RNG_XORSHIFT_COMPAT)
-        ok = dispatch<NQS_GPU_RNG_XORSHIFT_COMPAT, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, false);
+        ok = dispatch<NQS_GPU_RNG_XORSHIFT_COMPAT, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, false, md, 0);
     else if (sm->opts.move == NQS_GPU_MOVE_EXCHANGE)
-        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_EXCHANGE>(S, A, f32);
+        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_EXCHANGE>(S, A, f32, md, smem);
     else
-        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, f32);
+        ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, f32, md, smem);
     sm->move_counter += (uint64_t)S.total;
     return ok;
 }
@@ -476,6 +567,8 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
 bool sampler_produce(Sampler *sm, int n, uint64_t **d_out) {
     if (!sm->d_samples.ensure((size_t)n)) return false;
     if (!sampler_run(sm, 0, n, sm->d_samples.p)) return false;
+    // online training of the learned proposal on the chains' own samples
+    if (sm->made && !made_train(sm->made, sm->d_samples.p, n, sm->d_counts.p)) return false;
     *d_out = sm->d_samples.p;
     return true;
 }
@@ -548,13 +641,13 @@ nqs_sampler_t *nqs_sampler_create_gpu(int num_sites, const nqs_config_t *cfg,
             return nullptr;
         }
     }
-    if (!s->d_bits.ensure((size_t)s->C) || !s->d_rng.ensure((size_t)s->C) || !s->d_counts.ensure(2) ||
+    if (!s->d_bits.ensure((size_t)s->C) || !s->d_rng.ensure((size_t)s->C) || !s->d_counts.ensure(4) ||
         !NQS_CUDA(cudaMallocHost(&s->h_current, sizeof(int) * num_sites))) {
         delete s;
         return nullptr;
     }
     cudaStream_t st = ctx().stream;
-    NQS_CUDA(cudaMemsetAsync(s->d_counts.p, 0, 2 * sizeof(unsigned long long), st));
+    NQS_CUDA(cudaMemsetAsync(s->d_counts.p, 0, 4 * sizeof(unsigned long long), st));
     if (compat) {
         // upstream start: rng = seed (or a fixed constant), then one draw per site
         // (src/nqs/nqs_sampler.c:62-72); host-side set-up of the single chain
@@ -594,6 +687,7 @@ void nqs_sampler_free(nqs_sampler_t *h) {
     Sampler *s = (Sampler *)h;
     if (!s) return;
     if (s->h_current) cudaFreeHost(s->h_current);
+    if (s->made) made_free(s->made);
     delete s;
 }
 
@@ -652,5 +746,111 @@ const int *nqs_sampler_current(const nqs_sampler_t *h) {
 int nqs_sampler_num_sites(const nqs_sampler_t *h) { return h ? ((const Sampler *)h)->N : 0; }
 
 int nqs_sampler_num_chains(const nqs_sampler_t *h) { return h ? ((const Sampler *)h)->C : 0; }
+
+// ---------------------------------------------------------------- learned proposal
+nqs_gpu_made_options_t nqs_gpu_made_options_default(void) {
+    nqs_gpu_made_options_t o;
+    memset(&o, 0, sizeof(o));
+    o.hidden = 64;
+    o.train_iters = 2;
+    o.mix = 0.5;
+    o.learning_rate = 3e-3;
+    o.min_acceptance = 0.01;
+    o.seed = 20260214ull;
+    return o;
+}
+
+int nqs_sampler_set_learned_proposal(nqs_sampler_t *h, const nqs_gpu_made_options_t *o) {
+    clear_error();
+    Sampler *s = (Sampler *)h;
+    if (!s) return -1;
+    if (s->made) {
+        made_free(s->made);
+        s->made = nullptr;
+    }
+    if (!o) return 0;
+    if (s->opts.rng != NQS_GPU_RNG_PHILOX || s->opts.precision != NQS_GPU_PREC_MIXED || !s->opts.fp32_estimator) {
+        set_error("learned proposal needs Philox chains and the MIXED precision mode with fp32_estimator = 1");
+        return -1;
+    }
+    DevAmp A;
+    if (!build_amp(s->fn, s->user, s->N, &A, nullptr)) return -1;
+    if (!fp32_capable(A)) {
+        set_error("learned proposal needs an RBM / cRBM program without symmetry projection");
+        return -1;
+    }
+    const int n_ones = s->opts.move == NQS_GPU_MOVE_EXCHANGE && s->opts.n_down >= 0 ? s->opts.n_down : -1;
+    s->made = made_create(s->N, n_ones, *o);
+    return s->made ? 0 : -1;
+}
+
+int nqs_sampler_learned_stats(const nqs_sampler_t *h, nqs_gpu_made_stats_t *out) {
+    const Sampler *s = (const Sampler *)h;
+    if (!s || !out || !s->made) return -1;
+    return made_stats_read(s->made, out) ? 0 : -1;
+}
+
+long nqs_gpu_made_num_params(const nqs_sampler_t *h) {
+    const Sampler *s = (const Sampler *)h;
+    return s && s->made ? made_num_params(s->made) : 0;
+}
+
+int nqs_gpu_made_get_weights(const nqs_sampler_t *h, float *out) {
+    const Sampler *s = (const Sampler *)h;
+    if (!s || !s->made || !out) return -1;
+    return made_get(s->made, out) ? 0 : -1;
+}
+
+int nqs_gpu_made_set_weights(nqs_sampler_t *h, const float *in) {
+    Sampler *s = (Sampler *)h;
+    if (!s || !s->made || !in) return -1;
+    return made_set(s->made, in) ? 0 : -1;
+}
+
+int nqs_gpu_made_log_prob(const nqs_sampler_t *h, const int *spins, int batch, double *out) {
+    clear_error();
+    const Sampler *s = (const Sampler *)h;
+    if (!s || !s->made || !spins || !out || batch <= 0) return -1;
+    uint64_t *bits;
+    static DevBuf<float> lq;
+    if (!upload_spins(spins, batch, s->N, &bits) || !lq.ensure((size_t)batch) || !made_logq(s->made, bits, batch, lq.p))
+        return -1;
+    std::vector<float> h_((size_t)batch);
+    if (!NQS_CUDA(cudaMemcpyAsync(h_.data(), lq.p, sizeof(float) * batch, cudaMemcpyDeviceToHost, ctx().stream)) ||
+        !NQS_CUDA(cudaStreamSynchronize(ctx().stream)))
+        return -1;
+    for (int b = 0; b < batch; b++) out[b] = h_[b];
+    return 0;
+}
+
+int nqs_gpu_made_nll_grad(nqs_sampler_t *h, const int *spins, int batch, float *out_grad, double *out_nll) {
+    clear_error();
+    Sampler *s = (Sampler *)h;
+    if (!s || !s->made || !spins || !out_grad || batch <= 0) return -1;
+    uint64_t *bits;
+    if (!upload_spins(spins, batch, s->N, &bits)) return -1;
+    return made_grad(s->made, bits, batch, out_grad, out_nll) ? 0 : -1;
+}
+
+int nqs_gpu_made_sample(nqs_sampler_t *h, int count, int *out_spins, double *out_logq) {
+    clear_error();
+    Sampler *s = (Sampler *)h;
+    if (!s || !s->made || !out_spins || count <= 0) return -1;
+    DevAmp A;
+    if (!build_amp(s->fn, s->user, s->N, &A, nullptr)) return -1;
+    const uint64_t *bits;
+    const float *lq;
+    if (!made_sample(s->made, A, count, s->cfg.rng_seed ^ 0x5EEDull, &bits, &lq)) return -1;
+    if (!s->d_spins.ensure((size_t)count * s->N) || !launch_bits_to_spins(bits, count, s->N, s->d_spins.p)) return -1;
+    std::vector<float> h_((size_t)count);
+    if (!NQS_CUDA(cudaMemcpyAsync(out_spins, s->d_spins.p, sizeof(int) * (size_t)count * s->N, cudaMemcpyDeviceToHost,
+                                  ctx().stream)) ||
+        !NQS_CUDA(cudaMemcpyAsync(h_.data(), lq, sizeof(float) * count, cudaMemcpyDeviceToHost, ctx().stream)) ||
+        !NQS_CUDA(cudaStreamSynchronize(ctx().stream)))
+        return -1;
+    if (out_logq)
+        for (int b = 0; b < count; b++) out_logq[b] = h_[b];
+    return 0;
+}
 
 }  // extern "C"

@@ -85,6 +85,15 @@ def _declare(L):
         "nqs_gpu_minsr_solve_noalloc": (C.c_int, [VP, VP, C.c_int, C.c_long, C.c_double, VP, infop, VP]),
         "nqs_gpu_gram_tc": (C.c_int, [DP, C.c_int, C.c_long, C.c_int, C.c_double, C.POINTER(C.c_float)]),
         "nqs_gpu_ess": (C.c_int, [DP, C.c_int, C.c_int, DP, DP]),
+        "nqs_gpu_made_options_default": (abi.MadeOptions, []),
+        "nqs_sampler_set_learned_proposal": (C.c_int, [C.c_void_p, C.POINTER(abi.MadeOptions)]),
+        "nqs_sampler_learned_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.MadeStats)]),
+        "nqs_gpu_made_num_params": (C.c_long, [C.c_void_p]),
+        "nqs_gpu_made_get_weights": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "nqs_gpu_made_set_weights": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "nqs_gpu_made_log_prob": (C.c_int, [C.c_void_p, IP, C.c_int, DP]),
+        "nqs_gpu_made_nll_grad": (C.c_int, [C.c_void_p, IP, C.c_int, C.POINTER(C.c_float), DP]),
+        "nqs_gpu_made_sample": (C.c_int, [C.c_void_p, C.c_int, IP, DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -381,3 +390,55 @@ def ess(energies, num_chains):
     tau, n = C.c_double(), C.c_double()
     _check(lib().nqs_gpu_ess(_dp(e), len(e), num_chains, C.byref(tau), C.byref(n)), "nqs_gpu_ess")
     return tau.value, n.value
+
+
+class LearnedProposal:
+    """The learned (MADE) proposal attached to a Sampler (nqs_sampler_set_learned_proposal)."""
+
+    def __init__(self, sampler, **kw):
+        o = lib().nqs_gpu_made_options_default()
+        for k, v in kw.items():
+            setattr(o, k, v)
+        _check(lib().nqs_sampler_set_learned_proposal(sampler.h, C.byref(o)), "nqs_sampler_set_learned_proposal")
+        self.s = sampler
+        self.opts = o
+
+    def detach(self):
+        _check(lib().nqs_sampler_set_learned_proposal(self.s.h, None), "nqs_sampler_set_learned_proposal")
+
+    def stats(self):
+        st = abi.MadeStats()
+        _check(lib().nqs_sampler_learned_stats(self.s.h, C.byref(st)), "nqs_sampler_learned_stats")
+        return st
+
+    def num_params(self):
+        return lib().nqs_gpu_made_num_params(self.s.h)
+
+    def weights(self):
+        w = np.zeros(self.num_params(), np.float32)
+        _check(lib().nqs_gpu_made_get_weights(self.s.h, w.ctypes.data_as(C.POINTER(C.c_float))), "made_get_weights")
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(lib().nqs_gpu_made_set_weights(self.s.h, w.ctypes.data_as(C.POINTER(C.c_float))), "made_set_weights")
+
+    def log_prob(self, spins):
+        s = spins_array(spins)
+        out = np.zeros(s.shape[0])
+        _check(lib().nqs_gpu_made_log_prob(self.s.h, _ip(s), s.shape[0], _dp(out)), "made_log_prob")
+        return out
+
+    def nll_grad(self, spins):
+        s = spins_array(spins)
+        g = np.zeros(self.num_params(), np.float32)
+        nll = C.c_double()
+        _check(lib().nqs_gpu_made_nll_grad(self.s.h, _ip(s), s.shape[0], g.ctypes.data_as(C.POINTER(C.c_float)),
+                                          C.byref(nll)), "made_nll_grad")
+        return g, nll.value
+
+    def sample(self, count):
+        out = np.zeros((count, self.s.N), np.int32)
+        lq = np.zeros(count)
+        _check(lib().nqs_gpu_made_sample(self.s.h, count, _ip(out), _dp(lq)), "made_sample")
+        return out, lq
