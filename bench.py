@@ -298,6 +298,48 @@ def converge(nqs, abi, L, opts_kw, max_steps, tols=(1e-2, 1e-3, 1e-4), window=20
             "ess_per_s": float(np.sum(ess) / (sum(ms) / 1000.0)), "ms_per_step": float(np.mean(ms))}
 
 
+def proposal_run(nqs, abi, L, opts_kw, decor, learned, warm, steps):
+    """ESS per step, steps per second and ESS per second of the throughput
+    workload with `decor` moves between recorded samples, with local exchange
+    moves only or mixed with the learned proposal (mix 0.5, width 64, one Adam
+    iteration on 1024 samples of every batch, trained online from the first
+    step)."""
+    import numpy as np
+    nqs.set_options(**opts_kw)
+    cfg = workload_cfg(abi)
+    cfg.num_decorrelate = decor
+    a = nqs.Ansatz(cfg, N_SITES)
+    a.params[:] = init_params(a.P)
+    m = nqs.Marshall(a.log_amp_fn, a.user, LX, LY)
+    so = nqs.options(num_chains=CHAINS, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=N_SITES // 2,
+                     lattice_x=LX, lattice_y=LY, square_pbc=1, precision=opts_kw["precision"],
+                     fp32_estimator=opts_kw.get("fp32_estimator", 0))
+    s = nqs.Sampler(N_SITES, cfg, m.log_amp_fn, m.user, so)
+    lp = nqs.LearnedProposal(s, hidden=64, mix=0.5) if learned else None
+    s.thermalize()
+    for _ in range(warm):
+        nqs.sr_step_minsr(cfg, LX, LY, a, s, m.log_amp_fn, m.user)
+    ess, acc = [], []
+    e0 = L.nqs_gpu_event_record()
+    for _ in range(steps):
+        info = nqs.sr_step_minsr(cfg, LX, LY, a, s, m.log_amp_fn, m.user)
+        ess.append(nqs.last_step_stats().ess)
+        acc.append(info.acceptance_ratio)
+    e1 = L.nqs_gpu_event_record()
+    ms = L.nqs_gpu_event_elapsed_ms(e0, e1) / steps
+    L.nqs_gpu_event_destroy(e0)
+    L.nqs_gpu_event_destroy(e1)
+    out = {"decorrelate": decor, "learned": bool(learned), "ess_per_step": float(np.mean(ess)),
+           "tau_int": float(NS / np.mean(ess)), "ms_per_step": ms, "steps_per_s": 1000.0 / ms,
+           "ess_per_s": float(np.mean(ess)) * 1000.0 / ms}
+    if lp is not None:
+        st = lp.stats()
+        out.update({"learned_acceptance": st.accepted / max(st.proposals, 1.0), "nll": st.nll,
+                    "fallback_active": st.active == 0})
+        lp.detach()
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -433,6 +475,12 @@ def run_gpu(args):
         plain = {"value": k_plain / (pms / 1000.0), "unit": "steps/s", "steps": k_plain}
         nqs.set_options(**base_opts)
 
+    proposals = None
+    if prec == abi.PREC_MIXED and args.proposal_steps > 0:
+        proposals = [proposal_run(nqs, abi, L, base_opts, d, lr, 30, args.proposal_steps)
+                     for d in (DECOR, 2) for lr in (False, True)]
+        nqs.set_options(**base_opts)
+
     conv = None
     if args.converge_steps > 0:
         conv = converge(nqs, abi, L, base_opts, args.converge_steps)
@@ -461,7 +509,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": 8 * P + 16 * 8},
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
             "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
-            "convergence_vs_lanczos": conv,
+            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
@@ -522,6 +570,8 @@ def main():
     ap.add_argument("--converge-steps", type=int, default=1000,
                     help="max optimisation steps of the |dE/N| <= 1e-4 vs Lanczos run (0 = skip)")
     ap.add_argument("--converge-fp64", action="store_true", help="also run the FP64 path to the target")
+    ap.add_argument("--proposal-steps", type=int, default=20,
+                    help="timed steps of each plain / learned proposal run (0 = skip)")
     args = ap.parse_args()
     if args.gram_only:
         return run_gram_only(args)

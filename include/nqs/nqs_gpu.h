@@ -94,7 +94,8 @@ int nqs_sampler_num_chains(const nqs_sampler_t *s);
  * MIXED precision mode with fp32_estimator = 1 and an RBM / cRBM program. */
 typedef struct {
     int hidden;               /* width of both hidden layers: multiple of 32, <= 128 (64) */
-    int train_iters;          /* Adam iterations per produced batch (2) */
+    int train_iters;          /* Adam iterations per produced batch (1) */
+    int train_batch;          /* samples of each batch it trains on, 0 = all (1024) */
     double mix;               /* probability that a move is a learned proposal (0.5) */
     double learning_rate;     /* Adam step (3e-3) */
     double min_acceptance;    /* fallback threshold (0.01) */

@@ -141,7 +141,7 @@ class GpuOptions(C.Structure):
 
 class MadeOptions(C.Structure):
     """nqs_gpu_made_options_t (include/nqs/nqs_gpu.h)."""
-    _fields_ = [("hidden", C.c_int), ("train_iters", C.c_int), ("mix", C.c_double),
+    _fields_ = [("hidden", C.c_int), ("train_iters", C.c_int), ("train_batch", C.c_int), ("mix", C.c_double),
                 ("learning_rate", C.c_double), ("min_acceptance", C.c_double), ("seed", C.c_ulonglong)]
 
 

@@ -52,33 +52,68 @@ __global__ void k_made_publish(const float *master, __nv_bfloat16 *wb, long PM, 
 }
 
 // ---------------------------------------------------------------- proposal pool
-template <bool CPLX>
-__global__ void __launch_bounds__(128) k_made_pool(DevMade m, DevAmp A, long total, uint64_t seed, uint32_t launch,
-                                                   uint64_t *pbits, float *plq, float *plpsi) {
+// One thread per proposal: the hidden-1 pre-activations live in registers
+// (H is a template parameter), the weights in shared memory are read as
+// broadcasts (every thread of a warp reads the same entry), and the running
+// logits of the outputs sit in a shared-memory column per thread.  At site i
+// the hidden-2 units of degree i (all of x_<i drawn) are formed and added to
+// the logits of the outputs >= i in the order made_logq_warp uses, so the
+// pool's log q equals the teacher-forced log q of the same configuration.
+// made_h2 of one thread: W2n = W2 with unit-major rows (W2n[k][j] = W2t[j][k]),
+// read 8 weights per 16-byte load; same products and partial sums as made_h2.
+__device__ __forceinline__ void bf8(const __nv_bfloat16 *p, float (&w)[8]) {
+    const uint4 v = *(const uint4 *)p;
+    const uint32_t u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        w[2 * q] = __uint_as_float(u[q] << 16);
+        w[2 * q + 1] = __uint_as_float(u[q] & 0xFFFF0000u);
+    }
+}
+
+template <int H>
+__device__ __forceinline__ float made_h2_reg(const __nv_bfloat16 *W, const __nv_bfloat16 *W2n, const MadeOff &o,
+                                             int k, const float (&a1)[H]) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+    for (int j = 0; j < H; j += 8) {
+        float w[8];
+        bf8(W2n + (long)k * H + j, w);
+        s0 = fmaf(w[0], fmaxf(a1[j], 0.f), s0);
+        s1 = fmaf(w[1], fmaxf(a1[j + 1], 0.f), s1);
+        s2 = fmaf(w[2], fmaxf(a1[j + 2], 0.f), s2);
+        s3 = fmaf(w[3], fmaxf(a1[j + 3], 0.f), s3);
+        s0 = fmaf(w[4], fmaxf(a1[j + 4], 0.f), s0);
+        s1 = fmaf(w[5], fmaxf(a1[j + 5], 0.f), s1);
+        s2 = fmaf(w[6], fmaxf(a1[j + 6], 0.f), s2);
+        s3 = fmaf(w[7], fmaxf(a1[j + 7], 0.f), s3);
+    }
+    return fmaxf(bf(W, o.b2 + k) + ((s0 + s1) + (s2 + s3)), 0.f);
+}
+
+constexpr int POOL_T = 128;
+
+template <int H, bool CPLX>
+__global__ void __launch_bounds__(POOL_T, 3) k_made_pool(DevMade m, DevAmp A, long total, uint64_t seed, uint32_t launch,
+                                                      uint64_t *pbits, float *plq, float *plpsi) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (*m.active == 0) return;
-    const int N = m.N, H = m.H, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int N = m.N, tid = threadIdx.x;
     const MadeOff o = made_off(N, H);
     __nv_bfloat16 *W = (__nv_bfloat16 *)smraw;
     const long wbytes = (o.total * 2 + 15) / 16 * 16;
-    float *h1 = (float *)(smraw + wbytes) + (size_t)warp * 2 * H, *h2 = h1 + H;
-    for (long p = threadIdx.x; p < o.total; p += blockDim.x) W[p] = m.w[p];
+    __nv_bfloat16 *W2n = (__nv_bfloat16 *)(smraw + wbytes);                      // [H][H]
+    float *Ls = (float *)(smraw + wbytes + (long)H * H * 2);                     // [N][POOL_T]
+    float *Ps = Ls + (long)N * POOL_T;                                           // [32][POOL_T]
+    for (long p = tid; p < o.total; p += POOL_T) W[p] = m.w[p];
+    for (long p = tid; p < (long)H * H; p += POOL_T) W2n[(p % H) * H + p / H] = m.w[o.w2 + p];
     __syncthreads();
     const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-    const long nw = (long)gridDim.x * (blockDim.x >> 5);
-    for (long e = (long)blockIdx.x * (blockDim.x >> 5) + warp; e < total; e += nw) {
-        float a1[MADE_MAX_H / 32];
+    for (long e = (long)blockIdx.x * POOL_T + tid; e < total; e += (long)gridDim.x * POOL_T) {
+        float a1[H];
 #pragma unroll
-        for (int q = 0; q < MADE_MAX_H / 32; q++) {
-            const int k = lane + 32 * q;
-            a1[q] = 0.f;
-            if (k < H) {
-                a1[q] = bf(W, o.b1 + k);
-                h1[k] = fmaxf(a1[q], 0.f);
-                h2[k] = 0.f;
-            }
-        }
-        __syncwarp();
+        for (int k = 0; k < H; k++) a1[k] = bf(W, o.b1 + k);
+        for (int i = 0; i < N; i++) Ls[i * POOL_T + tid] = 0.f;
         uint64_t x = 0;
         int ones = 0;
         float lq = 0.f;
@@ -87,11 +122,15 @@ __global__ void __launch_bounds__(128) k_made_pool(DevMade m, DevAmp A, long tot
             if ((i & 3) == 0)
                 r = philox4x32(make_uint4((uint32_t)e, (uint32_t)(e >> 32) ^ (launch << 8), (uint32_t)(i >> 2), 2u),
                                key);
-            // hidden-2 units of degree i see only x_<i, all drawn by now
-            for (int k = lane; k < H; k += 32)
-                if (made_degree(k, N) == i) h2[k] = made_h2(W, o, H, k, h1);
-            __syncwarp();
-            const float l = made_logit(W, o, N, H, i, h2);
+            if (i >= 1) {
+                const int k1 = made_first(i + 1, N, H);
+                for (int k = made_first(i, N, H); k < k1; k++) {
+                    const float h2 = made_h2_reg<H>(W, W2n, o, k, a1);
+                    for (int io = i; io < N; io++)
+                        Ls[io * POOL_T + tid] = fmaf(bf(W, o.w3 + (long)k * N + io), h2, Ls[io * POOL_T + tid]);
+                }
+            }
+            const float l = Ls[i * POOL_T + tid] + bf(W, o.b3 + i);
             const int f = made_forced(i, ones, N, m.n_ones);
             int xi;
             if (f >= 0) {
@@ -106,23 +145,41 @@ __global__ void __launch_bounds__(128) k_made_pool(DevMade m, DevAmp A, long tot
                 x |= 1ull << i;
                 ones++;
 #pragma unroll
-                for (int q = 0; q < MADE_MAX_H / 32; q++) {
-                    const int k = lane + 32 * q;
-                    if (k < H) {
-                        a1[q] += bf(W, o.w1 + (long)i * H + k);
-                        h1[k] = fmaxf(a1[q], 0.f);
-                    }
+                for (int k = 0; k < H; k += 8) {                  // masked entries are 0
+                    float w[8];
+                    bf8(W + o.w1 + (long)i * H + k, w);
+#pragma unroll
+                    for (int q = 0; q < 8; q++) a1[k + q] += w[q];
                 }
             }
-            __syncwarp();
         }
-        const float lp = rbm_logabs32<CPLX>(A.a, x);
-        if (lane == 0) {
-            pbits[e] = x;
-            plq[e] = lq;
-            plpsi[e] = lp;
+        // log|psi(x)| of the RBM in FP32: the 32 lane partials of rbm_logabs32
+        // combined in its XOR-butterfly order, so the chains' warp evaluation of
+        // the same configuration gives the same number
+        const DevAnsatz &a = A.a;
+        for (int l = 0; l < 32; l++) {
+            float acc = 0.f;
+            for (int h = l; h < a.M; h += 32) {
+                float xr = a.b32[h].x, xim = a.b32[h].y;
+                for (int i = 0; i < a.N; i++) {
+                    const float sp = (x >> i) & 1ull ? -1.f : 1.f;
+                    const float2 w = a.w32[(long)i * a.M + h];
+                    xr = fmaf(sp, w.x, xr);
+                    if (CPLX) xim = fmaf(sp, w.y, xim);
+                }
+                const float ax = fabsf(xr), ee = expf(-2.f * ax);
+                acc += CPLX ? ax + 0.5f * log1pf(ee * (2.f * cosf(2.f * xim) + ee)) : ax + log1pf(ee);
+            }
+            for (int i = l; i < a.N; i += 32) acc += ((x >> i) & 1ull ? -1.f : 1.f) * a.a32[i].x;
+            Ps[l * POOL_T + tid] = acc;
         }
-        __syncwarp();
+        for (int off = 16; off > 0; off >>= 1)
+            for (int l = 0; l < off; l++)
+                Ps[l * POOL_T + tid] = Ps[l * POOL_T + tid] + Ps[(l + off) * POOL_T + tid];
+        const float lp = Ps[tid];
+        pbits[e] = x;
+        plq[e] = lq;
+        plpsi[e] = lp;
     }
 }
 
@@ -240,12 +297,11 @@ __global__ void k_made_adam(float *w, float *m1, float *v1, const float *__restr
 // proposals, 3: accepted).
 __global__ void k_made_stats(const float *nllp, int nw, int B, double *stats, const unsigned long long *counts,
                              int *active, double min_acc) {
+    double s = 0.0;
+    for (int q = threadIdx.x; q < nw; q += 32) s += (double)nllp[q];
+    s = warp_sum(s);
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (nw > 0) {
-        double s = 0.0;
-        for (int q = 0; q < nw; q++) s += (double)nllp[q];
-        stats[0] = s / (double)B;
-    }
+    if (nw > 0) stats[0] = s / (double)B;
     const double p = (double)counts[2], a = (double)counts[3];
     const double dp = p - stats[4], da = a - stats[5];
     stats[1] = p;
@@ -338,7 +394,25 @@ size_t made_chain_smem(const Made *m, int warps) {
     return (size_t)(wbytes + (long)warps * 2 * m->H * 4);
 }
 
-static size_t pool_smem(const Made *m) { return made_chain_smem(m, 4); }
+static size_t pool_smem(const Made *m) {
+    const long wbytes = (m->PM * 2 + 15) / 16 * 16;
+    return (size_t)(wbytes + (long)m->H * m->H * 2 + (long)(m->N + 32) * POOL_T * 4);
+}
+
+template <int H>
+static void pool_kernel(const Made *m, unsigned grid, size_t smem, const DevMade &d, const DevAmp &A, long count,
+                        uint64_t seed, float *plq, float *plpsi, uint64_t *pbits) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_made_pool<H, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_made_pool<H, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    if (A.a.kind == KIND_CRBM)
+        k_made_pool<H, true><<<grid, POOL_T, smem, ctx().stream>>>(d, A, count, seed, m->launch_id, pbits, plq, plpsi);
+    else
+        k_made_pool<H, false><<<grid, POOL_T, smem, ctx().stream>>>(d, A, count, seed, m->launch_id, pbits, plq, plpsi);
+}
 
 // Draw `count` proposals into the pool (count = chains x per_chain).
 static bool pool_launch(Made *m, const DevAmp &A, long count, uint64_t seed, DevMade &d) {
@@ -348,22 +422,15 @@ static bool pool_launch(Made *m, const DevAmp &A, long count, uint64_t seed, Dev
     d.plq = m->plq.p;
     d.plpsi = m->plpsi.p;
     const size_t smem = pool_smem(m);
-    static bool attr = false;
-    if (!attr) {
-        if (!NQS_CUDA(cudaFuncSetAttribute(k_made_pool<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) ||
-            !NQS_CUDA(cudaFuncSetAttribute(k_made_pool<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)))
-            return false;
-        attr = true;
-    }
-    const long blocks = (count + 3) / 4;
-    const unsigned grid = (unsigned)(blocks < (long)ctx().sm_count * 16 ? blocks : (long)ctx().sm_count * 16);
+    const long blocks = (count + POOL_T - 1) / POOL_T;
+    const unsigned grid = (unsigned)(blocks < (long)ctx().sm_count * 8 ? blocks : (long)ctx().sm_count * 8);
     NQS_LAUNCH("made_pool");
-    if (A.a.kind == KIND_CRBM)
-        k_made_pool<true><<<grid, 128, smem, ctx().stream>>>(d, A, count, seed, m->launch_id, m->pbits.p, m->plq.p,
-                                                              m->plpsi.p);
-    else
-        k_made_pool<false><<<grid, 128, smem, ctx().stream>>>(d, A, count, seed, m->launch_id, m->pbits.p, m->plq.p,
-                                                               m->plpsi.p);
+    switch (m->H) {
+        case 32: pool_kernel<32>(m, grid, smem, d, A, count, seed, m->plq.p, m->plpsi.p, m->pbits.p); break;
+        case 64: pool_kernel<64>(m, grid, smem, d, A, count, seed, m->plq.p, m->plpsi.p, m->pbits.p); break;
+        case 96: pool_kernel<96>(m, grid, smem, d, A, count, seed, m->plq.p, m->plpsi.p, m->pbits.p); break;
+        default: pool_kernel<128>(m, grid, smem, d, A, count, seed, m->plq.p, m->plpsi.p, m->pbits.p); break;
+    }
     m->launch_id++;
     return NQS_CUDA(cudaGetLastError());
 }
@@ -375,7 +442,10 @@ bool made_prepare(Made *m, const DevAmp &A, int C, int total_moves, uint64_t see
         *out = d;
         return true;
     }
-    const int per = (int)ceil((double)total_moves * mix * 1.25) + 16;
+    // learned slots per chain ~ Binomial(total_moves, mix): the pool holds the
+    // mean + 4 standard deviations + 2 (a chain that runs out rejects)
+    const double mean = (double)total_moves * mix, sd = sqrt(mean * (1.0 - mix));
+    const int per = (int)ceil(mean + 4.0 * sd) + 2;
     if (!pool_launch(m, A, (long)C * per, seed, d)) return false;
     d.per_chain = per;
     d.mix_thr = mix >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(mix * 4294967296.0);
@@ -417,6 +487,9 @@ static int grad_launch(Made *m, const uint64_t *bits, int B) {
 
 bool made_train(Made *m, const uint64_t *bits, int B, const unsigned long long *counts) {
     if (B <= 0) return true;
+    // train on the first train_batch rows: with the sampler's layout (sample k
+    // of chain c at row k C + c) these are the latest states of distinct chains
+    if (m->opt.train_batch > 0 && B > m->opt.train_batch) B = m->opt.train_batch;
     cudaStream_t s = ctx().stream;
     int nw = 0;
     for (int it = 0; it < m->opt.train_iters; it++) {

@@ -5,7 +5,8 @@
 //   h1 = relu(W1 x + b1), h2 = relu(W2 h1 + b2), p(x_i = 1 | x_<i) = sigmoid(W3 h2 + b3)_i
 //
 // x_i = 1 marks a down spin (the bit convention of the configurations).  Unit
-// k of either hidden layer has degree m(k) = 1 + k mod (N - 1); the masks keep
+// k of either hidden layer has degree m(k) = 1 + floor(k (N - 1) / H), so the
+// units of one degree are contiguous; the masks keep
 // W1[k][i] for m(k) >= i + 1, W2[k][j] for m(k) >= m(j) and W3[i][k] for
 // i + 1 > m(k), so output i sees only x_<i.  With a fixed number of down spins
 // (exchange moves conserve it) a site whose value is already determined by the
@@ -42,19 +43,22 @@ __host__ __device__ inline MadeOff made_off(int N, int H) {
     return o;
 }
 
-__host__ __device__ inline int made_degree(int k, int N) { return N > 1 ? 1 + k % (N - 1) : 1; }
+__host__ __device__ inline int made_degree(int k, int N, int H) { return 1 + (k * (N - 1)) / H; }
+
+// first unit of degree d (d = 1 .. N; made_first(N) = H)
+__host__ __device__ inline int made_first(int d, int N, int H) { return ((d - 1) * H + N - 2) / (N - 1); }
 
 // Whether parameter p of the layout is kept by the masks.
 __host__ __device__ inline bool made_kept(long p, int N, int H) {
     const MadeOff o = made_off(N, H);
-    if (p < o.b1) return made_degree((int)(p % H), N) >= (int)(p / H) + 1;               // W1t[i][k]
+    if (p < o.b1) return made_degree((int)(p % H), N, H) >= (int)(p / H) + 1;            // W1t[i][k]
     if (p >= o.w2 && p < o.b2) {
         const long q = p - o.w2;
-        return made_degree((int)(q % H), N) >= made_degree((int)(q / H), N);           // W2t[j][k]
+        return made_degree((int)(q % H), N, H) >= made_degree((int)(q / H), N, H);     // W2t[j][k]
     }
     if (p >= o.w3 && p < o.b3) {
         const long q = p - o.w3;
-        return (int)(q % N) + 1 > made_degree((int)(q / N), N);                        // W3t[k][i]
+        return (int)(q % N) + 1 > made_degree((int)(q / N), N, H);                     // W3t[k][i]
     }
     return true;                                                                       // biases
 }
@@ -94,30 +98,41 @@ __device__ __forceinline__ float warp_sumf(float v) {
 __device__ __forceinline__ float bf(const __nv_bfloat16 *p, long i) { return __bfloat162float(p[i]); }
 
 // Building blocks shared by the autoregressive sampler, the teacher-forced
-// log q and the training forward pass, written once so that all of them round
-// identically (q(x) is the same FP32 number whichever path computes it).
-// Lanes own hidden units k = lane + 32 q.
+// log q and the chains, written once so that all of them round identically
+// (q(x) is the same FP32 number whichever path computes it).  Lanes own
+// hidden units k = lane + 32 q and outputs i = lane + 32 q.
 
-// h2_k = relu(b2_k + sum_j W2t[j][k] h1_j), ascending j
+// h2_k = relu(b2_k + sum_j W2t[j][k] h1_j), four interleaved partial sums
 __device__ __forceinline__ float made_h2(const __nv_bfloat16 *W, const MadeOff &o, int H, int k, const float *h1,
                                          float *a2_out = nullptr) {
-    float a = bf(W, o.b2 + k);
-    for (int j = 0; j < H; j++) a = fmaf(bf(W, o.w2 + (long)j * H + k), h1[j], a);
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    const __nv_bfloat16 *w = W + o.w2 + k;
+#pragma unroll 4
+    for (int j = 0; j < H; j += 4) {
+        s0 = fmaf(__bfloat162float(w[(long)j * H]), h1[j], s0);
+        s1 = fmaf(__bfloat162float(w[(long)(j + 1) * H]), h1[j + 1], s1);
+        s2 = fmaf(__bfloat162float(w[(long)(j + 2) * H]), h1[j + 2], s2);
+        s3 = fmaf(__bfloat162float(w[(long)(j + 3) * H]), h1[j + 3], s3);
+    }
+    const float a = bf(W, o.b2 + k) + ((s0 + s1) + (s2 + s3));
     if (a2_out) *a2_out = a;
     return fmaxf(a, 0.f);
 }
 
-// logit_i = b3_i + warp sum of the lane partials sum_q W3t[k][i] h2_k
-__device__ __forceinline__ float made_logit(const __nv_bfloat16 *W, const MadeOff &o, int N, int H, int i,
-                                            const float *h2) {
-    const int lane = threadIdx.x & 31;
-    float part = 0.f;
-    for (int k = lane; k < H; k += 32) part = fmaf(bf(W, o.w3 + (long)k * N + i), h2[k], part);
-    return warp_sumf(part) + bf(W, o.b3 + i);
+// Contribution of the hidden-2 units of degree d (contiguous, ascending k) to
+// the running logit of output i.
+__device__ __forceinline__ float made_logit_add(const __nv_bfloat16 *W, const MadeOff &o, int N, int H, int d, int i,
+                                                const float *h2, float L) {
+    const int k1 = made_first(d + 1, N, H);
+    for (int k = made_first(d, N, H); k < k1; k++) L = fmaf(bf(W, o.w3 + (long)k * N + i), h2[k], L);
+    return L;
 }
 
 // log q(x) with teacher forcing, one warp.  W: BF16 weights (shared or global),
-// h1 / h2: per-warp scratch of H floats each.
+// h1 / h2: per-warp scratch of H floats each.  The logit of output i sums the
+// hidden-2 units degree by degree (d = 1 .. i), the order in which the
+// autoregressive sampler finalises them, and log q adds the free sites in
+// ascending order.
 __device__ __forceinline__ float made_logq_warp(const DevMade &m, const __nv_bfloat16 *W, uint64_t x, float *h1,
                                                 float *h2) {
     const int lane = threadIdx.x & 31, N = m.N, H = m.H;
@@ -131,14 +146,21 @@ __device__ __forceinline__ float made_logq_warp(const DevMade &m, const __nv_bfl
     __syncwarp();
     for (int k = lane; k < H; k += 32) h2[k] = made_h2(W, o, H, k, h1);
     __syncwarp();
-    float lq = 0.f;
-    int ones = 0;
-    for (int i = 0; i < N; i++) {
-        const float l = made_logit(W, o, N, H, i, h2);
-        const int xi = (int)((x >> i) & 1ull);
-        if (made_forced(i, ones, N, m.n_ones) < 0) lq += xi ? log_sigmoid(l) : log_sigmoid(-l);
-        ones += xi;
+    float term[2] = {0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int i = lane + 32 * q;
+        if (i < N) {
+            float L = 0.f;
+            for (int d = 1; d <= i && d < N; d++) L = made_logit_add(W, o, N, H, d, i, h2, L);
+            const float l = L + bf(W, o.b3 + i);
+            const int xi = (int)((x >> i) & 1ull);
+            if (made_forced(i, __popcll(x & ((1ull << i) - 1ull)), N, m.n_ones) < 0)
+                term[q] = xi ? log_sigmoid(l) : log_sigmoid(-l);
+        }
     }
+    float lq = 0.f;
+    for (int i = 0; i < N; i++) lq += __shfl_sync(0xffffffffu, i < 32 ? term[0] : term[1], i & 31);
     __syncwarp();
     return lq;
 }

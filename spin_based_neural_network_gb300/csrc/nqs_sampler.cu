@@ -752,7 +752,8 @@ nqs_gpu_made_options_t nqs_gpu_made_options_default(void) {
     nqs_gpu_made_options_t o;
     memset(&o, 0, sizeof(o));
     o.hidden = 64;
-    o.train_iters = 2;
+    o.train_iters = 1;
+    o.train_batch = 1024;
     o.mix = 0.5;
     o.learning_rate = 3e-3;
     o.min_acceptance = 0.01;

@@ -13,7 +13,7 @@ def bf16(a):
 
 
 def degrees(N, H):
-    return 1 + np.arange(H) % (N - 1)
+    return 1 + (np.arange(H) * (N - 1)) // H
 
 
 def masks(N, H):
