@@ -135,48 +135,69 @@ bool hamiltonian_build(const nqs_config_t *cfg, int size_x, int size_y, DevHam *
 
 constexpr int kWarps = 4;
 
+// v * s_i for s_i = +-1: a sign flip, exact
+__device__ __forceinline__ double sflip(double v, uint64_t bits, int i) { return ((bits >> i) & 1ull) ? -v : v; }
+
 // Jacobian row from precomputed tanh(theta) (tr, ti in shared memory);
-// same layouts as warp_grad_row in nqs_ansatz.cu.
+// same layouts and values as warp_grad_row in nqs_ansatz.cu.  The weight block
+// W[h][i] (entry N + M + h N + i) is swept with per-lane (h, i) counters and
+// the products t_h s_i are sign flips, so the row costs stores, not FP64
+// arithmetic or integer division.
 __device__ void rbm_row_from_t(const DevAnsatz &a, uint64_t bits, int mode, double *o, double *oi,
                                const double *tr, const double *ti) {
-    int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
     const int N = a.N, M = a.M;
-    if (a.kind == KIND_RBM) {
-        for (long k = lane; k < a.P; k += 32) {
-            double v;
-            if (k < N) v = (double)spin_of(bits, (int)k);
-            else if (k < N + M) v = tr[k - N];
-            else {
-                long q = k - N - M;
-                v = tr[q / N] * (double)spin_of(bits, (int)(q % N));
-            }
-            o[k] = v;
-            if (mode == 2) oi[k] = 0.0;
-        }
-        return;
-    }
-    long Pr = crbm_pr(a);
-    for (long k = lane; k < Pr; k += 32) {
-        double sr, si;
-        if (k < N) {
-            sr = (double)spin_of(bits, (int)k);
-            si = 0.0;
-        } else if (k < N + M) {
-            sr = tr[k - N];
-            si = ti[k - N];
-        } else {
-            long q = k - N - M;
-            double s = (double)spin_of(bits, (int)(q % N));
-            sr = tr[q / N] * s;
-            si = ti[q / N] * s;
-        }
+    const bool cx = a.kind == KIND_CRBM;
+    const long Pr = cx ? crbm_pr(a) : a.P;
+    for (int k = lane; k < N; k += 32) {
+        const double sr = sflip(1.0, bits, k);
         o[k] = sr;
-        if (mode == 2) {
+        if (!cx) {
+            if (mode == 2) oi[k] = 0.0;
+        } else if (mode == 2) {
+            oi[k] = 0.0;
+            o[Pr + k] = -0.0;
+            oi[Pr + k] = sr;
+        } else {
+            o[Pr + k] = 0.0;
+        }
+    }
+    for (int h = lane; h < M; h += 32) {
+        const long k = N + h;
+        const double sr = tr[h], si = cx ? ti[h] : 0.0;
+        o[k] = sr;
+        if (!cx) {
+            if (mode == 2) oi[k] = 0.0;
+        } else if (mode == 2) {
             oi[k] = si;
             o[Pr + k] = -si;
             oi[Pr + k] = sr;
         } else {
-            o[Pr + k] = k < N ? 0.0 : -si;
+            o[Pr + k] = -si;
+        }
+    }
+    const long nw = (long)M * N, base = (long)N + M;
+    int h = lane / N, i = lane % N;
+    for (long e = lane; e < nw; e += 32) {
+        const long k = base + e;
+        const double sr = sflip(tr[h], bits, i);
+        o[k] = sr;
+        if (!cx) {
+            if (mode == 2) oi[k] = 0.0;
+        } else {
+            const double si = sflip(ti[h], bits, i);
+            if (mode == 2) {
+                oi[k] = si;
+                o[Pr + k] = -si;
+                oi[Pr + k] = sr;
+            } else {
+                o[Pr + k] = -si;
+            }
+        }
+        i += 32;
+        while (i >= N) {
+            i -= N;
+            h++;
         }
     }
 }

@@ -154,6 +154,7 @@ struct GramTcArgs {
     float *C;             // [n][n] lower triangle written
     int n;
     int *err;
+    int split;            // 1: blockIdx.y = pass, raw partial sums into C + pass * n * n
 };
 
 __global__ void __launch_bounds__(128, 1)
@@ -196,7 +197,7 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int total = g.kt_per_seg * g.nseg;
+    const int total = g.split ? g.kt_per_seg : g.kt_per_seg * g.nseg;
     bool ok = true;
 
     if (warp == 0 && lane == 0) {
@@ -205,7 +206,8 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
             int s = it % TC_STAGES, u = it / TC_STAGES;
             if (u > 0) ok = mbar_wait(&empty[s], (u - 1) & 1, g.err);
             if (!ok) break;
-            int seg = it / g.kt_per_seg, kt = it - seg * g.kt_per_seg;
+            const int seg = g.split ? (int)blockIdx.y : it / g.kt_per_seg;
+            const int kt = g.split ? it : it - seg * g.kt_per_seg;
             const CUtensorMap *ma = seg == 2 ? &map_lo : &map_hi;   // segments: (hi,hi) (hi,lo) (lo,hi)
             const CUtensorMap *mb = seg == 1 ? &map_lo : &map_hi;
             uint8_t *sa = sm + s * TC_STAGE_BYTES;
@@ -243,7 +245,14 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
             float v[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
             int col0 = bj * TC_N + c * 32;
-            if (row < g.n) {
+            if (row < g.n && g.split) {
+                float *dst = g.C + (size_t)blockIdx.y * g.n * g.n + (size_t)row * g.n;
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int col = col0 + j;
+                    if (col <= row && col < g.n) dst[col] = v[j];
+                }
+            } else if (row < g.n) {
                 float *dst = g.C + (size_t)row * g.n;
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
@@ -257,6 +266,16 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
+    }
+}
+
+// T = scale ((P0 + P1) + P2) + shift I on the lower triangle, from the three
+// per-pass partial Grams of a split launch.
+__global__ void k_gram_sum(const float *__restrict__ Pp, int n, float scale, float shift, float *T) {
+    const size_t nn = (size_t)n * n;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e / n), c = (int)(e % n);
+        if (c <= r) T[e] = ((Pp[e] + Pp[nn + e]) + Pp[2 * nn + e]) * scale + (r == c ? shift : 0.f);
     }
 }
 
@@ -1037,7 +1056,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
 
 // ---------------------------------------------------------------- driver
 struct MixedWs {
-    DevBuf<float> hi, lo, T, Li, LiT, rf, zf;
+    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf;
     DevBuf<double> rhs, r, u, upart, nrm;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -1049,19 +1068,22 @@ struct MixedWs {
 static MixedWs g_mx;
 
 struct MixedPlan {
+    bool split;       // tensor-core Gram with one CTA per (tile, pass)
     int space;        // 0 samples, 1 parameters
     int n;            // order of the solved system
     long rows_pad;    // Gram operand rows (n padded to TC_M)
     long k_pad;       // Gram operand K (the other dimension padded to TC_K)
 };
 
-static MixedPlan plan_mixed(int Ns, long P, int space_opt) {
+static MixedPlan plan_mixed(int Ns, long P, int space_opt, int passes) {
     MixedPlan p;
     p.space = space_opt == 1 ? 0 : space_opt == 2 ? 1 : ((long)Ns > P ? 1 : 0);
     const long rows = p.space ? P : Ns, k = p.space ? Ns : P;
     p.n = (int)rows;
     p.rows_pad = (rows + TC_M - 1) / TC_M * TC_M;
     p.k_pad = (k + TC_K - 1) / TC_K * TC_K;
+    const long nt = p.rows_pad / TC_M;
+    p.split = passes >= 3 && 2 * nt * (nt + 1) / 2 <= ctx().sm_count;
     return p;
 }
 
@@ -1123,7 +1145,17 @@ static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, cons
     g.n = pl.n;
     g.err = err;
     const int nt = (int)(pl.rows_pad / TC_M);
-    {
+    g.split = pl.split ? 1 : 0;
+    if (pl.split) {
+        // few lower-triangular tiles (parameter space): one CTA per tile and pass
+        g.C = w.Tp.p;
+        {
+            NQS_LAUNCH("gram_tc");
+            k_gram_tf32_tc<<<dim3(nt * (nt + 1) / 2, 3), 128, TC_SMEM, st>>>(mh, ml, g);
+        }
+        NQS_LAUNCH("gram_sum");
+        k_gram_sum<<<ctx().sm_count * 4, 256, 0, st>>>(w.Tp.p, pl.n, g.scale, g.shift, w.T.p);
+    } else {
         NQS_LAUNCH("gram_tc");
         k_gram_tf32_tc<<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(mh, ml, g);
     }
@@ -1191,7 +1223,7 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
     Context &c = ctx();
     cudaStream_t st = c.stream;
     MixedWs &w = g_mx;
-    const MixedPlan pl = plan_mixed(Ns, P, space_opt);
+    const MixedPlan pl = plan_mixed(Ns, P, space_opt, passes);
     const int n = pl.n;
     bool moved = false;
     if (pl.rows_pad != w.rows_pad || pl.k_pad != w.k_pad || pl.space != w.space) {
@@ -1206,17 +1238,17 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
         moved = true;
     }
     const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[12] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                              w.nrm.p, w.bar.p, w.tm.p};
+    const void *before[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
     const int ldl = (n + 31) / 32 * 32;
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
         !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(2) || !w.status.ensure(2) ||
-        !w.bar.ensure(2) || !w.tm.ensure(8))
+        !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
-    const void *after[12] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                             w.nrm.p, w.bar.p, w.tm.p};
-    for (int i = 0; i < 12; i++) moved |= before[i] != after[i];
+    const void *after[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
+    for (int i = 0; i < 13; i++) moved |= before[i] != after[i];
     if (moved || w.n != n) {
         // the pad columns of L^{-1} are read (as zeros) by the vectorised solves
         if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
@@ -1347,6 +1379,7 @@ int nqs_gpu_gram_tc(const double *O_host, int Ns, long P, int passes, double sca
     g.C = w.T.p;
     g.n = Ns;
     g.err = err.p;
+    g.split = 0;
     if (!NQS_CUDA(cudaFuncSetAttribute(k_gram_tf32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM)))
         return -1;
     int nt = ns_pad / TC_M;
