@@ -135,8 +135,13 @@ bool hamiltonian_build(const nqs_config_t *cfg, int size_x, int size_y, DevHam *
 
 constexpr int kWarps = 4;
 
-// v * s_i for s_i = +-1: a sign flip, exact
-__device__ __forceinline__ double sflip(double v, uint64_t bits, int i) { return ((bits >> i) & 1ull) ? -v : v; }
+// v * s_i for s_i = +-1 and -v: sign-bit flips on the integer pipe, exact
+__device__ __forceinline__ double sflip(double v, uint64_t bits, int i) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (long long)(((bits >> i) & 1ull) << 63));
+}
+__device__ __forceinline__ double dneg(double v) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (long long)(1ull << 63));
+}
 
 // Jacobian row from precomputed tanh(theta) (tr, ti in shared memory);
 // same layouts and values as warp_grad_row in nqs_ansatz.cu.  The weight block
@@ -170,10 +175,10 @@ __device__ void rbm_row_from_t(const DevAnsatz &a, uint64_t bits, int mode, doub
             if (mode == 2) oi[k] = 0.0;
         } else if (mode == 2) {
             oi[k] = si;
-            o[Pr + k] = -si;
+            o[Pr + k] = dneg(si);
             oi[Pr + k] = sr;
         } else {
-            o[Pr + k] = -si;
+            o[Pr + k] = dneg(si);
         }
     }
     const long nw = (long)M * N, base = (long)N + M;
@@ -188,10 +193,10 @@ __device__ void rbm_row_from_t(const DevAnsatz &a, uint64_t bits, int mode, doub
             const double si = sflip(ti[h], bits, i);
             if (mode == 2) {
                 oi[k] = si;
-                o[Pr + k] = -si;
+                o[Pr + k] = dneg(si);
                 oi[Pr + k] = sr;
             } else {
-                o[Pr + k] = -si;
+                o[Pr + k] = dneg(si);
             }
         }
         i += 32;

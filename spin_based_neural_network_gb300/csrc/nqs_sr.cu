@@ -153,6 +153,49 @@ __global__ void k_col_stats(const double *__restrict__ O, int Ns, long P, const 
     }
 }
 
+// The same statistics over a 2-D grid: partial column sums over row chunks
+// (32 columns x 8 row groups per block), then a fixed-order sum over the
+// chunks (deterministic).
+__global__ void k_col_part(const double *__restrict__ O, int Ns, long P, const double *__restrict__ E, int rows_per,
+                           double *part) {
+    __shared__ double a[8][33], b[8][33];
+    const long k = (long)blockIdx.x * 32 + threadIdx.x;
+    const int r0 = blockIdx.y * rows_per, r1 = min(Ns, r0 + rows_per);
+    double s = 0.0, se = 0.0;
+    if (k < P)
+        for (int i = r0 + threadIdx.y; i < r1; i += 8) {
+            const double g = O[(size_t)i * P + k];
+            s += g;
+            if (E) se += g * E[i];
+        }
+    a[threadIdx.y][threadIdx.x] = s;
+    b[threadIdx.y][threadIdx.x] = se;
+    __syncthreads();
+    if (threadIdx.y == 0 && k < P) {
+        double S = 0.0, SE = 0.0;
+        for (int y = 0; y < 8; y++) {
+            S += a[y][threadIdx.x];
+            SE += b[y][threadIdx.x];
+        }
+        part[(size_t)blockIdx.y * 2 * P + k] = S;
+        part[(size_t)blockIdx.y * 2 * P + P + k] = SE;
+    }
+}
+
+__global__ void k_col_fin(const double *__restrict__ part, int nchunk, int Ns, long P, const double *__restrict__ scal,
+                          double *gm, double *F) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P) return;
+    double S = 0.0, SE = 0.0;
+    for (int c = 0; c < nchunk; c++) {
+        S += part[(size_t)c * 2 * P + k];
+        SE += part[(size_t)c * 2 * P + P + k];
+    }
+    const double m = S / (double)Ns;
+    gm[k] = m;
+    if (F) F[k] = SE / (double)Ns - m * scal[S_EMEAN];     // src/nqs/nqs_optimizer.c:213-215
+}
+
 __global__ void k_center(double *O, int Ns, long P, const double *__restrict__ gm) {
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, tot = (size_t)Ns * P;
     for (; t < tot; t += (size_t)gridDim.x * blockDim.x) O[t] -= gm[t % P];
@@ -577,6 +620,25 @@ struct StepIn {
     int minsr;
 };
 
+// Column means of O (and the CG-SR force F when E != NULL) over a 2-D grid of
+// about four blocks per SM.
+static bool col_stats(const double *O, int Ns, long P, const double *E, const double *scal, double *gm, double *F) {
+    static DevBuf<double> part;
+    const int gx = (int)((P + 31) / 32);
+    int rb = (4 * ctx().sm_count + gx - 1) / gx;
+    rb = rb < 1 ? 1 : rb > (Ns + 63) / 64 ? (Ns + 63) / 64 : rb;
+    const int rows_per = (Ns + rb - 1) / rb;
+    rb = (Ns + rows_per - 1) / rows_per;
+    if (!part.ensure((size_t)rb * 2 * P)) return false;
+    cudaStream_t st = ctx().stream;
+    k_col_part<<<dim3((unsigned)gx, (unsigned)rb), dim3(32, 8), 0, st>>>(O, Ns, P, E, rows_per, part.p);
+    {
+        NQS_LAUNCH("col_sum");
+        k_col_fin<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(part.p, rb, Ns, P, scal, gm, F);
+    }
+    return NQS_CUDA(cudaGetLastError());
+}
+
 static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
     clear_error();
     const nqs_config_t *cfg = in.cfg;
@@ -695,7 +757,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, w.O.p, nullptr, 1, false)) return -1;
         dim3 cb0(32, 8), cg0((unsigned)((P + 31) / 32));
         k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
-        k_col_stats<<<cg0, cb0, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
+        if (!col_stats(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr)) return -1;
         k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
         int conv64 = 0;
         if (fp64_solve(w.y64.p, &conv64) != 0) return -1;
@@ -734,7 +796,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns)) return -1;
         {
             NQS_LAUNCH("col_mean");
-            k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr);
+            if (!col_stats(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr)) return -1;
         }
         ss.refine_residual = 0.0;
         ss.refine_sweeps = 0;
@@ -802,7 +864,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             return -1;
         {
             NQS_LAUNCH("col_stats");
-            k_col_stats<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.E.p, w.scal.p, w.gm.p, w.F.p);
+            if (!col_stats(w.O.p, Ns, P, w.E.p, w.scal.p, w.gm.p, w.F.p)) return -1;
         }
         {
             NQS_LAUNCH("cg_init");
