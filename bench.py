@@ -248,6 +248,13 @@ def exact_e0(name="heisenberg_4x4_pbc_sz0"):
         return json.load(f)[name]["E0"]
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of the kernel on this
+# workload (dram__bytes_read.sum + dram__bytes_write.sum), and the summary file.
+NCU_TRAFFIC = {
+    "factor_refine": (39.525632e6 + 0.218368e6, "profiles/factor_refine_heisenberg4x4_params1120_full.md"),
+    "gram_tc": (37.775616e6 + 7.168e3, "profiles/gram_tc_split_params1120_ns4096_full.md"),
+}
+
 CONV_LR = 0.02        # learning rate of the accuracy run (real RBM alpha = 2, same lattice and sampler)
 
 
@@ -445,7 +452,9 @@ def run_gpu(args):
         return {"bound": "tensor", "kernel": name, "pipe": pipe, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": "bf16_tflops of measured",
                 "frac_of_pipe_nominal": achieved / nominal[pipe], "pipe_nominal_tflops": nominal[pipe],
-                "traffic": None, "share_of_step": ms / total, "avg_launch_us": 1000.0 * ms / cnt}
+                "traffic": NCU_TRAFFIC.get(name, (None, None))[0],
+                "traffic_source": NCU_TRAFFIC.get(name, (None, None))[1],
+                "share_of_step": ms / total, "avg_launch_us": 1000.0 * ms / cnt}
 
     top_name = max(prof.items(), key=lambda kv: kv[1][1])[0]
     roof = roofline_of(top_name)
