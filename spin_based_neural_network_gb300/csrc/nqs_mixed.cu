@@ -341,13 +341,13 @@ __device__ __forceinline__ unsigned long long gtimer() {
     return t;
 }
 
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned count) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = bar + 1;
         const unsigned g0 = *gen;
         __threadfence();
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+        if (atomicAdd(bar, 1u) == count - 1) {
             bar[0] = 0;
             __threadfence();
             atomicAdd(bar + 1, 1u);
@@ -782,21 +782,24 @@ struct FrArgs {
     unsigned long long *tm;   // [8] phase nanoseconds: [0..6] CTA 0's view, [7] owners' block work
 };
 
-__global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
+// The solve of one system by the CTAs bx = 0 .. G-1 of a cooperative launch
+// (all co-resident): the whole grid for a single system, a slice of it when a
+// batch of systems shares one launch.
+__device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int G) {
     extern __shared__ float psm[];
     float (*S0)[BT + 1] = (float (*)[BT + 1])psm;
     float (*S1)[BT + 1] = (float (*)[BT + 1])(psm + BT * (BT + 1));
     TileSmem &TS = *(TileSmem *)psm;
     float (*ST)[GT + 1] = (float (*)[GT + 1])psm;           // 64 x 65 staging tile
-    const int n = a.n, ldl = a.ldl, tid = threadIdx.x, G = gridDim.x;
+    const int n = a.n, ldl = a.ldl, tid = threadIdx.x;
     const int lane = tid & 31, tx = tid & 15, ty = tid >> 4;
-    const int gtid = blockIdx.x * PS_THREADS + tid, gthreads = G * PS_THREADS;
-    const int gwarp = blockIdx.x * (PS_THREADS / 32) + (tid >> 5), gwarps = G * (PS_THREADS / 32);
+    const int gtid = bx * PS_THREADS + tid, gthreads = G * PS_THREADS;
+    const int gwarp = bx * (PS_THREADS / 32) + (tid >> 5), gwarps = G * (PS_THREADS / 32);
     const int nb = (n + BT - 1) / BT;
     __shared__ int s_flag;
     __shared__ float tmpb[3 * 1024];
     unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const bool timing = blockIdx.x == 0 && tid == 0;
+    const bool timing = a.tm != nullptr && bx == 0 && tid == 0;
     unsigned long long tstart = timing ? gtimer() : 0, tprev = tstart;
 #define NQS_PHASE(k)                                  \
     if (timing) {                                     \
@@ -808,7 +811,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
     // ---------------- factor
     for (int kb = 0; kb < nb; kb++) {
         const int k0 = kb * BT, bs = min(BT, n - k0), k1 = k0 + bs, rest = n - k1;
-        if (blockIdx.x == kb % G) {
+        if (bx == kb % G) {
             const unsigned long long t_own = tid == 0 ? gtimer() : 0;
             for (int e0 = 0; e0 < BT * BT; e0 += 8 * PS_THREADS) {
                 float v[8];
@@ -841,16 +844,16 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                     }
                 }
             }
-            if (tid == 0) atomicAdd(a.tm + 7, gtimer() - t_own);
+            if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
         NQS_PHASE(0);
         if (rest <= 0) break;
         // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1
         {
             const int ntr = (rest + GT - 1) / GT;
-            for (int t = blockIdx.x; t < 2 * ntr; t += G) {
+            for (int t = bx; t < 2 * ntr; t += G) {
                 const int c0 = (t & 1) * GT, r0 = k1 + (t >> 1) * GT;
                 if (c0 >= bs) continue;
                 float acc[4][4] = {};
@@ -865,12 +868,12 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                     }
             }
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(1);
         // trailing update: A[i][j] -= sum_m U[k0 + m][i] U[k0 + m][j], k1 <= j <= i
         {
             const int ntt = (rest + GT - 1) / GT, ntiles = ntt * (ntt + 1) / 2;
-            for (int t = blockIdx.x; t < ntiles; t += G) {
+            for (int t = bx; t < ntiles; t += G) {
                 int bi, bj;
                 tri_tile(t, bi, bj);
                 const int r0 = k1 + bi * GT, c0 = k1 + bj * GT;
@@ -889,7 +892,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                     }
             }
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(2);
     }
 
@@ -897,7 +900,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
     for (int h = 1; h < nb; h *= 2) {
         const int span = 2 * h * BT, ngrp = (n + span - 1) / span, per = 4 * h * h;
         // W = L21 X11 (into the dead lower triangle of T)
-        for (int t = blockIdx.x; t < ngrp * per; t += G) {
+        for (int t = bx; t < ngrp * per; t += G) {
             const int g = t / per, rt = (t % per) / (2 * h), ct = t % (2 * h);
             const int a0 = g * span, a1 = a0 + h * BT, a2 = min(n, a0 + span);
             const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
@@ -912,9 +915,9 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                     if (i < a2) a.T[(size_t)i * n + j] = acc[u][v];
                 }
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         // X21 = -X22 W
-        for (int t = blockIdx.x; t < ngrp * per; t += G) {
+        for (int t = bx; t < ngrp * per; t += G) {
             const int g = t / per, rt = (t % per) / (2 * h), ct = t % (2 * h);
             const int a0 = g * span, a1 = a0 + h * BT, a2 = min(n, a0 + span);
             const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
@@ -936,7 +939,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
             }
             __syncthreads();
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
     }
     NQS_PHASE(3);
 
@@ -945,7 +948,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
     const long P = a.P;
     if (a.space == 1) {
         colsum_partial(a.O, Ns, P, a.eps, a.upart, gwarp, gwarps, lane);
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         for (long k = gwarp; k < P; k += gwarps) {
             const double s = colsum_reduce(a.upart, Ns, P, k, lane) / (double)Ns;
             if (lane == 0) {
@@ -959,7 +962,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
             a.rf[i] = (float)a.eps[i];
         }
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!grid_barrier(a.bar, a.err, G)) return;
     NQS_PHASE(5);
 
     // ---------------- refinement sweeps
@@ -970,24 +973,24 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
             const float t = dot4_range(a.Li + (size_t)i * ldl, a.rf, 0, (i >> 2) + 1, lane);
             if (lane == 0) a.zf[i] = t;
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         // x += L^{-T} z (zf and the pad columns are zero beyond n)
         for (int j = gwarp; j < n; j += gwarps) {
             const float t = dot4_range(a.LiT + (size_t)j * ldl, a.zf, j >> 2, ldl >> 2, lane);
             if (lane == 0) a.x[j] = (s == 0 ? 0.0 : __ldcg(a.x + j)) + (double)t;
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(4);
         // FP64 residual r = rhs - A x
         if (a.space == 0) {
             // A y = O_c (O_c^T y) / N_s + shift y
             colsum_partial(a.O, Ns, P, a.x, a.upart, gwarp, gwarps, lane);
-            if (!grid_barrier(a.bar, a.err)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return;
             for (long k = gwarp; k < P; k += gwarps) {
                 const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
                 if (lane == 0) a.u[k] = sk;
             }
-            if (!grid_barrier(a.bar, a.err)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return;
             const double *us = stage_vec(a.u, P, (double *)psm, PS_SMEM / 8);
             for (int i = gwarp; i < Ns; i += gwarps) {
                 const double d = us == a.u ? rowdot<true>(a.O + (size_t)i * P, P, us, lane)
@@ -1006,9 +1009,9 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                                            : rowdot<false>(a.O + (size_t)i * P, P, xs, lane);
                 if (lane == 0) a.u[i] = d;
             }
-            if (!grid_barrier(a.bar, a.err)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return;
             colsum_partial(a.O, Ns, P, a.u, a.upart, gwarp, gwarps, lane);
-            if (!grid_barrier(a.bar, a.err)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return;
             for (long k = gwarp; k < P; k += gwarps) {
                 const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
                 if (lane == 0) {
@@ -1018,11 +1021,11 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
                 }
             }
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(5);
     }
     // ---------------- |r|^2 and |rhs|^2
-    if (blockIdx.x == 0) {
+    if (bx == 0) {
         double s1 = 0.0, s2 = 0.0;
         for (int i = tid; i < n; i += PS_THREADS) {
             const double ri = __ldcg(a.r + i), bi = __ldcg(a.rhs + i);
@@ -1052,6 +1055,20 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
         for (int k = 0; k < 7; k++) a.tm[k] = tacc[k];     // [7]: summed by the block owners
     }
 #undef NQS_PHASE
+}
+
+__global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) { fr_body(a, blockIdx.x, gridDim.x); }
+
+// A batch of independent systems in one cooperative launch: system i owns the
+// CTAs [cta0[i], cta0[i] + nctas[i]) and has its own barrier, status and error
+// words; cta_sys maps a CTA to its system.
+__global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrArgs *__restrict__ sys,
+                                                                       const int *__restrict__ cta_sys,
+                                                                       const int *__restrict__ cta0,
+                                                                       const int *__restrict__ nctas) {
+    const int i = cta_sys[blockIdx.x];
+    const FrArgs a = sys[i];
+    fr_body(a, blockIdx.x - cta0[i], nctas[i]);
 }
 
 // ---------------------------------------------------------------- driver
