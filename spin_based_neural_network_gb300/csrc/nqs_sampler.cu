@@ -36,12 +36,15 @@ struct Sampler {
     Made *made = nullptr;            // learned proposal (optional)
 };
 
+bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out, unsigned long long *move_dev = nullptr);
+
 struct SampleArgs {
     int C, N;
     uint64_t *bits;
     uint64_t *rng;
     uint64_t seed;
     uint64_t move0;
+    const unsigned long long *move_dev;   // when set, the first move index is read here (graph replay)
     int skip, decor, total;          // proposals: skip, then `total - skip` recorded in groups of decor
     uint64_t *out;
     int n_out;
@@ -120,6 +123,7 @@ constexpr int kSW = 4;   // warps (chains) per block
 
 template <int J, bool CPLX, int RNG, int MOVE>
 __global__ void __launch_bounds__(32 * kSW) k_sample_rbm(SampleArgs S, DevAmp A) {
+    if (S.move_dev) S.move0 = *S.move_dev;
     const int lane = threadIdx.x & 31;
     const int c = blockIdx.x * kSW + (threadIdx.x >> 5);
     if (c >= S.C) return;
@@ -251,6 +255,7 @@ __device__ __forceinline__ float2 ctanh32s(float x, float y) {
 
 template <int J, bool CPLX, int MOVE, bool LEARNED>
 __global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp A, DevMade md) {
+    if (S.move_dev) S.move0 = *S.move_dev;
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c = blockIdx.x * kSW + warp;
@@ -406,6 +411,7 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm32(SampleArgs S, DevAmp 
 // every proposal, as upstream.
 template <int RNG, int MOVE>
 __global__ void __launch_bounds__(32 * kSW) k_sample_generic(SampleArgs S, DevAmp A) {
+    if (S.move_dev) S.move0 = *S.move_dev;
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c = blockIdx.x * kSW + warp;
@@ -433,6 +439,9 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_generic(SampleArgs S, DevAm
 
 // Philox chain start: uniform bits, or a Fisher-Yates shuffle of n_down down
 // spins (fixed-magnetisation sector).  One thread per chain.
+// Device-side move counter of a replayed sampler launch.
+__global__ void k_move_advance(unsigned long long *ctr, unsigned long long total) { *ctr += total; }
+
 __global__ void k_chain_init(int C, int N, uint64_t seed, int n_down, uint64_t *bits) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
@@ -525,7 +534,7 @@ static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32, const DevMa
 
 // Advance all chains: `skip` proposals, then record `n_out` samples
 // (sample k of chain c at row k*C + c), `decor` proposals apart.
-bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
+bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out, unsigned long long *move_dev) {
     DevAmp A;
     if (!build_amp(sm->fn, sm->user, sm->N, &A, nullptr)) return false;
     int per = sm->cfg.num_decorrelate > 0 ? sm->cfg.num_decorrelate : 1;
@@ -537,6 +546,7 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
     S.rng = sm->d_rng.p;
     S.seed = sm->cfg.rng_seed;
     S.move0 = sm->move_counter;
+    S.move_dev = move_dev;
     S.skip = skip;
     S.decor = per;
     S.total = skip + n_spc * per;
@@ -550,7 +560,7 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
     const bool f32 = sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator;
     DevMade md{};
     size_t smem = 0;
-    if (sm->made && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
+    if (sm->made && !move_dev && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
         if (!made_prepare(sm->made, A, sm->C, S.total, sm->cfg.rng_seed ^ 0x9E3779B97F4A7C15ull, &md)) return false;
         smem = made_chain_smem(sm->made, kSW);
     }
@@ -562,6 +572,33 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out) {
         ok = dispatch<NQS_GPU_RNG_PHILOX, NQS_GPU_MOVE_SINGLE_FLIP>(S, A, f32, md, smem);
     sm->move_counter += (uint64_t)S.total;
     return ok;
+}
+
+// Moves per chain of a sampler_produce(sm, n) call.
+int sampler_moves(const Sampler *sm, int n) {
+    const int per = sm->cfg.num_decorrelate > 0 ? sm->cfg.num_decorrelate : 1;
+    return (n + sm->C - 1) / sm->C * per;
+}
+
+// sampler_produce for a captured step: the first move index comes from the
+// device counter move_dev, which the captured sequence advances; the host
+// counter is advanced by sampler_host_advance() once per replay.  No learned
+// proposal.
+bool sampler_produce_dev(Sampler *sm, int n, uint64_t **d_out, unsigned long long *move_dev) {
+    if (!sm->d_samples.ensure((size_t)n)) return false;
+    const uint64_t host = sm->move_counter;
+    if (!sampler_run(sm, 0, n, sm->d_samples.p, move_dev)) return false;
+    sm->move_counter = host;
+    k_move_advance<<<1, 1, 0, ctx().stream>>>(move_dev, (unsigned long long)sampler_moves(sm, n));
+    *d_out = sm->d_samples.p;
+    return NQS_CUDA(cudaGetLastError());
+}
+
+void sampler_host_advance(Sampler *sm, int n) { sm->move_counter += (uint64_t)sampler_moves(sm, n); }
+uint64_t sampler_move_counter(const Sampler *sm) { return sm->move_counter; }
+int sampler_chains(const Sampler *sm) { return sm->C; }
+bool sampler_fp32(const Sampler *sm) {
+    return sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator && sm->opts.rng == NQS_GPU_RNG_PHILOX;
 }
 
 bool sampler_produce(Sampler *sm, int n, uint64_t **d_out) {
