@@ -186,6 +186,38 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
                        int passes, int space_opt, double *y, double *delta, bool *param_space, double *out_resid,
                        int *out_fail);
 
+// Device scalar block of an SR step (doubles): [0] e_mean [1] e_sq_mean
+// [2] ||delta||^2 [3] rs [4] rs0 [5] pAp [6] alpha [7] u mean [8] tau_int
+// [9] ESS; status ints: [0] chol fail column (-1 ok) [1] cg done flag [2] cg
+// iterations [3] cg converged [4] retry ran [5] failure after the retry.
+enum { S_EMEAN = 0, S_ESQ = 1, S_NORM2 = 2, S_RS = 3, S_RS0 = 4, S_PAP = 5, S_ALPHA = 6, S_UMEAN = 7,
+       S_TAU = 8, S_ESS = 9 };
+enum { I_FAIL = 0, I_DONE = 1, I_ITERS = 2, I_CONV = 3, I_RETRY = 4, I_FAIL2 = 5 };
+
+// Batches of mixed solves (nqs_mixed.cu): one system per instance, the
+// factor / inverse / refinement of all of them in one cooperative launch.
+struct MixedSys;
+struct MixedBatch;
+MixedSys *mixed_sys_create();
+void mixed_sys_free(MixedSys *m);
+bool mixed_sys_prepare(MixedSys *m, double *O, const double *gm, const double *eps, int Ns, long P, double shift,
+                       int sweeps, int passes, int space_opt, double *y, double *delta);
+void mixed_sys_front(MixedSys *m, cudaStream_t st, bool with_split);
+bool mixed_sys_param_space(const MixedSys *m);
+int mixed_sys_order(const MixedSys *m);
+const int *mixed_sys_status(const MixedSys *m);
+const int *mixed_sys_err(const MixedSys *m);
+const double *mixed_sys_nrm(const MixedSys *m);
+int mixed_batch_capacity();
+MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas);
+void mixed_batch_free(MixedBatch *b);
+bool mixed_batch_launch(MixedBatch *b, cudaStream_t st);
+
+// Stream-only pieces of the SR step (nqs_sr.cu), for captured sequences.
+bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps);
+bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm);
+bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double scale, double *out);
+
 // thread-local statistics of the last SR step
 nqs_gpu_step_stats_t &step_stats();
 

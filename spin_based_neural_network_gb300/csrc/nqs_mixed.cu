@@ -1140,13 +1140,14 @@ __global__ void k_center_split_t(double *O, int Ns, long P, const double *__rest
 // Enqueue the whole mixed solve with no host synchronisation: centring and
 // split, tensor-core Gram, then the cooperative factor / inverse / refinement
 // kernel.  A broken factor is reported through status[0].
-static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, const double *eps, int Ns, long P,
-                          double shift, int sweeps, int passes, double *x, const CUtensorMap &mh,
-                          const CUtensorMap &ml, int *err, cudaStream_t st) {
-    MixedWs &w = g_mx;
+// Front of the mixed solve: status words, centring and TF32 split, tensor-core Gram.
+static void enqueue_front(MixedWs &w, const MixedPlan &pl, double *O, const double *gm, int Ns, long P, double shift,
+                          int passes, const CUtensorMap &mh, const CUtensorMap &ml, int *err, cudaStream_t st,
+                          bool with_split = true) {
     cudaMemsetAsync(w.status.p, 0xff, 2 * sizeof(int), st);
     cudaMemsetAsync(err, 0, sizeof(int), st);
-    if (pl.space == 0) {
+    if (!with_split) {
+    } else if (pl.space == 0) {
         NQS_LAUNCH("center_split");
         k_center_split<<<ctx().sm_count * 8, 256, 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, pl.k_pad);
     } else {
@@ -1176,6 +1177,10 @@ static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, cons
         NQS_LAUNCH("gram_tc");
         k_gram_tf32_tc<<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(mh, ml, g);
     }
+}
+
+static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const double *eps, int Ns, long P, double shift,
+                          int sweeps, double *x, int *err) {
     FrArgs fa;
     fa.T = w.T.p;
     fa.Li = w.Li.p;
@@ -1201,10 +1206,24 @@ static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, cons
     fa.bar = w.bar.p;
     fa.err = err;
     fa.tm = w.tm.p;
+    return fa;
+}
+
+// Zeroed words and vectors the factor / refinement kernel expects.
+static void enqueue_fr_clear(MixedWs &w, const FrArgs &fa, cudaStream_t st) {
     cudaMemsetAsync(w.bar.p, 0, 2 * sizeof(unsigned), st);
     cudaMemsetAsync(w.tm.p, 0, 8 * sizeof(unsigned long long), st);
     cudaMemsetAsync(w.rf.p, 0, sizeof(float) * fa.ldl, st);
     cudaMemsetAsync(w.zf.p, 0, sizeof(float) * fa.ldl, st);
+}
+
+static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, const double *eps, int Ns, long P,
+                          double shift, int sweeps, int passes, double *x, const CUtensorMap &mh,
+                          const CUtensorMap &ml, int *err, cudaStream_t st) {
+    MixedWs &w = g_mx;
+    enqueue_front(w, pl, O, gm, Ns, P, shift, passes, mh, ml, err, st);
+    const FrArgs fa = make_frargs(w, pl, O, eps, Ns, P, shift, sweeps, x, err);
+    enqueue_fr_clear(w, fa, st);
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)ctx().sm_count);
     lc.blockDim = dim3(PS_THREADS);
@@ -1219,6 +1238,61 @@ static void enqueue_mixed(const MixedPlan &pl, double *O, const double *gm, cons
         NQS_LAUNCH("factor_refine");
         cudaLaunchKernelEx(&lc, k_factor_refine, fa);
     }
+}
+
+// Buffers of a workspace for plan pl; *moved reports reallocation.
+static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStream_t st, bool *moved) {
+    const int n = pl.n;
+    if (pl.rows_pad != w.rows_pad || pl.k_pad != w.k_pad || pl.space != w.space) {
+        const size_t ne = (size_t)pl.rows_pad * pl.k_pad;
+        if (!w.hi.ensure(ne) || !w.lo.ensure(ne)) return false;
+        if (!NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ne, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ne, st)))
+            return false;
+        w.rows_pad = pl.rows_pad;
+        w.k_pad = pl.k_pad;
+        w.space = pl.space;
+        *moved = true;
+    }
+    const long big = (long)Ns > P ? (long)Ns : P;
+    const void *before[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
+    const int ldl = (n + 31) / 32 * 32;
+    if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
+        !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
+        !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(2) || !w.status.ensure(2) ||
+        !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
+        return false;
+    const void *after[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
+    for (int i = 0; i < 13; i++) *moved |= before[i] != after[i];
+    if (*moved || w.n != n) {
+        // the pad columns of L^{-1} are read (as zeros) by the vectorised solves
+        if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.LiT.p, 0, sizeof(float) * (size_t)n * ldl, st)))
+            return false;
+        w.n = n;
+        *moved = true;
+    }
+    return true;
+}
+
+static bool ensure_attrs() {
+    static bool attr = false;
+    if (attr) return true;
+    if (!NQS_CUDA(cudaFuncSetAttribute(k_gram_tf32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM)) ||
+        !NQS_CUDA(cudaFuncSetAttribute(k_factor_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, PS_SMEM)) ||
+        !NQS_CUDA(cudaFuncSetAttribute(k_factor_refine_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, PS_SMEM)))
+        return false;
+    int per_sm = 0;
+    if (!NQS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_refine, PS_THREADS, PS_SMEM)))
+        return false;
+    if (per_sm < 1) {
+        set_error("factor / refinement kernel does not fit on an SM");
+        return false;
+    }
+    attr = true;
+    return true;
 }
 
 // The launch sequence above is fixed for given buffers and sizes: it is
@@ -1241,55 +1315,10 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
     cudaStream_t st = c.stream;
     MixedWs &w = g_mx;
     const MixedPlan pl = plan_mixed(Ns, P, space_opt, passes);
-    const int n = pl.n;
     bool moved = false;
-    if (pl.rows_pad != w.rows_pad || pl.k_pad != w.k_pad || pl.space != w.space) {
-        const size_t ne = (size_t)pl.rows_pad * pl.k_pad;
-        if (!w.hi.ensure(ne) || !w.lo.ensure(ne)) return false;
-        if (!NQS_CUDA(cudaMemsetAsync(w.hi.p, 0, sizeof(float) * ne, st)) ||
-            !NQS_CUDA(cudaMemsetAsync(w.lo.p, 0, sizeof(float) * ne, st)))
-            return false;
-        w.rows_pad = pl.rows_pad;
-        w.k_pad = pl.k_pad;
-        w.space = pl.space;
-        moved = true;
-    }
-    const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
-    const int ldl = (n + 31) / 32 * 32;
-    if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
-        !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
-        !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(2) || !w.status.ensure(2) ||
-        !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
-        return false;
-    const void *after[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
-    for (int i = 0; i < 13; i++) moved |= before[i] != after[i];
-    if (moved || w.n != n) {
-        // the pad columns of L^{-1} are read (as zeros) by the vectorised solves
-        if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
-            !NQS_CUDA(cudaMemsetAsync(w.LiT.p, 0, sizeof(float) * (size_t)n * ldl, st)))
-            return false;
-        w.n = n;
-        moved = true;
-    }
+    if (!prepare_ws(w, pl, Ns, P, st, &moved)) return false;
     static DevBuf<int> err;
-    if (!err.ensure(1)) return false;
-    static bool attr = false;
-    if (!attr) {
-        if (!NQS_CUDA(cudaFuncSetAttribute(k_gram_tf32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM)) ||
-            !NQS_CUDA(cudaFuncSetAttribute(k_factor_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, PS_SMEM)))
-            return false;
-        int per_sm = 0;
-        if (!NQS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_refine, PS_THREADS, PS_SMEM)))
-            return false;
-        if (per_sm < 1) {
-            set_error("factor / refinement kernel does not fit on an SM");
-            return false;
-        }
-        attr = true;
-    }
+    if (!err.ensure(1) || !ensure_attrs()) return false;
     CUtensorMap mh, ml;
     if (!make_map(&mh, w.hi.p, pl.rows_pad, pl.k_pad) || !make_map(&ml, w.lo.p, pl.rows_pad, pl.k_pad))
         return false;
@@ -1349,6 +1378,121 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
     *out_resid = h[1] > 0 ? sqrt(h[0] / h[1]) : 0.0;
     for (int k = 0; k < 8; k++) step_stats().phase_us[k] = 1e-3 * (double)tns[k];
     return NQS_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- batches of systems
+// One system of a batch: its own workspace, tensor maps, status and error words.
+struct MixedSys {
+    MixedWs w;
+    MixedPlan pl{};
+    DevBuf<int> err;
+    CUtensorMap mh, ml;
+    FrArgs fa{};
+    double *O = nullptr;
+    const double *gm = nullptr;
+    int Ns = 0, passes = 3;
+    long P = 0;
+    double shift = 0.0;
+};
+
+MixedSys *mixed_sys_create() { return new MixedSys(); }
+void mixed_sys_free(MixedSys *m) { delete m; }
+
+bool mixed_sys_prepare(MixedSys *m, double *O, const double *gm, const double *eps, int Ns, long P, double shift,
+                       int sweeps, int passes, int space_opt, double *y, double *delta) {
+    cudaStream_t st = ctx().stream;
+    m->pl = plan_mixed(Ns, P, space_opt, passes);
+    bool moved = false;
+    if (!prepare_ws(m->w, m->pl, Ns, P, st, &moved) || !m->err.ensure(1) || !ensure_attrs()) return false;
+    if (!make_map(&m->mh, m->w.hi.p, m->pl.rows_pad, m->pl.k_pad) ||
+        !make_map(&m->ml, m->w.lo.p, m->pl.rows_pad, m->pl.k_pad))
+        return false;
+    m->O = O;
+    m->gm = gm;
+    m->Ns = Ns;
+    m->P = P;
+    m->shift = shift;
+    m->passes = passes;
+    m->fa = make_frargs(m->w, m->pl, O, eps, Ns, P, shift, sweeps, m->pl.space ? delta : y, m->err.p);
+    m->fa.tm = nullptr;
+    return true;
+}
+
+// Status words, centring + split (unless the operands are already split), Gram,
+// and the cleared words of the factor kernel.
+void mixed_sys_front(MixedSys *m, cudaStream_t st, bool with_split) {
+    enqueue_front(m->w, m->pl, m->O, m->gm, m->Ns, m->P, m->shift, m->passes, m->mh, m->ml, m->err.p, st, with_split);
+    enqueue_fr_clear(m->w, m->fa, st);
+}
+
+bool mixed_sys_param_space(const MixedSys *m) { return m->pl.space == 1; }
+int mixed_sys_order(const MixedSys *m) { return m->pl.n; }
+const int *mixed_sys_status(const MixedSys *m) { return m->w.status.p; }
+const int *mixed_sys_err(const MixedSys *m) { return m->err.p; }
+const double *mixed_sys_nrm(const MixedSys *m) { return m->w.nrm.p; }
+
+struct MixedBatch {
+    DevBuf<FrArgs> sys;
+    DevBuf<int> cta_sys, cta0, nctas;
+    int total = 0, count = 0;
+};
+
+// CTAs that can be co-resident for the batched kernel.
+int mixed_batch_capacity() {
+    if (!ensure_attrs()) return 0;
+    int per_sm = 0;
+    if (!NQS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_factor_refine_batch, PS_THREADS, PS_SMEM)))
+        return 0;
+    return per_sm * ctx().sm_count;
+}
+
+MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas) {
+    std::vector<FrArgs> fa((size_t)count);
+    std::vector<int> c0((size_t)count), nc((size_t)count), map;
+    for (int i = 0; i < count; i++) {
+        fa[i] = sys[i]->fa;
+        c0[i] = (int)map.size();
+        nc[i] = ctas[i] > 0 ? ctas[i] : 1;
+        for (int k = 0; k < nc[i]; k++) map.push_back(i);
+    }
+    const int cap = mixed_batch_capacity();
+    if ((int)map.size() > cap) {
+        set_error("batched solve needs %d co-resident CTAs, the device holds %d", (int)map.size(), cap);
+        return nullptr;
+    }
+    MixedBatch *b = new MixedBatch();
+    b->total = (int)map.size();
+    b->count = count;
+    if (!b->sys.ensure(count) || !b->cta_sys.ensure(map.size()) || !b->cta0.ensure(count) || !b->nctas.ensure(count) ||
+        !NQS_CUDA(cudaMemcpy(b->sys.p, fa.data(), sizeof(FrArgs) * count, cudaMemcpyHostToDevice)) ||
+        !NQS_CUDA(cudaMemcpy(b->cta_sys.p, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice)) ||
+        !NQS_CUDA(cudaMemcpy(b->cta0.p, c0.data(), sizeof(int) * count, cudaMemcpyHostToDevice)) ||
+        !NQS_CUDA(cudaMemcpy(b->nctas.p, nc.data(), sizeof(int) * count, cudaMemcpyHostToDevice))) {
+        delete b;
+        return nullptr;
+    }
+    return b;
+}
+
+void mixed_batch_free(MixedBatch *b) { delete b; }
+
+// Factor, inverse and refinement of every system of the batch in one
+// cooperative launch.
+bool mixed_batch_launch(MixedBatch *b, cudaStream_t st) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)b->total);
+    lc.blockDim = dim3(PS_THREADS);
+    lc.dynamicSmemBytes = PS_SMEM;
+    lc.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    NQS_LAUNCH("factor_refine_batch");
+    const FrArgs *s = b->sys.p;
+    const int *m = b->cta_sys.p, *c0 = b->cta0.p, *nc = b->nctas.p;
+    return NQS_CUDA(cudaLaunchKernelEx(&lc, k_factor_refine_batch, s, m, c0, nc));
 }
 
 }  // namespace nqs

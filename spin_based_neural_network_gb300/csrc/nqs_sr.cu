@@ -28,12 +28,6 @@ struct Workspace {
 };
 static Workspace g_ws;
 
-// device scalars (doubles): [0] e_mean [1] e_sq_mean [2] ||delta||^2 [3] rs
-// [4] rs0 [5] pAp [6] alpha  ; status ints: [0] chol fail column (-1 ok)
-// [1] cg done flag [2] cg iterations [3] cg converged [4] retry ran
-enum { S_EMEAN = 0, S_ESQ = 1, S_NORM2 = 2, S_RS = 3, S_RS0 = 4, S_PAP = 5, S_ALPHA = 6, S_UMEAN = 7,
-       S_TAU = 8, S_ESS = 9 };
-enum { I_FAIL = 0, I_DONE = 1, I_ITERS = 2, I_CONV = 3, I_RETRY = 4, I_FAIL2 = 5 };
 
 // ---------------------------------------------------------------- statistics
 // Neumaier-compensated sums of E and E^2 (one block), then eps_i = E_i - <E>.
@@ -636,6 +630,31 @@ static bool col_stats(const double *O, int Ns, long P, const double *E, const do
         NQS_LAUNCH("col_sum");
         k_col_fin<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(part.p, rb, Ns, P, scal, gm, F);
     }
+    return NQS_CUDA(cudaGetLastError());
+}
+
+bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps) {
+    cudaStream_t st = ctx().stream;
+    {
+        NQS_LAUNCH("energy_stats");
+        k_energy_stats<<<1, 1024, 0, st>>>(E, Ns, scal, eps);
+    }
+    {
+        NQS_LAUNCH("ess");
+        k_ess<<<1, 256, 0, st>>>(eps, Ns, chains, scal);
+    }
+    return NQS_CUDA(cudaGetLastError());
+}
+
+bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm) {
+    NQS_LAUNCH("col_mean");
+    return col_stats(O, Ns, P, nullptr, scal, gm, nullptr);
+}
+
+bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double scale, double *out) {
+    dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
+    NQS_LAUNCH("delta");
+    k_col_dot<<<cg, cb, 0, ctx().stream>>>(O, Ns, P, y, scale, out);
     return NQS_CUDA(cudaGetLastError());
 }
 
