@@ -125,6 +125,36 @@ int nqs_gpu_made_log_prob(const nqs_sampler_t *s, const int *spins, int batch, d
 int nqs_gpu_made_nll_grad(nqs_sampler_t *s, const int *spins, int batch, float *out_grad, double *out_nll);
 int nqs_gpu_made_sample(nqs_sampler_t *s, int count, int *out_spins, double *out_logq);
 
+/* ---- batches of independent problems -------------------------------------
+ * `count` independent VMC problems (each its own Hamiltonian, lattice, ansatz
+ * and sampler; sizes may differ) advanced together: nqs_gpu_batch_step runs one
+ * MinSR step of every instance.  Precision: the MIXED mode with the FP32
+ * estimator; each sampler must be a Philox sampler created in that mode and
+ * each program an RBM / cRBM (with Marshall layers) of the instance's ansatz.
+ * The refinement sweeps, Gram passes and solve space are taken from the process
+ * options at creation.  The factor / inverse / refinement of all instances run
+ * in ONE cooperative launch whose CTAs are split between the instances by an
+ * autotuner on the first step (nqs_gpu_batch_ctas reports the split,
+ * nqs_gpu_batch_tune_ms the candidates' times); from the second step the whole
+ * batch step is one CUDA graph replayed per step.  An instance whose FP32
+ * factor breaks down keeps its parameters for that step (converged = 0).
+ * The samplers advance as in nqs_sampler_batch (no learned proposal inside a
+ * batch).  infos (optional) receives count step infos. */
+typedef struct {
+    const nqs_config_t *cfg;      /* Hamiltonian, couplings, num_samples, shift, learning rate */
+    int size_x, size_y;           /* lattice */
+    nqs_ansatz_t *ansatz;
+    nqs_sampler_t *sampler;
+    nqs_log_amp_fn_t log_amp;     /* NULL: nqs_ansatz_log_amp of the ansatz */
+    void *log_amp_user;
+} nqs_gpu_instance_t;
+typedef struct nqs_gpu_batch nqs_gpu_batch_t;
+nqs_gpu_batch_t *nqs_gpu_batch_create(const nqs_gpu_instance_t *instances, int count);
+int nqs_gpu_batch_step(nqs_gpu_batch_t *b, nqs_sr_step_info_t *infos);
+int nqs_gpu_batch_ctas(const nqs_gpu_batch_t *b, int *out_ctas);
+int nqs_gpu_batch_tune_ms(const nqs_gpu_batch_t *b, double *out_ms, int cap);
+void nqs_gpu_batch_free(nqs_gpu_batch_t *b);
+
 /* Human-readable reason of the last failure on this thread ("" if none). */
 const char *nqs_gpu_last_error(void);
 /* Device name and SM count of the device in use; 0 on success. */
