@@ -149,3 +149,9 @@ class MadeStats(C.Structure):
     """nqs_gpu_made_stats_t (include/nqs/nqs_gpu.h)."""
     _fields_ = [("proposals", C.c_double), ("accepted", C.c_double), ("nll", C.c_double),
                 ("active", C.c_int), ("train_steps", C.c_int)]
+
+
+class Instance(C.Structure):
+    """nqs_gpu_instance_t (include/nqs/nqs_gpu.h)."""
+    _fields_ = [("cfg", C.POINTER(NqsConfig)), ("size_x", C.c_int), ("size_y", C.c_int), ("ansatz", C.c_void_p),
+                ("sampler", C.c_void_p), ("log_amp", C.c_void_p), ("log_amp_user", C.c_void_p)]

@@ -85,6 +85,11 @@ def _declare(L):
         "nqs_gpu_minsr_solve_noalloc": (C.c_int, [VP, VP, C.c_int, C.c_long, C.c_double, VP, infop, VP]),
         "nqs_gpu_gram_tc": (C.c_int, [DP, C.c_int, C.c_long, C.c_int, C.c_double, C.POINTER(C.c_float)]),
         "nqs_gpu_ess": (C.c_int, [DP, C.c_int, C.c_int, DP, DP]),
+        "nqs_gpu_batch_create": (C.c_void_p, [C.POINTER(abi.Instance), C.c_int]),
+        "nqs_gpu_batch_step": (C.c_int, [C.c_void_p, C.POINTER(abi.StepInfo)]),
+        "nqs_gpu_batch_ctas": (C.c_int, [C.c_void_p, IP]),
+        "nqs_gpu_batch_tune_ms": (C.c_int, [C.c_void_p, DP, C.c_int]),
+        "nqs_gpu_batch_free": (None, [C.c_void_p]),
         "nqs_gpu_made_options_default": (abi.MadeOptions, []),
         "nqs_sampler_set_learned_proposal": (C.c_int, [C.c_void_p, C.POINTER(abi.MadeOptions)]),
         "nqs_sampler_learned_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.MadeStats)]),
@@ -442,3 +447,48 @@ class LearnedProposal:
         lq = np.zeros(count)
         _check(lib().nqs_gpu_made_sample(self.s.h, count, _ip(out), _dp(lq)), "made_sample")
         return out, lq
+
+
+class Batch:
+    """A batch of independent problems stepped together (nqs_gpu_batch_*).
+    items: (cfg, size_x, size_y, Ansatz, Sampler, log_amp_fn or None, user)."""
+
+    def __init__(self, items):
+        self.items = list(items)           # keeps the configs and objects alive
+        arr = (abi.Instance * len(self.items))()
+        for i, (cfg, sx, sy, a, s, fn, user) in enumerate(self.items):
+            arr[i].cfg = C.pointer(cfg)
+            arr[i].size_x, arr[i].size_y = sx, sy
+            arr[i].ansatz, arr[i].sampler = a.h, s.h
+            arr[i].log_amp = fn
+            arr[i].log_amp_user = user
+        self._arr = arr
+        self.h = lib().nqs_gpu_batch_create(arr, len(self.items))
+        if not self.h:
+            raise NqsError("nqs_gpu_batch_create failed: " + last_error())
+
+    def step(self):
+        infos = (abi.StepInfo * len(self.items))()
+        _check(lib().nqs_gpu_batch_step(self.h, infos), "nqs_gpu_batch_step")
+        return list(infos)
+
+    def ctas(self):
+        out = (C.c_int * len(self.items))()
+        _check(lib().nqs_gpu_batch_ctas(self.h, out), "nqs_gpu_batch_ctas")
+        return list(out)
+
+    def tune_ms(self):
+        out = (C.c_double * 16)()
+        n = lib().nqs_gpu_batch_tune_ms(self.h, out, 16)
+        return list(out)[:max(n, 0)]
+
+    def free(self):
+        if getattr(self, "h", None):
+            lib().nqs_gpu_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
