@@ -23,6 +23,7 @@ bool sampler_produce_dev(Sampler *sm, int n, uint64_t **d_out, unsigned long lon
 void sampler_host_advance(Sampler *sm, int n);
 uint64_t sampler_move_counter(const Sampler *sm);
 int sampler_chains(const Sampler *sm);
+const unsigned long long *sampler_counts(const Sampler *sm);
 bool sampler_fp32(const Sampler *sm);
 
 struct BatchInst {
@@ -36,15 +37,17 @@ struct BatchInst {
     DevHam H{};
     int Ns = 0, C = 0;
     long P = 0;
-    DevBuf<double> E, Ei, eps, O, gm, scal, delta, y;
+    DevBuf<double> E, Ei, eps, O, gm, scal, delta, y, part;
     DevBuf<unsigned long long> move;
     MixedSys *mx = nullptr;
     double *h = nullptr;      // pinned: scal[16], nrm[2]
     int *hs = nullptr;        // pinned: mixed status, error word
+    unsigned long long *hc = nullptr;   // pinned: sampler counters (accepted, proposed)
     ~BatchInst() {
         if (mx) mixed_sys_free(mx);
         if (h) cudaFreeHost(h);
         if (hs) cudaFreeHost(hs);
+        if (hc) cudaFreeHost(hc);
     }
 };
 
@@ -57,8 +60,14 @@ struct Batch {
     long graph_kernels = 0;
     int steps = 0;
     int sweeps = 5, passes = 3, space = 0;
+    std::vector<cudaStream_t> side;      // instances' work forks onto these and joins the main stream
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
     ~Batch() {
         if (exec) cudaGraphExecDestroy(exec);
+        for (cudaStream_t s : side) cudaStreamDestroy(s);
+        for (cudaEvent_t e : join) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
         if (mb) mixed_batch_free(mb);
         for (BatchInst *b : inst) delete b;
     }
@@ -90,7 +99,7 @@ static bool enqueue_front(BatchInst &b, cudaStream_t st) {
     if (!ansatz_refresh_derived(b.a) || !sampler_produce_dev(b.s, b.Ns, &bits, b.move.p) ||
         !launch_local_estimator(b.A, b.H, bits, b.Ns, b.E.p, b.Ei.p, b.O.p, nullptr, 1, true) ||
         !enqueue_energy_stats(b.E.p, b.Ns, b.C, b.scal.p, b.eps.p) ||
-        !enqueue_col_means(b.O.p, b.Ns, b.P, b.scal.p, b.gm.p))
+        !enqueue_col_means(b.O.p, b.Ns, b.P, b.scal.p, b.gm.p, b.part.p))
         return false;
     mixed_sys_front(b.mx, st, true);
     return NQS_CUDA(cudaGetLastError());
@@ -108,8 +117,32 @@ static bool enqueue_back(BatchInst &b, cudaStream_t st) {
            NQS_CUDA(cudaMemcpyAsync(b.h + 16, mixed_sys_nrm(b.mx), 2 * sizeof(double), cudaMemcpyDeviceToHost, st)) &&
            NQS_CUDA(cudaMemcpyAsync(b.hs, mixed_sys_status(b.mx), sizeof(int), cudaMemcpyDeviceToHost, st)) &&
            NQS_CUDA(cudaMemcpyAsync(b.hs + 1, mixed_sys_err(b.mx), sizeof(int), cudaMemcpyDeviceToHost, st)) &&
+           NQS_CUDA(cudaMemcpyAsync(b.hc, sampler_counts(b.s), 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                    st)) &&
            NQS_CUDA(cudaMemcpyAsync(b.a->h_params, b.a->d_params.p, sizeof(double) * b.P, cudaMemcpyDeviceToHost,
                                     st));
+}
+
+// Run `work(instance)` for every instance on the side streams (instance i on
+// stream i mod S, the library's launches redirected there), forked from and
+// joined back into the main stream: independent instances overlap, and in a
+// captured sequence they become parallel branches of the graph.
+template <typename F>
+static bool fork_join(Batch &B, cudaStream_t main, F work) {
+    Context &c = ctx();
+    if (!NQS_CUDA(cudaEventRecord(B.fork, main))) return false;
+    for (cudaStream_t s : B.side)
+        if (!NQS_CUDA(cudaStreamWaitEvent(s, B.fork, 0))) return false;
+    bool ok = true;
+    for (size_t i = 0; i < B.inst.size() && ok; i++) {
+        c.stream = B.side[i % B.side.size()];
+        ok = work(*B.inst[i], c.stream);
+    }
+    c.stream = main;
+    for (size_t k = 0; k < B.side.size(); k++)
+        ok = ok && NQS_CUDA(cudaEventRecord(B.join[k], B.side[k])) &&
+             NQS_CUDA(cudaStreamWaitEvent(main, B.join[k], 0));
+    return ok;
 }
 
 // Candidate splits of the cooperative launch's CTAs between the instances:
@@ -204,6 +237,19 @@ nqs_gpu_batch_t *nqs_gpu_batch_create(const nqs_gpu_instance_t *in, int count) {
     B.sweeps = c.opts.refine_sweeps;
     B.passes = c.opts.gram_passes;
     B.space = c.opts.mixed_space;
+    const int nside = count < 8 ? count : 8;
+    B.side.resize((size_t)nside, nullptr);
+    B.join.resize((size_t)nside, nullptr);
+    for (int k = 0; k < nside; k++)
+        if (!NQS_CUDA(cudaStreamCreateWithFlags(&B.side[k], cudaStreamNonBlocking)) ||
+            !NQS_CUDA(cudaEventCreateWithFlags(&B.join[k], cudaEventDisableTiming))) {
+            delete h;
+            return nullptr;
+        }
+    if (!NQS_CUDA(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming))) {
+        delete h;
+        return nullptr;
+    }
     for (int i = 0; i < count; i++) {
         BatchInst *b = new BatchInst();
         B.inst.push_back(b);
@@ -238,9 +284,11 @@ nqs_gpu_batch_t *nqs_gpu_batch_create(const nqs_gpu_instance_t *in, int count) {
         if (b->Ns <= 0 || !b->E.ensure(b->Ns) || !b->Ei.ensure(b->Ns) || !b->eps.ensure(b->Ns) ||
             !b->O.ensure((size_t)b->Ns * b->P) || !b->gm.ensure(b->P) || !b->scal.ensure(16) ||
             !b->delta.ensure(b->P) || !b->y.ensure(b->Ns) || !b->move.ensure(1) ||
+            !b->part.ensure((size_t)col_stats_scratch(b->Ns, b->P)) ||
             !NQS_CUDA(cudaMemcpy(b->move.p, &mv, sizeof(mv), cudaMemcpyHostToDevice)) ||
             !NQS_CUDA(cudaMallocHost(&b->h, 18 * sizeof(double))) ||
-            !NQS_CUDA(cudaMallocHost(&b->hs, 2 * sizeof(int)))) {
+            !NQS_CUDA(cudaMallocHost(&b->hs, 2 * sizeof(int))) ||
+            !NQS_CUDA(cudaMallocHost(&b->hc, 2 * sizeof(unsigned long long)))) {
             delete h;
             return nullptr;
         }
@@ -266,25 +314,24 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
     cudaStream_t st = c.stream;
     for (BatchInst *b : B.inst)
         if (!ansatz_sync(b->a)) return -1;
+    auto front = [](BatchInst &b, cudaStream_t s) { return enqueue_front(b, s); };
+    auto back = [](BatchInst &b, cudaStream_t s) { return enqueue_back(b, s); };
     if (B.steps == 0 || c.profiling) {
-        for (BatchInst *b : B.inst)
-            if (!enqueue_front(*b, st)) return -1;
+        if (!fork_join(B, st, front)) return -1;
         if (B.steps == 0) {
             if (!autotune(B, st)) return -1;
         } else if (!mixed_batch_launch(B.mb, st)) {
             return -1;
         }
-        for (BatchInst *b : B.inst)
-            if (!enqueue_back(*b, st)) return -1;
+        if (!fork_join(B, st, back)) return -1;
     } else {
         if (!B.exec) {
             cudaGraph_t graph;
             const long l0 = c.launches;
             if (!NQS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal))) return -1;
-            bool ok = true;
-            for (BatchInst *b : B.inst) ok = ok && enqueue_front(*b, st);
+            bool ok = fork_join(B, st, front);
             ok = ok && mixed_batch_launch(B.mb, st);
-            for (BatchInst *b : B.inst) ok = ok && enqueue_back(*b, st);
+            ok = ok && fork_join(B, st, back);
             const bool ended = NQS_CUDA(cudaStreamEndCapture(st, &graph));
             if (!ok || !ended) return -1;
             B.graph_kernels = c.launches - l0;
@@ -312,7 +359,7 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
             f.mean_energy = b->h[S_EMEAN];
             f.variance_energy = b->h[S_ESQ] - b->h[S_EMEAN] * b->h[S_EMEAN];
             f.update_norm = sqrt(b->h[S_NORM2]) * b->cfg.learning_rate;
-            f.acceptance_ratio = nqs_sampler_acceptance_ratio((nqs_sampler_t *)b->s);
+            f.acceptance_ratio = b->hc[1] ? (double)b->hc[0] / (double)b->hc[1] : 0.0;
             f.cg_iterations = 0;
             f.converged = b->hs[0] < 0 && b->hs[1] == 0;
         }

@@ -215,7 +215,8 @@ bool mixed_batch_launch(MixedBatch *b, cudaStream_t st);
 
 // Stream-only pieces of the SR step (nqs_sr.cu), for captured sequences.
 bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps);
-bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm);
+bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm, double *part);
+long col_stats_scratch(int Ns, long P);
 bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double scale, double *out);
 
 // thread-local statistics of the last SR step

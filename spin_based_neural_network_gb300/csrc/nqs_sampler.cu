@@ -597,6 +597,7 @@ bool sampler_produce_dev(Sampler *sm, int n, uint64_t **d_out, unsigned long lon
 void sampler_host_advance(Sampler *sm, int n) { sm->move_counter += (uint64_t)sampler_moves(sm, n); }
 uint64_t sampler_move_counter(const Sampler *sm) { return sm->move_counter; }
 int sampler_chains(const Sampler *sm) { return sm->C; }
+const unsigned long long *sampler_counts(const Sampler *sm) { return sm->d_counts.p; }
 bool sampler_fp32(const Sampler *sm) {
     return sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator && sm->opts.rng == NQS_GPU_RNG_PHILOX;
 }

@@ -616,19 +616,35 @@ struct StepIn {
 
 // Column means of O (and the CG-SR force F when E != NULL) over a 2-D grid of
 // about four blocks per SM.
-static bool col_stats(const double *O, int Ns, long P, const double *E, const double *scal, double *gm, double *F) {
-    static DevBuf<double> part;
+static int col_chunks(int Ns, long P, int *rows_per) {
     const int gx = (int)((P + 31) / 32);
     int rb = (4 * ctx().sm_count + gx - 1) / gx;
     rb = rb < 1 ? 1 : rb > (Ns + 63) / 64 ? (Ns + 63) / 64 : rb;
-    const int rows_per = (Ns + rb - 1) / rb;
-    rb = (Ns + rows_per - 1) / rows_per;
-    if (!part.ensure((size_t)rb * 2 * P)) return false;
+    *rows_per = (Ns + rb - 1) / rb;
+    return (Ns + *rows_per - 1) / *rows_per;
+}
+
+// Doubles of partial sums col_stats needs (callers that run concurrently pass
+// their own buffer).
+long col_stats_scratch(int Ns, long P) {
+    int rp;
+    return (long)col_chunks(Ns, P, &rp) * 2 * P;
+}
+
+static bool col_stats(const double *O, int Ns, long P, const double *E, const double *scal, double *gm, double *F,
+                      double *part_buf = nullptr) {
+    static DevBuf<double> part;
+    int rows_per;
+    const int gx = (int)((P + 31) / 32), rb = col_chunks(Ns, P, &rows_per);
+    if (!part_buf) {
+        if (!part.ensure((size_t)rb * 2 * P)) return false;
+        part_buf = part.p;
+    }
     cudaStream_t st = ctx().stream;
-    k_col_part<<<dim3((unsigned)gx, (unsigned)rb), dim3(32, 8), 0, st>>>(O, Ns, P, E, rows_per, part.p);
+    k_col_part<<<dim3((unsigned)gx, (unsigned)rb), dim3(32, 8), 0, st>>>(O, Ns, P, E, rows_per, part_buf);
     {
         NQS_LAUNCH("col_sum");
-        k_col_fin<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(part.p, rb, Ns, P, scal, gm, F);
+        k_col_fin<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(part_buf, rb, Ns, P, scal, gm, F);
     }
     return NQS_CUDA(cudaGetLastError());
 }
@@ -646,9 +662,9 @@ bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, dou
     return NQS_CUDA(cudaGetLastError());
 }
 
-bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm) {
+bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm, double *part) {
     NQS_LAUNCH("col_mean");
-    return col_stats(O, Ns, P, nullptr, scal, gm, nullptr);
+    return col_stats(O, Ns, P, nullptr, scal, gm, nullptr, part);
 }
 
 bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double scale, double *out) {
