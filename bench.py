@@ -356,6 +356,102 @@ def proposal_run(nqs, abi, L, opts_kw, decor, learned, warm, steps):
     return out
 
 
+def batch_instances(count=64, seed=SEED + 5):
+    """The multi-instance workload: `count` Hamiltonians alternating TFIM
+    (h ~ U[0.5, 1.5]) and XXZ (Delta ~ U[0.5, 2.0], Marshall sign) on chains or
+    periodic 2-D lattices with even sides, N in {12, ..., 32}, real RBM with
+    alpha in {1, 2}, N_s in {512, 1024, 2048, 4096} from N_s / 4 Philox chains
+    (single flips for TFIM, exchange moves in Sz = 0 for XXZ)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        kind = "tfim" if i % 2 == 0 else "xxz"
+        N = int(rng.choice([12, 16, 20, 24, 28, 32]))
+        if rng.integers(0, 2) == 0:
+            Lx, Ly = N, 1
+        else:
+            Ly = 4 if N % 8 == 0 else 2
+            Lx = N // Ly
+        alpha = int(rng.choice([1, 2]))
+        Ns = int(rng.choice([512, 1024, 2048, 4096]))
+        h, delta = float(rng.uniform(0.5, 1.5)), float(rng.uniform(0.5, 2.0))
+        out.append({"kind": kind, "N": N, "Lx": Lx, "Ly": Ly, "alpha": alpha, "Ns": Ns, "h": h, "delta": delta,
+                    "seed": int(seed * 1000 + i)})
+    return out
+
+
+def batch_objects(nqs, abi, spec, lr=0.02, shift=1e-3):
+    """Ansatz, amplitude program and sampler of one instance of batch_instances."""
+    xxz = spec["kind"] == "xxz"
+    N, Lx, Ly = spec["N"], spec["Lx"], spec["Ly"]
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=spec["alpha"] * N, rbm_init_scale=0.1,
+                              hamiltonian=4 if xxz else 0, j_coupling=1.0, j_z_coupling=spec["delta"],
+                              transverse_field=spec["h"], rng_seed=spec["seed"], num_samples=spec["Ns"],
+                              num_thermalize=4 * N, num_decorrelate=N, sr_diag_shift=shift, learning_rate=lr)
+    a = nqs.Ansatz(cfg, N)
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly) if xxz else None
+    fn, user = (m.log_amp_fn, m.user) if m else (a.log_amp_fn, a.user)
+    o = nqs.options(num_chains=spec["Ns"] // 4, rng=abi.RNG_PHILOX,
+                    move=abi.MOVE_EXCHANGE if xxz else abi.MOVE_SINGLE_FLIP, n_down=N // 2 if xxz else -1,
+                    lattice_x=Lx, lattice_y=Ly, square_pbc=1, precision=abi.PREC_MIXED, fp32_estimator=1)
+    s = nqs.Sampler(N, cfg, fn, user, o)
+    return {"cfg": cfg, "a": a, "m": m, "s": s, "fn": fn if m else None, "user": user if m else None,
+            "Lx": Lx, "Ly": Ly, "spec": spec}
+
+
+def multi_instance(nqs, abi, L, base_opts, timed, total):
+    """The 64-instance workload stepped as one batch (nqs_gpu_batch_step): one
+    cooperative launch for all solves with an autotuned CTA split, the whole
+    batch step replayed as a CUDA graph from the second step.  Throughput over
+    `timed` steps after 3 warm-up steps; then the optimisation continues to
+    `total` steps and each instance with an exact energy (N <= 20,
+    tests/golden/batch_exact_energies.json) reports |E/N - E0/N| of its energy
+    averaged over the last 20 steps."""
+    import numpy as np
+    nqs.set_options(**base_opts)
+    specs = batch_instances()
+    objs = [batch_objects(nqs, abi, sp) for sp in specs]
+    for o in objs:
+        o["s"].thermalize()
+    bt = nqs.Batch([(o["cfg"], o["Lx"], o["Ly"], o["a"], o["s"], o["fn"], o["user"]) for o in objs])
+    hist = []
+    for _ in range(3):
+        hist.append([i.mean_energy for i in bt.step()])
+    e0 = L.nqs_gpu_event_record()
+    for _ in range(timed):
+        hist.append([i.mean_energy for i in bt.step()])
+    e1 = L.nqs_gpu_event_record()
+    ms = L.nqs_gpu_event_elapsed_ms(e0, e1) / timed
+    L.nqs_gpu_event_destroy(e0)
+    L.nqs_gpu_event_destroy(e1)
+    infos = None
+    while len(hist) < total:
+        infos = bt.step()
+        hist.append([i.mean_energy for i in infos])
+    with open(os.path.join(ROOT, "tests", "golden", "batch_exact_energies.json")) as f:
+        exact = json.load(f)
+    H = np.array(hist)
+    errs = {}
+    for k, v in exact.items():
+        i = int(k)
+        errs[k] = abs(float(np.mean(H[-20:, i])) / specs[i]["N"] - v["E0_per_site"])
+    ev = np.array(list(errs.values()))
+    out = {"instances": len(specs), "kinds": "TFIM h~U[0.5,1.5] / XXZ Delta~U[0.5,2.0] (Marshall), chains and "
+                                               "2-D PBC, N in 12..32, real RBM alpha in {1,2}, N_s in 512..4096",
+           "batch_ms_per_step": ms, "batch_steps_per_s": 1000.0 / ms,
+           "instance_steps_per_s": len(specs) * 1000.0 / ms,
+           "samples_per_s": sum(sp["Ns"] for sp in specs) * 1000.0 / ms,
+           "autotuned_ctas": bt.ctas(), "autotune_candidates_ms": bt.tune_ms(),
+           "steps_for_accuracy": len(hist), "exact_checked": len(errs),
+           "abs_err_per_site_median": float(np.median(ev)), "abs_err_per_site_max": float(np.max(ev)),
+           "within_1e-2": int(np.sum(ev <= 1e-2)), "within_1e-3": int(np.sum(ev <= 1e-3)),
+           "converged_last_step": int(sum(i.converged for i in infos)) if infos else None}
+    bt.free()
+    nqs.set_options(**base_opts)
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -499,6 +595,10 @@ def run_gpu(args):
                      for d in (DECOR, 2) for lr in (False, True)]
         nqs.set_options(**base_opts)
 
+    multi = None
+    if prec == abi.PREC_MIXED and args.batch_steps > 0:
+        multi = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps)
+
     conv = None
     if args.converge_steps > 0:
         conv = converge(nqs, abi, L, base_opts, args.converge_steps)
@@ -527,7 +627,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": 8 * P + 16 * 8},
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
             "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
-            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals,
+            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
@@ -588,6 +688,8 @@ def main():
     ap.add_argument("--converge-steps", type=int, default=1000,
                     help="max optimisation steps of the |dE/N| <= 1e-4 vs Lanczos run (0 = skip)")
     ap.add_argument("--converge-fp64", action="store_true", help="also run the FP64 path to the target")
+    ap.add_argument("--batch-steps", type=int, default=300,
+                    help="steps of the 64-instance batch run (0 = skip)")
     ap.add_argument("--proposal-steps", type=int, default=20,
                     help="timed steps of each plain / learned proposal run (0 = skip)")
     args = ap.parse_args()

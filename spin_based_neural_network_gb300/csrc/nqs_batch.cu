@@ -147,21 +147,24 @@ static bool fork_join(Batch &B, cudaStream_t main, F work) {
 
 // Candidate splits of the cooperative launch's CTAs between the instances:
 // the same count for every instance (1, 2, 4, ...) and counts proportional to
-// n_i^2 (n_i the order of instance i's system), within the co-resident limit.
+// n_i^e for e = 1, 2, 3 (n_i the order of instance i's system: its factor is
+// n^3 work on a chain of n / 128 diagonal blocks), within the co-resident limit.
 static std::vector<std::vector<int>> cta_candidates(const Batch &B, int cap) {
     const int K = (int)B.inst.size();
     std::vector<std::vector<int>> c;
     for (int u = 1; u * K <= cap && u <= 32; u *= 2) c.push_back(std::vector<int>((size_t)K, u));
-    double tot = 0.0;
-    for (BatchInst *b : B.inst) tot += (double)mixed_sys_order(b->mx) * mixed_sys_order(b->mx);
-    std::vector<int> prop((size_t)K);
-    int used = 0;
-    for (int i = 0; i < K; i++) {
-        const double w = (double)mixed_sys_order(B.inst[i]->mx) * mixed_sys_order(B.inst[i]->mx) / tot;
-        prop[i] = (int)floor(w * (double)(cap - K)) + 1;
-        used += prop[i];
+    for (int e = 1; e <= 3; e++) {
+        std::vector<double> w((size_t)K);
+        double tot = 0.0;
+        for (int i = 0; i < K; i++) tot += (w[i] = pow((double)mixed_sys_order(B.inst[i]->mx), (double)e));
+        std::vector<int> prop((size_t)K);
+        int used = 0;
+        for (int i = 0; i < K; i++) {
+            prop[i] = (int)floor(w[i] / tot * (double)(cap - K)) + 1;
+            used += prop[i];
+        }
+        if (used <= cap) c.push_back(prop);
     }
-    if (used <= cap) c.push_back(prop);
     return c;
 }
 
