@@ -446,7 +446,8 @@ def multi_instance(nqs, abi, L, base_opts, timed, total):
            "steps_for_accuracy": len(hist), "exact_checked": len(errs),
            "abs_err_per_site_median": float(np.median(ev)), "abs_err_per_site_max": float(np.max(ev)),
            "within_1e-2": int(np.sum(ev <= 1e-2)), "within_1e-3": int(np.sum(ev <= 1e-3)),
-           "converged_last_step": int(sum(i.converged for i in infos)) if infos else None}
+           "converged_last_step": int(sum(i.converged for i in infos)) if infos else None,
+           "fp64_fallback_instance_steps": bt.fallbacks()}
     bt.free()
     nqs.set_options(**base_opts)
     return out

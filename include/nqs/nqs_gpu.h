@@ -137,7 +137,9 @@ int nqs_gpu_made_sample(nqs_sampler_t *s, int count, int *out_spins, double *out
  * autotuner on the first step (nqs_gpu_batch_ctas reports the split,
  * nqs_gpu_batch_tune_ms the candidates' times); from the second step the whole
  * batch step is one CUDA graph replayed per step.  An instance whose FP32
- * factor breaks down keeps its parameters for that step (converged = 0).
+ * factor breaks down is solved again in FP64 on the same samples after the
+ * graph (as nqs_sr_step_minsr_full does in the MIXED mode);
+ * nqs_gpu_batch_fallbacks counts those instance steps.
  * The samplers advance as in nqs_sampler_batch (no learned proposal inside a
  * batch).  infos (optional) receives count step infos. */
 typedef struct {
@@ -153,6 +155,7 @@ nqs_gpu_batch_t *nqs_gpu_batch_create(const nqs_gpu_instance_t *instances, int c
 int nqs_gpu_batch_step(nqs_gpu_batch_t *b, nqs_sr_step_info_t *infos);
 int nqs_gpu_batch_ctas(const nqs_gpu_batch_t *b, int *out_ctas);
 int nqs_gpu_batch_tune_ms(const nqs_gpu_batch_t *b, double *out_ms, int cap);
+long nqs_gpu_batch_fallbacks(const nqs_gpu_batch_t *b);
 void nqs_gpu_batch_free(nqs_gpu_batch_t *b);
 
 /* Human-readable reason of the last failure on this thread ("" if none). */

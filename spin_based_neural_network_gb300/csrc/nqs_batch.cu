@@ -43,6 +43,7 @@ struct BatchInst {
     double *h = nullptr;      // pinned: scal[16], nrm[2]
     int *hs = nullptr;        // pinned: mixed status, error word
     unsigned long long *hc = nullptr;   // pinned: sampler counters (accepted, proposed)
+    int fp64_fallback = 0, fp64_conv = 0;   // last step solved in FP64 after an FP32 breakdown
     ~BatchInst() {
         if (mx) mixed_sys_free(mx);
         if (h) cudaFreeHost(h);
@@ -59,6 +60,7 @@ struct Batch {
     cudaGraphExec_t exec = nullptr;
     long graph_kernels = 0;
     int steps = 0;
+    long fallbacks = 0;                  // instance steps re-solved in FP64
     int sweeps = 5, passes = 3, space = 0;
     std::vector<cudaStream_t> side;      // instances' work forks onto these and joins the main stream
     std::vector<cudaEvent_t> join;
@@ -76,9 +78,9 @@ struct Batch {
 // theta -= lr delta and ||delta||^2, with delta = 0 when the instance's FP32
 // factor broke down or its kernels reported an error.
 __global__ void k_batch_apply(double *params, const double *__restrict__ delta, long P, double lr, double *scal,
-                              const int *mstatus, const int *merr) {
+                              const int *mstatus, const int *merr, int unconditional) {
     __shared__ double red[1024];
-    const bool zero = mstatus[0] >= 0 || merr[0] != 0;
+    const bool zero = !unconditional && (mstatus[0] >= 0 || merr[0] != 0);
     double s = 0.0;
     for (long k = threadIdx.x; k < P; k += blockDim.x) {
         const double d = zero ? 0.0 : delta[k];
@@ -111,7 +113,7 @@ static bool enqueue_back(BatchInst &b, cudaStream_t st) {
     {
         NQS_LAUNCH("apply_update");
         k_batch_apply<<<1, 1024, 0, st>>>(b.a->d_params.p, b.delta.p, b.P, b.cfg.learning_rate, b.scal.p,
-                                          mixed_sys_status(b.mx), mixed_sys_err(b.mx));
+                                          mixed_sys_status(b.mx), mixed_sys_err(b.mx), 0);
     }
     return NQS_CUDA(cudaMemcpyAsync(b.h, b.scal.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st)) &&
            NQS_CUDA(cudaMemcpyAsync(b.h + 16, mixed_sys_nrm(b.mx), 2 * sizeof(double), cudaMemcpyDeviceToHost, st)) &&
@@ -351,6 +353,28 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
     }
     if (!NQS_CUDA(cudaStreamSynchronize(st))) return -1;
     B.steps++;
+    // An instance whose FP32 factor broke down (a pivot <= 0) had its update
+    // held at zero inside the graph; solve it again in FP64 on the same
+    // centred O and eps, as the single-system step does.
+    for (size_t i = 0; i < B.inst.size(); i++) {
+        BatchInst *b = B.inst[i];
+        b->fp64_fallback = 0;
+        if (b->hs[0] < 0 || b->hs[1] != 0) continue;
+        int conv = 0;
+        if (minsr_fp64_delta(b->O.p, b->eps.p, b->Ns, b->P, b->cfg.sr_diag_shift, b->delta.p, &conv) != 0)
+            return -1;
+        k_batch_apply<<<1, 1024, 0, st>>>(b->a->d_params.p, b->delta.p, b->P, b->cfg.learning_rate, b->scal.p,
+                                          mixed_sys_status(b->mx), mixed_sys_err(b->mx), 1);
+        if (!NQS_CUDA(cudaMemcpyAsync(b->h + S_NORM2, b->scal.p + S_NORM2, sizeof(double), cudaMemcpyDeviceToHost,
+                                      st)) ||
+            !NQS_CUDA(cudaMemcpyAsync(b->a->h_params, b->a->d_params.p, sizeof(double) * b->P,
+                                      cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaStreamSynchronize(st)))
+            return -1;
+        b->fp64_fallback = 1;
+        b->fp64_conv = conv;
+        B.fallbacks++;
+    }
     int failed = 0;
     for (size_t i = 0; i < B.inst.size(); i++) {
         BatchInst *b = B.inst[i];
@@ -364,7 +388,7 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
             f.update_norm = sqrt(b->h[S_NORM2]) * b->cfg.learning_rate;
             f.acceptance_ratio = b->hc[1] ? (double)b->hc[0] / (double)b->hc[1] : 0.0;
             f.cg_iterations = 0;
-            f.converged = b->hs[0] < 0 && b->hs[1] == 0;
+            f.converged = b->fp64_fallback ? b->fp64_conv : (b->hs[0] < 0 && b->hs[1] == 0);
         }
     }
     if (failed) {
@@ -387,6 +411,8 @@ int nqs_gpu_batch_tune_ms(const nqs_gpu_batch_t *h, double *out, int cap) {
     for (int i = 0; i < n; i++) out[i] = h->b.tune_ms[i];
     return n;
 }
+
+long nqs_gpu_batch_fallbacks(const nqs_gpu_batch_t *h) { return h ? h->b.fallbacks : -1; }
 
 void nqs_gpu_batch_free(nqs_gpu_batch_t *h) { delete h; }
 

@@ -218,6 +218,10 @@ bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, dou
 bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm, double *part);
 long col_stats_scratch(int Ns, long P);
 bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double scale, double *out);
+// FP64 MinSR solve (upstream retry semantics) on a centred O; and the update
+// delta = O^T y / N_s from it.  Return 0 / -1 (CUDA error).
+int minsr_fp64_solve(const double *O, const double *eps, int Ns, long P, double shift, double *y, int *conv);
+int minsr_fp64_delta(const double *O, const double *eps, int Ns, long P, double shift, double *delta, int *conv);
 
 // thread-local statistics of the last SR step
 nqs_gpu_step_stats_t &step_stats();

@@ -674,6 +674,76 @@ bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double sc
     return NQS_CUDA(cudaGetLastError());
 }
 
+// FP64 factorisation and solve of (O O^T / N_s + shift I) y = eps on the
+// centred O [N_s][N_p], with the upstream retry semantics on a Cholesky
+// breakdown (src/nqs/nqs_optimizer.c:1148-1170): the retry adds 1e-6 to the
+// diagonal of the partially overwritten matrix; a second breakdown sets the
+// update to 0.  Writes y [N_s] and *conv (1 when solved).  Uses the shared
+// workspace; returns 0 on success, -1 on a CUDA error.
+int minsr_fp64_solve(const double *O, const double *eps, int Ns, long P, double shift, double *y_out, int *conv) {
+    Workspace &w = g_ws;
+    Context &c = ctx();
+    cudaStream_t st = c.stream;
+    *conv = 0;
+    if (!w.T.ensure((size_t)Ns * Ns) || !w.z.ensure(Ns) || !w.status.ensure(16)) return -1;
+    int nt = (Ns + TG - 1) / TG;
+    NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));
+    {
+        NQS_LAUNCH("gram_fp64");
+        k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(O, Ns, P, 1.0 / (double)Ns, shift, w.T.p);
+    }
+    if (!cholesky_fp64(w.T.p, Ns, w.status.p)) return -1;
+    int fail = -1;
+    if (!NQS_CUDA(cudaMemcpyAsync(&fail, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaStreamSynchronize(st)))
+        return -1;
+    step_stats().chol_fail_col = fail;
+    step_stats().chol_retry = 0;
+    int fail2 = -1;
+    if (fail >= 0) {
+        // upstream retry on the partially overwritten matrix (+1e-6)
+        step_stats().chol_retry = 1;
+        if (!w.T0.ensure((size_t)Ns * Ns)) return -1;
+        {
+            NQS_LAUNCH("gram_fp64");
+            k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(O, Ns, P, 1.0 / (double)Ns, shift, w.T0.p);
+        }
+        int k0 = (fail / NB) * NB, kb = Ns - k0 < NB ? Ns - k0 : NB;
+        if (fail > k0 && k0 + kb < Ns) {
+            NQS_LAUNCH("chol_panel");
+            k_trsm_panel<<<(Ns - k0 - kb + 127) / 128, 128, 0, st>>>(w.T.p, Ns, k0, kb, fail - k0, k0 + kb,
+                                                                    w.status.p, 1);
+        }
+        {
+            NQS_LAUNCH("chol_restore");
+            k_quirk_restore<<<c.sm_count * 8, 256, 0, st>>>(w.T.p, w.T0.p, Ns, fail);
+        }
+        NQS_CUDA(cudaMemsetAsync(w.status.p + I_FAIL, 0xff, sizeof(int), st));
+        if (!cholesky_fp64(w.T.p, Ns, w.status.p)) return -1;
+        if (!NQS_CUDA(cudaMemcpyAsync(&fail2, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaStreamSynchronize(st)))
+            return -1;
+    }
+    if (fail2 < 0) {
+        if (!cholesky_solve(w.T.p, Ns, eps, w.z.p, y_out)) return -1;
+        *conv = 1;
+    } else {
+        fprintf(stderr, "nqs_sr_step_minsr: Cholesky breakdown after retry; increase "
+                        "sr_diag_shift or num_samples. Update set to 0.\n");
+        NQS_CUDA(cudaMemsetAsync(y_out, 0, sizeof(double) * Ns, st));
+    }
+    return 0;
+}
+
+// The FP64 MinSR update delta = O^T y / N_s of one system whose mixed solve
+// broke down (FP32 pivot <= 0), on its centred O and eps.
+int minsr_fp64_delta(const double *O, const double *eps, int Ns, long P, double shift, double *delta, int *conv) {
+    Workspace &w = g_ws;
+    if (!w.y.ensure(Ns)) return -1;
+    if (minsr_fp64_solve(O, eps, Ns, P, shift, w.y.p, conv) != 0) return -1;
+    return enqueue_col_dot(O, Ns, P, w.y.p, 1.0 / (double)Ns, delta) ? 0 : -1;
+}
+
 static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
     clear_error();
     const nqs_config_t *cfg = in.cfg;
@@ -724,59 +794,9 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     } else {
         if (!upload_spins(in.host_batch, Ns, H.N, &bits)) return -1;
     }
-        // FP64 factorisation and solve of (T + shift I) y = eps on the centred O,
-        // with the upstream retry semantics; writes y_out.
-        auto fp64_solve = [&](double *y_out, int *conv) -> int {
-        int nt = (Ns + TG - 1) / TG;
-        NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));
-        {
-            NQS_LAUNCH("gram_fp64");
-            k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(w.O.p, Ns, P, 1.0 / (double)Ns,
-                                                            cfg->sr_diag_shift, w.T.p);
-        }
-        if (!cholesky_fp64(w.T.p, Ns, w.status.p)) return -1;
-        int fail = -1;
-        if (!NQS_CUDA(cudaMemcpyAsync(&fail, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
-            !NQS_CUDA(cudaStreamSynchronize(st)))
-            return -1;
-        step_stats().chol_fail_col = fail;
-        step_stats().chol_retry = 0;
-        int fail2 = -1;
-        if (fail >= 0) {
-            // upstream retry on the partially overwritten matrix (+1e-6)
-            step_stats().chol_retry = 1;
-            if (!w.T0.ensure((size_t)Ns * Ns)) return -1;
-            {
-                NQS_LAUNCH("gram_fp64");
-                k_gram_fp64<<<nt * (nt + 1) / 2, 256, 0, st>>>(w.O.p, Ns, P, 1.0 / (double)Ns,
-                                                                cfg->sr_diag_shift, w.T0.p);
-            }
-            int k0 = (fail / NB) * NB, kb = Ns - k0 < NB ? Ns - k0 : NB;
-            if (fail > k0 && k0 + kb < Ns) {
-                NQS_LAUNCH("chol_panel");
-                k_trsm_panel<<<(Ns - k0 - kb + 127) / 128, 128, 0, st>>>(w.T.p, Ns, k0, kb, fail - k0,
-                                                                        k0 + kb, w.status.p, 1);
-            }
-            {
-                NQS_LAUNCH("chol_restore");
-                k_quirk_restore<<<c.sm_count * 8, 256, 0, st>>>(w.T.p, w.T0.p, Ns, fail);
-            }
-            NQS_CUDA(cudaMemsetAsync(w.status.p + I_FAIL, 0xff, sizeof(int), st));
-            if (!cholesky_fp64(w.T.p, Ns, w.status.p)) return -1;
-            if (!NQS_CUDA(cudaMemcpyAsync(&fail2, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
-                !NQS_CUDA(cudaStreamSynchronize(st)))
-                return -1;
-        }
-        if (fail2 < 0) {
-            if (!cholesky_solve(w.T.p, Ns, w.eps.p, w.z.p, y_out)) return -1;
-            *conv = 1;
-        } else {
-            fprintf(stderr, "nqs_sr_step_minsr: Cholesky breakdown after retry; increase "
-                            "sr_diag_shift or num_samples. Update set to 0.\n");
-            NQS_CUDA(cudaMemsetAsync(y_out, 0, sizeof(double) * Ns, st));
-        }
-        return 0;
-        };
+    auto fp64_solve = [&](double *y_out, int *conv) -> int {
+        return minsr_fp64_solve(w.O.p, w.eps.p, Ns, P, cfg->sr_diag_shift, y_out, conv);
+    };
     const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
     const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && fp32_capable(A);
     nqs_gpu_step_stats_t &ss = step_stats();

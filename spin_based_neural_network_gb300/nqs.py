@@ -90,6 +90,7 @@ def _declare(L):
         "nqs_gpu_batch_ctas": (C.c_int, [C.c_void_p, IP]),
         "nqs_gpu_batch_tune_ms": (C.c_int, [C.c_void_p, DP, C.c_int]),
         "nqs_gpu_batch_free": (None, [C.c_void_p]),
+        "nqs_gpu_batch_fallbacks": (C.c_long, [C.c_void_p]),
         "nqs_gpu_made_options_default": (abi.MadeOptions, []),
         "nqs_sampler_set_learned_proposal": (C.c_int, [C.c_void_p, C.POINTER(abi.MadeOptions)]),
         "nqs_sampler_learned_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.MadeStats)]),
@@ -481,6 +482,10 @@ class Batch:
         out = (C.c_double * 16)()
         n = lib().nqs_gpu_batch_tune_ms(self.h, out, 16)
         return list(out)[:max(n, 0)]
+
+    def fallbacks(self):
+        """Instance steps whose FP32 factor broke down and were solved in FP64."""
+        return int(lib().nqs_gpu_batch_fallbacks(self.h))
 
     def free(self):
         if getattr(self, "h", None):

@@ -85,3 +85,35 @@ def test_batch_rejects_fp64_sampler(nqs):
     s = nqs.Sampler(8, cfg, a.log_amp_fn, a.user, o)
     with pytest.raises(nqs.NqsError):
         nqs.Batch([(cfg, 8, 1, a, s, None, None)])
+
+
+def test_batch_fp32_breakdown_falls_back_to_fp64(nqs):
+    """A negative diagonal shift makes the first pivot negative: the FP32 factor
+    of every instance breaks down inside the graph, the batch re-solves each in
+    FP64 afterwards (upstream retry semantics: breakdown again, update 0,
+    converged 0), exactly as the single-system MIXED step does."""
+    from spin_based_neural_network_gb300 import abi
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, fp32_estimator=1, refine_sweeps=5, gram_passes=3)
+    cases = CASES[:2]
+    try:
+        bat = [build(nqs, abi, c, 300 + i) for i, c in enumerate(cases)]
+        ref = [build(nqs, abi, c, 300 + i) for i, c in enumerate(cases)]
+        for b in bat + ref:
+            b["cfg"].sr_diag_shift = -2.0
+        B = nqs.Batch([(b["cfg"], b["Lx"], b["Ly"], b["a"], b["s"], b["fn"], b["user"]) for b in bat])
+        p0 = [b["a"].params.copy() for b in bat]
+        for step in range(3):
+            infos = B.step()
+            for i, r in enumerate(ref):
+                info = nqs.sr_step_minsr(r["cfg"], r["Lx"], r["Ly"], r["a"], r["s"],
+                                         r["fn"] if r["fn"] else r["a"].log_amp_fn,
+                                         r["user"] if r["user"] else r["a"].user)
+                assert infos[i].converged == info.converged == 0
+                assert infos[i].update_norm == info.update_norm == 0.0
+                assert infos[i].mean_energy == pytest.approx(info.mean_energy, rel=1e-12, abs=1e-12)
+                assert np.array_equal(bat[i]["a"].params, p0[i])
+                assert np.array_equal(r["a"].params, p0[i])
+        assert B.fallbacks() == 3 * len(cases)
+        B.free()
+    finally:
+        nqs.set_options()
