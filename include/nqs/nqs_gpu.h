@@ -51,7 +51,7 @@ typedef struct {
     int n_down;          /* >= 0: start each chain with this many down spins */
     int square_pbc;      /* 1: periodic chain / square lattices */
     int precision;       /* nqs_gpu_precision_t for MinSR */
-    int refine_sweeps;   /* MIXED: FP64 iterative-refinement sweeps */
+    int refine_sweeps;   /* MIXED: maximum FP64 preconditioned-CG iterations of the solve (stops at |r|/|rhs| <= 1e-10) */
     int gram_passes;     /* MIXED: 1 = single TF32 pass, 3 = split (hi/lo) passes */
     int mixed_space;     /* MIXED: system solved, 0 = the smaller one, 1 = sample space
                           * (N_s x N_s, O O^T), 2 = parameter space (N_p x N_p, O^T O);
@@ -246,7 +246,7 @@ typedef struct {
     double tau_int;          /* integrated autocorrelation time of E_loc (see nqs_gpu_ess) */
     double ess;              /* effective sample size of the step's batch */
     double refine_residual;  /* MIXED: relative residual after refinement */
-    int    refine_sweeps;    /* sweeps used */
+    int    refine_sweeps;    /* CG iterations used */
     int    chol_retry;       /* 1 if the +1e-6 retry ran */
     int    chol_fail_col;    /* first failing column or -1 */
     int    gpu_launches;     /* kernels launched by the step */

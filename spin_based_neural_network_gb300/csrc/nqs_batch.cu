@@ -75,12 +75,19 @@ struct Batch {
     }
 };
 
-// theta -= lr delta and ||delta||^2, with delta = 0 when the instance's FP32
-// factor broke down or its kernels reported an error.
+// True when the mixed solve of an instance broke down: a non-positive FP32
+// pivot, or a CG residual above the bound (nrm = |r|^2, |rhs|^2).
+__host__ __device__ inline bool mixed_broken(int status, const double *nrm) {
+    const double rel = nrm[1] > 0.0 ? sqrt(nrm[0] / nrm[1]) : 0.0;
+    return status >= 0 || !(rel <= MIXED_RESID_MAX);
+}
+
+// theta -= lr delta and ||delta||^2, with delta = 0 when the instance's mixed
+// solve broke down or its kernels reported an error.
 __global__ void k_batch_apply(double *params, const double *__restrict__ delta, long P, double lr, double *scal,
-                              const int *mstatus, const int *merr, int unconditional) {
+                              const int *mstatus, const int *merr, const double *mnrm, int unconditional) {
     __shared__ double red[1024];
-    const bool zero = !unconditional && (mstatus[0] >= 0 || merr[0] != 0);
+    const bool zero = !unconditional && (mixed_broken(mstatus[0], mnrm) || merr[0] != 0);
     double s = 0.0;
     for (long k = threadIdx.x; k < P; k += blockDim.x) {
         const double d = zero ? 0.0 : delta[k];
@@ -113,7 +120,7 @@ static bool enqueue_back(BatchInst &b, cudaStream_t st) {
     {
         NQS_LAUNCH("apply_update");
         k_batch_apply<<<1, 1024, 0, st>>>(b.a->d_params.p, b.delta.p, b.P, b.cfg.learning_rate, b.scal.p,
-                                          mixed_sys_status(b.mx), mixed_sys_err(b.mx), 0);
+                                          mixed_sys_status(b.mx), mixed_sys_err(b.mx), mixed_sys_nrm(b.mx), 0);
     }
     return NQS_CUDA(cudaMemcpyAsync(b.h, b.scal.p, 16 * sizeof(double), cudaMemcpyDeviceToHost, st)) &&
            NQS_CUDA(cudaMemcpyAsync(b.h + 16, mixed_sys_nrm(b.mx), 2 * sizeof(double), cudaMemcpyDeviceToHost, st)) &&
@@ -353,18 +360,18 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
     }
     if (!NQS_CUDA(cudaStreamSynchronize(st))) return -1;
     B.steps++;
-    // An instance whose FP32 factor broke down (a pivot <= 0) had its update
-    // held at zero inside the graph; solve it again in FP64 on the same
-    // centred O and eps, as the single-system step does.
+    // An instance whose mixed solve broke down (a pivot <= 0, or a CG residual
+    // above the bound) had its update held at zero inside the graph; solve it
+    // again in FP64 on the same centred O and eps, as the single-system step does.
     for (size_t i = 0; i < B.inst.size(); i++) {
         BatchInst *b = B.inst[i];
         b->fp64_fallback = 0;
-        if (b->hs[0] < 0 || b->hs[1] != 0) continue;
+        if (!mixed_broken(b->hs[0], b->h + 16) || b->hs[1] != 0) continue;
         int conv = 0;
         if (minsr_fp64_delta(b->O.p, b->eps.p, b->Ns, b->P, b->cfg.sr_diag_shift, b->delta.p, &conv) != 0)
             return -1;
         k_batch_apply<<<1, 1024, 0, st>>>(b->a->d_params.p, b->delta.p, b->P, b->cfg.learning_rate, b->scal.p,
-                                          mixed_sys_status(b->mx), mixed_sys_err(b->mx), 1);
+                                          mixed_sys_status(b->mx), mixed_sys_err(b->mx), mixed_sys_nrm(b->mx), 1);
         if (!NQS_CUDA(cudaMemcpyAsync(b->h + S_NORM2, b->scal.p + S_NORM2, sizeof(double), cudaMemcpyDeviceToHost,
                                       st)) ||
             !NQS_CUDA(cudaMemcpyAsync(b->a->h_params, b->a->d_params.p, sizeof(double) * b->P,
@@ -388,7 +395,7 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
             f.update_norm = sqrt(b->h[S_NORM2]) * b->cfg.learning_rate;
             f.acceptance_ratio = b->hc[1] ? (double)b->hc[0] / (double)b->hc[1] : 0.0;
             f.cg_iterations = 0;
-            f.converged = b->fp64_fallback ? b->fp64_conv : (b->hs[0] < 0 && b->hs[1] == 0);
+            f.converged = b->fp64_fallback ? b->fp64_conv : (!mixed_broken(b->hs[0], b->h + 16) && b->hs[1] == 0);
         }
     }
     if (failed) {

@@ -177,6 +177,10 @@ bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, 
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
 
+// Relative residual |r| / |rhs| above which a mixed solve counts as broken down
+// and the step is solved again in FP64.
+constexpr double MIXED_RESID_MAX = 1e-6;
+
 // Mixed-precision MinSR solve (nqs_mixed.cu): centres O in place and solves in
 // sample space, (O_c O_c^T / N_s + shift I) y = eps (writes y), or in parameter
 // space, (O_c^T O_c / N_s + shift I) delta = O_c^T eps / N_s (writes delta and

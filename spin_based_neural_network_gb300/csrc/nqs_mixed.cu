@@ -759,6 +759,25 @@ __device__ __forceinline__ float dot4_range(const float *row, const float *v, in
     return t;
 }
 
+// a . b over [0, n), computed by every CTA in the same fixed order (thread-
+// strided partial sums, a warp butterfly, then the warps in order), so that all
+// CTAs hold the same value whatever the grid size.
+__device__ __forceinline__ double dot_all(const double *a, const double *b, int n, double *red) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += PS_THREADS) s += __ldcg(a + i) * __ldcg(b + i);
+    s = warp_sum(s);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < PS_THREADS / 32; w++) t += red[w];
+    return t;
+}
+
+// Relative residual |r| / |rhs| at which the CG refinement stops.
+constexpr double CG_RTOL = 1e-10;
+
 struct FrArgs {
     float *T;           // [n][n] Gram + shift (lower) on entry; U = L^T in the upper triangle after
     float *Li, *LiT;    // [n][ldl] L^{-1} (lower) and its transpose; pad columns are zero
@@ -773,9 +792,10 @@ struct FrArgs {
     double *x;          // [n] solution
     double *rhs, *r;    // [n] right-hand side and residual
     double *u, *upart;  // intermediate vector, partial column sums
+    double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
-    double *nrm;        // [2] |r|^2, |rhs|^2
-    int sweeps;
+    double *nrm;        // [3] |r|^2, |rhs|^2, CG iterations run
+    int sweeps;         // maximum CG iterations
     int *status;        // [0] first failing column or -1
     unsigned *bar;      // [0] arrivals, [1] generation
     int *err;
@@ -965,90 +985,101 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     if (!grid_barrier(a.bar, a.err, G)) return;
     NQS_PHASE(5);
 
-    // ---------------- refinement sweeps
-    for (int s = 0; s <= a.sweeps; s++) {
-        // z = L^{-1} rf (row i reads the 4-aligned groups up to i; the entries
-        // right of the diagonal inside a group are the zeros of the diagonal block)
+    // ---------------- preconditioned conjugate gradients in FP64 on the exact
+    // operator, preconditioner M = L L^T from the FP32 factor.  Unlike plain
+    // iterative refinement this still converges when cond(A) * eps_fp32 is not
+    // small.  Scalars come from dot_all, so every CTA takes the same branches.
+    // M^{-1} v with rf = float(v): zf = L^{-1} rf, out = L^{-T} zf (row i of
+    // L^{-1} reads the 4-aligned groups up to i; the entries right of the
+    // diagonal inside a group are the zeros of the diagonal block).
+    auto precond = [&](double *out) -> bool {
         for (int i = gwarp; i < n; i += gwarps) {
             const float t = dot4_range(a.Li + (size_t)i * ldl, a.rf, 0, (i >> 2) + 1, lane);
             if (lane == 0) a.zf[i] = t;
         }
-        if (!grid_barrier(a.bar, a.err, G)) return;
-        // x += L^{-T} z (zf and the pad columns are zero beyond n)
+        if (!grid_barrier(a.bar, a.err, G)) return false;
         for (int j = gwarp; j < n; j += gwarps) {
             const float t = dot4_range(a.LiT + (size_t)j * ldl, a.zf, j >> 2, ldl >> 2, lane);
-            if (lane == 0) a.x[j] = (s == 0 ? 0.0 : __ldcg(a.x + j)) + (double)t;
+            if (lane == 0) out[j] = (double)t;
         }
-        if (!grid_barrier(a.bar, a.err, G)) return;
-        NQS_PHASE(4);
-        // FP64 residual r = rhs - A x
+        return grid_barrier(a.bar, a.err, G);
+    };
+    // q = A v: O_c (O_c^T v) / N_s + shift v (samples) or O_c^T (O_c v) / N_s + shift v (parameters)
+    auto apply_op = [&](const double *v, double *q) -> bool {
         if (a.space == 0) {
-            // A y = O_c (O_c^T y) / N_s + shift y
-            colsum_partial(a.O, Ns, P, a.x, a.upart, gwarp, gwarps, lane);
-            if (!grid_barrier(a.bar, a.err, G)) return;
+            colsum_partial(a.O, Ns, P, v, a.upart, gwarp, gwarps, lane);
+            if (!grid_barrier(a.bar, a.err, G)) return false;
             for (long k = gwarp; k < P; k += gwarps) {
                 const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
                 if (lane == 0) a.u[k] = sk;
             }
-            if (!grid_barrier(a.bar, a.err, G)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return false;
             const double *us = stage_vec(a.u, P, (double *)psm, PS_SMEM / 8);
             for (int i = gwarp; i < Ns; i += gwarps) {
                 const double d = us == a.u ? rowdot<true>(a.O + (size_t)i * P, P, us, lane)
                                            : rowdot<false>(a.O + (size_t)i * P, P, us, lane);
-                if (lane == 0) {
-                    const double ri = a.rhs[i] - d / (double)Ns - a.shift * __ldcg(a.x + i);
-                    a.r[i] = ri;
-                    a.rf[i] = (float)ri;
-                }
+                if (lane == 0) q[i] = d / (double)Ns + a.shift * __ldcg(v + i);
             }
         } else {
-            // A delta = O_c^T (O_c delta) / N_s + shift delta
-            const double *xs = stage_vec(a.x, P, (double *)psm, PS_SMEM / 8);
+            const double *vs = stage_vec(v, P, (double *)psm, PS_SMEM / 8);
             for (int i = gwarp; i < Ns; i += gwarps) {
-                const double d = xs == a.x ? rowdot<true>(a.O + (size_t)i * P, P, xs, lane)
-                                           : rowdot<false>(a.O + (size_t)i * P, P, xs, lane);
+                const double d = vs == v ? rowdot<true>(a.O + (size_t)i * P, P, vs, lane)
+                                         : rowdot<false>(a.O + (size_t)i * P, P, vs, lane);
                 if (lane == 0) a.u[i] = d;
             }
-            if (!grid_barrier(a.bar, a.err, G)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return false;
             colsum_partial(a.O, Ns, P, a.u, a.upart, gwarp, gwarps, lane);
-            if (!grid_barrier(a.bar, a.err, G)) return;
+            if (!grid_barrier(a.bar, a.err, G)) return false;
             for (long k = gwarp; k < P; k += gwarps) {
                 const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
-                if (lane == 0) {
-                    const double rk = __ldcg(a.rhs + k) - sk / (double)Ns - a.shift * __ldcg(a.x + k);
-                    a.r[k] = rk;
-                    a.rf[k] = (float)rk;
-                }
+                if (lane == 0) q[k] = sk / (double)Ns + a.shift * __ldcg(v + k);
             }
+        }
+        return grid_barrier(a.bar, a.err, G);
+    };
+    __shared__ double red[PS_THREADS / 32];
+    if (!precond(a.x)) return;                          // x0 = M^{-1} rhs
+    NQS_PHASE(4);
+    if (!apply_op(a.x, a.q)) return;
+    for (int i = gtid; i < n; i += gthreads) {
+        const double ri = __ldcg(a.rhs + i) - __ldcg(a.q + i);
+        a.r[i] = ri;
+        a.rf[i] = (float)ri;
+    }
+    if (!grid_barrier(a.bar, a.err, G)) return;
+    NQS_PHASE(5);
+    if (!precond(a.z)) return;
+    NQS_PHASE(4);
+    const double bb = dot_all(a.rhs, a.rhs, n, red);
+    double rho = dot_all(a.r, a.z, n, red), rr = dot_all(a.r, a.r, n, red), beta = 0.0;
+    int it = 0;
+    for (; it < a.sweeps && rr > CG_RTOL * CG_RTOL * bb && rho > 0.0; it++) {
+        for (int i = gtid; i < n; i += gthreads)
+            a.p[i] = it == 0 ? __ldcg(a.z + i) : __ldcg(a.z + i) + beta * __ldcg(a.p + i);
+        if (!grid_barrier(a.bar, a.err, G)) return;
+        if (!apply_op(a.p, a.q)) return;
+        const double pq = dot_all(a.p, a.q, n, red);
+        if (!(pq > 0.0)) break;
+        const double alpha = rho / pq;
+        for (int i = gtid; i < n; i += gthreads) {
+            a.x[i] = __ldcg(a.x + i) + alpha * __ldcg(a.p + i);
+            const double ri = __ldcg(a.r + i) - alpha * __ldcg(a.q + i);
+            a.r[i] = ri;
+            a.rf[i] = (float)ri;
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(5);
+        if (!precond(a.z)) return;
+        NQS_PHASE(4);
+        const double rho1 = dot_all(a.r, a.z, n, red);
+        rr = dot_all(a.r, a.r, n, red);
+        beta = rho1 / rho;
+        rho = rho1;
     }
-    // ---------------- |r|^2 and |rhs|^2
-    if (bx == 0) {
-        double s1 = 0.0, s2 = 0.0;
-        for (int i = tid; i < n; i += PS_THREADS) {
-            const double ri = __ldcg(a.r + i), bi = __ldcg(a.rhs + i);
-            s1 += ri * ri;
-            s2 += bi * bi;
-        }
-        s1 = warp_sum(s1);
-        s2 = warp_sum(s2);
-        __shared__ double red[2][PS_THREADS / 32];
-        if (lane == 0) {
-            red[0][tid >> 5] = s1;
-            red[1][tid >> 5] = s2;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            double t1 = 0.0, t2 = 0.0;
-            for (int q = 0; q < PS_THREADS / 32; q++) {
-                t1 += red[0][q];
-                t2 += red[1][q];
-            }
-            a.nrm[0] = t1;
-            a.nrm[1] = t2;
-        }
+    if (bx == 0 && tid == 0) {
+        a.nrm[0] = rr;
+        a.nrm[1] = bb;
+        a.nrm[2] = (double)it;
     }
     if (timing) {
         tacc[6] = gtimer() - tstart;
@@ -1074,7 +1105,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrA
 // ---------------------------------------------------------------- driver
 struct MixedWs {
     DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf;
-    DevBuf<double> rhs, r, u, upart, nrm;
+    DevBuf<double> rhs, r, u, upart, nrm, p, q, z;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
     DevBuf<unsigned long long> tm;
@@ -1198,6 +1229,9 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     fa.r = w.r.p;
     fa.u = w.u.p;
     fa.upart = w.upart.p;
+    fa.p = w.p.p;
+    fa.q = w.q.p;
+    fa.z = w.z.p;
     fa.rf = w.rf.p;
     fa.zf = w.zf.p;
     fa.nrm = w.nrm.p;
@@ -1255,17 +1289,18 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         *moved = true;
     }
     const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
+    const void *before[16] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p};
     const int ldl = (n + 31) / 32 * 32;
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
-        !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(2) || !w.status.ensure(2) ||
+        !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) ||
+        !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(3) || !w.status.ensure(2) ||
         !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
-    const void *after[13] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p};
-    for (int i = 0; i < 13; i++) *moved |= before[i] != after[i];
+    const void *after[16] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p};
+    for (int i = 0; i < 16; i++) *moved |= before[i] != after[i];
     if (*moved || w.n != n) {
         // the pad columns of L^{-1} are read (as zeros) by the vectorised solves
         if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
@@ -1360,7 +1395,7 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
         c.launches += Gr.kernels;
     }
     int hs[2] = {-1, 0};
-    double h[2] = {0.0, 0.0};
+    double h[3] = {0.0, 0.0, 0.0};
     unsigned long long tns[8] = {};
     if (!NQS_CUDA(cudaMemcpyAsync(&hs[0], w.status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
         !NQS_CUDA(cudaMemcpyAsync(tns, w.tm.p, sizeof(tns), cudaMemcpyDeviceToHost, st)) ||
@@ -1374,8 +1409,11 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
         return false;
     }
     *param_space = pl.space == 1;
-    *out_fail = hs[0];
     *out_resid = h[1] > 0 ? sqrt(h[0] / h[1]) : 0.0;
+    // a factor too inaccurate for the CG to reach the residual bound counts as
+    // a breakdown (the caller solves the step in FP64)
+    *out_fail = hs[0] >= 0 ? hs[0] : (*out_resid > MIXED_RESID_MAX || !(*out_resid == *out_resid)) ? pl.n : -1;
+    step_stats().refine_sweeps = (int)h[2];
     for (int k = 0; k < 8; k++) step_stats().phase_us[k] = 1e-3 * (double)tns[k];
     return NQS_CUDA(cudaGetLastError());
 }

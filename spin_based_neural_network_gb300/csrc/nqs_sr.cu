@@ -867,7 +867,6 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
                                    &resid, &f32))
                 return -1;
             ss.refine_residual = resid;
-            ss.refine_sweeps = c.opts.refine_sweeps;
             if (f32 < 0) {
                 solved = true;
                 converged = 1;
