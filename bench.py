@@ -42,8 +42,8 @@ THERM = 512
 SHIFT = 1e-4
 LR = 0.005
 SEED = 2026
-SWEEPS = 5           # FP64 refinement sweeps: the parameter-space refinement error (~2e-7 after 5)
-                     # is below the FP32 estimator's own delta-theta error (~3e-6)
+SWEEPS = 5           # maximum FP64 preconditioned-CG iterations of the solve (stops at |r|/|rhs| <= 1e-10);
+                     # the solve error is then far below the FP32 estimator's own delta-theta error (~3e-6)
 METRIC = "MinSR steps/s (4x4 Heisenberg PBC, complex RBM alpha=2, N_s=4096)"
 
 
@@ -501,8 +501,8 @@ def run_gpu(args):
     phases = None
     if prec == abi.PREC_MIXED:
         ph = nqs.last_step_stats().phase_us
-        phases = dict(zip(("diag_blocks", "panels", "trailing", "triangular_inverse", "triangular_solves",
-                           "rhs_and_residuals", "total", "diag_block_owner_work"),
+        phases = dict(zip(("diag_blocks", "panels", "trailing", "triangular_inverse",
+                           "preconditioner", "rhs_operator_cg", "total", "diag_block_owner_work"),
                           [round(ph[i], 1) for i in range(8)]))
     L.nqs_gpu_event_destroy(e0)
     L.nqs_gpu_event_destroy(e1)

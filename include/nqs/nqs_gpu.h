@@ -254,10 +254,11 @@ typedef struct {
     int    mixed_fallback;   /* 1 if the FP32 factor failed and FP64 solved the step */
     int    pad_;
     /* MIXED: microseconds spent in the phases of the cooperative factor /
-     * inverse / refinement kernel: [0] diagonal blocks, [1] panels, [2] trailing
-     * updates, [3] triangular inverse, [4] triangular solves, [5] right-hand
-     * side and FP64 residuals, [6] total; [7] the part of [0] spent by the
-     * owning CTAs on factoring and inverting the diagonal blocks */
+     * inverse / CG kernel (seen from CTA 0): [0] diagonal blocks, [1] panels,
+     * [2] trailing updates, [3] triangular inverse, [4] preconditioner
+     * applications, [5] right-hand side, operator products and CG updates, [6]
+     * total; [7] the part of [0] spent by the owning CTAs on factoring and
+     * inverting the diagonal blocks */
     double phase_us[8];
     /* MIXED with mixed_check and fp32_estimator: |<E> - <E>_fp64| / |<E>_fp64|
      * on the same samples (-1 when not measured) */

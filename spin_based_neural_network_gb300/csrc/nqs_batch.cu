@@ -37,7 +37,7 @@ struct BatchInst {
     DevHam H{};
     int Ns = 0, C = 0;
     long P = 0;
-    DevBuf<double> E, Ei, eps, O, gm, scal, delta, y, part;
+    DevBuf<double> E, Ei, eps, O, gm, scal, delta, y, part, es;
     DevBuf<unsigned long long> move;
     MixedSys *mx = nullptr;
     double *h = nullptr;      // pinned: scal[16], nrm[2]
@@ -107,7 +107,7 @@ static bool enqueue_front(BatchInst &b, cudaStream_t st) {
     uint64_t *bits = nullptr;
     if (!ansatz_refresh_derived(b.a) || !sampler_produce_dev(b.s, b.Ns, &bits, b.move.p) ||
         !launch_local_estimator(b.A, b.H, bits, b.Ns, b.E.p, b.Ei.p, b.O.p, nullptr, 1, true) ||
-        !enqueue_energy_stats(b.E.p, b.Ns, b.C, b.scal.p, b.eps.p) ||
+        !enqueue_energy_stats(b.E.p, b.Ns, b.C, b.scal.p, b.eps.p, b.es.p) ||
         !enqueue_col_means(b.O.p, b.Ns, b.P, b.scal.p, b.gm.p, b.part.p))
         return false;
     mixed_sys_front(b.mx, st, true);
@@ -297,6 +297,8 @@ nqs_gpu_batch_t *nqs_gpu_batch_create(const nqs_gpu_instance_t *in, int count) {
             !b->O.ensure((size_t)b->Ns * b->P) || !b->gm.ensure(b->P) || !b->scal.ensure(16) ||
             !b->delta.ensure(b->P) || !b->y.ensure(b->Ns) || !b->move.ensure(1) ||
             !b->part.ensure((size_t)col_stats_scratch(b->Ns, b->P)) ||
+            !b->es.ensure(energy_scratch_doubles(b->Ns)) ||
+            !NQS_CUDA(cudaMemset(b->es.p, 0, sizeof(double) * energy_scratch_doubles(b->Ns))) ||
             !NQS_CUDA(cudaMemcpy(b->move.p, &mv, sizeof(mv), cudaMemcpyHostToDevice)) ||
             !NQS_CUDA(cudaMallocHost(&b->h, 18 * sizeof(double))) ||
             !NQS_CUDA(cudaMallocHost(&b->hs, 2 * sizeof(int))) ||

@@ -218,7 +218,11 @@ void mixed_batch_free(MixedBatch *b);
 bool mixed_batch_launch(MixedBatch *b, cudaStream_t st);
 
 // Stream-only pieces of the SR step (nqs_sr.cu), for captured sequences.
-bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps);
+// <E>, <E^2> (scal), eps = E - <E>, tau_int and ESS (scal) over multiple
+// blocks; scratch holds energy_scratch_doubles(Ns) doubles, zero before its
+// first use (its tickets return to zero after each call).
+size_t energy_scratch_doubles(int Ns);
+bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps, double *scratch);
 bool enqueue_col_means(const double *O, int Ns, long P, const double *scal, double *gm, double *part);
 long col_stats_scratch(int Ns, long P);
 bool enqueue_col_dot(const double *O, int Ns, long P, const double *y, double scale, double *out);

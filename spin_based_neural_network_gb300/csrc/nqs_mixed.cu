@@ -381,31 +381,29 @@ __device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int
         if (warp == 0) {
             // right-looking, lane = row in registers; the scaled column j is
             // broadcast through shared memory (a shuffle per entry is ~3x slower)
+            // Lane = row; column j of L is broadcast by shuffles.  Branch-free:
+            // every lane updates its whole row, and the entries right of a lane's
+            // diagonal (zero on entry) become scratch that nothing reads (lane i's
+            // row[c], c > i, is only broadcast at steps j = c > i, which read lanes
+            // c' > j only).  A non-positive pivot records the first failing column
+            // and continues on a unit pivot; the block is discarded then.  (With
+            // a per-entry `c <= lane` guard this loop ran ~4x slower.)
             float row[32];
 #pragma unroll
-            for (int c = 0; c < 32; c++) row[c] = (c <= lane) ? S[c0 + lane][c0 + c] : 0.f;
-            float *colj = tmp;                                 // 32 floats
+            for (int c = 0; c < 32; c++) row[c] = S[c0 + lane][c0 + c];
             int fail = -1;
             float dinv = 0.f;                                  // lane j keeps 1 / L_jj
 #pragma unroll
             for (int j = 0; j < 32; j++) {
-                if (fail < 0) {
-                    const float d = __shfl_sync(0xffffffffu, row[j], j);
-                    if (!(d > 0.f)) {
-                        fail = j;
-                    } else {
-                        const float inv = rsqrtf(d);
-                        row[j] = lane == j ? d * inv : row[j] * inv;
-                        if (lane == j) dinv = inv;
-                        colj[lane] = row[j];
-                        __syncwarp();
-                        const float lrj = row[j];
+                const float d = __shfl_sync(0xffffffffu, row[j], j);
+                const bool ok = d > 0.f;
+                fail = (fail < 0 && !ok) ? j : fail;
+                const float inv = rsqrtf(ok ? d : 1.f);
+                row[j] *= inv;                                 // lane j: d / sqrt(d) = L_jj
+                dinv = lane == j ? inv : dinv;
+                const float lrj = row[j];                     // L[lane][j]
 #pragma unroll
-                        for (int c = j + 1; c < 32; c++)
-                            if (c <= lane) row[c] -= lrj * colj[c];
-                        __syncwarp();
-                    }
-                }
+                for (int c = j + 1; c < 32; c++) row[c] = fmaf(-lrj, __shfl_sync(0xffffffffu, lrj, c), row[c]);
             }
 #pragma unroll
             for (int c = 0; c < 32; c++)
@@ -829,43 +827,68 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     }
 
     // ---------------- factor
+    // Diagonal block kb: its owner CTA loads it, factors and inverts it in
+    // shared memory and stores X_kk in Li / LiT (a breakdown goes to status[0]).
+    auto factor_diag = [&](int kb) {
+        const int k0 = kb * BT, bs = min(BT, n - k0);
+        const unsigned long long t_own = tid == 0 ? gtimer() : 0;
+        for (int e0 = 0; e0 < BT * BT; e0 += 8 * PS_THREADS) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int e = e0 + tid + q * PS_THREADS, rr = e / BT, cc = e % BT;
+                const bool in = rr < bs && cc <= rr;
+                v[q] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) : (rr == cc ? 1.f : 0.f);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int e = e0 + tid + q * PS_THREADS;
+                S0[e / BT][e % BT] = v[q];
+            }
+        }
+        __syncthreads();
+        const int f = block_chol128(S0, S1, bs, &s_flag, tmpb);
+        if (f >= 0) {
+            if (tid == 0) {
+                a.status[0] = k0 + f;
+                __threadfence();
+            }
+        } else {
+            block_inv128(S0, S1, tmpb);
+            for (int e = tid; e < BT * BT; e += PS_THREADS) {
+                const int rr = e >> 7, q = e & (BT - 1);
+                if (rr < bs && q < bs) {
+                    a.Li[(size_t)(k0 + rr) * ldl + k0 + q] = S1[rr][q];
+                    a.LiT[(size_t)(k0 + rr) * ldl + k0 + q] = S1[q][rr];
+                }
+            }
+        }
+        __syncthreads();                                    // S0 / S1 are reused as GEMM staging
+        if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
+    };
+    // one 64 x 64 tile t (lower-triangular order) of the trailing update of
+    // block kb: A[i][j] -= sum_m U[k0 + m][i] U[k0 + m][j], k1 <= j <= i
+    auto trailing_tile = [&](int k0, int bs, int k1, int t) {
+        int bi, bj;
+        tri_tile(t, bi, bj);
+        const int r0 = k1 + bi * GT, c0 = k1 + bj * GT;
+        float acc[4][4] = {};
+        const float *U = a.T + (size_t)k0 * n;
+        gemm64<true, true>(acc, U, n, r0, n, U, n, c0, n, 0, bs, TS);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
+                if (i < n && j <= i) {
+                    const size_t idx = (size_t)i * n + j;
+                    a.T[idx] = __ldcg(&a.T[idx]) - acc[u][v];
+                }
+            }
+    };
     for (int kb = 0; kb < nb; kb++) {
         const int k0 = kb * BT, bs = min(BT, n - k0), k1 = k0 + bs, rest = n - k1;
-        if (bx == kb % G) {
-            const unsigned long long t_own = tid == 0 ? gtimer() : 0;
-            for (int e0 = 0; e0 < BT * BT; e0 += 8 * PS_THREADS) {
-                float v[8];
-#pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    const int e = e0 + tid + q * PS_THREADS, rr = e / BT, cc = e % BT;
-                    const bool in = rr < bs && cc <= rr;
-                    v[q] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) : (rr == cc ? 1.f : 0.f);
-                }
-#pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    const int e = e0 + tid + q * PS_THREADS;
-                    S0[e / BT][e % BT] = v[q];
-                }
-            }
-            __syncthreads();
-            const int f = block_chol128(S0, S1, bs, &s_flag, tmpb);
-            if (f >= 0) {
-                if (tid == 0) {
-                    a.status[0] = k0 + f;
-                    __threadfence();
-                }
-            } else {
-                block_inv128(S0, S1, tmpb);
-                for (int e = tid; e < BT * BT; e += PS_THREADS) {
-                    const int rr = e >> 7, q = e & (BT - 1);
-                    if (rr < bs && q < bs) {
-                        a.Li[(size_t)(k0 + rr) * ldl + k0 + q] = S1[rr][q];
-                        a.LiT[(size_t)(k0 + rr) * ldl + k0 + q] = S1[q][rr];
-                    }
-                }
-            }
-            if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
-        }
+        if (bx == kb % G) factor_diag(kb);
         if (!grid_barrier(a.bar, a.err, G)) return;
         if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
         NQS_PHASE(0);
@@ -890,27 +913,12 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(1);
-        // trailing update: A[i][j] -= sum_m U[k0 + m][i] U[k0 + m][j], k1 <= j <= i
+        // trailing update (look-ahead of the next diagonal block was tried: one
+        // CTA updating that block's three 64 x 64 tiles alone costs more than
+        // the trailing phase it hides)
         {
             const int ntt = (rest + GT - 1) / GT, ntiles = ntt * (ntt + 1) / 2;
-            for (int t = bx; t < ntiles; t += G) {
-                int bi, bj;
-                tri_tile(t, bi, bj);
-                const int r0 = k1 + bi * GT, c0 = k1 + bj * GT;
-                float acc[4][4] = {};
-                const float *U = a.T + (size_t)k0 * n;
-                gemm64<true, true>(acc, U, n, r0, n, U, n, c0, n, 0, bs, TS);
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-#pragma unroll
-                    for (int v = 0; v < 4; v++) {
-                        const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
-                        if (i < n && j <= i) {
-                            const size_t idx = (size_t)i * n + j;
-                            a.T[idx] = __ldcg(&a.T[idx]) - acc[u][v];
-                        }
-                    }
-            }
+            for (int t = bx; t < ntiles; t += G) trailing_tile(k0, bs, k1, t);
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(2);

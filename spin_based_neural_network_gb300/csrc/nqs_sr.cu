@@ -22,7 +22,7 @@ bool sampler_produce(Sampler *s, int n, uint64_t **d_out);
 
 // ---------------------------------------------------------------- workspace
 struct Workspace {
-    DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part, y64, d64;
+    DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part, y64, d64, es;
     DevBuf<int> status;
     DevBuf<uint64_t> batch_bits;
 };
@@ -71,46 +71,174 @@ __global__ void k_energy_stats(const double *__restrict__ E, int n, double *scal
         for (int i = t; i < n; i += blockDim.x) eps[i] = E[i] - mean;
 }
 
-// Integrated autocorrelation time of E_loc over C chains whose samples sit at
-// rows k * C + c (k = 0 .. K-1): gamma(t) pooled over chains, rho = gamma /
-// gamma(0), tau(M) = 1 + 2 sum_{t=1}^{M} rho(t) with the self-consistent
-// window, the smallest M >= 5 tau(M) (Sokal; the automatic window of emcee),
-// and ESS = K C / tau.  One block; eps holds E - <E>.
-__global__ void k_ess(const double *__restrict__ eps, int Ns, int C, double *scal) {
-    __shared__ double red[256];
-    __shared__ int stop;
-    const int K = C > 0 ? Ns / C : 0, n = K * C, t0 = threadIdx.x;
+// ---- multi-block statistics.  GB300's FP64 rate is ~2 FMA / clock / SM, so
+// the compensated sums and the lag products are spread over blocks of
+// ES_CHUNK samples; the last block to finish (an atomic ticket) merges the
+// partials in block order, so results do not depend on scheduling.
+constexpr int ES_THREADS = 256, ES_CHUNK = 1024, ES_LAGS = 16;
+
+static int es_blocks(int n) { return (n + ES_CHUNK - 1) / ES_CHUNK; }
+
+// doubles of scratch enqueue_energy_stats needs for n samples: 2 words of
+// tickets (zero on first use) followed by the block partials
+size_t energy_scratch_doubles(int n) { return (size_t)es_blocks(n) * (4 + ES_LAGS + 1) + 2; }
+
+__device__ __forceinline__ void two_sum_merge(double &s, double &c, double s2, double c2) {
+    const double t = s + s2, bb = t - s;
+    c = c + c2 + ((s - (t - bb)) + (s2 - bb));
+    s = t;
+}
+
+// Sums of E and E^2 with Neumaier compensation per thread, merged by exact
+// TwoSum trees; the last block merges the block partials in order and writes
+// <E>, <E^2>.
+__global__ void __launch_bounds__(ES_THREADS) k_energy_mb(const double *__restrict__ E, int n, double *part,
+                                                         unsigned *ticket, double *scal) {
+    __shared__ double ss[ES_THREADS], sc[ES_THREADS], qs[ES_THREADS], qc[ES_THREADS];
+    __shared__ bool last;
+    const int t = threadIdx.x, i0 = blockIdx.x * ES_CHUNK, i1 = min(n, i0 + ES_CHUNK);
+    double s = 0.0, c = 0.0, q = 0.0, qcc = 0.0;
+    for (int i = i0 + t; i < i1; i += ES_THREADS) {
+        const double x = E[i], tt = s + x;
+        c += fabs(s) >= fabs(x) ? (s - tt) + x : (x - tt) + s;
+        s = tt;
+        const double x2 = x * x, t2 = q + x2;
+        qcc += fabs(q) >= fabs(x2) ? (q - t2) + x2 : (x2 - t2) + q;
+        q = t2;
+    }
+    ss[t] = s;
+    sc[t] = c;
+    qs[t] = q;
+    qc[t] = qcc;
+    __syncthreads();
+    for (int o = ES_THREADS / 2; o > 0; o >>= 1) {
+        if (t < o) {
+            two_sum_merge(ss[t], sc[t], ss[t + o], sc[t + o]);
+            two_sum_merge(qs[t], qc[t], qs[t + o], qc[t + o]);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        double *p = part + (size_t)blockIdx.x * 4;
+        p[0] = ss[0];
+        p[1] = sc[0];
+        p[2] = qs[0];
+        p[3] = qc[0];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || t != 0) return;
+    __threadfence();
+    double S = 0.0, Sc = 0.0, Q = 0.0, Qc = 0.0;
+    for (int b = 0; b < (int)gridDim.x; b++) {
+        const double *p = part + (size_t)b * 4;
+        two_sum_merge(S, Sc, __ldcg(p), __ldcg(p + 1));
+        two_sum_merge(Q, Qc, __ldcg(p + 2), __ldcg(p + 3));
+    }
+    scal[S_EMEAN] = (S + Sc) / (double)n;
+    scal[S_ESQ] = (Q + Qc) / (double)n;
+    *ticket = 0;
+}
+
+// eps_i = E_i - <E> for every sample, and the lag sums of the integrated
+// autocorrelation time of E_loc over C chains whose samples sit at rows
+// k * C + c (k = 0 .. K-1): gamma(t) = sum_e eps_e eps_{e + tC} over e < (K - t) C,
+// t <= ES_LAGS, as block partials; the last block sums them in block order and
+// applies the self-consistent window: tau(M) = 1 + 2 sum_{t=1}^{M} gamma(t) /
+// gamma(0) with the smallest M >= 5 tau(M) (Sokal; the automatic window of
+// emcee), continuing past ES_LAGS itself (up to 512) when the window is wider.
+// ESS = K C / tau.
+__global__ void __launch_bounds__(ES_THREADS) k_ess_mb(const double *__restrict__ E, int Ns, int C, double *gpart,
+                                                      unsigned *ticket, double *scal, double *eps) {
+    __shared__ double red[ES_THREADS / 32][ES_LAGS + 1];
+    __shared__ bool last;
+    const int t0 = threadIdx.x, lane = t0 & 31, w = t0 >> 5;
+    const double mean = scal[S_EMEAN];
+    const int i0 = blockIdx.x * ES_CHUNK, i1 = min(Ns, i0 + ES_CHUNK);
+    for (int i = i0 + t0; i < i1; i += ES_THREADS) eps[i] = E[i] - mean;
+    const int K = C > 0 ? Ns / C : 0, n = K * C;
+    const int maxlag = K - 1 < 512 ? K - 1 : 512, T1 = maxlag < ES_LAGS ? maxlag : ES_LAGS;
     if (K < 2) {
-        if (t0 == 0) {
+        if (blockIdx.x == 0 && t0 == 0) {
             scal[S_TAU] = 1.0;
             scal[S_ESS] = (double)Ns;
         }
         return;
     }
-    double g0 = 0.0, tau = 1.0;
-    const int maxlag = K - 1 < 512 ? K - 1 : 512;
-    if (t0 == 0) stop = 0;
-    for (int t = 0; t <= maxlag; t++) {
-        double s = 0.0;
-        const int m = (K - t) * C;
-        for (int e = t0; e < m; e += blockDim.x) s += eps[e] * eps[e + t * C];
-        red[t0] = s;
-        __syncthreads();
-        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-            if (t0 < o) red[t0] += red[t0 + o];
+    double g[ES_LAGS + 1];
+#pragma unroll
+    for (int t = 0; t <= ES_LAGS; t++) g[t] = 0.0;
+    for (int e = i0 + t0; e < min(i1, n); e += ES_THREADS) {
+        const double a = E[e] - mean;
+#pragma unroll
+        for (int t = 0; t <= ES_LAGS; t++)
+            if (t <= T1 && e < (K - t) * C) g[t] += a * (E[e + t * C] - mean);
+    }
+#pragma unroll
+    for (int t = 0; t <= ES_LAGS; t++) {
+        const double v = warp_sum(g[t]);
+        if (lane == 0) red[w][t] = v;
+    }
+    __syncthreads();
+    if (t0 <= ES_LAGS) {
+        double v = 0.0;
+        for (int q = 0; q < ES_THREADS / 32; q++) v += red[q][t0];
+        gpart[(size_t)blockIdx.x * (ES_LAGS + 1) + t0] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (t0 == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // gamma(t) in block order; the window over t <= T1
+    __shared__ double gam[ES_LAGS + 1];
+    if (t0 <= T1) {
+        double v = 0.0;
+        for (int b = 0; b < (int)gridDim.x; b++) v += __ldcg(gpart + (size_t)b * (ES_LAGS + 1) + t0);
+        gam[t0] = v / (double)((K - t0) * C);
+    }
+    __syncthreads();
+    __shared__ double s_tau;
+    __shared__ int s_done;
+    if (t0 == 0) {
+        double tau = 1.0;
+        int done = 0;
+        const double g0 = gam[0];
+        if (!(g0 > 0.0)) {
+            done = 1;
+        } else {
+            for (int t = 1; t <= T1; t++) {
+                tau += 2.0 * gam[t] / g0;
+                if ((double)t >= 5.0 * tau) {
+                    done = 1;
+                    break;
+                }
+            }
+        }
+        s_tau = tau;
+        s_done = done || T1 == maxlag;
+        *ticket = 0;
+    }
+    __syncthreads();
+    double tau = s_tau;
+    if (!s_done) {
+        // wide window: further lags by this block (eps of every block is written)
+        const double g0 = gam[0];
+        for (int t = T1 + 1; t <= maxlag; t++) {
+            double v = 0.0;
+            const int m = (K - t) * C;
+            for (int e = t0; e < m; e += ES_THREADS) v += (E[e] - mean) * (E[e + t * C] - mean);
+            v = warp_sum(v);
             __syncthreads();
+            if (lane == 0) red[w][0] = v;
+            __syncthreads();
+            double gt = 0.0;
+            for (int q = 0; q < ES_THREADS / 32; q++) gt += red[q][0];
+            tau += 2.0 * (gt / (double)m) / g0;
+            if ((double)t >= 5.0 * tau) break;
         }
-        const double g = red[0] / (double)m;
-        __syncthreads();
-        if (t == 0) {
-            g0 = g;
-            if (!(g0 > 0.0)) break;
-            continue;
-        }
-        tau += 2.0 * g / g0;
-        if (t0 == 0 && (double)t >= 5.0 * tau) stop = 1;
-        __syncthreads();
-        if (stop) break;
     }
     if (t0 == 0) {
         if (!(tau > 0.0)) tau = 1.0;
@@ -649,15 +777,27 @@ static bool col_stats(const double *O, int Ns, long P, const double *E, const do
     return NQS_CUDA(cudaGetLastError());
 }
 
-bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps) {
+// Scratch for enqueue_energy_stats, zeroed when (re)allocated.
+static bool ensure_energy_scratch(DevBuf<double> &b, int Ns) {
+    const size_t nd = energy_scratch_doubles(Ns), n0 = b.p ? b.n : 0;
+    if (!b.ensure(nd)) return false;
+    // a new allocation starts zeroed (the ticket words, at its start, stay zero between calls)
+    if (b.n != n0 && !NQS_CUDA(cudaMemsetAsync(b.p, 0, sizeof(double) * b.n, ctx().stream))) return false;
+    return true;
+}
+
+bool enqueue_energy_stats(const double *E, int Ns, int chains, double *scal, double *eps, double *scratch) {
     cudaStream_t st = ctx().stream;
+    const int G = es_blocks(Ns);
+    unsigned *tickets = (unsigned *)scratch;
+    double *part = scratch + 2, *gpart = part + (size_t)G * 4;
     {
         NQS_LAUNCH("energy_stats");
-        k_energy_stats<<<1, 1024, 0, st>>>(E, Ns, scal, eps);
+        k_energy_mb<<<G, ES_THREADS, 0, st>>>(E, Ns, part, tickets, scal);
     }
     {
         NQS_LAUNCH("ess");
-        k_ess<<<1, 256, 0, st>>>(eps, Ns, chains, scal);
+        k_ess_mb<<<G, ES_THREADS, 0, st>>>(E, Ns, chains, gpart, tickets + 1, scal, eps);
     }
     return NQS_CUDA(cudaGetLastError());
 }
@@ -836,13 +976,9 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     }
     // 3. statistics
     {
-        NQS_LAUNCH("energy_stats");
-        k_energy_stats<<<1, 1024, 0, st>>>(w.E.p, Ns, w.scal.p, w.eps.p);
-    }
-    {
         const int chains = in.sampler ? nqs_sampler_num_chains((nqs_sampler_t *)in.sampler) : 0;
-        NQS_LAUNCH("ess");
-        k_ess<<<1, 256, 0, st>>>(w.eps.p, Ns, chains, w.scal.p);
+        if (!ensure_energy_scratch(w.es, Ns) || !enqueue_energy_stats(w.E.p, Ns, chains, w.scal.p, w.eps.p, w.es.p))
+            return -1;
     }
     NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
     dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
@@ -997,20 +1133,15 @@ int nqs_gpu_ess(const double *energies, int num_samples, int num_chains, double 
     }
     if (!ensure_context()) return -1;
     cudaStream_t st = ctx().stream;
-    static DevBuf<double> dE, deps, dscal;
-    if (!dE.ensure(num_samples) || !deps.ensure(num_samples) || !dscal.ensure(16)) return -1;
+    static DevBuf<double> dE, deps, dscal, des;
+    if (!dE.ensure(num_samples) || !deps.ensure(num_samples) || !dscal.ensure(16) ||
+        !ensure_energy_scratch(des, num_samples))
+        return -1;
     double hs[16];
     if (!NQS_CUDA(cudaMemcpyAsync(dE.p, energies, sizeof(double) * num_samples, cudaMemcpyHostToDevice, st)))
         return -1;
-    {
-        NQS_LAUNCH("energy_stats");
-        k_energy_stats<<<1, 1024, 0, st>>>(dE.p, num_samples, dscal.p, deps.p);
-    }
-    {
-        NQS_LAUNCH("ess");
-        k_ess<<<1, 256, 0, st>>>(deps.p, num_samples, num_chains, dscal.p);
-    }
-    if (!NQS_CUDA(cudaGetLastError()) ||
+    if (!enqueue_energy_stats(dE.p, num_samples, num_chains, dscal.p, deps.p, des.p) ||
+        !NQS_CUDA(cudaGetLastError()) ||
         !NQS_CUDA(cudaMemcpyAsync(hs, dscal.p, sizeof(hs), cudaMemcpyDeviceToHost, st)) ||
         !NQS_CUDA(cudaStreamSynchronize(st)))
         return -1;

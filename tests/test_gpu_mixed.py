@@ -77,9 +77,9 @@ def minsr_mixed(nqs, sweeps, check=0, space=0, Ns=4096):
 
 
 # (N_s, space, sweeps): 4096 > N_p = 1120 picks parameter space, 512 < N_p picks
-# samples.  The N_p x N_p system keeps the small-eigenvalue directions that the
-# sample-space update projects out through O_c^T, so its refinement contracts
-# ~7x per sweep here against ~200x in sample space and needs more sweeps.
+# samples; sweeps = maximum CG iterations.  The N_p x N_p system keeps the
+# small-eigenvalue directions that the sample-space update projects out through
+# O_c^T, so it converges more slowly and gets more iterations.
 @pytest.mark.parametrize("Ns,space,sweeps", [(4096, 0, 8), (4096, 1, 3), (512, 0, 3), (512, 2, 3)])
 def test_mixed_minsr_against_fp64_oracle(nqs, Ns, space, sweeps):
     info, E, delta, stats, Eo, do, io = minsr_mixed(nqs, sweeps=sweeps, check=1, space=space, Ns=Ns)
@@ -93,7 +93,7 @@ def test_mixed_minsr_against_fp64_oracle(nqs, Ns, space, sweeps):
 
 @pytest.mark.parametrize("space", [1, 2])
 def test_refinement_contracts(nqs, space):
-    """More sweeps, smaller residual: the refinement converges."""
+    """More CG iterations, smaller residual: the preconditioned CG converges."""
     r = [minsr_mixed(nqs, sweeps=s, space=space)[3].refine_residual for s in (0, 1, 2)]
     assert r[1] < r[0] and r[2] < r[1]
 
