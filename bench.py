@@ -453,6 +453,123 @@ def multi_instance(nqs, abi, L, base_opts, timed, total):
     return out
 
 
+def timed_steps(nqs, L, step, warm, steps):
+    """Run `warm` untimed then `steps` timed calls of step(); device ms per step
+    (CUDA events on the library stream) and the last step's info."""
+    info = None
+    for _ in range(warm):
+        info = step()
+    e0 = L.nqs_gpu_event_record()
+    for _ in range(steps):
+        info = step()
+    e1 = L.nqs_gpu_event_record()
+    ms = L.nqs_gpu_event_elapsed_ms(e0, e1) / max(steps, 1)
+    L.nqs_gpu_event_destroy(e0)
+    L.nqs_gpu_event_destroy(e1)
+    return ms, info
+
+
+def other_configs(nqs, abi, L, base_opts, which):
+    """The other workloads of the measurement table, each on its own shapes
+    (seeded synthetic parameters, configurations from the sampler):
+      cfg1  1-D TFIM N = 16 PBC, h = 1, real RBM alpha = 1 (N_p = 288), 16 chains x 64 = 1024
+            samples, single flips, 2N sweeps thermalisation, CG-SR shift 1e-3, lr 0.01, all FP64,
+            200 steps; |E/N - E0/N| against the oracle's Lanczos energy;
+      cfg3  J1-J2 6x6 PBC, J2 = 0.5, complex RBM alpha = 4 (N_p = 10728), N(0, 0.005^2),
+            1024 chains x 8 = 8192 samples, exchange moves in Sz = 0, MinSR shift 1e-4, lr 0.005
+            (the 2-D workload's values), mixed precision; the solve runs in sample space
+            (8192 x 8192); delta-theta and energy errors against the FP64 step on the same samples,
+            and the FP64 path's own steps/s;
+      cfg4  kagome 3x3 PBC (N = 27) Heisenberg, Sz = 1/2, MLP 27-108-108-(Re, Im) tanh (Xavier,
+            N_p = 15014), 1024 chains x 16 = 16384 samples, exchange moves on the kagome bonds,
+            MinSR shift 1e-3, lr 0.005, mixed precision (FP64 estimator: the MLP has no FP32
+            product form); a few timed steps; the recorded upstream ground-state energy
+            (tests/golden/kagome_3x3_e0.json) for reference."""
+    import numpy as np
+    out = {}
+    if "1" in which:
+        nqs.set_options(**dict(base_opts, precision=abi.PREC_FP64, fp32_estimator=0))
+        N = 16
+        cfg = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=N, hamiltonian=abi.HAM_TFIM,
+                                  j_coupling=1.0, transverse_field=1.0, rng_seed=SEED + 11, num_samples=1024,
+                                  num_thermalize=2 * N * N, num_decorrelate=N, sr_diag_shift=1e-3,
+                                  learning_rate=0.01, sr_cg_max_iters=100, sr_cg_tol=1e-6)
+        a = nqs.Ansatz(cfg, N)
+        a.params[:] = init_params(a.P, SEED + 11)
+        o = nqs.options(num_chains=16, rng=abi.RNG_PHILOX, move=abi.MOVE_SINGLE_FLIP, lattice_x=N, lattice_y=1,
+                        square_pbc=1, precision=abi.PREC_FP64)
+        s = nqs.Sampler(N, cfg, a.log_amp_fn, a.user, o)
+        s.thermalize()
+        es = []
+
+        def step1():
+            info = nqs.sr_step_cg(cfg, N, 1, a, s, a.log_amp_fn, a.user)
+            es.append(info.mean_energy)
+            return info
+        ms, info = timed_steps(nqs, L, step1, 3, 197)
+        with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
+            e0 = json.load(f)["tfim_chain16_pbc_h1"]["E0_per_site"]
+        run = float(np.mean(es[-20:])) / N
+        out["cfg1_tfim16_cgsr_fp64"] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "steps": 200,
+                                        "cg_iterations_last": info.cg_iterations,
+                                        "energy_per_site_last20": run, "e0_per_site": e0,
+                                        "abs_err_per_site": abs(run - e0)}
+    if "3" in which:
+        nqs.set_options(**base_opts)
+        Lx = Ly = 6
+        N, M = 36, 144
+        cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, hamiltonian=abi.HAM_J1_J2,
+                                  j_coupling=1.0, j2_coupling=0.5, rng_seed=SEED + 33, num_samples=8192,
+                                  num_thermalize=4 * N, num_decorrelate=N, sr_diag_shift=1e-4, learning_rate=0.005)
+        a = nqs.Ansatz(cfg, N)
+        a.params[:] = np.random.default_rng(SEED + 33).normal(0.0, 0.005, size=a.P)
+        o = nqs.options(num_chains=1024, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=N // 2,
+                        lattice_x=Lx, lattice_y=Ly, square_pbc=1, precision=abi.PREC_MIXED, fp32_estimator=1)
+        s = nqs.Sampler(N, cfg, a.log_amp_fn, a.user, o)
+        s.thermalize()
+        step3 = lambda: nqs.sr_step_minsr(cfg, Lx, Ly, a, s, a.log_amp_fn, a.user)
+        ms, info = timed_steps(nqs, L, step3, 2, 10)
+        ph = list(nqs.last_step_stats().phase_us)
+        nqs.set_options(**dict(base_opts, mixed_check=1))
+        step3()
+        st = nqs.last_step_stats()
+        nqs.set_options(**dict(base_opts, precision=abi.PREC_FP64, fp32_estimator=0))
+        s64 = nqs.Sampler(N, cfg, a.log_amp_fn, a.user,
+                          nqs.options(num_chains=1024, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=N // 2,
+                                      lattice_x=Lx, lattice_y=Ly, square_pbc=1, precision=abi.PREC_FP64))
+        s64.thermalize()
+        ms64, _ = timed_steps(nqs, L, lambda: nqs.sr_step_minsr(cfg, Lx, Ly, a, s64, a.log_amp_fn, a.user), 1, 2)
+        out["cfg3_j1j2_6x6_crbm_alpha4_ns8192"] = {
+            "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "solve_space": "samples (N_s = 8192 < N_p = 10728)",
+            "num_params": a.P, "delta_theta_rel_err_vs_fp64": st.delta_rel_err, "energy_rel_err": st.energy_rel_err,
+            "cg_residual": st.refine_residual, "cg_iterations": st.refine_sweeps,
+            "factor_solve_phases_us": [round(x, 1) for x in ph],
+            "plain_fp64_steps_per_s": 1000.0 / ms64, "speedup_vs_fp64": ms64 / ms}
+    if "4" in which:
+        nqs.set_options(**dict(base_opts, fp32_estimator=0))
+        N, W = 27, 108
+        cfg = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=W, depth=2, hamiltonian=abi.HAM_KAGOME_HEISENBERG,
+                                  kagome_pbc=1, j_coupling=1.0, rng_seed=SEED + 44, num_samples=16384,
+                                  num_thermalize=4 * N, num_decorrelate=N, sr_diag_shift=1e-3, learning_rate=0.005)
+        a = nqs.Ansatz(cfg, N)
+        o = nqs.options(num_chains=1024, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=13, lattice_x=3,
+                        lattice_y=3, lattice_kagome=1, precision=abi.PREC_MIXED, fp32_estimator=0)
+        s = nqs.Sampler(N, cfg, a.log_amp_fn, a.user, o)
+        s.thermalize()
+        step4 = lambda: nqs.sr_step_minsr(cfg, 3, 3, a, s, a.log_amp_fn, a.user)
+        ms, info = timed_steps(nqs, L, step4, 1, 3)
+        ph = list(nqs.last_step_stats().phase_us)
+        with open(os.path.join(ROOT, "tests", "golden", "kagome_3x3_e0.json")) as f:
+            e0 = json.load(f)["kagome_3x3_pbc_heisenberg"]["E0_per_site"]
+        out["cfg4_kagome3x3_mlp108_ns16384"] = {
+            "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "num_params": a.P,
+            "solve_space": "parameters (N_p = 15014 < N_s = 16384)", "energy_per_site_last": info.mean_energy / N,
+            "e0_per_site_recorded_upstream": e0, "factor_solve_phases_us": [round(x, 1) for x in ph],
+            "estimator": "FP64 generic (MLP)", "sampler": "FP64 generic chains"}
+    nqs.set_options(**base_opts)
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -596,6 +713,10 @@ def run_gpu(args):
                      for d in (DECOR, 2) for lr in (False, True)]
         nqs.set_options(**base_opts)
 
+    others = None
+    if prec == abi.PREC_MIXED and args.configs:
+        others = other_configs(nqs, abi, L, base_opts, args.configs)
+
     multi = None
     if prec == abi.PREC_MIXED and args.batch_steps > 0:
         multi = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps)
@@ -628,7 +749,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": 8 * P + 16 * 8},
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
             "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
-            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi,
+            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi, "other_configs": others,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
@@ -689,6 +810,8 @@ def main():
     ap.add_argument("--converge-steps", type=int, default=1000,
                     help="max optimisation steps of the |dE/N| <= 1e-4 vs Lanczos run (0 = skip)")
     ap.add_argument("--converge-fp64", action="store_true", help="also run the FP64 path to the target")
+    ap.add_argument("--configs", default="134",
+                    help="which of the other workloads to run (digits of 1, 3, 4; empty = none)")
     ap.add_argument("--batch-steps", type=int, default=300,
                     help="steps of the 64-instance batch run (0 = skip)")
     ap.add_argument("--proposal-steps", type=int, default=20,
