@@ -324,7 +324,10 @@ static bool make_map(CUtensorMap *m, const float *ptr, long rows, long cols_pad)
 // Phases are separated by a grid barrier on a generation word with a bounded
 // spin budget; on timeout it raises *err and every CTA leaves at its next
 // barrier.  Data written by other CTAs is read with L1-bypassing loads.
-constexpr int BT = 128;                              // diagonal block
+constexpr int BT = 128;                              // shared-memory tile of the diagonal block
+constexpr int BD = 64;                               // diagonal block width (<= BT, multiple of 32)
+constexpr int NSUB = BD / 32;                        // 32-column sub-panels per diagonal block
+static_assert(BD % 64 == 0 && BD <= BT, "the diagonal block is a multiple of the 64-wide GEMM tile");
 constexpr int PS_THREADS = 256;
 constexpr int PS_SMEM = 2 * BT * (BT + 1) * 4;       // two 128 x 129 float tiles
 constexpr int GT = 64, GKC = 32;                     // GEMM tile and K chunk
@@ -342,6 +345,7 @@ __device__ __forceinline__ unsigned long long gtimer() {
 }
 
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned count) {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = bar + 1;
@@ -363,9 +367,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
             }
         }
         __threadfence();
+        s_ok = *((volatile int *)err) == 0;
     }
     __syncthreads();
-    return *((volatile int *)err) == 0;
+    return s_ok != 0;                                 // one answer for the whole CTA
 }
 
 // Factor the 128 x 128 block in S (rows >= bs padded with the identity) in four
@@ -375,8 +380,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
 // rest of the block use the whole CTA.  Returns the first failing column or -1.
 __device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s_flag, float *tmp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int e = tid; e < BT * BT; e += PS_THREADS) X[e / BT][e % BT] = 0.f;
-    for (int sb = 0; sb < 4; sb++) {
+    for (int e = tid; e < BD * BD; e += PS_THREADS) X[e / BD][e % BD] = 0.f;
+    for (int sb = 0; sb < NSUB; sb++) {
         const int c0 = sb * 32;
         if (warp == 0) {
             // right-looking, lane = row in registers; the scaled column j is
@@ -430,7 +435,7 @@ __device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int
         }
         __syncthreads();
         if (*s_flag >= 0) return *s_flag;
-        const int t0 = c0 + 32, nr = BT - t0;
+        const int t0 = c0 + 32, nr = BD - t0;
         if (nr == 0) break;
         // rows below the sub-panel: L[r][c0+j] = sum_m A[r][c0+m] X_s[j][m]
         for (int w = tid; w < nr * 8; w += PS_THREADS) {
@@ -494,8 +499,8 @@ __device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int
 // 4 x 4 outputs per thread (rows and columns strided by 8).
 __device__ void block_inv128(float (*S)[BT + 1], float (*X)[BT + 1], float *tmp) {
     const int tid = threadIdx.x, r8 = (tid >> 3) & 7, c8 = tid & 7;
-    for (int d = 1; d < 4; d++) {
-        const int pairs = 4 - d;
+    for (int d = 1; d < NSUB; d++) {
+        const int pairs = NSUB - d;
         for (int w = tid; w < pairs * 64; w += PS_THREADS) {
             const int pa = w >> 6, ob = (pa + d) * 32, oa = pa * 32;
             float acc[4][4] = {};
@@ -773,6 +778,155 @@ __device__ __forceinline__ double dot_all(const double *a, const double *b, int 
     return t;
 }
 
+// ---- tensor-core trailing update.  The panel phase stores U^T split into TF32
+// hi / lo words, K contiguous ([row][BD]); a 128 x 128 tile of the trailing
+// matrix is then C = U_i^T U_j over K = BD in three tcgen05.mma.kind::tf32
+// passes (hi hi, hi lo, lo hi) accumulated in TMEM, with the operands staged by
+// cp.async straight into the 128-byte-swizzle layout (double-buffered 32-wide K
+// chunks) and the tile subtracted through shared memory with coalesced
+// accesses.
+constexpr int TT = 128;                              // trailing tile
+constexpr int TT_CHUNK_BYTES = TT * 32 * 4;          // one operand, one 32-wide K chunk (16 KB)
+constexpr int TT_STAGE_BYTES = 4 * TT_CHUNK_BYTES;   // A hi, A lo, B hi, B lo
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// rows R0 .. R0+127, K columns 32q .. 32q+31 of X ([row][BD]) -> the SW128
+// K-major tile at sbase (1024-byte aligned): row m at m * 128 B, its 16-byte
+// chunk c at chunk position c ^ (m % 8)
+__device__ __forceinline__ void stage_sw128(uint32_t sbase, const float *X, int R0, int q) {
+    for (int e = threadIdx.x; e < TT * 8; e += PS_THREADS) {
+        const int m = e >> 3, c = e & 7;
+        cp_async16(sbase + m * 128 + ((c ^ (m & 7)) << 4), X + (size_t)(R0 + m) * BD + q * 32 + c * 4);
+    }
+}
+
+struct TcState {
+    uint8_t *sm;          // 2 stages of TT_STAGE_BYTES, 1024-byte aligned (also the epilogue tile)
+    uint64_t *mbar;       // [2] MMA completion per stage
+    uint32_t cnt[2];      // commits issued per stage (mbarrier phase tracking)
+    uint32_t tmem;        // 128 TMEM columns (128 x 128 FP32 accumulator)
+    int *err;
+};
+
+// C[i][j] -= (U^T U)[i][j] for the tile rows R0.., columns C0.. (j <= i < n);
+// returns false when a bounded wait gave up (err raised).
+__device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, float *T, int n, int R0, int C0) {
+    constexpr int NQ = BD / 32;
+    const int tid = threadIdx.x;
+    const uint32_t s0 = smem_u32(ts.sm);
+    auto stage = [&](int q, int b) {
+        const uint32_t sb = s0 + b * TT_STAGE_BYTES;
+        stage_sw128(sb, uh, R0, q);
+        stage_sw128(sb + TT_CHUNK_BYTES, ul, R0, q);
+        stage_sw128(sb + 2 * TT_CHUNK_BYTES, uh, C0, q);
+        stage_sw128(sb + 3 * TT_CHUNK_BYTES, ul, C0, q);
+        cp_async_commit();
+    };
+    // M = N = 128, FP32 accumulate, TF32 operands, both K-major
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TT >> 3) << 17) | ((uint32_t)(TT >> 4) << 24);
+    stage(0, 0);
+    for (int q = 0; q < NQ; q++) {
+        const int b = q & 1;
+        cp_async_wait_all();
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t sb = s0 + b * TT_STAGE_BYTES;
+#pragma unroll
+            for (int pass = 0; pass < 3; pass++) {
+                const uint32_t sa = sb + (pass == 2 ? TT_CHUNK_BYTES : 0);                       // A hi, hi, lo
+                const uint32_t sbb = sb + 2 * TT_CHUNK_BYTES + (pass == 1 ? TT_CHUNK_BYTES : 0);  // B hi, lo, hi
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    umma_tf32(ts.tmem, sw128_desc(sa + k * 32), sw128_desc(sbb + k * 32), idesc,
+                              (q | pass | k) ? 1u : 0u);
+            }
+            umma_commit(&ts.mbar[b]);
+        }
+        ts.cnt[b]++;
+        if (q + 1 < NQ) {
+            const int nb = (q + 1) & 1;
+            // the stage being refilled was read by the MMAs of chunk q - 1
+            if (q >= 1 && !__syncthreads_and(mbar_wait(&ts.mbar[nb], (ts.cnt[nb] - 1) & 1, ts.err))) return false;
+            stage(q + 1, nb);
+        }
+    }
+    const int lb = (NQ - 1) & 1;
+    bool done = mbar_wait(&ts.mbar[lb], (ts.cnt[lb] - 1) & 1, ts.err);
+    if (NQ > 1) done = done && mbar_wait(&ts.mbar[lb ^ 1], (ts.cnt[lb ^ 1] - 1) & 1, ts.err);
+    if (!__syncthreads_and(done)) return false;             // uniform over the CTA
+    tc_fence_after();
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .., columns 64 (w / 4) .. + 63
+    // into a shared tile of pitch EP (16-byte rows: conflict-free 128-bit
+    // accesses), then the tile is subtracted from T with coalesced accesses
+    constexpr int EP = TT + 4;
+    float *ep = (float *)ts.sm;
+    {
+        const int warp = tid >> 5, lane = tid & 31, row = 32 * (warp & 3) + lane;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int col = 64 * (warp >> 2) + 32 * h;
+            float v[32];
+            tmem_ld32(ts.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)col, v);
+#pragma unroll
+            for (int j = 0; j < 32; j += 4)
+                *(float4 *)&ep[row * EP + col + j] = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if ((n & 3) == 0) {
+        // 16 float4 per thread, all loads before the stores
+        float4 v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int e4 = tid + q * PS_THREADS, i = R0 + (e4 >> 5), j = C0 + 4 * (e4 & 31);
+            v[q] = (i < n && j <= i) ? __ldcg((const float4 *)&T[(size_t)i * n + j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int e4 = tid + q * PS_THREADS, r = e4 >> 5, c = 4 * (e4 & 31), i = R0 + r, j = C0 + c;
+            if (i < n && j <= i) {
+                const float4 d = *(const float4 *)&ep[r * EP + c];
+                float4 o = make_float4(v[q].x - d.x, v[q].y - d.y, v[q].z - d.z, v[q].w - d.w);
+                if (j + 3 <= i) {
+                    *(float4 *)&T[(size_t)i * n + j] = o;
+                } else {                                    // the diagonal crosses this group
+                    float *t = &T[(size_t)i * n + j];
+                    t[0] = o.x;
+                    if (j + 1 <= i) t[1] = o.y;
+                    if (j + 2 <= i) t[2] = o.z;
+                }
+            }
+        }
+    } else {
+        // 32 independent loads in flight per thread before the stores (a load after
+        // a store to the same array is not hoisted)
+        for (int e0 = tid; e0 < TT * TT; e0 += 32 * PS_THREADS) {
+            float v[32];
+#pragma unroll
+            for (int q = 0; q < 32; q++) {
+                const int e = e0 + q * PS_THREADS, i = R0 + e / TT, j = C0 + e % TT;
+                v[q] = (i < n && j <= i) ? __ldcg(&T[(size_t)i * n + j]) : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 32; q++) {
+                const int e = e0 + q * PS_THREADS, i = R0 + e / TT, j = C0 + e % TT;
+                if (i < n && j <= i) T[(size_t)i * n + j] = v[q] - ep[(e / TT) * EP + e % TT];
+            }
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
 // Relative residual |r| / |rhs| at which the CG refinement stops.
 constexpr double CG_RTOL = 1e-10;
 
@@ -792,6 +946,7 @@ struct FrArgs {
     double *u, *upart;  // intermediate vector, partial column sums
     double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
+    float *uh, *ul;     // [round_up(n, 128)][BD] TF32 hi / lo words of the current panel U^T (K contiguous; pad rows zero)
     double *nrm;        // [3] |r|^2, |rhs|^2, CG iterations run
     int sweeps;         // maximum CG iterations
     int *status;        // [0] first failing column or -1
@@ -803,7 +958,7 @@ struct FrArgs {
 // The solve of one system by the CTAs bx = 0 .. G-1 of a cooperative launch
 // (all co-resident): the whole grid for a single system, a slice of it when a
 // batch of systems shares one launch.
-__device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int G) {
+__device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int G, TcState &ts) {
     extern __shared__ float psm[];
     float (*S0)[BT + 1] = (float (*)[BT + 1])psm;
     float (*S1)[BT + 1] = (float (*)[BT + 1])(psm + BT * (BT + 1));
@@ -813,7 +968,7 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     const int lane = tid & 31, tx = tid & 15, ty = tid >> 4;
     const int gtid = bx * PS_THREADS + tid, gthreads = G * PS_THREADS;
     const int gwarp = bx * (PS_THREADS / 32) + (tid >> 5), gwarps = G * (PS_THREADS / 32);
-    const int nb = (n + BT - 1) / BT;
+    const int nb = (n + BD - 1) / BD;
     __shared__ int s_flag;
     __shared__ float tmpb[3 * 1024];
     unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -830,20 +985,20 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     // Diagonal block kb: its owner CTA loads it, factors and inverts it in
     // shared memory and stores X_kk in Li / LiT (a breakdown goes to status[0]).
     auto factor_diag = [&](int kb) {
-        const int k0 = kb * BT, bs = min(BT, n - k0);
+        const int k0 = kb * BD, bs = min(BD, n - k0);
         const unsigned long long t_own = tid == 0 ? gtimer() : 0;
-        for (int e0 = 0; e0 < BT * BT; e0 += 8 * PS_THREADS) {
+        for (int e0 = 0; e0 < BD * BD; e0 += 8 * PS_THREADS) {
             float v[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                const int e = e0 + tid + q * PS_THREADS, rr = e / BT, cc = e % BT;
-                const bool in = rr < bs && cc <= rr;
+                const int e = e0 + tid + q * PS_THREADS, rr = e / BD, cc = e % BD;
+                const bool in = e < BD * BD && rr < bs && cc <= rr;
                 v[q] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) : (rr == cc ? 1.f : 0.f);
             }
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const int e = e0 + tid + q * PS_THREADS;
-                S0[e / BT][e % BT] = v[q];
+                if (e < BD * BD) S0[e / BD][e % BD] = v[q];
             }
         }
         __syncthreads();
@@ -855,8 +1010,8 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
             }
         } else {
             block_inv128(S0, S1, tmpb);
-            for (int e = tid; e < BT * BT; e += PS_THREADS) {
-                const int rr = e >> 7, q = e & (BT - 1);
+            for (int e = tid; e < BD * BD; e += PS_THREADS) {
+                const int rr = e / BD, q = e % BD;
                 if (rr < bs && q < bs) {
                     a.Li[(size_t)(k0 + rr) * ldl + k0 + q] = S1[rr][q];
                     a.LiT[(size_t)(k0 + rr) * ldl + k0 + q] = S1[q][rr];
@@ -866,28 +1021,8 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         __syncthreads();                                    // S0 / S1 are reused as GEMM staging
         if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
     };
-    // one 64 x 64 tile t (lower-triangular order) of the trailing update of
-    // block kb: A[i][j] -= sum_m U[k0 + m][i] U[k0 + m][j], k1 <= j <= i
-    auto trailing_tile = [&](int k0, int bs, int k1, int t) {
-        int bi, bj;
-        tri_tile(t, bi, bj);
-        const int r0 = k1 + bi * GT, c0 = k1 + bj * GT;
-        float acc[4][4] = {};
-        const float *U = a.T + (size_t)k0 * n;
-        gemm64<true, true>(acc, U, n, r0, n, U, n, c0, n, 0, bs, TS);
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-#pragma unroll
-            for (int v = 0; v < 4; v++) {
-                const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
-                if (i < n && j <= i) {
-                    const size_t idx = (size_t)i * n + j;
-                    a.T[idx] = __ldcg(&a.T[idx]) - acc[u][v];
-                }
-            }
-    };
     for (int kb = 0; kb < nb; kb++) {
-        const int k0 = kb * BT, bs = min(BT, n - k0), k1 = k0 + bs, rest = n - k1;
+        const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
         if (bx == kb % G) factor_diag(kb);
         if (!grid_barrier(a.bar, a.err, G)) return;
         if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
@@ -895,9 +1030,10 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         if (rest <= 0) break;
         // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1
         {
+            constexpr int NCT = (BD + GT - 1) / GT;          // column tiles of the panel
             const int ntr = (rest + GT - 1) / GT;
-            for (int t = bx; t < 2 * ntr; t += G) {
-                const int c0 = (t & 1) * GT, r0 = k1 + (t >> 1) * GT;
+            for (int t = bx; t < NCT * ntr; t += G) {
+                const int c0 = (t % NCT) * GT, r0 = k1 + (t / NCT) * GT;
                 if (c0 >= bs) continue;
                 float acc[4][4] = {};
                 gemm64<false, false>(acc, a.Li + (size_t)k0 * ldl + k0, ldl, c0, bs, a.T + k0, n, r0, n, 0,
@@ -908,7 +1044,19 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
                     for (int v = 0; v < 4; v++) {
                         const int c = c0 + ty + 16 * u, r = r0 + tx + 16 * v;
                         if (c < bs && r < n) a.T[(size_t)(k0 + c) * n + r] = acc[u][v];
+                        ST[ty + 16 * u][tx + 16 * v] = acc[u][v];
                     }
+                __syncthreads();
+                // U^T split into TF32 hi / lo, rows r (K = panel column contiguous)
+                for (int e = tid; e < GT * GT; e += PS_THREADS) {
+                    const int rr = e / GT, cc = e % GT, r = r0 + rr, c = c0 + cc;
+                    if (c < bs && r < n) {
+                        const float x = ST[cc][rr], h = tf32_rna(x);
+                        a.uh[(size_t)r * BD + c] = h;
+                        a.ul[(size_t)r * BD + c] = tf32_rna(x - h);
+                    }
+                }
+                __syncthreads();
             }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
@@ -917,8 +1065,12 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         // CTA updating that block's three 64 x 64 tiles alone costs more than
         // the trailing phase it hides)
         {
-            const int ntt = (rest + GT - 1) / GT, ntiles = ntt * (ntt + 1) / 2;
-            for (int t = bx; t < ntiles; t += G) trailing_tile(k0, bs, k1, t);
+            const int ntt = (rest + TT - 1) / TT, ntiles = ntt * (ntt + 1) / 2;
+            for (int t = bx; t < ntiles; t += G) {
+                int bi, bj;
+                tri_tile(t, bi, bj);
+                if (!trailing_tile_tc(ts, a.uh, a.ul, a.T, n, k1 + bi * TT, k1 + bj * TT)) return;
+            }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(2);
@@ -926,11 +1078,12 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
 
     // ---------------- L^{-1}: join halves of h blocks, h = 1, 2, 4, ...
     for (int h = 1; h < nb; h *= 2) {
-        const int span = 2 * h * BT, ngrp = (n + span - 1) / span, per = 4 * h * h;
+        // hb 64-tiles per half; a group's W / X21 have hb x hb tiles
+        const int span = 2 * h * BD, ngrp = (n + span - 1) / span, hb = h * BD / GT, per = hb * hb;
         // W = L21 X11 (into the dead lower triangle of T)
         for (int t = bx; t < ngrp * per; t += G) {
-            const int g = t / per, rt = (t % per) / (2 * h), ct = t % (2 * h);
-            const int a0 = g * span, a1 = a0 + h * BT, a2 = min(n, a0 + span);
+            const int g = t / per, rt = (t % per) / hb, ct = t % hb;
+            const int a0 = g * span, a1 = a0 + h * BD, a2 = min(n, a0 + span);
             const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
             if (a1 >= a2 || r0 >= a2) continue;
             float acc[4][4] = {};
@@ -946,8 +1099,8 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         if (!grid_barrier(a.bar, a.err, G)) return;
         // X21 = -X22 W
         for (int t = bx; t < ngrp * per; t += G) {
-            const int g = t / per, rt = (t % per) / (2 * h), ct = t % (2 * h);
-            const int a0 = g * span, a1 = a0 + h * BT, a2 = min(n, a0 + span);
+            const int g = t / per, rt = (t % per) / hb, ct = t % hb;
+            const int a0 = g * span, a1 = a0 + h * BD, a2 = min(n, a0 + span);
             const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
             if (a1 >= a2 || r0 >= a2) continue;
             float acc[4][4] = {};
@@ -1096,7 +1249,47 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
 #undef NQS_PHASE
 }
 
-__global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) { fr_body(a, blockIdx.x, gridDim.x); }
+// Per-CTA setup of the tensor-core state: two mbarriers, 128 TMEM columns
+// (released again after the body, whichever way it returned).
+__device__ __forceinline__ void tc_setup(TcState &ts, uint64_t *mbar, uint32_t *slot, int *err) {
+    extern __shared__ float psm[];
+    const uint32_t base = smem_u32(psm);
+    ts.sm = (uint8_t *)psm + (((base + 1023u) & ~1023u) - base);
+    ts.mbar = mbar;
+    ts.cnt[0] = ts.cnt[1] = 0;
+    ts.err = err;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(TT)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    ts.tmem = *slot;
+}
+
+__device__ __forceinline__ void tc_teardown(const TcState &ts) {
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(ts.tmem), "r"(TT) : "memory");
+}
+
+__global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t slot;
+    TcState ts;
+    tc_setup(ts, mbar, &slot, a.err);
+    fr_body(a, blockIdx.x, gridDim.x, ts);
+    tc_teardown(ts);
+}
 
 // A batch of independent systems in one cooperative launch: system i owns the
 // CTAs [cta0[i], cta0[i] + nctas[i]) and has its own barrier, status and error
@@ -1107,12 +1300,17 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrA
                                                                        const int *__restrict__ nctas) {
     const int i = cta_sys[blockIdx.x];
     const FrArgs a = sys[i];
-    fr_body(a, blockIdx.x - cta0[i], nctas[i]);
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t slot;
+    TcState ts;
+    tc_setup(ts, mbar, &slot, a.err);
+    fr_body(a, blockIdx.x - cta0[i], nctas[i], ts);
+    tc_teardown(ts);
 }
 
 // ---------------------------------------------------------------- driver
 struct MixedWs {
-    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf;
+    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf, uh, ul;
     DevBuf<double> rhs, r, u, upart, nrm, p, q, z;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -1241,6 +1439,8 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     fa.q = w.q.p;
     fa.z = w.z.p;
     fa.rf = w.rf.p;
+    fa.uh = w.uh.p;
+    fa.ul = w.ul.p;
     fa.zf = w.zf.p;
     fa.nrm = w.nrm.p;
     fa.sweeps = sweeps;
@@ -1297,22 +1497,27 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         *moved = true;
     }
     const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[16] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p};
+    const void *before[18] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p};
     const int ldl = (n + 31) / 32 * 32;
+    // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero
+    const size_t nu = (size_t)(n + TT) * BD;
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
-        !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) ||
+        !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
         !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(3) || !w.status.ensure(2) ||
         !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
-    const void *after[16] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p};
-    for (int i = 0; i < 16; i++) *moved |= before[i] != after[i];
+    const void *after[18] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p};
+    for (int i = 0; i < 18; i++) *moved |= before[i] != after[i];
     if (*moved || w.n != n) {
-        // the pad columns of L^{-1} are read (as zeros) by the vectorised solves
+        // the pad columns of L^{-1} are read (as zeros) by the vectorised solves,
+        // the pad rows of the split U^T by the tensor-core trailing tiles
         if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
-            !NQS_CUDA(cudaMemsetAsync(w.LiT.p, 0, sizeof(float) * (size_t)n * ldl, st)))
+            !NQS_CUDA(cudaMemsetAsync(w.LiT.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.uh.p, 0, sizeof(float) * w.uh.n, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.ul.p, 0, sizeof(float) * w.ul.n, st)))
             return false;
         w.n = n;
         *moved = true;
