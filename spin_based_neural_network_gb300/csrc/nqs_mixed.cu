@@ -325,9 +325,11 @@ static bool make_map(CUtensorMap *m, const float *ptr, long rows, long cols_pad)
 // spin budget; on timeout it raises *err and every CTA leaves at its next
 // barrier.  Data written by other CTAs is read with L1-bypassing loads.
 constexpr int BT = 128;                              // shared-memory tile of the diagonal block
-constexpr int BD = 64;                               // diagonal block width (<= BT, multiple of 32)
-constexpr int NSUB = BD / 32;                        // 32-column sub-panels per diagonal block
-static_assert(BD % 64 == 0 && BD <= BT, "the diagonal block is a multiple of the 64-wide GEMM tile");
+// Diagonal block width BD (a template parameter of the factor; chosen per
+// system): 64 below BD_SWITCH, where the sequential chain of diagonal blocks
+// dominates, 128 above, where wider tensor-core K and half the block steps pay.
+constexpr int BD_SMALL = 64, BD_LARGE = 128, BD_SWITCH = 4096;
+static_assert(BD_SMALL % 64 == 0 && BD_LARGE <= BT, "diagonal blocks are multiples of the 64-wide GEMM tile");
 constexpr int PS_THREADS = 256;
 constexpr int PS_SMEM = 2 * BT * (BT + 1) * 4;       // two 128 x 129 float tiles
 constexpr int GT = 64, GKC = 32;                     // GEMM tile and K chunk
@@ -378,7 +380,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
 // factors in the matching diagonal blocks of X.  The 32 x 32 factor and its
 // inverse run in one warp's registers; the panel below it and the update of the
 // rest of the block use the whole CTA.  Returns the first failing column or -1.
-__device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s_flag, float *tmp) {
+template <int BD>
+__device__ int block_chol(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s_flag, float *tmp) {
+    constexpr int NSUB = BD / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int e = tid; e < BD * BD; e += PS_THREADS) X[e / BD][e % BD] = 0.f;
     for (int sb = 0; sb < NSUB; sb++) {
@@ -497,7 +501,9 @@ __device__ int block_chol128(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int
 // 32-blocks are already in X): for d = 1..3, X_ba = -X_bb (sum_{m=a}^{b-1}
 // L_bm X_ma), b = a + d, all pairs of one block diagonal computed by the CTA,
 // 4 x 4 outputs per thread (rows and columns strided by 8).
-__device__ void block_inv128(float (*S)[BT + 1], float (*X)[BT + 1], float *tmp) {
+template <int BD>
+__device__ void block_inv(float (*S)[BT + 1], float (*X)[BT + 1], float *tmp) {
+    constexpr int NSUB = BD / 32;
     const int tid = threadIdx.x, r8 = (tid >> 3) & 7, c8 = tid & 7;
     for (int d = 1; d < NSUB; d++) {
         const int pairs = NSUB - d;
@@ -799,6 +805,7 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // rows R0 .. R0+127, K columns 32q .. 32q+31 of X ([row][BD]) -> the SW128
 // K-major tile at sbase (1024-byte aligned): row m at m * 128 B, its 16-byte
 // chunk c at chunk position c ^ (m % 8)
+template <int BD>
 __device__ __forceinline__ void stage_sw128(uint32_t sbase, const float *X, int R0, int q) {
     for (int e = threadIdx.x; e < TT * 8; e += PS_THREADS) {
         const int m = e >> 3, c = e & 7;
@@ -816,16 +823,17 @@ struct TcState {
 
 // C[i][j] -= (U^T U)[i][j] for the tile rows R0.., columns C0.. (j <= i < n);
 // returns false when a bounded wait gave up (err raised).
+template <int BD>
 __device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, float *T, int n, int R0, int C0) {
     constexpr int NQ = BD / 32;
     const int tid = threadIdx.x;
     const uint32_t s0 = smem_u32(ts.sm);
     auto stage = [&](int q, int b) {
         const uint32_t sb = s0 + b * TT_STAGE_BYTES;
-        stage_sw128(sb, uh, R0, q);
-        stage_sw128(sb + TT_CHUNK_BYTES, ul, R0, q);
-        stage_sw128(sb + 2 * TT_CHUNK_BYTES, uh, C0, q);
-        stage_sw128(sb + 3 * TT_CHUNK_BYTES, ul, C0, q);
+        stage_sw128<BD>(sb, uh, R0, q);
+        stage_sw128<BD>(sb + TT_CHUNK_BYTES, ul, R0, q);
+        stage_sw128<BD>(sb + 2 * TT_CHUNK_BYTES, uh, C0, q);
+        stage_sw128<BD>(sb + 3 * TT_CHUNK_BYTES, ul, C0, q);
         cp_async_commit();
     };
     // M = N = 128, FP32 accumulate, TF32 operands, both K-major
@@ -927,6 +935,10 @@ __device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, 
     return true;
 }
 
+// Order from which the preconditioner is applied by blocked substitution
+// instead of through an explicit L^{-1}.
+constexpr int BLOCKED_SOLVE_MIN = 4608;
+
 // Relative residual |r| / |rhs| at which the CG refinement stops.
 constexpr double CG_RTOL = 1e-10;
 
@@ -946,7 +958,8 @@ struct FrArgs {
     double *u, *upart;  // intermediate vector, partial column sums
     double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
-    float *uh, *ul;     // [round_up(n, 128)][BD] TF32 hi / lo words of the current panel U^T (K contiguous; pad rows zero)
+    float *uh, *ul;     // [n + 128][bd] TF32 hi / lo words of the current panel U^T (K contiguous; pad rows zero)
+    int bd;             // diagonal block width (BD_SMALL or BD_LARGE)
     double *nrm;        // [3] |r|^2, |rhs|^2, CG iterations run
     int sweeps;         // maximum CG iterations
     int *status;        // [0] first failing column or -1
@@ -958,6 +971,7 @@ struct FrArgs {
 // The solve of one system by the CTAs bx = 0 .. G-1 of a cooperative launch
 // (all co-resident): the whole grid for a single system, a slice of it when a
 // batch of systems shares one launch.
+template <int BD>
 __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int G, TcState &ts) {
     extern __shared__ float psm[];
     float (*S0)[BT + 1] = (float (*)[BT + 1])psm;
@@ -1002,14 +1016,14 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
             }
         }
         __syncthreads();
-        const int f = block_chol128(S0, S1, bs, &s_flag, tmpb);
+        const int f = block_chol<BD>(S0, S1, bs, &s_flag, tmpb);
         if (f >= 0) {
             if (tid == 0) {
                 a.status[0] = k0 + f;
                 __threadfence();
             }
         } else {
-            block_inv128(S0, S1, tmpb);
+            block_inv<BD>(S0, S1, tmpb);
             for (int e = tid; e < BD * BD; e += PS_THREADS) {
                 const int rr = e / BD, q = e % BD;
                 if (rr < bs && q < bs) {
@@ -1069,15 +1083,20 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
             for (int t = bx; t < ntiles; t += G) {
                 int bi, bj;
                 tri_tile(t, bi, bj);
-                if (!trailing_tile_tc(ts, a.uh, a.ul, a.T, n, k1 + bi * TT, k1 + bj * TT)) return;
+                if (!trailing_tile_tc<BD>(ts, a.uh, a.ul, a.T, n, k1 + bi * TT, k1 + bj * TT)) return;
             }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(2);
     }
 
+    // Large systems skip the explicit L^{-1} (n^3 / 3 flops) and apply the
+    // preconditioner by blocked substitution (one grid barrier per diagonal
+    // block and direction); below BLOCKED_SOLVE_MIN the inverse is cheaper than
+    // those barriers over the CG iterations.
+    const bool blocked = n >= BLOCKED_SOLVE_MIN;
     // ---------------- L^{-1}: join halves of h blocks, h = 1, 2, 4, ...
-    for (int h = 1; h < nb; h *= 2) {
+    for (int h = 1; h < nb && !blocked; h *= 2) {
         // hb 64-tiles per half; a group's W / X21 have hb x hb tiles
         const int span = 2 * h * BD, ngrp = (n + span - 1) / span, hb = h * BD / GT, per = hb * hb;
         // W = L21 X11 (into the dead lower triangle of T)
@@ -1153,7 +1172,94 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     // M^{-1} v with rf = float(v): zf = L^{-1} rf, out = L^{-T} zf (row i of
     // L^{-1} reads the 4-aligned groups up to i; the entries right of the
     // diagonal inside a group are the zeros of the diagonal block).
+    __shared__ float vk[BD], yk[BD];
     auto precond = [&](double *out) -> bool {
+        if (blocked) {
+            const int warp = tid >> 5;
+            constexpr int RL = BD / 32;
+            // yk[t] = sum_c X[t][c] vk[c] over the diagonal block (rows of X at
+            // xb + t * ldl; the zeros of the triangle are read too), a warp
+            // taking 4 rows at a time with all their loads issued first
+            auto diag_gemv = [&](const float *xb, int bs) {
+                for (int c = bs + tid; c < BD; c += PS_THREADS) vk[c] = 0.f;
+                __syncthreads();
+                for (int t0 = 4 * warp; t0 < bs; t0 += 4 * (PS_THREADS / 32)) {
+                    float xv[4][RL];
+#pragma unroll
+                    for (int h = 0; h < 4; h++)
+#pragma unroll
+                        for (int q = 0; q < RL; q++) {
+                            const int t = t0 + h, c = lane + 32 * q;
+                            xv[h][q] = (t < bs && c < bs) ? __ldcg(xb + (size_t)t * ldl + c) : 0.f;
+                        }
+#pragma unroll
+                    for (int h = 0; h < 4; h++) {
+                        float sacc = 0.f;
+#pragma unroll
+                        for (int q = 0; q < RL; q++) sacc = fmaf(xv[h][q], vk[lane + 32 * q], sacc);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+                        if (lane == 0 && t0 + h < bs) yk[t0 + h] = sacc;
+                    }
+                }
+                for (int t = bs + tid; t < BD; t += PS_THREADS) yk[t] = 0.f;   // read (times 0) past a partial block
+                __syncthreads();
+            };
+            // forward, L y = rf (rf is the working vector): y_k = X_kk w_k, then
+            // w_i -= sum_c L[i][k0 + c] y_k[c] = sum_c U[k0 + c][i] y_k[c] below the block
+            for (int kb = 0; kb < nb; kb++) {
+                const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs;
+                for (int c = tid; c < bs; c += PS_THREADS) vk[c] = __ldcg(a.rf + k0 + c);
+                diag_gemv(a.Li + (size_t)k0 * ldl + k0, bs);      // X_kk (lower triangle)
+                if (bx == 0)
+                    for (int c = tid; c < bs; c += PS_THREADS) a.zf[k0 + c] = yk[c];
+                for (int i = k1 + gtid; i < n; i += gthreads) {
+                    // 32 loads in flight per round (coalesced over i)
+                    const float *u = a.T + (size_t)k0 * n + i;
+                    float sacc = 0.f;
+                    for (int c0 = 0; c0 < bs; c0 += 32) {
+                        float uv[32];
+#pragma unroll
+                        for (int q = 0; q < 32; q++) uv[q] = c0 + q < bs ? __ldcg(u + (size_t)(c0 + q) * n) : 0.f;
+#pragma unroll
+                        for (int q = 0; q < 32; q++) sacc = fmaf(uv[q], yk[min(c0 + q, BD - 1)], sacc);
+                    }
+                    a.rf[i] = __ldcg(a.rf + i) - sacc;
+                }
+                if (!grid_barrier(a.bar, a.err, G)) return false;
+            }
+            // backward, L^T z = y (zf is the working vector): z_k = X_kk^T v_k, then
+            // v_i -= sum_r L[k0 + r][i] z_k[r] = sum_r U[i][k0 + r] z_k[r] above the block
+            for (int kb = nb - 1; kb >= 0; kb--) {
+                const int k0 = kb * BD, bs = min(BD, n - k0);
+                for (int c = tid; c < bs; c += PS_THREADS) vk[c] = __ldcg(a.zf + k0 + c);
+                diag_gemv(a.LiT + (size_t)k0 * ldl + k0, bs);     // X_kk^T (upper triangle)
+                if (bx == 0)
+                    for (int c = tid; c < bs; c += PS_THREADS) out[k0 + c] = (double)yk[c];
+                // a warp takes 4 rows at a time, all BD / 32 loads per row issued first
+                for (int i0 = 4 * gwarp; i0 < k0; i0 += 4 * gwarps) {
+                    float uv[4][RL];
+#pragma unroll
+                    for (int h = 0; h < 4; h++)
+#pragma unroll
+                        for (int q = 0; q < RL; q++) {
+                            const int r = lane + 32 * q;
+                            uv[h][q] = (i0 + h < k0 && r < bs) ? __ldcg(a.T + (size_t)(i0 + h) * n + k0 + r) : 0.f;
+                        }
+#pragma unroll
+                    for (int h = 0; h < 4; h++) {
+                        float sacc = 0.f;
+#pragma unroll
+                        for (int q = 0; q < RL; q++) sacc = fmaf(uv[h][q], yk[lane + 32 * q], sacc);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+                        if (lane == 0 && i0 + h < k0) a.zf[i0 + h] = __ldcg(a.zf + i0 + h) - sacc;
+                    }
+                }
+                if (!grid_barrier(a.bar, a.err, G)) return false;
+            }
+            return true;
+        }
         for (int i = gwarp; i < n; i += gwarps) {
             const float t = dot4_range(a.Li + (size_t)i * ldl, a.rf, 0, (i >> 2) + 1, lane);
             if (lane == 0) a.zf[i] = t;
@@ -1287,7 +1393,8 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine(FrArgs a) {
     __shared__ uint32_t slot;
     TcState ts;
     tc_setup(ts, mbar, &slot, a.err);
-    fr_body(a, blockIdx.x, gridDim.x, ts);
+    if (a.bd == BD_LARGE) fr_body<BD_LARGE>(a, blockIdx.x, gridDim.x, ts);
+    else fr_body<BD_SMALL>(a, blockIdx.x, gridDim.x, ts);
     tc_teardown(ts);
 }
 
@@ -1304,7 +1411,8 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrA
     __shared__ uint32_t slot;
     TcState ts;
     tc_setup(ts, mbar, &slot, a.err);
-    fr_body(a, blockIdx.x - cta0[i], nctas[i], ts);
+    if (a.bd == BD_LARGE) fr_body<BD_LARGE>(a, blockIdx.x - cta0[i], nctas[i], ts);
+    else fr_body<BD_SMALL>(a, blockIdx.x - cta0[i], nctas[i], ts);
     tc_teardown(ts);
 }
 
@@ -1441,6 +1549,7 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     fa.rf = w.rf.p;
     fa.uh = w.uh.p;
     fa.ul = w.ul.p;
+    fa.bd = pl.n >= BD_SWITCH ? BD_LARGE : BD_SMALL;
     fa.zf = w.zf.p;
     fa.nrm = w.nrm.p;
     fa.sweeps = sweeps;
@@ -1501,7 +1610,7 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
                               w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p};
     const int ldl = (n + 31) / 32 * 32;
     // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero
-    const size_t nu = (size_t)(n + TT) * BD;
+    const size_t nu = (size_t)(n + TT) * (n >= BD_SWITCH ? BD_LARGE : BD_SMALL);
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
         !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
@@ -1629,6 +1738,151 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
     step_stats().refine_sweeps = (int)h[2];
     for (int k = 0; k < 8; k++) step_stats().phase_us[k] = 1e-3 * (double)tns[k];
     return NQS_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- CG-SR
+// The CG solve of (S + eps I) d = F with S v = O^T (O v) / N_s - <O> (<O> . v)
+// (src/nqs/nqs_optimizer.c:44-139: qgt_apply, cg_solve) as one cooperative
+// launch: every iteration is the operator (rows, partial column sums, column
+// reduce) and the vector updates separated by bounded grid barriers, with the
+// scalars from dot_all so every CTA takes the same branches.  Upstream
+// semantics: d0 = 0, r0 = p0 = F; stop when r.r <= tol^2 r0.r0 (converged) or
+// |p.Ap| < 1e-30 (Krylov breakdown, unconverged) or after max_iters.
+struct CgArgs {
+    const double *O;      // [N_s][N_p] (uncentred)
+    int Ns;
+    long P;
+    const double *F, *gm; // force, column means
+    double eps, tol;
+    int max_iters;
+    double *d, *r, *p, *Ap, *u, *upart;
+    double *scal;         // S_RS, S_RS0, S_PAP
+    int *status;          // I_DONE, I_ITERS, I_CONV
+    unsigned *bar;
+    int *err;
+};
+
+__global__ void __launch_bounds__(PS_THREADS, 1) k_cg_sr(CgArgs a) {
+    __shared__ double red[PS_THREADS / 32];
+    const int G = gridDim.x, bx = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    const int gtid = bx * PS_THREADS + tid, gthreads = G * PS_THREADS;
+    const int gwarp = bx * (PS_THREADS / 32) + (tid >> 5), gwarps = G * (PS_THREADS / 32);
+    const long P = a.P;
+    const int Ns = a.Ns, np = (int)P;
+    for (long k = gtid; k < P; k += gthreads) {
+        a.d[k] = 0.0;
+        a.r[k] = a.F[k];
+        a.p[k] = a.F[k];
+    }
+    const double rs0 = dot_all(a.F, a.F, np, red);
+    double rs = rs0;
+    int it = 0, done = 0, conv = 0;
+    double pap_last = 0.0;
+    if (!grid_barrier(a.bar, a.err, G)) return;
+    for (; it < a.max_iters; it++) {
+        // u = O p
+        for (int i = gwarp; i < Ns; i += gwarps) {
+            const double v = rowdot<true>(a.O + (size_t)i * P, P, a.p, lane);
+            if (lane == 0) a.u[i] = v;
+        }
+        if (!grid_barrier(a.bar, a.err, G)) return;
+        colsum_partial(a.O, Ns, P, a.u, a.upart, gwarp, gwarps, lane);
+        // <u> (the same in every CTA)
+        double um;
+        {
+            double sacc = 0.0;
+            for (int i = tid; i < Ns; i += PS_THREADS) sacc += __ldcg(a.u + i);
+            sacc = warp_sum(sacc);
+            __syncthreads();
+            if (lane == 0) red[tid >> 5] = sacc;
+            __syncthreads();
+            um = 0.0;
+            for (int w = 0; w < PS_THREADS / 32; w++) um += red[w];
+            um /= (double)Ns;
+        }
+        if (!grid_barrier(a.bar, a.err, G)) return;
+        for (long k = gwarp; k < P; k += gwarps) {
+            const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
+            if (lane == 0) a.Ap[k] = sk / (double)Ns - __ldcg(a.gm + k) * um + a.eps * __ldcg(a.p + k);
+        }
+        if (!grid_barrier(a.bar, a.err, G)) return;
+        const double pap = dot_all(a.p, a.Ap, np, red);
+        if (!(fabs(pap) >= 1e-30)) {                    // Krylov breakdown: stop, unconverged
+            done = 1;
+            pap_last = pap;
+            break;
+        }
+        const double alpha = rs / pap;
+        for (long k = gtid; k < P; k += gthreads) {
+            a.d[k] = __ldcg(a.d + k) + alpha * __ldcg(a.p + k);
+            a.r[k] = __ldcg(a.r + k) - alpha * __ldcg(a.Ap + k);
+        }
+        if (!grid_barrier(a.bar, a.err, G)) return;
+        const double rs_new = dot_all(a.r, a.r, np, red);
+        if (rs_new <= a.tol * a.tol * rs0) {
+            done = 1;
+            conv = 1;
+            it++;
+            break;
+        }
+        const double beta = rs_new / rs;
+        for (long k = gtid; k < P; k += gthreads) a.p[k] = __ldcg(a.r + k) + beta * __ldcg(a.p + k);
+        rs = rs_new;
+        if (!grid_barrier(a.bar, a.err, G)) return;
+    }
+    if (bx == 0 && tid == 0) {
+        a.scal[S_RS] = rs;
+        a.scal[S_RS0] = rs0;
+        a.scal[S_PAP] = pap_last;
+        a.status[I_DONE] = done;
+        a.status[I_CONV] = conv;
+        a.status[I_ITERS] = it;
+    }
+}
+
+bool cg_sr_solve(const double *O, int Ns, long P, const double *F, const double *gm, double eps, double tol,
+                 int max_iters, double *d, double *scal, int *status) {
+    Context &c = ctx();
+    cudaStream_t st = c.stream;
+    static DevBuf<double> r, p, Ap, u, upart;
+    static DevBuf<unsigned> bar;
+    static DevBuf<int> err;
+    if (!r.ensure(P) || !p.ensure(P) || !Ap.ensure(P) || !u.ensure(Ns) ||
+        !upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !bar.ensure(2) || !err.ensure(1))
+        return false;
+    if (!NQS_CUDA(cudaMemsetAsync(bar.p, 0, 2 * sizeof(unsigned), st)) ||
+        !NQS_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st)))
+        return false;
+    CgArgs a{O, Ns, P, F, gm, eps, tol, max_iters, d, r.p, p.p, Ap.p, u.p, upart.p, scal, status, bar.p, err.p};
+    int per_sm = 0;
+    if (!NQS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_sr, PS_THREADS, 0))) return false;
+    if (per_sm < 1) {
+        set_error("CG kernel does not fit on an SM");
+        return false;
+    }
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)c.sm_count);
+    lc.blockDim = dim3(PS_THREADS);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    {
+        NQS_LAUNCH("cg_sr");
+        if (!NQS_CUDA(cudaLaunchKernelEx(&lc, k_cg_sr, a))) return false;
+    }
+    int herr = 0;
+    if (!NQS_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        !NQS_CUDA(cudaStreamSynchronize(st)))
+        return false;
+    if (herr) {
+        set_error("CG-SR solve: grid barrier timed out");
+        return false;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------- batches of systems

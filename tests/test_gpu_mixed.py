@@ -102,3 +102,30 @@ def test_phase_times_reported(nqs):
     stats = minsr_mixed(nqs, sweeps=2)[3]
     ph = list(stats.phase_us)
     assert ph[6] > 0 and all(p >= 0 for p in ph[:6]) and sum(ph[:6]) <= ph[6] * 1.01
+
+
+def test_mixed_blocked_substitution_large(nqs):
+    """Systems of order >= 4608 apply the preconditioner by blocked substitution
+    instead of an explicit L^{-1}: a 5120 x 5120 sample-space solve (N_s = 5120 >
+    N_p, forced sample space) against the FP64 step on the same samples (the
+    step's own check, FP64 estimator so the error is the solve's alone)."""
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    N, M = 16, 32
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, rbm_init_scale=0.3,
+                              hamiltonian=1, rng_seed=77, sr_diag_shift=1e-3, learning_rate=0.005)
+    a = nqs.Ansatz(cfg, N)
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    rng = np.random.default_rng(5)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(5120)])
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=8, gram_passes=3, mixed_check=1,
+                    mixed_space=abi.SPACE_SAMPLES)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True, log_amp_fn=m.log_amp_fn, user=m.user)
+        st = nqs.last_step_stats()
+    finally:
+        nqs.set_options()
+    assert info.converged == 1 and st.mixed_fallback == 0
+    assert st.refine_residual < 1e-8
+    assert 0 <= st.delta_rel_err < 1e-7
+    assert st.phase_us[3] < 1.0               # no explicit triangular inverse (microseconds)
