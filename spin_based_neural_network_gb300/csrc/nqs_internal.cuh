@@ -177,6 +177,11 @@ bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, 
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
 
+// CG-SR solve (S + eps I) d = F in one cooperative launch (upstream cg_solve
+// semantics); writes d, scal[S_RS, S_RS0, S_PAP], status[I_DONE, I_ITERS, I_CONV].
+bool cg_sr_solve(const double *O, int Ns, long P, const double *F, const double *gm, double eps, double tol,
+                 int max_iters, double *d, double *scal, int *status);
+
 // Relative residual |r| / |rhs| above which a mixed solve counts as broken down
 // and the step is solved again in FP64.
 constexpr double MIXED_RESID_MAX = 1e-6;

@@ -617,115 +617,6 @@ __global__ void k_apply(double *params, const double *__restrict__ delta, long P
     if (threadIdx.x == 0) scal[S_NORM2] = red[0];
 }
 
-// ---------------------------------------------------------------- CG-SR
-// u_i = sum_k O_ik p_k (warp per row) and per-block partial sums of u.
-__global__ void k_qgt_rows(const double *__restrict__ O, int Ns, long P, const double *__restrict__ p,
-                           double *u, const int *status) {
-    if (status[I_DONE]) return;
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= Ns) return;
-    double s = 0.0;
-    for (long k = lane; k < P; k += 32) s += O[(size_t)w * P + k] * p[k];
-    s = warp_sum(s);
-    if (lane == 0) u[w] = s;
-}
-
-// (S + eps) p = O^T u / Ns - <O> mean(u) + eps p  (src/nqs/nqs_optimizer.c:44-80)
-__global__ void k_qgt_cols(const double *__restrict__ O, int Ns, long P, const double *__restrict__ u,
-                           const double *__restrict__ gm, const double *__restrict__ p, double eps,
-                           double *Ap, const int *status) {
-    if (status[I_DONE]) return;
-    __shared__ double a[8][33];
-    __shared__ double um;
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        double s = 0.0;
-        for (int i = 0; i < Ns; i++) s += u[i];
-        um = s / (double)Ns;
-    }
-    long k = (long)blockIdx.x * 32 + threadIdx.x;
-    double s = 0.0;
-    if (k < P)
-        for (int i = threadIdx.y; i < Ns; i += 8) s += O[(size_t)i * P + k] * u[i];
-    a[threadIdx.y][threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.y == 0 && k < P) {
-        double S = 0.0;
-        for (int q = 0; q < 8; q++) S += a[q][threadIdx.x];
-        Ap[k] = (S / (double)Ns) - gm[k] * um + eps * p[k];
-    }
-}
-
-__device__ double block_dot(const double *a, const double *b, long n, double *red) {
-    double s = 0.0;
-    for (long k = threadIdx.x; k < n; k += blockDim.x) s += a[k] * b[k];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
-    double r = red[0];
-    __syncthreads();
-    return r;
-}
-
-// One CG update (src/nqs/nqs_optimizer.c:105-135), single block of 1024.
-__global__ void k_cg_update(double *d, double *r, double *p, const double *__restrict__ Ap, long P,
-                            double *scal, int *status, int it, double tol) {
-    if (status[I_DONE]) return;
-    __shared__ double red[1024];
-    double pAp = block_dot(p, Ap, P, red);
-    if (!(fabs(pAp) >= 1e-30)) {                 // Krylov breakdown: stop, unconverged
-        if (threadIdx.x == 0) {
-            status[I_DONE] = 1;
-            status[I_ITERS] = it;
-            scal[S_PAP] = pAp;
-        }
-        return;
-    }
-    double alpha = scal[S_RS] / pAp;
-    for (long k = threadIdx.x; k < P; k += blockDim.x) {
-        d[k] += alpha * p[k];
-        r[k] += -alpha * Ap[k];
-    }
-    __syncthreads();
-    double rs_new = block_dot(r, r, P, red);
-    if (rs_new <= tol * tol * scal[S_RS0]) {
-        if (threadIdx.x == 0) {
-            status[I_DONE] = 1;
-            status[I_CONV] = 1;
-            status[I_ITERS] = it + 1;
-        }
-        return;
-    }
-    double beta = rs_new / scal[S_RS];
-    for (long k = threadIdx.x; k < P; k += blockDim.x) p[k] = r[k] + beta * p[k];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        scal[S_RS] = rs_new;
-        status[I_ITERS] = it + 1;
-    }
-}
-
-__global__ void k_cg_init(const double *__restrict__ F, double *d, double *r, double *p, long P,
-                          double *scal, int *status) {
-    __shared__ double red[1024];
-    for (long k = threadIdx.x; k < P; k += blockDim.x) {
-        d[k] = 0.0;
-        r[k] = F[k];
-        p[k] = F[k];
-    }
-    __syncthreads();
-    double rs = block_dot(r, r, P, red);
-    if (threadIdx.x == 0) {
-        scal[S_RS] = rs;
-        scal[S_RS0] = rs;
-        status[I_DONE] = 0;
-        status[I_ITERS] = 0;
-        status[I_CONV] = 0;
-    }
-}
-
 // ---------------------------------------------------------------- the step
 
 struct StepIn {
@@ -1056,27 +947,11 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             NQS_LAUNCH("col_stats");
             if (!col_stats(w.O.p, Ns, P, w.E.p, w.scal.p, w.gm.p, w.F.p)) return -1;
         }
-        {
-            NQS_LAUNCH("cg_init");
-            k_cg_init<<<1, 1024, 0, st>>>(w.F.p, w.delta.p, w.r.p, w.p.p, P, w.scal.p, w.status.p);
-        }
-        int maxit = cfg->sr_cg_max_iters;
-        for (int it = 0; it < maxit; it++) {
-            {
-                NQS_LAUNCH("qgt_rows");
-                k_qgt_rows<<<(Ns * 32 + 255) / 256, 256, 0, st>>>(w.O.p, Ns, P, w.p.p, w.u.p, w.status.p);
-            }
-            {
-                NQS_LAUNCH("qgt_cols");
-                k_qgt_cols<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.u.p, w.gm.p, w.p.p, cfg->sr_diag_shift,
-                                              w.Ap.p, w.status.p);
-            }
-            {
-                NQS_LAUNCH("cg_update");
-                k_cg_update<<<1, 1024, 0, st>>>(w.delta.p, w.r.p, w.p.p, w.Ap.p, P, w.scal.p, w.status.p,
-                                                it, cfg->sr_cg_tol);
-            }
-        }
+        const int maxit = cfg->sr_cg_max_iters;
+        // the whole CG (all iterations) in one cooperative launch
+        if (!cg_sr_solve(w.O.p, Ns, P, w.F.p, w.gm.p, cfg->sr_diag_shift, cfg->sr_cg_tol, maxit, w.delta.p, w.scal.p,
+                         w.status.p))
+            return -1;
         int h[16];
         double hs[16];
         if (!NQS_CUDA(cudaMemcpyAsync(h, w.status.p, sizeof(h), cudaMemcpyDeviceToHost, st)) ||
