@@ -71,6 +71,86 @@ __device__ __forceinline__ void warp_mlp_eval(const DevAnsatz &a, uint64_t bits,
     ar = warp_sum(im) + wi[M + 1];
 }
 
+// ---- FP32 MLP (mixed precision).  Lane l owns hidden units l + 32 q, q < MQ.
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// layer-1 pre-activations z1 = W1 s + b1 (ascending i)
+template <int MQ>
+__device__ __forceinline__ void mlp32_z1(const DevAnsatz &a, uint64_t s, float (&z1)[MQ]) {
+    const int lane = threadIdx.x & 31, M = a.M, N = a.N;
+    const float *b1 = a.m32 + (long)N * M + 2L * M * mlp32_pitch(M);
+#pragma unroll
+    for (int q = 0; q < MQ; q++) {
+        const int k = lane + 32 * q;
+        float z = k < M ? b1[k] : 0.f;
+        if (k < M)
+            for (int i = 0; i < N; i++) z = fmaf((float)spin_of(s, i), a.m32[(long)i * M + k], z);
+        z1[q] = z;
+    }
+}
+
+// z1 after flipping site u (and v >= 0): z1 - 2 s_u W1[:, u] - 2 s_v W1[:, v]
+template <int MQ>
+__device__ __forceinline__ void mlp32_z1_flip(const DevAnsatz &a, uint64_t s, int u, int v, const float (&z1)[MQ],
+                                              float (&out)[MQ]) {
+    const int lane = threadIdx.x & 31, M = a.M;
+    const float su = -2.f * (float)spin_of(s, u), sv = v >= 0 ? -2.f * (float)spin_of(s, v) : 0.f;
+#pragma unroll
+    for (int q = 0; q < MQ; q++) {
+        const int k = lane + 32 * q;
+        float z = z1[q];
+        if (k < M) {
+            z = fmaf(su, a.m32[(long)u * M + k], z);
+            if (v >= 0) z = fmaf(sv, a.m32[(long)v * M + k], z);
+        }
+        out[q] = z;
+    }
+}
+
+// h1 = tanh(z1) (to the warp's shared row h1s and h1), h2 = tanh(W2 h1 + b2)
+// with W2^T rows from shared memory (pitch MQ * 32), log|psi| and arg; every
+// lane returns the same la / ar
+template <int MQ>
+__device__ __forceinline__ void mlp32_forward(const DevAnsatz &a, const float *w2t, const float (&z1)[MQ],
+                                              float *h1s, float (&h1)[MQ], float (&h2)[MQ], float &la, float &ar) {
+    const int lane = threadIdx.x & 31, M = a.M;
+    constexpr int MP = 32 * MQ;
+    const float *vec = a.m32 + (long)a.N * M + 2L * M * MP;
+    const float *b2 = vec + M, *wr = vec + 2 * M, *wi = vec + 3 * M;
+#pragma unroll
+    for (int q = 0; q < MQ; q++) {
+        h1[q] = lane + 32 * q < M ? tanhf(z1[q]) : 0.f;
+        h1s[lane + 32 * q] = h1[q];
+    }
+    __syncwarp();
+    float z[MQ];
+#pragma unroll
+    for (int q = 0; q < MQ; q++) z[q] = lane + 32 * q < M ? b2[lane + 32 * q] : 0.f;
+    for (int k = 0; k < M; k++) {
+        const float h = h1s[k];
+        const float *row = w2t + k * MP + lane;
+#pragma unroll
+        for (int q = 0; q < MQ; q++) z[q] = fmaf(row[32 * q], h, z[q]);
+    }
+    float r = 0.f, im = 0.f;
+#pragma unroll
+    for (int q = 0; q < MQ; q++) {
+        const int j = lane + 32 * q;
+        h2[q] = j < M ? tanhf(z[q]) : 0.f;
+        if (j < M) {
+            r = fmaf(wr[j], h2[q], r);
+            im = fmaf(wi[j], h2[q], im);
+        }
+    }
+    la = warp_sum_f(r) + vec[4 * M];
+    ar = warp_sum_f(im) + vec[4 * M + 1];
+    __syncwarp();
+}
+
 // log psi of the base ansatz (all lanes return the same value).
 __device__ __forceinline__ void warp_base_eval(const DevAnsatz &a, uint64_t bits, double &la, double &ar,
                                                double *scratch) {

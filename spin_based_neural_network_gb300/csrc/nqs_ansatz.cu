@@ -96,13 +96,33 @@ __global__ void k_derive(DevAnsatz a, double *wtr, double *wti, float2 *f32) {
         if (t < M) f32[3 * NM + N + t] = make_float2((float)a.p[N + t], cx ? (float)a.p[Pr + N + t] : 0.f);
     } else if (a.kind == KIND_MLP) {
         long nW1 = (long)M * N;
+        float *m = (float *)f32;
+        const int MP = mlp32_pitch(M);
+        float *w2t = m + nW1, *w2 = w2t + (long)M * MP, *vec = w2 + (long)M * MP;
         if (t < nW1) {
             int k = (int)(t / N), i = (int)(t % N);
             wtr[(long)i * M + k] = a.p[t];
-        } else if (t < nW1 + (long)M * M) {
+            m[(long)i * M + k] = (float)a.p[t];
+        } else if (t < nW1 + (long)M * MP) {
             long u = t - nW1;
-            int j = (int)(u / M), k = (int)(u % M);
-            wti[(long)k * M + j] = a.p[nW1 + M + u];
+            int r = (int)(u / MP), c = (int)(u % MP);           // row r, padded column c
+            if (c < M) {
+                const double w_rc = a.p[nW1 + M + (long)r * M + c];   // W2[r][c]
+                wti[(long)c * M + r] = w_rc;
+                w2[(long)r * MP + c] = (float)w_rc;
+                w2t[(long)c * MP + r] = (float)w_rc;
+            } else {
+                w2[(long)r * MP + c] = 0.f;
+                w2t[(long)r * MP + c] = 0.f;
+            }
+        }
+        if (t < M) {
+            const double *b1 = a.p + nW1, *b2 = b1 + M + (long)M * M, *wr = b2 + M, *wi = wr + M;
+            vec[t] = (float)b1[t];
+            vec[M + t] = (float)b2[t];
+            vec[2 * M + t] = (float)wr[t];
+            vec[3 * M + t] = (float)wi[t];
+            if (t < 2) vec[4 * M + t] = (float)wi[M + t];
         }
     }
 }
@@ -123,12 +143,13 @@ DevAnsatz ansatz_dev(const Ansatz *a) {
     d.sh32 = rbm ? a->d_f32.p + 2 * NM : nullptr;
     d.a32 = rbm ? a->d_f32.p + 3 * NM : nullptr;
     d.b32 = rbm ? a->d_f32.p + 3 * NM + a->N : nullptr;
+    d.m32 = a->kind == KIND_MLP ? (const float *)a->d_f32.p : nullptr;
     return d;
 }
 
 bool ansatz_refresh_derived(Ansatz *a) {
     if (a->kind == KIND_MF) return true;
-    long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * a->M : (long)a->M * a->N;
+    long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * mlp32_pitch(a->M) : (long)a->M * a->N;
     NQS_LAUNCH("derive_weights");
     k_derive<<<(unsigned)((work + 255) / 256), 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
                                                                         a->d_wti.p, a->d_f32.p);
@@ -572,7 +593,8 @@ nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
         !a->d_params.ensure((size_t)a->P) ||
         !a->d_wtr.ensure((size_t)num_sites * (M ? M : 1) + (kind == KIND_MLP ? 0 : 0)) ||
         !a->d_wti.ensure(kind == KIND_MLP ? (size_t)M * M : (size_t)num_sites * (M ? M : 1)) ||
-        !a->d_f32.ensure(3 * (size_t)num_sites * (M ? M : 1) + num_sites + (M ? M : 1))) {
+        !a->d_f32.ensure(kind == KIND_MLP ? (mlp32_floats(num_sites, M) + 1) / 2
+                                          : 3 * (size_t)num_sites * (M ? M : 1) + num_sites + (M ? M : 1))) {
         nqs_ansatz_free((nqs_ansatz_t *)a);
         return nullptr;
     }

@@ -105,6 +105,10 @@ struct DevBuf {
 // ---------------------------------------------------------------- device program
 enum : int { KIND_MF = 0, KIND_RBM = 5, KIND_CRBM = 6, KIND_MLP = NQS_GPU_ANSATZ_MLP };
 
+// Padded row pitch of the MLP's FP32 W2 tables and the floats of its FP32 tables.
+__host__ __device__ inline int mlp32_pitch(int M) { return (M + 31) / 32 * 32; }
+inline size_t mlp32_floats(int N, int M) { return (size_t)N * M + 2 * (size_t)M * mlp32_pitch(M) + 4 * (size_t)M + 2; }
+
 struct DevAnsatz {
     int kind, N, M;
     long P;
@@ -115,6 +119,10 @@ struct DevAnsatz {
     // rebuilt with the transposed copies: W^T [N][M], cosh(2 W^T), sinh(2 W^T)
     // [N][M], visible bias [N], hidden bias [M]
     const float2 *w32, *ch32, *sh32, *a32, *b32;
+    // FP32 tables of the MLP (floats): W1^T [N][M], then W2^T and W2 as [M][MP]
+    // rows padded with zeros to MP = 32 ceil(M / 32), then b1, b2, w_re, w_im
+    // [M], c_re, c_im
+    const float *m32;
 };
 
 struct DevAmp {
@@ -146,7 +154,7 @@ struct Ansatz {
     double *h_params = nullptr;     // pinned host mirror (returned by params_raw)
     double *h_shadow = nullptr;     // last value known to be on the device
     DevBuf<double> d_params, d_wtr, d_wti;
-    DevBuf<float2> d_f32;           // RBM / cRBM FP32 tables (see DevAnsatz)
+    DevBuf<float2> d_f32;           // RBM / cRBM / MLP FP32 tables (see DevAnsatz)
     bool dev_valid = false;
 };
 
@@ -172,7 +180,8 @@ bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bi
                             bool fp32 = false);
 // True when the FP32 estimator / sampler can run this program (RBM or cRBM
 // with Marshall layers, no symmetry projection).
-bool fp32_capable(const DevAmp &A);
+bool fp32_capable(const DevAmp &A);        // RBM / cRBM FP32 product-form tables
+bool fp32_mlp_capable(const DevAmp &A);    // MLP with width <= 128 and FP32 tables
 bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, double *O, double *Oi);
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);

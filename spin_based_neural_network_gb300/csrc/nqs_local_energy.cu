@@ -610,6 +610,162 @@ k_local_generic(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, do
     }
 }
 
+// ---------------------------------------------------------------- FP32 MLP estimator
+// Mixed-precision local energies and Jacobian rows of the 2-hidden-layer MLP:
+// warp = sample.  A connected configuration changes the layer-1 pre-activations
+// by one or two weight columns (O(M)); layer 2 is a full GEMV against W2^T in
+// shared memory; ratios psi(s') / psi(s) = exp(d log|psi| + i d arg) in FP32.
+// The Jacobian row (d log|psi| / d theta, the real projection) comes from FP32
+// back-propagation and is stored in FP64.
+constexpr int kMlpWarps = 16;
+
+template <int MQ>
+__global__ void __launch_bounds__(32 * kMlpWarps)
+k_local_mlp32(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, double *__restrict__ Er,
+              double *__restrict__ Ei, double *__restrict__ O) {
+    extern __shared__ float fsm[];
+    constexpr int MP = 32 * MQ;
+    const DevAnsatz &a = A.a;
+    const int N = a.N, M = a.M, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *w2t = fsm, *w2 = fsm + M * MP, *ws = fsm + 2 * M * MP + warp * 3 * MP;
+    float *h1s = ws, *d2s = ws + MP, *d1s = ws + 2 * MP;
+    {
+        const float *g = a.m32 + (long)N * M;                  // W2^T then W2, both [M][MP]
+        for (int e = threadIdx.x; e < 2 * M * MP; e += blockDim.x) fsm[e] = g[e];
+    }
+    __syncthreads();
+    const int b = blockIdx.x * kMlpWarps + warp;
+    if (b >= B) return;
+    const uint64_t s = bits[b];
+    float z1[MQ], h1[MQ], h2[MQ], la0, ar0;
+    mlp32_z1<MQ>(a, s, z1);
+    mlp32_forward<MQ>(a, w2t, z1, h1s, h1, h2, la0, ar0);
+    const int par0 = marshall_count(A, s);
+
+    auto ratio = [&](int u, int v, float &rre, float &rim) {
+        float zp[MQ], g1[MQ], g2[MQ], la, ar;
+        mlp32_z1_flip<MQ>(a, s, u, v, z1, zp);
+        mlp32_forward<MQ>(a, w2t, zp, h1s, g1, g2, la, ar);
+        uint64_t s2 = s ^ (1ull << u);
+        if (v >= 0) s2 ^= 1ull << v;
+        const float mag = expf(la - la0);
+        float sn, cs;
+        sincosf(ar - ar0, &sn, &cs);
+        const float sg = ((marshall_count(A, s2) - par0) & 1) ? -1.f : 1.f;
+        rre = sg * mag * cs;
+        rim = sg * mag * sn;
+    };
+
+    float e_re = 0.f, e_im = 0.f;
+    if (H.kind == NQS_HAM_TFIM) {
+        for (int k = 0; k < H.nb1; k++)
+            e_re += -(float)H.J * (float)(spin_of(s, H.b1[2 * k]) * spin_of(s, H.b1[2 * k + 1]));
+        for (int i = 0; i < N; i++) {
+            float r, q;
+            ratio(i, -1, r, q);
+            e_re += -(float)H.Gamma * r;
+            e_im += -(float)H.Gamma * q;
+        }
+    } else {
+        for (int g = 0; g < 2; g++) {
+            const int nb = g ? H.nb2 : H.nb1;
+            const int *bl = g ? H.b2 : H.b1;
+            const float jz = g ? (float)H.J2 : (float)H.Jz, jxy = g ? (float)H.J2 : (float)H.Jxy;
+            for (int k = 0; k < nb; k++) {
+                const int u = bl[2 * k], v = bl[2 * k + 1];
+                const int su = spin_of(s, u), sv = spin_of(s, v);
+                e_re += 0.25f * jz * (float)(su * sv);
+                if (su != sv) {
+                    float r, q;
+                    ratio(u, v, r, q);
+                    e_re += 0.5f * jxy * r;
+                    e_im += 0.5f * jxy * q;
+                }
+            }
+        }
+    }
+    if (lane == 0) {
+        if (Er) Er[b] = (double)e_re;
+        if (Ei) Ei[b] = (double)e_im;
+    }
+    if (!O) return;
+    // back-propagation of log|psi| = w_re . h2 + c_re
+    const float *wr = a.m32 + (long)N * M + 2L * M * MP + 2 * M;
+#pragma unroll
+    for (int q = 0; q < MQ; q++) {
+        const int j = lane + 32 * q;
+        d2s[j] = j < M ? wr[j] * (1.f - h2[q] * h2[q]) : 0.f;
+        h1s[j] = h1[q];
+    }
+    __syncwarp();
+    float d1[MQ];
+#pragma unroll
+    for (int q = 0; q < MQ; q++) d1[q] = 0.f;
+    for (int j = 0; j < M; j++) {
+        const float d = d2s[j];
+        const float *row = w2 + j * MP + lane;
+#pragma unroll
+        for (int q = 0; q < MQ; q++) d1[q] = fmaf(row[32 * q], d, d1[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < MQ; q++) d1s[lane + 32 * q] = d1[q] * (1.f - h1[q] * h1[q]);
+    __syncwarp();
+    double *row = O + (size_t)b * a.P;
+    const long oW2 = (long)M * N + M, ob2 = oW2 + (long)M * M, owr = ob2 + M;
+    for (long q = lane; q < (long)M * N; q += 32) {
+        const int k = (int)(q / N), i = (int)(q % N);
+        row[q] = (double)(spin_of(s, i) > 0 ? d1s[k] : -d1s[k]);
+    }
+    for (int k = lane; k < M; k += 32) row[(long)M * N + k] = (double)d1s[k];
+    for (long q = lane; q < (long)M * M; q += 32) {
+        const int j = (int)(q / M), k = (int)(q % M);
+        row[oW2 + q] = (double)(d2s[j] * h1s[k]);
+    }
+#pragma unroll
+    for (int q = 0; q < MQ; q++) {
+        const int j = lane + 32 * q;
+        if (j < M) {
+            row[ob2 + j] = (double)d2s[j];
+            row[owr + j] = (double)h2[q];
+            row[owr + M + j] = 0.0;
+        }
+    }
+    if (lane == 0) {
+        row[owr + 2 * M] = 1.0;
+        row[owr + 2 * M + 1] = 0.0;
+    }
+}
+
+bool fp32_mlp_capable(const DevAmp &A) {
+    return A.G == 0 && A.a.kind == KIND_MLP && A.a.m32 != nullptr && A.a.M <= 128 && A.a.N <= 64;
+}
+
+static bool launch_mlp32(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er, double *Ei,
+                         double *O) {
+    const int MQ = (A.a.M + 31) / 32, MP = 32 * MQ;
+    const size_t smem = sizeof(float) * (2 * (size_t)A.a.M * MP + (size_t)kMlpWarps * 3 * MP);
+    const dim3 grid((B + kMlpWarps - 1) / kMlpWarps), block(32 * kMlpWarps);
+    cudaStream_t st = ctx().stream;
+#define NQS_MCASE(QQ)                                                                                        \
+    case QQ: {                                                                                               \
+        static bool attr = false;                                                                            \
+        if (!attr && !NQS_CUDA(cudaFuncSetAttribute(k_local_mlp32<QQ>,                                       \
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024))) \
+            return false;                                                                                    \
+        attr = true;                                                                                         \
+        k_local_mlp32<QQ><<<grid, block, smem, st>>>(A, H, bits, B, Er, Ei, O);                              \
+        break;                                                                                               \
+    }
+    switch (MQ) {
+        NQS_MCASE(1) NQS_MCASE(2) NQS_MCASE(3) NQS_MCASE(4)
+        default:
+            set_error("MLP width %d unsupported by the FP32 estimator", A.a.M);
+            return false;
+    }
+#undef NQS_MCASE
+    return NQS_CUDA(cudaGetLastError());
+}
+
 template <int J, bool C>
 static void launch_rbm(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er,
                        double *Ei, double *O, double *Oi, int gm, bool f32) {
@@ -632,6 +788,10 @@ bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bi
     if (A.a.N != H.N) {
         set_error("ansatz has %d sites, lattice has %d", A.a.N, H.N);
         return false;
+    }
+    if (fp32 && fp32_mlp_capable(A) && grad_mode != 2) {
+        NQS_LAUNCH("local_estimator_mlp32");
+        return launch_mlp32(A, H, bits, B, Er, Ei, grad_mode ? O : nullptr);
     }
     const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
     if (fused) {

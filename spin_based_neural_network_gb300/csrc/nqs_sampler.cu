@@ -437,6 +437,72 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_generic(SampleArgs S, DevAm
     }
 }
 
+// FP32 chains of the MLP (mixed precision): the warp keeps the layer-1
+// pre-activations of its configuration in registers; a proposal moves them by
+// one or two weight columns and runs layer 2 against W2^T in shared memory.
+template <int RNG, int MOVE, int MQ>
+__global__ void __launch_bounds__(32 * kSW) k_sample_mlp32(SampleArgs S, DevAmp A) {
+    if (S.move_dev) S.move0 = *S.move_dev;
+    extern __shared__ float fsm[];
+    constexpr int MP = 32 * MQ;
+    const DevAnsatz &a = A.a;
+    const int M = a.M, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *w2t = fsm, *h1s = fsm + M * MP + warp * MP;
+    {
+        const float *g = a.m32 + (long)a.N * M;
+        for (int e = threadIdx.x; e < M * MP; e += blockDim.x) w2t[e] = g[e];
+    }
+    __syncthreads();
+    const int c = blockIdx.x * kSW + warp;
+    if (c >= S.C) return;
+    uint64_t s = S.bits[c];
+    float z1[MQ], nz1[MQ], h1[MQ], h2[MQ], la, ar, nla = 0.f;
+    mlp32_z1<MQ>(a, s, z1);
+    mlp32_forward<MQ>(a, w2t, z1, h1s, h1, h2, la, ar);
+    auto eval = [&](int u, int v) -> double {
+        mlp32_z1_flip<MQ>(a, s, u, v, z1, nz1);
+        float g;
+        mlp32_forward<MQ>(a, w2t, nz1, h1s, h1, h2, nla, g);
+        return (double)(nla - la);
+    };
+    auto commit = [&](int, int) {
+#pragma unroll
+        for (int q = 0; q < MQ; q++) z1[q] = nz1[q];
+        la = nla;
+    };
+    unsigned long long acc = 0, pro = 0;
+    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro);
+    if (lane == 0) {
+        S.bits[c] = s;
+        atomicAdd(&S.counts[0], acc);
+        atomicAdd(&S.counts[1], pro);
+    }
+}
+
+template <int RNG, int MOVE>
+static bool launch_mlp32_chains(const SampleArgs &S, const DevAmp &A, dim3 grid, dim3 block, cudaStream_t st) {
+    const int MQ = (A.a.M + 31) / 32, MP = 32 * MQ;
+    const size_t smem = sizeof(float) * ((size_t)A.a.M * MP + (size_t)kSW * MP);
+#define NQS_MCASE(QQ)                                                                                        \
+    case QQ: {                                                                                               \
+        static bool attr = false;                                                                            \
+        if (!attr && !NQS_CUDA(cudaFuncSetAttribute(k_sample_mlp32<RNG, MOVE, QQ>,                           \
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024))) \
+            return false;                                                                                    \
+        attr = true;                                                                                         \
+        k_sample_mlp32<RNG, MOVE, QQ><<<grid, block, smem, st>>>(S, A);                                       \
+        break;                                                                                               \
+    }
+    switch (MQ) {
+        NQS_MCASE(1) NQS_MCASE(2) NQS_MCASE(3) NQS_MCASE(4)
+        default:
+            set_error("MLP width %d unsupported by the FP32 chains", A.a.M);
+            return false;
+    }
+#undef NQS_MCASE
+    return NQS_CUDA(cudaGetLastError());
+}
+
 // Philox chain start: uniform bits, or a Fisher-Yates shuffle of n_down down
 // spins (fixed-magnetisation sector).  One thread per chain.
 // Device-side move counter of a replayed sampler launch.
@@ -488,6 +554,10 @@ static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32, const DevMa
     dim3 grid((S.C + kSW - 1) / kSW), block(32 * kSW);
     cudaStream_t st = ctx().stream;
     const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
+    if (f32 && RNG == NQS_GPU_RNG_PHILOX && fp32_mlp_capable(A)) {
+        NQS_LAUNCH("sampler_mlp32");
+        return launch_mlp32_chains<RNG, MOVE>(S, A, grid, block, st);
+    }
     if (f32 && RNG == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
         const int J = (A.a.M + 31) / 32;
         const bool cx = A.a.kind == KIND_CRBM;

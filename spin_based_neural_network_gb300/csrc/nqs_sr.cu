@@ -75,7 +75,7 @@ __global__ void k_energy_stats(const double *__restrict__ E, int n, double *scal
 // the compensated sums and the lag products are spread over blocks of
 // ES_CHUNK samples; the last block to finish (an atomic ticket) merges the
 // partials in block order, so results do not depend on scheduling.
-constexpr int ES_THREADS = 256, ES_CHUNK = 1024, ES_LAGS = 16;
+constexpr int ES_THREADS = 256, ES_CHUNK = 256, ES_LAGS = 16;
 
 static int es_blocks(int n) { return (n + ES_CHUNK - 1) / ES_CHUNK; }
 
@@ -829,7 +829,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         return minsr_fp64_solve(w.O.p, w.eps.p, Ns, P, cfg->sr_diag_shift, y_out, conv);
     };
     const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
-    const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && fp32_capable(A);
+    const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && (fp32_capable(A) || fp32_mlp_capable(A));
     nqs_gpu_step_stats_t &ss = step_stats();
     ss.energy_rel_err = -1.0;
     double e64 = 0.0;

@@ -111,3 +111,60 @@ def test_fp32_chains_follow_fp64_chains(nqs, kind):
     same = np.mean(np.all(b64 == b32, axis=1))
     assert same >= 0.9, same
     assert abs(acc64 - acc32) <= 0.02
+
+
+# ---- the 2-hidden-layer MLP (extension): FP32 forward from incrementally
+# updated layer-1 pre-activations, FP32 back-propagation for the Jacobian.
+
+def mlp_kagome_case(nqs, abi, width, Ns, seed=5):
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=width, depth=2, hamiltonian=abi.HAM_KAGOME_HEISENBERG,
+                              kagome_pbc=1, j_coupling=1.0, rng_seed=seed, sr_diag_shift=1e-3, learning_rate=0.01)
+    a = nqs.Ansatz(cfg, 12)
+    rng = np.random.default_rng(seed)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 6, np.int32)) for _ in range(Ns)])
+    return cfg, a, batch
+
+
+@pytest.mark.parametrize("width", [24, 40, 108])
+def test_fp32_mlp_kagome_step_against_oracle(nqs, width):
+    """Kagome 2x2 PBC (N = 12) with the MLP: FP32 local energies within 2e-5 of
+    max|E_loc| of the FP64 oracle, delta-theta within 1e-3 (FP32 Jacobian), and
+    the step's own FP64 cross-check agreeing."""
+    from spin_based_neural_network_gb300 import abi
+    cfg, a, batch = mlp_kagome_case(nqs, abi, width, 1024)
+    p0 = a.params.copy()
+    nqs.set_options(precision=abi.PREC_MIXED, refine_sweeps=8, gram_passes=3, mixed_check=1, fp32_estimator=1)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, 2, 2, a, batch, minsr=True)
+        st = nqs.last_step_stats()
+    finally:
+        nqs.set_options()
+    amp = O.Amp(O.OR_MLP, 12, width, p0.copy(), [])
+    Eo, do, io = O.minsr_step(O.ham(O.OR_KAGOME, 2, 2, kagome_pbc=1), amp, batch, 1e-3, 0.01)
+    assert info.converged == 1
+    assert np.max(np.abs(E - Eo)) <= 2e-5 * np.max(np.abs(Eo))
+    assert 0 <= st.energy_rel_err <= 1e-5
+    err = np.linalg.norm(delta - do) / np.linalg.norm(do)
+    assert err < 1e-3 and 0 <= st.delta_rel_err < 1e-3
+
+
+def test_fp32_mlp_chains_follow_fp64_chains(nqs):
+    from spin_based_neural_network_gb300 import abi
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=40, depth=2, hamiltonian=abi.HAM_KAGOME_HEISENBERG,
+                              kagome_pbc=1, rng_seed=17)
+    a = nqs.Ansatz(cfg, 12)
+    chains = 128
+
+    def run(prec, f32):
+        o = nqs.options(num_chains=chains, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=6, lattice_x=2,
+                        lattice_y=2, lattice_kagome=1, precision=prec, fp32_estimator=f32)
+        s = nqs.Sampler(12, cfg, a.log_amp_fn, a.user, o)
+        s.thermalize()
+        return s.batch(chains * 8), s.acceptance_ratio()
+
+    b64, acc64 = run(abi.PREC_FP64, 0)
+    b32, acc32 = run(abi.PREC_MIXED, 1)
+    assert np.all(b32.sum(axis=1) == 0)                  # Sz = 0 kept
+    same = np.mean(np.all(b64 == b32, axis=1))
+    assert same >= 0.9, same
+    assert abs(acc64 - acc32) <= 0.02
