@@ -469,6 +469,18 @@ def timed_steps(nqs, L, step, warm, steps):
     return ms, info
 
 
+def step_kernels(nqs, step, top=8):
+    """Per-kernel device time of one step (CUDA events around each launch; ms)."""
+    nqs.profile_reset()
+    nqs.profile(True)
+    try:
+        step()
+    finally:
+        nqs.profile(False)
+    prof = nqs.profile_read()
+    return {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:top]}
+
+
 def other_configs(nqs, abi, L, base_opts, which):
     """The other workloads of the measurement table, each on its own shapes
     (seeded synthetic parameters, configurations from the sampler):
@@ -482,9 +494,10 @@ def other_configs(nqs, abi, L, base_opts, which):
             and the FP64 path's own steps/s;
       cfg4  kagome 3x3 PBC (N = 27) Heisenberg, Sz = 1/2, MLP 27-108-108-(Re, Im) tanh (Xavier,
             N_p = 15014), 1024 chains x 16 = 16384 samples, exchange moves on the kagome bonds,
-            MinSR shift 1e-3, lr 0.005, mixed precision (FP64 estimator: the MLP has no FP32
-            product form); a few timed steps; the recorded upstream ground-state energy
-            (tests/golden/kagome_3x3_e0.json) for reference."""
+            MinSR shift 1e-3, lr 0.005, mixed precision (FP32 MLP estimator and chains: layer 1
+            updated by weight columns, layer 2 against W2^T in shared memory); a few timed
+            steps; the recorded upstream ground-state energy (tests/golden/kagome_3x3_e0.json)
+            for reference."""
     import numpy as np
     out = {}
     if "1" in which:
@@ -530,6 +543,7 @@ def other_configs(nqs, abi, L, base_opts, which):
         step3 = lambda: nqs.sr_step_minsr(cfg, Lx, Ly, a, s, a.log_amp_fn, a.user)
         ms, info = timed_steps(nqs, L, step3, 2, 10)
         ph = list(nqs.last_step_stats().phase_us)
+        k3 = step_kernels(nqs, step3)
         nqs.set_options(**dict(base_opts, mixed_check=1))
         step3()
         st = nqs.last_step_stats()
@@ -543,29 +557,60 @@ def other_configs(nqs, abi, L, base_opts, which):
             "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "solve_space": "samples (N_s = 8192 < N_p = 10728)",
             "num_params": a.P, "delta_theta_rel_err_vs_fp64": st.delta_rel_err, "energy_rel_err": st.energy_rel_err,
             "cg_residual": st.refine_residual, "cg_iterations": st.refine_sweeps,
-            "factor_solve_phases_us": [round(x, 1) for x in ph],
+            "factor_solve_phases_us": [round(x, 1) for x in ph], "kernels_ms_one_step": k3,
             "plain_fp64_steps_per_s": 1000.0 / ms64, "speedup_vs_fp64": ms64 / ms}
     if "4" in which:
-        nqs.set_options(**dict(base_opts, fp32_estimator=0))
+        nqs.set_options(**base_opts)
         N, W = 27, 108
         cfg = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=W, depth=2, hamiltonian=abi.HAM_KAGOME_HEISENBERG,
                                   kagome_pbc=1, j_coupling=1.0, rng_seed=SEED + 44, num_samples=16384,
                                   num_thermalize=4 * N, num_decorrelate=N, sr_diag_shift=1e-3, learning_rate=0.005)
         a = nqs.Ansatz(cfg, N)
         o = nqs.options(num_chains=1024, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=13, lattice_x=3,
-                        lattice_y=3, lattice_kagome=1, precision=abi.PREC_MIXED, fp32_estimator=0)
+                        lattice_y=3, lattice_kagome=1, precision=abi.PREC_MIXED, fp32_estimator=1)
         s = nqs.Sampler(N, cfg, a.log_amp_fn, a.user, o)
         s.thermalize()
         step4 = lambda: nqs.sr_step_minsr(cfg, 3, 3, a, s, a.log_amp_fn, a.user)
         ms, info = timed_steps(nqs, L, step4, 1, 3)
         ph = list(nqs.last_step_stats().phase_us)
+        k4 = step_kernels(nqs, step4)
+
+        def run4(learned, decor, warm=2, steps=4):
+            # plain exchange moves, or mixed with the learned proposal (MADE width 64,
+            # BF16, mix 0.5, trained online on every batch)
+            c4 = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=W, depth=2,
+                                     hamiltonian=abi.HAM_KAGOME_HEISENBERG, kagome_pbc=1, j_coupling=1.0,
+                                     rng_seed=SEED + 44, num_samples=16384, num_thermalize=4 * N,
+                                     num_decorrelate=decor, sr_diag_shift=1e-3, learning_rate=0.005)
+            a4 = nqs.Ansatz(c4, N)
+            s4 = nqs.Sampler(N, c4, a4.log_amp_fn, a4.user, o)
+            lp = nqs.LearnedProposal(s4, hidden=64, mix=0.5) if learned else None
+            s4.thermalize()
+            ess = []
+
+            def st4():
+                r = nqs.sr_step_minsr(c4, 3, 3, a4, s4, a4.log_amp_fn, a4.user)
+                ess.append(nqs.last_step_stats().ess)
+                return r
+            ms4, _ = timed_steps(nqs, L, st4, warm, steps)
+            e = float(np.mean(ess[warm:]))
+            out4 = {"decorrelate": decor, "learned": learned, "ess_per_step": e, "tau_int": 16384.0 / e,
+                    "ms_per_step": ms4, "ess_per_s": e * 1000.0 / ms4}
+            if lp is not None:
+                stl = lp.stats()
+                out4.update({"learned_acceptance": stl.accepted / max(stl.proposals, 1.0),
+                             "fallback_active": stl.active == 0})
+                lp.detach()
+            return out4
+        proposals4 = [run4(False, N), run4(True, N), run4(False, 4), run4(True, 4)]
         with open(os.path.join(ROOT, "tests", "golden", "kagome_3x3_e0.json")) as f:
             e0 = json.load(f)["kagome_3x3_pbc_heisenberg"]["E0_per_site"]
         out["cfg4_kagome3x3_mlp108_ns16384"] = {
             "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "num_params": a.P,
             "solve_space": "parameters (N_p = 15014 < N_s = 16384)", "energy_per_site_last": info.mean_energy / N,
             "e0_per_site_recorded_upstream": e0, "factor_solve_phases_us": [round(x, 1) for x in ph],
-            "estimator": "FP64 generic (MLP)", "sampler": "FP64 generic chains"}
+            "kernels_ms_one_step": k4, "plain_vs_learned_proposal": proposals4,
+            "estimator": "FP32 MLP (k_local_mlp32)", "sampler": "FP32 MLP chains (k_sample_mlp32)"}
     nqs.set_options(**base_opts)
     return out
 

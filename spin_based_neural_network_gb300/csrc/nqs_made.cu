@@ -157,6 +157,12 @@ __global__ void __launch_bounds__(POOL_T, 3) k_made_pool(DevMade m, DevAmp A, lo
         // combined in its XOR-butterfly order, so the chains' warp evaluation of
         // the same configuration gives the same number
         const DevAnsatz &a = A.a;
+        if (a.kind != KIND_RBM && a.kind != KIND_CRBM) {    // MLP: the chain evaluates log|psi| itself
+            pbits[e] = x;
+            plq[e] = lq;
+            plpsi[e] = 0.f;
+            continue;
+        }
         for (int l = 0; l < 32; l++) {
             float acc = 0.f;
             for (int h = l; h < a.M; h += 32) {

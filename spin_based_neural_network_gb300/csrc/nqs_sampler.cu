@@ -438,59 +438,123 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_generic(SampleArgs S, DevAm
 }
 
 // FP32 chains of the MLP (mixed precision): the warp keeps the layer-1
-// pre-activations of its configuration in registers; a proposal moves them by
-// one or two weight columns and runs layer 2 against W2^T in shared memory.
-template <int RNG, int MOVE, int MQ>
-__global__ void __launch_bounds__(32 * kSW) k_sample_mlp32(SampleArgs S, DevAmp A) {
+// pre-activations of its configuration in registers; a local proposal moves
+// them by one or two weight columns and runs layer 2 against W2^T in shared
+// memory.  With a learned proposal, its slots (chosen by the random word only)
+// take the chain's next pool entry x' ~ q and accept with min(1, |psi(x')|^2
+// q(s) / (|psi(s)|^2 q(x'))), both log|psi| evaluated from scratch so the ratio
+// uses one function of the configuration.
+template <int MOVE, int MQ, bool LEARNED>
+__global__ void __launch_bounds__(32 * kSW) k_sample_mlp32(SampleArgs S, DevAmp A, DevMade md) {
     if (S.move_dev) S.move0 = *S.move_dev;
-    extern __shared__ float fsm[];
+    extern __shared__ __align__(16) unsigned char smraw[];
     constexpr int MP = 32 * MQ;
     const DevAnsatz &a = A.a;
     const int M = a.M, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float *w2t = fsm, *h1s = fsm + M * MP + warp * MP;
+    float *w2t = (float *)smraw, *h1s = w2t + M * MP + warp * MP;
     {
         const float *g = a.m32 + (long)a.N * M;
         for (int e = threadIdx.x; e < M * MP; e += blockDim.x) w2t[e] = g[e];
+    }
+    const __nv_bfloat16 *Wsm = nullptr;
+    float *mh1 = nullptr, *mh2 = nullptr;
+    uint32_t mix_thr = 0;
+    if (LEARNED) {
+        unsigned char *mb = smraw + sizeof(float) * (size_t)(M * MP + kSW * MP);
+        const long PM = made_off(md.N, md.H).total, wbytes = (PM * 2 + 15) / 16 * 16;
+        __nv_bfloat16 *W = (__nv_bfloat16 *)mb;
+        for (long p = threadIdx.x; p < PM; p += blockDim.x) W[p] = md.w[p];
+        Wsm = W;
+        mh1 = (float *)(mb + wbytes) + (size_t)warp * 2 * md.H;
+        mh2 = mh1 + md.H;
+        mix_thr = *md.active ? md.mix_thr : 0u;
     }
     __syncthreads();
     const int c = blockIdx.x * kSW + warp;
     if (c >= S.C) return;
     uint64_t s = S.bits[c];
     float z1[MQ], nz1[MQ], h1[MQ], h2[MQ], la, ar, nla = 0.f;
-    mlp32_z1<MQ>(a, s, z1);
-    mlp32_forward<MQ>(a, w2t, z1, h1s, h1, h2, la, ar);
-    auto eval = [&](int u, int v) -> double {
+    auto rebuild = [&]() {
+        mlp32_z1<MQ>(a, s, z1);
+        mlp32_forward<MQ>(a, w2t, z1, h1s, h1, h2, la, ar);
+    };
+    rebuild();
+    auto eval = [&](int u, int v) -> float {
         mlp32_z1_flip<MQ>(a, s, u, v, z1, nz1);
         float g;
         mlp32_forward<MQ>(a, w2t, nz1, h1s, h1, h2, nla, g);
-        return (double)(nla - la);
+        return nla - la;
     };
+    bool dirty = true;          // log q of the current configuration not known
+    float lq = 0.f;
+    int used = 0;
     auto commit = [&](int, int) {
 #pragma unroll
         for (int q = 0; q < MQ; q++) z1[q] = nz1[q];
         la = nla;
+        dirty = true;
     };
-    unsigned long long acc = 0, pro = 0;
-    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro);
+    auto learned = [&](const uint4 &r) -> bool {
+        if (!LEARNED || used >= md.per_chain) return false;
+        const long e = (long)c * md.per_chain + used;
+        used++;
+        const uint64_t x2 = md.pbits[e];
+        if (x2 == s) return false;
+        const float lq2 = md.plq[e];
+        float zs[MQ], g1[MQ], g2[MQ], lp, lp2, g;
+        mlp32_z1<MQ>(a, s, zs);
+        mlp32_forward<MQ>(a, w2t, zs, h1s, g1, g2, lp, g);
+        mlp32_z1<MQ>(a, x2, zs);
+        mlp32_forward<MQ>(a, w2t, zs, h1s, g1, g2, lp2, g);
+        if (dirty) {
+            lq = made_logq_warp(md, Wsm, s, mh1, mh2);
+            dirty = false;
+        }
+        const float lr = 2.f * (lp2 - lp) + lq - lq2;
+        bool accept = lr >= 0.f;
+        if (!accept) {
+            const float uni = ((float)(r.z >> 8) + 0.5f) * (1.f / 16777216.f);
+            accept = __logf(uni) < lr;
+        }
+        if (accept) {
+            s = x2;
+            lq = lq2;
+            rebuild();
+        }
+        return accept;
+    };
+    unsigned long long acc = 0, pro = 0, lacc = 0, lpro = 0;
+    run_chain32<MOVE, LEARNED>(S, c, s, eval, commit, learned, mix_thr, acc, pro, lacc, lpro);
     if (lane == 0) {
         S.bits[c] = s;
         atomicAdd(&S.counts[0], acc);
         atomicAdd(&S.counts[1], pro);
+        if (LEARNED) {
+            atomicAdd(&S.counts[2], lpro);
+            atomicAdd(&S.counts[3], lacc);
+        }
     }
 }
 
-template <int RNG, int MOVE>
-static bool launch_mlp32_chains(const SampleArgs &S, const DevAmp &A, dim3 grid, dim3 block, cudaStream_t st) {
+template <int MOVE>
+static bool launch_mlp32_chains(const SampleArgs &S, const DevAmp &A, const DevMade &md, size_t made_smem,
+                                dim3 grid, dim3 block, cudaStream_t st) {
     const int MQ = (A.a.M + 31) / 32, MP = 32 * MQ;
-    const size_t smem = sizeof(float) * ((size_t)A.a.M * MP + (size_t)kSW * MP);
+    const bool learned = md.per_chain > 0;
+    const size_t smem = sizeof(float) * ((size_t)A.a.M * MP + (size_t)kSW * MP) + (learned ? made_smem : 0);
 #define NQS_MCASE(QQ)                                                                                        \
     case QQ: {                                                                                               \
         static bool attr = false;                                                                            \
-        if (!attr && !NQS_CUDA(cudaFuncSetAttribute(k_sample_mlp32<RNG, MOVE, QQ>,                           \
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024))) \
-            return false;                                                                                    \
-        attr = true;                                                                                         \
-        k_sample_mlp32<RNG, MOVE, QQ><<<grid, block, smem, st>>>(S, A);                                       \
+        if (!attr) {                                                                                         \
+            if (!NQS_CUDA(cudaFuncSetAttribute(k_sample_mlp32<MOVE, QQ, false>,                              \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) ||  \
+                !NQS_CUDA(cudaFuncSetAttribute(k_sample_mlp32<MOVE, QQ, true>,                               \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)))    \
+                return false;                                                                                \
+            attr = true;                                                                                     \
+        }                                                                                                    \
+        if (learned) k_sample_mlp32<MOVE, QQ, true><<<grid, block, smem, st>>>(S, A, md);                    \
+        else k_sample_mlp32<MOVE, QQ, false><<<grid, block, smem, st>>>(S, A, md);                           \
         break;                                                                                               \
     }
     switch (MQ) {
@@ -555,8 +619,8 @@ static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32, const DevMa
     cudaStream_t st = ctx().stream;
     const bool fused = A.G == 0 && (A.a.kind == KIND_RBM || A.a.kind == KIND_CRBM);
     if (f32 && RNG == NQS_GPU_RNG_PHILOX && fp32_mlp_capable(A)) {
-        NQS_LAUNCH("sampler_mlp32");
-        return launch_mlp32_chains<RNG, MOVE>(S, A, grid, block, st);
+        NQS_LAUNCH(md.per_chain > 0 ? "sampler_mlp32_learned" : "sampler_mlp32");
+        return launch_mlp32_chains<MOVE>(S, A, md, smem, grid, block, st);
     }
     if (f32 && RNG == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
         const int J = (A.a.M + 31) / 32;
@@ -630,7 +694,7 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out, unsigned long 
     const bool f32 = sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator;
     DevMade md{};
     size_t smem = 0;
-    if (sm->made && !move_dev && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && fp32_capable(A)) {
+    if (sm->made && !move_dev && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && (fp32_capable(A) || fp32_mlp_capable(A))) {
         if (!made_prepare(sm->made, A, sm->C, S.total, sm->cfg.rng_seed ^ 0x9E3779B97F4A7C15ull, &md)) return false;
         smem = made_chain_smem(sm->made, kSW);
     }
@@ -884,8 +948,8 @@ int nqs_sampler_set_learned_proposal(nqs_sampler_t *h, const nqs_gpu_made_option
     }
     DevAmp A;
     if (!build_amp(s->fn, s->user, s->N, &A, nullptr)) return -1;
-    if (!fp32_capable(A)) {
-        set_error("learned proposal needs an RBM / cRBM program without symmetry projection");
+    if (!fp32_capable(A) && !fp32_mlp_capable(A)) {
+        set_error("learned proposal needs an RBM / cRBM or MLP program without symmetry projection");
         return -1;
     }
     const int n_ones = s->opts.move == NQS_GPU_MOVE_EXCHANGE && s->opts.n_down >= 0 ? s->opts.n_down : -1;
