@@ -520,11 +520,12 @@ def other_configs(nqs, abi, L, base_opts, which):
             es.append(info.mean_energy)
             return info
         ms, info = timed_steps(nqs, L, step1, 3, 197)
+        k1 = step_kernels(nqs, step1)
         with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
             e0 = json.load(f)["tfim_chain16_pbc_h1"]["E0_per_site"]
         run = float(np.mean(es[-20:])) / N
         out["cfg1_tfim16_cgsr_fp64"] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "steps": 200,
-                                        "cg_iterations_last": info.cg_iterations,
+                                        "cg_iterations_last": info.cg_iterations, "kernels_ms_one_step": k1,
                                         "energy_per_site_last20": run, "e0_per_site": e0,
                                         "abs_err_per_site": abs(run - e0)}
     if "3" in which:

@@ -140,8 +140,9 @@ int nqs_gpu_made_sample(nqs_sampler_t *s, int count, int *out_spins, double *out
  * factor breaks down is solved again in FP64 on the same samples after the
  * graph (as nqs_sr_step_minsr_full does in the MIXED mode);
  * nqs_gpu_batch_fallbacks counts those instance steps.
- * The samplers advance as in nqs_sampler_batch (no learned proposal inside a
- * batch).  infos (optional) receives count step infos. */
+ * The samplers advance as in nqs_sampler_batch, with their learned proposal
+ * when one is attached (pool draws, training and fallback are replayable from
+ * the graph).  infos (optional) receives count step infos. */
 typedef struct {
     const nqs_config_t *cfg;      /* Hamiltonian, couplings, num_samples, shift, learning rate */
     int size_x, size_y;           /* lattice */

@@ -35,9 +35,13 @@ struct Made {
     DevBuf<int> active;
     DevBuf<double> stats;            // [0] mean NLL of the last batch [1] proposals [2] accepted
                                      // [3] probe countdown [4] prev proposals [5] prev accepted
-    int t_adam = 0;
-    uint32_t launch_id = 0;
+    // device counters ([0] pool draws, [1] Adam steps), so that a sampler
+    // launch replayed from a CUDA graph still draws a fresh pool and applies the
+    // right bias corrections
+    DevBuf<unsigned> ctr;
 };
+
+__global__ void k_made_count(unsigned *c) { *c += 1u; }
 
 static inline uint64_t splitmix64(uint64_t &s) {
     uint64_t z = (s += 0x9E3779B97F4A7C15ull);
@@ -94,10 +98,12 @@ __device__ __forceinline__ float made_h2_reg(const __nv_bfloat16 *W, const __nv_
 constexpr int POOL_T = 128;
 
 template <int H, bool CPLX>
-__global__ void __launch_bounds__(POOL_T, 3) k_made_pool(DevMade m, DevAmp A, long total, uint64_t seed, uint32_t launch,
+__global__ void __launch_bounds__(POOL_T, 3) k_made_pool(DevMade m, DevAmp A, long total, uint64_t seed,
+                                                      const unsigned *__restrict__ launch_ctr,
                                                       uint64_t *pbits, float *plq, float *plpsi) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (*m.active == 0) return;
+    const uint32_t launch = *launch_ctr;
     const int N = m.N, tid = threadIdx.x;
     const MadeOff o = made_off(N, H);
     __nv_bfloat16 *W = (__nv_bfloat16 *)smraw;
@@ -276,10 +282,12 @@ __global__ void k_made_grad(DevMade m, const uint64_t *__restrict__ bits, int B,
 // Sum of the warp partials (fixed order) / B, masked; with lr > 0 an Adam step
 // on the masters and a new BF16 copy, else the gradient itself into `out`.
 __global__ void k_made_adam(float *w, float *m1, float *v1, const float *__restrict__ partials, int nw, long PM,
-                            int N, int H, float inv_b, float lr, float bc1, float bc2, __nv_bfloat16 *wb,
-                            float *out) {
+                            int N, int H, float inv_b, float lr, const unsigned *__restrict__ t_ctr,
+                            __nv_bfloat16 *wb, float *out) {
     const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= PM) return;
+    const float tt = (float)(*t_ctr + 1u);                   // this Adam step
+    const float bc1 = 1.f - powf(0.9f, tt), bc2 = 1.f - powf(0.999f, tt);
     float g = 0.f;
     for (int q = 0; q < nw; q++) g += partials[(size_t)q * PM + p];
     g = made_kept(p, N, H) ? g * inv_b : 0.f;
@@ -362,7 +370,8 @@ Made *made_create(int N, int n_ones, const nqs_gpu_made_options_t &opt) {
     double zs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int one = 1;
     if (!m->master.ensure(o.total) || !m->m1.ensure(o.total) || !m->v1.ensure(o.total) || !m->wb.ensure(o.total) ||
-        !m->active.ensure(1) || !m->stats.ensure(8) ||
+        !m->active.ensure(1) || !m->stats.ensure(8) || !m->ctr.ensure(2) ||
+        !NQS_CUDA(cudaMemsetAsync(m->ctr.p, 0, 2 * sizeof(unsigned), s)) ||
         !NQS_CUDA(cudaMemcpyAsync(m->master.p, w.data(), sizeof(float) * o.total, cudaMemcpyHostToDevice, s)) ||
         !NQS_CUDA(cudaMemsetAsync(m->m1.p, 0, sizeof(float) * o.total, s)) ||
         !NQS_CUDA(cudaMemsetAsync(m->v1.p, 0, sizeof(float) * o.total, s)) ||
@@ -415,9 +424,10 @@ static void pool_kernel(const Made *m, unsigned grid, size_t smem, const DevMade
         attr = true;
     }
     if (A.a.kind == KIND_CRBM)
-        k_made_pool<H, true><<<grid, POOL_T, smem, ctx().stream>>>(d, A, count, seed, m->launch_id, pbits, plq, plpsi);
+        k_made_pool<H, true><<<grid, POOL_T, smem, ctx().stream>>>(d, A, count, seed, m->ctr.p, pbits, plq, plpsi);
     else
-        k_made_pool<H, false><<<grid, POOL_T, smem, ctx().stream>>>(d, A, count, seed, m->launch_id, pbits, plq, plpsi);
+        k_made_pool<H, false><<<grid, POOL_T, smem, ctx().stream>>>(d, A, count, seed, m->ctr.p, pbits, plq, plpsi);
+    k_made_count<<<1, 1, 0, ctx().stream>>>(m->ctr.p);
 }
 
 // Draw `count` proposals into the pool (count = chains x per_chain).
@@ -437,7 +447,6 @@ static bool pool_launch(Made *m, const DevAmp &A, long count, uint64_t seed, Dev
         case 96: pool_kernel<96>(m, grid, smem, d, A, count, seed, m->plq.p, m->plpsi.p, m->pbits.p); break;
         default: pool_kernel<128>(m, grid, smem, d, A, count, seed, m->plq.p, m->plpsi.p, m->pbits.p); break;
     }
-    m->launch_id++;
     return NQS_CUDA(cudaGetLastError());
 }
 
@@ -501,13 +510,12 @@ bool made_train(Made *m, const uint64_t *bits, int B, const unsigned long long *
     for (int it = 0; it < m->opt.train_iters; it++) {
         nw = grad_launch(m, bits, B);
         if (nw < 0) return false;
-        m->t_adam++;
-        const float bc1 = 1.f - powf(0.9f, (float)m->t_adam), bc2 = 1.f - powf(0.999f, (float)m->t_adam);
         NQS_LAUNCH("made_adam");
         k_made_adam<<<(unsigned)((m->PM + 255) / 256), 256, 0, s>>>(m->master.p, m->m1.p, m->v1.p, m->partials.p, nw,
                                                                    m->PM, m->N, m->H, 1.f / (float)B,
-                                                                   (float)m->opt.learning_rate, bc1, bc2, m->wb.p,
+                                                                   (float)m->opt.learning_rate, m->ctr.p + 1, m->wb.p,
                                                                    nullptr);
+        k_made_count<<<1, 1, 0, s>>>(m->ctr.p + 1);
     }
     {
         // nw = 0 (no training): acceptance bookkeeping and fallback only
@@ -520,7 +528,9 @@ bool made_train(Made *m, const uint64_t *bits, int B, const unsigned long long *
 bool made_stats_read(const Made *m, nqs_gpu_made_stats_t *out) {
     double h[8];
     int act = 0;
+    unsigned ctr[2] = {0, 0};
     if (!NQS_CUDA(cudaMemcpyAsync(h, m->stats.p, sizeof(h), cudaMemcpyDeviceToHost, ctx().stream)) ||
+        !NQS_CUDA(cudaMemcpyAsync(ctr, m->ctr.p, sizeof(ctr), cudaMemcpyDeviceToHost, ctx().stream)) ||
         !NQS_CUDA(cudaMemcpyAsync(&act, m->active.p, sizeof(int), cudaMemcpyDeviceToHost, ctx().stream)) ||
         !NQS_CUDA(cudaStreamSynchronize(ctx().stream)))
         return false;
@@ -528,7 +538,7 @@ bool made_stats_read(const Made *m, nqs_gpu_made_stats_t *out) {
     out->proposals = h[1];
     out->accepted = h[2];
     out->active = act;
-    out->train_steps = m->t_adam;
+    out->train_steps = (int)ctr[1];
     return true;
 }
 
@@ -570,7 +580,7 @@ bool made_grad(Made *m, const uint64_t *bits, int B, float *out_grad, double *ou
     static DevBuf<float> g;
     if (!g.ensure((size_t)m->PM)) return false;
     k_made_adam<<<(unsigned)((m->PM + 255) / 256), 256, 0, ctx().stream>>>(
-        m->master.p, m->m1.p, m->v1.p, m->partials.p, nw, m->PM, m->N, m->H, 1.f / (float)B, 0.f, 1.f, 1.f, m->wb.p,
+        m->master.p, m->m1.p, m->v1.p, m->partials.p, nw, m->PM, m->N, m->H, 1.f / (float)B, 0.f, m->ctr.p + 1, m->wb.p,
         g.p);
     std::vector<float> nl((size_t)nw);
     if (!NQS_CUDA(cudaMemcpyAsync(out_grad, g.p, sizeof(float) * m->PM, cudaMemcpyDeviceToHost, ctx().stream)) ||

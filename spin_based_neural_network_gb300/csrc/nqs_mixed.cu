@@ -134,8 +134,9 @@ __global__ void k_center_split(double *O, int Ns, long P, const double *__restri
         size_t i = t / P, k = t % P;
         double x = O[t] - gm[k];
         O[t] = x;
-        float h = tf32_rna((float)x);
-        float l = tf32_rna((float)(x - (double)h));
+        const float xf = (float)x;                  // x - xf (2^-24 relative) is below the split's 2^-21
+        float h = tf32_rna(xf);
+        float l = tf32_rna(xf - h);
         hi[i * ldp + k] = h;
         lo[i * ldp + k] = l;
     }
@@ -1464,8 +1465,9 @@ __global__ void k_center_split_t(double *O, int Ns, long P, const double *__rest
             if (i < Ns && k < P) {
                 const double x = O[i * P + k] - gm[k];
                 O[i * P + k] = x;
-                h = tf32_rna((float)x);
-                l = tf32_rna((float)(x - (double)h));
+                const float xf = (float)x;
+                h = tf32_rna(xf);
+                l = tf32_rna(xf - h);
             }
             th[r][tx] = h;
             tl[r][tx] = l;

@@ -694,7 +694,7 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out, unsigned long 
     const bool f32 = sm->opts.precision == NQS_GPU_PREC_MIXED && sm->opts.fp32_estimator;
     DevMade md{};
     size_t smem = 0;
-    if (sm->made && !move_dev && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && (fp32_capable(A) || fp32_mlp_capable(A))) {
+    if (sm->made && f32 && sm->opts.rng == NQS_GPU_RNG_PHILOX && (fp32_capable(A) || fp32_mlp_capable(A))) {
         if (!made_prepare(sm->made, A, sm->C, S.total, sm->cfg.rng_seed ^ 0x9E3779B97F4A7C15ull, &md)) return false;
         smem = made_chain_smem(sm->made, kSW);
     }
@@ -724,6 +724,9 @@ bool sampler_produce_dev(Sampler *sm, int n, uint64_t **d_out, unsigned long lon
     if (!sampler_run(sm, 0, n, sm->d_samples.p, move_dev)) return false;
     sm->move_counter = host;
     k_move_advance<<<1, 1, 0, ctx().stream>>>(move_dev, (unsigned long long)sampler_moves(sm, n));
+    // online training of the learned proposal (its counters are on the device,
+    // so this is replayable from a graph)
+    if (sm->made && !made_train(sm->made, sm->d_samples.p, n, sm->d_counts.p)) return false;
     *d_out = sm->d_samples.p;
     return NQS_CUDA(cudaGetLastError());
 }

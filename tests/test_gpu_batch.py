@@ -117,3 +117,32 @@ def test_batch_fp32_breakdown_falls_back_to_fp64(nqs):
         B.free()
     finally:
         nqs.set_options()
+
+
+def test_batch_with_learned_proposals_matches_single_steps(nqs):
+    """Learned proposals attached to the instances' samplers: the pool draws,
+    training and fallback run inside the batch graph (device counters), and the
+    batch still equals the same instances stepped one by one."""
+    from spin_based_neural_network_gb300 import abi
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, fp32_estimator=1, refine_sweeps=5, gram_passes=3)
+    cases = CASES[:2]
+    try:
+        bat = [build(nqs, abi, c, 500 + i) for i, c in enumerate(cases)]
+        ref = [build(nqs, abi, c, 500 + i) for i, c in enumerate(cases)]
+        lps = [nqs.LearnedProposal(b["s"], hidden=32, mix=0.5) for b in bat + ref]
+        B = nqs.Batch([(b["cfg"], b["Lx"], b["Ly"], b["a"], b["s"], b["fn"], b["user"]) for b in bat])
+        for step in range(4):
+            infos = B.step()
+            for i, r in enumerate(ref):
+                info = nqs.sr_step_minsr(r["cfg"], r["Lx"], r["Ly"], r["a"], r["s"],
+                                         r["fn"] if r["fn"] else r["a"].log_amp_fn,
+                                         r["user"] if r["user"] else r["a"].user)
+                assert infos[i].mean_energy == pytest.approx(info.mean_energy, rel=1e-12, abs=1e-12), (step, i)
+                pb, pr = bat[i]["a"].params, r["a"].params
+                assert np.max(np.abs(pb - pr)) <= 1e-12 * max(1.0, np.max(np.abs(pr))), (step, i)
+        for lp in lps[:len(cases)]:
+            st = lp.stats()
+            assert st.proposals > 0 and st.accepted > 0 and st.train_steps >= 4
+        B.free()
+    finally:
+        nqs.set_options()
