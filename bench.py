@@ -400,7 +400,7 @@ def batch_objects(nqs, abi, spec, lr=0.02, shift=1e-3):
             "Lx": Lx, "Ly": Ly, "spec": spec}
 
 
-def multi_instance(nqs, abi, L, base_opts, timed, total):
+def multi_instance(nqs, abi, L, base_opts, timed, total, learned=False):
     """The 64-instance workload stepped as one batch (nqs_gpu_batch_step): one
     cooperative launch for all solves with an autotuned CTA split, the whole
     batch step replayed as a CUDA graph from the second step.  Throughput over
@@ -412,6 +412,8 @@ def multi_instance(nqs, abi, L, base_opts, timed, total):
     nqs.set_options(**base_opts)
     specs = batch_instances()
     objs = [batch_objects(nqs, abi, sp) for sp in specs]
+    # learned proposals (MADE width 64, BF16, mix 0.5, trained online inside the batch graph)
+    lps = [nqs.LearnedProposal(o["s"], hidden=64, mix=0.5) for o in objs] if learned else []
     for o in objs:
         o["s"].thermalize()
     bt = nqs.Batch([(o["cfg"], o["Lx"], o["Ly"], o["a"], o["s"], o["fn"], o["user"]) for o in objs])
@@ -447,7 +449,11 @@ def multi_instance(nqs, abi, L, base_opts, timed, total):
            "abs_err_per_site_median": float(np.median(ev)), "abs_err_per_site_max": float(np.max(ev)),
            "within_1e-2": int(np.sum(ev <= 1e-2)), "within_1e-3": int(np.sum(ev <= 1e-3)),
            "converged_last_step": int(sum(i.converged for i in infos)) if infos else None,
-           "fp64_fallback_instance_steps": bt.fallbacks()}
+           "fp64_fallback_instance_steps": bt.fallbacks(), "learned_proposals": learned}
+    if lps:
+        sts = [lp.stats() for lp in lps]
+        out["learned_acceptance_mean"] = float(np.mean([s.accepted / max(s.proposals, 1.0) for s in sts]))
+        out["learned_fallback_active"] = int(sum(s.active == 0 for s in sts))
     bt.free()
     nqs.set_options(**base_opts)
     return out
@@ -763,9 +769,10 @@ def run_gpu(args):
     if prec == abi.PREC_MIXED and args.configs:
         others = other_configs(nqs, abi, L, base_opts, args.configs)
 
-    multi = None
+    multi = multi_learned = None
     if prec == abi.PREC_MIXED and args.batch_steps > 0:
         multi = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps)
+        multi_learned = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps, learned=True)
 
     conv = None
     if args.converge_steps > 0:
@@ -795,7 +802,8 @@ def run_gpu(args):
                     "d2h_bytes_per_step": 8 * P + 16 * 8},
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
             "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
-            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi, "other_configs": others,
+            "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi, "multi_instance_learned": multi_learned,
+            "other_configs": others,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
