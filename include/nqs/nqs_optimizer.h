@@ -114,6 +114,55 @@ int nqs_sr_run_minsr(const nqs_config_t *cfg,
                       void *log_amp_user,
                       double *out_energy_trace);
 
+/* Holomorphic-gradient callback (upstream include/nqs/nqs_optimizer.h:155-159).
+ * The GPU step accepts NULL only (the base ansatz's complex gradient). */
+typedef int (*nqs_holomorphic_gradient_fn_t)(void *grad_user,
+                                              nqs_ansatz_t *ansatz,
+                                              const int *spins, int num_sites,
+                                              double *out_re,
+                                              double *out_im);
+
+/* Replaces upstream nqs_sr_step_holomorphic (include/nqs/nqs_optimizer.h:135):
+ * CG on the complex QGT G = 2 Re{<O* O> - <O*><O>} with complex local energies. */
+int nqs_sr_step_holomorphic(const nqs_config_t *cfg,
+                             int size_x, int size_y,
+                             nqs_ansatz_t *ansatz,
+                             nqs_sampler_t *sampler,
+                             nqs_log_amp_fn_t log_amp_fn,
+                             void *log_amp_user,
+                             nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run_holomorphic (include/nqs/nqs_optimizer.h:143). */
+int nqs_sr_run_holomorphic(const nqs_config_t *cfg,
+                            int size_x, int size_y,
+                            nqs_ansatz_t *ansatz,
+                            nqs_sampler_t *sampler,
+                            nqs_log_amp_fn_t log_amp_fn,
+                            void *log_amp_user,
+                            double *out_energy_trace);
+
+/* Replaces upstream nqs_sr_step_holomorphic_full (include/nqs/nqs_optimizer.h:168). */
+int nqs_sr_step_holomorphic_full(const nqs_config_t *cfg,
+                                  int size_x, int size_y,
+                                  nqs_ansatz_t *ansatz,
+                                  nqs_sampler_t *sampler,
+                                  nqs_log_amp_fn_t log_amp_fn,
+                                  void *log_amp_user,
+                                  nqs_holomorphic_gradient_fn_t grad_fn,
+                                  void *grad_user,
+                                  nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run_holomorphic_full (include/nqs/nqs_optimizer.h:178). */
+int nqs_sr_run_holomorphic_full(const nqs_config_t *cfg,
+                                 int size_x, int size_y,
+                                 nqs_ansatz_t *ansatz,
+                                 nqs_sampler_t *sampler,
+                                 nqs_log_amp_fn_t log_amp_fn,
+                                 void *log_amp_user,
+                                 nqs_holomorphic_gradient_fn_t grad_fn,
+                                 void *grad_user,
+                                 double *out_energy_trace);
+
 #ifdef __cplusplus
 }
 #endif

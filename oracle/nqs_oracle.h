@@ -138,6 +138,14 @@ int oracle_cgsr_step(const or_ham_t *h, const or_amp_t *amp, int grad_mode,
                      const int *batch, int Ns, double shift, double lr,
                      int max_iters, double tol, double *params_inout, long P,
                      double *out_energies, double *out_delta, or_step_info_t *info);
+/* Holomorphic SR, src/nqs/nqs_optimizer.c:415-524 (qgt_complex_apply :317-356,
+ * cg_solve_complex :358-401): complex local energies, complex gradient of the
+ * base ansatz, F = 2 [(R^T E_re + I^T E_im) / N_s - <R> <E_re> - <I> <E_im>],
+ * CG on G v = 2 [(R^T R v + I^T I v) / N_s - <R> <R.v> - <I> <I.v>] + eps v. */
+int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns,
+                     double shift, double lr, int max_iters, double tol,
+                     double *params_inout, long P, double *out_energies,
+                     double *out_delta, or_step_info_t *info);
 
 /* Exact ground-state energy by Lanczos with full re-orthogonalisation (the
  * upstream src/mps/lanczos.c:119-303 scheme) over either the full 2^N basis

@@ -381,6 +381,90 @@ int oracle_cgsr_step(const or_ham_t *h, const or_amp_t *amp, int grad_mode,
     return 0;
 }
 
+/* Holomorphic SR: the step of src/nqs/nqs_optimizer.c:415-524 on a given
+ * batch.  G v (qgt_complex_apply, :317-356) and the CG (cg_solve_complex,
+ * :358-401) as upstream. */
+static void qgt_complex_apply(const double *R, const double *I, long Ns, long P, const double *Rm,
+                              const double *Im, double eps, const double *v, double *out,
+                              double *uR, double *uI) {
+    for (long i = 0; i < Ns; i++) {
+        double sR = 0.0, sI = 0.0;
+        for (long k = 0; k < P; k++) {
+            sR += R[i * P + k] * v[k];
+            sI += I[i * P + k] * v[k];
+        }
+        uR[i] = sR; uI[i] = sI;
+    }
+    double mR = 0.0, mI = 0.0;
+    for (long i = 0; i < Ns; i++) { mR += uR[i]; mI += uI[i]; }
+    mR /= (double)Ns; mI /= (double)Ns;
+    for (long k = 0; k < P; k++) {
+        double aR = 0.0, aI = 0.0;
+        for (long i = 0; i < Ns; i++) {
+            aR += R[i * P + k] * uR[i];
+            aI += I[i * P + k] * uI[i];
+        }
+        out[k] = 2.0 * ((aR + aI) / (double)Ns - Rm[k] * mR - Im[k] * mI) + eps * v[k];
+    }
+}
+
+int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns,
+                     double shift, double lr, int max_iters, double tol,
+                     double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
+    double *Er = malloc(sizeof(double) * (size_t)Ns), *Ei = malloc(sizeof(double) * (size_t)Ns);
+    double *R = malloc(sizeof(double) * (size_t)Ns * P), *I = malloc(sizeof(double) * (size_t)Ns * P);
+    double *Rm = calloc((size_t)P, sizeof(double)), *Im = calloc((size_t)P, sizeof(double));
+    double *F = calloc((size_t)P, sizeof(double)), *d = calloc((size_t)P, sizeof(double));
+    double *r = malloc(sizeof(double) * (size_t)P), *p = malloc(sizeof(double) * (size_t)P);
+    double *Ap = malloc(sizeof(double) * (size_t)P);
+    double *uR = malloc(sizeof(double) * (size_t)Ns), *uI = malloc(sizeof(double) * (size_t)Ns);
+    oracle_local_energy_batch(h, amp, batch, Ns, Er, Ei);               /* :455-456 */
+    if (oracle_gradient_complex_batch(&amp->base, batch, Ns, R, I)) return -1;   /* :458-469 */
+    double erm = 0.0, eim = 0.0, ersq = 0.0;                           /* :471-481 */
+    for (int i = 0; i < Ns; i++) { erm += Er[i]; eim += Ei[i]; ersq += Er[i] * Er[i]; }
+    erm /= (double)Ns; eim /= (double)Ns; ersq /= (double)Ns;
+    for (long k = 0; k < P; k++) {                                     /* :483-498 */
+        double sR = 0.0, sI = 0.0, sRe = 0.0, sIe = 0.0;
+        for (int i = 0; i < Ns; i++) {
+            double rk = R[(size_t)i * P + k], ik = I[(size_t)i * P + k];
+            sR += rk; sI += ik; sRe += rk * Er[i]; sIe += ik * Ei[i];
+        }
+        Rm[k] = sR / (double)Ns;
+        Im[k] = sI / (double)Ns;
+        F[k] = 2.0 * ((sRe + sIe) / (double)Ns - Rm[k] * erm - Im[k] * eim);
+    }
+    memcpy(r, F, sizeof(double) * (size_t)P);                          /* cg_solve_complex */
+    memcpy(p, r, sizeof(double) * (size_t)P);
+    double rs_old = vdot(r, r, P), rs0 = rs_old;
+    int it, conv = 0;
+    for (it = 0; it < max_iters; it++) {
+        qgt_complex_apply(R, I, Ns, P, Rm, Im, shift, p, Ap, uR, uI);
+        double pAp = vdot(p, Ap, P);
+        if (!(fabs(pAp) >= 1e-30)) break;
+        double alpha = rs_old / pAp;
+        for (long k = 0; k < P; k++) d[k] += alpha * p[k];
+        for (long k = 0; k < P; k++) r[k] += -alpha * Ap[k];
+        double rs_new = vdot(r, r, P);
+        if (rs_new <= tol * tol * rs0) { conv = 1; it++; break; }
+        double beta = rs_new / rs_old;
+        for (long k = 0; k < P; k++) p[k] = r[k] + beta * p[k];
+        rs_old = rs_new;
+    }
+    for (long k = 0; k < P; k++) params[k] += -lr * d[k];             /* :503 */
+    if (info) {
+        info->mean_energy = erm;
+        info->variance_energy = ersq - erm * erm;
+        info->update_norm = sqrt(vdot(d, d, P)) * lr;
+        info->cg_iterations = it;
+        info->converged = conv;
+    }
+    if (out_E) memcpy(out_E, Er, sizeof(double) * (size_t)Ns);
+    if (out_delta) memcpy(out_delta, d, sizeof(double) * (size_t)P);
+    free(Er); free(Ei); free(R); free(I); free(Rm); free(Im); free(F); free(d);
+    free(r); free(p); free(Ap); free(uR); free(uI);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* Exact ground-state energy                                            */
 /* ------------------------------------------------------------------ */

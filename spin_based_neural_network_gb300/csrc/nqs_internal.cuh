@@ -189,7 +189,8 @@ bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
 // CG-SR solve (S + eps I) d = F in one cooperative launch (upstream cg_solve
 // semantics); writes d, scal[S_RS, S_RS0, S_PAP], status[I_DONE, I_ITERS, I_CONV].
 bool cg_sr_solve(const double *O, int Ns, long P, const double *F, const double *gm, double eps, double tol,
-                 int max_iters, double *d, double *scal, int *status);
+                 int max_iters, double *d, double *scal, int *status, const double *O2 = nullptr,
+                 const double *gm2 = nullptr, double fac = 1.0);
 
 // Relative residual |r| / |rhs| above which a mixed solve counts as broken down
 // and the step is solved again in FP64.

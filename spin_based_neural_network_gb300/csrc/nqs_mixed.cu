@@ -1749,15 +1749,20 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
 // reduce) and the vector updates separated by bounded grid barriers, with the
 // scalars from dot_all so every CTA takes the same branches.  Upstream
 // semantics: d0 = 0, r0 = p0 = F; stop when r.r <= tol^2 r0.r0 (converged) or
-// |p.Ap| < 1e-30 (Krylov breakdown, unconverged) or after max_iters.
+// |p.Ap| < 1e-30 (Krylov breakdown, unconverged) or after max_iters.  With a
+// second matrix O2 (the imaginary part I of a complex O = R + i I) the operator
+// is the holomorphic one, G v = fac [(R^T R v + I^T I v) / N_s - <R> (<R>.v)
+// - <I> (<I>.v)] + eps v (src/nqs/nqs_optimizer.c:317-356, fac = 2).
 struct CgArgs {
     const double *O;      // [N_s][N_p] (uncentred)
     int Ns;
     long P;
     const double *F, *gm; // force, column means
+    const double *O2, *gm2;   // optional second matrix and its column means
+    double fac;               // operator factor (1 real, 2 holomorphic)
     double eps, tol;
     int max_iters;
-    double *d, *r, *p, *Ap, *u, *upart;
+    double *d, *r, *p, *Ap, *u, *upart, *u2, *upart2;
     double *scal;         // S_RS, S_RS0, S_PAP
     int *status;          // I_DONE, I_ITERS, I_CONV
     unsigned *bar;
@@ -1782,30 +1787,42 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_cg_sr(CgArgs a) {
     double pap_last = 0.0;
     if (!grid_barrier(a.bar, a.err, G)) return;
     for (; it < a.max_iters; it++) {
-        // u = O p
+        // u = O p (and u2 = O2 p)
         for (int i = gwarp; i < Ns; i += gwarps) {
             const double v = rowdot<true>(a.O + (size_t)i * P, P, a.p, lane);
             if (lane == 0) a.u[i] = v;
+            if (a.O2) {
+                const double v2 = rowdot<true>(a.O2 + (size_t)i * P, P, a.p, lane);
+                if (lane == 0) a.u2[i] = v2;
+            }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         colsum_partial(a.O, Ns, P, a.u, a.upart, gwarp, gwarps, lane);
-        // <u> (the same in every CTA)
-        double um;
-        {
+        if (a.O2) colsum_partial(a.O2, Ns, P, a.u2, a.upart2, gwarp, gwarps, lane);
+        // <u>, <u2> (the same in every CTA)
+        auto mean_all = [&](const double *v) {
             double sacc = 0.0;
-            for (int i = tid; i < Ns; i += PS_THREADS) sacc += __ldcg(a.u + i);
+            for (int i = tid; i < Ns; i += PS_THREADS) sacc += __ldcg(v + i);
             sacc = warp_sum(sacc);
             __syncthreads();
             if (lane == 0) red[tid >> 5] = sacc;
             __syncthreads();
-            um = 0.0;
-            for (int w = 0; w < PS_THREADS / 32; w++) um += red[w];
-            um /= (double)Ns;
-        }
+            double m = 0.0;
+            for (int w = 0; w < PS_THREADS / 32; w++) m += red[w];
+            return m / (double)Ns;
+        };
+        const double um = mean_all(a.u), um2 = a.O2 ? mean_all(a.u2) : 0.0;
         if (!grid_barrier(a.bar, a.err, G)) return;
         for (long k = gwarp; k < P; k += gwarps) {
-            const double sk = colsum_reduce(a.upart, Ns, P, k, lane);
-            if (lane == 0) a.Ap[k] = sk / (double)Ns - __ldcg(a.gm + k) * um + a.eps * __ldcg(a.p + k);
+            double sk = colsum_reduce(a.upart, Ns, P, k, lane);
+            if (a.O2) {
+                const double sk2 = colsum_reduce(a.upart2, Ns, P, k, lane);
+                if (lane == 0)
+                    a.Ap[k] = a.fac * ((sk + sk2) / (double)Ns - __ldcg(a.gm + k) * um - __ldcg(a.gm2 + k) * um2) +
+                              a.eps * __ldcg(a.p + k);
+            } else if (lane == 0) {
+                a.Ap[k] = sk / (double)Ns - __ldcg(a.gm + k) * um + a.eps * __ldcg(a.p + k);
+            }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         const double pap = dot_all(a.p, a.Ap, np, red);
@@ -1843,19 +1860,22 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_cg_sr(CgArgs a) {
 }
 
 bool cg_sr_solve(const double *O, int Ns, long P, const double *F, const double *gm, double eps, double tol,
-                 int max_iters, double *d, double *scal, int *status) {
+                 int max_iters, double *d, double *scal, int *status, const double *O2, const double *gm2,
+                 double fac) {
     Context &c = ctx();
     cudaStream_t st = c.stream;
-    static DevBuf<double> r, p, Ap, u, upart;
+    static DevBuf<double> r, p, Ap, u, upart, u2, upart2;
     static DevBuf<unsigned> bar;
     static DevBuf<int> err;
     if (!r.ensure(P) || !p.ensure(P) || !Ap.ensure(P) || !u.ensure(Ns) ||
-        !upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !bar.ensure(2) || !err.ensure(1))
+        !upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !bar.ensure(2) || !err.ensure(1) ||
+        (O2 && (!u2.ensure(Ns) || !upart2.ensure((size_t)((Ns + RCH - 1) / RCH) * P))))
         return false;
     if (!NQS_CUDA(cudaMemsetAsync(bar.p, 0, 2 * sizeof(unsigned), st)) ||
         !NQS_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st)))
         return false;
-    CgArgs a{O, Ns, P, F, gm, eps, tol, max_iters, d, r.p, p.p, Ap.p, u.p, upart.p, scal, status, bar.p, err.p};
+    CgArgs a{O,   Ns,  P,   F,    gm,      O2,   gm2,      fac,  eps,   tol,   max_iters, d,
+             r.p, p.p, Ap.p, u.p, upart.p, u2.p, upart2.p, scal, status, bar.p, err.p};
     int per_sm = 0;
     if (!NQS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_sr, PS_THREADS, 0))) return false;
     if (per_sm < 1) {

@@ -23,6 +23,7 @@ bool sampler_produce(Sampler *s, int n, uint64_t **d_out);
 // ---------------------------------------------------------------- workspace
 struct Workspace {
     DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part, y64, d64, es;
+    DevBuf<double> Oi, gm2, F2, scal2, eps2, es2;     // holomorphic SR: imaginary halves
     DevBuf<int> status;
     DevBuf<uint64_t> batch_bits;
 };
@@ -630,8 +631,17 @@ struct StepIn {
     void *user;
     nqs_gradient_fn_t gfn;
     void *guser;
-    int minsr;
+    int minsr;                         // 0 CG-SR, 1 MinSR, 2 holomorphic SR (CG on the complex QGT)
+    nqs_holomorphic_gradient_fn_t hgfn;
+    void *hguser;
 };
+
+// F = 2 (F_R + F_I): the holomorphic force from the real and imaginary halves
+// (src/nqs/nqs_optimizer.c:471-498)
+__global__ void k_holo_force(double *F, const double *__restrict__ F2, long P) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < P; k += (long)gridDim.x * blockDim.x)
+        F[k] = 2.0 * (F[k] + F2[k]);
+}
 
 // Column means of O (and the CG-SR force F when E != NULL) over a 2-D grid of
 // about four blocks per SM.
@@ -814,9 +824,17 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         set_error("gradient callback is not supported on the GPU (NULL or nqs_symproj_gradient)");
         return -1;
     }
+    const bool holo = in.minsr == 2;
+    if (holo && in.hgfn) {
+        set_error("holomorphic gradient callback is not supported on the GPU (NULL: the base ansatz gradient)");
+        return -1;
+    }
     Workspace &w = g_ws;
     if (!w.E.ensure(Ns) || !w.Ei.ensure(Ns) || !w.eps.ensure(Ns) || !w.O.ensure((size_t)Ns * P) ||
         !w.gm.ensure(P) || !w.delta.ensure(P) || !w.scal.ensure(16) || !w.status.ensure(16))
+        return -1;
+    if (holo && (!w.Oi.ensure((size_t)Ns * P) || !w.gm2.ensure(P) || !w.F2.ensure(P) || !w.scal2.ensure(16) ||
+                 !w.eps2.ensure(Ns)))
         return -1;
     // 1. samples
     uint64_t *bits = nullptr;
@@ -829,12 +847,12 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         return minsr_fp64_solve(w.O.p, w.eps.p, Ns, P, cfg->sr_diag_shift, y_out, conv);
     };
     const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
-    const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && (fp32_capable(A) || fp32_mlp_capable(A));
+    const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && !holo && (fp32_capable(A) || fp32_mlp_capable(A));
     nqs_gpu_step_stats_t &ss = step_stats();
     ss.energy_rel_err = -1.0;
     double e64 = 0.0;
     bool have64 = false;
-    if (in.minsr && fp32est && c.opts.mixed_check) {
+    if (in.minsr == 1 && fp32est && c.opts.mixed_check) {
         // reference for the check: the FP64 estimator, statistics and FP64
         // MinSR solve on the same samples
         if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns) || !w.y64.ensure(Ns) ||
@@ -853,12 +871,17 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             return -1;
         have64 = true;
     }
-    // 2. local energies + Jacobian rows (fused when the program allows)
+    // 2. local energies + Jacobian rows (fused when the program allows); the
+    // holomorphic step takes the complex gradient of the base ansatz
+    // (nqs_ansatz_logpsi_gradient_complex, src/nqs/nqs_optimizer.c:458-469)
     bool fused_grad = !grad_sym && A.G == 0;
-    if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
-                                fused_grad ? 1 : 0, fp32est))
+    if (holo) {
+        if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, w.O.p, w.Oi.p, 2, false)) return -1;
+    } else if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
+                                       fused_grad ? 1 : 0, fp32est)) {
         return -1;
-    if (!fused_grad) {
+    }
+    if (!fused_grad && !holo) {
         if (grad_sym) {
             if (!launch_symproj_gradient(Ag, bits, Ns, w.O.p)) return -1;
         } else if (!launch_gradient(Ag.a, bits, Ns, 1, w.O.p, nullptr)) {
@@ -870,11 +893,15 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         const int chains = in.sampler ? nqs_sampler_num_chains((nqs_sampler_t *)in.sampler) : 0;
         if (!ensure_energy_scratch(w.es, Ns) || !enqueue_energy_stats(w.E.p, Ns, chains, w.scal.p, w.eps.p, w.es.p))
             return -1;
+        // <E_im> for the holomorphic force
+        if (holo && (!ensure_energy_scratch(w.es2, Ns) ||
+                     !enqueue_energy_stats(w.Ei.p, Ns, 0, w.scal2.p, w.eps2.p, w.es2.p)))
+            return -1;
     }
     NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
     dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
     int converged = 0, cg_iters = 0;
-    if (in.minsr) {
+    if (in.minsr == 1) {
         if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns)) return -1;
         {
             NQS_LAUNCH("col_mean");
@@ -946,11 +973,16 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         {
             NQS_LAUNCH("col_stats");
             if (!col_stats(w.O.p, Ns, P, w.E.p, w.scal.p, w.gm.p, w.F.p)) return -1;
+            if (holo) {
+                // <I>, (I^T E_im) / N_s - <I> <E_im>; then F = 2 (F_R + F_I)
+                if (!col_stats(w.Oi.p, Ns, P, w.Ei.p, w.scal2.p, w.gm2.p, w.F2.p)) return -1;
+                k_holo_force<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(w.F.p, w.F2.p, P);
+            }
         }
         const int maxit = cfg->sr_cg_max_iters;
         // the whole CG (all iterations) in one cooperative launch
         if (!cg_sr_solve(w.O.p, Ns, P, w.F.p, w.gm.p, cfg->sr_diag_shift, cfg->sr_cg_tol, maxit, w.delta.p, w.scal.p,
-                         w.status.p))
+                         w.status.p, holo ? w.Oi.p : nullptr, holo ? w.gm2.p : nullptr, holo ? 2.0 : 1.0))
             return -1;
         int h[16];
         double hs[16];
@@ -986,7 +1018,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         info->variance_energy = hs[S_ESQ] - hs[S_EMEAN] * hs[S_EMEAN];
         info->update_norm = sqrt(hs[S_NORM2]) * cfg->learning_rate;
         info->acceptance_ratio = in.sampler ? nqs_sampler_acceptance_ratio((nqs_sampler_t *)in.sampler) : 0.0;
-        info->cg_iterations = in.minsr ? 0 : cg_iters;
+        info->cg_iterations = in.minsr == 1 ? 0 : cg_iters;
         info->converged = converged;
     }
     return 0;
@@ -1075,6 +1107,45 @@ int nqs_sr_run_custom(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, 
 
 int nqs_sr_run(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s, double *trace) {
     return nqs_sr_run_custom(cfg, sx, sy, a, s, nullptr, nullptr, trace);
+}
+
+// Holomorphic SR (src/nqs/nqs_optimizer.c:307-558): CG on the complex QGT
+// G = 2 Re{<O* O> - <O*><O>} with the complex local energies.
+int nqs_sr_step_holomorphic_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                                 nqs_log_amp_fn_t fn, void *user, nqs_holomorphic_gradient_fn_t gfn, void *guser,
+                                 nqs_sr_step_info_t *info) {
+    if (!cfg || !a || !s) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, (Sampler *)s, nullptr, cfg->num_samples, fn, user, nullptr, nullptr, 2,
+              gfn, guser};
+    if (nqs_sampler_num_sites(s) != ((Ansatz *)a)->N) {
+        set_error("sampler and ansatz disagree on num_sites");
+        return -1;
+    }
+    return sr_step_impl(in, info, nullptr, nullptr);
+}
+
+int nqs_sr_step_holomorphic(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                            nqs_log_amp_fn_t fn, void *user, nqs_sr_step_info_t *info) {
+    return nqs_sr_step_holomorphic_full(cfg, sx, sy, a, s, fn, user, nullptr, nullptr, info);
+}
+
+int nqs_sr_run_holomorphic_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                                nqs_log_amp_fn_t fn, void *user, nqs_holomorphic_gradient_fn_t gfn, void *guser,
+                                double *trace) {
+    if (!cfg || !a || !s) return -1;
+    nqs_sampler_thermalize(s);
+    for (int it = 0; it < cfg->num_iterations; it++) {
+        nqs_sr_step_info_t info;
+        int rc = nqs_sr_step_holomorphic_full(cfg, sx, sy, a, s, fn, user, gfn, guser, &info);
+        if (rc != 0) return rc;
+        if (trace) trace[it] = info.mean_energy;
+    }
+    return 0;
+}
+
+int nqs_sr_run_holomorphic(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                           nqs_log_amp_fn_t fn, void *user, double *trace) {
+    return nqs_sr_run_holomorphic_full(cfg, sx, sy, a, s, fn, user, nullptr, nullptr, trace);
 }
 
 int nqs_sr_step_minsr_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,

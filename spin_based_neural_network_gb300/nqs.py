@@ -54,6 +54,8 @@ def _declare(L):
         "nqs_sr_run_custom": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
         "nqs_sr_step_custom_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_custom_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, DP]),
+        "nqs_sr_step_holomorphic_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
+        "nqs_sr_run_holomorphic": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
         "nqs_sr_step_minsr_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_minsr": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
         "nqs_marshall_parity": (C.c_int, [IP, C.c_int, C.c_int]),
@@ -336,6 +338,14 @@ def sr_step_minsr(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=No
     return info
 
 
+def sr_step_holomorphic(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None):
+    """nqs_sr_step_holomorphic_full (upstream include/nqs/nqs_optimizer.h:168)."""
+    info = abi.StepInfo()
+    _check(lib().nqs_sr_step_holomorphic_full(C.byref(cfg), size_x, size_y, ansatz.h, sampler.h, log_amp_fn, user,
+                                              None, None, C.byref(info)), "nqs_sr_step_holomorphic_full")
+    return info
+
+
 def sr_step_cg(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, grad_fn=None,
                grad_user=None):
     info = abi.StepInfo()
@@ -346,7 +356,8 @@ def sr_step_cg(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None,
 
 def sr_step_batch(cfg, size_x, size_y, ansatz, batch, minsr=True, log_amp_fn=None, user=None, grad_fn=None,
                   grad_user=None):
-    """One SR step on a caller-supplied batch; returns (info, energies, delta)."""
+    """One SR step on a caller-supplied batch; returns (info, energies, delta).
+    minsr: True / 1 MinSR, False / 0 CG-SR, 2 holomorphic SR."""
     s = spins_array(batch, ansatz.N)
     Ns = s.shape[0]
     E, d = np.zeros(Ns), np.zeros(ansatz.P)

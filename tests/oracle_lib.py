@@ -96,6 +96,8 @@ def lib():
         L.oracle_cgsr_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), C.c_int, IP, C.c_int,
                                        C.c_double, C.c_double, C.c_int, C.c_double, DP, C.c_long,
                                        DP, DP, C.POINTER(OrStepInfo)]
+        L.oracle_holo_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), IP, C.c_int, C.c_double, C.c_double,
+                                       C.c_int, C.c_double, DP, C.c_long, DP, DP, C.POINTER(OrStepInfo)]
         L.oracle_exact_energy.argtypes = [C.POINTER(OrHam), C.c_int, C.c_int, C.c_double, DP]
     return _LIB
 
@@ -241,6 +243,18 @@ def cgsr_step(h, amp, batch, shift, lr, max_iters, tol, grad_mode=0):
     assert lib().oracle_cgsr_step(C.byref(h), amp.ref(), grad_mode, ip(batch), Ns, shift, lr,
                                   max_iters, tol, dp(amp.params), P, dp(E), dp(d),
                                   C.byref(info)) == 0
+    return E, d, info
+
+
+def holo_step(h, amp, batch, shift, lr, max_iters, tol):
+    """Holomorphic SR on a batch (src/nqs/nqs_optimizer.c:415-524)."""
+    batch = np.ascontiguousarray(batch, dtype=np.int32)
+    Ns = batch.shape[0]
+    P = len(amp.params)
+    E, d = np.zeros(Ns), np.zeros(P)
+    info = OrStepInfo()
+    assert lib().oracle_holo_step(C.byref(h), amp.ref(), ip(batch), Ns, shift, lr, max_iters, tol,
+                                  dp(amp.params), P, dp(E), dp(d), C.byref(info)) == 0
     return E, d, info
 
 

@@ -6,6 +6,7 @@ local energies 1e-12 relative (arg compared mod 2 pi; relative to max(|x|, 1));
 parameter updates delta-theta 1e-10 relative in the 2-norm; integer work
 (samples, parities) bit-exact.
 """
+import ctypes as C
 import glob
 import os
 
@@ -380,3 +381,60 @@ def test_minsr_full_size_against_oracle(nqs, Ns, M):
     assert rel(E, Eo) < TOL
     assert np.linalg.norm(delta - do) <= TOL_DELTA * np.linalg.norm(do)
     assert info.update_norm == pytest.approx(io.update_norm, rel=TOL_DELTA)
+
+
+@pytest.mark.parametrize("Ns,iters,shift,tol", [(256, 10, 1e-3, 1e-6), (2048, 600, 1e-2, 1e-13)])
+def test_holomorphic_sr_against_oracle(nqs, Ns, iters, shift, tol):
+    """Holomorphic SR (nqs_sr_step_holomorphic_full) on a batch: complex RBM on
+    the 4x4 Heisenberg torus with the Marshall sign, complex local energies,
+    CG on G = 2 Re{<O* O> - <O*><O>}; energies at 1e-12, delta-theta at the
+    1e-10 bar for an iteration-capped solve and a converged one."""
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    N, M = 16, 16
+    a = make_ansatz(nqs, O.OR_CRBM, N, M, None, 0.3, 2718)
+    p0 = a.params.copy()
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    rng = np.random.default_rng(Ns + 1)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(Ns)])
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, hamiltonian=1,
+                              sr_diag_shift=shift, learning_rate=0.01, sr_cg_max_iters=iters, sr_cg_tol=tol)
+    nqs.set_options(square_pbc=1)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=2, log_amp_fn=m.log_amp_fn, user=m.user)
+    finally:
+        nqs.set_options()
+    amp = O.Amp(O.OR_CRBM, N, M, p0.copy(), [("marshall", Lx, Ly)])
+    Eo, do, io = O.holo_step(O.ham(O.OR_HEIS, Lx, Ly, pbc=1), amp, batch, shift, 0.01, iters, tol)
+    assert rel(E, Eo) < TOL
+    assert np.linalg.norm(delta - do) <= TOL_DELTA * np.linalg.norm(do)
+    assert info.converged == io.converged
+    assert rel(a.params, amp.params) < TOL
+    if Ns == 2048:
+        assert io.converged == 1 and abs(info.cg_iterations - io.cg_iterations) <= 3
+    else:
+        assert info.cg_iterations == io.cg_iterations == iters
+
+
+def test_holomorphic_run_with_sampler(nqs):
+    """nqs_sr_run_holomorphic drives the sampler: a finite energy trace that
+    goes down on the 4x4 Heisenberg torus (complex RBM, Marshall sign)."""
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=16, rbm_init_scale=0.05,
+                              hamiltonian=1, num_samples=1024, num_iterations=30, sr_diag_shift=1e-2,
+                              learning_rate=0.05, rng_seed=9)
+    a = nqs.Ansatz(cfg, 16)
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    o = nqs.options(num_chains=256, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=8, lattice_x=Lx,
+                    lattice_y=Ly, square_pbc=1)
+    nqs.set_options(square_pbc=1)
+    try:
+        s = nqs.Sampler(16, cfg, m.log_amp_fn, m.user, o)
+        trace = np.zeros(30)
+        rc = nqs.lib().nqs_sr_run_holomorphic(C.byref(cfg), Lx, Ly, a.h, s.h, m.log_amp_fn, m.user,
+                                             trace.ctypes.data_as(C.POINTER(C.c_double)))
+    finally:
+        nqs.set_options()
+    assert rc == 0 and np.all(np.isfinite(trace))
+    assert np.mean(trace[-5:]) < np.mean(trace[:5])

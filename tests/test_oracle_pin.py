@@ -167,3 +167,19 @@ def test_exact_energy_fixture():
         ex = json.load(f)
     assert ex["tfim_chain16_pbc_h1"]["E0"] == pytest.approx(-2.0 / math.sin(math.pi / 32), abs=1e-9)
     assert ex["heisenberg_4x4_pbc_sz0"]["E0"] == pytest.approx(-11.2284832084, abs=1e-9)
+
+
+def test_holomorphic_step_reduces_to_cg_sr_for_a_real_rbm():
+    """Holomorphic SR restated from src/nqs/nqs_optimizer.c:415-524: for a real
+    ansatz the imaginary parts vanish, G = 2 S and F = 2 F_real, so the step
+    with shift 2 eps equals CG-SR with shift eps (converged solves)."""
+    N, M = 8, 8
+    p = O.init_params(O.OR_RBM, N, M, 0.3, 11)
+    rng = np.random.default_rng(4)
+    batch = rng.choice(np.array([-1, 1], np.int32), size=(256, N))
+    h = O.ham(O.OR_TFIM, N, 1, Gamma=0.7)
+    Eh, dh, ih = O.holo_step(h, O.Amp(O.OR_RBM, N, M, p.copy()), batch, 2e-3, 0.01, 1000, 1e-12)
+    Ec, dc, ic = O.cgsr_step(h, O.Amp(O.OR_RBM, N, M, p.copy()), batch, 1e-3, 0.01, 1000, 1e-12)
+    assert ih.converged == 1 and ic.converged == 1
+    assert np.array_equal(Eh, Ec)
+    assert np.linalg.norm(dh - dc) <= 1e-8 * np.linalg.norm(dc)
