@@ -622,6 +622,78 @@ def other_configs(nqs, abi, L, base_opts, which):
     return out
 
 
+ED_RECORD = os.path.join(ROOT, "tests", "golden", "kagome_lean_ed.json")
+
+
+def sector_ed(nqs, L, irreps, cpu_sample=True):
+    """Sector exact diagonalisation of the kagome 3 x 3 PBC Heisenberg model (2^27 states,
+    p6m, J = 1) by the memory-lean projecting Lanczos with the upstream research run's
+    settings (max_iters 100, tol 1e-9): device time of the whole call (CUDA events on the
+    library stream; vectors resident in HBM, only the tridiagonal crosses to the host),
+    per-kernel time of 8 iterations, E0 against the upstream recorded run and the
+    independent sector ED, and the oracle's single-thread time for a bounded sample of one
+    iteration (matvec + direct 108-element projector over the first 2^18 states, scaled by
+    2^27 / 2^18)."""
+    with open(ED_RECORD) as f:
+        rec = json.load(f)["kagome_3x3_recorded"]
+    out = {"workload": "kagome_3x3_pbc_heisenberg_p6m_lean_lanczos", "states": 1 << 27, "max_iters": rec["max_iters"],
+           "tol": rec["tol"], "sectors": {}}
+    for irrep in irreps:
+        perm, chars = nqs.kagome_perm(3, 3, "p6m", irrep)
+        e0 = L.nqs_gpu_event_record()
+        t0 = time.perf_counter()
+        e, _, res = nqs.lanczos_e0_kagome_lean(3, 3, 1.0, 1, perm, chars, rec["max_iters"], rec["tol"])
+        wall = time.perf_counter() - t0
+        e1 = L.nqs_gpu_event_record()
+        dev = L.nqs_gpu_event_elapsed_ms(e0, e1)
+        L.nqs_gpu_event_destroy(e0)
+        L.nqs_gpu_event_destroy(e1)
+        want = rec["sectors"][irrep]
+        out["sectors"][irrep] = {
+            "E0": e, "iterations": res["iterations"], "converged": res["converged"], "device_s": dev / 1e3,
+            "wall_s": wall, "ms_per_iteration": dev / max(res["iterations"], 1),
+            "E0_upstream_recorded": want["E0"], "abs_err_vs_recorded": abs(e - want["E0"]),
+            "abs_err_vs_independent_ed": abs(e - want["independent_ED"]),
+            "upstream_recorded_wall_s": want["wall_seconds"], "upstream_iterations": want["iters"],
+            "speedup_vs_upstream_recorded": want["wall_seconds"] / wall}
+    perm, chars = nqs.kagome_perm(3, 3, "p6m", irreps[0])
+    nqs.profile_reset()
+    nqs.profile(True)
+    try:
+        nqs.lanczos_e0_kagome_lean(3, 3, 1.0, 1, perm, chars, 8, 0.0)
+    finally:
+        nqs.profile(False)
+    prof = nqs.profile_read()
+    per_iter = {k: (v[0] / 8.0, v[1] / 8.0) for k, v in prof.items() if k != "ed_seed"}
+    out["kernels_ms_per_iteration"] = {k: round(v[1], 3) for k, v in sorted(per_iter.items(), key=lambda kv: -kv[1][1])}
+    out["launches_per_iteration"] = {k: v[0] for k, v in per_iter.items()}
+    # compulsory traffic: one read and one write of 2^27 doubles per pass (the gathered
+    # operands beyond that come from L2 or HBM depending on their distance)
+    gb = 2 * 8 * (1 << 27) / 1e9
+    passes = per_iter.get("ed_project_pass", (0, 0))
+    if passes[0] > 0:
+        out["projector_pass_ms"] = passes[1] / passes[0]
+        out["projector_pass_compulsory_gbs"] = gb / (passes[1] / passes[0] / 1e3)
+    mv = per_iter.get("ed_matvec", (0, 0))
+    if mv[0] > 0:
+        out["matvec_ms"] = mv[1] / mv[0]
+        out["matvec_compulsory_gbs"] = gb / (mv[1] / mv[0] / 1e3)
+    if cpu_sample:
+        import oracle_lib as O
+        count = 1 << 18
+        x = np.random.default_rng(SEED).standard_normal(1 << 27)
+        pg, cg = nqs.kagome_perm(3, 3, "p6m", irreps[0])
+        tm, tp = O.ed_iteration_sample(3, 3, pg, cg, x, count)
+        scale = float(1 << 27) / count
+        out["cpu_baseline"] = {"kind": "port", "cores": 1,
+                               "sample": "oracle matvec + direct projector over 2^18 of the 2^27 states, scaled",
+                               "s_per_iteration": (tm + tp) * scale, "matvec_s": tm * scale,
+                               "projector_s": tp * scale,
+                               "upstream_recorded_s_per_iteration_14_threads":
+                                   rec["sectors"][irreps[0]]["wall_seconds"] / rec["sectors"][irreps[0]]["iters"]}
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -769,6 +841,10 @@ def run_gpu(args):
     if prec == abi.PREC_MIXED and args.configs:
         others = other_configs(nqs, abi, L, base_opts, args.configs)
 
+    ed = None
+    if prec == abi.PREC_MIXED and args.ed:
+        ed = sector_ed(nqs, L, args.ed.split(","), cpu_sample=rank == 0 and not args.no_cpu_baseline)
+
     multi = multi_learned = None
     if prec == abi.PREC_MIXED and args.batch_steps > 0:
         multi = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps)
@@ -803,7 +879,7 @@ def run_gpu(args):
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
             "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
             "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi, "multi_instance_learned": multi_learned,
-            "other_configs": others,
+            "other_configs": others, "sector_ed": ed,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
@@ -866,6 +942,8 @@ def main():
     ap.add_argument("--converge-fp64", action="store_true", help="also run the FP64 path to the target")
     ap.add_argument("--configs", default="134",
                     help="which of the other workloads to run (digits of 1, 3, 4; empty = none)")
+    ap.add_argument("--ed", default="A1",
+                    help="comma-separated p6m irreps of the kagome 3x3 sector-ED run (empty = skip)")
     ap.add_argument("--batch-steps", type=int, default=300,
                     help="steps of the 64-instance batch run (0 = skip)")
     ap.add_argument("--proposal-steps", type=int, default=20,

@@ -1,0 +1,93 @@
+/*
+ * include/nqs/nqs_lanczos.h -- exact diagonalisation on the device.
+ *
+ * The memory-lean projecting Lanczos of the kagome Heisenberg model over the full
+ * 2^N basis (N = 3 Lx Ly <= 30), with the symmetry-sector projector
+ * (1/|G|) sum_g chi(g) T(g) applied to every Krylov vector.  Every vector lives in
+ * HBM (four vectors of 2^N doubles, five with the eigenvector); the host keeps only
+ * the tridiagonal coefficients.
+ *
+ * Upstream interfaces replaced (names, arguments and return codes are the same):
+ *   nqs_lanczos_e0_kagome_heisenberg_projected_lean        include/nqs/nqs_lanczos.h:192-197
+ *   nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec include/nqs/nqs_lanczos.h:202-208
+ *   lanczos_result_t                                       include/mps/lanczos.h:37-42
+ */
+#ifndef NQS_LANCZOS_H
+#define NQS_LANCZOS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef NQS_LANCZOS_RESULT_DEFINED
+#define NQS_LANCZOS_RESULT_DEFINED
+typedef struct {
+    double eigenvalue;       /* smallest Ritz value found */
+    int    iterations;       /* Krylov steps used */
+    int    converged;        /* 1 when the Ritz value moved by less than tol */
+    double residual_norm;    /* |lambda_k - lambda_{k-1}| at exit */
+} lanczos_result_t;
+#endif
+
+/* Replaces upstream nqs_lanczos_e0_kagome_heisenberg_projected_lean
+ * (src/nqs/nqs_lanczos.c:629-647 over src/mps/lanczos.c:824-960).  Seed: the upstream
+ * xorshift sequence from 0xA5A5A5A5A5A5A5A5 ^ 2^N (bit-identical), projected and
+ * normalised; three-term recurrence with the projector after each matvec; stops when
+ * beta < 1e-14 or, after step 5, when the lowest Ritz value moves by less than tol.
+ * (perm, characters, G): the sector, perm[g*N + i] = site whose spin lands on site i.
+ * Returns 0, or -1 on invalid arguments / device failure (nqs_gpu_last_error). */
+int nqs_lanczos_e0_kagome_heisenberg_projected_lean(
+    int Lx_cells, int Ly_cells, double J, int pbc,
+    const int *perm, const double *characters, int G,
+    int max_iters, double tol,
+    double *out_eigenvalue,
+    lanczos_result_t *out_result);
+
+/* Replaces upstream nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec
+ * (src/nqs/nqs_lanczos.c:651-672 over src/mps/lanczos.c:972-1119): the same first pass,
+ * then the lowest eigenvector of the K x K tridiagonal and a replay of the recurrence
+ * that accumulates the Ritz vector on the device.  out_eigenvector: host array of 2^N
+ * doubles, unit norm (its overall sign is arbitrary, as upstream). */
+int nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec(
+    int Lx_cells, int Ly_cells, double J, int pbc,
+    const int *perm, const double *characters, int G,
+    int max_iters, double tol,
+    double *out_eigenvalue,
+    double *out_eigenvector,
+    lanczos_result_t *out_result);
+
+/* ---- device-resident building blocks (GB300 additions) ---------------------------
+ * Pointers marked d_ are device pointers of 2^N doubles. */
+
+/* y = H x for H = J sum_<ij> S_i.S_j on the kagome bonds of src/nqs/nqs_lanczos.c:380-432
+ * (up triangles always, down triangles with PBC or away from the open edges). */
+int nqs_gpu_kagome_heis_matvec(int Lx_cells, int Ly_cells, double J, int pbc,
+                               const double *d_in, double *d_out);
+
+/* d_out = (1/G) sum_g characters[g] T(g) d_in (d_out may equal d_in).  When the
+ * characters are multiplicative over a subgroup factorisation G = R.H the sum runs as two
+ * passes of |H| and |R| gathers per state, else as one pass of |G| gathers. */
+int nqs_gpu_sector_project(int N, int G, const int *perm, const double *characters,
+                           const double *d_in, double *d_out);
+
+/* The Lanczos seed before projection: d_out[i] = u_i - 1/2, u_i the (i+1)-th output of
+ * xorshift64 (13, 7, 17) from 0xA5A5A5A5A5A5A5A5 ^ 2^N (alternate = 0) or from
+ * 0xBEEFBABE ^ 2^N (alternate = 1), scaled by 2^-53 after >> 11. */
+int nqs_gpu_lanczos_seed(int N, int alternate, double *d_out);
+
+/* Tridiagonal coefficients of the last Lanczos run on this thread's context:
+ * alpha[0..K-1], beta[1..K] (beta[0] = 0).  Returns K (<= cap copied). */
+int nqs_gpu_lanczos_last_coeffs(int cap, double *alpha, double *beta);
+
+/* Host-side plan of the sector projector (no device needed): *out_passes = 1 (direct) or
+ * 2 (factored); sizes[0..passes-1] = elements per pass; elems (G ints) = the group
+ * indices of pass 1 followed by those of pass 2.  Pass 1 sums over the subgroup H,
+ * pass 2 over coset representatives r with T(r)T(h) = T(g(r,h)), each g exactly once. */
+int nqs_ed_projector_plan(int N, int G, const int *perm, const double *characters,
+                          int *out_passes, int *sizes, int *elems);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NQS_LANCZOS_H */

@@ -49,6 +49,43 @@ int nqs_kagome_p2_perm(int Lx, int Ly,
                         double **out_characters,
                         int *out_num_elements);
 
+/* Upstream nqs_symproj_kagome_irrep_t (include/nqs/nqs_symproj.h:193-200): the C_6v
+ * irreps at Gamma.  For E_1 / E_2 the characters carry the factor d_E = 2. */
+typedef enum {
+    NQS_SYMPROJ_KAGOME_GAMMA_A1 = 0,
+    NQS_SYMPROJ_KAGOME_GAMMA_A2 = 1,
+    NQS_SYMPROJ_KAGOME_GAMMA_B1 = 2,
+    NQS_SYMPROJ_KAGOME_GAMMA_B2 = 3,
+    NQS_SYMPROJ_KAGOME_GAMMA_E1 = 4,
+    NQS_SYMPROJ_KAGOME_GAMMA_E2 = 5
+} nqs_symproj_kagome_irrep_t;
+
+/* Replaces upstream nqs_kagome_p6m_perm_irrep (include/nqs/nqs_symproj.h:225-229,
+ * src/nqs/nqs_symproj.c:738-776): the |G| = 12 L^2 p6m table of the L x L kagome torus,
+ * g = op * L^2 + tx * L + ty, op 0..5 = rotation by 60 op degrees about a hexagon
+ * centre, op 6..11 = the horizontal mirror after that rotation; characters = the
+ * C_6v character of op for the named irrep (translations carry +1 at Gamma).
+ * Built in exact integer half-lattice coordinates.  Host only; caller frees both. */
+int nqs_kagome_p6m_perm_irrep(int L,
+                               nqs_symproj_kagome_irrep_t irrep_name,
+                               int **out_perm,
+                               double **out_characters,
+                               int *out_num_elements);
+
+/* Replaces upstream nqs_kagome_p6m_perm (include/nqs/nqs_symproj.h:178-181): A_1. */
+int nqs_kagome_p6m_perm(int L,
+                         int **out_perm,
+                         double **out_characters,
+                         int *out_num_elements);
+
+/* Replaces upstream nqs_kagome_p6m_project_inplace (include/nqs/nqs_symproj.h:247-250,
+ * src/nqs/nqs_symproj.c:786-852): psi <- (1/G) sum_g chi(g) T(g) psi on a host array of
+ * 2^N doubles, computed on the device (copy in, project, copy out).  Failures leave psi
+ * unchanged and set nqs_gpu_last_error. */
+void nqs_kagome_p6m_project_inplace(double *psi, int N, int G,
+                                     const int *perm,
+                                     const double *characters);
+
 #ifdef __cplusplus
 }
 #endif

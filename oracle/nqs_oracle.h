@@ -154,6 +154,32 @@ int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, i
 int oracle_exact_energy(const or_ham_t *h, int n_down, int max_iters, double tol,
                         double *out_e0);
 
+/* ---- exact diagonalisation (oracle_ed.c) ---------------------------------------- */
+#define OR_LZ_MAX 512
+typedef struct {
+    int iterations, converged;
+    double residual;
+    double alpha[OR_LZ_MAX], beta[OR_LZ_MAX + 1];
+} or_lanczos_info_t;
+
+/* Kagome Heisenberg H x over the full 2^N basis, src/nqs/nqs_lanczos.c:380-432. */
+void oracle_kagome_heis_matvec(int Lx, int Ly, double J, int pbc, const double *in, double *out);
+/* The same for the states s0 <= s < s1 only (out indexed by s). */
+void oracle_kagome_heis_matvec_range(int Lx, int Ly, double J, int pbc, const double *in, double *out,
+                                     long s0, long s1);
+/* psi <- (1/G) sum_g chi(g) T(g) psi, bit i of T(g)'s source = bit perm[g][i],
+ * src/nqs/nqs_symproj.c:786-852 (direct gather form). */
+void oracle_sector_project(double *psi, int N, int G, const int *perm, const double *chars);
+/* Out-of-place projector for the states s0 <= s < s1 (out[s - s0]). */
+void oracle_sector_project_range(const double *psi, double *out, int N, int G, const int *perm,
+                                 const double *chars, long s0, long s1);
+/* The lean Lanczos seed before projection, src/mps/lanczos.c:864-880. */
+void oracle_lanczos_seed(int N, int alternate, double *out);
+/* Memory-lean projecting Lanczos for the kagome Heisenberg sector E_0, src/mps/lanczos.c:824-960,
+ * with the eigenvector replay of :972-1119 when out_vec is not NULL.  N <= 24. */
+int oracle_lanczos_lean_kagome(int Lx, int Ly, double J, int pbc, const int *perm, const double *chars, int G,
+                               int max_iters, double tol, double *out_e, double *out_vec, or_lanczos_info_t *info);
+
 #ifdef __cplusplus
 }
 #endif

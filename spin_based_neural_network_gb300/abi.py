@@ -155,3 +155,9 @@ class Instance(C.Structure):
     """nqs_gpu_instance_t (include/nqs/nqs_gpu.h)."""
     _fields_ = [("cfg", C.POINTER(NqsConfig)), ("size_x", C.c_int), ("size_y", C.c_int), ("ansatz", C.c_void_p),
                 ("sampler", C.c_void_p), ("log_amp", C.c_void_p), ("log_amp_user", C.c_void_p)]
+
+
+class LanczosResult(C.Structure):
+    """lanczos_result_t (include/nqs/nqs_lanczos.h; upstream include/mps/lanczos.h:37-42)."""
+    _fields_ = [("eigenvalue", C.c_double), ("iterations", C.c_int), ("converged", C.c_int),
+                ("residual_norm", C.c_double)]

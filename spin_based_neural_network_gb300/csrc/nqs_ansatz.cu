@@ -829,4 +829,90 @@ int nqs_kagome_p2_perm(int Lx, int Ly, int **out_perm, double **out_chars, int *
     return 0;
 }
 
+// p6m on the L x L kagome torus, restating src/nqs/nqs_symproj.c:618-776 in exact
+// integer coordinates: a point is (u, v) in units of a1/2 and a2/2, so sites are the
+// points with u or v even (A = (2cx, 2cy), B = A + (1, 0), C = A + (0, 1)) and (1, 1) is
+// the hexagon centre the rotations turn about.  Row g = op * L^2 + tx * L + ty maps output
+// site p to the source site R(-60 k) M^m (p - t): translation t = (2tx, 2ty); mirror
+// y -> sqrt(3)/2 - y is (u, v) -> (u + v - 1, 2 - v); rotation by -60 degrees is
+// (u, v) -> (u + v, -u).
+static int p6m_source_site(int L, int op, int tx, int ty, int cx, int cy, int sub) {
+    int u = 2 * cx + (sub == 1) - 2 * tx, v = 2 * cy + (sub == 2) - 2 * ty;
+    if (op >= 6) {
+        int nu = u + v - 1, nv = 2 - v;
+        u = nu;
+        v = nv;
+    }
+    u -= 1;
+    v -= 1;
+    for (int r = 0; r < op % 6; r++) {
+        int nu = u + v, nv = -u;
+        u = nu;
+        v = nv;
+    }
+    u += 1;
+    v += 1;
+    int bu = u & 1, bv = v & 1;
+    if (bu && bv) return -1;                          // a hexagon centre, not a site
+    int s = bu ? 1 : (bv ? 2 : 0);
+    int X = ((((u - bu) / 2) % L) + L) % L, Y = ((((v - bv) / 2) % L) + L) % L;
+    return KG_SITE(X, Y, s, L);
+}
+
+// C_6v character of op (src/nqs/nqs_symproj.c:683-736): ops 1, 5 = C6; 2, 4 = C3; 3 = C2;
+// mirrors with even rotation index are sigma_v, odd are sigma_d.  E irreps carry d_E = 2.
+static double c6v_character(int op, int irrep) {
+    bool mir = op >= 6;
+    int k = op % 6;
+    bool c6 = !mir && (k == 1 || k == 5), c3 = !mir && (k == 2 || k == 4), c2 = !mir && k == 3;
+    bool sv = mir && k % 2 == 0, sd = mir && k % 2 == 1;
+    switch (irrep) {
+    case NQS_SYMPROJ_KAGOME_GAMMA_A1: return 1.0;
+    case NQS_SYMPROJ_KAGOME_GAMMA_A2: return mir ? -1.0 : 1.0;
+    case NQS_SYMPROJ_KAGOME_GAMMA_B1: return (c6 || c2 || sd) ? -1.0 : 1.0;
+    case NQS_SYMPROJ_KAGOME_GAMMA_B2: return (c6 || c2 || sv) ? -1.0 : 1.0;
+    case NQS_SYMPROJ_KAGOME_GAMMA_E1: return mir ? 0.0 : c6 ? 2.0 : c3 ? -2.0 : c2 ? -4.0 : 4.0;
+    case NQS_SYMPROJ_KAGOME_GAMMA_E2: return mir ? 0.0 : (c6 || c3) ? -2.0 : 4.0;
+    }
+    return 1.0;
+}
+
+int nqs_kagome_p6m_perm_irrep(int L, nqs_symproj_kagome_irrep_t irrep, int **out_perm, double **out_chars,
+                              int *out_G) {
+    if (L <= 0 || !out_perm || !out_chars || !out_G || (int)irrep < 0 || (int)irrep > 5) return -1;
+    int N = 3 * L * L, G = 12 * L * L;
+    int *perm = (int *)malloc(sizeof(int) * (size_t)G * N);
+    double *chars = (double *)malloc(sizeof(double) * (size_t)G);
+    if (!perm || !chars) {
+        free(perm);
+        free(chars);
+        return -1;
+    }
+    int g = 0;
+    for (int op = 0; op < 12; op++)
+        for (int tx = 0; tx < L; tx++)
+            for (int ty = 0; ty < L; ty++, g++) {
+                for (int cx = 0; cx < L; cx++)
+                    for (int cy = 0; cy < L; cy++)
+                        for (int sub = 0; sub < 3; sub++) {
+                            int src = p6m_source_site(L, op, tx, ty, cx, cy, sub);
+                            if (src < 0) {
+                                free(perm);
+                                free(chars);
+                                return -1;
+                            }
+                            perm[(size_t)g * N + KG_SITE(cx, cy, sub, L)] = src;
+                        }
+                chars[g] = c6v_character(op, (int)irrep);
+            }
+    *out_perm = perm;
+    *out_chars = chars;
+    *out_G = G;
+    return 0;
+}
+
+int nqs_kagome_p6m_perm(int L, int **out_perm, double **out_chars, int *out_G) {
+    return nqs_kagome_p6m_perm_irrep(L, NQS_SYMPROJ_KAGOME_GAMMA_A1, out_perm, out_chars, out_G);
+}
+
 }  // extern "C"

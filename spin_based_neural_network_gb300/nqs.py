@@ -64,6 +64,19 @@ def _declare(L):
         "nqs_symproj_gradient": (C.c_int, [VP, VP, IP, C.c_int, DP]),
         "nqs_kagome_translation_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), IP]),
         "nqs_kagome_p2_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
+        "nqs_kagome_p6m_perm_irrep": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
+        "nqs_kagome_p6m_project_inplace": (None, [DP, C.c_int, C.c_int, IP, DP]),
+        "nqs_lanczos_e0_kagome_heisenberg_projected_lean": (
+            C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, IP, DP, C.c_int, C.c_int, C.c_double, DP,
+                      C.POINTER(abi.LanczosResult)]),
+        "nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec": (
+            C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, IP, DP, C.c_int, C.c_int, C.c_double, DP, DP,
+                      C.POINTER(abi.LanczosResult)]),
+        "nqs_gpu_kagome_heis_matvec": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, VP, VP]),
+        "nqs_gpu_sector_project": (C.c_int, [C.c_int, C.c_int, IP, DP, VP, VP]),
+        "nqs_gpu_lanczos_seed": (C.c_int, [C.c_int, C.c_int, VP]),
+        "nqs_gpu_lanczos_last_coeffs": (C.c_int, [C.c_int, DP, DP]),
+        "nqs_ed_projector_plan": (C.c_int, [C.c_int, C.c_int, IP, DP, IP, IP, IP]),
         "nqs_gpu_options_default": (abi.GpuOptions, []),
         "nqs_gpu_set_options": (C.c_int, [optp]),
         "nqs_gpu_get_options": (C.c_int, [optp]),
@@ -241,10 +254,22 @@ class Symproj:
         return C.addressof(self.s)
 
 
-def kagome_perm(Lx, Ly, group="p2"):
+P6M_IRREPS = {"A1": 0, "A2": 1, "B1": 2, "B2": 3, "E1": 4, "E2": 5}
+
+
+def kagome_perm(Lx, Ly, group="p2", irrep="A1"):
+    """(perm [G, N], characters [G]) of a kagome symmetry group: "p2", "translations", or
+    "p6m" (L x L torus, irrep one of A1 A2 B1 B2 E1 E2)."""
     p = IP()
     G = C.c_int()
-    if group == "p2":
+    if group == "p6m":
+        if Lx != Ly:
+            raise NqsError("p6m needs an L x L torus")
+        ch = DP()
+        _check(lib().nqs_kagome_p6m_perm_irrep(Lx, P6M_IRREPS[irrep], C.byref(p), C.byref(ch), C.byref(G)),
+               "p6m perm")
+        chars = np.ctypeslib.as_array(ch, shape=(G.value,)).copy()
+    elif group == "p2":
         ch = DP()
         _check(lib().nqs_kagome_p2_perm(Lx, Ly, C.byref(p), C.byref(ch), C.byref(G)), "p2 perm")
         chars = np.ctypeslib.as_array(ch, shape=(G.value,)).copy()
@@ -508,3 +533,75 @@ class Batch:
             self.free()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- exact diagonalisation
+
+def _perm_args(perm, chars):
+    perm = np.ascontiguousarray(perm, dtype=np.int32).reshape(-1)
+    chars = np.ascontiguousarray(chars, dtype=np.float64).reshape(-1)
+    return perm, chars
+
+
+def lanczos_e0_kagome_lean(Lx, Ly, J, pbc, perm, chars, max_iters=100, tol=1e-9, eigvec=False):
+    """Memory-lean projecting Lanczos of the kagome Heisenberg sector (perm, chars) on the
+    device: nqs_lanczos_e0_kagome_heisenberg_projected_lean[_eigvec].  Returns
+    (E0, eigenvector or None, {"iterations", "converged", "residual_norm"})."""
+    perm, chars = _perm_args(perm, chars)
+    e = C.c_double()
+    r = abi.LanczosResult()
+    vec = None
+    if eigvec:
+        vec = np.zeros(1 << (3 * Lx * Ly))
+        rc = lib().nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec(
+            Lx, Ly, J, pbc, _ip(perm), _dp(chars), len(chars), max_iters, tol, C.byref(e), _dp(vec), C.byref(r))
+    else:
+        rc = lib().nqs_lanczos_e0_kagome_heisenberg_projected_lean(
+            Lx, Ly, J, pbc, _ip(perm), _dp(chars), len(chars), max_iters, tol, C.byref(e), C.byref(r))
+    _check(rc, "lean Lanczos")
+    return e.value, vec, {"iterations": r.iterations, "converged": r.converged, "residual_norm": r.residual_norm}
+
+
+def lanczos_last_coeffs(cap=4096):
+    """(alpha[K], beta[K+1]) of the last Lanczos run (beta[0] = 0)."""
+    a, b = np.zeros(cap), np.zeros(cap + 1)
+    K = lib().nqs_gpu_lanczos_last_coeffs(cap + 1, _dp(a), _dp(b))
+    return a[:K].copy(), b[:K + 1].copy()
+
+
+def sector_project_host(psi, N, perm, chars):
+    """nqs_kagome_p6m_project_inplace on a copy of psi (host array of 2^N doubles)."""
+    perm, chars = _perm_args(perm, chars)
+    out = np.array(psi, dtype=np.float64, copy=True)
+    lib().nqs_kagome_p6m_project_inplace(_dp(out), N, len(chars), _ip(perm), _dp(chars))
+    err = last_error()
+    if err:
+        raise NqsError("sector projection failed: " + err)
+    return out
+
+
+def gpu_sector_project(N, perm, chars, d_in, d_out):
+    """Device-pointer projector (d_out may equal d_in)."""
+    perm, chars = _perm_args(perm, chars)
+    _check(lib().nqs_gpu_sector_project(N, len(chars), _ip(perm), _dp(chars), d_in, d_out), "sector projection")
+
+
+def gpu_kagome_heis_matvec(Lx, Ly, J, pbc, d_in, d_out):
+    _check(lib().nqs_gpu_kagome_heis_matvec(Lx, Ly, J, pbc, d_in, d_out), "kagome matvec")
+
+
+def gpu_lanczos_seed(N, alternate, d_out):
+    _check(lib().nqs_gpu_lanczos_seed(N, alternate, d_out), "Lanczos seed")
+
+
+def projector_plan(N, perm, chars):
+    """(passes, [sizes], element order) of the device sector projector (host only)."""
+    perm, chars = _perm_args(perm, chars)
+    G = len(chars)
+    npass = C.c_int()
+    sizes = (C.c_int * 2)()
+    elems = np.zeros(G, dtype=np.int32)
+    _check(lib().nqs_ed_projector_plan(N, G, _ip(perm), _dp(chars), C.byref(npass), sizes, _ip(elems)),
+           "projector plan")
+    sz = [sizes[i] for i in range(npass.value)]
+    return npass.value, sz, elems[:sum(sz)].copy()

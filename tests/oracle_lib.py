@@ -53,7 +53,7 @@ class OrChainOpts(C.Structure):
 
 
 def build_oracle(force=False):
-    srcs = [os.path.join(ORACLE_DIR, f) for f in ("nqs_oracle.c", "oracle_sampler_sr.c")]
+    srcs = [os.path.join(ORACLE_DIR, f) for f in ("nqs_oracle.c", "oracle_sampler_sr.c", "oracle_ed.c")]
     if not force and os.path.exists(ORACLE_SO) and all(
             os.path.getmtime(ORACLE_SO) >= os.path.getmtime(s) for s in srcs):
         return ORACLE_SO
@@ -262,3 +262,62 @@ def exact_energy(h, n_down=-1, max_iters=300, tol=1e-12):
     e = C.c_double()
     assert lib().oracle_exact_energy(C.byref(h), n_down, max_iters, tol, C.byref(e)) == 0
     return e.value
+
+
+class OrLanczosInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("residual", C.c_double),
+                ("alpha", C.c_double * 512), ("beta", C.c_double * 513)]
+
+
+def kagome_matvec(Lx, Ly, J, pbc, x):
+    """H x on the full 2^N basis (src/nqs/nqs_lanczos.c:380-432)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    lib().oracle_kagome_heis_matvec(Lx, Ly, C.c_double(J), pbc, dp(x), dp(y))
+    return y
+
+
+def sector_project(psi, N, perm, chars):
+    """(1/G) sum_g chi(g) T(g) psi (src/nqs/nqs_symproj.c:786-852)."""
+    out = np.array(psi, dtype=np.float64, copy=True)
+    perm = np.ascontiguousarray(perm, dtype=np.int32)
+    chars = np.ascontiguousarray(chars, dtype=np.float64)
+    lib().oracle_sector_project(dp(out), N, len(chars), ip(perm), dp(chars))
+    return out
+
+
+def lanczos_seed(N, alternate=0):
+    out = np.zeros(1 << N)
+    lib().oracle_lanczos_seed(N, alternate, dp(out))
+    return out
+
+
+def lanczos_lean_kagome(Lx, Ly, J, pbc, perm, chars, max_iters, tol, eigvec=False):
+    """Memory-lean projecting Lanczos (src/mps/lanczos.c:824-960, :972-1119)."""
+    perm = np.ascontiguousarray(perm, dtype=np.int32)
+    chars = np.ascontiguousarray(chars, dtype=np.float64)
+    e = C.c_double()
+    vec = np.zeros(1 << (3 * Lx * Ly)) if eigvec else None
+    info = OrLanczosInfo()
+    assert lib().oracle_lanczos_lean_kagome(Lx, Ly, C.c_double(J), pbc, ip(perm), dp(chars), len(chars),
+                                            max_iters, C.c_double(tol), C.byref(e),
+                                            dp(vec) if eigvec else None, C.byref(info)) == 0
+    return e.value, vec, info
+
+
+def ed_iteration_sample(Lx, Ly, perm, chars, x, count):
+    """Seconds for the oracle's matvec and direct projector over the first `count` states
+    (single thread): the CPU baseline's bounded sample of one Lanczos iteration."""
+    import time
+    perm = np.ascontiguousarray(perm, dtype=np.int32)
+    chars = np.ascontiguousarray(chars, dtype=np.float64)
+    N = 3 * Lx * Ly
+    y = np.zeros(1 << N)
+    t = np.zeros(count)
+    t0 = time.perf_counter()
+    lib().oracle_kagome_heis_matvec_range(Lx, Ly, C.c_double(1.0), 1, dp(x), dp(y), C.c_long(0), C.c_long(count))
+    t1 = time.perf_counter()
+    lib().oracle_sector_project_range(dp(x), dp(t), N, len(chars), ip(perm), dp(chars), C.c_long(0),
+                                      C.c_long(count))
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1
