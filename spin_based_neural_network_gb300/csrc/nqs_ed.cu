@@ -289,8 +289,8 @@ struct ProjPlan {
     std::vector<int> elems;          // pass 1 elements, then pass 2
     std::vector<int> key_perm;
     std::vector<double> key_chars;
-    DevBuf<unsigned> tab;            // [G][ED_NCH][16] in elems order
-    DevBuf<double> chi;              // [G] in elems order
+    DevBuf<unsigned> tab;            // [elems][ED_NCH][16] in elems order
+    DevBuf<double> chi;              // [elems] in elems order
 };
 
 // Smallest d + G/d over the divisors 1 < d < G (G when G is prime or small).
@@ -447,9 +447,10 @@ ProjPlan *plan_get(int N, int G, const int *perm, const double *chars) {
             P.N = 0;
             return nullptr;
         }
-    std::vector<unsigned> tab((size_t)G * ED_TAB, 0u);
-    std::vector<double> chi(G);
-    for (int e = 0; e < G; e++) {
+    const int ne = (int)P.elems.size();               // |H| + |R|, or G for the direct form
+    std::vector<unsigned> tab((size_t)ne * ED_TAB, 0u);
+    std::vector<double> chi(ne);
+    for (int e = 0; e < ne; e++) {
         const int g = P.elems[e];
         const int *pg = perm + (size_t)g * N;
         std::vector<int> pinv(N);
@@ -466,9 +467,9 @@ ProjPlan *plan_get(int N, int G, const int *perm, const double *chars) {
             }
         chi[e] = chars[g];
     }
-    if (!P.tab.ensure(tab.size()) || !P.chi.ensure(G) ||
+    if (!P.tab.ensure(tab.size()) || !P.chi.ensure(ne) ||
         !NQS_CUDA(cudaMemcpy(P.tab.p, tab.data(), tab.size() * sizeof(unsigned), cudaMemcpyHostToDevice)) ||
-        !NQS_CUDA(cudaMemcpy(P.chi.p, chi.data(), G * sizeof(double), cudaMemcpyHostToDevice))) {
+        !NQS_CUDA(cudaMemcpy(P.chi.p, chi.data(), ne * sizeof(double), cudaMemcpyHostToDevice))) {
         P.N = 0;
         return nullptr;
     }
