@@ -679,6 +679,7 @@ def sector_ed(nqs, L, irreps, cpu_sample=True):
         out["matvec_ms"] = mv[1] / mv[0]
         out["matvec_compulsory_gbs"] = gb / (mv[1] / mv[0] / 1e3)
     if cpu_sample:
+        import numpy as np
         import oracle_lib as O
         count = 1 << 18
         x = np.random.default_rng(SEED).standard_normal(1 << 27)
