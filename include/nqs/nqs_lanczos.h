@@ -65,8 +65,9 @@ int nqs_gpu_kagome_heis_matvec(int Lx_cells, int Ly_cells, double J, int pbc,
                                const double *d_in, double *d_out);
 
 /* d_out = (1/G) sum_g characters[g] T(g) d_in (d_out may equal d_in).  When the
- * characters are multiplicative over a subgroup factorisation G = R.H the sum runs as two
- * passes of |H| and |R| gathers per state, else as one pass of |G| gathers. */
+ * characters are multiplicative on the group the sum runs as up to four passes over a
+ * chain of subgroups and coset representatives (G = R1 H1, H1 = R2 H2, ...; |H_k| + sum
+ * |R_k| gathers per state), else as one pass of |G| gathers. */
 int nqs_gpu_sector_project(int N, int G, const int *perm, const double *characters,
                            const double *d_in, double *d_out);
 
@@ -79,10 +80,11 @@ int nqs_gpu_lanczos_seed(int N, int alternate, double *d_out);
  * alpha[0..K-1], beta[1..K] (beta[0] = 0).  Returns K (<= cap copied). */
 int nqs_gpu_lanczos_last_coeffs(int cap, double *alpha, double *beta);
 
-/* Host-side plan of the sector projector (no device needed): *out_passes = 1 (direct) or
- * 2 (factored); sizes[0..passes-1] = elements per pass; elems (G ints) = the group
- * indices of pass 1 followed by those of pass 2.  Pass 1 sums over the subgroup H,
- * pass 2 over coset representatives r with T(r)T(h) = T(g(r,h)), each g exactly once. */
+/* Host-side plan of the sector projector (no device needed): *out_passes = 1 (direct) to
+ * 4; sizes[0..passes-1] (4 ints) = elements per pass; elems (G ints) = the group indices
+ * of pass 0, then pass 1, ...  Pass 0 sums over the innermost subgroup H_k, each later
+ * pass over coset representatives of the previous group in the next larger one, so that
+ * the product of the passes' sums runs over every g of G exactly once. */
 int nqs_ed_projector_plan(int N, int G, const int *perm, const double *characters,
                           int *out_passes, int *sizes, int *elems);
 

@@ -15,9 +15,9 @@
 //   nqs_lanczos_e0_kagome_heisenberg_projected_lean[_eigvec]  src/nqs/nqs_lanczos.c:629-672
 //
 // The projector (1/G) sum_g chi(g) T(g) is evaluated, when chi is multiplicative on the
-// group, as two passes over a subgroup H and coset representatives R (G = R.H): |H| + |R|
-// gathers per state (9 + 12 for the 108-element p6m group of the 3 x 3 torus) instead of
-// |G|.  Other character sets (the E irreps' traces) take the one-pass |G|-gather form.
+// group, as passes over a chain of subgroups and coset representatives (G = R1 H1,
+// H1 = R2 H2, ...): 3 + 3 + 12 gathers per state for the 108-element p6m group of the
+// 3 x 3 torus instead of 108.  Other character sets (the E irreps' traces) take the one-pass |G|-gather form.
 // Reductions are block partials summed in a fixed order, so every run is deterministic
 // and the eigenvector replay reproduces the first pass bit for bit.
 #include <algorithm>
@@ -42,8 +42,10 @@ constexpr int ED_SEED_RUN = 256;          // consecutive seed values per thread
 constexpr size_t ED_MAX_SMEM = 200 * 1024;
 constexpr double ED_BETA_MIN = 1e-14;     // src/mps/lanczos.c:919
 
+// Bond masks; the first nlow touch one of the five lane bits (bits 0-4), the rest have
+// both sites at bit 5 or above, where all 32 states of a warp agree.
 struct Bonds {
-    int nb;
+    int nb, nlow;
     unsigned m[ED_MAX_BONDS];
 };
 
@@ -94,16 +96,27 @@ __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__rest
     __shared__ unsigned sm[ED_MAX_BONDS];
     for (int i = threadIdx.x; i < B.nb; i += ED_THREADS) sm[i] = B.m[i];
     __syncthreads();
-    const int nb = B.nb;
+    const int nb = B.nb, nlow = B.nlow;
     double dot = 0.0;
     const unsigned stride = gridDim.x * ED_THREADS;
     for (unsigned s = blockIdx.x * ED_THREADS + threadIdx.x; s < dim; s += stride) {
         double off = 0.0;
         int anti = 0;
 #pragma unroll 4
-        for (int b = 0; b < nb; b++) {
+        for (int b = 0; b < nlow; b++) {
             const unsigned m = sm[b];
             if (__popc(s & m) == 1) {
+                off += __ldg(x + (s ^ m));
+                anti++;
+            }
+        }
+        // High bonds exist only for N >= 7, where dim is a multiple of 32 and every warp is
+        // full, so the vote is over 32 lanes that already agree: a uniform branch that
+        // skips the FP64 add for the whole warp when its spins are parallel.
+#pragma unroll 4
+        for (int b = nlow; b < nb; b++) {
+            const unsigned m = sm[b];
+            if (__all_sync(0xffffffffu, __popc(s & m) == 1)) {
                 off += __ldg(x + (s ^ m));
                 anti++;
             }
@@ -117,8 +130,8 @@ __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__rest
 }
 
 // y[s] = scale * sum_e chi[e] x[pi_e(s)] over m group elements, pi_e(s) = OR_c tab[e][c][nibble c
-// of s] (bit i of pi_e(s) = bit perm_e[i] of s); zero characters are skipped.  part (may be
-// null) receives the block partials of y.y.
+// of s] (bit i of pi_e(s) = bit perm_e[i] of s).  part (may be null) receives the block
+// partials of y.y.
 __global__ void __launch_bounds__(ED_THREADS) k_perm_sum(const double *__restrict__ x, double *__restrict__ y,
                                                          unsigned dim, int m, const unsigned *__restrict__ tab,
                                                          const double *__restrict__ chi, double scale,
@@ -136,7 +149,6 @@ __global__ void __launch_bounds__(ED_THREADS) k_perm_sum(const double *__restric
 #pragma unroll 2
         for (int e = 0; e < m; e++) {
             const double c = s_chi[e];
-            if (c == 0.0) continue;
             const unsigned *t = s_tab + e * ED_TAB;
             unsigned src = 0;
 #pragma unroll
@@ -262,6 +274,7 @@ bool kagome_bonds(int Lx, int Ly, int pbc, Bonds &B) {
         B.m[B.nb++] = (1u << u) | (1u << v);
         return true;
     };
+    B.nlow = 0;
     for (int cx = 0; cx < Lx; cx++)
         for (int cy = 0; cy < Ly; cy++) {
             int A = site(cx, cy, 0), Bs = site(cx, cy, 1), Cs = site(cx, cy, 2);
@@ -279,14 +292,19 @@ bool kagome_bonds(int Lx, int Ly, int pbc, Bonds &B) {
             int Bm = site(cxm, cy, 1), Cm = site(cx, cym, 2);
             if (!add(A, Bm) || !add(A, Cm) || !add(Bm, Cm)) return false;
         }
+    // lane-bit bonds first (a stable partition keeps the loop order within each group)
+    std::stable_partition(B.m, B.m + B.nb, [](unsigned m) { return (m & 31u) != 0; });
+    while (B.nlow < B.nb && (B.m[B.nlow] & 31u)) B.nlow++;
     return true;
 }
 
 // ---- sector projector plan
+constexpr int ED_MAX_PASSES = 4;
+
 struct ProjPlan {
     int N = 0, G = 0, passes = 0;
-    int size[2] = {0, 0};
-    std::vector<int> elems;          // pass 1 elements, then pass 2
+    int size[ED_MAX_PASSES] = {0, 0, 0, 0};
+    std::vector<int> elems;          // pass 0 elements, then pass 1, ...
     std::vector<int> key_perm;
     std::vector<double> key_chars;
     DevBuf<unsigned> tab;            // [elems][ED_NCH][16] in elems order
@@ -299,6 +317,72 @@ int best_split_cost(int G) {
     for (int d = 2; d < G; d++)
         if (G % d == 0) best = std::min(best, d + G / d);
     return best;
+}
+
+// Best split of the group grp (element indices, closed under mul, G x G table) into a
+// subgroup H generated by one or two elements and left-coset representatives R (every
+// element of grp exactly once as r o h) with |H| + |R| minimal; false when no split makes
+// |H| + |R| < |grp|.
+bool split_group(const std::vector<int> &grp, const std::vector<int> &mul, int G, std::vector<int> &Hout,
+                 std::vector<int> &Rout) {
+    const int n = (int)grp.size();
+    const int target = best_split_cost(n);
+    if (target >= n) return false;
+    int best_cost = n;
+    std::vector<int> best, H;
+    std::vector<char> in(G);
+    auto closure = [&](int g1, int g2) {
+        std::fill(in.begin(), in.end(), 0);
+        H.clear();
+        int gens[2] = {g1, g2};
+        int ng = g2 < 0 ? 1 : 2;
+        for (int i = 0; i < ng; i++)
+            if (!in[gens[i]]) {
+                in[gens[i]] = 1;
+                H.push_back(gens[i]);
+            }
+        for (size_t q = 0; q < H.size(); q++)
+            for (int i = 0; i < ng; i++) {
+                int c = mul[(size_t)H[q] * G + gens[i]];
+                if (!in[c]) {
+                    in[c] = 1;
+                    H.push_back(c);
+                }
+            }
+    };
+    auto consider = [&]() {
+        int h = (int)H.size();
+        if (h <= 1 || h >= n || n % h) return;
+        if (h + n / h < best_cost) {
+            best_cost = h + n / h;
+            best = H;
+        }
+    };
+    for (int i = 0; i < n && best_cost > target; i++) {
+        closure(grp[i], -1);
+        consider();
+    }
+    for (int i = 0; i < n && best_cost > target; i++)
+        for (int j = i + 1; j < n && best_cost > target; j++) {
+            closure(grp[i], grp[j]);
+            consider();
+        }
+    if (best_cost >= n) return false;
+    std::vector<char> cov(G, 0);
+    std::vector<int> R;
+    for (int g : grp) {
+        if (cov[g]) continue;
+        R.push_back(g);
+        for (int h : best) {
+            int c = mul[(size_t)g * G + h];
+            if (cov[c]) return false;                   // not a partition
+            cov[c] = 1;
+        }
+    }
+    if (R.size() * best.size() != (size_t)n) return false;
+    Hout = best;
+    Rout = R;
+    return true;
 }
 
 // Host plan (no device work): validates the table and picks the factorisation.
@@ -325,12 +409,18 @@ bool plan_host(int N, int G, const int *perm, const double *chars, ProjPlan &P) 
     P.N = N;
     P.G = G;
     P.passes = 1;
+    for (int k = 0; k < ED_MAX_PASSES; k++) P.size[k] = 0;
     P.size[0] = G;
-    P.size[1] = 0;
     P.elems.resize(G);
     for (int g = 0; g < G; g++) P.elems[g] = g;
-    const int target = best_split_cost(G);
-    if (target >= G) return true;
+    auto drop_zero_characters = [&]() {              // the one-pass form skips chi = 0
+        P.elems.clear();
+        for (int g = 0; g < G; g++)
+            if (chars[g] != 0.0) P.elems.push_back(g);
+        P.size[0] = (int)P.elems.size();
+        return true;
+    };
+    if (best_split_cost(G) >= G) return drop_zero_characters();
 
     // Row lookup by content (rows are permutations of N <= 30 sites: hash by a 64-bit mix).
     auto row_hash = [&](const int *r) {
@@ -358,71 +448,27 @@ bool plan_host(int N, int G, const int *perm, const double *chars, ProjPlan &P) 
     for (int a = 0; a < G; a++)
         for (int b = 0; b < G; b++) {
             int c = compose(a, b);
-            if (c < 0 || !close_to(chars[c], chars[a] * chars[b])) return true;
+            if (c < 0 || !close_to(chars[c], chars[a] * chars[b])) return drop_zero_characters();
             mul[(size_t)a * G + b] = c;
         }
-    // Subgroups generated by one or two elements; the first whose cost reaches the target wins.
-    int best_cost = G;
-    std::vector<int> best_H;
-    std::vector<char> in(G);
-    std::vector<int> H;
-    auto closure = [&](int g1, int g2) {
-        std::fill(in.begin(), in.end(), 0);
-        H.clear();
-        int gens[2] = {g1, g2};
-        int ng = g2 < 0 ? 1 : 2;
-        for (int i = 0; i < ng; i++)
-            if (!in[gens[i]]) {
-                in[gens[i]] = 1;
-                H.push_back(gens[i]);
-            }
-        for (size_t q = 0; q < H.size(); q++)
-            for (int i = 0; i < ng; i++) {
-                int c = mul[(size_t)H[q] * G + gens[i]];
-                if (!in[c]) {
-                    in[c] = 1;
-                    H.push_back(c);
-                }
-            }
-    };
-    auto consider = [&]() {
-        int h = (int)H.size();
-        if (h <= 1 || h >= G || G % h) return;
-        int cost = h + G / h;
-        if (cost < best_cost) {
-            best_cost = cost;
-            best_H = H;
-        }
-    };
-    for (int g = 0; g < G && best_cost > target; g++) {
-        closure(g, -1);
-        consider();
+    // Peel subgroups: G = R1 H1, H1 = R2 H2, ...; passes run H_k, R_k, ..., R1.
+    std::vector<int> cur(G);
+    for (int g = 0; g < G; g++) cur[g] = g;
+    std::vector<std::vector<int>> outer;
+    std::vector<int> H, R;
+    while ((int)outer.size() < ED_MAX_PASSES - 1 && split_group(cur, mul, G, H, R)) {
+        outer.push_back(R);
+        cur = H;
     }
-    for (int a = 0; a < G && best_cost > target; a++)
-        for (int b = a + 1; b < G && best_cost > target; b++) {
-            closure(a, b);
-            consider();
-        }
-    if (best_cost >= G) return true;
-    // Left cosets r H: each element exactly once as r o h.
-    std::vector<char> cov(G, 0);
-    std::vector<int> R;
-    for (int g = 0; g < G; g++) {
-        if (cov[g]) continue;
-        R.push_back(g);
-        for (int h : best_H) {
-            int c = mul[(size_t)g * G + h];
-            if (cov[c]) return true;                   // not a partition: stay direct
-            cov[c] = 1;
-        }
+    if (outer.empty()) return drop_zero_characters();
+    P.passes = 1 + (int)outer.size();
+    P.elems = cur;
+    P.size[0] = (int)cur.size();
+    for (int k = 0; k < (int)outer.size(); k++) {
+        const std::vector<int> &r = outer[outer.size() - 1 - k];
+        P.size[k + 1] = (int)r.size();
+        P.elems.insert(P.elems.end(), r.begin(), r.end());
     }
-    if ((int)(R.size() * best_H.size()) != G) return true;
-    P.passes = 2;
-    P.size[0] = (int)best_H.size();
-    P.size[1] = (int)R.size();
-    P.elems.clear();
-    P.elems.insert(P.elems.end(), best_H.begin(), best_H.end());
-    P.elems.insert(P.elems.end(), R.begin(), R.end());
     return true;
 }
 
@@ -493,7 +539,8 @@ bool launch_perm_pass(const ProjPlan &P, int pass, const double *x, double *y, u
             return false;
         attr = true;
     }
-    const int off = pass == 0 ? 0 : P.size[0];
+    int off = 0;
+    for (int k = 0; k < pass; k++) off += P.size[k];
     const int m = P.size[pass];
     const size_t smem = (size_t)m * (ED_TAB * sizeof(unsigned) + sizeof(double));
     NQS_LAUNCH("ed_project_pass");
@@ -506,12 +553,11 @@ bool launch_perm_pass(const ProjPlan &P, int pass, const double *x, double *y, u
 // result is in *a).  part (may be null) receives the partials of the result's norm.
 bool project(const ProjPlan &P, double *&a, double *&t, unsigned dim, double *part, cudaStream_t st) {
     const double invG = 1.0 / (double)P.G;
-    if (P.passes == 2) {
-        return launch_perm_pass(P, 0, a, t, dim, 1.0, nullptr, st) &&
-               launch_perm_pass(P, 1, t, a, dim, invG, part, st);
+    for (int k = 0; k < P.passes; k++) {
+        const bool last = k + 1 == P.passes;
+        if (!launch_perm_pass(P, k, a, t, dim, last ? invG : 1.0, last ? part : nullptr, st)) return false;
+        std::swap(a, t);
     }
-    if (!launch_perm_pass(P, 0, a, t, dim, invG, part, st)) return false;
-    std::swap(a, t);
     return true;
 }
 
@@ -865,20 +911,21 @@ int nqs_gpu_sector_project(int N, int G, const int *perm, const double *chars, c
     if (!P) return -1;
     const unsigned dim = 1u << N;
     cudaStream_t st = ctx().stream;
-    static DevBuf<double> tmp;
-    if (!tmp.ensure(dim)) return -1;
+    static DevBuf<double> tmp[2];
+    if (!tmp[0].ensure(dim) || (P->passes > 2 && !tmp[1].ensure(dim))) return -1;
     const double invG = 1.0 / (double)G;
-    bool ok;
-    if (P->passes == 2) {
-        ok = launch_perm_pass(*P, 0, d_in, tmp.p, dim, 1.0, nullptr, st) &&
-             launch_perm_pass(*P, 1, tmp.p, d_out, dim, invG, nullptr, st);
-    } else if (d_in != d_out) {
-        ok = launch_perm_pass(*P, 0, d_in, d_out, dim, invG, nullptr, st);
-    } else {
-        ok = launch_perm_pass(*P, 0, d_in, tmp.p, dim, invG, nullptr, st) &&
-             NQS_CUDA(cudaMemcpyAsync(d_out, tmp.p, sizeof(double) * dim, cudaMemcpyDeviceToDevice, st));
+    const double *src = d_in;
+    for (int k = 0; k < P->passes; k++) {
+        const bool last = k + 1 == P->passes;
+        double *dst = last ? d_out : tmp[k % 2].p;
+        if (dst == src) dst = tmp[0].p;              // a single pass in place: copied back below
+        if (!launch_perm_pass(*P, k, src, dst, dim, last ? invG : 1.0, nullptr, st)) return -1;
+        src = dst;
     }
-    return ok ? 0 : -1;
+    if (src != d_out &&
+        !NQS_CUDA(cudaMemcpyAsync(d_out, src, sizeof(double) * dim, cudaMemcpyDeviceToDevice, st)))
+        return -1;
+    return 0;
 }
 
 int nqs_gpu_lanczos_seed(int N, int alternate, double *d_out) {
@@ -908,10 +955,8 @@ int nqs_ed_projector_plan(int N, int G, const int *perm, const double *chars, in
     ProjPlan P;
     if (!plan_host(N, G, perm, chars, P)) return -1;
     if (out_passes) *out_passes = P.passes;
-    if (sizes) {
-        sizes[0] = P.size[0];
-        if (P.passes == 2) sizes[1] = P.size[1];
-    }
+    if (sizes)
+        for (int k = 0; k < P.passes; k++) sizes[k] = P.size[k];
     if (elems) std::copy(P.elems.begin(), P.elems.end(), elems);
     return 0;
 }

@@ -599,7 +599,7 @@ def projector_plan(N, perm, chars):
     perm, chars = _perm_args(perm, chars)
     G = len(chars)
     npass = C.c_int()
-    sizes = (C.c_int * 2)()
+    sizes = (C.c_int * 4)()
     elems = np.zeros(G, dtype=np.int32)
     _check(lib().nqs_ed_projector_plan(N, G, _ip(perm), _dp(chars), C.byref(npass), sizes, _ip(elems)),
            "projector plan")
