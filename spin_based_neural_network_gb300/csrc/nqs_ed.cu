@@ -86,15 +86,21 @@ __device__ __forceinline__ double block_total(const double *part, int np) {
     return tot;
 }
 
-// y = H x, H = J sum_b S_u.S_v: diagonal J/4 (nb - 2 n_anti), off-diagonal J/2 for every
-// antiparallel bond (src/nqs/nqs_lanczos.c:380-432).  Within a warp the states differ in
-// bits 0-4 only, so each bond's partner loads fall in one 256-byte segment.  part (may
-// be null) receives the block partials of x.y.
+// y = H x, H = J sum_b S_u.S_v: diagonal J/4 (nb - 2 n_anti) (a table indexed by n_anti),
+// off-diagonal J/2 for every antiparallel bond (src/nqs/nqs_lanczos.c:380-432).  Within a
+// warp the states differ in bits 0-4, so each bond's partner loads of a warp fall in one
+// 256-byte segment.  GB300 issues an FP64 add for a whole warp at 16 cycles whatever its
+// active lanes, so the bonds away from the lane bits -- where all 32 states of the warp
+// agree -- are first collected into a warp-uniform bit mask and only the antiparallel ones
+// are loaded (four at a time) and added.  part (may be null) receives the block partials
+// of x.y.
 __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__restrict__ x, double *__restrict__ y,
                                                             unsigned dim, Bonds B, double qJ, double hJ,
                                                             double *__restrict__ part) {
     __shared__ unsigned sm[ED_MAX_BONDS];
+    __shared__ double diag[ED_MAX_BONDS + 1];
     for (int i = threadIdx.x; i < B.nb; i += ED_THREADS) sm[i] = B.m[i];
+    for (int i = threadIdx.x; i <= B.nb; i += ED_THREADS) diag[i] = qJ * (double)(B.nb - 2 * i);
     __syncthreads();
     const int nb = B.nb, nlow = B.nlow;
     double dot = 0.0;
@@ -110,21 +116,26 @@ __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__rest
                 anti++;
             }
         }
-        // High bonds exist only for N >= 7, where dim is a multiple of 32 and every warp is
-        // full, so the vote is over 32 lanes that already agree: a uniform branch that
-        // skips the FP64 add for the whole warp when its spins are parallel.
-#pragma unroll 4
-        for (int b = nlow; b < nb; b++) {
-            const unsigned m = sm[b];
-            if (__all_sync(0xffffffffu, __popc(s & m) == 1)) {
-                off += __ldg(x + (s ^ m));
-                anti++;
+        uint64_t hm = 0;                                 // antiparallel high bonds (same in all lanes)
+        for (int b = nlow; b < nb; b++) hm |= (uint64_t)(__popc(s & sm[b]) == 1) << (b - nlow);
+        anti += __popcll(hm);
+        while (hm) {
+            double v[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                v[j] = 0.0;
+                if (hm) {
+                    const int b = __ffsll((long long)hm) - 1;
+                    hm &= hm - 1;
+                    v[j] = __ldg(x + (s ^ sm[nlow + b]));
+                }
             }
+            off += (v[0] + v[1]) + (v[2] + v[3]);
         }
         const double xs = __ldg(x + s);
-        const double v = qJ * (double)(nb - 2 * anti) * xs + hJ * off;
-        y[s] = v;
-        dot = fma(xs, v, dot);
+        const double val = fma(diag[anti], xs, hJ * off);
+        y[s] = val;
+        dot = fma(xs, val, dot);
     }
     if (part) block_store(dot, part);
 }
