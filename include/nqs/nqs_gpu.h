@@ -194,6 +194,22 @@ int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int size_x, int size_y,
                           nqs_sr_step_info_t *out_info,
                           double *out_energies, double *out_delta);
 
+/* The excited-state SR step (nqs_sr_step_excited) and the Euler tVMC step
+ * (nqs_tvmc_step_real_time) on a caller-supplied batch: the parity entry points. */
+int nqs_gpu_sr_step_batch_excited(const nqs_config_t *cfg, int size_x, int size_y,
+                                  nqs_ansatz_t *ansatz,
+                                  nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,
+                                  nqs_log_amp_fn_t ref_log_amp_fn, void *ref_log_amp_user,
+                                  double penalty_mu, const int *batch, int num_samples,
+                                  nqs_sr_step_info_t *out_info,
+                                  double *out_energies, double *out_delta);
+int nqs_gpu_tvmc_step_batch(const nqs_config_t *cfg, double dt, int size_x, int size_y,
+                            nqs_ansatz_t *ansatz,
+                            nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,
+                            const int *batch, int num_samples,
+                            nqs_sr_step_info_t *out_info,
+                            double *out_energies, double *out_delta);
+
 /* MinSR solve that allocates no device memory.  It has no counterpart in the
  * upstream library.
  *

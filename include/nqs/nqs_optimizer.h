@@ -163,6 +163,57 @@ int nqs_sr_run_holomorphic_full(const nqs_config_t *cfg,
                                  void *grad_user,
                                  double *out_energy_trace);
 
+/* Replaces upstream nqs_tvmc_step_real_time (include/nqs/nqs_optimizer.h:206-212;
+ * src/nqs/nqs_optimizer.c:888-993): Re(S) delta = Im(F) with
+ * F_k = 2 [Cov(R_k, E_im) - Cov(I_k, E_re)] on the holomorphic metric, CG as in
+ * nqs_sr_step_holomorphic, theta += dt delta (forward Euler).  update_norm uses |dt|. */
+int nqs_tvmc_step_real_time(const nqs_config_t *cfg, double dt,
+                             int size_x, int size_y,
+                             nqs_ansatz_t *ansatz,
+                             nqs_sampler_t *sampler,
+                             nqs_log_amp_fn_t log_amp_fn,
+                             void *log_amp_user,
+                             nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_step_excited (include/nqs/nqs_optimizer.h:242-251;
+ * src/nqs/nqs_optimizer.c:562-723): holomorphic SR with the local energies augmented by
+ * penalty_mu r(s) conj(<r>), r = psi_ref / psi (log-modulus difference clamped to +-10);
+ * mean_energy reports the physical energy. */
+int nqs_sr_step_excited(const nqs_config_t *cfg,
+                         int size_x, int size_y,
+                         nqs_ansatz_t *ansatz,
+                         nqs_sampler_t *sampler,
+                         nqs_log_amp_fn_t log_amp_fn,
+                         void *log_amp_user,
+                         nqs_log_amp_fn_t ref_log_amp_fn,
+                         void *ref_log_amp_user,
+                         double penalty_mu,
+                         nqs_sr_step_info_t *out_info);
+
+/* Replaces upstream nqs_sr_run_excited (include/nqs/nqs_optimizer.h:253-262). */
+int nqs_sr_run_excited(const nqs_config_t *cfg,
+                        int size_x, int size_y,
+                        nqs_ansatz_t *ansatz,
+                        nqs_sampler_t *sampler,
+                        nqs_log_amp_fn_t log_amp_fn,
+                        void *log_amp_user,
+                        nqs_log_amp_fn_t ref_log_amp_fn,
+                        void *ref_log_amp_user,
+                        double penalty_mu,
+                        double *out_energy_trace);
+
+/* Replaces upstream nqs_tvmc_step_heun (include/nqs/nqs_optimizer.h:267-273;
+ * src/nqs/nqs_optimizer.c:815-886): k1 = delta(theta), k2 = delta(theta + dt k1) from a
+ * second sampling, theta += dt (k1 + k2) / 2; mean / variance from the first evaluation,
+ * cg_iterations summed, converged if both solves converged. */
+int nqs_tvmc_step_heun(const nqs_config_t *cfg, double dt,
+                        int size_x, int size_y,
+                        nqs_ansatz_t *ansatz,
+                        nqs_sampler_t *sampler,
+                        nqs_log_amp_fn_t log_amp_fn,
+                        void *log_amp_user,
+                        nqs_sr_step_info_t *out_info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -147,6 +147,20 @@ int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, i
                      double *params_inout, long P, double *out_energies,
                      double *out_delta, or_step_info_t *info);
 
+/* Excited-state SR, src/nqs/nqs_optimizer.c:562-723: the holomorphic step with
+ * E_loc += mu r conj(<r>), r = psi_ref / psi (log-modulus difference clamped to +-10), the
+ * force's means <E_re> + mu |<r>|^2 and <E_im> + mu (<r_im><r_re> - <r_re><r_im>); the
+ * step info reports the physical energy; out_E the augmented local energies. */
+int oracle_excited_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu,
+                        const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
+                        double *params_inout, long P, double *out_energies, double *out_delta,
+                        or_step_info_t *info);
+/* Real-time tVMC, forward Euler, src/nqs/nqs_optimizer.c:888-993: F_k = 2 [(R^T E_im -
+ * I^T E_re) / N_s - <R><E_im> + <I><E_re>], CG on the holomorphic QGT, theta += dt delta. */
+int oracle_tvmc_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns, double shift,
+                     double dt, int max_iters, double tol, double *params_inout, long P,
+                     double *out_energies, double *out_delta, or_step_info_t *info);
+
 /* Exact ground-state energy by Lanczos with full re-orthogonalisation (the
  * upstream src/mps/lanczos.c:119-303 scheme) over either the full 2^N basis
  * (n_down < 0) or the fixed-magnetisation sector with n_down down spins

@@ -371,7 +371,7 @@ int oracle_cgsr_step(const or_ham_t *h, const or_amp_t *amp, int grad_mode,
     if (info) {
         info->mean_energy = em;
         info->variance_energy = esq - em * em;
-        info->update_norm = sqrt(vdot(d, d, P)) * lr;
+        info->update_norm = sqrt(vdot(d, d, P)) * fabs(lr);
         info->cg_iterations = it;
         info->converged = conv;
     }
@@ -408,9 +408,37 @@ static void qgt_complex_apply(const double *R, const double *I, long Ns, long P,
     }
 }
 
+/* The holomorphic family on one batch: mode 0 holomorphic SR (src/nqs/nqs_optimizer.c:415-524),
+ * 1 excited-state SR (the penalty of :600-658 on top of mode 0; ref and mu used), 2 the
+ * real-time tVMC force with theta += dt delta (:888-993; lr carries -dt). */
+static int holo_family_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu, int mode,
+                            const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
+                            double *params, long P, double *out_E, double *out_delta, or_step_info_t *info);
+
 int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns,
                      double shift, double lr, int max_iters, double tol,
                      double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
+    return holo_family_step(h, amp, NULL, 0.0, 0, batch, Ns, shift, lr, max_iters, tol, params, P, out_E,
+                            out_delta, info);
+}
+
+int oracle_excited_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu,
+                        const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
+                        double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
+    return holo_family_step(h, amp, ref, mu, 1, batch, Ns, shift, lr, max_iters, tol, params, P, out_E,
+                            out_delta, info);
+}
+
+int oracle_tvmc_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns, double shift,
+                     double dt, int max_iters, double tol, double *params, long P, double *out_E,
+                     double *out_delta, or_step_info_t *info) {
+    return holo_family_step(h, amp, NULL, 0.0, 2, batch, Ns, shift, -dt, max_iters, tol, params, P, out_E,
+                            out_delta, info);
+}
+
+static int holo_family_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu, int mode,
+                            const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
+                            double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
     double *Er = malloc(sizeof(double) * (size_t)Ns), *Ei = malloc(sizeof(double) * (size_t)Ns);
     double *R = malloc(sizeof(double) * (size_t)Ns * P), *I = malloc(sizeof(double) * (size_t)Ns * P);
     double *Rm = calloc((size_t)P, sizeof(double)), *Im = calloc((size_t)P, sizeof(double));
@@ -423,15 +451,47 @@ int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, i
     double erm = 0.0, eim = 0.0, ersq = 0.0;                           /* :471-481 */
     for (int i = 0; i < Ns; i++) { erm += Er[i]; eim += Ei[i]; ersq += Er[i] * Er[i]; }
     erm /= (double)Ns; eim /= (double)Ns; ersq /= (double)Ns;
+    double erm_f = erm, eim_f = eim;                  /* the means the force uses */
+    if (mode == 1) {                                  /* :600-658: penalty mu r conj(<r>) */
+        double *rr = malloc(sizeof(double) * (size_t)Ns), *ri = malloc(sizeof(double) * (size_t)Ns);
+        double *la = malloc(sizeof(double) * (size_t)Ns), *ar = malloc(sizeof(double) * (size_t)Ns);
+        double *lb = malloc(sizeof(double) * (size_t)Ns), *br = malloc(sizeof(double) * (size_t)Ns);
+        oracle_log_amp_batch(amp, batch, Ns, la, ar);
+        oracle_log_amp_batch(ref, batch, Ns, lb, br);
+        double Rr = 0.0, Ri = 0.0;
+        for (int i = 0; i < Ns; i++) {
+            double dl = lb[i] - la[i];
+            if (dl > 10.0) dl = 10.0;
+            if (dl < -10.0) dl = -10.0;
+            double m = exp(dl), th = br[i] - ar[i];
+            rr[i] = m * cos(th);
+            ri[i] = m * sin(th);
+            Rr += rr[i];
+            Ri += ri[i];
+        }
+        Rr /= (double)Ns;
+        Ri /= (double)Ns;
+        for (int i = 0; i < Ns; i++) {
+            Er[i] += mu * (rr[i] * Rr + ri[i] * Ri);
+            Ei[i] += mu * (ri[i] * Rr - rr[i] * Ri);
+        }
+        erm_f = erm + mu * (Rr * Rr + Ri * Ri);
+        eim_f = eim + mu * (Ri * Rr - Rr * Ri);
+        free(rr); free(ri); free(la); free(ar); free(lb); free(br);
+    }
     for (long k = 0; k < P; k++) {                                     /* :483-498 */
-        double sR = 0.0, sI = 0.0, sRe = 0.0, sIe = 0.0;
+        double sR = 0.0, sI = 0.0, sRe = 0.0, sIe = 0.0, sRi = 0.0, sIr = 0.0;
         for (int i = 0; i < Ns; i++) {
             double rk = R[(size_t)i * P + k], ik = I[(size_t)i * P + k];
             sR += rk; sI += ik; sRe += rk * Er[i]; sIe += ik * Ei[i];
+            sRi += rk * Ei[i]; sIr += ik * Er[i];
         }
         Rm[k] = sR / (double)Ns;
         Im[k] = sI / (double)Ns;
-        F[k] = 2.0 * ((sRe + sIe) / (double)Ns - Rm[k] * erm - Im[k] * eim);
+        if (mode == 2)                                                 /* :929-941 */
+            F[k] = 2.0 * ((sRi - sIr) / (double)Ns - Rm[k] * eim + Im[k] * erm);
+        else
+            F[k] = 2.0 * ((sRe + sIe) / (double)Ns - Rm[k] * erm_f - Im[k] * eim_f);
     }
     memcpy(r, F, sizeof(double) * (size_t)P);                          /* cg_solve_complex */
     memcpy(p, r, sizeof(double) * (size_t)P);
@@ -454,7 +514,7 @@ int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, i
     if (info) {
         info->mean_energy = erm;
         info->variance_energy = ersq - erm * erm;
-        info->update_norm = sqrt(vdot(d, d, P)) * lr;
+        info->update_norm = sqrt(vdot(d, d, P)) * fabs(lr);
         info->cg_iterations = it;
         info->converged = conv;
     }

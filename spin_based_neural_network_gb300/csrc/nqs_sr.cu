@@ -24,6 +24,8 @@ bool sampler_produce(Sampler *s, int n, uint64_t **d_out);
 struct Workspace {
     DevBuf<double> E, Ei, eps, O, gm, T, T0, y, z, delta, scal, F, r, p, Ap, u, part, y64, d64, es;
     DevBuf<double> Oi, gm2, F2, scal2, eps2, es2;     // holomorphic SR: imaginary halves
+    DevBuf<double> la, ar, la_ref, ar_ref, aug;       // excited-state SR: amplitude ratios, augmented means
+    DevBuf<double> theta0, kacc;                      // Heun tVMC: parameter snapshot, averaged slope
     DevBuf<int> status;
     DevBuf<uint64_t> batch_bits;
 };
@@ -631,16 +633,70 @@ struct StepIn {
     void *user;
     nqs_gradient_fn_t gfn;
     void *guser;
-    int minsr;                         // 0 CG-SR, 1 MinSR, 2 holomorphic SR (CG on the complex QGT)
+    // 0 CG-SR, 1 MinSR, 2 holomorphic SR (CG on the complex QGT), 3 excited-state SR (2 with
+    // the orthogonality penalty), 4 real-time tVMC force (same metric)
+    int minsr;
     nqs_holomorphic_gradient_fn_t hgfn;
     void *hguser;
+    nqs_log_amp_fn_t ref_fn;           // excited-state SR: the reference wavefunction
+    void *ref_user;
+    double mu;                         //   and the penalty strength
+    int custom_scale;                  // 1: params += scale * delta (tVMC), else -= lr * delta
+    double scale;
+    int no_apply;                      // 1: leave delta in the workspace, parameters unchanged
 };
 
-// F = 2 (F_R + F_I): the holomorphic force from the real and imaginary halves
-// (src/nqs/nqs_optimizer.c:471-498)
-__global__ void k_holo_force(double *F, const double *__restrict__ F2, long P) {
+// F = 2 (F_R + sign F_I): the holomorphic force (sign +1, src/nqs/nqs_optimizer.c:471-498)
+// and the real-time force (sign -1 with the energy halves swapped, :929-941)
+__global__ void k_holo_force(double *F, const double *__restrict__ F2, long P, double sign) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < P; k += (long)gridDim.x * blockDim.x)
-        F[k] = 2.0 * (F[k] + F2[k]);
+        F[k] = 2.0 * (F[k] + sign * F2[k]);
+}
+
+// Excited-state penalty (src/nqs/nqs_optimizer.c:600-658): r_i = psi_ref / psi at sample i
+// with the log-modulus difference clamped to +-10, <r> over the batch, then
+// E_i += mu r_i conj(<r>) and the augmented means
+// <E_re> + mu |<r>|^2, <E_im> + mu (<r_im><r_re> - <r_re><r_im>) into aug[S_EMEAN] and
+// aug[16 + S_EMEAN].  One block; the sums run in a fixed order.
+__global__ void k_excited_augment(double *Er, double *Ei, const double *__restrict__ la,
+                                  const double *__restrict__ ar, const double *__restrict__ lr,
+                                  const double *__restrict__ arr, int Ns, double mu, const double *scal,
+                                  const double *scal2, double *aug) {
+    __shared__ double sr[1024], si[1024];
+    const double cap = 10.0;
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < Ns; i += blockDim.x) {
+        double d = fmin(fmax(lr[i] - la[i], -cap), cap), m = exp(d), th = arr[i] - ar[i];
+        a += m * cos(th);
+        b += m * sin(th);
+    }
+    sr[threadIdx.x] = a;
+    si[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sr[threadIdx.x] += sr[threadIdx.x + o];
+            si[threadIdx.x] += si[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    const double Rr = sr[0] / (double)Ns, Ri = si[0] / (double)Ns;
+    for (int i = threadIdx.x; i < Ns; i += blockDim.x) {
+        double d = fmin(fmax(lr[i] - la[i], -cap), cap), m = exp(d), th = arr[i] - ar[i];
+        const double rr = m * cos(th), ri = m * sin(th);
+        Er[i] += mu * (rr * Rr + ri * Ri);
+        Ei[i] += mu * (ri * Rr - rr * Ri);
+    }
+    if (threadIdx.x == 0) {
+        aug[S_EMEAN] = scal[S_EMEAN] + mu * (Rr * Rr + Ri * Ri);
+        aug[16 + S_EMEAN] = scal2[S_EMEAN] + mu * (Ri * Rr - Rr * Ri);
+    }
+}
+
+// k1 <- (k1 + k2) / 2 (Heun's averaged slope, src/nqs/nqs_optimizer.c:864)
+__global__ void k_heun_average(double *k1, const double *__restrict__ k2, long P) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < P; k += (long)gridDim.x * blockDim.x)
+        k1[k] = 0.5 * (k1[k] + k2[k]);
 }
 
 // Column means of O (and the CG-SR force F when E != NULL) over a 2-D grid of
@@ -824,7 +880,11 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         set_error("gradient callback is not supported on the GPU (NULL or nqs_symproj_gradient)");
         return -1;
     }
-    const bool holo = in.minsr == 2;
+    const bool holo = in.minsr >= 2, excited = in.minsr == 3, realtime = in.minsr == 4;
+    if (excited && !in.ref_fn) {
+        set_error("excited-state SR needs the reference log-amplitude");
+        return -1;
+    }
     if (holo && in.hgfn) {
         set_error("holomorphic gradient callback is not supported on the GPU (NULL: the base ansatz gradient)");
         return -1;
@@ -835,6 +895,10 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         return -1;
     if (holo && (!w.Oi.ensure((size_t)Ns * P) || !w.gm2.ensure(P) || !w.F2.ensure(P) || !w.scal2.ensure(16) ||
                  !w.eps2.ensure(Ns)))
+        return -1;
+    DevAmp Aref;
+    if (excited && (!build_amp(in.ref_fn, in.ref_user, H.N, &Aref, nullptr) || !w.la.ensure(Ns) ||
+                    !w.ar.ensure(Ns) || !w.la_ref.ensure(Ns) || !w.ar_ref.ensure(Ns) || !w.aug.ensure(32)))
         return -1;
     // 1. samples
     uint64_t *bits = nullptr;
@@ -897,6 +961,15 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         if (holo && (!ensure_energy_scratch(w.es2, Ns) ||
                      !enqueue_energy_stats(w.Ei.p, Ns, 0, w.scal2.p, w.eps2.p, w.es2.p)))
             return -1;
+        // excited-state SR: the physical statistics stay in scal for the step info; the force
+        // takes the augmented local energies and means
+        if (excited) {
+            if (!launch_log_amp(A, bits, Ns, w.la.p, w.ar.p) || !launch_log_amp(Aref, bits, Ns, w.la_ref.p, w.ar_ref.p))
+                return -1;
+            NQS_LAUNCH("excited_penalty");
+            k_excited_augment<<<1, 1024, 0, st>>>(w.E.p, w.Ei.p, w.la.p, w.ar.p, w.la_ref.p, w.ar_ref.p, Ns, in.mu,
+                                                  w.scal.p, w.scal2.p, w.aug.p);
+        }
     }
     NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
     dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
@@ -972,11 +1045,20 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             return -1;
         {
             NQS_LAUNCH("col_stats");
-            if (!col_stats(w.O.p, Ns, P, w.E.p, w.scal.p, w.gm.p, w.F.p)) return -1;
-            if (holo) {
-                // <I>, (I^T E_im) / N_s - <I> <E_im>; then F = 2 (F_R + F_I)
-                if (!col_stats(w.Oi.p, Ns, P, w.Ei.p, w.scal2.p, w.gm2.p, w.F2.p)) return -1;
-                k_holo_force<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(w.F.p, w.F2.p, P);
+            if (realtime) {
+                // F = 2 [(R^T E_im - I^T E_re) / N_s - <R><E_im> + <I><E_re>]
+                if (!col_stats(w.O.p, Ns, P, w.Ei.p, w.scal2.p, w.gm.p, w.F.p) ||
+                    !col_stats(w.Oi.p, Ns, P, w.E.p, w.scal.p, w.gm2.p, w.F2.p))
+                    return -1;
+                k_holo_force<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(w.F.p, w.F2.p, P, -1.0);
+            } else {
+                const double *m_re = excited ? w.aug.p : w.scal.p, *m_im = excited ? w.aug.p + 16 : w.scal2.p;
+                if (!col_stats(w.O.p, Ns, P, w.E.p, m_re, w.gm.p, w.F.p)) return -1;
+                if (holo) {
+                    // <I>, (I^T E_im) / N_s - <I> <E_im>; then F = 2 (F_R + F_I)
+                    if (!col_stats(w.Oi.p, Ns, P, w.Ei.p, m_im, w.gm2.p, w.F2.p)) return -1;
+                    k_holo_force<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(w.F.p, w.F2.p, P, 1.0);
+                }
             }
         }
         const int maxit = cfg->sr_cg_max_iters;
@@ -996,10 +1078,11 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             fprintf(stderr, "nqs_sr cg_solve: Krylov breakdown at iter=%d, pAp=%.3e. Returning "
                             "unconverged partial step.\n", h[I_ITERS], hs[S_PAP]);
     }
-    // 4. update
-    {
+    // 4. update: theta -= lr delta, or theta += scale delta for tVMC
+    const double lr_eff = in.custom_scale ? -in.scale : cfg->learning_rate;
+    if (!in.no_apply) {
         NQS_LAUNCH("apply_update");
-        k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.delta.p, P, cfg->learning_rate, w.scal.p, w.status.p, 0);
+        k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.delta.p, P, lr_eff, w.scal.p, w.status.p, 0);
     }
     if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a)) return -1;
     double hs[16];
@@ -1016,7 +1099,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     if (info) {
         info->mean_energy = hs[S_EMEAN];
         info->variance_energy = hs[S_ESQ] - hs[S_EMEAN] * hs[S_EMEAN];
-        info->update_norm = sqrt(hs[S_NORM2]) * cfg->learning_rate;
+        info->update_norm = in.no_apply ? 0.0 : sqrt(hs[S_NORM2]) * fabs(lr_eff);
         info->acceptance_ratio = in.sampler ? nqs_sampler_acceptance_ratio((nqs_sampler_t *)in.sampler) : 0.0;
         info->cg_iterations = in.minsr == 1 ? 0 : cg_iters;
         info->converged = converged;
@@ -1173,6 +1256,116 @@ int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t 
     if (!cfg || !a || !batch || Ns <= 0) return -1;
     StepIn in{cfg, sx, sy, (Ansatz *)a, nullptr, batch, Ns, fn, user, gfn, guser, minsr};
     return sr_step_impl(in, info, out_E, out_delta);
+}
+
+int nqs_gpu_sr_step_batch_excited(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_log_amp_fn_t fn,
+                                  void *user, nqs_log_amp_fn_t ref_fn, void *ref_user, double mu, const int *batch,
+                                  int Ns, nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
+    if (!cfg || !a || !batch || Ns <= 0 || !ref_fn) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, nullptr, batch, Ns, fn, user, nullptr, nullptr, 3, nullptr, nullptr,
+              ref_fn, ref_user, mu, 0, 0.0, 0};
+    return sr_step_impl(in, info, out_E, out_delta);
+}
+
+int nqs_gpu_tvmc_step_batch(const nqs_config_t *cfg, double dt, int sx, int sy, nqs_ansatz_t *a,
+                            nqs_log_amp_fn_t fn, void *user, const int *batch, int Ns, nqs_sr_step_info_t *info,
+                            double *out_E, double *out_delta) {
+    if (!cfg || !a || !batch || Ns <= 0) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, nullptr, batch, Ns, fn, user, nullptr, nullptr, 4, nullptr, nullptr,
+              nullptr, nullptr, 0.0, 1, dt, 0};
+    return sr_step_impl(in, info, out_E, out_delta);
+}
+
+// Excited-state SR, src/nqs/nqs_optimizer.c:562-742: the holomorphic step with the
+// orthogonality penalty mu r(s) conj(<r>) added to the local energies for the force; the
+// step info reports the physical energy.
+int nqs_sr_step_excited(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                        nqs_log_amp_fn_t fn, void *user, nqs_log_amp_fn_t ref_fn, void *ref_user, double mu,
+                        nqs_sr_step_info_t *info) {
+    if (!cfg || !a || !s || !ref_fn) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, (Sampler *)s, nullptr, cfg->num_samples, fn, user, nullptr, nullptr, 3,
+              nullptr, nullptr, ref_fn, ref_user, mu, 0, 0.0, 0};
+    if (nqs_sampler_num_sites(s) != ((Ansatz *)a)->N) {
+        set_error("sampler and ansatz disagree on num_sites");
+        return -1;
+    }
+    return sr_step_impl(in, info, nullptr, nullptr);
+}
+
+int nqs_sr_run_excited(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                       nqs_log_amp_fn_t fn, void *user, nqs_log_amp_fn_t ref_fn, void *ref_user, double mu,
+                       double *trace) {
+    if (!cfg || !a || !s || !ref_fn) return -1;        // src/nqs/nqs_optimizer.c:725-742
+    nqs_sampler_thermalize(s);
+    for (int it = 0; it < cfg->num_iterations; it++) {
+        nqs_sr_step_info_t info;
+        int rc = nqs_sr_step_excited(cfg, sx, sy, a, s, fn, user, ref_fn, ref_user, mu, &info);
+        if (rc != 0) return rc;
+        if (trace) trace[it] = info.mean_energy;
+    }
+    return 0;
+}
+
+// Real-time tVMC, forward Euler (src/nqs/nqs_optimizer.c:888-993): Re(S) delta = Im(F)
+// on the holomorphic metric, theta += dt delta.
+int nqs_tvmc_step_real_time(const nqs_config_t *cfg, double dt, int sx, int sy, nqs_ansatz_t *a,
+                            nqs_sampler_t *s, nqs_log_amp_fn_t fn, void *user, nqs_sr_step_info_t *info) {
+    if (!cfg || !a || !s) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, (Sampler *)s, nullptr, cfg->num_samples, fn, user, nullptr, nullptr, 4,
+              nullptr, nullptr, nullptr, nullptr, 0.0, 1, dt, 0};
+    if (nqs_sampler_num_sites(s) != ((Ansatz *)a)->N) {
+        set_error("sampler and ansatz disagree on num_sites");
+        return -1;
+    }
+    return sr_step_impl(in, info, nullptr, nullptr);
+}
+
+// Real-time tVMC, Heun (src/nqs/nqs_optimizer.c:815-886): k1 at theta, k2 at theta + dt k1
+// (a second sampling), theta += dt (k1 + k2) / 2.  The snapshot, probe and average stay on
+// the device.
+int nqs_tvmc_step_heun(const nqs_config_t *cfg, double dt, int sx, int sy, nqs_ansatz_t *ah, nqs_sampler_t *s,
+                       nqs_log_amp_fn_t fn, void *user, nqs_sr_step_info_t *info) {
+    if (!cfg || !ah || !s) return -1;
+    Ansatz *a = (Ansatz *)ah;
+    if (nqs_sampler_num_sites(s) != a->N) {
+        set_error("sampler and ansatz disagree on num_sites");
+        return -1;
+    }
+    StepIn in{cfg, sx, sy, a, (Sampler *)s, nullptr, cfg->num_samples, fn, user, nullptr, nullptr, 4,
+              nullptr, nullptr, nullptr, nullptr, 0.0, 1, dt, 1};
+    nqs_sr_step_info_t i1{}, i2{};
+    if (sr_step_impl(in, &i1, nullptr, nullptr) != 0) return -1;      // k1 in the workspace, theta unchanged
+    Workspace &w = g_ws;
+    const long P = a->P;
+    cudaStream_t st = ctx().stream;
+    if (!w.theta0.ensure(P) || !w.kacc.ensure(P) ||
+        !NQS_CUDA(cudaMemcpyAsync(w.theta0.p, a->d_params.p, sizeof(double) * P, cudaMemcpyDeviceToDevice, st)) ||
+        !NQS_CUDA(cudaMemcpyAsync(w.kacc.p, w.delta.p, sizeof(double) * P, cudaMemcpyDeviceToDevice, st)))
+        return -1;
+    k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.kacc.p, P, -dt, w.scal.p, w.status.p, 0);   // theta0 + dt k1
+    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a)) return -1;
+    const int rc2 = sr_step_impl(in, &i2, nullptr, nullptr);                                  // k2
+    if (!NQS_CUDA(cudaMemcpyAsync(a->d_params.p, w.theta0.p, sizeof(double) * P, cudaMemcpyDeviceToDevice, st)))
+        return -1;
+    if (rc2 == 0) {
+        k_heun_average<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(w.kacc.p, w.delta.p, P);
+        k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.kacc.p, P, -dt, w.scal.p, w.status.p, 0);
+    }
+    double norm2 = 0.0;
+    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a) ||
+        !NQS_CUDA(cudaMemcpyAsync(&norm2, w.scal.p + S_NORM2, sizeof(double), cudaMemcpyDeviceToHost, st)) ||
+        !ansatz_pull(a))
+        return -1;
+    if (rc2 != 0) return rc2;
+    if (info) {
+        info->mean_energy = i1.mean_energy;
+        info->variance_energy = i1.variance_energy;
+        info->update_norm = sqrt(norm2) * fabs(dt);
+        info->acceptance_ratio = nqs_sampler_acceptance_ratio(s);
+        info->cg_iterations = i1.cg_iterations + i2.cg_iterations;
+        info->converged = i1.converged && i2.converged;
+    }
+    return 0;
 }
 
 }  // extern "C"

@@ -56,6 +56,14 @@ def _declare(L):
         "nqs_sr_run_custom_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, DP]),
         "nqs_sr_step_holomorphic_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_holomorphic": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
+        "nqs_sr_step_excited": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, C.c_double, infop]),
+        "nqs_sr_run_excited": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, C.c_double, DP]),
+        "nqs_tvmc_step_real_time": (C.c_int, [cfgp, C.c_double, C.c_int, C.c_int, VP, VP, VP, VP, infop]),
+        "nqs_tvmc_step_heun": (C.c_int, [cfgp, C.c_double, C.c_int, C.c_int, VP, VP, VP, VP, infop]),
+        "nqs_gpu_sr_step_batch_excited": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, C.c_double, IP,
+                                                    C.c_int, infop, DP, DP]),
+        "nqs_gpu_tvmc_step_batch": (C.c_int, [cfgp, C.c_double, C.c_int, C.c_int, VP, VP, VP, IP, C.c_int, infop,
+                                              DP, DP]),
         "nqs_sr_step_minsr_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_minsr": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
         "nqs_marshall_parity": (C.c_int, [IP, C.c_int, C.c_int]),
@@ -390,6 +398,50 @@ def sr_step_batch(cfg, size_x, size_y, ansatz, batch, minsr=True, log_amp_fn=Non
     _check(lib().nqs_gpu_sr_step_batch(C.byref(cfg), size_x, size_y, ansatz.h, log_amp_fn, user, grad_fn,
                                        grad_user, _ip(s), Ns, int(minsr), C.byref(info), _dp(E), _dp(d)),
            "nqs_gpu_sr_step_batch")
+    return info, E, d
+
+
+def sr_step_excited(cfg, size_x, size_y, ansatz, sampler, ref_log_amp_fn, ref_user, mu, log_amp_fn=None,
+                    user=None):
+    """nqs_sr_step_excited (upstream include/nqs/nqs_optimizer.h:242): holomorphic SR with
+    the orthogonality penalty against the reference wavefunction."""
+    info = abi.StepInfo()
+    _check(lib().nqs_sr_step_excited(C.byref(cfg), size_x, size_y, ansatz.h, sampler.h, log_amp_fn, user,
+                                     ref_log_amp_fn, ref_user, mu, C.byref(info)), "nqs_sr_step_excited")
+    return info
+
+
+def tvmc_step(cfg, dt, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, heun=False):
+    """nqs_tvmc_step_real_time (forward Euler) or nqs_tvmc_step_heun (upstream
+    include/nqs/nqs_optimizer.h:206, :267)."""
+    info = abi.StepInfo()
+    f = lib().nqs_tvmc_step_heun if heun else lib().nqs_tvmc_step_real_time
+    _check(f(C.byref(cfg), dt, size_x, size_y, ansatz.h, sampler.h, log_amp_fn, user, C.byref(info)),
+           "tvmc step")
+    return info
+
+
+def excited_step_batch(cfg, size_x, size_y, ansatz, batch, ref_log_amp_fn, ref_user, mu, log_amp_fn=None,
+                       user=None):
+    """Excited-state SR on a caller-supplied batch; returns (info, augmented energies, delta)."""
+    s = spins_array(batch, ansatz.N)
+    Ns = s.shape[0]
+    E, d = np.zeros(Ns), np.zeros(ansatz.P)
+    info = abi.StepInfo()
+    _check(lib().nqs_gpu_sr_step_batch_excited(C.byref(cfg), size_x, size_y, ansatz.h, log_amp_fn, user,
+                                               ref_log_amp_fn, ref_user, mu, _ip(s), Ns, C.byref(info), _dp(E),
+                                               _dp(d)), "nqs_gpu_sr_step_batch_excited")
+    return info, E, d
+
+
+def tvmc_step_batch(cfg, dt, size_x, size_y, ansatz, batch, log_amp_fn=None, user=None):
+    """Forward-Euler real-time tVMC step on a caller-supplied batch; returns (info, energies, delta)."""
+    s = spins_array(batch, ansatz.N)
+    Ns = s.shape[0]
+    E, d = np.zeros(Ns), np.zeros(ansatz.P)
+    info = abi.StepInfo()
+    _check(lib().nqs_gpu_tvmc_step_batch(C.byref(cfg), dt, size_x, size_y, ansatz.h, log_amp_fn, user, _ip(s), Ns,
+                                         C.byref(info), _dp(E), _dp(d)), "nqs_gpu_tvmc_step_batch")
     return info, E, d
 
 

@@ -98,6 +98,11 @@ def lib():
                                        DP, DP, C.POINTER(OrStepInfo)]
         L.oracle_holo_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), IP, C.c_int, C.c_double, C.c_double,
                                        C.c_int, C.c_double, DP, C.c_long, DP, DP, C.POINTER(OrStepInfo)]
+        L.oracle_excited_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), C.POINTER(OrAmp), C.c_double, IP,
+                                          C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, DP, C.c_long,
+                                          DP, DP, C.POINTER(OrStepInfo)]
+        L.oracle_tvmc_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), IP, C.c_int, C.c_double, C.c_double,
+                                       C.c_int, C.c_double, DP, C.c_long, DP, DP, C.POINTER(OrStepInfo)]
         L.oracle_exact_energy.argtypes = [C.POINTER(OrHam), C.c_int, C.c_int, C.c_double, DP]
     return _LIB
 
@@ -254,6 +259,31 @@ def holo_step(h, amp, batch, shift, lr, max_iters, tol):
     E, d = np.zeros(Ns), np.zeros(P)
     info = OrStepInfo()
     assert lib().oracle_holo_step(C.byref(h), amp.ref(), ip(batch), Ns, shift, lr, max_iters, tol,
+                                  dp(amp.params), P, dp(E), dp(d), C.byref(info)) == 0
+    return E, d, info
+
+
+def excited_step(h, amp, ref, mu, batch, shift, lr, max_iters, tol):
+    """Excited-state SR on a batch (src/nqs/nqs_optimizer.c:562-723); returns the
+    augmented local energies, the update and the info."""
+    batch = np.ascontiguousarray(batch, dtype=np.int32)
+    Ns = batch.shape[0]
+    P = len(amp.params)
+    E, d = np.zeros(Ns), np.zeros(P)
+    info = OrStepInfo()
+    assert lib().oracle_excited_step(C.byref(h), amp.ref(), ref.ref(), mu, ip(batch), Ns, shift, lr, max_iters,
+                                     tol, dp(amp.params), P, dp(E), dp(d), C.byref(info)) == 0
+    return E, d, info
+
+
+def tvmc_step(h, amp, batch, shift, dt, max_iters, tol):
+    """Forward-Euler real-time tVMC step on a batch (src/nqs/nqs_optimizer.c:888-993)."""
+    batch = np.ascontiguousarray(batch, dtype=np.int32)
+    Ns = batch.shape[0]
+    P = len(amp.params)
+    E, d = np.zeros(Ns), np.zeros(P)
+    info = OrStepInfo()
+    assert lib().oracle_tvmc_step(C.byref(h), amp.ref(), ip(batch), Ns, shift, dt, max_iters, tol,
                                   dp(amp.params), P, dp(E), dp(d), C.byref(info)) == 0
     return E, d, info
 

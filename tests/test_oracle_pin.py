@@ -183,3 +183,75 @@ def test_holomorphic_step_reduces_to_cg_sr_for_a_real_rbm():
     assert ih.converged == 1 and ic.converged == 1
     assert np.array_equal(Eh, Ec)
     assert np.linalg.norm(dh - dc) <= 1e-8 * np.linalg.norm(dc)
+
+
+def _holo_dense(R, I, Er, Ei, erm, eim, shift, realtime=False):
+    """Dense restatement of the holomorphic family's linear system: G = 2 [(R^T R + I^T I)/N_s
+    - <R><R>^T - <I><I>^T] + eps 1 and the force of src/nqs/nqs_optimizer.c:483-498 (or
+    :929-941 for the real-time force)."""
+    Ns = R.shape[0]
+    Rm, Im = R.mean(0), I.mean(0)
+    G = 2.0 * ((R.T @ R + I.T @ I) / Ns - np.outer(Rm, Rm) - np.outer(Im, Im)) + shift * np.eye(R.shape[1])
+    if realtime:
+        F = 2.0 * ((R.T @ Ei - I.T @ Er) / Ns - Rm * eim + Im * erm)
+    else:
+        F = 2.0 * ((R.T @ Er + I.T @ Ei) / Ns - Rm * erm - Im * eim)
+    return np.linalg.solve(G, F)
+
+
+def _holo_case():
+    N, M = 8, 6
+    p = O.init_params(O.OR_CRBM, N, M, 0.3, 21)
+    pref = O.init_params(O.OR_CRBM, N, M, 0.3, 22)
+    rng = np.random.default_rng(5)
+    batch = rng.choice(np.array([-1, 1], np.int32), size=(192, N))
+    return N, M, p, pref, batch, O.ham(O.OR_TFIM, N, 1, Gamma=0.8)
+
+
+def test_excited_step_with_zero_penalty_is_holomorphic_sr():
+    """Excited-state SR restated from src/nqs/nqs_optimizer.c:562-723: with mu = 0 the local
+    energies and the force's means are unchanged, so the step is the holomorphic step bit
+    for bit (the upstream unit test checks the same equivalence on energy traces)."""
+    N, M, p, pref, batch, h = _holo_case()
+    Eh, dh, ih = O.holo_step(h, O.Amp(O.OR_CRBM, N, M, p.copy()), batch, 1e-2, 0.02, 50, 1e-10)
+    Ee, de, ie = O.excited_step(h, O.Amp(O.OR_CRBM, N, M, p.copy()), O.Amp(O.OR_CRBM, N, M, pref.copy()), 0.0,
+                                batch, 1e-2, 0.02, 50, 1e-10)
+    assert np.array_equal(Eh, Ee) and np.array_equal(dh, de)
+    assert ih.mean_energy == ie.mean_energy and ih.cg_iterations == ie.cg_iterations
+
+
+def test_excited_step_matches_dense_penalised_solve():
+    """The penalty mu r conj(<r>) (r = psi_ref / psi, log-modulus difference clamped at 10)
+    and the augmented means, checked against a dense solve of the same system."""
+    N, M, p, pref, batch, h = _holo_case()
+    mu = 0.7
+    amp, ref = O.Amp(O.OR_CRBM, N, M, p.copy()), O.Amp(O.OR_CRBM, N, M, pref.copy())
+    Er, Ei = O.local_energy(h, amp, batch, complex_out=True)
+    la, ar = O.log_amp(amp, batch)
+    lb, br = O.log_amp(ref, batch)
+    r = np.exp(np.clip(lb - la, -10, 10)) * np.exp(1j * (br - ar))
+    rm = r.mean()
+    Eaug = Er + 1j * Ei + mu * r * np.conj(rm)
+    R, I = O.gradient_complex(amp, batch)
+    want = _holo_dense(R, I, Eaug.real, Eaug.imag, Er.mean() + mu * abs(rm) ** 2, Ei.mean(), 1e-2)
+    Ee, de, ie = O.excited_step(h, amp, ref, mu, batch, 1e-2, 0.02, 2000, 1e-13)
+    assert ie.converged == 1
+    np.testing.assert_allclose(Ee, Eaug.real, rtol=0, atol=1e-12)
+    assert np.linalg.norm(de - want) <= 1e-8 * np.linalg.norm(want)
+    assert ie.mean_energy == pytest.approx(Er.mean(), abs=1e-12)       # the physical energy
+
+
+def test_tvmc_step_matches_dense_real_time_solve():
+    """Real-time tVMC (src/nqs/nqs_optimizer.c:888-993): Re(S) delta = Im(F) on the
+    holomorphic metric and theta += dt delta, against a dense solve."""
+    N, M, p, _, batch, h = _holo_case()
+    amp = O.Amp(O.OR_CRBM, N, M, p.copy())
+    Er, Ei = O.local_energy(h, amp, batch, complex_out=True)
+    R, I = O.gradient_complex(amp, batch)
+    want = _holo_dense(R, I, Er, Ei, Er.mean(), Ei.mean(), 1e-2, realtime=True)
+    dt = 0.01
+    Et, dtv, it = O.tvmc_step(h, amp, batch, 1e-2, dt, 2000, 1e-13)
+    assert it.converged == 1
+    assert np.linalg.norm(dtv - want) <= 1e-8 * np.linalg.norm(want)
+    np.testing.assert_allclose(amp.params, p + dt * dtv, rtol=0, atol=1e-15)
+    assert it.update_norm == pytest.approx(np.linalg.norm(dtv) * dt, rel=1e-12)
