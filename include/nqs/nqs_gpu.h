@@ -184,8 +184,9 @@ int nqs_gpu_gradient_batch(nqs_ansatz_t *a, nqs_gradient_fn_t gradient_fn,
                            int complex_out, double *out_re, double *out_im);
 
 /* One SR step on a caller-supplied batch (no sampling): the parity entry
- * points.  `minsr` = 1 runs MinSR, 0 runs CG-SR, 2 holomorphic SR.  Optional outputs:
- * out_energies[batch], out_delta[num_params]. */
+ * points.  `minsr` = 1 runs MinSR, 0 runs CG-SR, 2 holomorphic SR (then gradient_fn,
+ * when set, is the holomorphic gradient: nqs_symproj_gradient_complex).  Optional
+ * outputs: out_energies[batch], out_delta[num_params]. */
 int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int size_x, int size_y,
                           nqs_ansatz_t *ansatz,
                           nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,

@@ -37,6 +37,18 @@ int nqs_symproj_gradient(void *grad_user,
                          const int *spins, int num_sites,
                          double *out_grad);
 
+/* Replaces upstream nqs_symproj_gradient_complex (include/nqs/nqs_symproj.h:69;
+ * src/nqs/nqs_symproj.c:157-261): the
+ * holomorphic gradient of the projected amplitude, sum_g w_g d log psi_base(g s) / d theta
+ * with complex weights w_g = chi_g psi_base(g s) / sum_g' chi_g' psi_base(g' s).  Usable as
+ * the nqs_holomorphic_gradient_fn_t of nqs_sr_step_holomorphic_full with the wrapper as
+ * grad_user.  Base ansatz: mean-field, RBM or complex RBM. */
+int nqs_symproj_gradient_complex(void *grad_user,
+                                  nqs_ansatz_t *ansatz,
+                                  const int *spins, int num_sites,
+                                  double *out_grad_re,
+                                  double *out_grad_im);
+
 /* Replaces upstream nqs_kagome_translation_perm (include/nqs/nqs_symproj.h:92).
  * Host-side table builder; *out_perm is malloc'd, the caller frees it. */
 int nqs_kagome_translation_perm(int Lx, int Ly,

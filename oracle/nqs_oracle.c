@@ -441,6 +441,57 @@ int oracle_symproj_gradient_batch(const or_amp_t *amp, const int *spins, int B,
     return 0;
 }
 
+/* Complex symmetry-projected gradient, src/nqs/nqs_symproj.c:157-261: complex weights
+ * w_g = c_g / sum c, c_g = chi_g e^{lp_g - max} (cos arg_g + i sin arg_g), times the
+ * holomorphic gradient of the base ansatz at g s. */
+int oracle_symproj_gradient_complex_batch(const or_amp_t *amp, const int *spins, int B,
+                                          double *out_re, double *out_im) {
+    int k = -1;
+    for (int l = 0; l < amp->n_layers; l++)
+        if (amp->layers[l].type == OR_LAYER_SYMPROJ) { k = l; break; }
+    if (k < 0) return -1;
+    const or_layer_t *L = &amp->layers[k];
+    int N = amp->base.N, G = L->G;
+    long P = oracle_num_params(amp->base.kind, N, amp->base.M);
+    int *sh = malloc(sizeof(int) * (size_t)G * N);
+    double *lp = malloc(sizeof(double) * (size_t)G), *ag = malloc(sizeof(double) * (size_t)G);
+    double *cr = malloc(sizeof(double) * (size_t)G), *ci = malloc(sizeof(double) * (size_t)G);
+    double *tr = malloc(sizeof(double) * (size_t)P), *ti = malloc(sizeof(double) * (size_t)P);
+    for (int b = 0; b < B; b++) {
+        const int *s = spins + (size_t)b * N;
+        double *ore = out_re + (size_t)b * P, *oim = out_im + (size_t)b * P;
+        double mx = -1e300;
+        for (int g = 0; g < G; g++) {
+            for (int i = 0; i < N; i++) sh[(size_t)g * N + i] = s[L->perm[(size_t)g * N + i]];
+            amp_eval(amp, k + 1, sh + (size_t)g * N, &lp[g], &ag[g]);
+            if (lp[g] > mx) mx = lp[g];
+        }
+        double dr = 0.0, di = 0.0;
+        for (int g = 0; g < G; g++) {
+            double m = L->chars[g] * exp(lp[g] - mx);
+            cr[g] = m * cos(ag[g]);
+            ci[g] = m * sin(ag[g]);
+            dr += cr[g];
+            di += ci[g];
+        }
+        memset(ore, 0, (size_t)P * sizeof(double));
+        memset(oim, 0, (size_t)P * sizeof(double));
+        double d2 = dr * dr + di * di;
+        if (d2 == 0.0) continue;
+        for (int g = 0; g < G; g++) {
+            double wr = (cr[g] * dr + ci[g] * di) / d2, wi = (ci[g] * dr - cr[g] * di) / d2;
+            if (wr == 0.0 && wi == 0.0) continue;
+            if (oracle_gradient_complex_batch(&amp->base, sh + (size_t)g * N, 1, tr, ti)) return -1;
+            for (long q = 0; q < P; q++) {
+                ore[q] += wr * tr[q] - wi * ti[q];
+                oim[q] += wr * ti[q] + wi * tr[q];
+            }
+        }
+    }
+    free(sh); free(lp); free(ag); free(cr); free(ci); free(tr); free(ti);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* Local energies                                                      */
 /* ------------------------------------------------------------------ */

@@ -147,6 +147,17 @@ int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, i
                      double *params_inout, long P, double *out_energies,
                      double *out_delta, or_step_info_t *info);
 
+/* Complex symmetry-projected gradient (src/nqs/nqs_symproj.c:157-261) of the amplitude's
+ * symproj layer: rows of Re and Im. */
+int oracle_symproj_gradient_complex_batch(const or_amp_t *amp, const int *spins, int B,
+                                          double *out_re, double *out_im);
+/* Holomorphic SR with the gradient from the symproj layer (grad_sym = 1,
+ * nqs_symproj_gradient_complex as the holomorphic gradient callback) or the base ansatz
+ * (grad_sym = 0, as oracle_holo_step). */
+int oracle_holo_step_grad(const or_ham_t *h, const or_amp_t *amp, int grad_sym, const int *batch, int Ns,
+                          double shift, double lr, int max_iters, double tol, double *params_inout, long P,
+                          double *out_energies, double *out_delta, or_step_info_t *info);
+
 /* Excited-state SR, src/nqs/nqs_optimizer.c:562-723: the holomorphic step with
  * E_loc += mu r conj(<r>), r = psi_ref / psi (log-modulus difference clamped to +-10), the
  * force's means <E_re> + mu |<r>|^2 and <E_im> + mu (<r_im><r_re> - <r_re><r_im>); the

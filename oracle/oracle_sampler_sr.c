@@ -412,33 +412,42 @@ static void qgt_complex_apply(const double *R, const double *I, long Ns, long P,
  * 1 excited-state SR (the penalty of :600-658 on top of mode 0; ref and mu used), 2 the
  * real-time tVMC force with theta += dt delta (:888-993; lr carries -dt). */
 static int holo_family_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu, int mode,
-                            const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
-                            double *params, long P, double *out_E, double *out_delta, or_step_info_t *info);
+                            int grad_sym, const int *batch, int Ns, double shift, double lr, int max_iters,
+                            double tol, double *params, long P, double *out_E, double *out_delta,
+                            or_step_info_t *info);
 
 int oracle_holo_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns,
                      double shift, double lr, int max_iters, double tol,
                      double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
-    return holo_family_step(h, amp, NULL, 0.0, 0, batch, Ns, shift, lr, max_iters, tol, params, P, out_E,
+    return holo_family_step(h, amp, NULL, 0.0, 0, 0, batch, Ns, shift, lr, max_iters, tol, params, P, out_E,
                             out_delta, info);
+}
+
+int oracle_holo_step_grad(const or_ham_t *h, const or_amp_t *amp, int grad_sym, const int *batch, int Ns,
+                          double shift, double lr, int max_iters, double tol, double *params, long P,
+                          double *out_E, double *out_delta, or_step_info_t *info) {
+    return holo_family_step(h, amp, NULL, 0.0, 0, grad_sym, batch, Ns, shift, lr, max_iters, tol, params, P,
+                            out_E, out_delta, info);
 }
 
 int oracle_excited_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu,
                         const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
                         double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
-    return holo_family_step(h, amp, ref, mu, 1, batch, Ns, shift, lr, max_iters, tol, params, P, out_E,
+    return holo_family_step(h, amp, ref, mu, 1, 0, batch, Ns, shift, lr, max_iters, tol, params, P, out_E,
                             out_delta, info);
 }
 
 int oracle_tvmc_step(const or_ham_t *h, const or_amp_t *amp, const int *batch, int Ns, double shift,
                      double dt, int max_iters, double tol, double *params, long P, double *out_E,
                      double *out_delta, or_step_info_t *info) {
-    return holo_family_step(h, amp, NULL, 0.0, 2, batch, Ns, shift, -dt, max_iters, tol, params, P, out_E,
+    return holo_family_step(h, amp, NULL, 0.0, 2, 0, batch, Ns, shift, -dt, max_iters, tol, params, P, out_E,
                             out_delta, info);
 }
 
 static int holo_family_step(const or_ham_t *h, const or_amp_t *amp, const or_amp_t *ref, double mu, int mode,
-                            const int *batch, int Ns, double shift, double lr, int max_iters, double tol,
-                            double *params, long P, double *out_E, double *out_delta, or_step_info_t *info) {
+                            int grad_sym, const int *batch, int Ns, double shift, double lr, int max_iters,
+                            double tol, double *params, long P, double *out_E, double *out_delta,
+                            or_step_info_t *info) {
     double *Er = malloc(sizeof(double) * (size_t)Ns), *Ei = malloc(sizeof(double) * (size_t)Ns);
     double *R = malloc(sizeof(double) * (size_t)Ns * P), *I = malloc(sizeof(double) * (size_t)Ns * P);
     double *Rm = calloc((size_t)P, sizeof(double)), *Im = calloc((size_t)P, sizeof(double));
@@ -447,7 +456,8 @@ static int holo_family_step(const or_ham_t *h, const or_amp_t *amp, const or_amp
     double *Ap = malloc(sizeof(double) * (size_t)P);
     double *uR = malloc(sizeof(double) * (size_t)Ns), *uI = malloc(sizeof(double) * (size_t)Ns);
     oracle_local_energy_batch(h, amp, batch, Ns, Er, Ei);               /* :455-456 */
-    if (oracle_gradient_complex_batch(&amp->base, batch, Ns, R, I)) return -1;   /* :458-469 */
+    if (grad_sym ? oracle_symproj_gradient_complex_batch(amp, batch, Ns, R, I)
+                 : oracle_gradient_complex_batch(&amp->base, batch, Ns, R, I)) return -1;   /* :458-469 */
     double erm = 0.0, eim = 0.0, ersq = 0.0;                           /* :471-481 */
     for (int i = 0; i < Ns; i++) { erm += Er[i]; eim += Ei[i]; ersq += Er[i] * Er[i]; }
     erm /= (double)Ns; eim /= (double)Ns; ersq /= (double)Ns;

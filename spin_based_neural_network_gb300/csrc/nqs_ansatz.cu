@@ -341,20 +341,32 @@ bool launch_log_amp(const DevAmp &A, const uint64_t *bits, int B, double *la, do
 
 // Writes alpha * d log psi / d theta of configuration `bits` into row `o`
 // (accumulating when acc).  mode 1: real projection (src/nqs/nqs_ansatz.c:885-995);
-// mode 2: holomorphic pair (o = Re, oi = Im; :1025-1091).  `t` is a per-warp
-// scratch of 2*M doubles (4*M for the MLP).
+// mode 2: holomorphic pair (o = Re, oi = Im; :1025-1091), where the weight may be
+// complex, alpha + i alpha_im (MF / RBM / complex RBM).  `t` is a per-warp scratch of
+// 2*M doubles (4*M for the MLP).
 __device__ void warp_grad_row(const DevAnsatz &a, uint64_t bits, int mode, double *o, double *oi,
-                              double alpha, bool acc, double *t) {
+                              double alpha, bool acc, double *t, double alpha_im = 0.0) {
     int lane = threadIdx.x & 31;
     const int N = a.N, M = a.M;
     auto put = [&](double *row, long k, double v) {
         if (acc) row[k] += alpha * v;
         else row[k] = alpha * v;
     };
+    // (alpha + i alpha_im)(re + i im) into (o, oi)
+    auto put2 = [&](long k, double re, double im) {
+        const double vr = alpha * re - alpha_im * im, vi = alpha * im + alpha_im * re;
+        if (acc) {
+            o[k] += vr;
+            oi[k] += vi;
+        } else {
+            o[k] = vr;
+            oi[k] = vi;
+        }
+    };
     if (a.kind == KIND_MF) {
         for (int i = lane; i < N; i += 32) {
-            put(o, i, (double)spin_of(bits, i));
-            if (mode == 2) put(oi, i, 0.0);
+            if (mode == 2) put2(i, (double)spin_of(bits, i), 0.0);
+            else put(o, i, (double)spin_of(bits, i));
         }
         return;
     }
@@ -434,8 +446,8 @@ __device__ void warp_grad_row(const DevAnsatz &a, uint64_t bits, int mode, doubl
                 long q = k - N - M;
                 v = tr[q / N] * (double)spin_of(bits, (int)(q % N));
             }
-            put(o, k, v);
-            if (mode == 2) put(oi, k, 0.0);
+            if (mode == 2) put2(k, v, 0.0);
+            else put(o, k, v);
         }
         __syncwarp();
         return;
@@ -456,10 +468,8 @@ __device__ void warp_grad_row(const DevAnsatz &a, uint64_t bits, int mode, doubl
             si = ti[q / N] * s;
         }
         if (mode == 2) {
-            put(o, k, sr);
-            put(oi, k, si);
-            put(o, Pr + k, -si);
-            put(oi, Pr + k, sr);
+            put2(k, sr, si);
+            put2(Pr + k, -si, sr);
         } else {
             put(o, k, sr);
             // real projection: d log|psi| / d theta_I = -Im(...), and 0 for the visible block
@@ -520,7 +530,72 @@ __global__ void k_symproj_gradient(DevAmp A, const uint64_t *__restrict__ bits, 
     }
 }
 
+// Complex symmetry-projected gradient, src/nqs/nqs_symproj.c:157-261: with
+// c_g = chi_g e^{lp_g - max + i arg_g} and w_g = c_g / sum_g' c_g', the rows
+// (Re, Im) = sum_g w_g d log psi_base(g s) / d theta (holomorphic base gradient).
+__global__ void k_symproj_gradient_complex(DevAmp A, const uint64_t *__restrict__ bits, int B, double *O,
+                                           double *Oi, double *wbuf) {
+    extern __shared__ double sm[];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int b = blockIdx.x * kWarpsPerBlock + warp;
+    double *scr = sm + warp * 2 * A.a.M;
+    if (b >= B) return;
+    const int N = A.a.N, G = A.G;
+    uint64_t s = bits[b];
+    double *lp = wbuf + (size_t)b * 2 * G, *ag = lp + G;
+    double mx = -1e300;
+    for (int g = 0; g < G; g++) {
+        uint64_t pb = permute_bits(s, A.perm + (long)g * N, N);
+        double l, a;
+        warp_base_eval(A.a, pb, l, a, scr);
+        a = apply_marshall(a, pb, A.n_inner, A.inner_mask);
+        if (lane == 0) {
+            lp[g] = l;
+            ag[g] = a;
+        }
+        mx = fmax(mx, l);
+    }
+    __syncwarp();
+    double dr = 0.0, di = 0.0;
+    for (int g = 0; g < G; g++) {
+        double m = A.chars[g] * exp(lp[g] - mx), sn, cs;
+        sincos(ag[g], &sn, &cs);
+        dr += m * cs;
+        di += m * sn;
+    }
+    double *row = O + (size_t)b * A.a.P, *rowi = Oi + (size_t)b * A.a.P;
+    for (long k = lane; k < A.a.P; k += 32) {
+        row[k] = 0.0;
+        rowi[k] = 0.0;
+    }
+    __syncwarp();
+    const double d2 = dr * dr + di * di;
+    if (d2 == 0.0) return;
+    for (int g = 0; g < G; g++) {
+        double m = A.chars[g] * exp(lp[g] - mx), sn, cs;
+        sincos(ag[g], &sn, &cs);
+        const double cr = m * cs, ci = m * sn;
+        const double wr = (cr * dr + ci * di) / d2, wi = (ci * dr - cr * di) / d2;
+        if (wr == 0.0 && wi == 0.0) continue;
+        uint64_t pb = permute_bits(s, A.perm + (long)g * N, N);
+        warp_grad_row(A.a, pb, 2, row, rowi, wr, true, scr, wi);
+    }
+}
+
 static DevBuf<double> g_symw;
+
+bool launch_symproj_gradient_complex(const DevAmp &A, const uint64_t *bits, int B, double *O, double *Oi) {
+    if (A.a.kind == KIND_MLP) {
+        set_error("complex symmetry-projected gradient: MF, RBM and complex RBM base ansatze only");
+        return false;
+    }
+    if (!g_symw.ensure((size_t)B * 2 * A.G)) return false;
+    size_t smem = sizeof(double) * (size_t)scratch_per_warp(A.a) * kWarpsPerBlock;
+    NQS_LAUNCH("symproj_gradient_complex");
+    k_symproj_gradient_complex<<<(B + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, smem,
+                                 ctx().stream>>>(A, bits, B, O, Oi, g_symw.p);
+    return NQS_CUDA(cudaGetLastError());
+}
 
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O) {
     if (!g_symw.ensure((size_t)B * 2 * A.G)) return false;
@@ -738,6 +813,10 @@ int nqs_gpu_gradient_batch(nqs_ansatz_t *h, nqs_gradient_fn_t gfn, void *guser, 
         DevAmp A;
         if (!build_amp(nqs_symproj_log_amp, guser, a->N, &A, nullptr)) return -1;
         if (!launch_symproj_gradient(A, bits, B, O.p)) return -1;
+    } else if ((void *)gfn == (void *)nqs_symproj_gradient_complex && complex_out) {
+        DevAmp A;
+        if (!build_amp(nqs_symproj_log_amp, guser, a->N, &A, nullptr)) return -1;
+        if (!launch_symproj_gradient_complex(A, bits, B, O.p, O.p + (size_t)B * a->P)) return -1;
     } else {
         set_error("gradient callback is not supported on the GPU");
         return -1;
@@ -762,6 +841,14 @@ int nqs_ansatz_logpsi_gradient_complex(nqs_ansatz_t *h, const int *spins, int nu
     Ansatz *a = (Ansatz *)h;
     if (!a || !spins || !re || !im || num_sites != a->N) return -1;
     return nqs_gpu_gradient_batch(h, nullptr, nullptr, spins, 1, 1, re, im);
+}
+
+int nqs_symproj_gradient_complex(void *grad_user, nqs_ansatz_t *h, const int *spins, int num_sites,
+                                 double *out_re, double *out_im) {
+    auto *w = (nqs_symproj_wrapper_t *)grad_user;
+    if (!w || !h || !spins || !out_re || !out_im || num_sites != w->num_sites) return -1;
+    return nqs_gpu_gradient_batch(h, (nqs_gradient_fn_t)(void *)nqs_symproj_gradient_complex, grad_user, spins, 1,
+                                  1, out_re, out_im);
 }
 
 int nqs_symproj_gradient(void *grad_user, nqs_ansatz_t *h, const int *spins, int num_sites,

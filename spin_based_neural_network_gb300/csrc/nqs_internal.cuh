@@ -184,6 +184,7 @@ bool fp32_capable(const DevAmp &A);        // RBM / cRBM FP32 product-form table
 bool fp32_mlp_capable(const DevAmp &A);    // MLP with width <= 128 and FP32 tables
 bool launch_gradient(const DevAnsatz &a, const uint64_t *bits, int B, int mode, double *O, double *Oi);
 bool launch_symproj_gradient(const DevAmp &A, const uint64_t *bits, int B, double *O);
+bool launch_symproj_gradient_complex(const DevAmp &A, const uint64_t *bits, int B, double *O, double *Oi);
 bool launch_bits_to_spins(const uint64_t *bits, int B, int N, int *out);
 
 // CG-SR solve (S + eps I) d = F in one cooperative launch (upstream cg_solve

@@ -885,9 +885,21 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         set_error("excited-state SR needs the reference log-amplitude");
         return -1;
     }
-    if (holo && in.hgfn) {
-        set_error("holomorphic gradient callback is not supported on the GPU (NULL: the base ansatz gradient)");
+    // holomorphic gradient: NULL = the base ansatz's (src/nqs/nqs_optimizer.c:458-469), or the
+    // symmetry-projected one (nqs_symproj_gradient_complex with its wrapper)
+    const bool hg_sym = holo && (void *)in.hgfn == (void *)nqs_symproj_gradient_complex;
+    if (holo && in.hgfn && !hg_sym) {
+        set_error("holomorphic gradient callback is not supported on the GPU (NULL or nqs_symproj_gradient_complex)");
         return -1;
+    }
+    DevAmp Ahg;
+    if (hg_sym) {
+        Ansatz *hbase = nullptr;
+        if (!build_amp(nqs_symproj_log_amp, in.hguser, H.N, &Ahg, &hbase)) return -1;
+        if (hbase != a) {
+            set_error("the gradient's symmetry wrapper does not wrap the ansatz being optimised");
+            return -1;
+        }
     }
     Workspace &w = g_ws;
     if (!w.E.ensure(Ns) || !w.Ei.ensure(Ns) || !w.eps.ensure(Ns) || !w.O.ensure((size_t)Ns * P) ||
@@ -939,8 +951,13 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     // holomorphic step takes the complex gradient of the base ansatz
     // (nqs_ansatz_logpsi_gradient_complex, src/nqs/nqs_optimizer.c:458-469)
     bool fused_grad = !grad_sym && A.G == 0;
-    if (holo) {
+    if (holo && A.G == 0 && !hg_sym) {
         if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, w.O.p, w.Oi.p, 2, false)) return -1;
+    } else if (holo) {
+        if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, nullptr, nullptr, 0, false)) return -1;
+        if (hg_sym ? !launch_symproj_gradient_complex(Ahg, bits, Ns, w.O.p, w.Oi.p)
+                   : !launch_gradient(A.a, bits, Ns, 2, w.O.p, w.Oi.p))
+            return -1;
     } else if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
                                        fused_grad ? 1 : 0, fp32est)) {
         return -1;
@@ -1255,6 +1272,12 @@ int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t 
                           nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
     if (!cfg || !a || !batch || Ns <= 0) return -1;
     StepIn in{cfg, sx, sy, (Ansatz *)a, nullptr, batch, Ns, fn, user, gfn, guser, minsr};
+    if (minsr == 2 && gfn) {          // holomorphic: the callback is a holomorphic gradient
+        in.hgfn = (nqs_holomorphic_gradient_fn_t)(void *)gfn;
+        in.hguser = guser;
+        in.gfn = nullptr;
+        in.guser = nullptr;
+    }
     return sr_step_impl(in, info, out_E, out_delta);
 }
 

@@ -70,6 +70,7 @@ def _declare(L):
         "nqs_marshall_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
         "nqs_symproj_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
         "nqs_symproj_gradient": (C.c_int, [VP, VP, IP, C.c_int, DP]),
+        "nqs_symproj_gradient_complex": (C.c_int, [VP, VP, IP, C.c_int, DP, DP]),
         "nqs_kagome_translation_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), IP]),
         "nqs_kagome_p2_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
         "nqs_kagome_p6m_perm_irrep": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
@@ -256,6 +257,7 @@ class Symproj:
                                     _dp(self.chars))
         self.log_amp_fn = fn("nqs_symproj_log_amp")
         self.gradient_fn = fn("nqs_symproj_gradient")
+        self.gradient_complex_fn = fn("nqs_symproj_gradient_complex")
 
     @property
     def user(self):
@@ -304,6 +306,16 @@ def local_energy_batch(cfg, size_x, size_y, spins, log_amp_fn, user, complex_out
     _check(lib().nqs_gpu_local_energy_batch(C.byref(cfg), size_x, size_y, _ip(s), B, log_amp_fn, user,
                                             _dp(re), _dp(im)), "local_energy_batch")
     return (re, im) if complex_out else re
+
+
+def symproj_gradient_complex_batch(ansatz, sym, spins):
+    """nqs_symproj_gradient_complex over a batch: (Re, Im) rows [B, P]."""
+    s = spins_array(spins, ansatz.N)
+    B = s.shape[0]
+    re, im = np.zeros((B, ansatz.P)), np.zeros((B, ansatz.P))
+    _check(lib().nqs_gpu_gradient_batch(ansatz.h, sym.gradient_complex_fn, sym.user, _ip(s), B, 1, _dp(re),
+                                        _dp(im)), "symproj complex gradient")
+    return re, im
 
 
 def symproj_gradient_batch(ansatz, sym, spins):

@@ -98,6 +98,9 @@ def lib():
                                        DP, DP, C.POINTER(OrStepInfo)]
         L.oracle_holo_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), IP, C.c_int, C.c_double, C.c_double,
                                        C.c_int, C.c_double, DP, C.c_long, DP, DP, C.POINTER(OrStepInfo)]
+        L.oracle_holo_step_grad.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), C.c_int, IP, C.c_int, C.c_double,
+                                            C.c_double, C.c_int, C.c_double, DP, C.c_long, DP, DP,
+                                            C.POINTER(OrStepInfo)]
         L.oracle_excited_step.argtypes = [C.POINTER(OrHam), C.POINTER(OrAmp), C.POINTER(OrAmp), C.c_double, IP,
                                           C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, DP, C.c_long,
                                           DP, DP, C.POINTER(OrStepInfo)]
@@ -260,6 +263,28 @@ def holo_step(h, amp, batch, shift, lr, max_iters, tol):
     info = OrStepInfo()
     assert lib().oracle_holo_step(C.byref(h), amp.ref(), ip(batch), Ns, shift, lr, max_iters, tol,
                                   dp(amp.params), P, dp(E), dp(d), C.byref(info)) == 0
+    return E, d, info
+
+
+def symproj_gradient_complex(amp, spins):
+    spins = np.ascontiguousarray(spins, dtype=np.int32)
+    B = spins.shape[0]
+    P = num_params(amp.s.base.kind, amp.N, amp.s.base.M)
+    re, im = np.zeros((B, P)), np.zeros((B, P))
+    assert lib().oracle_symproj_gradient_complex_batch(amp.ref(), ip(spins), B, dp(re), dp(im)) == 0
+    return re, im
+
+
+def holo_step_sym(h, amp, batch, shift, lr, max_iters, tol):
+    """Holomorphic SR with nqs_symproj_gradient_complex as the gradient (the amplitude's
+    symproj layer)."""
+    batch = np.ascontiguousarray(batch, dtype=np.int32)
+    Ns = batch.shape[0]
+    P = len(amp.params)
+    E, d = np.zeros(Ns), np.zeros(P)
+    info = OrStepInfo()
+    assert lib().oracle_holo_step_grad(C.byref(h), amp.ref(), 1, ip(batch), Ns, shift, lr, max_iters, tol,
+                                       dp(amp.params), P, dp(E), dp(d), C.byref(info)) == 0
     return E, d, info
 
 

@@ -438,3 +438,51 @@ def test_holomorphic_run_with_sampler(nqs):
         nqs.set_options()
     assert rc == 0 and np.all(np.isfinite(trace))
     assert np.mean(trace[-5:]) < np.mean(trace[:5])
+
+
+@pytest.mark.parametrize("name", ["p2", "trans"])
+def test_symproj_gradient_complex_against_reference(nqs, name):
+    """nqs_symproj_gradient_complex (src/nqs/nqs_symproj.c:157-261) against the upstream
+    function's output (tests/golden/symproj_complex.npz), batched and per configuration."""
+    d = load("symproj_" + name)
+    g = load("symproj_complex")
+    N = int(d["N"])
+    a = make_ansatz(nqs, int(d["kind"]), N, int(d["M"]), d["params"])
+    sp = nqs.Symproj(a.log_amp_fn, a.user, N, d["perm"], d["chars"])
+    re, im = nqs.symproj_gradient_complex_batch(a, sp, d["spins"])
+    assert rel(re, g[name + "_re"]) < 1e-11 and rel(im, g[name + "_im"]) < 1e-11
+    r1, i1 = np.zeros(a.P), np.zeros(a.P)
+    s0 = np.ascontiguousarray(d["spins"][3], dtype=np.int32)
+    assert nqs.lib().nqs_symproj_gradient_complex(sp.user, a.h, s0.ctypes.data_as(nqs.IP), N,
+                                                  r1.ctypes.data_as(nqs.DP), i1.ctypes.data_as(nqs.DP)) == 0
+    assert rel(r1, g[name + "_re"][3]) < 1e-11 and rel(i1, g[name + "_im"][3]) < 1e-11
+
+
+@pytest.mark.parametrize("grad", ["symproj", "base"])
+def test_holomorphic_sr_through_symmetry_projection(nqs, grad):
+    """Holomorphic SR of the p2-projected complex RBM on the 2x2 kagome torus, with
+    nqs_symproj_gradient_complex as the gradient callback or with the base ansatz's
+    gradient (NULL), against the oracle on the same batch (converged CG)."""
+    from spin_based_neural_network_gb300 import abi
+    d = load("symproj_p2")
+    N, M = 12, 12
+    a = make_ansatz(nqs, O.OR_CRBM, N, M, d["params"])
+    p0 = a.params.copy()
+    sp = nqs.Symproj(a.log_amp_fn, a.user, N, d["perm"], d["chars"])
+    rng = np.random.default_rng(17)
+    batch = rng.choice(np.array([-1, 1], np.int32), size=(512, N))
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, hamiltonian=6, kagome_pbc=1,
+                              sr_diag_shift=1e-2, learning_rate=0.01, sr_cg_max_iters=600, sr_cg_tol=1e-13)
+    gfn, gu = (sp.gradient_complex_fn, sp.user) if grad == "symproj" else (None, None)
+    info, E, delta = nqs.sr_step_batch(cfg, 2, 2, a, batch, minsr=2, log_amp_fn=sp.log_amp_fn, user=sp.user,
+                                       grad_fn=gfn, grad_user=gu)
+    amp = O.Amp(O.OR_CRBM, N, M, p0.copy(), [("symproj", d["perm"], d["chars"])])
+    h = O.ham(O.OR_KAGOME, 2, 2, kagome_pbc=1)
+    if grad == "symproj":
+        Eo, do, io = O.holo_step_sym(h, amp, batch, 1e-2, 0.01, 600, 1e-13)
+    else:
+        Eo, do, io = O.holo_step(h, amp, batch, 1e-2, 0.01, 600, 1e-13)
+    assert io.converged == 1 and info.converged == 1
+    assert rel(E, Eo) < TOL
+    assert np.linalg.norm(delta - do) <= TOL_DELTA * np.linalg.norm(do)
+    assert rel(a.params, amp.params) < TOL

@@ -255,3 +255,35 @@ def test_tvmc_step_matches_dense_real_time_solve():
     assert np.linalg.norm(dtv - want) <= 1e-8 * np.linalg.norm(want)
     np.testing.assert_allclose(amp.params, p + dt * dtv, rtol=0, atol=1e-15)
     assert it.update_norm == pytest.approx(np.linalg.norm(dtv) * dt, rel=1e-12)
+
+
+@pytest.mark.parametrize("name", ["p2", "trans"])
+def test_symproj_gradient_complex_matches_upstream(name):
+    """oracle_symproj_gradient_complex_batch restates src/nqs/nqs_symproj.c:157-261; the
+    fixture is the upstream function's output on the symproj_{p2,trans} cases."""
+    d = load("symproj_" + name)
+    g = load("symproj_complex")
+    amp = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params"], [("symproj", d["perm"], d["chars"])])
+    re, im = O.symproj_gradient_complex(amp, d["spins"])
+    assert rel(re, g[name + "_re"]) < 1e-12 and rel(im, g[name + "_im"]) < 1e-12
+    # its real part is the real-projected symmetric gradient only for real amplitudes; the
+    # imaginary part is non-trivial for the complex RBM
+    assert np.abs(im).max() > 1e-3
+
+
+def test_holo_step_with_symproj_gradient_identity():
+    """With the trivial group (identity only, character 1) the projected gradient is the
+    base gradient, so the holomorphic step with nqs_symproj_gradient_complex equals the
+    plain holomorphic step."""
+    N, M = 8, 6
+    p = O.init_params(O.OR_CRBM, N, M, 0.3, 31)
+    rng = np.random.default_rng(9)
+    batch = rng.choice(np.array([-1, 1], np.int32), size=(128, N))
+    h = O.ham(O.OR_TFIM, N, 1, Gamma=0.6)
+    perm = np.arange(N, dtype=np.int32)
+    a1 = O.Amp(O.OR_CRBM, N, M, p.copy(), [("symproj", perm, np.ones(1))])
+    a2 = O.Amp(O.OR_CRBM, N, M, p.copy(), [("symproj", perm, np.ones(1))])
+    E1, d1, _ = O.holo_step_sym(h, a1, batch, 1e-2, 0.01, 40, 1e-10)
+    E2, d2, _ = O.holo_step(h, a2, batch, 1e-2, 0.01, 40, 1e-10)
+    assert np.array_equal(E1, E2)
+    assert np.linalg.norm(d1 - d2) <= 1e-13 * np.linalg.norm(d2)
