@@ -12,6 +12,8 @@ import ctypes as C
 ANSATZ_LEGACY_MLP = 0
 ANSATZ_RBM = 5
 ANSATZ_COMPLEX_RBM = 6
+ANSATZ_FACTORED_VIT = 2       # factored-attention ViT, real amplitude
+ANSATZ_FACTORED_VIT_COMPLEX = 7
 ANSATZ_GPU_MLP = 100          # 2-hidden-layer tanh MLP with a complex head (extension)
 
 # nqs_hamiltonian_kind_t (upstream include/nqs/nqs_config.h:58-79)

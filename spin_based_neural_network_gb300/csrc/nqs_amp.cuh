@@ -151,12 +151,40 @@ __device__ __forceinline__ void mlp32_forward(const DevAnsatz &a, const float *w
     __syncwarp();
 }
 
+// Factored-attention ViT (src/nqs/nqs_ansatz.c:357-473, :571-729).  Its attention scores
+// depend on the parameters only, so with the tables of k_derive
+// log psi = b_out + sum_j s_pred_j W_out.V e_j = b_out + c1 A + c0 B, A = sum_j s_pred_j s_j,
+// B = sum_j s_pred_j: one warp sum per configuration.  Returns A (all lanes).
+__device__ __forceinline__ double vit_spin_sum(const DevAnsatz &a, uint64_t bits, double *S = nullptr) {
+    int lane = threadIdx.x & 31;
+    double A = 0.0, s1 = 0.0;
+    for (int j = lane; j < a.N; j += 32) {
+        const double sj = (double)spin_of(bits, j);
+        A = fma(a.wtr[j], sj, A);
+        s1 += sj;
+    }
+    if (S) *S = warp_sum(s1);
+    return warp_sum(A);
+}
+
+__device__ __forceinline__ void warp_vit_eval(const DevAnsatz &a, uint64_t bits, double &la, double &ar) {
+    const VitTab T = vit_tab(a.N, a.M);
+    const double *t = a.wtr;
+    const double A = vit_spin_sum(a, bits), B = t[T.bsum];
+    la = t[T.bout] + t[T.c1] * A + t[T.c0] * B;
+    ar = t[T.bout + 1] + t[T.c1 + 1] * A + t[T.c0 + 1] * B;
+}
+
 // log psi of the base ansatz (all lanes return the same value).
 __device__ __forceinline__ void warp_base_eval(const DevAnsatz &a, uint64_t bits, double &la, double &ar,
                                                double *scratch) {
     int lane = threadIdx.x & 31;
     if (a.kind == KIND_MLP) {
         warp_mlp_eval(a, bits, la, ar, scratch);
+        return;
+    }
+    if (is_vit(a.kind)) {
+        warp_vit_eval(a, bits, la, ar);
         return;
     }
     double vr, vi;

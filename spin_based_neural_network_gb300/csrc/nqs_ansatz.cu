@@ -15,6 +15,8 @@ static long num_params_of(int kind, int N, int M) {
         case KIND_RBM: return n + m + m * n;                      // :88
         case KIND_CRBM: return 2 * (n + m + m * n);               // :223
         case KIND_MLP: return m * n + m + m * m + m + 2 * m + 2;  // GPU extension
+        case KIND_VIT: return 3 * m + m * m + n + 1;              // :113-130 (m = d)
+        case KIND_VITC: return 6 * m + 2 * m * m + n + 2;         // :155-172
         default: return -1;
     }
 }
@@ -42,6 +44,35 @@ static void init_params(const nqs_config_t *cfg, int kind, int N, int M, double 
     double scale = cfg->rbm_init_scale > 0.0 ? cfg->rbm_init_scale : 0.01;
     if (kind == KIND_MF) {
         for (int i = 0; i < N; i++) p[i] = 0.01 * (xs_uniform(&st) - 0.5);
+        return;
+    }
+    if (kind == KIND_VIT) {                                // src/nqs/nqs_ansatz.c:131-151 (M = d)
+        const int d = M;
+        const double vs = scale / sqrt((double)d);
+        for (int i = 0; i < d; i++) p[i] = scale * xs_gauss(&st);
+        for (int i = 0; i < d; i++) p[d + i] = scale * (xs_uniform(&st) - 0.5);
+        for (long k = 0; k < (long)d * d; k++) p[2L * d + k] = vs * xs_gauss(&st);
+        const long ao = 2L * d + (long)d * d;
+        for (long k = 0; k < N; k++) p[ao + k] = scale * (xs_uniform(&st) - 0.5);
+        for (int i = 0; i < d; i++) p[ao + N + i] = scale * (xs_uniform(&st) - 0.5);
+        p[ao + N + d] = 0.0;
+        return;
+    }
+    if (kind == KIND_VITC) {                               // :173-214
+        const int d = M;
+        const double vs = scale / sqrt((double)d), is = 0.1 * scale;
+        for (int i = 0; i < d; i++) p[i] = scale * xs_gauss(&st);
+        for (int i = 0; i < d; i++) p[d + i] = is * xs_gauss(&st);
+        for (int i = 0; i < d; i++) p[2 * d + i] = scale * (xs_uniform(&st) - 0.5);
+        for (int i = 0; i < d; i++) p[3 * d + i] = is * (xs_uniform(&st) - 0.5);
+        const long vr = 4L * d, vi = vr + (long)d * d, ao = vi + (long)d * d;
+        for (long k = 0; k < (long)d * d; k++) p[vr + k] = vs * xs_gauss(&st);
+        for (long k = 0; k < (long)d * d; k++) p[vi + k] = 0.1 * vs * xs_gauss(&st);
+        for (long k = 0; k < N; k++) p[ao + k] = scale * (xs_uniform(&st) - 0.5);
+        for (int i = 0; i < d; i++) p[ao + N + i] = scale * (xs_uniform(&st) - 0.5);
+        for (int i = 0; i < d; i++) p[ao + N + d + i] = is * (xs_uniform(&st) - 0.5);
+        p[ao + N + 2 * d] = 0.0;
+        p[ao + N + 2 * d + 1] = 0.0;
         return;
     }
     if (kind == KIND_RBM || kind == KIND_CRBM) {
@@ -127,6 +158,93 @@ __global__ void k_derive(DevAnsatz a, double *wtr, double *wti, float2 *f32) {
     }
 }
 
+// ViT tables (one block): softmax weights, attention column sums, u = V^T W_out and the
+// products the configuration-dependent terms need (layout VitTab).  Complex parameters
+// are read from the complex ViT's layout; the real ViT has zero imaginary parts.
+__global__ void k_vit_tables(DevAnsatz a, double *t) {
+    const int N = a.N, d = a.M, tid = threadIdx.x;
+    const VitTab T = vit_tab(N, d);
+    const bool cx = a.kind == KIND_VITC;
+    // offsets of the (re, im) blocks
+    const long wR = 0, wI = cx ? d : -1, bR = cx ? 2L * d : d, bI = cx ? 3L * d : -1;
+    const long VR = cx ? 4L * d : 2L * d, VI = cx ? VR + (long)d * d : -1;
+    const long at = cx ? 4L * d + 2L * d * d : 2L * d + (long)d * d;
+    const long WR = at + N, WI = cx ? WR + d : -1, boR = cx ? WR + 2L * d : WR + d, boI = cx ? boR + 1 : -1;
+    const double *p = a.p;
+    auto im = [&](long off, long k) { return off < 0 ? 0.0 : p[off + k]; };
+    __shared__ double s_max, s_invz;
+    if (tid == 0) {                                        // src/nqs/nqs_ansatz.c:431-447
+        double mx = -1e300;
+        for (int r = 0; r < N; r++) mx = fmax(mx, p[at + r]);
+        double z = 0.0;
+        for (int r = 0; r < N; r++) z += exp(p[at + r] - mx);
+        s_max = mx;
+        s_invz = 1.0 / z;
+    }
+    __syncthreads();
+    for (int r = tid; r < N; r += blockDim.x) t[T.f + r] = exp(p[at + r] - s_max) * s_invz;
+    for (int l = tid; l < d; l += blockDim.x) {
+        t[T.w + 2 * l] = p[wR + l];
+        t[T.w + 2 * l + 1] = im(wI, l);
+        t[T.b + 2 * l] = p[bR + l];
+        t[T.b + 2 * l + 1] = im(bI, l);
+        t[T.W + 2 * l] = p[WR + l];
+        t[T.W + 2 * l + 1] = im(WI, l);
+    }
+    __syncthreads();
+    for (int j = tid; j < N; j += blockDim.x) {            // s_pred[j] = sum_i P_ij
+        double sp = 0.0;
+        for (int i = 0; i < N; i++) sp += t[T.f + ((i - j) % N + N) % N];
+        t[T.sp + j] = sp;
+    }
+    for (int l = tid; l < d; l += blockDim.x) {            // u_l = sum_k W_k V_kl
+        double ur = 0.0, ui = 0.0;
+        for (int k = 0; k < d; k++) {
+            const double vr = p[VR + (long)k * d + l], vi = im(VI, (long)k * d + l);
+            const double Wr = p[WR + k], Wi = im(WI, k);
+            ur += vr * Wr - vi * Wi;
+            ui += vr * Wi + vi * Wr;
+        }
+        t[T.u + 2 * l] = ur;
+        t[T.u + 2 * l + 1] = ui;
+    }
+    for (int k = tid; k < d; k += blockDim.x) {            // (V w)_k, (V b)_k
+        double ar = 0.0, ai = 0.0, br = 0.0, bi = 0.0;
+        for (int l = 0; l < d; l++) {
+            const double vr = p[VR + (long)k * d + l], vi = im(VI, (long)k * d + l);
+            const double xr = p[wR + l], xi = im(wI, l), yr = p[bR + l], yi = im(bI, l);
+            ar += vr * xr - vi * xi;
+            ai += vr * xi + vi * xr;
+            br += vr * yr - vi * yi;
+            bi += vr * yi + vi * yr;
+        }
+        t[T.vw + 2 * k] = ar;
+        t[T.vw + 2 * k + 1] = ai;
+        t[T.vb + 2 * k] = br;
+        t[T.vb + 2 * k + 1] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double bs = 0.0, c1r = 0.0, c1i = 0.0, c0r = 0.0, c0i = 0.0;
+        for (int j = 0; j < N; j++) bs += t[T.sp + j];
+        for (int l = 0; l < d; l++) {
+            const double ur = t[T.u + 2 * l], ui = t[T.u + 2 * l + 1];
+            const double xr = t[T.w + 2 * l], xi = t[T.w + 2 * l + 1], yr = t[T.b + 2 * l], yi = t[T.b + 2 * l + 1];
+            c1r += ur * xr - ui * xi;
+            c1i += ur * xi + ui * xr;
+            c0r += ur * yr - ui * yi;
+            c0i += ur * yi + ui * yr;
+        }
+        t[T.bsum] = bs;
+        t[T.bout] = p[boR];
+        t[T.bout + 1] = im(boI, 0);
+        t[T.c1] = c1r;
+        t[T.c1 + 1] = c1i;
+        t[T.c0] = c0r;
+        t[T.c0 + 1] = c0i;
+    }
+}
+
 DevAnsatz ansatz_dev(const Ansatz *a) {
     DevAnsatz d;
     d.kind = a->kind;
@@ -149,6 +267,11 @@ DevAnsatz ansatz_dev(const Ansatz *a) {
 
 bool ansatz_refresh_derived(Ansatz *a) {
     if (a->kind == KIND_MF) return true;
+    if (is_vit(a->kind)) {
+        NQS_LAUNCH("derive_vit_tables");
+        k_vit_tables<<<1, 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p);
+        return NQS_CUDA(cudaGetLastError());
+    }
     long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * mlp32_pitch(a->M) : (long)a->M * a->N;
     NQS_LAUNCH("derive_weights");
     k_derive<<<(unsigned)((work + 255) / 256), 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
@@ -368,6 +491,86 @@ __device__ void warp_grad_row(const DevAnsatz &a, uint64_t bits, int mode, doubl
             if (mode == 2) put2(i, (double)spin_of(bits, i), 0.0);
             else put(o, i, (double)spin_of(bits, i));
         }
+        return;
+    }
+    if (is_vit(a.kind)) {
+        // src/nqs/nqs_ansatz.c:475-567 (real), :732-843 (real projection of the complex ViT),
+        // :1104-1256 (holomorphic): with A = sum_j s_pred_j s_j, B = sum_j s_pred_j,
+        // S = sum_j s_j every complex derivative z is a table entry times A or B:
+        // w_emb: A u, b_emb: B u, V_kl: W_k (w_l A + b_l B), attention r:
+        // f_r (c1 (S - A) + c0 (N - B)), W_out_k: (V w)_k A + (V b)_k B, b_out: 1.
+        const VitTab T = vit_tab(N, M);
+        const double *tb = a.wtr;
+        const int d = M;
+        const bool cx = a.kind == KIND_VITC;
+        double S;
+        const double A = vit_spin_sum(a, bits, &S), B = tb[T.bsum];
+        const double gs_r = tb[T.c1] * (S - A) + tb[T.c0] * ((double)N - B);
+        const double gs_i = tb[T.c1 + 1] * (S - A) + tb[T.c0 + 1] * ((double)N - B);
+        const long nblk = 3L * d + (long)d * d + N + 1;     // complex derivatives
+        // block order of the real ViT layout: w_emb, b_emb, V, attention, W_out, b_out
+        for (long q = lane; q < nblk; q += 32) {
+            double zr, zi;
+            long blk_off;                                    // index of the block start in q
+            bool real_param = false;
+            if (q < d) {
+                zr = A * tb[T.u + 2 * q];
+                zi = A * tb[T.u + 2 * q + 1];
+                blk_off = 0;
+            } else if (q < 2L * d) {
+                const long l = q - d;
+                zr = B * tb[T.u + 2 * l];
+                zi = B * tb[T.u + 2 * l + 1];
+                blk_off = 1;
+            } else if (q < 2L * d + (long)d * d) {
+                const long kl = q - 2L * d, k = kl / d, l = kl % d;
+                const double er = tb[T.w + 2 * l] * A + tb[T.b + 2 * l] * B;
+                const double ei = tb[T.w + 2 * l + 1] * A + tb[T.b + 2 * l + 1] * B;
+                const double Wr = tb[T.W + 2 * k], Wi = tb[T.W + 2 * k + 1];
+                zr = Wr * er - Wi * ei;
+                zi = Wr * ei + Wi * er;
+                blk_off = 2;
+            } else if (q < 2L * d + (long)d * d + N) {
+                const long r = q - 2L * d - (long)d * d;
+                zr = tb[T.f + r] * gs_r;
+                zi = tb[T.f + r] * gs_i;
+                real_param = true;
+                blk_off = 3;
+            } else if (q < 3L * d + (long)d * d + N) {
+                const long k = q - 2L * d - (long)d * d - N;
+                zr = tb[T.vw + 2 * k] * A + tb[T.vb + 2 * k] * B;
+                zi = tb[T.vw + 2 * k + 1] * A + tb[T.vb + 2 * k + 1] * B;
+                blk_off = 4;
+            } else {
+                zr = 1.0;
+                zi = 0.0;
+                blk_off = 5;
+            }
+            if (!cx) {                                       // real ViT: same index q
+                if (mode == 2) put2(q, zr, 0.0);
+                else put(o, q, zr);
+                continue;
+            }
+            // complex ViT: (re, im) parameter pairs at their own offsets
+            long iR, iI;
+            if (blk_off == 0) { iR = q; iI = d + q; }
+            else if (blk_off == 1) { iR = 2L * d + (q - d); iI = 3L * d + (q - d); }
+            else if (blk_off == 2) { iR = 4L * d + (q - 2L * d); iI = iR + (long)d * d; }
+            else if (blk_off == 3) { iR = 4L * d + 2L * d * d + (q - 2L * d - (long)d * d); iI = -1; }
+            else if (blk_off == 4) {
+                const long k = q - 2L * d - (long)d * d - N;
+                iR = 4L * d + 2L * d * d + N + k;
+                iI = iR + d;
+            } else { iR = 6L * d + 2L * d * d + N; iI = iR + 1; }
+            if (mode == 2) {
+                put2(iR, zr, zi);
+                if (!real_param) put2(iI, -zi, zr);
+            } else {
+                put(o, iR, zr);
+                if (!real_param) put(o, iI, -zi);
+            }
+        }
+        __syncwarp();
         return;
     }
     if (a.kind == KIND_MLP) {
@@ -635,7 +838,7 @@ nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
     clear_error();
     if (!cfg || num_sites <= 0) return nullptr;
     int kind = (int)cfg->ansatz;
-    if (kind != KIND_MF && kind != KIND_RBM && kind != KIND_CRBM && kind != KIND_MLP) {
+    if (kind != KIND_MF && kind != KIND_RBM && kind != KIND_CRBM && kind != KIND_MLP && !is_vit(kind)) {
         set_error("ansatz kind %d is not available in this build", kind);
         return nullptr;
     }
@@ -654,6 +857,7 @@ nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
             return nullptr;
         }
     }
+    if (is_vit(kind)) M = cfg->width > 0 ? cfg->width : 4;     // src/nqs/nqs_ansatz.c:124 (d)
     if (M > 32 * kMaxJ) {
         set_error("hidden width %d > %d", M, 32 * kMaxJ);
         return nullptr;
@@ -666,7 +870,8 @@ nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
     size_t bytes = sizeof(double) * (size_t)a->P;
     if (!NQS_CUDA(cudaMallocHost(&a->h_params, bytes)) || !(a->h_shadow = (double *)malloc(bytes)) ||
         !a->d_params.ensure((size_t)a->P) ||
-        !a->d_wtr.ensure((size_t)num_sites * (M ? M : 1) + (kind == KIND_MLP ? 0 : 0)) ||
+        !a->d_wtr.ensure(is_vit(kind) ? (size_t)vit_tab(num_sites, M).total
+                                      : (size_t)num_sites * (M ? M : 1)) ||
         !a->d_wti.ensure(kind == KIND_MLP ? (size_t)M * M : (size_t)num_sites * (M ? M : 1)) ||
         !a->d_f32.ensure(kind == KIND_MLP ? (mlp32_floats(num_sites, M) + 1) / 2
                                           : 3 * (size_t)num_sites * (M ? M : 1) + num_sites + (M ? M : 1))) {
@@ -694,7 +899,7 @@ long nqs_ansatz_num_params(const nqs_ansatz_t *h) { return h ? ((const Ansatz *)
 int nqs_ansatz_is_complex(const nqs_ansatz_t *h) {
     if (!h) return 0;
     int k = ((const Ansatz *)h)->kind;
-    return (k == KIND_CRBM || k == KIND_MLP) ? 1 : 0;
+    return (k == KIND_CRBM || k == KIND_MLP || k == KIND_VITC) ? 1 : 0;
 }
 
 double *nqs_ansatz_params_raw(nqs_ansatz_t *h) { return h ? ((Ansatz *)h)->h_params : nullptr; }

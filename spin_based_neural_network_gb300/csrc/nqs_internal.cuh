@@ -103,7 +103,34 @@ struct DevBuf {
 };
 
 // ---------------------------------------------------------------- device program
-enum : int { KIND_MF = 0, KIND_RBM = 5, KIND_CRBM = 6, KIND_MLP = NQS_GPU_ANSATZ_MLP };
+enum : int { KIND_MF = 0, KIND_VIT = 2, KIND_RBM = 5, KIND_CRBM = 6, KIND_VITC = 7, KIND_MLP = NQS_GPU_ANSATZ_MLP };
+
+// Factored-attention ViT tables (doubles, derived from the parameters after every
+// update; complex quantities as (re, im) pairs, imaginary parts 0 for the real ViT):
+// column sums s_pred[N] of the attention matrix, softmax weights f[N]
+// (P_ij = f[(i - j) mod N]), sum_j s_pred_j, b_out, c1 = u.w_emb, c0 = u.b_emb with
+// u = V^T W_out, then u, V w_emb, V b_emb, w_emb, b_emb, W_out [d] each.
+struct VitTab {
+    int sp, f, bsum, bout, c1, c0, u, vw, vb, w, b, W, total;
+};
+__host__ __device__ inline VitTab vit_tab(int N, int d) {
+    VitTab t;
+    t.sp = 0;
+    t.f = N;
+    t.bsum = 2 * N;
+    t.bout = t.bsum + 1;
+    t.c1 = t.bout + 2;
+    t.c0 = t.c1 + 2;
+    t.u = t.c0 + 2;
+    t.vw = t.u + 2 * d;
+    t.vb = t.vw + 2 * d;
+    t.w = t.vb + 2 * d;
+    t.b = t.w + 2 * d;
+    t.W = t.b + 2 * d;
+    t.total = t.W + 2 * d;
+    return t;
+}
+__host__ __device__ inline bool is_vit(int kind) { return kind == KIND_VIT || kind == KIND_VITC; }
 
 // Padded row pitch of the MLP's FP32 W2 tables and the floats of its FP32 tables.
 __host__ __device__ inline int mlp32_pitch(int M) { return (M + 31) / 32 * 32; }
@@ -113,7 +140,7 @@ struct DevAnsatz {
     int kind, N, M;
     long P;
     const double *p;     // device params, upstream layout
-    const double *wtr;   // [N][M] real weights transposed (RBM, cRBM); MLP: W1^T
+    const double *wtr;   // [N][M] real weights transposed (RBM, cRBM); MLP: W1^T; ViT: VitTab tables
     const double *wti;   // [N][M] imaginary weights transposed (cRBM); MLP: W2^T [M][M]
     // FP32 tables of the RBM / cRBM (complex, imaginary part 0 for the RBM),
     // rebuilt with the transposed copies: W^T [N][M], cosh(2 W^T), sinh(2 W^T)
