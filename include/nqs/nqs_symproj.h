@@ -61,6 +61,23 @@ int nqs_kagome_p2_perm(int Lx, int Ly,
                         double **out_characters,
                         int *out_num_elements);
 
+/* Replaces upstream nqs_kagome_p3_perm (include/nqs/nqs_symproj.h:129-133,
+ * src/nqs/nqs_symproj.c:436-523): |G| = 3 L^2, g = k L^2 + tx L + ty, the rotation by
+ * 120 k degrees about the centroid of the up triangle of cell (0,0) followed by the
+ * translation (tx, ty); characters 1. */
+int nqs_kagome_p3_perm(int L,
+                        int **out_perm,
+                        double **out_characters,
+                        int *out_num_elements);
+
+/* Replaces upstream nqs_kagome_p6_perm (include/nqs/nqs_symproj.h:156-160,
+ * src/nqs/nqs_symproj.c:525-590): |G| = 6 L^2, the rotation by 60 k degrees about the
+ * hexagon centre (a1 + a2)/2 followed by the translation; characters 1. */
+int nqs_kagome_p6_perm(int L,
+                        int **out_perm,
+                        double **out_characters,
+                        int *out_num_elements);
+
 /* Upstream nqs_symproj_kagome_irrep_t (include/nqs/nqs_symproj.h:193-200): the C_6v
  * irreps at Gamma.  For E_1 / E_2 the characters carry the factor d_E = 2. */
 typedef enum {

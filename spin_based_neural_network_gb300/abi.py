@@ -101,6 +101,12 @@ class MarshallWrapper(C.Structure):
                 ("size_x", C.c_int), ("size_y", C.c_int)]
 
 
+class TranslationWrapper(C.Structure):
+    """nqs_translation_wrapper_t (upstream include/nqs/nqs_translation.h)."""
+    _fields_ = [("base_log_amp", C.c_void_p), ("base_user", C.c_void_p),
+                ("size_x", C.c_int), ("size_y", C.c_int)]
+
+
 class SymprojWrapper(C.Structure):
     """nqs_symproj_wrapper_t (upstream include/nqs/nqs_symproj.h:39-47)."""
     _fields_ = [("base_log_amp", C.c_void_p), ("base_user", C.c_void_p),

@@ -339,6 +339,23 @@ static bool stage_perm(const nqs_symproj_wrapper_t *w, const int **dp, const dou
     return true;
 }
 
+// Square-lattice translation table of upstream src/nqs/nqs_translation.c:37-50:
+// row g = tx * Ly + ty, entry x * Ly + y = ((x + tx) mod Lx) * Ly + (y + ty) mod Ly.
+static const std::vector<int> *translation_table(int Lx, int Ly) {
+    static std::map<std::pair<int, int>, std::vector<int>> tabs;
+    std::vector<int> &t = tabs[{Lx, Ly}];
+    if (t.empty()) {
+        const int N = Lx * Ly;
+        t.resize((size_t)N * N);
+        for (int tx = 0; tx < Lx; tx++)
+            for (int ty = 0; ty < Ly; ty++)
+                for (int x = 0; x < Lx; x++)
+                    for (int y = 0; y < Ly; y++)
+                        t[(size_t)(tx * Ly + ty) * N + x * Ly + y] = ((x + tx) % Lx) * Ly + (y + ty) % Ly;
+    }
+    return &t;
+}
+
 static uint64_t marshall_mask(int sx, int sy, int N) {
     uint64_t m = 0;
     for (int x = 0; x < sx; x++)
@@ -366,6 +383,16 @@ bool build_amp(nqs_log_amp_fn_t fn, void *user, int num_sites, DevAmp *out, Ansa
             auto *w = (const nqs_marshall_wrapper_t *)user;
             if (!w) { set_error("NULL Marshall wrapper"); return false; }
             layers_type[nl] = 1;
+            layers_user[nl++] = w;
+            fn = w->base_log_amp;
+            user = w->base_user;
+        } else if (fn == nqs_translation_log_amp) {
+            auto *w = (const nqs_translation_wrapper_t *)user;
+            if (!w || w->size_x <= 0 || w->size_y <= 0) {
+                set_error("invalid translation wrapper");
+                return false;
+            }
+            layers_type[nl] = 3;
             layers_user[nl++] = w;
             fn = w->base_log_amp;
             user = w->base_user;
@@ -410,7 +437,16 @@ bool build_amp(nqs_log_amp_fn_t fn, void *user, int num_sites, DevAmp *out, Ansa
                 return false;
             }
             seen_sym = 1;
+            nqs_symproj_wrapper_t tw;
             auto *w = (const nqs_symproj_wrapper_t *)layers_user[k];
+            if (layers_type[k] == 3) {                 // translations as a symmetry projection
+                auto *t = (const nqs_translation_wrapper_t *)layers_user[k];
+                const std::vector<int> *tab = translation_table(t->size_x, t->size_y);
+                static const std::vector<double> ones(64, 1.0);
+                tw = nqs_symproj_wrapper_t{nullptr, nullptr, t->size_x * t->size_y, t->size_x * t->size_y,
+                                           tab->data(), ones.data()};
+                w = &tw;
+            }
             if (w->num_sites != num_sites) {
                 set_error("symproj num_sites %d != %d", w->num_sites, num_sites);
                 return false;
@@ -1018,6 +1054,10 @@ int nqs_gpu_gradient_batch(nqs_ansatz_t *h, nqs_gradient_fn_t gfn, void *guser, 
         DevAmp A;
         if (!build_amp(nqs_symproj_log_amp, guser, a->N, &A, nullptr)) return -1;
         if (!launch_symproj_gradient(A, bits, B, O.p)) return -1;
+    } else if (gfn == nqs_translation_gradient && !complex_out) {
+        DevAmp A;
+        if (!build_amp(nqs_translation_log_amp, guser, a->N, &A, nullptr)) return -1;
+        if (!launch_symproj_gradient(A, bits, B, O.p)) return -1;
     } else if ((void *)gfn == (void *)nqs_symproj_gradient_complex && complex_out) {
         DevAmp A;
         if (!build_amp(nqs_symproj_log_amp, guser, a->N, &A, nullptr)) return -1;
@@ -1046,6 +1086,22 @@ int nqs_ansatz_logpsi_gradient_complex(nqs_ansatz_t *h, const int *spins, int nu
     Ansatz *a = (Ansatz *)h;
     if (!a || !spins || !re || !im || num_sites != a->N) return -1;
     return nqs_gpu_gradient_batch(h, nullptr, nullptr, spins, 1, 1, re, im);
+}
+
+void nqs_translation_log_amp(const int *spins, int num_sites, void *user, double *out_log_abs,
+                             double *out_arg) {
+    double la = 0.0, ar = 0.0;
+    auto *w = (nqs_translation_wrapper_t *)user;
+    if (w && spins && num_sites == w->size_x * w->size_y)
+        if (scalar_log_amp(nqs_translation_log_amp, spins, num_sites, user, &la, &ar) != 0) la = ar = 0.0;
+    if (out_log_abs) *out_log_abs = la;
+    if (out_arg) *out_arg = ar;
+}
+
+int nqs_translation_gradient(void *grad_user, nqs_ansatz_t *h, const int *spins, int num_sites, double *out) {
+    auto *w = (nqs_translation_wrapper_t *)grad_user;
+    if (!w || !h || !spins || !out || num_sites != w->size_x * w->size_y) return -1;
+    return nqs_gpu_gradient_batch(h, nqs_translation_gradient, grad_user, spins, 1, 0, out, nullptr);
 }
 
 int nqs_symproj_gradient_complex(void *grad_user, nqs_ansatz_t *h, const int *spins, int num_sites,
@@ -1205,6 +1261,73 @@ int nqs_kagome_p6m_perm_irrep(int L, nqs_symproj_kagome_irrep_t irrep, int **out
 
 int nqs_kagome_p6m_perm(int L, int **out_perm, double **out_chars, int *out_G) {
     return nqs_kagome_p6m_perm_irrep(L, NQS_SYMPROJ_KAGOME_GAMMA_A1, out_perm, out_chars, out_G);
+}
+
+// Rotations about a fixed centre, then a translation (src/nqs/nqs_symproj.c:436-590), in
+// exact integer coordinates of 1/S lattice vectors: site (cx, cy, sub) sits at
+// (S cx + h [sub = 1], S cy + h [sub = 2]), h = S / 2; the source of output site p is
+// R(-60 steps)(p - c) + c - S t, with R(-60)(u, v) = (u + v, -u).
+static int rot_shift_source(int L, int S, int cu, int cv, int steps, int tx, int ty, int cx, int cy, int sub) {
+    const int h = S / 2;
+    int u = S * cx + (sub == 1 ? h : 0) - cu, v = S * cy + (sub == 2 ? h : 0) - cv;
+    for (int r = 0; r < steps; r++) {
+        int nu = u + v, nv = -u;
+        u = nu;
+        v = nv;
+    }
+    u += cu - S * tx;
+    v += cv - S * ty;
+    auto fdiv = [](int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); };
+    const int qu = fdiv(u, h), qv = fdiv(v, h);
+    if (qu * h != u || qv * h != v) return -1;         // not on the half-lattice
+    const int bu = qu & 1, bv = qv & 1;
+    if (bu && bv) return -1;                            // a hexagon centre
+    const int X = ((fdiv(qu - bu, 2)) % L + L) % L, Y = ((fdiv(qv - bv, 2)) % L + L) % L;
+    return KG_SITE(X, Y, bu ? 1 : (bv ? 2 : 0), L);
+}
+
+static int rot_group_perm(int L, int S, int cu, int cv, int nops, int step_per_op, int **out_perm, double **out_chars,
+                          int *out_G) {
+    if (L <= 0 || !out_perm || !out_chars || !out_G) return -1;
+    const int N = 3 * L * L, G = nops * L * L;
+    int *perm = (int *)malloc(sizeof(int) * (size_t)G * N);
+    double *chars = (double *)malloc(sizeof(double) * (size_t)G);
+    if (!perm || !chars) {
+        free(perm);
+        free(chars);
+        return -1;
+    }
+    int g = 0;
+    for (int k = 0; k < nops; k++)
+        for (int tx = 0; tx < L; tx++)
+            for (int ty = 0; ty < L; ty++, g++) {
+                for (int cx = 0; cx < L; cx++)
+                    for (int cy = 0; cy < L; cy++)
+                        for (int sub = 0; sub < 3; sub++) {
+                            int src = rot_shift_source(L, S, cu, cv, k * step_per_op, tx, ty, cx, cy, sub);
+                            if (src < 0) {
+                                free(perm);
+                                free(chars);
+                                return -1;
+                            }
+                            perm[(size_t)g * N + KG_SITE(cx, cy, sub, L)] = src;
+                        }
+                chars[g] = 1.0;
+            }
+    *out_perm = perm;
+    *out_chars = chars;
+    *out_G = G;
+    return 0;
+}
+
+// C3 about the up-triangle centroid (a1 + a2)/6 = (1, 1) in sixths
+int nqs_kagome_p3_perm(int L, int **out_perm, double **out_chars, int *out_G) {
+    return rot_group_perm(L, 6, 1, 1, 3, 2, out_perm, out_chars, out_G);
+}
+
+// C6 about the hexagon centre (a1 + a2)/2 = (1, 1) in halves
+int nqs_kagome_p6_perm(int L, int **out_perm, double **out_chars, int *out_G) {
+    return rot_group_perm(L, 2, 1, 1, 6, 1, out_perm, out_chars, out_G);
 }
 
 }  // extern "C"

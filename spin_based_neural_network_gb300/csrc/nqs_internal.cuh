@@ -27,6 +27,7 @@ extern "C" {
 #include "nqs/nqs_ansatz.h"
 #include "nqs/nqs_sampler.h"
 #include "nqs/nqs_gradient.h"
+#include "nqs/nqs_translation.h"
 #include "nqs/nqs_optimizer.h"
 #include "nqs/nqs_marshall.h"
 #include "nqs/nqs_symproj.h"

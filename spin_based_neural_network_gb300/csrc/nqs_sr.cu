@@ -876,8 +876,12 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     } else if (in.gfn == nqs_symproj_gradient) {
         if (!build_amp(nqs_symproj_log_amp, in.guser, H.N, &Ag, nullptr)) return -1;
         grad_sym = 1;
+    } else if (in.gfn == nqs_translation_gradient) {
+        if (!build_amp(nqs_translation_log_amp, in.guser, H.N, &Ag, nullptr)) return -1;
+        grad_sym = 1;
     } else {
-        set_error("gradient callback is not supported on the GPU (NULL or nqs_symproj_gradient)");
+        set_error("gradient callback is not supported on the GPU (NULL, nqs_symproj_gradient or "
+                  "nqs_translation_gradient)");
         return -1;
     }
     const bool holo = in.minsr >= 2, excited = in.minsr == 3, realtime = in.minsr == 4;

@@ -71,6 +71,10 @@ def _declare(L):
         "nqs_symproj_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
         "nqs_symproj_gradient": (C.c_int, [VP, VP, IP, C.c_int, DP]),
         "nqs_symproj_gradient_complex": (C.c_int, [VP, VP, IP, C.c_int, DP, DP]),
+        "nqs_translation_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
+        "nqs_translation_gradient": (C.c_int, [VP, VP, IP, C.c_int, DP]),
+        "nqs_kagome_p3_perm": (C.c_int, [C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
+        "nqs_kagome_p6_perm": (C.c_int, [C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
         "nqs_kagome_translation_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), IP]),
         "nqs_kagome_p2_perm": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
         "nqs_kagome_p6m_perm_irrep": (C.c_int, [C.c_int, C.c_int, C.POINTER(IP), C.POINTER(DP), IP]),
@@ -264,15 +268,36 @@ class Symproj:
         return C.addressof(self.s)
 
 
+class Translation:
+    """nqs_translation_wrapper_t: the translation-symmetric projection of a square or chain
+    lattice amplitude (upstream include/nqs/nqs_translation.h)."""
+
+    def __init__(self, base_fn, base_user, size_x, size_y):
+        self.s = abi.TranslationWrapper(base_fn, base_user, size_x, size_y)
+        self.log_amp_fn = fn("nqs_translation_log_amp")
+        self.gradient_fn = fn("nqs_translation_gradient")
+
+    @property
+    def user(self):
+        return C.addressof(self.s)
+
+
 P6M_IRREPS = {"A1": 0, "A2": 1, "B1": 2, "B2": 3, "E1": 4, "E2": 5}
 
 
 def kagome_perm(Lx, Ly, group="p2", irrep="A1"):
     """(perm [G, N], characters [G]) of a kagome symmetry group: "p2", "translations", or
-    "p6m" (L x L torus, irrep one of A1 A2 B1 B2 E1 E2)."""
+    on an L x L torus "p3", "p6", "p6m" (irrep one of A1 A2 B1 B2 E1 E2 for p6m)."""
     p = IP()
     G = C.c_int()
-    if group == "p6m":
+    if group in ("p3", "p6"):
+        if Lx != Ly:
+            raise NqsError(group + " needs an L x L torus")
+        ch = DP()
+        f = lib().nqs_kagome_p3_perm if group == "p3" else lib().nqs_kagome_p6_perm
+        _check(f(Lx, C.byref(p), C.byref(ch), C.byref(G)), group + " perm")
+        chars = np.ctypeslib.as_array(ch, shape=(G.value,)).copy()
+    elif group == "p6m":
         if Lx != Ly:
             raise NqsError("p6m needs an L x L torus")
         ch = DP()

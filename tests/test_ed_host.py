@@ -132,3 +132,15 @@ def test_recorded_3x3_sector_spectrum_is_consistent():
     assert rec["A1"]["E0"] < rec["A2"]["E0"] < rec["B2"]["E0"]      # A1 is the global ground state
     for s in rec.values():
         assert abs(s["E0"] - s["independent_ED"]) < 5e-9
+
+
+@pytest.mark.parametrize("group", ["p3", "p6"])
+@pytest.mark.parametrize("L", [2, 3])
+def test_p3_p6_tables_match_upstream(group, L):
+    """nqs_kagome_p3_perm / nqs_kagome_p6_perm (rotation about the up-triangle centroid /
+    the hexagon centre, then translation) equal upstream's tables
+    (tests/golden/translation.npz, from the reference)."""
+    g = np.load(os.path.join(GOLD, "translation.npz"))
+    perm, chars = nqs.kagome_perm(L, L, group)
+    assert np.array_equal(perm.astype(np.int32).reshape(-1), g["%s_L%d__perm" % (group, L)])
+    assert np.array_equal(chars, g["%s_L%d__chars" % (group, L)])

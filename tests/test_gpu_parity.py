@@ -486,3 +486,34 @@ def test_holomorphic_sr_through_symmetry_projection(nqs, grad):
     assert rel(E, Eo) < TOL
     assert np.linalg.norm(delta - do) <= TOL_DELTA * np.linalg.norm(do)
     assert rel(a.params, amp.params) < TOL
+
+
+@pytest.mark.parametrize("name", ["rbm_4x3", "crbm_4x4_marshall", "rbm_chain8"])
+def test_translation_projector_against_reference(nqs, name):
+    """nqs_translation_log_amp / nqs_translation_gradient (src/nqs/nqs_translation.c:23-145)
+    against the upstream functions' outputs (tests/golden/translation.npz); the device runs
+    them as the symmetry projection with the square translation table."""
+    gz = np.load(os.path.join(GOLD, "translation.npz"))
+    d = {k.split("__")[1]: gz[k] for k in gz.files if k.startswith(name + "__")}
+    Lx, Ly = int(d["Lx"]), int(d["Ly"])
+    N = Lx * Ly
+    a = make_ansatz(nqs, int(d["kind"]), N, N, d["params"])
+    if int(d["marshall"]):
+        m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+        base_fn, base_user = m.log_amp_fn, m.user
+    else:
+        base_fn, base_user = a.log_amp_fn, a.user
+    t = nqs.Translation(base_fn, base_user, Lx, Ly)
+    la, ar = nqs.log_amp_batch(t.log_amp_fn, t.user, d["spins"])
+    assert rel(la, d["la"]) < TOL
+    assert np.array_equal(ar, d["arg"])
+    B = len(d["spins"])
+    g = np.zeros((B, a.P))
+    s = np.ascontiguousarray(d["spins"], dtype=np.int32)
+    assert nqs.lib().nqs_gpu_gradient_batch(a.h, t.gradient_fn, t.user, s.ctypes.data_as(nqs.IP), B, 0,
+                                            g.ctypes.data_as(nqs.DP), None) == 0
+    assert rel(g, d["grad"]) < 1e-11
+    g1 = np.zeros(a.P)
+    assert nqs.lib().nqs_translation_gradient(t.user, a.h, s[5].ctypes.data_as(nqs.IP), N,
+                                              g1.ctypes.data_as(nqs.DP)) == 0
+    assert rel(g1, d["grad"][5]) < 1e-11
