@@ -26,6 +26,8 @@ long oracle_num_params(int kind, int N, int M) {
         case OR_RBM:  return n + m + m * n;                       /* src/nqs/nqs_ansatz.c:88 */
         case OR_CRBM: return 2 * (n + m + m * n);                 /* src/nqs/nqs_ansatz.c:223 */
         case OR_MLP:  return m * n + m + m * m + m + 2 * m + 2;   /* extension */
+        case OR_VIT:  return 3 * m + m * m + n + 1;                /* :113-130, m = d */
+        case OR_VITC: return 6 * m + 2 * m * m + n + 2;            /* :155-172 */
         default:      return -1;
     }
 }
@@ -68,6 +70,33 @@ int oracle_ansatz_init(int kind, int N, int M, double scale, unsigned seed,
         }
         return 0;
     }
+    if (kind == OR_VIT || kind == OR_VITC) {                      /* :131-151, :173-214 (M = d) */
+        int d = M;
+        double vs = scale / sqrt((double)d), is = 0.1 * scale;
+        if (kind == OR_VIT) {
+            for (int i = 0; i < d; i++) p[i] = scale * xs_gauss(&st);
+            for (int i = 0; i < d; i++) p[d + i] = scale * (xs_uniform(&st) - 0.5);
+            for (long k = 0; k < (long)d * d; k++) p[2L * d + k] = vs * xs_gauss(&st);
+            long ao = 2L * d + (long)d * d;
+            for (int k = 0; k < N; k++) p[ao + k] = scale * (xs_uniform(&st) - 0.5);
+            for (int i = 0; i < d; i++) p[ao + N + i] = scale * (xs_uniform(&st) - 0.5);
+            p[ao + N + d] = 0.0;
+        } else {
+            for (int i = 0; i < d; i++) p[i] = scale * xs_gauss(&st);
+            for (int i = 0; i < d; i++) p[d + i] = is * xs_gauss(&st);
+            for (int i = 0; i < d; i++) p[2 * d + i] = scale * (xs_uniform(&st) - 0.5);
+            for (int i = 0; i < d; i++) p[3 * d + i] = is * (xs_uniform(&st) - 0.5);
+            long vr = 4L * d, vi = vr + (long)d * d, ao = vi + (long)d * d;
+            for (long k = 0; k < (long)d * d; k++) p[vr + k] = vs * xs_gauss(&st);
+            for (long k = 0; k < (long)d * d; k++) p[vi + k] = 0.1 * vs * xs_gauss(&st);
+            for (int k = 0; k < N; k++) p[ao + k] = scale * (xs_uniform(&st) - 0.5);
+            for (int i = 0; i < d; i++) p[ao + N + i] = scale * (xs_uniform(&st) - 0.5);
+            for (int i = 0; i < d; i++) p[ao + N + d + i] = is * (xs_uniform(&st) - 0.5);
+            p[ao + N + 2 * d] = 0.0;
+            p[ao + N + 2 * d + 1] = 0.0;
+        }
+        return 0;
+    }
     if (kind == OR_MLP) {
         /* Extension: Xavier-normal weights drawn in layout order from the same
          * xorshift/Box-Muller stream, biases zero. */
@@ -90,6 +119,184 @@ int oracle_ansatz_init(int kind, int N, int M, double scale, unsigned seed,
 /* ------------------------------------------------------------------ */
 /* Base log-amplitudes                                                 */
 /* ------------------------------------------------------------------ */
+
+/* Factored-attention ViT, src/nqs/nqs_ansatz.c:357-473 (real) and :571-729 (complex), in
+ * upstream's loop order on the complex form (imaginary parts 0 for the real ViT):
+ * e_i = w s_i + b, v_i = V e_i, P_ij = softmax_j a[(i-j) mod N], o_i = sum_j P_ij v_j,
+ * log psi = sum_i W . o_i + b_out. */
+typedef struct {
+    int N, d;
+    const double *wR, *wI, *bR, *bI, *VR, *VI, *attn, *WR, *WI;
+    double boR, boI;
+    double *eR, *eI, *vR, *vI, *P, *oR, *oI;   /* scratch */
+} vit_t;
+
+static void vit_bind(const or_ansatz_t *a, vit_t *v) {
+    int N = a->N, d = a->M;
+    const double *p = a->params;
+    v->N = N;
+    v->d = d;
+    if (a->kind == OR_VITC) {
+        v->wR = p; v->wI = p + d; v->bR = p + 2 * d; v->bI = p + 3 * d;
+        v->VR = p + 4 * d; v->VI = v->VR + (long)d * d; v->attn = v->VI + (long)d * d;
+        v->WR = v->attn + N; v->WI = v->WR + d; v->boR = v->WI[d]; v->boI = v->WI[d + 1];
+    } else {
+        v->wR = p; v->wI = NULL; v->bR = p + d; v->bI = NULL;
+        v->VR = p + 2 * d; v->VI = NULL; v->attn = v->VR + (long)d * d;
+        v->WR = v->attn + N; v->WI = NULL; v->boR = v->WR[d]; v->boI = 0.0;
+    }
+    size_t nd = (size_t)N * d;
+    v->eR = calloc(nd, sizeof(double)); v->eI = calloc(nd, sizeof(double));
+    v->vR = calloc(nd, sizeof(double)); v->vI = calloc(nd, sizeof(double));
+    v->P = calloc((size_t)N * N, sizeof(double));
+    v->oR = calloc(nd, sizeof(double)); v->oI = calloc(nd, sizeof(double));
+}
+
+static void vit_free(vit_t *v) {
+    free(v->eR); free(v->eI); free(v->vR); free(v->vI); free(v->P); free(v->oR); free(v->oI);
+}
+
+#define VI_(arr, k) ((arr) ? (arr)[k] : 0.0)
+
+static void vit_forward(vit_t *v, const int *s, double *la, double *ar) {
+    int N = v->N, d = v->d;
+    for (int i = 0; i < N; i++)
+        for (int k = 0; k < d; k++) {
+            v->eR[i * d + k] = v->wR[k] * (double)s[i] + v->bR[k];
+            v->eI[i * d + k] = VI_(v->wI, k) * (double)s[i] + VI_(v->bI, k);
+        }
+    for (int i = 0; i < N; i++)
+        for (int k = 0; k < d; k++) {
+            double sr = 0.0, si = 0.0;
+            for (int l = 0; l < d; l++) {
+                double vrr = v->VR[k * d + l], vii = VI_(v->VI, k * d + l);
+                double er = v->eR[i * d + l], ei = v->eI[i * d + l];
+                sr += vrr * er - vii * ei;
+                si += vrr * ei + vii * er;
+            }
+            v->vR[i * d + k] = sr;
+            v->vI[i * d + k] = si;
+        }
+    for (int i = 0; i < N; i++) {
+        double mx = -1e300;
+        for (int j = 0; j < N; j++) {
+            double S = v->attn[((i - j) % N + N) % N];
+            if (S > mx) mx = S;
+        }
+        double Z = 0.0;
+        for (int j = 0; j < N; j++) {
+            double e = exp(v->attn[((i - j) % N + N) % N] - mx);
+            v->P[i * N + j] = e;
+            Z += e;
+        }
+        double iz = 1.0 / Z;
+        for (int j = 0; j < N; j++) v->P[i * N + j] *= iz;
+    }
+    for (int i = 0; i < N; i++)
+        for (int k = 0; k < d; k++) {
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < N; j++) {
+                sr += v->P[i * N + j] * v->vR[j * d + k];
+                si += v->P[i * N + j] * v->vI[j * d + k];
+            }
+            v->oR[i * d + k] = sr;
+            v->oI[i * d + k] = si;
+        }
+    double l = v->boR, g = v->boI;
+    for (int i = 0; i < N; i++)
+        for (int k = 0; k < d; k++) {
+            double orr = v->oR[i * d + k], oii = v->oI[i * d + k];
+            l += v->WR[k] * orr - VI_(v->WI, k) * oii;
+            g += v->WR[k] * oii + VI_(v->WI, k) * orr;
+        }
+    *la = l;
+    *ar = g;
+}
+
+/* Holomorphic derivatives z_k = d log psi / d(complex weight), src/nqs/nqs_ansatz.c:1104-1256,
+ * written into the real-projected row (mode 1: Re z for real parts, -Im z for imaginary
+ * parts; the real ViT's gradient, :475-567) or the holomorphic pair (mode 2). */
+static void vit_gradient(const or_ansatz_t *a, const int *s, int mode, double *re, double *im) {
+    vit_t v;
+    vit_bind(a, &v);
+    int N = v.N, d = v.d;
+    const int cx = a->kind == OR_VITC;
+    double la, ar;
+    vit_forward(&v, s, &la, &ar);
+    long P = oracle_num_params(a->kind, N, d);
+    memset(re, 0, sizeof(double) * (size_t)P);
+    if (im) memset(im, 0, sizeof(double) * (size_t)P);
+    double *sp = calloc((size_t)N, sizeof(double)), *WvR = calloc((size_t)N, sizeof(double));
+    double *WvI = calloc((size_t)N, sizeof(double)), *WoR = calloc((size_t)N, sizeof(double));
+    double *WoI = calloc((size_t)N, sizeof(double)), *ga_r = calloc((size_t)N, sizeof(double));
+    double *ga_i = calloc((size_t)N, sizeof(double));
+    double *evR = calloc((size_t)d, sizeof(double)), *evI = calloc((size_t)d, sizeof(double));
+    double *alR = calloc((size_t)d, sizeof(double)), *alI = calloc((size_t)d, sizeof(double));
+    double *sWR = calloc((size_t)d, sizeof(double)), *sWI = calloc((size_t)d, sizeof(double));
+    for (int k = 0; k < d; k++)
+        for (int i = 0; i < N; i++) { sWR[k] += v.oR[i * d + k]; sWI[k] += v.oI[i * d + k]; }
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) sp[j] += v.P[i * N + j];
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < d; k++) {
+            double vr = v.vR[j * d + k], vi = v.vI[j * d + k];
+            WvR[j] += v.WR[k] * vr - VI_(v.WI, k) * vi;
+            WvI[j] += v.WR[k] * vi + VI_(v.WI, k) * vr;
+        }
+    for (int i = 0; i < N; i++)
+        for (int k = 0; k < d; k++) {
+            double orr = v.oR[i * d + k], oii = v.oI[i * d + k];
+            WoR[i] += v.WR[k] * orr - VI_(v.WI, k) * oii;
+            WoI[i] += v.WR[k] * oii + VI_(v.WI, k) * orr;
+        }
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) {
+            int rel = ((i - j) % N + N) % N;
+            ga_r[rel] += v.P[i * N + j] * (WvR[j] - WoR[i]);
+            ga_i[rel] += v.P[i * N + j] * (WvI[j] - WoI[i]);
+        }
+    for (int j = 0; j < N; j++)
+        for (int l = 0; l < d; l++) { evR[l] += sp[j] * v.eR[j * d + l]; evI[l] += sp[j] * v.eI[j * d + l]; }
+    for (int l = 0; l < d; l++)
+        for (int k = 0; k < d; k++) {
+            alR[l] += v.VR[k * d + l] * v.WR[k] - VI_(v.VI, k * d + l) * VI_(v.WI, k);
+            alI[l] += v.VR[k * d + l] * VI_(v.WI, k) + VI_(v.VI, k * d + l) * v.WR[k];
+        }
+    double sps = 0.0, spp = 0.0;
+    for (int j = 0; j < N; j++) { sps += sp[j] * (double)s[j]; spp += sp[j]; }
+    /* (re, im) of z at the real slot kR and the imaginary slot kI (kI < 0: real parameter) */
+    #define PUT(kR, kI, zr, zi) do {                                              \
+        if (mode == 2) {                                                           \
+            re[kR] = (zr); im[kR] = (zi);                                          \
+            if ((kI) >= 0) { re[kI] = -(zi); im[kI] = (zr); }                      \
+        } else {                                                                   \
+            re[kR] = (zr);                                                         \
+            if ((kI) >= 0) re[kI] = -(zi);                                         \
+        }                                                                          \
+    } while (0)
+    long o_w = 0, o_wI = cx ? d : -1, o_b = cx ? 2L * d : d, o_bI = cx ? 3L * d : -1;
+    long o_V = cx ? 4L * d : 2L * d, o_VI = cx ? o_V + (long)d * d : -1;
+    long o_a = cx ? 4L * d + 2L * d * d : 2L * d + (long)d * d;
+    long o_W = o_a + N, o_WI = cx ? o_W + d : -1, o_bo = cx ? o_W + 2L * d : o_W + d;
+    for (int l = 0; l < d; l++) {
+        PUT(o_w + l, o_wI < 0 ? -1 : o_wI + l, sps * alR[l], sps * alI[l]);
+        PUT(o_b + l, o_bI < 0 ? -1 : o_bI + l, spp * alR[l], spp * alI[l]);
+    }
+    for (int k = 0; k < d; k++)
+        for (int l = 0; l < d; l++) {
+            double zr = v.WR[k] * evR[l] - VI_(v.WI, k) * evI[l];
+            double zi = v.WR[k] * evI[l] + VI_(v.WI, k) * evR[l];
+            long q = (long)k * d + l;
+            PUT(o_V + q, o_VI < 0 ? -1 : o_VI + q, zr, zi);
+        }
+    for (int r = 0; r < N; r++) PUT(o_a + r, -1, ga_r[r], ga_i[r]);
+    for (int k = 0; k < d; k++) PUT(o_W + k, o_WI < 0 ? -1 : o_WI + k, sWR[k], sWI[k]);
+    PUT(o_bo, cx ? o_bo + 1 : -1, 1.0, 0.0);
+    #undef PUT
+    free(sp); free(WvR); free(WvI); free(WoR); free(WoI); free(ga_r); free(ga_i);
+    free(evR); free(evI); free(alR); free(alI); free(sWR); free(sWI);
+    vit_free(&v);
+}
 
 /* complex log(2 cosh z), the stable form of src/nqs/nqs_ansatz.c:309-318 */
 static void clogcosh(double x, double y, double *la, double *ar) {
@@ -162,6 +369,11 @@ static void base_log_amp(const or_ansatz_t *a, const int *s, double *la, double 
         double *h1 = malloc(sizeof(double) * 2 * (size_t)M);
         mlp_forward(a, s, h1, h1 + M, la, ar);
         free(h1);
+    } else if (a->kind == OR_VIT || a->kind == OR_VITC) {
+        vit_t v;
+        vit_bind(a, &v);
+        vit_forward(&v, s, la, ar);
+        vit_free(&v);
     } else {                                                       /* :265-270 */
         double acc = 0.0;
         for (int i = 0; i < N; i++) acc += p[i] * (double)s[i];
@@ -332,6 +544,10 @@ static int grad_one(const or_ansatz_t *a, const int *s, double *out) {
         out[P - 1] = 0.0;
         return 0;
     }
+    if (a->kind == OR_VIT || a->kind == OR_VITC) {                /* :475-567, :732-843 */
+        vit_gradient(a, s, 1, out, NULL);
+        return 0;
+    }
     for (int i = 0; i < N; i++) out[i] = (double)s[i];            /* :875-879 */
     return 0;
 }
@@ -383,6 +599,10 @@ static int grad_complex_one(const or_ansatz_t *a, const int *s, double *re, doub
         re[P - 2] = 1.0; im[P - 2] = 0.0;
         re[P - 1] = 0.0; im[P - 1] = 1.0;
         free(h2);
+        return 0;
+    }
+    if (a->kind == OR_VITC) {                                      /* :1104-1256 */
+        vit_gradient(a, s, 2, re, im);
         return 0;
     }
     int rc = grad_one(a, s, re);                                   /* :1268-1272 */

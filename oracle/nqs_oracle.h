@@ -26,7 +26,7 @@ extern "C" {
 
 /* Ansatz kinds: upstream values (include/nqs/nqs_config.h:25-45) + the deep MLP
  * extension (value 100, same as the product's NQS_GPU_ANSATZ_MLP). */
-enum { OR_MF = 0, OR_RBM = 5, OR_CRBM = 6, OR_MLP = 100 };
+enum { OR_MF = 0, OR_VIT = 2, OR_RBM = 5, OR_CRBM = 6, OR_VITC = 7, OR_MLP = 100 };
 /* Hamiltonian kinds: upstream values (include/nqs/nqs_config.h:58-79). */
 enum { OR_TFIM = 0, OR_HEIS = 1, OR_J1J2 = 2, OR_XXZ = 4, OR_KAGOME = 6 };
 

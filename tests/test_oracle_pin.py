@@ -287,3 +287,31 @@ def test_holo_step_with_symproj_gradient_identity():
     E2, d2, _ = O.holo_step(h, a2, batch, 1e-2, 0.01, 40, 1e-10)
     assert np.array_equal(E1, E2)
     assert np.linalg.norm(d1 - d2) <= 1e-13 * np.linalg.norm(d2)
+
+
+def _vit_cases():
+    g = np.load(os.path.join(GOLD, "ansatz_vit.npz"))
+    names = sorted({k.split("__")[0] for k in g.files})
+    return {n: {k.split("__")[1]: g[k] for k in g.files if k.startswith(n + "__")} for n in names}
+
+
+@pytest.mark.parametrize("name", sorted(_vit_cases()))
+def test_oracle_vit_matches_upstream(name):
+    """The oracle's factored-attention ViT (src/nqs/nqs_ansatz.c:113-215, 357-844,
+    1093-1256 in upstream's loop order) against the upstream library's outputs
+    (tests/golden/ansatz_vit.npz): initialisation bit for bit, log-amplitudes, both
+    gradients and the local energies."""
+    from spin_based_neural_network_gb300 import abi
+    d = _vit_cases()[name]
+    kind, N, w = int(d["kind"]), int(d["N"]), int(d["d"])
+    scale = float(d["scale"]) if float(d["scale"]) > 0 else abi.config_defaults().rbm_init_scale
+    assert np.array_equal(O.init_params(kind, N, w, scale, int(d["seed"])), d["params0"])
+    amp = O.Amp(kind, N, w, d["params"].copy())
+    la, ar = O.log_amp(amp, d["spins"])
+    assert rel(la, d["la"]) < 1e-13 and np.max(np.abs(ar - d["arg"])) < 1e-13
+    assert rel(O.gradient(amp, d["spins"]), d["grad"]) < 1e-13
+    gr, gi = O.gradient_complex(amp, d["spins"])
+    assert rel(gr, d["grad_re"]) < 1e-13 and rel(gi, d["grad_im"]) < 1e-13
+    h = O.ham(int(d["ham"]), int(d["Lx"]), int(d["Ly"]), Gamma=0.8)
+    er, ei = O.local_energy(h, amp, d["spins"], complex_out=True)
+    assert rel(er, d["eloc_re"]) < 1e-12 and rel(ei, d["eloc_im"]) < 1e-12
