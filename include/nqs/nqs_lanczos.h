@@ -76,8 +76,9 @@ int nqs_gpu_sector_project(int N, int G, const int *perm, const double *characte
  * 0xBEEFBABE ^ 2^N (alternate = 1), scaled by 2^-53 after >> 11. */
 int nqs_gpu_lanczos_seed(int N, int alternate, double *d_out);
 
-/* Tridiagonal coefficients of the last Lanczos run on this thread's context:
- * alpha[0..K-1], beta[1..K] (beta[0] = 0).  Returns K (<= cap copied). */
+/* Tridiagonal coefficients of the last Lanczos run: alpha[0..K-1] and beta[0..K]
+ * (beta[0] = 0); at most cap entries of alpha and cap + 1 of beta are written (beta holds
+ * cap + 1 doubles).  Returns K. */
 int nqs_gpu_lanczos_last_coeffs(int cap, double *alpha, double *beta);
 
 /* Host-side plan of the sector projector (no device needed): *out_passes = 1 (direct) to

@@ -955,7 +955,7 @@ int nqs_gpu_lanczos_last_coeffs(int cap, double *alpha, double *beta) {
     const int K = (int)a.size();
     for (int i = 0; i < K && i < cap; i++)
         if (alpha) alpha[i] = a[i];
-    for (int i = 0; i <= K && i < cap; i++)
+    for (int i = 0; i <= K && i <= cap; i++)
         if (beta) beta[i] = i == 0 ? 0.0 : b[i];
     return K;
 }

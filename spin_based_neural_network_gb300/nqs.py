@@ -654,7 +654,8 @@ def lanczos_e0_kagome_lean(Lx, Ly, J, pbc, perm, chars, max_iters=100, tol=1e-9,
 def lanczos_last_coeffs(cap=4096):
     """(alpha[K], beta[K+1]) of the last Lanczos run (beta[0] = 0)."""
     a, b = np.zeros(cap), np.zeros(cap + 1)
-    K = lib().nqs_gpu_lanczos_last_coeffs(cap + 1, _dp(a), _dp(b))
+    K = lib().nqs_gpu_lanczos_last_coeffs(cap, _dp(a), _dp(b))
+    K = min(K, cap)
     return a[:K].copy(), b[:K + 1].copy()
 
 
