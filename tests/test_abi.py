@@ -50,10 +50,13 @@ def test_struct_layouts_match_c(tmp_path):
 #include "nqs/nqs_gpu.h"
 #include "nqs/nqs_marshall.h"
 #include "nqs/nqs_symproj.h"
+#include "nqs/nqs_translation.h"
+#include "nqs/nqs_lanczos.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(nqs_config_t), offsetof(nqs_config_t, sr_cg_tol),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(nqs_config_t), offsetof(nqs_config_t, sr_cg_tol),
          offsetof(nqs_config_t, rng_seed), sizeof(nqs_sr_step_info_t), sizeof(nqs_gpu_options_t),
-         sizeof(nqs_marshall_wrapper_t), sizeof(nqs_symproj_wrapper_t), sizeof(nqs_gpu_step_stats_t));
+         sizeof(nqs_marshall_wrapper_t), sizeof(nqs_symproj_wrapper_t), sizeof(nqs_gpu_step_stats_t),
+         sizeof(nqs_translation_wrapper_t), sizeof(lanczos_result_t), offsetof(lanczos_result_t, residual_norm));
   return 0;
 }
 """)
@@ -63,7 +66,8 @@ int main(void) {
     from spin_based_neural_network_gb300 import nqs
     want = [C.sizeof(abi.NqsConfig), abi.NqsConfig.sr_cg_tol.offset, abi.NqsConfig.rng_seed.offset,
             C.sizeof(abi.StepInfo), C.sizeof(abi.GpuOptions), C.sizeof(abi.MarshallWrapper),
-            C.sizeof(abi.SymprojWrapper), C.sizeof(nqs.StepStats)]
+            C.sizeof(abi.SymprojWrapper), C.sizeof(nqs.StepStats), C.sizeof(abi.TranslationWrapper),
+            C.sizeof(abi.LanczosResult), abi.LanczosResult.residual_norm.offset]
     assert got == want
 
 
@@ -101,6 +105,8 @@ def test_c_header_compiles_as_c11_and_cxx(tmp_path):
     for comp, std in (("gcc", "-std=c11"), ("g++", "-std=c++17")):
         src = tmp_path / ("h." + ("c" if comp == "gcc" else "cpp"))
         src.write_text('#include "nqs/nqs_gpu.h"\n#include "nqs/nqs_gradient.h"\n'
-                       '#include "nqs/nqs_marshall.h"\n#include "nqs/nqs_symproj.h"\nint main(void){return 0;}\n')
+                       '#include "nqs/nqs_marshall.h"\n#include "nqs/nqs_symproj.h"\n'
+                       '#include "nqs/nqs_optimizer.h"\n#include "nqs/nqs_translation.h"\n'
+                       '#include "nqs/nqs_lanczos.h"\nint main(void){return 0;}\n')
         subprocess.check_call([comp, std, "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
                                str(src), "-o", str(tmp_path / "h")])
