@@ -487,18 +487,18 @@ def step_kernels(nqs, step, top=8):
     return {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:top]}
 
 
-def other_configs(nqs, abi, L, base_opts, which):
+def other_workloads(nqs, abi, L, base_opts, which):
     """The other workloads of the measurement table, each on its own shapes
     (seeded synthetic parameters, configurations from the sampler):
-      cfg1  1-D TFIM N = 16 PBC, h = 1, real RBM alpha = 1 (N_p = 288), 16 chains x 64 = 1024
+      tfim   1-D TFIM N = 16 PBC, h = 1, real RBM alpha = 1 (N_p = 288), 16 chains x 64 = 1024
             samples, single flips, 2N sweeps thermalisation, CG-SR shift 1e-3, lr 0.01, all FP64,
             200 steps; |E/N - E0/N| against the oracle's Lanczos energy;
-      cfg3  J1-J2 6x6 PBC, J2 = 0.5, complex RBM alpha = 4 (N_p = 10728), N(0, 0.005^2),
+      j1j2   J1-J2 6x6 PBC, J2 = 0.5, complex RBM alpha = 4 (N_p = 10728), N(0, 0.005^2),
             1024 chains x 8 = 8192 samples, exchange moves in Sz = 0, MinSR shift 1e-4, lr 0.005
             (the 2-D workload's values), mixed precision; the solve runs in sample space
             (8192 x 8192); delta-theta and energy errors against the FP64 step on the same samples,
             and the FP64 path's own steps/s;
-      cfg4  kagome 3x3 PBC (N = 27) Heisenberg, Sz = 1/2, MLP 27-108-108-(Re, Im) tanh (Xavier,
+      kagome kagome 3x3 PBC (N = 27) Heisenberg, Sz = 1/2, MLP 27-108-108-(Re, Im) tanh (Xavier,
             N_p = 15014), 1024 chains x 16 = 16384 samples, exchange moves on the kagome bonds,
             MinSR shift 1e-3, lr 0.005, mixed precision (FP32 MLP estimator and chains: layer 1
             updated by weight columns, layer 2 against W2^T in shared memory); a few timed
@@ -506,7 +506,7 @@ def other_configs(nqs, abi, L, base_opts, which):
             for reference."""
     import numpy as np
     out = {}
-    if "1" in which:
+    if "tfim" in which:
         nqs.set_options(**dict(base_opts, precision=abi.PREC_FP64, fp32_estimator=0))
         N = 16
         cfg = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=N, hamiltonian=abi.HAM_TFIM,
@@ -530,11 +530,11 @@ def other_configs(nqs, abi, L, base_opts, which):
         with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
             e0 = json.load(f)["tfim_chain16_pbc_h1"]["E0_per_site"]
         run = float(np.mean(es[-20:])) / N
-        out["cfg1_tfim16_cgsr_fp64"] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "steps": 200,
+        out["tfim_chain16_rbm_cgsr_fp64"] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "steps": 200,
                                         "cg_iterations_last": info.cg_iterations, "kernels_ms_one_step": k1,
                                         "energy_per_site_last20": run, "e0_per_site": e0,
                                         "abs_err_per_site": abs(run - e0)}
-    if "3" in which:
+    if "j1j2" in which:
         nqs.set_options(**base_opts)
         Lx = Ly = 6
         N, M = 36, 144
@@ -560,13 +560,13 @@ def other_configs(nqs, abi, L, base_opts, which):
                                       lattice_x=Lx, lattice_y=Ly, square_pbc=1, precision=abi.PREC_FP64))
         s64.thermalize()
         ms64, _ = timed_steps(nqs, L, lambda: nqs.sr_step_minsr(cfg, Lx, Ly, a, s64, a.log_amp_fn, a.user), 1, 2)
-        out["cfg3_j1j2_6x6_crbm_alpha4_ns8192"] = {
+        out["j1j2_6x6_crbm_alpha4_ns8192_minsr"] = {
             "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "solve_space": "samples (N_s = 8192 < N_p = 10728)",
             "num_params": a.P, "delta_theta_rel_err_vs_fp64": st.delta_rel_err, "energy_rel_err": st.energy_rel_err,
             "cg_residual": st.refine_residual, "cg_iterations": st.refine_sweeps,
             "factor_solve_phases_us": [round(x, 1) for x in ph], "kernels_ms_one_step": k3,
             "plain_fp64_steps_per_s": 1000.0 / ms64, "speedup_vs_fp64": ms64 / ms}
-    if "4" in which:
+    if "kagome" in which:
         nqs.set_options(**base_opts)
         N, W = 27, 108
         cfg = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=W, depth=2, hamiltonian=abi.HAM_KAGOME_HEISENBERG,
@@ -612,7 +612,7 @@ def other_configs(nqs, abi, L, base_opts, which):
         proposals4 = [run4(False, N), run4(True, N), run4(False, 4), run4(True, 4)]
         with open(os.path.join(ROOT, "tests", "golden", "kagome_3x3_e0.json")) as f:
             e0 = json.load(f)["kagome_3x3_pbc_heisenberg"]["E0_per_site"]
-        out["cfg4_kagome3x3_mlp108_ns16384"] = {
+        out["kagome3x3_mlp108_ns16384_minsr"] = {
             "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "num_params": a.P,
             "solve_space": "parameters (N_p = 15014 < N_s = 16384)", "energy_per_site_last": info.mean_energy / N,
             "e0_per_site_recorded_upstream": e0, "factor_solve_phases_us": [round(x, 1) for x in ph],
@@ -839,8 +839,8 @@ def run_gpu(args):
         nqs.set_options(**base_opts)
 
     others = None
-    if prec == abi.PREC_MIXED and args.configs:
-        others = other_configs(nqs, abi, L, base_opts, args.configs)
+    if prec == abi.PREC_MIXED and args.workloads:
+        others = other_workloads(nqs, abi, L, base_opts, args.workloads.split(","))
 
     ed = None
     if prec == abi.PREC_MIXED and args.ed:
@@ -880,7 +880,7 @@ def run_gpu(args):
             "roofline": roof, "roofline_other": extra_roofs, "clocks": clk, "kernels": kernels,
             "delta_theta_vs_fp64": delta_err, "plain_fp64": plain, "factor_solve_phases_us": phases,
             "convergence_vs_lanczos": conv, "plain_vs_learned_proposal": proposals, "multi_instance": multi, "multi_instance_learned": multi_learned,
-            "other_configs": others, "sector_ed": ed,
+            "other_workloads": others, "sector_ed": ed,
             "final_energy_per_site": energies[-1] / N_SITES if energies else None}
     if rank == 0 and not args.no_cpu_baseline:
         secs = cpu_step(("port", SEED))
@@ -941,8 +941,10 @@ def main():
     ap.add_argument("--converge-steps", type=int, default=1000,
                     help="max optimisation steps of the |dE/N| <= 1e-4 vs Lanczos run (0 = skip)")
     ap.add_argument("--converge-fp64", action="store_true", help="also run the FP64 path to the target")
-    ap.add_argument("--configs", default="134",
-                    help="which of the other workloads to run (digits of 1, 3, 4; empty = none)")
+    ap.add_argument("--configs", default=None, help=argparse.SUPPRESS)   # older spelling: digits 1, 3, 4
+    ap.add_argument("--workloads", default="tfim,j1j2,kagome",
+                    help="comma-separated other workloads to run: tfim (1-D TFIM chain, CG-SR FP64), j1j2 "
+                         "(J1-J2 6x6, MinSR), kagome (kagome 3x3 MLP, MinSR); empty = none")
     ap.add_argument("--ed", default="A1",
                     help="comma-separated p6m irreps of the kagome 3x3 sector-ED run (empty = skip)")
     ap.add_argument("--batch-steps", type=int, default=300,
@@ -950,6 +952,8 @@ def main():
     ap.add_argument("--proposal-steps", type=int, default=20,
                     help="timed steps of each plain / learned proposal run (0 = skip)")
     args = ap.parse_args()
+    if args.configs is not None:
+        args.workloads = ",".join(n for d, n in (("1", "tfim"), ("3", "j1j2"), ("4", "kagome")) if d in args.configs)
     if args.gram_only:
         return run_gram_only(args)
     if args.impl == "reference":

@@ -4,6 +4,7 @@ and with no device the entry points fail cleanly instead of computing on the
 CPU."""
 import ctypes as C
 import os
+import sys
 import re
 import subprocess
 import tempfile
@@ -73,7 +74,9 @@ int main(void) {
 
 def test_config_layout_matches_upstream_header(tmp_path):
     """nqs_config_t must stay byte-identical to the upstream struct."""
-    up = "/root/reference/include"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import link_upstream_tests as LU
+    up = os.path.join(LU.default_reference(), "include")
     if not os.path.isdir(up):
         pytest.skip("upstream headers not mounted")
     src = tmp_path / "u.c"

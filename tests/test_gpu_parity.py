@@ -1,7 +1,7 @@
 """Parity of the CUDA path (through the C ABI) with the upstream reference
 (golden vectors under tests/golden/) and with the CPU oracle on seeded inputs.
 
-Tolerances (BASELINE parity bar for the plain FP64 path): log-amplitudes and
+Tolerances (the parity bar of the plain FP64 path): log-amplitudes and
 local energies 1e-12 relative (arg compared mod 2 pi; relative to max(|x|, 1));
 parameter updates delta-theta 1e-10 relative in the 2-norm; integer work
 (samples, parities) bit-exact.
@@ -358,7 +358,7 @@ def test_minsr_cholesky_failure_path(nqs):
 
 @pytest.mark.parametrize("Ns,M", [(4096, 32)])
 def test_minsr_full_size_against_oracle(nqs, Ns, M):
-    """BASELINE config-2 shape (4x4 Heisenberg, Marshall, complex RBM M=32,
+    """The 2-D workload's shape (4x4 Heisenberg, Marshall, complex RBM M=32,
     N_s=4096, shift 1e-4): the GPU FP64 update equals the oracle's on the same
     samples."""
     from spin_based_neural_network_gb300 import abi
