@@ -205,6 +205,15 @@ void oracle_lanczos_seed(int N, int alternate, double *out);
 int oracle_lanczos_lean_kagome(int Lx, int Ly, double J, int pbc, const int *perm, const double *chars, int G,
                                int max_iters, double tol, double *out_e, double *out_vec, or_lanczos_info_t *info);
 
+/* The NQS state on the full basis (2^N doubles, N <= 24), src/nqs/nqs_lanczos.c:65-106. */
+int oracle_materialise(const or_amp_t *amp, int N, double *psi);
+/* Open square lattice H x: kind 0 TFIM (X = Gamma), 1 XXZ (X = Jz), src/nqs/nqs_lanczos.c:151-281. */
+void oracle_square_matvec(int kind, int Lx, int Ly, double J, double X, const double *in, double *out);
+/* Variational energy of the materialised state: ham 0 TFIM, 1 XXZ, 6 kagome Heisenberg,
+ * src/nqs/nqs_lanczos.c:188-224, 283-321, 434-455. */
+int oracle_variational_energy(const or_amp_t *amp, int ham, int Lx, int Ly, double J, double X, int pbc,
+                              double *out_e);
+
 #ifdef __cplusplus
 }
 #endif

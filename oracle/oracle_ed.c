@@ -7,6 +7,8 @@
  *   the sector projector (direct form)    src/nqs/nqs_symproj.c:786-852
  *   the memory-lean projecting Lanczos    src/mps/lanczos.c:824-960
  *   and its eigenvector replay            src/mps/lanczos.c:972-1119
+ *   the NQS state on the full basis and its variational energy
+ *                                         src/nqs/nqs_lanczos.c:65-149, 151-321, 434-455
  * The tridiagonal eigenproblem is solved here by Sturm bisection (the lowest value) and
  * a dense cyclic Jacobi sweep (the eigenvector) instead of upstream's QL; both give the
  * lowest pair to rounding.
@@ -251,5 +253,88 @@ int oracle_lanczos_lean_kagome(int Lx, int Ly, double J, int pbc, const int *per
         for (int i = 0; i <= K && i < OR_LZ_MAX + 1; i++) info->beta[i] = be[i];
     }
     free(vc); free(vp); free(w); free(seed); free(al); free(be);
+    return 0;
+}
+
+
+/* psi(s) = cos(arg) exp(log|psi| - max), normalised, over the 2^N basis states (bit i of s
+ * = 1 <-> spin -1), src/nqs/nqs_lanczos.c:65-106. */
+int oracle_materialise(const or_amp_t *amp, int N, double *psi) {
+    if (N <= 0 || N > 24) return -1;
+    long dim = 1L << N;
+    int *spins = malloc(sizeof(int) * (size_t)N);
+    double *lp = malloc(sizeof(double) * (size_t)dim), *ag = malloc(sizeof(double) * (size_t)dim);
+    double mx = -INFINITY;
+    for (long s = 0; s < dim; s++) {
+        for (int i = 0; i < N; i++) spins[i] = ((s >> i) & 1) ? -1 : 1;
+        oracle_log_amp_batch(amp, spins, 1, &lp[s], &ag[s]);
+        if (lp[s] > mx) mx = lp[s];
+    }
+    double n2 = 0.0;
+    for (long s = 0; s < dim; s++) {
+        psi[s] = cos(ag[s]) * exp(lp[s] - mx);
+        n2 += psi[s] * psi[s];
+    }
+    double inv = n2 > 0 ? 1.0 / sqrt(n2) : 1.0;
+    for (long s = 0; s < dim; s++) psi[s] *= inv;
+    free(spins); free(lp); free(ag);
+    return 0;
+}
+
+/* H x on the full basis of an open Lx x Ly square lattice: kind 0 TFIM
+ * -J sum s_i s_j - Gamma sum sigma^x (src/nqs/nqs_lanczos.c:151-184), kind 1 XXZ with
+ * J/4 Jz diagonal and J/2 flips (:226-281). */
+void oracle_square_matvec(int kind, int Lx, int Ly, double J, double X, const double *in, double *out) {
+    int N = Lx * Ly;
+    long dim = 1L << N;
+    for (long s = 0; s < dim; s++) {
+        double e = 0.0;
+        for (int x = 0; x < Lx; x++)
+            for (int y = 0; y < Ly; y++) {
+                int a = x * Ly + y, sa = ((s >> a) & 1) ? -1 : 1;
+                int nb[2], k = 0;
+                if (x + 1 < Lx) nb[k++] = (x + 1) * Ly + y;
+                if (y + 1 < Ly) nb[k++] = x * Ly + y + 1;
+                for (int q = 0; q < k; q++) {
+                    int sb = ((s >> nb[q]) & 1) ? -1 : 1;
+                    e += kind == 0 ? -J * (double)(sa * sb) : 0.25 * X * (double)(sa * sb);
+                }
+            }
+        double y = e * in[s];
+        if (kind == 0) {
+            for (int i = 0; i < N; i++) y += -X * in[s ^ (1L << i)];
+        } else {
+            for (int x = 0; x < Lx; x++)
+                for (int yy = 0; yy < Ly; yy++) {
+                    int a = x * Ly + yy, sa = ((s >> a) & 1) ? -1 : 1;
+                    int nb[2], k = 0;
+                    if (x + 1 < Lx) nb[k++] = (x + 1) * Ly + yy;
+                    if (yy + 1 < Ly) nb[k++] = x * Ly + yy + 1;
+                    for (int q = 0; q < k; q++) {
+                        int sb = ((s >> nb[q]) & 1) ? -1 : 1;
+                        if (sa == -sb) y += 0.5 * J * in[s ^ (1L << a) ^ (1L << nb[q])];
+                    }
+                }
+        }
+        out[s] = y;
+    }
+}
+
+/* <psi|H|psi> / <psi|psi> of the materialised NQS state: ham 0 TFIM (X = Gamma), 1 XXZ
+ * (X = Jz) on the open square lattice, 6 kagome Heisenberg (Lx, Ly cells; X unused, pbc)
+ * (src/nqs/nqs_lanczos.c:188-224, 283-321, 434-455). */
+int oracle_variational_energy(const or_amp_t *amp, int ham, int Lx, int Ly, double J, double X, int pbc,
+                              double *out_e) {
+    int N = ham == 6 ? 3 * Lx * Ly : Lx * Ly;
+    if (N > 24) return -1;
+    long dim = 1L << N;
+    double *psi = malloc(sizeof(double) * (size_t)dim), *hp = malloc(sizeof(double) * (size_t)dim);
+    if (oracle_materialise(amp, N, psi)) { free(psi); free(hp); return -1; }
+    if (ham == 6) oracle_kagome_heis_matvec(Lx, Ly, J, pbc, psi, hp);
+    else oracle_square_matvec(ham == 0 ? 0 : 1, Lx, Ly, J, X, psi, hp);
+    double num = 0.0, den = 0.0;
+    for (long s = 0; s < dim; s++) { num += psi[s] * hp[s]; den += psi[s] * psi[s]; }
+    *out_e = num / den;
+    free(psi); free(hp);
     return 0;
 }

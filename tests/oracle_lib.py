@@ -376,3 +376,19 @@ def ed_iteration_sample(Lx, Ly, perm, chars, x, count):
                                       C.c_long(count))
     t2 = time.perf_counter()
     return t1 - t0, t2 - t1
+
+
+def materialise(amp, N):
+    """The NQS state on the full basis (src/nqs/nqs_lanczos.c:65-106)."""
+    psi = np.zeros(1 << N)
+    assert lib().oracle_materialise(amp.ref(), N, dp(psi)) == 0
+    return psi
+
+
+def variational_energy(amp, ham, Lx, Ly, J, X, pbc=0):
+    """<psi|H|psi>/<psi|psi> of the materialised state: ham 0 TFIM (X = Gamma), 1 XXZ
+    (X = Jz), 6 kagome Heisenberg (src/nqs/nqs_lanczos.c:188-224, 283-321, 434-455)."""
+    e = C.c_double()
+    assert lib().oracle_variational_energy(amp.ref(), ham, Lx, Ly, C.c_double(J), C.c_double(X), pbc,
+                                           C.byref(e)) == 0
+    return e.value

@@ -144,3 +144,18 @@ def test_p3_p6_tables_match_upstream(group, L):
     perm, chars = nqs.kagome_perm(L, L, group)
     assert np.array_equal(perm.astype(np.int32).reshape(-1), g["%s_L%d__perm" % (group, L)])
     assert np.array_equal(chars, g["%s_L%d__chars" % (group, L)])
+
+
+@pytest.mark.parametrize("name", ["tfim_3x3_rbm", "xxz_4x3_crbm", "heis_2x4_rbm", "kagome_2x2_pbc_rbm"])
+def test_oracle_dense_ed_matches_upstream(name):
+    """The oracle's materialised NQS state and variational energies against upstream
+    nqs_materialise_state / nqs_exact_energy_* (tests/golden/dense_ed.npz)."""
+    g = np.load(os.path.join(GOLD, "dense_ed.npz"))
+    d = {k.split("__")[1]: g[k] for k in g.files if k.startswith(name + "__")}
+    N = int(d["N"])
+    amp = O.Amp(int(d["kind"]), N, N, d["params"].copy())
+    e = O.variational_energy(amp, int(d["ham"]), int(d["Lx"]), int(d["Ly"]), float(d["J"]), float(d["X"]),
+                             int(d["pbc"]))
+    assert abs(e - float(d["energy"])) < 1e-12 * max(1.0, abs(float(d["energy"])))
+    if "psi" in d:
+        np.testing.assert_allclose(O.materialise(amp, N), d["psi"], rtol=0, atol=1e-14)
