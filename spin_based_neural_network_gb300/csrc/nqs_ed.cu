@@ -3,7 +3,7 @@
 // The memory-lean projecting Lanczos over the full 2^N basis (N <= 30):
 //   w = H v                     k_heis_matvec   (bond masks, one state per thread)
 //   w -= alpha v + beta v_prev  k_lz_orth       (alpha reduced from the matvec partials)
-//   w = P w                     k_perm_sum x1-2 (sector projector, nibble bit-permute tables)
+//   w = P w                     k_perm_sum x1-4 (sector projector, nibble bit-permute tables)
 //   v_next = w / ||w||          k_lz_scale      (beta reduced from the projector partials)
 // with the host holding only the tridiagonal (alpha, beta) and its lowest Ritz value.
 //
