@@ -232,12 +232,19 @@ int nqs_gpu_tvmc_step_batch(const nqs_config_t *cfg, double dt, int size_x, int 
  * Limits: num_samples <= 1024 and num_params <= 16384; larger sizes are
  * rejected with -1 and a message in nqs_gpu_last_error().  All scratch
  * (the 1024 x 1024 Gram matrix, vectors, status words: about 8.5 MB) is one
- * statically sized device array that every GPU which loads this library keeps
- * until the process exits.  The first call on a device looks up that array's
- * device address (cudaGetSymbolAddress) with the device current; make that
- * first call before any stream capture.  Every call reuses the same array and
- * it keeps the last call's contents, so calls that overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller. */
+ * statically sized device array that every GPU which loads this library's
+ * device code keeps until the process exits.  With CUDA's lazy module loading
+ * (the default) that code, and the array with it, is loaded onto a device the
+ * first time this routine runs there, not when the library is loaded: a caller
+ * that reserves the rest of the device memory for its own pool should make one
+ * warm-up call first (or set CUDA_MODULE_LOADING=EAGER), so the array is
+ * already in place when the pool takes the remainder.  The first call on a
+ * device (and the first after a cudaDeviceReset, which gives the device a new
+ * context and a new copy of the array) looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before
+ * any stream capture.  Every call reuses the same array and it keeps the last
+ * call's contents, so calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
 int nqs_gpu_minsr_solve_noalloc(const double *d_O, const double *d_E,
                                 int num_samples, long num_params, double diag_shift,
                                 double *d_delta, nqs_sr_step_info_t *out_info,

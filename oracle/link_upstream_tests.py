@@ -21,7 +21,16 @@ LIBDIR = os.path.join(ROOT, "spin_based_neural_network_gb300")
 
 
 def default_reference():
-    return os.environ.get("NQS_REFERENCE_SRC", "/root/reference")
+    """Root of the upstream checkout: $NQS_REFERENCE_SRC, else the root that oracle/Makefile
+    recorded when it built oracle/_ref (None when neither is set)."""
+    env = os.environ.get("NQS_REFERENCE_SRC")
+    if env:
+        return env
+    rec = os.path.join(HERE, "_ref", "source_root.txt")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            return f.read().strip() or None
+    return None
 
 
 def check(ref):
@@ -47,4 +56,8 @@ def check(ref):
 
 
 if __name__ == "__main__":
-    print(json.dumps(check(sys.argv[1] if len(sys.argv) > 1 else default_reference()), indent=1))
+    ref = sys.argv[1] if len(sys.argv) > 1 else default_reference()
+    if not ref:
+        raise SystemExit("usage: link_upstream_tests.py <root of the upstream checkout> "
+                         "(or set NQS_REFERENCE_SRC, or build oracle/_ref with make -C oracle REF=...)")
+    print(json.dumps(check(ref), indent=1))

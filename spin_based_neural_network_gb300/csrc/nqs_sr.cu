@@ -11,6 +11,7 @@
 //      panel triangular solve, trailing SYRK update), status word on device
 //   -> forward / backward blocked triangular solves
 //   -> delta = O_c^T y / N_s, theta -= lr delta, ||delta||.
+#include <cuda.h>
 #include <math.h>
 
 #include "nqs_amp.cuh"
@@ -1495,8 +1496,15 @@ __global__ void k_norm2(const double *__restrict__ d, long P, double *scal) {
     if (threadIdx.x == 0) scal[S_NORM2] = red[0];
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device and context.
+// The address belongs to the context that loaded this module: after a
+// cudaDeviceReset the device gets a new primary context (and a new copy of the
+// array), so the cached address is looked up again when the current context's
+// unique id (cuCtxGetId: unique for the life of the process, unlike the handle
+// value, which a re-created primary context may reuse) differs from the one it
+// was taken in.
 static double *g_noalloc_ptr[64];
+static unsigned long long g_noalloc_ctx[64];
 static std::mutex g_noalloc_mu;
 
 static double *noalloc_scratch(int dev) {
@@ -1505,7 +1513,18 @@ static double *noalloc_scratch(int dev) {
         set_error("device ordinal %d out of range", dev);
         return nullptr;
     }
-    if (!g_noalloc_ptr[dev]) {
+    CUcontext cur = nullptr;
+    if (cuCtxGetCurrent(&cur) == CUDA_SUCCESS && !cur) {
+        // no context current on this thread yet: make the device's primary context
+        // current (cudaSetDevice initialises it)
+        if (cudaSetDevice(dev) != cudaSuccess || cuCtxGetCurrent(&cur) != CUDA_SUCCESS) cur = nullptr;
+    }
+    unsigned long long id = 0;
+    if (!cur || cuCtxGetId(cur, &id) != CUDA_SUCCESS) {
+        set_error("nqs_gpu_minsr_solve_noalloc: no current CUDA context on device %d", dev);
+        return nullptr;
+    }
+    if (!g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != id) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -1513,6 +1532,7 @@ static double *noalloc_scratch(int dev) {
             return nullptr;
         }
         g_noalloc_ptr[dev] = (double *)p;
+        g_noalloc_ctx[dev] = id;
     }
     return g_noalloc_ptr[dev];
 }

@@ -408,11 +408,13 @@ def sr_step_minsr(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=No
     return info
 
 
-def sr_step_holomorphic(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None):
-    """nqs_sr_step_holomorphic_full (upstream include/nqs/nqs_optimizer.h:168)."""
+def sr_step_holomorphic(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, grad_fn=None,
+                        grad_user=None):
+    """nqs_sr_step_holomorphic_full (upstream include/nqs/nqs_optimizer.h:168); grad_fn is
+    NULL (the base ansatz's holomorphic gradient) or nqs_symproj_gradient_complex."""
     info = abi.StepInfo()
     _check(lib().nqs_sr_step_holomorphic_full(C.byref(cfg), size_x, size_y, ansatz.h, sampler.h, log_amp_fn, user,
-                                              None, None, C.byref(info)), "nqs_sr_step_holomorphic_full")
+                                              grad_fn, grad_user, C.byref(info)), "nqs_sr_step_holomorphic_full")
     return info
 
 

@@ -17,13 +17,17 @@ import ctypes as C
 import hashlib
 import json
 import os
+import sys
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "libnqs_ref.so")
-REF_SRC = os.environ.get("NQS_REFERENCE_SRC", "/root/reference")
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+from link_upstream_tests import default_reference  # noqa: E402
+
+REF_SRC = default_reference()   # $NQS_REFERENCE_SRC or the checkout oracle/_ref was built from
 IP, DP = C.POINTER(C.c_int), C.POINTER(C.c_double)
 
 

@@ -76,8 +76,9 @@ def test_config_layout_matches_upstream_header(tmp_path):
     """nqs_config_t must stay byte-identical to the upstream struct."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import link_upstream_tests as LU
-    up = os.path.join(LU.default_reference(), "include")
-    if not os.path.isdir(up):
+    ref = LU.default_reference()
+    up = os.path.join(ref, "include") if ref else ""
+    if not ref or not os.path.isdir(up):
         pytest.skip("upstream headers not mounted")
     src = tmp_path / "u.c"
     src.write_text("""

@@ -315,3 +315,84 @@ def test_oracle_vit_matches_upstream(name):
     h = O.ham(int(d["ham"]), int(d["Lx"]), int(d["Ly"]), Gamma=0.8)
     er, ei = O.local_energy(h, amp, d["spins"], complex_out=True)
     assert rel(er, d["eloc_re"]) < 1e-12 and rel(ei, d["eloc_im"]) < 1e-12
+
+
+# ------------------------------------------------------------------ holomorphic SR family
+# Fixtures written by tests/golden/make_holo_golden.py from the upstream library's own
+# nqs_sr_step_holomorphic_full, nqs_sr_step_excited, nqs_tvmc_step_real_time and
+# nqs_tvmc_step_heun (src/nqs/nqs_optimizer.c:415-524, 562-723, 830-993); the batches are
+# the ones the upstream steps drew.  CG is capped at 10 iterations or converged to 1e-13,
+# so the update is held to 1e-10.
+
+HOLO_FIXTURES = ["holo_heis_crbm_marshall", "holo_tfim_crbm_converged", "holo_kagome2x2_p2_symproj"]
+
+
+def holo_problem(d):
+    """Oracle amplitude and Hamiltonian of a holomorphic-family fixture."""
+    wrap = str(d["wrap"])
+    layers = []
+    if wrap == "marshall":
+        layers = [("marshall", int(d["Lx"]), int(d["Ly"]))]
+    elif wrap == "symproj":
+        layers = [("symproj", d["perm"], d["chars"])]
+    amp = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params0"].copy(), layers)
+    h = O.ham(int(d["ham"]), int(d["Lx"]), int(d["Ly"]), 0, int(d["kagome_pbc"]), float(d["J"]), float(d["J2"]),
+              float(d["Jz"]), float(d["Gamma"]))
+    return amp, h
+
+
+def check_step(info, d, amp, tol=1e-10):
+    ref = d["info"]
+    assert info.mean_energy == pytest.approx(ref[0], rel=1e-12)
+    assert info.variance_energy == pytest.approx(ref[1], rel=1e-9)
+    assert info.update_norm == pytest.approx(ref[2], rel=tol)
+    assert info.cg_iterations == int(ref[4]) and info.converged == int(ref[5])
+    step = d["params1"] - d["params0"]
+    assert np.linalg.norm((amp.params - d["params0"]) - step) <= tol * np.linalg.norm(step)
+
+
+@pytest.mark.parametrize("name", HOLO_FIXTURES)
+def test_holomorphic_step_against_upstream(name):
+    d = load(name)
+    amp, h = holo_problem(d)
+    args = (h, amp, d["batch"], float(d["shift"]), float(d["lr"]), int(d["cg_max"]), float(d["cg_tol"]))
+    E, delta, info = O.holo_step_sym(*args) if int(d["sym_grad"]) else O.holo_step(*args)
+    check_step(info, d, amp)
+
+
+@pytest.mark.parametrize("name", ["excited_tfim_crbm", "excited_tfim_crbm_converged"])
+def test_excited_step_against_upstream(name):
+    d = load(name)
+    amp, h = holo_problem(d)
+    ref = O.Amp(int(d["kind"]), int(d["N"]), int(d["M"]), d["params_ref"].copy())
+    E, delta, info = O.excited_step(h, amp, ref, float(d["mu"]), d["batch"], float(d["shift"]), float(d["lr"]),
+                                    int(d["cg_max"]), float(d["cg_tol"]))
+    check_step(info, d, amp)
+
+
+def test_tvmc_euler_against_upstream():
+    d = load("tvmc_euler_tfim_crbm")
+    amp, h = holo_problem(d)
+    E, delta, info = O.tvmc_step(h, amp, d["batch"], float(d["shift"]), float(d["dt"]), int(d["cg_max"]),
+                                 float(d["cg_tol"]))
+    check_step(info, d, amp)
+
+
+def test_tvmc_heun_against_upstream():
+    """Heun = two Euler forces (k1 on the first batch at theta, k2 on the second batch at the
+    probe theta + dt k1), theta + dt (k1 + k2) / 2."""
+    d = load("tvmc_heun_tfim_crbm")
+    amp, h = holo_problem(d)
+    dt = float(d["dt"])
+    shift, cmax, ctol = float(d["shift"]), int(d["cg_max"]), float(d["cg_tol"])
+    E1, k1, i1 = O.tvmc_step(h, amp, d["batch"], shift, dt, cmax, ctol)
+    probe = amp.params.copy()
+    assert np.linalg.norm(probe - d["params_probe"]) <= 1e-12 * np.linalg.norm(d["params_probe"])
+    E2, k2, i2 = O.tvmc_step(h, amp, d["batch2"], shift, dt, cmax, ctol)
+    final = d["params0"] + dt * (0.5 * (k1 + k2))
+    step = d["params1"] - d["params0"]
+    assert np.linalg.norm((final - d["params0"]) - step) <= 1e-10 * np.linalg.norm(step)
+    ref = d["info"]
+    assert i1.mean_energy == pytest.approx(ref[0], rel=1e-12)
+    assert i1.cg_iterations + i2.cg_iterations == int(ref[4])
+    assert np.linalg.norm(0.5 * (k1 + k2)) * dt == pytest.approx(ref[2], rel=1e-10)

@@ -20,7 +20,7 @@ LINKING = ["test_nqs", "test_nqs_complex_rbm", "test_nqs_convergence", "test_nqs
 def test_upstream_nqs_tests_link_against_the_drop_in():
     import link_upstream_tests as LU
     ref = LU.default_reference()
-    if not os.path.isdir(os.path.join(ref, "tests")):
+    if not ref or not os.path.isdir(os.path.join(ref, "tests")):
         pytest.skip("upstream sources not present")
     if not os.path.exists(os.path.join(LU.LIBDIR, "libnqs_gb300.so")):
         pytest.skip("library not built")
