@@ -186,24 +186,91 @@ class Clocks:
 # ------------------------------------------------------------------ CPU legs
 
 def cpu_step(task):
-    """One upstream MinSR step on the host: the upstream single-chain xorshift
-    sampler followed by nqs_sr_step_minsr_full's algorithm, through the
-    upstream library when it is loadable here, else the oracle restatement."""
+    """One MinSR step of the headline workload on one host core, by the oracle
+    restatement of the upstream algorithm (upstream loop order, FP64): the same
+    1024 Philox chains with exchange moves in Sz = 0 and 16 moves between samples as
+    the GPU arm (the oracle's chains are bit-exact with the GPU's; thermalisation is
+    outside the timed step, as in the GPU arm), then nqs_sr_step_minsr_full's
+    estimator, Gram, Cholesky and update.  Returns the step's seconds."""
     kind, seed = task
-    import numpy as np
     import oracle_lib as O
     P = O.num_params(O.OR_CRBM, N_SITES, M_HIDDEN)
     params = init_params(P, seed)
     amp = O.Amp(O.OR_CRBM, N_SITES, M_HIDDEN, params, [("marshall", LX, LY)])
     h = O.ham(O.OR_HEIS, LX, LY, pbc=1)
     t0 = time.perf_counter()
-    batch, _ = O.xorshift_sampler(amp, seed, THERM, DECOR, NS)
+    batch, _, _, _ = O.chain_sampler(amp, h, seed, CHAINS, 1, N_SITES // 2, 0, NS // CHAINS, DECOR)
     O.minsr_step(h, amp, batch, SHIFT, LR)
     return time.perf_counter() - t0
 
 
+def cpu_minsr_sample(h, make_amp, sample, n0, ns_full, shift, lr, what):
+    """Single-core time of one MinSR step of a workload too large to run whole on the
+    host within the bench, from a bounded sample: the oracle (upstream loop order, FP64)
+    draws n0 samples with the workload's chains and moves, evaluates the local energies
+    and the Jacobian, and runs the MinSR step at N_s = n0; the step is extrapolated to
+    N_s = ns_full with sampling, local energies and Jacobian linear in N_s and the solve
+    split between the Gram (N_s^2 N_p) and the Cholesky (N_s^3 / 3) by their FLOP shares
+    at n0."""
+    import oracle_lib as O
+    t0 = time.perf_counter()
+    batch = sample(n0)
+    t_samp = time.perf_counter() - t0
+    amp = make_amp()
+    t0 = time.perf_counter()
+    O.local_energy(h, amp, batch)
+    O.gradient(amp, batch)
+    t_lin = time.perf_counter() - t0
+    amp = make_amp()
+    t0 = time.perf_counter()
+    O.minsr_step(h, amp, batch, shift, lr)
+    t_step = time.perf_counter() - t0
+    P = len(amp.params)
+    t_solve = max(t_step - t_lin, 0.0)
+    gram0, chol0 = float(n0) * n0 * P, n0 ** 3 / 3.0
+    r = ns_full / float(n0)
+    t_full = (t_samp + t_lin) * r + t_solve * (gram0 * r * r + chol0 * r ** 3) / (gram0 + chol0)
+    return {"value": 1.0 / t_full, "unit": "steps/s", "cores": 1, "kind": "port", "s_per_step": t_full,
+            "sample": "%s: the oracle's MinSR step at N_s = %d on one host core (%.2f s: sampling %.2f, "
+                      "local energies + Jacobian %.2f), extrapolated to N_s = %d (linear parts x N_s, "
+                      "Gram x N_s^2, Cholesky x N_s^3)" % (what, n0, t_samp + t_step, t_samp, t_lin, ns_full)}
+
+
+def headline_config(ws):
+    """The workload both arms run (the reference arm prints the same dict)."""
+    return {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES, "hidden": M_HIDDEN,
+            "num_params": 2 * (N_SITES + M_HIDDEN + N_SITES * M_HIDDEN), "num_samples": NS, "chains": CHAINS,
+            "decorrelate": DECOR, "moves": "nn-exchange, Sz=0", "shift": SHIFT, "lr": LR,
+            "l2": "working set > L2 every step (O 37 MB FP64 + split 37 MB + Gram 67 MB FP32 + factor; "
+                  "FP64 path: Gram 134 MB)",
+            "parallelism": "replicas x%d" % ws}
+
+
 def reference_kind():
+    """The CPU arm runs the oracle restatement ("port"): the upstream library compiled from
+    its sources (oracle/_ref) exists only where the upstream checkout is mounted, which the
+    GPU hosts do not have; the oracle follows the upstream loop order and is pinned to the
+    upstream library's outputs (tests/test_oracle_pin.py)."""
     return "port"
+
+
+def host_cpu():
+    """CPU model and logical core count of this host."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                    model = v.strip()
+                    if k.strip() == "model name":
+                        break
+    except OSError:
+        pass
+    if model is None:
+        import platform
+        model = platform.processor() or platform.machine()
+    return {"cpu_model": model, "nproc": os.cpu_count() or 1}
 
 
 def run_reference(args):
@@ -214,28 +281,32 @@ def run_reference(args):
     import oracle_lib
     oracle_lib.build_oracle()
     cores = os.cpu_count() or 1
-    # a bounded sample: one MinSR step takes ~13 s on one Grace core, so at
-    # most two steps per host core are timed whatever --steps asks for
-    steps = max(1, min(args.steps, 2 * cores, 32))
-    workers = max(1, min(cores, steps))
+    # a bounded sample: one MinSR step takes ~13 s on one Grace core.  The steps are a
+    # whole number of waves over the workers (every worker runs the same number of
+    # steps, so no core idles in a partial last wave): one wave, or two when --steps
+    # asks for at least two per core.
+    workers = max(1, min(cores, args.steps))
+    waves = 2 if args.steps >= 2 * workers else 1
+    steps = waves * workers
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
         if args.warmup > 0:
-            pool.map(cpu_step, [("port", SEED + i) for i in range(min(args.warmup, workers))])
+            pool.map(cpu_step, [("port", SEED + i) for i in range(workers)])
         t0 = time.perf_counter()
-        pool.map(cpu_step, [("port", SEED + 100 + i) for i in range(steps)])
+        per = pool.map(cpu_step, [("port", SEED + 100 + i) for i in range(steps)])
         wall = time.perf_counter() - t0
     value = steps / wall
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * wall / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES,
-                       "hidden": M_HIDDEN, "num_samples": NS, "num_params": 1120, "shift": SHIFT, "lr": LR},
-            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": workers, "kind": reference_kind(),
-                             "sample": "%d independent MinSR steps (N_s=4096, N_p=1120, FP64, upstream "
-                                       "single-chain sampler) run concurrently on %d host processes"
-                                       % (steps, workers)},
+            "config": headline_config(args.gpus),
+            "method": {"precision": "fp64", "solve_space": "samples (upstream order)"},
+            "cpu_baseline": dict({"value": value, "unit": "steps/s", "cores": workers, "kind": reference_kind(),
+                                  "sample": "%d independent MinSR steps of the workload (N_s=4096, N_p=1120, "
+                                            "FP64, the same chains and moves) in %d wave(s) over %d host "
+                                            "processes" % (steps, waves, workers),
+                                  "one_step_s_mean": statistics.mean(per)}, **host_cpu()),
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -400,7 +471,33 @@ def batch_objects(nqs, abi, spec, lr=0.02, shift=1e-3):
             "Lx": Lx, "Ly": Ly, "spec": spec}
 
 
-def multi_instance(nqs, abi, L, base_opts, timed, total, learned=False):
+def multi_cpu_baseline(specs, n0=256):
+    """Single-core time of one step of every instance of the multi-instance workload: each
+    instance's MinSR step at N_s = n0 by the oracle (its chains and moves, real RBM with the
+    library's initialisation scale), extrapolated to its own N_s (cpu_minsr_sample), summed."""
+    import oracle_lib as O
+    total, measured = 0.0, 0.0
+    for sp in specs:
+        xxz = sp["kind"] == "xxz"
+        N, M = sp["N"], sp["alpha"] * sp["N"]
+        h = O.ham(O.OR_XXZ if xxz else O.OR_TFIM, sp["Lx"], sp["Ly"], pbc=1, Jz=sp["delta"], Gamma=sp["h"])
+        p0 = O.init_params(O.OR_RBM, N, M, 0.1, sp["seed"] & 0x7FFFFFFF)
+        layers = [("marshall", sp["Lx"], sp["Ly"])] if xxz else []
+        mk = lambda p0=p0, layers=layers, N=N, M=M: O.Amp(O.OR_RBM, N, M, p0.copy(), layers)
+        smp = lambda n, mk=mk, h=h, xxz=xxz, N=N, seed=sp["seed"]: O.chain_sampler(
+            mk(), h, seed, n // 4, 1 if xxz else 0, N // 2 if xxz else -1, 0, 4, N)[0]
+        n = min(n0, sp["Ns"])
+        t0 = time.perf_counter()
+        r = cpu_minsr_sample(h, mk, smp, n, sp["Ns"], 1e-3, 0.02, "")
+        measured += time.perf_counter() - t0
+        total += r["s_per_step"]
+    return {"value": len(specs) / total, "unit": "instance-steps/s", "cores": 1, "kind": "port",
+            "s_per_batch_step": total, "measured_s": measured,
+            "sample": "every instance's MinSR step by the oracle at N_s = %d on one host core, extrapolated to "
+                      "its own N_s (linear parts x N_s, Gram x N_s^2, Cholesky x N_s^3) and summed" % n0}
+
+
+def multi_instance(nqs, abi, L, base_opts, timed, total, learned=False, cpu=False):
     """The 64-instance workload stepped as one batch (nqs_gpu_batch_step): one
     cooperative launch for all solves with an autotuned CTA split, the whole
     batch step replayed as a CUDA graph from the second step.  Throughput over
@@ -450,6 +547,9 @@ def multi_instance(nqs, abi, L, base_opts, timed, total, learned=False):
            "within_1e-2": int(np.sum(ev <= 1e-2)), "within_1e-3": int(np.sum(ev <= 1e-3)),
            "converged_last_step": int(sum(i.converged for i in infos)) if infos else None,
            "fp64_fallback_instance_steps": bt.fallbacks(), "learned_proposals": learned}
+    if cpu:
+        out["cpu_baseline"] = multi_cpu_baseline(specs)
+        out["speedup_vs_cpu_core"] = out["cpu_baseline"]["s_per_batch_step"] / (ms / 1000.0)
     if lps:
         sts = [lp.stats() for lp in lps]
         out["learned_acceptance_mean"] = float(np.mean([s.accepted / max(s.proposals, 1.0) for s in sts]))
@@ -487,7 +587,7 @@ def step_kernels(nqs, step, top=8):
     return {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:top]}
 
 
-def other_workloads(nqs, abi, L, base_opts, which):
+def other_workloads(nqs, abi, L, base_opts, which, cpu=True):
     """The other workloads of the measurement table, each on its own shapes
     (seeded synthetic parameters, configurations from the sampler):
       tfim   1-D TFIM N = 16 PBC, h = 1, real RBM alpha = 1 (N_p = 288), 16 chains x 64 = 1024
@@ -534,6 +634,20 @@ def other_workloads(nqs, abi, L, base_opts, which):
                                         "cg_iterations_last": info.cg_iterations, "kernels_ms_one_step": k1,
                                         "energy_per_site_last20": run, "e0_per_site": e0,
                                         "abs_err_per_site": abs(run - e0)}
+        if cpu:
+            import oracle_lib as O
+            h1 = O.ham(O.OR_TFIM, N, 1, pbc=1, Gamma=1.0)
+            amp1 = O.Amp(O.OR_RBM, N, N, init_params(a.P, SEED + 11))
+            t0 = time.perf_counter()
+            for k in range(5):
+                b1, _, _, _ = O.chain_sampler(amp1, h1, SEED + k, 16, 0, -1, 0, 64, N)
+                O.cgsr_step(h1, amp1, b1, 1e-3, 0.01, 100, 1e-6)
+            t1 = (time.perf_counter() - t0) / 5
+            out["tfim_chain16_rbm_cgsr_fp64"]["cpu_baseline"] = {
+                "value": 1.0 / t1, "unit": "steps/s", "cores": 1, "kind": "port", "s_per_step": t1,
+                "sample": "5 whole steps of the workload by the oracle on one host core (16 chains x 64 "
+                          "samples, single flips, CG-SR at most 100 iterations)"}
+            out["tfim_chain16_rbm_cgsr_fp64"]["speedup_vs_cpu_core"] = t1 / (ms / 1000.0)
     if "j1j2" in which:
         nqs.set_options(**base_opts)
         Lx = Ly = 6
@@ -566,6 +680,15 @@ def other_workloads(nqs, abi, L, base_opts, which):
             "cg_residual": st.refine_residual, "cg_iterations": st.refine_sweeps,
             "factor_solve_phases_us": [round(x, 1) for x in ph], "kernels_ms_one_step": k3,
             "plain_fp64_steps_per_s": 1000.0 / ms64, "speedup_vs_fp64": ms64 / ms}
+        if cpu:
+            import oracle_lib as O
+            h3 = O.ham(O.OR_J1J2, Lx, Ly, pbc=1, J2=0.5)
+            p3 = a.params.copy()
+            mk3 = lambda: O.Amp(O.OR_CRBM, N, M, p3.copy())
+            smp3 = lambda n: O.chain_sampler(mk3(), h3, SEED + 33, n // 8, 1, N // 2, 0, 8, N)[0]
+            cb = cpu_minsr_sample(h3, mk3, smp3, 512, 8192, 1e-4, 0.005, "J1-J2 6x6 cRBM alpha=4")
+            out["j1j2_6x6_crbm_alpha4_ns8192_minsr"]["cpu_baseline"] = cb
+            out["j1j2_6x6_crbm_alpha4_ns8192_minsr"]["speedup_vs_cpu_core"] = cb["s_per_step"] / (ms / 1000.0)
     if "kagome" in which:
         nqs.set_options(**base_opts)
         N, W = 27, 108
@@ -618,6 +741,15 @@ def other_workloads(nqs, abi, L, base_opts, which):
             "e0_per_site_recorded_upstream": e0, "factor_solve_phases_us": [round(x, 1) for x in ph],
             "kernels_ms_one_step": k4, "plain_vs_learned_proposal": proposals4,
             "estimator": "FP32 MLP (k_local_mlp32)", "sampler": "FP32 MLP chains (k_sample_mlp32)"}
+        if cpu:
+            import oracle_lib as O
+            h4 = O.ham(O.OR_KAGOME, 3, 3, kagome_pbc=1)
+            p4 = a.params.copy()
+            mk4 = lambda: O.Amp(O.OR_MLP, N, W, p4.copy())
+            smp4 = lambda n: O.chain_sampler(mk4(), h4, SEED + 44, n // 8, 1, 13, 0, 8, N)[0]
+            cb = cpu_minsr_sample(h4, mk4, smp4, 512, 16384, 1e-3, 0.005, "kagome 3x3 MLP 27-108-108")
+            out["kagome3x3_mlp108_ns16384_minsr"]["cpu_baseline"] = cb
+            out["kagome3x3_mlp108_ns16384_minsr"]["speedup_vs_cpu_core"] = cb["s_per_step"] / (ms / 1000.0)
     nqs.set_options(**base_opts)
     return out
 
@@ -709,7 +841,7 @@ def run_gpu(args):
     prec = abi.PREC_FP64 if args.precision == "fp64" else abi.PREC_MIXED
     mixed = prec == abi.PREC_MIXED
     base_opts = dict(square_pbc=1, precision=prec, refine_sweeps=SWEEPS, gram_passes=3,
-                     fp32_estimator=1 if mixed else 0)
+                     fp32_estimator=1 if mixed else 0, fp64_space=abi.SPACE_SMALLER)
     nqs.set_options(**base_opts)
     cfg = workload_cfg(abi)
     a = nqs.Ansatz(cfg, N_SITES)
@@ -816,31 +948,54 @@ def run_gpu(args):
                      "reference": "FP64 estimator + FP64 MinSR (sample space) on the same samples"}
         nqs.set_options(**base_opts)
 
-    # the plain FP64 path on the same state, for the mixed / plain ratio
+    # the plain FP64 path on the same state (FP64 estimator, Jacobian, Gram, Cholesky;
+    # the sampler keeps its chains), for the mixed / plain ratios: the parameter-space
+    # solve (push-through identity, 1120 x 1120) and the upstream-order sample-space
+    # solve (4096 x 4096); steps/s and ESS/s (ESS of each batch over the step time)
     plain = None
     if prec == abi.PREC_MIXED and not args.no_plain:
-        nqs.set_options(**dict(base_opts, precision=abi.PREC_FP64))
-        step()
-        k_plain = max(2, args.steps // 4)
-        p0 = L.nqs_gpu_event_record()
-        for _ in range(k_plain):
+        plain = {}
+        for key, space in (("parameter_space", abi.SPACE_PARAMETERS), ("sample_space", abi.SPACE_SAMPLES)):
+            nqs.set_options(**dict(base_opts, precision=abi.PREC_FP64, fp32_estimator=0, fp64_space=space))
             step()
-        p1 = L.nqs_gpu_event_record()
-        pms = L.nqs_gpu_event_elapsed_ms(p0, p1)
-        L.nqs_gpu_event_destroy(p0)
-        L.nqs_gpu_event_destroy(p1)
-        plain = {"value": k_plain / (pms / 1000.0), "unit": "steps/s", "steps": k_plain}
+            k_plain = max(2, args.steps // 4) if space == abi.SPACE_PARAMETERS else max(2, args.steps // 10)
+            ess = []
+            p0 = L.nqs_gpu_event_record()
+            for _ in range(k_plain):
+                step()
+                ess.append(nqs.last_step_stats().ess)
+            p1 = L.nqs_gpu_event_record()
+            pms = L.nqs_gpu_event_elapsed_ms(p0, p1)
+            L.nqs_gpu_event_destroy(p0)
+            L.nqs_gpu_event_destroy(p1)
+            plain[key] = {"value": k_plain / (pms / 1000.0), "unit": "steps/s", "steps": k_plain,
+                          "ess_per_step": float(np.mean(ess)),
+                          "ess_per_s": float(np.mean(ess)) * k_plain / (pms / 1000.0)}
+        plain.update(plain["parameter_space"])
+        plain["note"] = ("value/ess_per_s: the parameter-space FP64 solve; sample_space: the upstream-order "
+                         "4096 x 4096 solve")
         nqs.set_options(**base_opts)
 
     proposals = None
     if prec == abi.PREC_MIXED and args.proposal_steps > 0:
         proposals = [proposal_run(nqs, abi, L, base_opts, d, lr, 30, args.proposal_steps)
                      for d in (DECOR, 2) for lr in (False, True)]
+        # the plain FP64 path (FP64 chains and estimator, local moves only) on the same runs
+        fp64_opts = dict(base_opts, precision=abi.PREC_FP64, fp32_estimator=0)
+        plain64 = {d: proposal_run(nqs, abi, L, fp64_opts, d, False, 10, max(4, args.proposal_steps // 4))
+                   for d in (DECOR, 2)}
+        for d, r in plain64.items():
+            r["precision"] = "fp64"
+            proposals.append(r)
+            for q in proposals:
+                if q.get("decorrelate") == d and q.get("learned") and "precision" not in q:
+                    q["ess_per_s_vs_plain_fp64"] = q["ess_per_s"] / r["ess_per_s"]
         nqs.set_options(**base_opts)
 
     others = None
     if prec == abi.PREC_MIXED and args.workloads:
-        others = other_workloads(nqs, abi, L, base_opts, args.workloads.split(","))
+        others = other_workloads(nqs, abi, L, base_opts, args.workloads.split(","),
+                                 cpu=rank == 0 and not args.no_cpu_baseline)
 
     ed = None
     if prec == abi.PREC_MIXED and args.ed:
@@ -848,7 +1003,8 @@ def run_gpu(args):
 
     multi = multi_learned = None
     if prec == abi.PREC_MIXED and args.batch_steps > 0:
-        multi = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps)
+        multi = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps,
+                               cpu=rank == 0 and not args.no_cpu_baseline)
         multi_learned = multi_instance(nqs, abi, L, base_opts, 20, args.batch_steps, learned=True)
 
     conv = None
@@ -866,14 +1022,9 @@ def run_gpu(args):
             "mixed: fp32 sampling/E_loc/O (product-form ratios), f64 centring and energy sums, "
             "tf32x3 tensor-core gram (fp32 accumulate), fp32 factor + inverse, f64 refinement",
             "data": "synthetic (sampled configurations; parameters N(0,0.01^2) from a seed)",
-            "config": {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES,
-                       "hidden": M_HIDDEN, "num_params": P, "num_samples": NS, "chains": CHAINS,
-                       "decorrelate": DECOR, "moves": "nn-exchange, Sz=0", "shift": SHIFT, "lr": LR,
-                       "precision": args.precision,
-                       "l2": "working set > L2 every step (O 37 MB FP64 + split 37 MB + Gram 67 MB FP32 "
-                             "+ factor; FP64 path: Gram 134 MB)",
-                       "refine_sweeps": SWEEPS, "solve_space": "parameters (N_p < N_s)" if mixed else "samples",
-                       "parallelism": "replicas x%d" % ws},
+            "config": headline_config(ws),
+            "method": {"precision": args.precision, "refine_sweeps": SWEEPS,
+                       "solve_space": "parameters (N_p < N_s)"},
             "gpu_launches": launches,
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * P,
                     "d2h_bytes_per_step": 8 * P + 16 * 8},

@@ -28,6 +28,7 @@ extern "C" {
 #define NQS_GPU_SPACE_AUTO       0
 #define NQS_GPU_SPACE_SAMPLES    1
 #define NQS_GPU_SPACE_PARAMETERS 2
+#define NQS_GPU_SPACE_SMALLER    3   /* fp64_space: whichever system is smaller */
 
 typedef enum {
     NQS_GPU_RNG_XORSHIFT_COMPAT = 0,  /* upstream single chain, same sequence */
@@ -65,7 +66,15 @@ typedef struct {
                           * Metropolis acceptance in FP32 (product form of the
                           * amplitude ratios); with mixed_check the FP64
                           * estimator is rerun on the same samples */
-    int reserved[2];
+    int fp64_space;      /* FP64 MinSR: system solved.  0 or NQS_GPU_SPACE_SAMPLES = the
+                          * N_s x N_s sample-space system in the upstream order (the
+                          * parity default); NQS_GPU_SPACE_PARAMETERS = the N_p x N_p
+                          * parameter-space system (O_c^T O_c / N_s + shift I) delta =
+                          * O_c^T eps / N_s, the same delta by the push-through identity;
+                          * NQS_GPU_SPACE_SMALLER = parameters when N_p < N_s.  A failed
+                          * parameter-space factorisation is retried once with the shift
+                          * raised by 1e-6, then delta = 0 and converged = 0 */
+    int reserved[1];
 } nqs_gpu_options_t;
 
 /* Defaults: compat sampler, single flips, open lattices, FP64. */

@@ -124,6 +124,7 @@ PREC_MIXED = 1               # tensor-core Gram + FP64 iterative refinement
 SPACE_AUTO = 0               # mixed MinSR: solve the smaller of the two systems
 SPACE_SAMPLES = 1            # N_s x N_s (O O^T)
 SPACE_PARAMETERS = 2         # N_p x N_p (O^T O)
+SPACE_SMALLER = 3            # fp64_space: whichever system is smaller
 
 
 class GpuOptions(C.Structure):
@@ -143,7 +144,8 @@ class GpuOptions(C.Structure):
         ("lattice_kagome", C.c_int),
         ("mixed_check", C.c_int),
         ("fp32_estimator", C.c_int),
-        ("reserved", C.c_int * 2),
+        ("fp64_space", C.c_int),
+        ("reserved", C.c_int * 1),
     ]
 
 

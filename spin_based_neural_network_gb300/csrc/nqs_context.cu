@@ -180,7 +180,7 @@ int nqs_gpu_set_options(const nqs_gpu_options_t *o) {
         (o->move == NQS_GPU_MOVE_EXCHANGE && o->rng != NQS_GPU_RNG_PHILOX) ||
         (o->precision != NQS_GPU_PREC_FP64 && o->precision != NQS_GPU_PREC_MIXED) || o->refine_sweeps < 0 ||
         (o->gram_passes != 1 && o->gram_passes != 3) || o->mixed_space < NQS_GPU_SPACE_AUTO ||
-        o->mixed_space > NQS_GPU_SPACE_PARAMETERS) {
+        o->mixed_space > NQS_GPU_SPACE_PARAMETERS || o->fp64_space < 0 || o->fp64_space > NQS_GPU_SPACE_SMALLER) {
         set_error("invalid nqs_gpu_options_t");
         return -1;
     }

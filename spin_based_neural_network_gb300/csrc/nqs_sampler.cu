@@ -29,6 +29,7 @@ struct Sampler {
     void *user = nullptr;
     uint64_t move_counter = 0;
     DevBuf<uint64_t> d_bits, d_rng, d_samples;
+    DevBuf<double> d_cla;                 // compat chain: upstream's cached log|psi|
     DevBuf<unsigned long long> d_counts;
     DevBuf<int> d_bonds, d_spins;
     int nb = 0;
@@ -51,6 +52,7 @@ struct SampleArgs {
     const int *bonds;
     int nb;
     unsigned long long *counts;
+    double *cla;                     // compat chain: log|psi| the upstream sampler has cached (NaN: none yet)
 };
 
 __device__ __forceinline__ uint64_t xs_next(uint64_t &s) {   // src/nqs/nqs_sampler.c:31-38
@@ -63,13 +65,25 @@ __device__ __forceinline__ uint64_t xs_next(uint64_t &s) {   // src/nqs/nqs_samp
 }
 
 // Shared proposal driver.  `delta(u, v, accept_fn)` evaluates the proposal.
+// la0 = log|psi| of the chain's configuration at the current parameters.  The compat
+// chain reproduces the upstream sampler's cache (src/nqs/nqs_sampler.c:74-75, 109-113):
+// upstream compares every proposal with the log|psi| stored when the current
+// configuration was accepted, which after a parameter update is the value at the old
+// parameters until the next accepted move.  off = la0 - cached carries that difference
+// into the acceptance until the first accept of the launch (off = 0 exactly when the
+// parameters did not change); the cache is written back at the end.
 template <int RNG, int MOVE, typename Eval, typename Commit>
 __device__ __forceinline__ void run_chain(const SampleArgs &S, int c, uint64_t &s, Eval eval,
                                           Commit commit, unsigned long long &acc,
-                                          unsigned long long &pro) {
+                                          unsigned long long &pro, double la0 = 0.0) {
     const int lane = threadIdx.x & 31;
     uint64_t st = RNG == NQS_GPU_RNG_XORSHIFT_COMPAT ? S.rng[c] : 0;
     const int per = S.decor > 0 ? S.decor : 1;
+    const bool cached = RNG == NQS_GPU_RNG_XORSHIFT_COMPAT && S.cla != nullptr;
+    double cache0 = cached ? S.cla[c] : 0.0;
+    if (cached && isnan(cache0)) cache0 = la0;
+    double off = cached ? la0 - cache0 : 0.0, cur = la0;
+    bool moved = false;
     for (int t = 0; t < S.total; t++) {
         int u, v = -1;
         uint4 r = make_uint4(0, 0, 0, 0);
@@ -90,7 +104,8 @@ __device__ __forceinline__ void run_chain(const SampleArgs &S, int c, uint64_t &
         pro++;
         bool parallel = v >= 0 && (((s >> u) ^ (s >> v)) & 1ull) == 0;
         if (!parallel) {
-            double lr = 2.0 * eval(u, v);
+            const double d = eval(u, v);
+            double lr = 2.0 * (d + off);
             bool accept;
             if (lr >= 0.0) {
                 accept = true;
@@ -109,6 +124,9 @@ __device__ __forceinline__ void run_chain(const SampleArgs &S, int c, uint64_t &
                 commit(u, v);
                 s ^= 1ull << u;
                 if (v >= 0) s ^= 1ull << v;
+                cur += d;
+                off = 0.0;
+                moved = true;
             }
         }
         if (t >= S.skip && ((t - S.skip + 1) % per) == 0) {
@@ -117,6 +135,7 @@ __device__ __forceinline__ void run_chain(const SampleArgs &S, int c, uint64_t &
         }
     }
     if (RNG == NQS_GPU_RNG_XORSHIFT_COMPAT && lane == 0) S.rng[c] = st;
+    if (cached && lane == 0) S.cla[c] = moved ? cur : cache0;
 }
 
 constexpr int kSW = 4;   // warps (chains) per block
@@ -174,8 +193,16 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm(SampleArgs S, DevAmp A)
             lr[j] = nl[j];
         }
     };
+    double la0 = 0.0;
+    if (RNG == NQS_GPU_RNG_XORSHIFT_COMPAT) {
+        // log|psi| of the start configuration (Re of the visible term + hidden log-cosh)
+#pragma unroll
+        for (int j = 0; j < J; j++) la0 += lr[j];
+        for (int i = lane; i < a.N; i += 32) la0 += aR[i] * (double)spin_of(s, i);
+        la0 = warp_sum(la0);
+    }
     unsigned long long acc = 0, pro = 0;
-    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro);
+    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro, la0);
     if (lane == 0) {
         S.bits[c] = s;
         atomicAdd(&S.counts[0], acc);
@@ -429,7 +456,7 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_generic(SampleArgs S, DevAm
     };
     auto commit = [&](int, int) { la = nla; };
     unsigned long long acc = 0, pro = 0;
-    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro);
+    run_chain<RNG, MOVE>(S, c, s, eval, commit, acc, pro, la);
     if (lane == 0) {
         S.bits[c] = s;
         atomicAdd(&S.counts[0], acc);
@@ -678,6 +705,7 @@ bool sampler_run(Sampler *sm, int skip, int n_out, uint64_t *out, unsigned long 
     S.N = sm->N;
     S.bits = sm->d_bits.p;
     S.rng = sm->d_rng.p;
+    S.cla = sm->opts.rng == NQS_GPU_RNG_XORSHIFT_COMPAT ? sm->d_cla.p : nullptr;
     S.seed = sm->cfg.rng_seed;
     S.move0 = sm->move_counter;
     S.move_dev = move_dev;
@@ -839,6 +867,12 @@ nqs_sampler_t *nqs_sampler_create_gpu(int num_sites, const nqs_config_t *cfg,
         uint64_t h[2] = {bits, rng};
         NQS_CUDA(cudaMemcpyAsync(s->d_bits.p, &h[0], 8, cudaMemcpyHostToDevice, st));
         NQS_CUDA(cudaMemcpyAsync(s->d_rng.p, &h[1], 8, cudaMemcpyHostToDevice, st));
+        // the cache starts empty (NaN): the first launch stores log|psi| of the start
+        // configuration at the parameters it sees, as upstream does at creation
+        if (!s->d_cla.ensure(1) || !NQS_CUDA(cudaMemsetAsync(s->d_cla.p, 0xff, sizeof(double), st))) {
+            delete s;
+            return nullptr;
+        }
     } else {
         NQS_LAUNCH("chain_init");
         k_chain_init<<<(s->C + 127) / 128, 128, 0, st>>>(s->C, num_sites, cfg->rng_seed,

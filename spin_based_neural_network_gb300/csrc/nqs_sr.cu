@@ -11,6 +11,7 @@
 //      panel triangular solve, trailing SYRK update), status word on device
 //   -> forward / backward blocked triangular solves
 //   -> delta = O_c^T y / N_s, theta -= lr delta, ||delta||.
+#include <algorithm>
 #include <cuda.h>
 #include <math.h>
 
@@ -833,6 +834,138 @@ int minsr_fp64_solve(const double *O, const double *eps, int Ns, long P, double 
     return 0;
 }
 
+// ---------------------------------------------------------------- FP64 parameter-space solve
+// Column Gram of the centred Jacobian, S[i][j] = sum_r O[r][i] O[r][j] over the
+// lower-triangular 64x64 tiles of the N_p x N_p matrix.  The sample dimension is
+// split over blockIdx.y so that small N_p still fills the GPU; split s writes
+// part[s][i][j], and k_gram_cols_sum adds the splits in a fixed order
+// (deterministic).  With one split the tile is written straight into S as
+// scale * sum + shift on the diagonal.  Rows of O are read along the parameter
+// index (one 512-byte segment per tile row and sample).
+__global__ void __launch_bounds__(256) k_gram_cols_fp64(const double *__restrict__ O, int Ns, long P, int rows_per,
+                                                        double scale, double shift, double *out) {
+    __shared__ double As[KC][TG + 1], Bs[KC][TG + 1];
+    int bi, bj;
+    tri_tile(blockIdx.x, bi, bj);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const long r0 = (long)bi * TG, c0 = (long)bj * TG;
+    const int s0 = blockIdx.y * rows_per, s1 = min(Ns, s0 + rows_per);
+    double acc[4][4] = {};
+    for (int ss = s0; ss < s1; ss += KC) {
+        for (int e = tid; e < TG * KC; e += 256) {
+            const int rr = e % TG, cc = e / TG, r = ss + cc;
+            const long ia = r0 + rr, ib = c0 + rr;
+            As[cc][rr] = (r < s1 && ia < P) ? O[(size_t)r * P + ia] : 0.0;
+            Bs[cc][rr] = (r < s1 && ib < P) ? O[(size_t)r * P + ib] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < KC; c++) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) av[m] = As[c][ty + 16 * m];
+#pragma unroll
+            for (int n = 0; n < 4; n++) bv[n] = Bs[c][tx + 16 * n];
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+#pragma unroll
+                for (int n = 0; n < 4; n++) acc[m][n] = fma(av[m], bv[n], acc[m][n]);
+        }
+        __syncthreads();
+    }
+    const bool direct = gridDim.y == 1;
+    double *dst = out + (direct ? 0 : (size_t)blockIdx.y * P * P);
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            const long i = r0 + ty + 16 * m, j = c0 + tx + 16 * n;
+            if (i < P && j <= i)
+                dst[(size_t)i * P + j] = direct ? acc[m][n] * scale + (i == j ? shift : 0.0) : acc[m][n];
+        }
+}
+
+// S[i][j] = scale * sum_s part[s][i][j] (+ shift on the diagonal), lower triangle.
+__global__ void k_gram_cols_sum(const double *__restrict__ part, int nsplit, long P, double scale, double shift,
+                                double *S) {
+    const size_t tot = (size_t)P * P;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (size_t)gridDim.x * blockDim.x) {
+        const long i = (long)(t / P), j = (long)(t % P);
+        if (j > i) continue;
+        double v = 0.0;
+        for (int q = 0; q < nsplit; q++) v += part[(size_t)q * tot + t];
+        S[t] = v * scale + (i == j ? shift : 0.0);
+    }
+}
+
+// Splits of the sample dimension for the column Gram: enough CTAs for about
+// eight per SM, at least 256 samples per split, and the partial sums within
+// 64 M doubles (512 MB).
+static int gram_cols_splits(int Ns, long P) {
+    const long nt = (P + TG - 1) / TG, tiles = nt * (nt + 1) / 2;
+    long want = (8L * ctx().sm_count + tiles - 1) / tiles;
+    want = std::min<long>(want, std::max(1, Ns / 256));
+    while (want > 1 && want * P * P > (64L << 20)) want--;
+    return (int)std::max<long>(1, want);
+}
+
+// S = O_c^T O_c / N_s + shift I into w.T (lower triangle) from the centred O.
+static bool gram_cols(const double *O, int Ns, long P, double shift) {
+    Workspace &w = g_ws;
+    cudaStream_t st = ctx().stream;
+    const int ns = gram_cols_splits(Ns, P);
+    const int rows_per = (Ns + ns - 1) / ns;
+    const long nt = (P + TG - 1) / TG;
+    if (!w.T.ensure((size_t)P * P)) return false;
+    if (ns > 1 && !w.T0.ensure((size_t)ns * P * P)) return false;
+    {
+        NQS_LAUNCH("gram_cols_fp64");
+        k_gram_cols_fp64<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)ns), 256, 0, st>>>(
+            O, Ns, P, rows_per, 1.0 / (double)Ns, shift, ns > 1 ? w.T0.p : w.T.p);
+    }
+    if (ns > 1) {
+        NQS_LAUNCH("gram_cols_sum");
+        k_gram_cols_sum<<<ctx().sm_count * 8, 256, 0, st>>>(w.T0.p, ns, P, 1.0 / (double)Ns, shift, w.T.p);
+    }
+    return NQS_CUDA(cudaGetLastError());
+}
+
+// The FP64 MinSR update in parameter space (push-through identity):
+// (O_c^T O_c / N_s + shift I) delta = O_c^T eps / N_s on the centred O [N_s][N_p].
+// Same FP64 blocked Cholesky and triangular solves as the sample-space path; a
+// failed factorisation is retried once with the shift raised by 1e-6 (the
+// upstream retry adds 1e-6 to its diagonal too), then delta = 0 and *conv = 0.
+// Writes delta [N_p]; returns 0 on success, -1 on a CUDA error.
+int minsr_fp64_params(const double *O, const double *eps, int Ns, long P, double shift, double *delta, int *conv) {
+    Workspace &w = g_ws;
+    cudaStream_t st = ctx().stream;
+    *conv = 0;
+    if (!w.z.ensure(P) || !w.r.ensure(P) || !w.status.ensure(16)) return -1;
+    // right-hand side b = O_c^T eps / N_s
+    if (!enqueue_col_dot(O, Ns, P, eps, 1.0 / (double)Ns, w.r.p)) return -1;
+    int fail = -1;
+    step_stats().chol_retry = 0;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (!gram_cols(O, Ns, P, shift + (attempt ? 1e-6 : 0.0))) return -1;
+        NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));
+        if (!cholesky_fp64(w.T.p, (int)P, w.status.p)) return -1;
+        if (!NQS_CUDA(cudaMemcpyAsync(&fail, w.status.p + I_FAIL, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+            !NQS_CUDA(cudaStreamSynchronize(st)))
+            return -1;
+        if (attempt == 0) step_stats().chol_fail_col = fail;
+        if (fail < 0) break;
+        step_stats().chol_retry = 1;
+    }
+    if (fail >= 0) {
+        fprintf(stderr, "nqs_sr_step_minsr: Cholesky breakdown after retry; increase "
+                        "sr_diag_shift or num_samples. Update set to 0.\n");
+        return NQS_CUDA(cudaMemsetAsync(delta, 0, sizeof(double) * P, st)) ? 0 : -1;
+    }
+    if (!cholesky_solve(w.T.p, (int)P, w.r.p, w.z.p, delta)) return -1;
+    *conv = 1;
+    return 0;
+}
+
 // The FP64 MinSR update delta = O^T y / N_s of one system whose mixed solve
 // broke down (FP32 pivot <= 0), on its centred O and eps.
 int minsr_fp64_delta(const double *O, const double *eps, int Ns, long P, double shift, double *delta, int *conv) {
@@ -1028,6 +1161,13 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         } else {
             NQS_LAUNCH("center");
             k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+            const int fs = c.opts.fp64_space;
+            if (fs == NQS_GPU_SPACE_PARAMETERS || (fs == NQS_GPU_SPACE_SMALLER && P < Ns)) {
+                // push-through form: the N_p x N_p system gives delta directly
+                if (minsr_fp64_params(w.O.p, w.eps.p, Ns, P, cfg->sr_diag_shift, w.delta.p, &converged) != 0)
+                    return -1;
+                solved = have_delta = true;
+            }
         }
         if (!solved && fp64_solve(w.y.p, &converged) != 0) return -1;
         if (!have_delta) {

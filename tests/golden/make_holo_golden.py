@@ -19,9 +19,10 @@ probe parameters theta + dt k1, which a twin ansatz reaches by one Euler step
 second batch.  CG is capped at a few iterations (or driven to a 1e-13
 residual on a well-conditioned system) so that the 1e-10 parity bar on the
 update is meaningful: a capped CG amplifies summation-order differences only
-slightly, a converged one not at all.
+slightly, a converged one not at all.  Two 5-iteration runs (nqs_sr_run_minsr,
+nqs_sr_run_holomorphic) record energy traces and final parameters.
 
-Runs here only; writes tests/golden/{holo,excited,tvmc}_*.npz.
+Runs here only; writes tests/golden/{holo,excited,tvmc,run}_*.npz.
 """
 import ctypes as C
 import os
@@ -208,6 +209,37 @@ def gen_tvmc(L, out):
         first.free(fs)
 
 
+def gen_runs(L, out):
+    """nqs_sr_run_minsr and nqs_sr_run_holomorphic over 5 iterations with the upstream sampler:
+    the energy trace and the final parameters.  After each update the upstream sampler keeps
+    the log|psi| it cached at the old parameters until its next accepted move, so a run checks
+    that the compat chain reproduces that across steps."""
+    run = [C.POINTER(abi.NqsConfig), C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+           C.POINTER(C.c_double)]
+    L.nqs_sr_run_minsr.argtypes = run
+    L.nqs_sr_run_holomorphic.argtypes = run
+    cases = [("run_minsr_heis_crbm_marshall", "minsr", abi.HAM_HEISENBERG, 4, 4, abi.ANSATZ_COMPLEX_RBM, 16,
+              dict(Ns=256, shift=1e-3, lr=0.01, cg_max=100, cg_tol=1e-6)),
+             ("run_holo_tfim_crbm", "holo", abi.HAM_TFIM, 8, 1, abi.ANSATZ_COMPLEX_RBM, 8,
+              dict(Ns=256, shift=1e-2, lr=0.02, cg_max=10, cg_tol=1e-6))]
+    for name, solver, ham, Lx, Ly, kind, M, sr in cases:
+        cfg = make_cfg(kind, M, ham, sr["Ns"], sr["shift"], sr["lr"], sr["cg_max"], sr["cg_tol"], 2718,
+                       transverse_field=0.9)
+        cfg.num_iterations = 5
+        wrap = "marshall" if ham == abi.HAM_HEISENBERG else None
+        pb = Problem(L, cfg, Lx * Ly, Lx, Ly, wrap)
+        p0 = pb.params()
+        s = L.nqs_sampler_create(pb.N, C.byref(cfg), pb.fn, pb.user)   # the run thermalises it
+        trace = np.zeros(5)
+        f = L.nqs_sr_run_minsr if solver == "minsr" else L.nqs_sr_run_holomorphic
+        assert f(C.byref(cfg), Lx, Ly, pb.a, s, pb.fn, pb.user, trace.ctypes.data_as(DP)) == 0
+        d = common(cfg, Lx * Ly, Lx, Ly, kind, M, ham, wrap)
+        d.update(params0=p0, params1=pb.params(), trace=trace, solver=solver, iterations=5,
+                 acceptance=L.nqs_sampler_acceptance_ratio(s))
+        out[name] = d
+        pb.free(s)
+
+
 def main():
     L = load_ref()
     declare(L)
@@ -215,9 +247,10 @@ def main():
     gen_holo(L, out)
     gen_excited(L, out)
     gen_tvmc(L, out)
+    gen_runs(L, out)
     for name, d in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
-        print(name, "info", d["info"])
+        print(name, "info", d.get("info", d.get("trace")))
     print("wrote", len(out), "fixtures")
 
 

@@ -356,11 +356,36 @@ def test_minsr_cholesky_failure_path(nqs):
     assert st.chol_retry == 1 and st.chol_fail_col >= 0
 
 
+def test_minsr_parameter_space_failure_path(nqs):
+    """Parameter-space FP64 solve with an indefinite system (negative shift): the retry
+    with the shift raised by 1e-6 fails too, so the step reports converged = 0 and leaves
+    the parameters unchanged."""
+    from spin_based_neural_network_gb300 import abi
+    N, M = 8, 8
+    a = make_ansatz(nqs, O.OR_RBM, N, M, None, 0.3, 11)
+    p0 = a.params.copy()
+    rng = np.random.default_rng(3)
+    batch = np.where(rng.random((512, N)) < 0.5, 1, -1).astype(np.int32)
+    cfg = abi.config_defaults(hamiltonian=0, sr_diag_shift=-0.5, learning_rate=0.1)
+    nqs.set_options(fp64_space=abi.SPACE_PARAMETERS)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, 8, 1, a, batch, minsr=True)
+    finally:
+        nqs.set_options()
+    assert info.converged == 0 and info.update_norm == 0.0
+    assert np.array_equal(a.params, p0)
+    st = nqs.last_step_stats()
+    assert st.chol_retry == 1 and st.chol_fail_col >= 0
+
+
+@pytest.mark.parametrize("space", ["samples", "parameters"])
 @pytest.mark.parametrize("Ns,M", [(4096, 32)])
-def test_minsr_full_size_against_oracle(nqs, Ns, M):
+def test_minsr_full_size_against_oracle(nqs, Ns, M, space):
     """The 2-D workload's shape (4x4 Heisenberg, Marshall, complex RBM M=32,
-    N_s=4096, shift 1e-4): the GPU FP64 update equals the oracle's on the same
-    samples."""
+    N_s=4096, shift 1e-4): the GPU FP64 update equals the oracle's (the upstream
+    sample-space order) on the same samples, whether the GPU solves the same
+    4096 x 4096 sample-space system or the 1120 x 1120 parameter-space one
+    (fp64_space, push-through identity)."""
     from spin_based_neural_network_gb300 import abi
     Lx = Ly = 4
     N = 16
@@ -371,11 +396,13 @@ def test_minsr_full_size_against_oracle(nqs, Ns, M):
     base = np.array([1, -1] * 8, np.int32)
     batch = np.stack([rng.permutation(base) for _ in range(Ns)])      # Sz = 0 sector
     cfg = abi.config_defaults(hamiltonian=1, sr_diag_shift=1e-4, learning_rate=0.005)
-    nqs.set_options(square_pbc=1)
+    fs = abi.SPACE_PARAMETERS if space == "parameters" else 0
+    nqs.set_options(square_pbc=1, fp64_space=fs)
     try:
         info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True, log_amp_fn=m.log_amp_fn, user=m.user)
     finally:
         nqs.set_options()
+    assert info.converged == 1
     amp = O.Amp(O.OR_CRBM, N, M, p0.copy(), [("marshall", Lx, Ly)])
     Eo, do, io = O.minsr_step(O.ham(O.OR_HEIS, Lx, Ly, pbc=1), amp, batch, 1e-4, 0.005)
     assert rel(E, Eo) < TOL
