@@ -1647,20 +1647,43 @@ static double *g_noalloc_ptr[64];
 static unsigned long long g_noalloc_ctx[64];
 static std::mutex g_noalloc_mu;
 
+// Driver entry points, looked up through the runtime (the library does not link the
+// driver library, so it loads on hosts without one).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+static bool driver_fn(const char *name, int version, void **fn) {
+    cudaDriverEntryPointQueryResult q;
+    *fn = nullptr;
+    return cudaGetDriverEntryPointByVersion(name, fn, version, cudaEnableDefault, &q) == cudaSuccess &&
+           q == cudaDriverEntryPointSuccess && *fn;
+}
+
+// The unique id of the context current on this thread (0 when there is none).
+static unsigned long long current_context_id(int dev) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current && !driver_fn("cuCtxGetCurrent", 4000, (void **)&get_current)) return 0;
+    if (!get_id && !driver_fn("cuCtxGetId", 12000, (void **)&get_id)) return 0;
+    CUcontext cur = nullptr;
+    if (get_current(&cur) == CUDA_SUCCESS && !cur) {
+        // no context current on this thread yet: make the device's primary context
+        // current (cudaSetDevice initialises it)
+        if (cudaSetDevice(dev) != cudaSuccess || get_current(&cur) != CUDA_SUCCESS) cur = nullptr;
+    }
+    unsigned long long id = 0;
+    if (!cur || get_id(cur, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
 static double *noalloc_scratch(int dev) {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (dev < 0 || dev >= 64) {
         set_error("device ordinal %d out of range", dev);
         return nullptr;
     }
-    CUcontext cur = nullptr;
-    if (cuCtxGetCurrent(&cur) == CUDA_SUCCESS && !cur) {
-        // no context current on this thread yet: make the device's primary context
-        // current (cudaSetDevice initialises it)
-        if (cudaSetDevice(dev) != cudaSuccess || cuCtxGetCurrent(&cur) != CUDA_SUCCESS) cur = nullptr;
-    }
-    unsigned long long id = 0;
-    if (!cur || cuCtxGetId(cur, &id) != CUDA_SUCCESS) {
+    const unsigned long long id = current_context_id(dev);
+    if (!id) {
         set_error("nqs_gpu_minsr_solve_noalloc: no current CUDA context on device %d", dev);
         return nullptr;
     }
