@@ -56,6 +56,29 @@ int nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec(
     double *out_eigenvector,
     lanczos_result_t *out_result);
 
+/* GB300 addition, the magnetisation-sector form of the lean projecting Lanczos that the
+ * upstream sector drivers run over the library's building blocks
+ * (scripts/research_kagome_sz_spatial.c:96-121, 196-240; scripts/research_kagome_spin_gap.c:
+ * 22-36, 118-145).  Their projector first zeroes every amplitude whose number of down spins
+ * (set bits) differs from `popcount`, then applies the spatial projection (perm, characters,
+ * G; the identity group G = 1 for the Sz sector alone).  Here that filter runs inside every
+ * matvec and projection pass, so states outside the sector are written as zero without being
+ * evaluated (H and the permutations keep the popcount).  popcount = -1: no filter.
+ * seed_state = 0: the seed of nqs_lanczos_e0_kagome_heisenberg_projected_lean; otherwise the
+ * drivers' seed protocol: u_i - 1/2 from xorshift64 (13, 7, 17) started at seed_state,
+ * projected and normalised, then handed to the lean Lanczos as its initial vector, which
+ * projects and normalises it again (the drivers use 0xA5A5A5A5A5A5A5A5 ^ 2^N for the Sz
+ * sectors and 0xC3C3C3C3C3C3C3C3 ^ 2^N ^ (irrep index * 0x9E3779B97F4A7C15) with a p6m
+ * irrep).  out_eigenvector (host, 2^N doubles) may be NULL.  Returns 0 or -1. */
+int nqs_gpu_lanczos_e0_kagome_sz_projected_lean(
+    int Lx_cells, int Ly_cells, double J, int pbc,
+    const int *perm, const double *characters, int G,
+    int popcount, unsigned long long seed_state,
+    int max_iters, double tol,
+    double *out_eigenvalue,
+    double *out_eigenvector,
+    lanczos_result_t *out_result);
+
 /* ---- device-resident building blocks (GB300 additions) ---------------------------
  * Pointers marked d_ are device pointers of 2^N doubles. */
 

@@ -93,10 +93,11 @@ __device__ __forceinline__ double block_total(const double *part, int np) {
 // active lanes, so the bonds away from the lane bits -- where all 32 states of the warp
 // agree -- are first collected into a warp-uniform bit mask and only the antiparallel ones
 // are loaded (four at a time) and added.  part (may be null) receives the block partials
-// of x.y.
+// of x.y.  popc >= 0 restricts to the states with that many set bits (down spins): the
+// others are written as 0 without being evaluated.
 __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__restrict__ x, double *__restrict__ y,
                                                             unsigned dim, Bonds B, double qJ, double hJ,
-                                                            double *__restrict__ part) {
+                                                            double *__restrict__ part, int popc) {
     __shared__ unsigned sm[ED_MAX_BONDS];
     __shared__ double diag[ED_MAX_BONDS + 1];
     for (int i = threadIdx.x; i < B.nb; i += ED_THREADS) sm[i] = B.m[i];
@@ -106,6 +107,11 @@ __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__rest
     double dot = 0.0;
     const unsigned stride = gridDim.x * ED_THREADS;
     for (unsigned s = blockIdx.x * ED_THREADS + threadIdx.x; s < dim; s += stride) {
+        if (popc >= 0 && __popc(s) != popc) {
+            // outside the magnetisation sector: H keeps the popcount, so x and H x are zero here
+            y[s] = 0.0;
+            continue;
+        }
         double off = 0.0;
         int anti = 0;
 #pragma unroll 4
@@ -142,11 +148,12 @@ __global__ void __launch_bounds__(ED_THREADS) k_heis_matvec(const double *__rest
 
 // y[s] = scale * sum_e chi[e] x[pi_e(s)] over m group elements, pi_e(s) = OR_c tab[e][c][nibble c
 // of s] (bit i of pi_e(s) = bit perm_e[i] of s).  part (may be null) receives the block
-// partials of y.y.
+// partials of y.y.  popc >= 0: states whose popcount differs are set to 0 (the permutations
+// keep the popcount, so the sum for a state in the sector reads only states in it).
 __global__ void __launch_bounds__(ED_THREADS) k_perm_sum(const double *__restrict__ x, double *__restrict__ y,
                                                          unsigned dim, int m, const unsigned *__restrict__ tab,
                                                          const double *__restrict__ chi, double scale,
-                                                         double *__restrict__ part) {
+                                                         double *__restrict__ part, int popc) {
     extern __shared__ __align__(16) unsigned char ed_smem[];
     double *s_chi = (double *)ed_smem;
     unsigned *s_tab = (unsigned *)(s_chi + m);
@@ -156,6 +163,10 @@ __global__ void __launch_bounds__(ED_THREADS) k_perm_sum(const double *__restric
     double nrm = 0.0;
     const unsigned stride = gridDim.x * ED_THREADS;
     for (unsigned s = blockIdx.x * ED_THREADS + threadIdx.x; s < dim; s += stride) {
+        if (popc >= 0 && __popc(s) != popc) {
+            y[s] = 0.0;                       // the magnetisation filter of the sector projector
+            continue;
+        }
         double acc = 0.0;
 #pragma unroll 2
         for (int e = 0; e < m; e++) {
@@ -542,7 +553,7 @@ int ed_grid(unsigned dim) {
 }
 
 bool launch_perm_pass(const ProjPlan &P, int pass, const double *x, double *y, unsigned dim, double scale,
-                      double *part, cudaStream_t st) {
+                      double *part, cudaStream_t st, int popc = -1) {
     static bool attr = false;
     if (!attr) {
         if (!NQS_CUDA(cudaFuncSetAttribute(k_perm_sum, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -556,17 +567,18 @@ bool launch_perm_pass(const ProjPlan &P, int pass, const double *x, double *y, u
     const size_t smem = (size_t)m * (ED_TAB * sizeof(unsigned) + sizeof(double));
     NQS_LAUNCH("ed_project_pass");
     k_perm_sum<<<ed_grid(dim), ED_THREADS, smem, st>>>(x, y, dim, m, P.tab.p + (size_t)off * ED_TAB,
-                                                       P.chi.p + off, scale, part);
+                                                       P.chi.p + off, scale, part, popc);
     return NQS_CUDA(cudaGetLastError());
 }
 
 // Projects *a in place (using *t as scratch; the pointers may be swapped so that the
 // result is in *a).  part (may be null) receives the partials of the result's norm.
-bool project(const ProjPlan &P, double *&a, double *&t, unsigned dim, double *part, cudaStream_t st) {
+bool project(const ProjPlan &P, double *&a, double *&t, unsigned dim, double *part, cudaStream_t st,
+             int popc = -1) {
     const double invG = 1.0 / (double)P.G;
     for (int k = 0; k < P.passes; k++) {
         const bool last = k + 1 == P.passes;
-        if (!launch_perm_pass(P, k, a, t, dim, last ? invG : 1.0, last ? part : nullptr, st)) return false;
+        if (!launch_perm_pass(P, k, a, t, dim, last ? invG : 1.0, last ? part : nullptr, st, popc)) return false;
         std::swap(a, t);
     }
     return true;
@@ -614,7 +626,7 @@ struct SeedDev {
     DevBuf<uint64_t> jump;
 };
 
-bool launch_seed(double *v, unsigned dim, int alternate, cudaStream_t st) {
+bool launch_seed(double *v, unsigned dim, int alternate, cudaStream_t st, uint64_t state = 0) {
     static SeedDev sd;
     const auto &J = seed_jumps();
     if (!sd.jump.p) {
@@ -625,7 +637,7 @@ bool launch_seed(double *v, unsigned dim, int alternate, cudaStream_t st) {
     const unsigned threads = (unsigned)(((uint64_t)dim + ED_SEED_RUN - 1) / ED_SEED_RUN);
     int nj = 0;
     while (nj < 32 && (threads - 1) >> nj) nj++;
-    const uint64_t x0 = (alternate ? 0xBEEFBABEull : 0xA5A5A5A5A5A5A5A5ull) ^ (uint64_t)dim;
+    const uint64_t x0 = state ? state : (alternate ? 0xBEEFBABEull : 0xA5A5A5A5A5A5A5A5ull) ^ (uint64_t)dim;
     NQS_LAUNCH("ed_seed");
     k_lz_seed<<<(threads + ED_THREADS - 1) / ED_THREADS, ED_THREADS, 0, st>>>(v, dim, x0, sd.jump.p, nj);
     return NQS_CUDA(cudaGetLastError());
@@ -722,8 +734,14 @@ struct LeanOut {
     int iters = 0, converged = 0;
 };
 
+// popc >= 0: the magnetisation sector (states with popc set bits), filtered inside every
+// matvec and projection.  seed_state != 0: the seed protocol of the upstream sector drivers
+// (scripts/research_kagome_sz_spatial.c:206-236, research_kagome_spin_gap.c:122-143): the
+// xorshift64 seed from that state is projected and normalised, then handed to the lean
+// Lanczos as its initial vector, which projects and normalises it again.
 int lanczos_kagome(int Lx, int Ly, double J, int pbc, const int *perm, const double *chars, int G, int max_iters,
-                   double tol, double *out_eig, double *out_vec, lanczos_result_t *out_res) {
+                   double tol, double *out_eig, double *out_vec, lanczos_result_t *out_res, int popc = -1,
+                   uint64_t seed_state = 0) {
     clear_error();
     if (out_res) *out_res = lanczos_result_t{0.0, 0, 0, 0.0};
     const int N = 3 * Lx * Ly;
@@ -758,7 +776,14 @@ int lanczos_kagome(int Lx, int Ly, double J, int pbc, const int *perm, const dou
     // leaves nothing, src/mps/lanczos.c:874-884); acc = z0 v0 on the replay
     int alt_used = 0;
     auto make_seed = [&](int alt, double *acc, double z0, double *norm_out) -> bool {
-        if (!launch_seed(vc, dim, alt, st) || !project(*P, vc, t, dim, E.part.p, st)) return false;
+        if (!launch_seed(vc, dim, alt, st, alt ? 0 : seed_state) || !project(*P, vc, t, dim, E.part.p, st, popc))
+            return false;
+        if (seed_state && !alt) {
+            // the caller-built seed: normalised once before the Lanczos projects it again
+            NQS_LAUNCH("ed_normalise");
+            k_lz_normalise<<<grid, ED_THREADS, 0, st>>>(vc, dim, E.part.p, grid, E.nrm.p, nullptr, 0.0);
+            if (!NQS_CUDA(cudaGetLastError()) || !project(*P, vc, t, dim, E.part.p, st, popc)) return false;
+        }
         {
             NQS_LAUNCH("ed_normalise");
             k_lz_normalise<<<grid, ED_THREADS, 0, st>>>(vc, dim, E.part.p, grid, E.nrm.p, acc, z0);
@@ -770,13 +795,13 @@ int lanczos_kagome(int Lx, int Ly, double J, int pbc, const int *perm, const dou
     auto step = [&](int k, bool with_scale, double *acc, double z) -> bool {
         {
             NQS_LAUNCH("ed_matvec");
-            k_heis_matvec<<<grid, ED_THREADS, 0, st>>>(vc, w, dim, B, qJ, hJ, E.part.p);
+            k_heis_matvec<<<grid, ED_THREADS, 0, st>>>(vc, w, dim, B, qJ, hJ, E.part.p, popc);
         }
         {
             NQS_LAUNCH("ed_orth");
             k_lz_orth<<<grid, ED_THREADS, 0, st>>>(w, vc, vp, dim, E.part.p, grid, E.al.p, E.be.p, k);
         }
-        if (!NQS_CUDA(cudaGetLastError()) || !project(*P, w, t, dim, E.part.p, st)) return false;
+        if (!NQS_CUDA(cudaGetLastError()) || !project(*P, w, t, dim, E.part.p, st, popc)) return false;
         if (with_scale) {
             NQS_LAUNCH("ed_scale");
             k_lz_scale<<<grid, ED_THREADS, 0, st>>>(w, dim, E.part.p, grid, E.be.p, k, acc, z);
@@ -891,6 +916,20 @@ int nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec(int Lx, int Ly, doubl
     return lanczos_kagome(Lx, Ly, J, pbc, perm, chars, G, max_iters, tol, out_eig, out_vec, out_res);
 }
 
+int nqs_gpu_lanczos_e0_kagome_sz_projected_lean(int Lx, int Ly, double J, int pbc, const int *perm,
+                                                const double *chars, int G, int popcount,
+                                                unsigned long long seed_state, int max_iters, double tol,
+                                                double *out_eig, double *out_vec, lanczos_result_t *out_res) {
+    const int N = 3 * Lx * Ly;
+    if (popcount < -1 || popcount > N) {
+        clear_error();
+        set_error("popcount %d out of range for N = %d", popcount, N);
+        return -1;
+    }
+    return lanczos_kagome(Lx, Ly, J, pbc, perm, chars, G, max_iters, tol, out_eig, out_vec, out_res, popcount,
+                          (uint64_t)seed_state);
+}
+
 int nqs_gpu_kagome_heis_matvec(int Lx, int Ly, double J, int pbc, const double *d_in, double *d_out) {
     clear_error();
     const int N = 3 * Lx * Ly;
@@ -905,7 +944,7 @@ int nqs_gpu_kagome_heis_matvec(int Lx, int Ly, double J, int pbc, const double *
     {
         NQS_LAUNCH("ed_matvec");
         k_heis_matvec<<<ed_grid(dim), ED_THREADS, 0, ctx().stream>>>(d_in, d_out, dim, B, 0.25 * J, 0.5 * J,
-                                                                     nullptr);
+                                                                     nullptr, -1);
     }
     return NQS_CUDA(cudaGetLastError()) ? 0 : -1;
 }

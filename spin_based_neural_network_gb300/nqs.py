@@ -82,6 +82,9 @@ def _declare(L):
         "nqs_lanczos_e0_kagome_heisenberg_projected_lean": (
             C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, IP, DP, C.c_int, C.c_int, C.c_double, DP,
                       C.POINTER(abi.LanczosResult)]),
+        "nqs_gpu_lanczos_e0_kagome_sz_projected_lean": (
+            C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, IP, DP, C.c_int, C.c_int, C.c_ulonglong, C.c_int,
+                      C.c_double, DP, DP, C.POINTER(abi.LanczosResult)]),
         "nqs_lanczos_e0_kagome_heisenberg_projected_lean_eigvec": (
             C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, IP, DP, C.c_int, C.c_int, C.c_double, DP, DP,
                       C.POINTER(abi.LanczosResult)]),
@@ -650,6 +653,34 @@ def lanczos_e0_kagome_lean(Lx, Ly, J, pbc, perm, chars, max_iters=100, tol=1e-9,
         rc = lib().nqs_lanczos_e0_kagome_heisenberg_projected_lean(
             Lx, Ly, J, pbc, _ip(perm), _dp(chars), len(chars), max_iters, tol, C.byref(e), C.byref(r))
     _check(rc, "lean Lanczos")
+    return e.value, vec, {"iterations": r.iterations, "converged": r.converged, "residual_norm": r.residual_norm}
+
+
+def sz_seed_state(N, irrep_index=None):
+    """The xorshift64 start state of the upstream sector drivers' seeds: 0xA5A5A5A5A5A5A5A5 ^ 2^N
+    for a magnetisation sector alone, 0xC3C3C3C3C3C3C3C3 ^ 2^N ^ (irrep index * 0x9E3779B97F4A7C15)
+    with a p6m irrep (index in A1 A2 B1 B2 E1 E2 order)."""
+    dim = 1 << N
+    if irrep_index is None:
+        return (0xA5A5A5A5A5A5A5A5 ^ dim) & 0xFFFFFFFFFFFFFFFF
+    return (0xC3C3C3C3C3C3C3C3 ^ dim ^ ((irrep_index * 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF)) \
+        & 0xFFFFFFFFFFFFFFFF
+
+
+def lanczos_e0_kagome_sz(Lx, Ly, J, pbc, perm, chars, popcount, seed_state=0, max_iters=200, tol=1e-10,
+                         eigvec=False):
+    """Magnetisation-sector lean Lanczos (nqs_gpu_lanczos_e0_kagome_sz_projected_lean): the states
+    with `popcount` down spins, projected on the sector (perm, chars); seed_state as
+    sz_seed_state() for the upstream sector drivers' seeds, 0 for the library seed.  Returns
+    (E0, eigenvector or None, {"iterations", "converged", "residual_norm"})."""
+    perm, chars = _perm_args(perm, chars)
+    e = C.c_double()
+    r = abi.LanczosResult()
+    vec = np.zeros(1 << (3 * Lx * Ly)) if eigvec else None
+    rc = lib().nqs_gpu_lanczos_e0_kagome_sz_projected_lean(
+        Lx, Ly, J, pbc, _ip(perm), _dp(chars), len(chars), popcount, seed_state, max_iters, tol, C.byref(e),
+        _dp(vec) if eigvec else None, C.byref(r))
+    _check(rc, "sector Lanczos")
     return e.value, vec, {"iterations": r.iterations, "converged": r.converged, "residual_norm": r.residual_norm}
 
 
