@@ -704,6 +704,14 @@ def other_workloads(nqs, abi, L, base_opts, which, cpu=True):
         ms, info = timed_steps(nqs, L, step4, 1, 3)
         ph = list(nqs.last_step_stats().phase_us)
         k4 = step_kernels(nqs, step4)
+        # accuracy of one mixed step against the FP64 estimator and FP64 MinSR on the same samples
+        nqs.set_options(**dict(base_opts, mixed_check=1))
+        step4()
+        st4 = nqs.last_step_stats()
+        check4 = {"delta_theta_rel_err_vs_fp64": st4.delta_rel_err, "energy_rel_err": st4.energy_rel_err,
+                  "cg_residual": st4.refine_residual, "cg_iterations": st4.refine_sweeps,
+                  "reference": "FP64 MLP estimator + FP64 MinSR (sample space, 16384 x 16384) on the same samples"}
+        nqs.set_options(**base_opts)
 
         def run4(learned, decor, warm=2, steps=4):
             # plain exchange moves, or mixed with the learned proposal (MADE width 64,
@@ -739,7 +747,7 @@ def other_workloads(nqs, abi, L, base_opts, which, cpu=True):
             "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "num_params": a.P,
             "solve_space": "parameters (N_p = 15014 < N_s = 16384)", "energy_per_site_last": info.mean_energy / N,
             "e0_per_site_recorded_upstream": e0, "factor_solve_phases_us": [round(x, 1) for x in ph],
-            "kernels_ms_one_step": k4, "plain_vs_learned_proposal": proposals4,
+            "kernels_ms_one_step": k4, "plain_vs_learned_proposal": proposals4, "accuracy_vs_fp64": check4,
             "estimator": "FP32 MLP (k_local_mlp32)", "sampler": "FP32 MLP chains (k_sample_mlp32)"}
         if cpu:
             import oracle_lib as O

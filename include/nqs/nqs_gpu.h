@@ -193,9 +193,10 @@ int nqs_gpu_gradient_batch(nqs_ansatz_t *a, nqs_gradient_fn_t gradient_fn,
                            int complex_out, double *out_re, double *out_im);
 
 /* One SR step on a caller-supplied batch (no sampling): the parity entry
- * points.  `minsr` = 1 runs MinSR, 0 runs CG-SR, 2 holomorphic SR (then gradient_fn,
- * when set, is the holomorphic gradient: nqs_symproj_gradient_complex).  Optional
- * outputs: out_energies[batch], out_delta[num_params]. */
+ * points.  `minsr` = 1 runs MinSR, 0 runs CG-SR, 2 holomorphic SR, 5 holomorphic
+ * MinSR (for 2 and 5 gradient_fn, when set, is the holomorphic gradient:
+ * nqs_symproj_gradient_complex).  Optional outputs: out_energies[batch],
+ * out_delta[num_params]. */
 int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int size_x, int size_y,
                           nqs_ansatz_t *ansatz,
                           nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,
@@ -203,6 +204,30 @@ int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int size_x, int size_y,
                           const int *batch, int num_samples, int minsr,
                           nqs_sr_step_info_t *out_info,
                           double *out_energies, double *out_delta);
+
+/* Holomorphic MinSR (no upstream counterpart): the linear system of the upstream
+ * holomorphic SR step (nqs_sr_step_holomorphic_full, src/nqs/nqs_optimizer.c:415-524:
+ * G = 2 Re[<O* O> - <O*><O>] + shift I, F = 2 Re[<O* E_loc> - <O*><E_loc>], theta -= lr delta)
+ * solved by MinSR instead of CG.  With O = R + i I for the real parameters,
+ * G = (2 / N_s)(R_c^T R_c + I_c^T I_c) + shift I and F = (2 / N_s)(R_c^T e_re + I_c^T e_im),
+ * which is the MinSR system of the stacked real matrix [R_c; I_c] (2 N_s rows) and the
+ * stacked centred energies [e_re; e_im] with the shift divided by 4; the update equals the
+ * converged holomorphic CG-SR update on the same samples.  It optimises complex ansaetze
+ * (complex RBM, the complex-output MLP) through both the phase and the modulus, where the
+ * upstream MinSR (real parts only) drops the phase.  Precision and solve space follow
+ * the process options (FP64: fp64_space; MIXED: tensor-core Gram of the stacked rows).
+ * grad_fn: NULL (the base ansatz's holomorphic gradient) or nqs_symproj_gradient_complex. */
+int nqs_sr_step_minsr_holomorphic_full(const nqs_config_t *cfg, int size_x, int size_y,
+                                       nqs_ansatz_t *ansatz, nqs_sampler_t *sampler,
+                                       nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,
+                                       nqs_holomorphic_gradient_fn_t grad_fn, void *grad_user,
+                                       nqs_sr_step_info_t *out_info);
+/* cfg->num_iterations steps after thermalising the sampler; out_energy_trace (optional)
+ * receives each step's mean energy, as nqs_sr_run_minsr. */
+int nqs_sr_run_minsr_holomorphic(const nqs_config_t *cfg, int size_x, int size_y,
+                                 nqs_ansatz_t *ansatz, nqs_sampler_t *sampler,
+                                 nqs_log_amp_fn_t log_amp_fn, void *log_amp_user,
+                                 double *out_energy_trace);
 
 /* The excited-state SR step (nqs_sr_step_excited) and the Euler tVMC step
  * (nqs_tvmc_step_real_time) on a caller-supplied batch: the parity entry points. */

@@ -636,7 +636,8 @@ struct StepIn {
     nqs_gradient_fn_t gfn;
     void *guser;
     // 0 CG-SR, 1 MinSR, 2 holomorphic SR (CG on the complex QGT), 3 excited-state SR (2 with
-    // the orthogonality penalty), 4 real-time tVMC force (same metric)
+    // the orthogonality penalty), 4 real-time tVMC force (same metric), 5 holomorphic MinSR
+    // (the holomorphic system solved as MinSR on the stacked real and imaginary parts)
     int minsr;
     nqs_holomorphic_gradient_fn_t hgfn;
     void *hguser;
@@ -1018,7 +1019,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
                   "nqs_translation_gradient)");
         return -1;
     }
-    const bool holo = in.minsr >= 2, excited = in.minsr == 3, realtime = in.minsr == 4;
+    const bool holo = in.minsr >= 2, excited = in.minsr == 3, realtime = in.minsr == 4, hm = in.minsr == 5;
     if (excited && !in.ref_fn) {
         set_error("excited-state SR needs the reference log-amplitude");
         return -1;
@@ -1040,12 +1041,17 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         }
     }
     Workspace &w = g_ws;
-    if (!w.E.ensure(Ns) || !w.Ei.ensure(Ns) || !w.eps.ensure(Ns) || !w.O.ensure((size_t)Ns * P) ||
+    // holomorphic MinSR keeps R and I as one stacked [2 N_s][N_p] matrix and the centred
+    // energies as one stacked [2 N_s] vector (the rows of its MinSR system)
+    const int rows = hm ? 2 * Ns : Ns;
+    if (!w.E.ensure(Ns) || !w.Ei.ensure(Ns) || !w.eps.ensure(rows) || !w.O.ensure((size_t)rows * P) ||
         !w.gm.ensure(P) || !w.delta.ensure(P) || !w.scal.ensure(16) || !w.status.ensure(16))
         return -1;
-    if (holo && (!w.Oi.ensure((size_t)Ns * P) || !w.gm2.ensure(P) || !w.F2.ensure(P) || !w.scal2.ensure(16) ||
-                 !w.eps2.ensure(Ns)))
+    if (holo && ((!hm && (!w.Oi.ensure((size_t)Ns * P) || !w.eps2.ensure(Ns))) || !w.gm2.ensure(P) ||
+                 !w.F2.ensure(P) || !w.scal2.ensure(16)))
         return -1;
+    double *const Oi = hm ? w.O.p + (size_t)Ns * P : w.Oi.p;
+    double *const eps2 = hm ? w.eps.p + Ns : w.eps2.p;
     DevAmp Aref;
     if (excited && (!build_amp(in.ref_fn, in.ref_user, H.N, &Aref, nullptr) || !w.la.ensure(Ns) ||
                     !w.ar.ensure(Ns) || !w.la_ref.ensure(Ns) || !w.ar_ref.ensure(Ns) || !w.aug.ensure(32)))
@@ -1057,8 +1063,12 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     } else {
         if (!upload_spins(in.host_batch, Ns, H.N, &bits)) return -1;
     }
+    // holomorphic MinSR: G + eps I = 4 (O_s^T O_s / (2 N_s) + eps / 4 I) with O_s = [R_c; I_c] and
+    // F = 4 O_s^T [e_re; e_im] / (2 N_s), so delta is the MinSR update of the stacked rows
+    // with the shift divided by 4
+    const double shift = hm ? 0.25 * cfg->sr_diag_shift : cfg->sr_diag_shift;
     auto fp64_solve = [&](double *y_out, int *conv) -> int {
-        return minsr_fp64_solve(w.O.p, w.eps.p, Ns, P, cfg->sr_diag_shift, y_out, conv);
+        return minsr_fp64_solve(w.O.p, w.eps.p, rows, P, shift, y_out, conv);
     };
     const bool mixed = c.opts.precision == NQS_GPU_PREC_MIXED;
     const bool fp32est = mixed && c.opts.fp32_estimator && !grad_sym && !holo && (fp32_capable(A) || fp32_mlp_capable(A));
@@ -1090,11 +1100,11 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     // (nqs_ansatz_logpsi_gradient_complex, src/nqs/nqs_optimizer.c:458-469)
     bool fused_grad = !grad_sym && A.G == 0;
     if (holo && A.G == 0 && !hg_sym) {
-        if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, w.O.p, w.Oi.p, 2, false)) return -1;
+        if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, w.O.p, Oi, 2, false)) return -1;
     } else if (holo) {
         if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, nullptr, nullptr, 0, false)) return -1;
-        if (hg_sym ? !launch_symproj_gradient_complex(Ahg, bits, Ns, w.O.p, w.Oi.p)
-                   : !launch_gradient(A.a, bits, Ns, 2, w.O.p, w.Oi.p))
+        if (hg_sym ? !launch_symproj_gradient_complex(Ahg, bits, Ns, w.O.p, Oi)
+                   : !launch_gradient(A.a, bits, Ns, 2, w.O.p, Oi))
             return -1;
     } else if (!launch_local_estimator(A, H, bits, Ns, w.E.p, w.Ei.p, fused_grad ? w.O.p : nullptr, nullptr,
                                        fused_grad ? 1 : 0, fp32est)) {
@@ -1114,7 +1124,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             return -1;
         // <E_im> for the holomorphic force
         if (holo && (!ensure_energy_scratch(w.es2, Ns) ||
-                     !enqueue_energy_stats(w.Ei.p, Ns, 0, w.scal2.p, w.eps2.p, w.es2.p)))
+                     !enqueue_energy_stats(w.Ei.p, Ns, 0, w.scal2.p, eps2, w.es2.p)))
             return -1;
         // excited-state SR: the physical statistics stay in scal for the step info; the force
         // takes the augmented local energies and means
@@ -1129,11 +1139,20 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
     dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
     int converged = 0, cg_iters = 0;
-    if (in.minsr == 1) {
-        if (!w.T.ensure((size_t)Ns * Ns) || !w.y.ensure(Ns) || !w.z.ensure(Ns)) return -1;
+    if (in.minsr == 1 || hm) {
+        if (!w.T.ensure((size_t)rows * rows) || !w.y.ensure(rows) || !w.z.ensure(rows)) return -1;
         {
             NQS_LAUNCH("col_mean");
             if (!col_stats(w.O.p, Ns, P, nullptr, w.scal.p, w.gm.p, nullptr)) return -1;
+        }
+        if (hm) {
+            // centre each half with its own column means; the stacked matrix then has zero
+            // means for the solvers below
+            NQS_LAUNCH("center");
+            if (!col_stats(Oi, Ns, P, nullptr, w.scal2.p, w.gm2.p, nullptr)) return -1;
+            k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+            k_center<<<c.sm_count * 8, 256, 0, st>>>(Oi, Ns, P, w.gm2.p);
+            if (!NQS_CUDA(cudaMemsetAsync(w.gm.p, 0, sizeof(double) * P, st))) return -1;
         }
         ss.refine_residual = 0.0;
         ss.refine_sweeps = 0;
@@ -1144,7 +1163,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             // centring happens inside the split kernel of the mixed solve
             double resid = 0.0;
             int f32 = -1;
-            if (!minsr_mixed_solve(w.O.p, w.gm.p, w.eps.p, Ns, P, cfg->sr_diag_shift, c.opts.refine_sweeps,
+            if (!minsr_mixed_solve(w.O.p, w.gm.p, w.eps.p, rows, P, shift, c.opts.refine_sweeps,
                                    c.opts.gram_passes, c.opts.mixed_space, w.y.p, w.delta.p, &have_delta,
                                    &resid, &f32))
                 return -1;
@@ -1159,22 +1178,23 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
                 have_delta = false;
             }
         } else {
-            NQS_LAUNCH("center");
-            k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+            if (!hm) {
+                NQS_LAUNCH("center");
+                k_center<<<c.sm_count * 8, 256, 0, st>>>(w.O.p, Ns, P, w.gm.p);
+            }
             const int fs = c.opts.fp64_space;
-            if (fs == NQS_GPU_SPACE_PARAMETERS || (fs == NQS_GPU_SPACE_SMALLER && P < Ns)) {
+            if (fs == NQS_GPU_SPACE_PARAMETERS || (fs == NQS_GPU_SPACE_SMALLER && P < rows)) {
                 // push-through form: the N_p x N_p system gives delta directly
-                if (minsr_fp64_params(w.O.p, w.eps.p, Ns, P, cfg->sr_diag_shift, w.delta.p, &converged) != 0)
-                    return -1;
+                if (minsr_fp64_params(w.O.p, w.eps.p, rows, P, shift, w.delta.p, &converged) != 0) return -1;
                 solved = have_delta = true;
             }
         }
         if (!solved && fp64_solve(w.y.p, &converged) != 0) return -1;
         if (!have_delta) {
             NQS_LAUNCH("delta");
-            k_col_dot<<<cg, cb, 0, st>>>(w.O.p, Ns, P, w.y.p, 1.0 / (double)Ns, w.delta.p);
+            k_col_dot<<<cg, cb, 0, st>>>(w.O.p, rows, P, w.y.p, 1.0 / (double)rows, w.delta.p);
         }
-        if (mixed && solved && c.opts.mixed_check) {
+        if (mixed && solved && c.opts.mixed_check && !hm) {
             // the FP64 solve on the same centred Jacobian (or, with the FP32
             // estimator, the whole FP64 step computed above), for the
             // delta-theta error
@@ -1263,7 +1283,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         info->variance_energy = hs[S_ESQ] - hs[S_EMEAN] * hs[S_EMEAN];
         info->update_norm = in.no_apply ? 0.0 : sqrt(hs[S_NORM2]) * fabs(lr_eff);
         info->acceptance_ratio = in.sampler ? nqs_sampler_acceptance_ratio((nqs_sampler_t *)in.sampler) : 0.0;
-        info->cg_iterations = in.minsr == 1 ? 0 : cg_iters;
+        info->cg_iterations = (in.minsr == 1 || hm) ? 0 : cg_iters;
         info->converged = converged;
     }
     return 0;
@@ -1412,12 +1432,43 @@ int nqs_sr_run_minsr(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, n
     return 0;
 }
 
+int nqs_sr_step_minsr_holomorphic_full(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a,
+                                       nqs_sampler_t *s, nqs_log_amp_fn_t fn, void *user,
+                                       nqs_holomorphic_gradient_fn_t gfn, void *guser, nqs_sr_step_info_t *info) {
+    if (!cfg || !a || !s) return -1;
+    StepIn in{cfg, sx, sy, (Ansatz *)a, (Sampler *)s, nullptr, cfg->num_samples, fn, user, nullptr, nullptr, 5,
+              gfn, guser};
+    if (nqs_sampler_num_sites(s) != ((Ansatz *)a)->N) {
+        set_error("sampler and ansatz disagree on num_sites");
+        return -1;
+    }
+    return sr_step_impl(in, info, nullptr, nullptr);
+}
+
+int nqs_sr_run_minsr_holomorphic(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_sampler_t *s,
+                                 nqs_log_amp_fn_t fn, void *user, double *trace) {
+    if (!cfg || !a || !s) return -1;
+    nqs_sampler_thermalize(s);
+    for (int it = 0; it < cfg->num_iterations; it++) {
+        nqs_sr_step_info_t info;
+        int rc = nqs_sr_step_minsr_holomorphic_full(cfg, sx, sy, a, s, fn, user, nullptr, nullptr, &info);
+        if (rc != 0) return rc;
+        if (trace) trace[it] = info.mean_energy;
+    }
+    return 0;
+}
+
 int nqs_gpu_sr_step_batch(const nqs_config_t *cfg, int sx, int sy, nqs_ansatz_t *a, nqs_log_amp_fn_t fn,
                           void *user, nqs_gradient_fn_t gfn, void *guser, const int *batch, int Ns, int minsr,
                           nqs_sr_step_info_t *info, double *out_E, double *out_delta) {
     if (!cfg || !a || !batch || Ns <= 0) return -1;
+    if (minsr < 0 || minsr > 5 || minsr == 3 || minsr == 4) {
+        set_error("nqs_gpu_sr_step_batch: minsr must be 0 (CG-SR), 1 (MinSR), 2 (holomorphic SR) or 5 "
+                  "(holomorphic MinSR)");
+        return -1;
+    }
     StepIn in{cfg, sx, sy, (Ansatz *)a, nullptr, batch, Ns, fn, user, gfn, guser, minsr};
-    if (minsr == 2 && gfn) {          // holomorphic: the callback is a holomorphic gradient
+    if ((minsr == 2 || minsr == 5) && gfn) {     // holomorphic: the callback is a holomorphic gradient
         in.hgfn = (nqs_holomorphic_gradient_fn_t)(void *)gfn;
         in.hguser = guser;
         in.gfn = nullptr;
@@ -1511,7 +1562,9 @@ int nqs_tvmc_step_heun(const nqs_config_t *cfg, double dt, int sx, int sy, nqs_a
         !NQS_CUDA(cudaMemcpyAsync(w.kacc.p, w.delta.p, sizeof(double) * P, cudaMemcpyDeviceToDevice, st)))
         return -1;
     k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.kacc.p, P, -dt, w.scal.p, w.status.p, 0);   // theta0 + dt k1
-    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a)) return -1;
+    // the probe parameters go to the host mirror too: every step starts by uploading the
+    // mirror (callers may edit the parameters in place through nqs_ansatz_params_raw)
+    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a) || !ansatz_pull(a)) return -1;
     const int rc2 = sr_step_impl(in, &i2, nullptr, nullptr);                                  // k2
     if (!NQS_CUDA(cudaMemcpyAsync(a->d_params.p, w.theta0.p, sizeof(double) * P, cudaMemcpyDeviceToDevice, st)))
         return -1;

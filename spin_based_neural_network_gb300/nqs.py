@@ -66,6 +66,8 @@ def _declare(L):
                                               DP, DP]),
         "nqs_sr_step_minsr_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_minsr": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
+        "nqs_sr_step_minsr_holomorphic_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
+        "nqs_sr_run_minsr_holomorphic": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
         "nqs_marshall_parity": (C.c_int, [IP, C.c_int, C.c_int]),
         "nqs_marshall_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
         "nqs_symproj_log_amp": (None, [IP, C.c_int, VP, DP, DP]),
@@ -421,6 +423,16 @@ def sr_step_holomorphic(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, u
     return info
 
 
+def sr_step_minsr_holomorphic(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, grad_fn=None,
+                              grad_user=None):
+    """nqs_sr_step_minsr_holomorphic_full: the holomorphic SR system solved by MinSR."""
+    info = abi.StepInfo()
+    _check(lib().nqs_sr_step_minsr_holomorphic_full(C.byref(cfg), size_x, size_y, ansatz.h, sampler.h, log_amp_fn,
+                                                    user, grad_fn, grad_user, C.byref(info)),
+           "nqs_sr_step_minsr_holomorphic_full")
+    return info
+
+
 def sr_step_cg(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None, grad_fn=None,
                grad_user=None):
     info = abi.StepInfo()
@@ -432,7 +444,7 @@ def sr_step_cg(cfg, size_x, size_y, ansatz, sampler, log_amp_fn=None, user=None,
 def sr_step_batch(cfg, size_x, size_y, ansatz, batch, minsr=True, log_amp_fn=None, user=None, grad_fn=None,
                   grad_user=None):
     """One SR step on a caller-supplied batch; returns (info, energies, delta).
-    minsr: True / 1 MinSR, False / 0 CG-SR, 2 holomorphic SR."""
+    minsr: True / 1 MinSR, False / 0 CG-SR, 2 holomorphic SR, 5 holomorphic MinSR."""
     s = spins_array(batch, ansatz.N)
     Ns = s.shape[0]
     E, d = np.zeros(Ns), np.zeros(ansatz.P)

@@ -193,3 +193,92 @@ def test_run_with_compat_sampler_matches_upstream(nqs, name):
     step = d["params1"] - d["params0"]
     assert np.linalg.norm((pb.a.params - d["params0"]) - step) <= 1e-9 * np.linalg.norm(step)
     assert s.acceptance_ratio() == pytest.approx(float(d["acceptance"]), abs=0)
+
+
+# ------------------------------------------------------------------ holomorphic MinSR
+# nqs_sr_step_minsr_holomorphic_full solves the upstream holomorphic SR system by MinSR on
+# the stacked rows [R_c; I_c].  Its update must equal the converged holomorphic CG-SR update
+# of the oracle (pinned above against nqs_sr_step_holomorphic_full) on the same batch.
+
+def _holo_minsr_case(nqs, Ns, M=16, seed=2718):
+    import oracle_lib as O
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, rbm_init_scale=0.3, rng_seed=seed,
+                              hamiltonian=abi.HAM_HEISENBERG, sr_diag_shift=1e-2, learning_rate=0.01,
+                              sr_cg_max_iters=2000, sr_cg_tol=1e-13)
+    a = nqs.Ansatz(cfg, 16)
+    m = nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    rng = np.random.default_rng(Ns + seed)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(Ns)])
+    amp = O.Amp(O.OR_CRBM, 16, M, a.params.copy(), [("marshall", Lx, Ly)])
+    Eo, do, io = O.holo_step(O.ham(O.OR_HEIS, Lx, Ly, pbc=1), amp, batch, cfg.sr_diag_shift, cfg.learning_rate,
+                             cfg.sr_cg_max_iters, cfg.sr_cg_tol)
+    assert io.converged == 1
+    return cfg, a, m, batch, Eo, do, io
+
+
+@pytest.mark.parametrize("Ns,prec,space,bar", [(512, "fp64", "samples", 1e-9), (512, "fp64", "parameters", 1e-9),
+                                               (256, "fp64", "parameters", 1e-9), (512, "mixed", "auto", 1e-6)])
+def test_holomorphic_minsr_equals_converged_holomorphic_sr(nqs, Ns, prec, space, bar):
+    """Complex RBM (N_p = 576) on the 4x4 Heisenberg torus with the Marshall sign: 2 N_s = 1024
+    or 512 stacked rows, sample- or parameter-space solve, FP64 or the mixed path."""
+    from spin_based_neural_network_gb300 import abi
+    cfg, a, m, batch, Eo, do, io = _holo_minsr_case(nqs, Ns)
+    opts = dict(square_pbc=1)
+    if prec == "mixed":
+        opts.update(precision=abi.PREC_MIXED, refine_sweeps=20)
+    else:
+        opts.update(fp64_space=abi.SPACE_PARAMETERS if space == "parameters" else 0)
+    nqs.set_options(**opts)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, 4, 4, a, batch, minsr=5, log_amp_fn=m.log_amp_fn, user=m.user)
+    finally:
+        nqs.set_options()
+    assert info.converged == 1 and info.cg_iterations == 0
+    assert np.max(np.abs(E - Eo) / np.maximum(np.abs(Eo), 1.0)) < TOL
+    assert info.mean_energy == pytest.approx(io.mean_energy, rel=TOL)
+    assert np.linalg.norm(delta - do) <= bar * np.linalg.norm(do)
+
+
+def test_holomorphic_minsr_of_a_real_rbm_is_minsr_at_half_shift(nqs):
+    """For a real RBM the imaginary rows vanish, so the holomorphic system is 2 R_c^T R_c / N_s
+    + shift I and its update equals the MinSR update with shift / 2."""
+    from spin_based_neural_network_gb300 import abi
+    N, M = 16, 16
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=M, rbm_init_scale=0.3, rng_seed=5,
+                              hamiltonian=abi.HAM_TFIM, transverse_field=0.9, sr_diag_shift=2e-3, learning_rate=0.01)
+    rng = np.random.default_rng(9)
+    batch = np.where(rng.random((384, N)) < 0.5, 1, -1).astype(np.int32)
+    a1 = nqs.Ansatz(cfg, N)
+    i1, E1, d1 = nqs.sr_step_batch(cfg, 4, 4, a1, batch, minsr=5)
+    cfg2 = abi.config_defaults(ansatz=abi.ANSATZ_RBM, rbm_hidden_units=M, rbm_init_scale=0.3, rng_seed=5,
+                               hamiltonian=abi.HAM_TFIM, transverse_field=0.9, sr_diag_shift=1e-3, learning_rate=0.01)
+    a2 = nqs.Ansatz(cfg2, N)
+    i2, E2, d2 = nqs.sr_step_batch(cfg2, 4, 4, a2, batch, minsr=1)
+    assert np.array_equal(E1, E2)
+    assert np.linalg.norm(d1 - d2) <= 1e-10 * np.linalg.norm(d2)
+
+
+def test_holomorphic_minsr_step_with_sampler(nqs):
+    """The sampled step (nqs_sr_step_minsr_holomorphic_full) lowers the energy of the complex
+    RBM on the 4x4 Heisenberg torus over a short run (nqs_sr_run_minsr_holomorphic)."""
+    import ctypes as C
+    from spin_based_neural_network_gb300 import abi
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=16, rbm_init_scale=0.05, rng_seed=9,
+                              hamiltonian=abi.HAM_HEISENBERG, num_samples=1024, num_iterations=40,
+                              sr_diag_shift=1e-3, learning_rate=0.02)
+    a = nqs.Ansatz(cfg, 16)
+    m = nqs.Marshall(a.log_amp_fn, a.user, 4, 4)
+    o = nqs.options(num_chains=256, rng=abi.RNG_PHILOX, move=abi.MOVE_EXCHANGE, n_down=8, lattice_x=4, lattice_y=4,
+                    square_pbc=1)
+    nqs.set_options(square_pbc=1)
+    try:
+        s = nqs.Sampler(16, cfg, m.log_amp_fn, m.user, o)
+        trace = np.zeros(40)
+        rc = nqs.lib().nqs_sr_run_minsr_holomorphic(C.byref(cfg), 4, 4, a.h, s.h, m.log_amp_fn, m.user,
+                                                    trace.ctypes.data_as(C.POINTER(C.c_double)))
+    finally:
+        nqs.set_options()
+    assert rc == 0 and np.all(np.isfinite(trace))
+    assert np.mean(trace[-5:]) < np.mean(trace[:5]) - 0.5
