@@ -300,6 +300,14 @@ int nqs_gpu_gram_tc(const double *O_host, int num_samples, long num_params, int 
  * tau = 1. */
 int nqs_gpu_ess(const double *energies, int num_samples, int num_chains, double *out_tau, double *out_ess);
 
+/* Test hook: the number of polls a grid-wide barrier of the cooperative solve kernels
+ * (mixed MinSR factor / refinement, CG-SR, batches) waits before it gives up; 0 restores
+ * the default (2^24).  A barrier that gives up raises the kernel's error word, every CTA
+ * leaves at its next barrier (releasing its tensor memory), and the step returns -1 with
+ * "grid barrier timed out" in nqs_gpu_last_error(); the next call starts from cleared
+ * barrier and error words. */
+int nqs_gpu_set_barrier_budget(unsigned polls);
+
 /* Statistics of the last SR step on this thread. */
 typedef struct {
     double tau_int;          /* integrated autocorrelation time of E_loc (see nqs_gpu_ess) */
@@ -313,8 +321,9 @@ typedef struct {
     int    mixed_fallback;   /* 1 if the FP32 factor failed and FP64 solved the step */
     int    pad_;
     /* MIXED: microseconds spent in the phases of the cooperative factor /
-     * inverse / CG kernel (seen from CTA 0): [0] diagonal blocks, [1] panels,
-     * [2] trailing updates, [3] triangular inverse, [4] preconditioner
+     * inverse / CG kernel (seen from CTA 0): [0] the first diagonal block, [1] panels,
+     * [2] trailing updates (each with the next diagonal block's update and factor,
+     * done by CTA 0 beside the trailing tiles), [3] triangular inverse, [4] preconditioner
      * applications, [5] right-hand side, operator products and CG updates, [6]
      * total; [7] the part of [0] spent by the owning CTAs on factoring and
      * inverting the diagonal blocks */

@@ -347,12 +347,18 @@ __device__ __forceinline__ unsigned long long gtimer() {
     return t;
 }
 
+// Polls a grid barrier waits before it gives up (raising *err = 2).  A device variable so
+// that graph replays read the current value; nqs_gpu_set_barrier_budget() lowers it for
+// the tests of the timeout path.
+__device__ unsigned g_barrier_budget = 1u << 24;
+
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned count) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = bar + 1;
         const unsigned g0 = *gen;
+        const unsigned budget = *(volatile unsigned *)&g_barrier_budget;
         __threadfence();
         if (atomicAdd(bar, 1u) == count - 1) {
             bar[0] = 0;
@@ -362,7 +368,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
             uint32_t it = 0;
             while (*gen == g0) {
                 if (*((volatile int *)err)) break;
-                if (++it > (1u << 24)) {
+                if (++it > budget) {
                     atomicExch(err, 2);
                     break;
                 }
@@ -822,10 +828,12 @@ struct TcState {
     int *err;
 };
 
-// C[i][j] -= (U^T U)[i][j] for the tile rows R0.., columns C0.. (j <= i < n);
-// returns false when a bounded wait gave up (err raised).
+// C[i][j] -= (U^T U)[i][j] for the tile rows R0.., columns C0.. (j <= i < n), except the
+// entries with i, j < skip (the next diagonal block, updated by its owner); returns false
+// when a bounded wait gave up (err raised).
 template <int BD>
-__device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, float *T, int n, int R0, int C0) {
+__device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, float *T, int n, int R0, int C0,
+                                 int skip = 0) {
     constexpr int NQ = BD / 32;
     const int tid = threadIdx.x;
     const uint32_t s0 = smem_u32(ts.sm);
@@ -902,7 +910,7 @@ __device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, 
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             const int e4 = tid + q * PS_THREADS, r = e4 >> 5, c = 4 * (e4 & 31), i = R0 + r, j = C0 + c;
-            if (i < n && j <= i) {
+            if (i < n && j <= i && !(i < skip && j < skip)) {   // skip is a multiple of 4 here
                 const float4 d = *(const float4 *)&ep[r * EP + c];
                 float4 o = make_float4(v[q].x - d.x, v[q].y - d.y, v[q].z - d.z, v[q].w - d.w);
                 if (j + 3 <= i) {
@@ -928,7 +936,7 @@ __device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, 
 #pragma unroll
             for (int q = 0; q < 32; q++) {
                 const int e = e0 + q * PS_THREADS, i = R0 + e / TT, j = C0 + e % TT;
-                if (i < n && j <= i) T[(size_t)i * n + j] = v[q] - ep[(e / TT) * EP + e % TT];
+                if (i < n && j <= i && !(i < skip && j < skip)) T[(size_t)i * n + j] = v[q] - ep[(e / TT) * EP + e % TT];
             }
         }
     }
@@ -1036,12 +1044,18 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         __syncthreads();                                    // S0 / S1 are reused as GEMM staging
         if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
     };
+    // Look-ahead: the diagonal block of step kb + 1 is updated and factored by CTA 0 during
+    // the trailing phase of step kb (64 x 64 SIMT tiles of U_kb^T U_kb over its lower
+    // triangle, then factor_diag), while the other CTAs update the trailing tiles, the
+    // first of which leaves that block's entries to CTA 0.  So each step has two grid
+    // barriers (after the panel and after the trailing update) and the block's factor runs
+    // beside the trailing tiles instead of in a phase of its own.
+    if (bx == 0) factor_diag(0);
+    if (!grid_barrier(a.bar, a.err, G)) return;
+    if (__ldcg(a.status) >= 0) return;                      // broken factor: every CTA leaves here
+    NQS_PHASE(0);
     for (int kb = 0; kb < nb; kb++) {
         const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
-        if (bx == kb % G) factor_diag(kb);
-        if (!grid_barrier(a.bar, a.err, G)) return;
-        if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
-        NQS_PHASE(0);
         if (rest <= 0) break;
         // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1
         {
@@ -1076,18 +1090,39 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(1);
-        // trailing update (look-ahead of the next diagonal block was tried: one
-        // CTA updating that block's three 64 x 64 tiles alone costs more than
-        // the trailing phase it hides)
+        // trailing update, with the next diagonal block updated and factored by CTA 0
         {
+            const int bs1 = min(BD, rest);                  // order of the next diagonal block
+            if (bx == 0) {
+                // D -= U_kb^T U_kb on the lower 64 x 64 tiles of the next diagonal block, FP32
+                // from U (= L^T, the upper triangle rows k0 .. k0 + bs - 1 of T)
+                const float *U = a.T + (size_t)k0 * n;
+                for (int ti = 0; ti * GT < bs1; ti++)
+                    for (int tj = 0; tj <= ti; tj++) {
+                        float acc[4][4] = {};
+                        gemm64<true, true>(acc, U, n, k1 + ti * GT, k1 + bs1, U, n, k1 + tj * GT, k1 + bs1, 0, bs, TS);
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+#pragma unroll
+                            for (int v = 0; v < 4; v++) {
+                                const int i = k1 + ti * GT + ty + 16 * u, j = k1 + tj * GT + tx + 16 * v;
+                                if (i < k1 + bs1 && j <= i) a.T[(size_t)i * n + j] -= acc[u][v];
+                            }
+                        __syncthreads();
+                    }
+                factor_diag(kb + 1);
+            }
             const int ntt = (rest + TT - 1) / TT, ntiles = ntt * (ntt + 1) / 2;
-            for (int t = bx; t < ntiles; t += G) {
+            const int t0 = G > 1 ? bx - 1 : 0, dt = G > 1 ? G - 1 : 1;
+            for (int t = t0; t >= 0 && t < ntiles; t += dt) {
                 int bi, bj;
                 tri_tile(t, bi, bj);
-                if (!trailing_tile_tc<BD>(ts, a.uh, a.ul, a.T, n, k1 + bi * TT, k1 + bj * TT)) return;
+                if (!trailing_tile_tc<BD>(ts, a.uh, a.ul, a.T, n, k1 + bi * TT, k1 + bj * TT, t == 0 ? k1 + bs1 : 0))
+                    return;
             }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
+        if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
         NQS_PHASE(2);
     }
 
@@ -2031,6 +2066,17 @@ extern "C" {
 // Diagnostic: the tensor-core Gram alone on a host matrix O [Ns][P] (FP64,
 // used as given, i.e. already centred): T_out [Ns][Ns] (lower triangle) =
 // scale * (hi hi^T [+ hi lo^T + lo hi^T]).
+int nqs_gpu_set_barrier_budget(unsigned polls) {
+    clear_error();
+    if (!ensure_context()) return -1;
+    const unsigned v = polls ? polls : (1u << 24);
+    cudaStream_t st = ctx().stream;
+    return NQS_CUDA(cudaMemcpyToSymbolAsync(g_barrier_budget, &v, sizeof(v), 0, cudaMemcpyHostToDevice, st)) &&
+                   NQS_CUDA(cudaStreamSynchronize(st))
+               ? 0
+               : -1;
+}
+
 int nqs_gpu_gram_tc(const double *O_host, int Ns, long P, int passes, double scale, float *T_out) {
     clear_error();
     if (!O_host || !T_out || Ns <= 0 || P <= 0) return -1;

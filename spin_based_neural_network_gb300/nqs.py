@@ -66,6 +66,7 @@ def _declare(L):
                                               DP, DP]),
         "nqs_sr_step_minsr_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_minsr": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
+        "nqs_gpu_set_barrier_budget": (C.c_int, [C.c_uint]),
         "nqs_sr_step_minsr_holomorphic_full": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP, infop]),
         "nqs_sr_run_minsr_holomorphic": (C.c_int, [cfgp, C.c_int, C.c_int, VP, VP, VP, VP, DP]),
         "nqs_marshall_parity": (C.c_int, [IP, C.c_int, C.c_int]),
