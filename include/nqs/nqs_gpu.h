@@ -143,8 +143,10 @@ int nqs_gpu_made_sample(nqs_sampler_t *s, int count, int *out_spins, double *out
  * The refinement sweeps, Gram passes and solve space are taken from the process
  * options at creation.  The factor / inverse / refinement of all instances run
  * in ONE cooperative launch whose CTAs are split between the instances by an
- * autotuner on the first step (nqs_gpu_batch_ctas reports the split,
- * nqs_gpu_batch_tune_ms the candidates' times); from the second step the whole
+ * autotuner on the first step, which also picks the factor's tile shape (the
+ * diagonal block width, 64 or 128, by instance order) (nqs_gpu_batch_ctas reports
+ * the split, nqs_gpu_batch_block_widths the widths, nqs_gpu_batch_tune_ms the
+ * candidates' times: every CTA split for each width rule); from the second step the whole
  * batch step is one CUDA graph replayed per step.  An instance whose FP32
  * factor breaks down is solved again in FP64 on the same samples after the
  * graph (as nqs_sr_step_minsr_full does in the MIXED mode);
@@ -165,6 +167,8 @@ nqs_gpu_batch_t *nqs_gpu_batch_create(const nqs_gpu_instance_t *instances, int c
 int nqs_gpu_batch_step(nqs_gpu_batch_t *b, nqs_sr_step_info_t *infos);
 int nqs_gpu_batch_ctas(const nqs_gpu_batch_t *b, int *out_ctas);
 int nqs_gpu_batch_tune_ms(const nqs_gpu_batch_t *b, double *out_ms, int cap);
+/* The factor's diagonal block width (64 or 128) the autotuner chose for each instance. */
+int nqs_gpu_batch_block_widths(const nqs_gpu_batch_t *b, int *out_bd);
 long nqs_gpu_batch_fallbacks(const nqs_gpu_batch_t *b);
 void nqs_gpu_batch_free(nqs_gpu_batch_t *b);
 

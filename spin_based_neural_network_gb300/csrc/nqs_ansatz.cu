@@ -106,7 +106,7 @@ static void init_params(const nqs_config_t *cfg, int kind, int N, int M, double 
 // Transposed weight copies: RBM/cRBM W[h][i] -> wt[i][h]; MLP W1 -> W1^T, W2 -> W2^T.
 // RBM / cRBM also get the FP32 tables of the mixed-precision estimator:
 // f32 = [W^T | cosh(2 W^T) | sinh(2 W^T)] ([N][M] each), a [N], b [M], complex.
-__global__ void k_derive(DevAnsatz a, double *wtr, double *wti, float2 *f32) {
+__global__ void k_derive(DevAnsatz a, double *wtr, double *wti, float2 *f32, double *cs64) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int N = a.N, M = a.M;
     if (a.kind == KIND_RBM || a.kind == KIND_CRBM) {
@@ -123,6 +123,13 @@ __global__ void k_derive(DevAnsatz a, double *wtr, double *wti, float2 *f32) {
         f32[(long)i * M + h] = make_float2((float)x, (float)y);
         f32[NM + (long)i * M + h] = make_float2((float)(c2x * c2y), (float)(s2x * s2y));
         f32[2 * NM + (long)i * M + h] = make_float2((float)(s2x * c2y), (float)(c2x * s2y));
+        if (cs64) {
+            const long q = (long)i * M + h;
+            cs64[q] = c2x * c2y;                 // cosh(2 W) = cosh 2x cos 2y + i sinh 2x sin 2y
+            cs64[NM + q] = s2x * s2y;
+            cs64[2 * NM + q] = s2x * c2y;        // sinh(2 W) = sinh 2x cos 2y + i cosh 2x sin 2y
+            cs64[3 * NM + q] = c2x * s2y;
+        }
         if (t < N) f32[3 * NM + t] = make_float2((float)a.p[t], cx ? (float)a.p[Pr + t] : 0.f);
         if (t < M) f32[3 * NM + N + t] = make_float2((float)a.p[N + t], cx ? (float)a.p[Pr + N + t] : 0.f);
     } else if (a.kind == KIND_MLP) {
@@ -262,6 +269,7 @@ DevAnsatz ansatz_dev(const Ansatz *a) {
     d.a32 = rbm ? a->d_f32.p + 3 * NM : nullptr;
     d.b32 = rbm ? a->d_f32.p + 3 * NM + a->N : nullptr;
     d.m32 = a->kind == KIND_MLP ? (const float *)a->d_f32.p : nullptr;
+    d.cs64 = rbm ? a->d_cs64.p : nullptr;
     return d;
 }
 
@@ -275,7 +283,7 @@ bool ansatz_refresh_derived(Ansatz *a) {
     long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * mlp32_pitch(a->M) : (long)a->M * a->N;
     NQS_LAUNCH("derive_weights");
     k_derive<<<(unsigned)((work + 255) / 256), 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
-                                                                        a->d_wti.p, a->d_f32.p);
+                                                                        a->d_wti.p, a->d_f32.p, a->d_cs64.p);
     return NQS_CUDA(cudaGetLastError());
 }
 
@@ -910,7 +918,8 @@ nqs_ansatz_t *nqs_ansatz_create(const nqs_config_t *cfg, int num_sites) {
                                       : (size_t)num_sites * (M ? M : 1)) ||
         !a->d_wti.ensure(kind == KIND_MLP ? (size_t)M * M : (size_t)num_sites * (M ? M : 1)) ||
         !a->d_f32.ensure(kind == KIND_MLP ? (mlp32_floats(num_sites, M) + 1) / 2
-                                          : 3 * (size_t)num_sites * (M ? M : 1) + num_sites + (M ? M : 1))) {
+                                          : 3 * (size_t)num_sites * (M ? M : 1) + num_sites + (M ? M : 1)) ||
+        ((kind == KIND_RBM || kind == KIND_CRBM) && !a->d_cs64.ensure(4 * (size_t)num_sites * M))) {
         nqs_ansatz_free((nqs_ansatz_t *)a);
         return nullptr;
     }

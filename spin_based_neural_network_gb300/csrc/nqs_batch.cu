@@ -56,6 +56,7 @@ struct Batch {
     std::vector<BatchInst *> inst;
     MixedBatch *mb = nullptr;
     std::vector<int> ctas;
+    int bd_from = 0;                     // systems of order >= bd_from use 128-wide diagonal blocks
     std::vector<double> tune_ms;
     cudaGraphExec_t exec = nullptr;
     long graph_kernels = 0;
@@ -178,8 +179,10 @@ static std::vector<std::vector<int>> cta_candidates(const Batch &B, int cap) {
 }
 
 // Autotune on the Grams of the first step: re-run each instance's Gram from
-// its split operands and time the cooperative launch for every candidate;
-// keep the fastest (its launch, after a last Gram, is the step's solve).
+// its split operands and time the cooperative launch for every candidate CTA
+// split and every tile shape of the factor (the diagonal block width: 128 from
+// order 4096, from 2048, from 1024, else 64); keep the fastest (its launch, after
+// a last Gram, is the step's solve).
 static bool autotune(Batch &B, cudaStream_t st) {
     const int cap = mixed_batch_capacity();
     if (cap < (int)B.inst.size()) {
@@ -190,18 +193,21 @@ static bool autotune(Batch &B, cudaStream_t st) {
     std::vector<MixedSys *> sys;
     for (BatchInst *b : B.inst) sys.push_back(b->mx);
     const std::vector<std::vector<int>> cand = cta_candidates(B, cap);
+    const int bd_cand[3] = {mixed_bd_default(), 2048, 1024};
     cudaEvent_t e0, e1;
     if (!NQS_CUDA(cudaEventCreate(&e0)) || !NQS_CUDA(cudaEventCreate(&e1))) return false;
     double best = 1e300;
-    int bi = -1;
+    int bi = -1, bb = 0;
     B.tune_ms.clear();
-    for (size_t c = 0; c < cand.size(); c++) {
-        MixedBatch *mb = mixed_batch_create(sys.data(), (int)sys.size(), cand[c].data());
+    for (size_t k = 0; k < cand.size() * 3; k++) {
+        const size_t c = k % cand.size();
+        const int t = (int)(k / cand.size());
+        MixedBatch *mb = mixed_batch_create(sys.data(), (int)sys.size(), cand[c].data(), bd_cand[t]);
         if (!mb) {
             B.tune_ms.push_back(-1.0);
             continue;
         }
-        if (c > 0)
+        if (k > 0)
             for (BatchInst *b : B.inst) mixed_sys_front(b->mx, st, false);
         float ms = 0.f;
         const bool ok = NQS_CUDA(cudaEventRecord(e0, st)) && mixed_batch_launch(mb, st) &&
@@ -213,13 +219,15 @@ static bool autotune(Batch &B, cudaStream_t st) {
         if (ms < best) {
             best = ms;
             bi = (int)c;
+            bb = bd_cand[t];
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (bi < 0) return false;
     B.ctas = cand[bi];
-    B.mb = mixed_batch_create(sys.data(), (int)sys.size(), B.ctas.data());
+    B.bd_from = bb;
+    B.mb = mixed_batch_create(sys.data(), (int)sys.size(), B.ctas.data(), B.bd_from);
     if (!B.mb) return false;
     for (BatchInst *b : B.inst) mixed_sys_front(b->mx, st, false);
     return mixed_batch_launch(B.mb, st);
@@ -411,6 +419,13 @@ int nqs_gpu_batch_step(nqs_gpu_batch_t *h, nqs_sr_step_info_t *infos) {
 int nqs_gpu_batch_ctas(const nqs_gpu_batch_t *h, int *out) {
     if (!h || !out || h->b.ctas.empty()) return -1;
     for (size_t i = 0; i < h->b.ctas.size(); i++) out[i] = h->b.ctas[i];
+    return 0;
+}
+
+int nqs_gpu_batch_block_widths(const nqs_gpu_batch_t *b, int *out_bd) {
+    if (!b || !out_bd || b->b.ctas.empty()) return -1;
+    for (size_t i = 0; i < b->b.inst.size(); i++)
+        out_bd[i] = mixed_sys_order(b->b.inst[i]->mx) >= b->b.bd_from ? 128 : 64;
     return 0;
 }
 

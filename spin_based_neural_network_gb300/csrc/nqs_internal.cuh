@@ -151,6 +151,9 @@ struct DevAnsatz {
     // rows padded with zeros to MP = 32 ceil(M / 32), then b1, b2, w_re, w_im
     // [M], c_re, c_im
     const float *m32;
+    // FP64 tables of the RBM / cRBM for the product-form FP64 chains: cosh(2 W^T) (re, im)
+    // then sinh(2 W^T) (re, im), each [N][M]
+    const double *cs64;
 };
 
 struct DevAmp {
@@ -183,6 +186,7 @@ struct Ansatz {
     double *h_shadow = nullptr;     // last value known to be on the device
     DevBuf<double> d_params, d_wtr, d_wti;
     DevBuf<float2> d_f32;           // RBM / cRBM / MLP FP32 tables (see DevAnsatz)
+    DevBuf<double> d_cs64;          // RBM / cRBM FP64 cosh / sinh(2 W^T) tables (see DevAnsatz)
     bool dev_valid = false;
 };
 
@@ -257,7 +261,8 @@ const int *mixed_sys_status(const MixedSys *m);
 const int *mixed_sys_err(const MixedSys *m);
 const double *mixed_sys_nrm(const MixedSys *m);
 int mixed_batch_capacity();
-MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas);
+MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas, int bd_from);
+int mixed_bd_default();
 void mixed_batch_free(MixedBatch *b);
 bool mixed_batch_launch(MixedBatch *b, cudaStream_t st);
 

@@ -504,6 +504,73 @@ __device__ int block_chol(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s
     return -1;
 }
 
+// The 64 x 64 diagonal block in one right-looking sweep by the whole CTA: at step j the
+// pivot L_jj = sqrt(S_jj), the column l_i = S_ij / L_jj and the row x_c = R_jc / L_jj of
+// X = L^{-1} are formed by 128 threads into shared vectors, then every thread updates
+// its 4 x 4 tile of S (S_ic -= l_i l_c, j < c <= i) and of R (R_ic -= l_i x_c, i > j,
+// c <= j), where R = I - L X over the columns eliminated so far (forward substitution of
+// L X = I, right-looking): two block barriers per column and all 256 threads busy,
+// instead of the warp-serial 32-column sub-panels of block_chol / block_inv.  S (rows >= bs
+// padded with the identity) is consumed; X is left in the lower triangle of X (zeros
+// above).  Returns the first non-positive pivot column below bs or -1 (the sweep goes on
+// with a unit pivot; the caller discards the block).
+__device__ int block_chol_inv64(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s_flag, float *lv) {
+    const int tid = threadIdx.x;
+    const int ti = tid >> 4, tj = tid & 15;              // 4 x 4 tile: rows 4 ti.., cols 4 tj..
+    float *xv = lv + 64;
+    for (int e = tid; e < 64 * 64; e += PS_THREADS) X[e >> 6][e & 63] = (e >> 6) == (e & 63) ? 1.f : 0.f;
+    if (tid == 0) *s_flag = -1;
+    __syncthreads();
+    for (int j = 0; j < 64; j++) {
+        if (tid < 128) {
+            const float d = S[j][j];
+            const bool ok = d > 0.f;
+            const float inv = rsqrtf(ok ? d : 1.f);
+            if (tid < 64) {
+                const int i = tid;
+                lv[i] = i > j ? S[i][j] * inv : (i == j ? (ok ? d : 1.f) * inv : 0.f);
+                if (i == 0 && !ok && j < bs && *s_flag < 0) *s_flag = j;
+            } else {
+                const int c = tid - 64;
+                const float x = c <= j ? X[j][c] * inv : 0.f;
+                xv[c] = x;
+                X[j][c] = x;                              // row j of R becomes row j of X
+            }
+        }
+        __syncthreads();
+        const int r0 = 4 * ti, c0 = 4 * tj;
+        if (r0 + 3 > j) {                                 // rows of this tile below the pivot
+            float li[4], lc[4], xc[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                li[u] = lv[r0 + u];
+                lc[u] = lv[c0 + u];
+                xc[u] = xv[c0 + u];
+            }
+            if (c0 + 3 > j && c0 <= r0 + 3) {             // S: j < c <= i
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int i = r0 + u, c = c0 + v;
+                        if (c > j && c <= i) S[i][c] = fmaf(-li[u], lc[v], S[i][c]);
+                    }
+            }
+            if (c0 <= j) {                                // R: i > j, c <= j
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int i = r0 + u, c = c0 + v;
+                        if (i > j && c <= j) X[i][c] = fmaf(-li[u], xc[v], X[i][c]);
+                    }
+            }
+        }
+        __syncthreads();
+    }
+    return *s_flag;
+}
+
 // Off-diagonal 32-blocks of X = L^{-1} inside the 128-block (the diagonal
 // 32-blocks are already in X): for d = 1..3, X_ba = -X_bb (sum_{m=a}^{b-1}
 // L_bm X_ma), b = a + d, all pairs of one block diagonal computed by the CTA,
@@ -1025,14 +1092,14 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
             }
         }
         __syncthreads();
-        const int f = block_chol<BD>(S0, S1, bs, &s_flag, tmpb);
+        const int f = BD == 64 ? block_chol_inv64(S0, S1, bs, &s_flag, tmpb) : block_chol<BD>(S0, S1, bs, &s_flag, tmpb);
         if (f >= 0) {
             if (tid == 0) {
                 a.status[0] = k0 + f;
                 __threadfence();
             }
         } else {
-            block_inv<BD>(S0, S1, tmpb);
+            if (BD != 64) block_inv<BD>(S0, S1, tmpb);
             for (int e = tid; e < BD * BD; e += PS_THREADS) {
                 const int rr = e / BD, q = e % BD;
                 if (rr < bs && q < bs) {
@@ -1646,8 +1713,9 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
     const void *before[18] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
                               w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p};
     const int ldl = (n + 31) / 32 * 32;
-    // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero
-    const size_t nu = (size_t)(n + TT) * (n >= BD_SWITCH ? BD_LARGE : BD_SMALL);
+    // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero.
+    // Sized for the wide diagonal block so a batch's autotuner can pick either width.
+    const size_t nu = (size_t)(n + TT) * BD_LARGE;
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
         !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
@@ -1917,8 +1985,15 @@ bool cg_sr_solve(const double *O, int Ns, long P, const double *F, const double 
         set_error("CG kernel does not fit on an SM");
         return false;
     }
+    // one CTA per 256 KB of Jacobian (at least 8, at most one per SM): a small system
+    // (the 1-D TFIM chain: 1024 x 288, 2.4 MB) then synchronises 10 CTAs instead of 152 at
+    // its five grid barriers per iteration; the dot products run in every CTA in a fixed
+    // order and the column sums are reduced over fixed row chunks, so the result does not
+    // depend on the grid size
+    const double jac_bytes = 8.0 * (double)Ns * (double)P * (O2 ? 2.0 : 1.0);
+    const int grid = std::max(8, std::min(c.sm_count, (int)std::ceil(jac_bytes / (256.0 * 1024.0))));
     cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3((unsigned)c.sm_count);
+    lc.gridDim = dim3((unsigned)grid);
     lc.blockDim = dim3(PS_THREADS);
     lc.dynamicSmemBytes = 0;
     lc.stream = st;
@@ -1988,6 +2063,7 @@ void mixed_sys_front(MixedSys *m, cudaStream_t st, bool with_split) {
 }
 
 bool mixed_sys_param_space(const MixedSys *m) { return m->pl.space == 1; }
+int mixed_bd_default() { return BD_SWITCH; }
 int mixed_sys_order(const MixedSys *m) { return m->pl.n; }
 const int *mixed_sys_status(const MixedSys *m) { return m->w.status.p; }
 const int *mixed_sys_err(const MixedSys *m) { return m->err.p; }
@@ -2008,11 +2084,14 @@ int mixed_batch_capacity() {
     return per_sm * ctx().sm_count;
 }
 
-MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas) {
+// bd_from: systems of order >= bd_from factor with 128-wide diagonal blocks, the others
+// with 64-wide ones (a tile shape the batch autotuner chooses).
+MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas, int bd_from) {
     std::vector<FrArgs> fa((size_t)count);
     std::vector<int> c0((size_t)count), nc((size_t)count), map;
     for (int i = 0; i < count; i++) {
         fa[i] = sys[i]->fa;
+        fa[i].bd = sys[i]->pl.n >= bd_from ? BD_LARGE : BD_SMALL;
         c0[i] = (int)map.size();
         nc[i] = ctas[i] > 0 ? ctas[i] : 1;
         for (int k = 0; k < nc[i]; k++) map.push_back(i);

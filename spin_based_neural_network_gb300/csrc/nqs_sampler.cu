@@ -210,6 +210,113 @@ __global__ void __launch_bounds__(32 * kSW) k_sample_rbm(SampleArgs S, DevAmp A)
     }
 }
 
+// ---------------------------------------------------------------- FP64 product-form chains
+// Philox single-flip chains in FP64 without a transcendental per hidden unit: flipping
+// site u moves theta_h by -2 s_u W_uh, and cosh(theta - d) / cosh(theta) = cosh d -
+// tanh(theta) sinh d with cosh d = cosh(2 W_uh), sinh d = s_u sinh(2 W_uh) from the
+// tables rebuilt after every update, so |psi(s') / psi(s)|^2 = exp(-4 s_u Re a_u)
+// prod_h |cosh 2W_uh - s_u t_h sinh 2W_uh|^2 is a complex multiply-add per hidden unit
+// and a warp product; t_h = tanh(theta_h) is recomputed for accepted moves only.  The
+// acceptance is the log form's (ratio >= 1, else the uniform of the same Philox word below
+// the ratio), so the chain is the same Markov chain.
+__device__ __forceinline__ void ctanh64(double x, double y, double &tr, double &ti) {
+    if (fabs(x) > 20.0) {                       // tanh(x + iy) -> sign(x) to double precision
+        tr = x > 0.0 ? 1.0 : -1.0;
+        ti = 0.0;
+        return;
+    }
+    double s2, c2;
+    sincos(2.0 * y, &s2, &c2);
+    const double den = cosh(2.0 * x) + c2;
+    tr = sinh(2.0 * x) / den;
+    ti = s2 / den;
+}
+
+template <int J, bool CPLX>
+__global__ void __launch_bounds__(32 * kSW) k_sample_rbm_prod(SampleArgs S, DevAmp A) {
+    if (S.move_dev) S.move0 = *S.move_dev;
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kSW + (threadIdx.x >> 5);
+    if (c >= S.C) return;
+    const DevAnsatz &a = A.a;
+    const int M = a.M;
+    const long NM = (long)a.N * M;
+    const double *c2r = a.cs64, *c2i = c2r + NM, *s2r = c2i + NM, *s2i = s2r + NM;
+    const double *aR = a.p;
+    uint64_t s = S.bits[c];
+    double thr[J], thi[J], tr[J], ti[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const int h = lane + 32 * j;
+        thr[j] = thi[j] = tr[j] = ti[j] = 0.0;
+        if (h < M) {
+            rbm_theta(a, s, h, thr[j], thi[j]);
+            if (CPLX) ctanh64(thr[j], thi[j], tr[j], ti[j]);
+            else tr[j] = tanh(thr[j]);
+        }
+    }
+    const int per = S.decor > 0 ? S.decor : 1;
+    unsigned long long acc = 0, pro = 0;
+    for (int t = 0; t < S.total; t++) {
+        const uint64_t m = S.move0 + (uint64_t)t;
+        const uint4 r = philox4x32(make_uint4((uint32_t)c, (uint32_t)m, (uint32_t)(m >> 32), 0u),
+                                   make_uint2((uint32_t)S.seed, (uint32_t)(S.seed >> 32)));
+        const int u = (int)(((uint64_t)r.x * (uint64_t)S.N) >> 32);
+        pro++;
+        const double su = (double)spin_of(s, u);
+        double q = 1.0;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int h = lane + 32 * j;
+            if (h < M) {
+                const long k = (long)u * M + h;
+                const double sr = su * s2r[k];
+                double fr = fma(-tr[j], sr, c2r[k]), fi = 0.0;
+                if (CPLX) {
+                    const double si = su * s2i[k];
+                    fr = fma(ti[j], si, fr);                       // Re(c - t s)
+                    fi = c2i[k] - fma(tr[j], si, ti[j] * sr);      // Im(c - t s)
+                }
+                q *= fr * fr + fi * fi;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) q *= __shfl_xor_sync(0xffffffffu, q, o);
+        const double R = q * exp(-4.0 * su * aR[u]);
+        bool accept = R >= 1.0;
+        if (!accept) {
+            const uint64_t u53 = ((((uint64_t)r.z) << 32) | r.w) >> 11;
+            accept = (double)u53 * (1.0 / 9007199254740992.0) < R;
+        }
+        if (accept) {
+            acc++;
+#pragma unroll
+            for (int j = 0; j < J; j++) {
+                const int h = lane + 32 * j;
+                if (h < M) {
+                    thr[j] -= 2.0 * su * a.wtr[(long)u * M + h];
+                    if (CPLX) {
+                        thi[j] -= 2.0 * su * a.wti[(long)u * M + h];
+                        ctanh64(thr[j], thi[j], tr[j], ti[j]);
+                    } else {
+                        tr[j] = tanh(thr[j]);
+                    }
+                }
+            }
+            s ^= 1ull << u;
+        }
+        if (t >= S.skip && ((t - S.skip + 1) % per) == 0) {
+            const long idx = (long)((t - S.skip + 1) / per - 1) * S.C + c;
+            if (idx < S.n_out && lane == 0) S.out[idx] = s;
+        }
+    }
+    if (lane == 0) {
+        S.bits[c] = s;
+        atomicAdd(&S.counts[0], acc);
+        atomicAdd(&S.counts[1], pro);
+    }
+}
+
 // ---------------------------------------------------------------- FP32 chains
 // Mixed-precision variant (Philox chains only).  The acceptance needs
 // log|psi'/psi| = sum_h log|cosh(delta_h) - t_h sinh(delta_h)| + Re(visible
@@ -666,6 +773,25 @@ static bool dispatch(const SampleArgs &S, const DevAmp &A, bool f32, const DevMa
                 return false;
         }
 #undef NQS_FCASE
+        return NQS_CUDA(cudaGetLastError());
+    }
+    if (fused && RNG == NQS_GPU_RNG_PHILOX && MOVE == NQS_GPU_MOVE_SINGLE_FLIP && A.a.cs64) {
+        const int J = (A.a.M + 31) / 32;
+        const bool cx = A.a.kind == KIND_CRBM;
+        NQS_LAUNCH("sampler");
+#define NQS_PCASE(JJ)                                                             \
+    case JJ:                                                                      \
+        if (cx) k_sample_rbm_prod<JJ, true><<<grid, block, 0, st>>>(S, A);        \
+        else k_sample_rbm_prod<JJ, false><<<grid, block, 0, st>>>(S, A);          \
+        break;
+        switch (J) {
+            NQS_PCASE(1) NQS_PCASE(2) NQS_PCASE(3) NQS_PCASE(4) NQS_PCASE(5) NQS_PCASE(6) NQS_PCASE(7)
+            NQS_PCASE(8)
+            default:
+                set_error("hidden width %d unsupported", A.a.M);
+                return false;
+        }
+#undef NQS_PCASE
         return NQS_CUDA(cudaGetLastError());
     }
     if (fused) {

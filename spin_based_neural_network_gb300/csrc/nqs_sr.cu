@@ -1176,6 +1176,12 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             } else {
                 ss.mixed_fallback = 1;          // FP32 factor failed: solve this step in FP64
                 have_delta = false;
+                if (hm && P < rows) {
+                    // holomorphic MinSR: the stacked sample space (2 N_s) is the larger system;
+                    // the FP64 solve takes the parameter-space one (no upstream retry order to keep)
+                    if (minsr_fp64_params(w.O.p, w.eps.p, rows, P, shift, w.delta.p, &converged) != 0) return -1;
+                    solved = have_delta = true;
+                }
             }
         } else {
             if (!hm) {

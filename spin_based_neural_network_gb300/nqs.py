@@ -123,6 +123,7 @@ def _declare(L):
         "nqs_gpu_batch_step": (C.c_int, [C.c_void_p, C.POINTER(abi.StepInfo)]),
         "nqs_gpu_batch_ctas": (C.c_int, [C.c_void_p, IP]),
         "nqs_gpu_batch_tune_ms": (C.c_int, [C.c_void_p, DP, C.c_int]),
+        "nqs_gpu_batch_block_widths": (C.c_int, [C.c_void_p, IP]),
         "nqs_gpu_batch_free": (None, [C.c_void_p]),
         "nqs_gpu_batch_fallbacks": (C.c_long, [C.c_void_p]),
         "nqs_gpu_made_options_default": (abi.MadeOptions, []),
@@ -622,9 +623,15 @@ class Batch:
         return list(out)
 
     def tune_ms(self):
-        out = (C.c_double * 16)()
-        n = lib().nqs_gpu_batch_tune_ms(self.h, out, 16)
+        out = (C.c_double * 96)()
+        n = lib().nqs_gpu_batch_tune_ms(self.h, out, 96)
         return list(out)[:max(n, 0)]
+
+    def block_widths(self):
+        """Diagonal block width (64 / 128) of each instance's factor, as autotuned."""
+        out = np.zeros(len(self.items), dtype=np.int32)
+        _check(lib().nqs_gpu_batch_block_widths(self.h, _ip(out)), "nqs_gpu_batch_block_widths")
+        return out.tolist()
 
     def fallbacks(self):
         """Instance steps whose FP32 factor broke down and were solved in FP64."""

@@ -396,3 +396,24 @@ def test_tvmc_heun_against_upstream():
     assert i1.mean_energy == pytest.approx(ref[0], rel=1e-12)
     assert i1.cg_iterations + i2.cg_iterations == int(ref[4])
     assert np.linalg.norm(0.5 * (k1 + k2)) * dt == pytest.approx(ref[2], rel=1e-10)
+
+
+def test_batch_exact_tfim_chains_match_free_fermions():
+    """The TFIM chain instances of the multi-instance fixture (periodic, J = 1, N up to 24)
+    against the free-fermion closed form of H = -sum s_i s_{i+1} - h sum sigma^x_i:
+    E0 = -sum_{n=0}^{N-1} sqrt(1 + h^2 - 2 h cos(pi (2n + 1) / N)) (Jordan-Wigner, even parity
+    sector; h = 1 gives the -2 / sin(pi / 2N) of the critical ring)."""
+    import json
+    with open(os.path.join(GOLD, "batch_exact_energies.json")) as f:
+        rec = json.load(f)
+    checked = 0
+    for v in rec.values():
+        sp = v["spec"]
+        if sp["kind"] != "tfim" or sp["Ly"] != 1:
+            continue
+        N, h = sp["N"], sp["h"]
+        k = np.pi * (2 * np.arange(N) + 1) / N
+        e0 = -np.sum(np.sqrt(1.0 + h * h - 2.0 * h * np.cos(k)))
+        assert v["E0"] == pytest.approx(e0, rel=1e-10, abs=1e-10), (sp, v["E0"], e0)
+        checked += 1
+    assert checked >= 5
