@@ -516,7 +516,7 @@ def multi_instance(nqs, abi, L, base_opts, timed, total, learned=False, cpu=Fals
     cooperative launch for all solves with an autotuned CTA split, the whole
     batch step replayed as a CUDA graph from the second step.  Throughput over
     `timed` steps after 3 warm-up steps; then the optimisation continues to
-    `total` steps and each instance with an exact energy (N <= 20,
+    `total` steps and each instance with an exact energy (N <= 24,
     tests/golden/batch_exact_energies.json) reports |E/N - E0/N| of its energy
     averaged over the last 20 steps."""
     import numpy as np

@@ -74,7 +74,9 @@ typedef struct {
                           * NQS_GPU_SPACE_SMALLER = parameters when N_p < N_s.  A failed
                           * parameter-space factorisation is retried once with the shift
                           * raised by 1e-6, then delta = 0 and converged = 0 */
-    int reserved[1];
+    int mlp_simt;        /* MIXED, MLP ansatz: 1 = the second layer of the local energies'
+                          * connected configurations as SIMT GEMVs; 0 (default) = on the
+                          * tensor cores (tcgen05 TF32, three hi / lo passes, FP32 accumulate) */
 } nqs_gpu_options_t;
 
 /* Defaults: compat sampler, single flips, open lattices, FP64. */

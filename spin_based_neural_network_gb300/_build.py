@@ -17,7 +17,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnqs_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["nqs_context.cu", "nqs_ansatz.cu", "nqs_local_energy.cu", "nqs_sampler.cu", "nqs_sr.cu",
-           "nqs_mixed.cu", "nqs_made.cu", "nqs_batch.cu", "nqs_ed.cu"]
+           "nqs_mixed.cu", "nqs_made.cu", "nqs_batch.cu", "nqs_ed.cu", "nqs_mlp_tc.cu"]
 
 
 def nvcc():

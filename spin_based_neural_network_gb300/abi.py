@@ -145,7 +145,7 @@ class GpuOptions(C.Structure):
         ("mixed_check", C.c_int),
         ("fp32_estimator", C.c_int),
         ("fp64_space", C.c_int),
-        ("reserved", C.c_int * 1),
+        ("mlp_simt", C.c_int),
     ]
 
 

@@ -262,6 +262,9 @@ const int *mixed_sys_err(const MixedSys *m);
 const double *mixed_sys_nrm(const MixedSys *m);
 int mixed_batch_capacity();
 MixedBatch *mixed_batch_create(MixedSys *const *sys, int count, const int *ctas, int bd_from);
+// MLP local energies with the second layer on the tensor cores (nqs_mlp_tc.cu)
+bool mlp_tc_capable(const DevAmp &A, const DevHam &H);
+bool launch_mlp_eloc_tc(const DevAmp &A, const DevHam &H, const uint64_t *bits, int B, double *Er, double *Ei);
 int mixed_bd_default();
 void mixed_batch_free(MixedBatch *b);
 bool mixed_batch_launch(MixedBatch *b, cudaStream_t st);

@@ -657,7 +657,9 @@ k_local_mlp32(DevAmp A, DevHam H, const uint64_t *__restrict__ bits, int B, doub
     };
 
     float e_re = 0.f, e_im = 0.f;
-    if (H.kind == NQS_HAM_TFIM) {
+    if (!Er && !Ei) {
+        // Jacobian rows only (the local energies come from the tensor-core kernel)
+    } else if (H.kind == NQS_HAM_TFIM) {
         for (int k = 0; k < H.nb1; k++)
             e_re += -(float)H.J * (float)(spin_of(s, H.b1[2 * k]) * spin_of(s, H.b1[2 * k + 1]));
         for (int i = 0; i < N; i++) {
@@ -790,6 +792,17 @@ bool launch_local_estimator(const DevAmp &A, const DevHam &H, const uint64_t *bi
         return false;
     }
     if (fp32 && fp32_mlp_capable(A) && grad_mode != 2) {
+        if ((Er || Ei) && !ctx().opts.mlp_simt && mlp_tc_capable(A, H)) {
+            // local energies with the second layer on the tensor cores; the Jacobian rows
+            // (one back-propagation per sample) by the SIMT kernel
+            {
+                NQS_LAUNCH("local_energy_mlp_tc");
+                if (!launch_mlp_eloc_tc(A, H, bits, B, Er, Ei)) return false;
+            }
+            if (!grad_mode) return true;
+            NQS_LAUNCH("local_estimator_mlp32");
+            return launch_mlp32(A, H, bits, B, nullptr, nullptr, O);
+        }
         NQS_LAUNCH("local_estimator_mlp32");
         return launch_mlp32(A, H, bits, B, Er, Ei, grad_mode ? O : nullptr);
     }

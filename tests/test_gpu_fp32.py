@@ -168,3 +168,40 @@ def test_fp32_mlp_chains_follow_fp64_chains(nqs):
     same = np.mean(np.all(b64 == b32, axis=1))
     assert same >= 0.9, same
     assert abs(acc64 - acc32) <= 0.02
+
+
+@pytest.mark.parametrize("ham,L,width", [("kagome", 3, 108), ("kagome", 2, 24), ("tfim", 16, 40)])
+def test_mlp_tensor_core_layer_local_energies(nqs, ham, L, width):
+    """The MLP local energies with the second layer on the tensor cores (tcgen05 TF32, three
+    hi / lo passes; the default in the mixed mode) against the SIMT layer (mlp_simt = 1) and
+    the FP64 oracle on the same batch: kagome 3x3 at width 108 (55 rows per sample, two
+    samples per 128-row tile), kagome 2x2 at width 24 (one K chunk), and a TFIM chain of 16
+    sites (single-site candidates).  Bar: 2e-5 of max|E_loc|, the FP32 estimator's."""
+    from spin_based_neural_network_gb300 import abi
+    if ham == "kagome":
+        N, Lx, Ly, h = 3 * L * L, L, L, abi.HAM_KAGOME_HEISENBERG
+        oh = O.ham(O.OR_KAGOME, L, L, kagome_pbc=1)
+    else:
+        N, Lx, Ly, h = L, L, 1, abi.HAM_TFIM
+        oh = O.ham(O.OR_TFIM, L, 1, Gamma=0.8)
+    cfg = abi.config_defaults(ansatz=abi.ANSATZ_GPU_MLP, width=width, depth=2, hamiltonian=h, kagome_pbc=1,
+                              transverse_field=0.8, j_coupling=1.0, rng_seed=11, sr_diag_shift=1e-3,
+                              learning_rate=0.01)
+    a = nqs.Ansatz(cfg, N)
+    p0 = a.params.copy()
+    rng = np.random.default_rng(N + width)
+    batch = np.where(rng.random((1000, N)) < 0.5, 1, -1).astype(np.int32)
+    E = {}
+    for simt in (0, 1):
+        a.params[:] = p0
+        nqs.set_options(precision=abi.PREC_MIXED, refine_sweeps=8, fp32_estimator=1, mlp_simt=simt)
+        try:
+            info, E[simt], _ = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True)
+        finally:
+            nqs.set_options()
+        assert np.all(np.isfinite(E[simt]))
+    Eo = O.local_energy(oh, O.Amp(O.OR_MLP, N, width, p0.copy(), []), batch)
+    scale = np.max(np.abs(Eo))
+    assert np.max(np.abs(E[0] - Eo)) <= 2e-5 * scale
+    assert np.max(np.abs(E[1] - Eo)) <= 2e-5 * scale
+    assert np.max(np.abs(E[0] - E[1])) <= 2e-5 * scale
