@@ -326,6 +326,16 @@ NCU_TRAFFIC = {
     "gram_tc": (37.775616e6 + 7.168e3, "profiles/gram_tc_split_params1120_ns4096_full.md"),
 }
 
+# What bounds each kernel whose roofline is reported ("bound" names the pipe the fraction is
+# taken against; these kernels do not run at that pipe's rate)
+LIMITERS = {
+    "factor_refine": "latency: a sequential chain of diagonal-block factors (one CTA) between grid "
+                     "barriers, SIMT FP32 panels and inverse, FP64 CG operator passes; the trailing "
+                     "updates alone run on the tensor cores",
+    "gram_tc": "tensor pipe and L2 / HBM operand traffic (TF32 split, three passes)",
+    "gram_fp64": "FP64 pipe (SIMT)",
+    "chol_syrk": "FP64 pipe (SIMT)",
+}
 CONV_LR0, CONV_LR1 = 0.02, 0.002   # learning-rate schedule of the accuracy run (geometric decay)
 CONV_SHIFT = 1e-4                   # its diagonal shift (the 2-D workload's)
 CONV_SWEEPS = 20                    # refinement iterations: the stacked holomorphic system is solved at shift / 4
@@ -971,7 +981,8 @@ def run_gpu(args):
                 "frac_of_pipe_nominal": achieved / nominal[pipe], "pipe_nominal_tflops": nominal[pipe],
                 "traffic": NCU_TRAFFIC.get(name, (None, None))[0],
                 "traffic_source": NCU_TRAFFIC.get(name, (None, None))[1],
-                "share_of_step": ms / total, "avg_launch_us": 1000.0 * ms / cnt}
+                "share_of_step": ms / total, "avg_launch_us": 1000.0 * ms / cnt,
+                "limiter": LIMITERS.get(name)}
 
     top_name = max(prof.items(), key=lambda kv: kv[1][1])[0]
     roof = roofline_of(top_name)
