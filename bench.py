@@ -932,8 +932,9 @@ def run_gpu(args):
     if prec == abi.PREC_MIXED:
         ph = nqs.last_step_stats().phase_us
         phases = dict(zip(("first_diag_block", "panels", "trailing_with_next_diag_block", "triangular_inverse",
-                           "preconditioner", "rhs_operator_cg", "total", "diag_block_owner_work"),
+                           "preconditioner", "rhs_and_operator", "total", "diag_block_owner_work"),
                           [round(ph[i], 1) for i in range(8)]))
+        phases["cg_vector_updates_and_dots"] = round(ph[6] - sum(ph[i] for i in range(6)), 1)
     L.nqs_gpu_event_destroy(e0)
     L.nqs_gpu_event_destroy(e1)
     nqs.lib().nqs_gpu_synchronize()

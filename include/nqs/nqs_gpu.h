@@ -330,9 +330,10 @@ typedef struct {
      * inverse / CG kernel (seen from CTA 0): [0] the first diagonal block, [1] panels,
      * [2] trailing updates (each with the next diagonal block's update and factor,
      * done by CTA 0 beside the trailing tiles), [3] triangular inverse, [4] preconditioner
-     * applications, [5] right-hand side, operator products and CG updates, [6]
-     * total; [7] the part of [0] spent by the owning CTAs on factoring and
-     * inverting the diagonal blocks */
+     * applications, [5] right-hand side and operator products, [6] total (the
+     * CG vector updates and dot products are the rest of it); [7] the time the
+     * owning CTAs spent on loading, updating, factoring and inverting the
+     * diagonal blocks (summed over the blocks) */
     double phase_us[8];
     /* MIXED with mixed_check and fp32_estimator: |<E> - <E>_fp64| / |<E>_fp64|
      * on the same samples (-1 when not measured) */

@@ -213,17 +213,19 @@ static bool make_map(CUtensorMap *m, const float *ptr, long rows, long cols_pad)
 // ---------------------------------------------------------------- FP32 factor, inverse and refinement
 // One cooperative launch (one CTA per SM, all co-resident) runs everything
 // after the Gram:
-//   factor   for each 128-column block k: the owner CTA factors the diagonal
-//            block in shared memory and inverts it (X_kk = L_kk^{-1}); every CTA
-//            forms 64 x 64 tiles of the panel U_k = X_kk A_k^T (stored as L^T in
-//            the unused upper triangle of T) and of the trailing update
-//            A -= U_k^T U_k (lower triangle);
-//   inverse  L^{-1} by recursive doubling over the 128-blocks: halves of h
-//            blocks are joined as [X11 0; -X22 L21 X11  X22], two GEMM phases
-//            per level, log2(n / 128) levels; L^{-1} is kept row-major (Li) and
+//   factor   for each BD-column block k (BD = 64 or 128): the owner CTA factors the
+//            diagonal block in shared memory and inverts it (X_kk = L_kk^{-1}); every
+//            CTA forms 64 x 64 tiles of the panel U_k = X_kk A_k^T (stored as L^T in
+//            the unused upper triangle of T), then 128 x 128 tensor-core tiles of the
+//            trailing update A -= U_k^T U_k (lower triangle), while the owner updates
+//            and factors the next diagonal block (look-ahead);
+//   inverse  L^{-1} beside the factor, by block rows: in the panel phase of step k
+//            row block k of X = L^{-1} is X_kk R_k (R = I - L X over the eliminated
+//            columns, accumulated in Li), in the trailing phase the rows below take
+//            R -= L_{:,k} X_k on the tensor cores; L^{-1} is kept row-major (Li) and
 //            transposed (LiT) so both triangular solves are row GEMVs;
-//   refine   sweeps of y <- y + L^{-T} L^{-1} r with the residual r formed in
-//            FP64 against the exact operator (two passes over O_c).
+//   refine   preconditioned CG on the exact operator in FP64 (two passes over O_c
+//            per product), preconditioner L^{-T} L^{-1} in FP32.
 // Phases are separated by a grid barrier on a generation word with a bounded
 // spin budget; on timeout it raises *err and every CTA leaves at its next
 // barrier.  Data written by other CTAs is read with L1-bypassing loads.
@@ -254,30 +256,33 @@ __device__ __forceinline__ unsigned long long gtimer() {
 // the tests of the timeout path.
 __device__ unsigned g_barrier_budget = 1u << 24;
 
+// A monotonic arrival counter (bar[0], cleared at every launch): the arrival that returns
+// old belongs to barrier instance old / count, which is passed once the counter reaches
+// (old / count + 1) * count, so no reset and no second word is needed (a CTA can only
+// arrive at the next instance after all arrivals of this one).  Ordering: the block
+// barrier, then an acq_rel fence at GPU scope around the relaxed atomic and the polls.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned count) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *gen = bar + 1;
-        const unsigned g0 = *gen;
         const unsigned budget = *(volatile unsigned *)&g_barrier_budget;
-        __threadfence();
-        if (atomicAdd(bar, 1u) == count - 1) {
-            bar[0] = 0;
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            uint32_t it = 0;
-            while (*gen == g0) {
-                if (*((volatile int *)err)) break;
-                if (++it > budget) {
-                    atomicExch(err, 2);
-                    break;
-                }
-                if (it > 64) __nanosleep(32);
+        unsigned old;
+        asm volatile("fence.acq_rel.gpu;\n\tatom.relaxed.gpu.global.add.u32 %0, [%1], 1;"
+                     : "=r"(old) : "l"(bar) : "memory");
+        const unsigned target = (old / count + 1u) * count;
+        uint32_t it = 0;
+        for (;;) {
+            unsigned cur;
+            asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(bar) : "memory");
+            if ((int)(cur - target) >= 0) break;
+            if (*((volatile int *)err)) break;
+            if (++it > budget) {
+                atomicExch(err, 2);
+                break;
             }
+            if (it > 64) __nanosleep(32);
         }
-        __threadfence();
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         s_ok = *((volatile int *)err) == 0;
     }
     __syncthreads();
@@ -406,71 +411,83 @@ __device__ int block_chol(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s
     return -1;
 }
 
-// The 64 x 64 diagonal block in one right-looking sweep by the whole CTA: at step j the
-// pivot L_jj = sqrt(S_jj), the column l_i = S_ij / L_jj and the row x_c = R_jc / L_jj of
-// X = L^{-1} are formed by 128 threads into shared vectors, then every thread updates
-// its 4 x 4 tile of S (S_ic -= l_i l_c, j < c <= i) and of R (R_ic -= l_i x_c, i > j,
-// c <= j), where R = I - L X over the columns eliminated so far (forward substitution of
-// L X = I, right-looking): two block barriers per column and all 256 threads busy,
-// instead of the warp-serial 32-column sub-panels of block_chol / block_inv.  S (rows >= bs
-// padded with the identity) is consumed; X is left in the lower triangle of X (zeros
-// above).  Returns the first non-positive pivot column below bs or -1 (the sweep goes on
-// with a unit pivot; the caller discards the block).
-__device__ int block_chol_inv64(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s_flag, float *lv) {
-    const int tid = threadIdx.x;
-    const int ti = tid >> 4, tj = tid & 15;              // 4 x 4 tile: rows 4 ti.., cols 4 tj..
-    float *xv = lv + 64;
-    for (int e = tid; e < 64 * 64; e += PS_THREADS) X[e >> 6][e & 63] = (e >> 6) == (e & 63) ? 1.f : 0.f;
-    if (tid == 0) *s_flag = -1;
-    __syncthreads();
-    for (int j = 0; j < 64; j++) {
-        if (tid < 128) {
-            const float d = S[j][j];
+// The 64 x 64 diagonal block, Cholesky and X = L^{-1} in one right-looking sweep with the
+// block in registers: thread (w, l) = (tid / 32, tid % 32) holds rows i = w + 8u (u < 8)
+// and columns c = l + 32v (v < 2) of S and of R = I - L X (forward substitution of L X = I,
+// right-looking).  At step j the owners publish the pivot column S[i][j] (i >= j) and row j
+// of R into shared memory, double-buffered, so one block barrier per column; then every
+// thread forms L_jj = sqrt(S_jj), l_i = S_ij / L_jj, x_c = R_jc / L_jj and updates its
+// entries: S_ic -= l_i l_c (l_i = 0 for i <= j, l_c = 0 for c <= j; entries above the
+// diagonal take values nothing reads) and R_ic -= l_i x_c (x_c = 0 for c > j), and row j
+// of R becomes row j of X.  Shared-memory traffic is broadcasts and unit-stride rows only.
+// S (rows >= bs padded with the identity) is read once; X (zeros above the diagonal) is
+// written to X.  Returns the first non-positive pivot column below bs or -1 (the sweep
+// goes on with a unit pivot; the caller discards the block).  buf: 256 floats.
+__device__ int block_chol_inv64(const float (*S)[BT + 1], float (*X)[BT + 1], int bs, float *buf) {
+    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+    float s[8][2], r[8][2];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int v = 0; v < 2; v++) {
+            const int i = w + 8 * u, c = l + 32 * v;
+            s[u][v] = S[i][c];
+            r[u][v] = i == c ? 1.f : 0.f;
+        }
+    int fail = -1;
+#pragma unroll
+    for (int jv = 0; jv < 2; jv++)
+        for (int jj = 0; jj < 32; jj++) {
+            const int j = 32 * jv + jj, jw = j & 7, ju = j >> 3;
+            float *lb = buf + (j & 1) * 128, *xb = lb + 64;
+            if (l == jj) {                                   // pivot column, rows >= j
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+                    if (w + 8 * u >= j) lb[w + 8 * u] = s[u][jv];
+            }
+            if (w == jw) {                                   // row j of R, columns <= j
+#pragma unroll
+                for (int v = 0; v < 2; v++) {
+                    float x = 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; u++) x = u == ju ? r[u][v] : x;
+                    if (l + 32 * v <= j) xb[l + 32 * v] = x;
+                }
+            }
+            __syncthreads();
+            const float d = lb[j];
             const bool ok = d > 0.f;
+            if (!ok && fail < 0 && j < bs) fail = j;
             const float inv = rsqrtf(ok ? d : 1.f);
-            if (tid < 64) {
-                const int i = tid;
-                lv[i] = i > j ? S[i][j] * inv : (i == j ? (ok ? d : 1.f) * inv : 0.f);
-                if (i == 0 && !ok && j < bs && *s_flag < 0) *s_flag = j;
-            } else {
-                const int c = tid - 64;
-                const float x = c <= j ? X[j][c] * inv : 0.f;
-                xv[c] = x;
-                X[j][c] = x;                              // row j of R becomes row j of X
+            float li[8], lc[2], xc[2];
+#pragma unroll
+            for (int u = 0; u < 8; u++) li[u] = w + 8 * u > j ? lb[w + 8 * u] * inv : 0.f;
+#pragma unroll
+            for (int v = 0; v < 2; v++) {
+                const int c = l + 32 * v;
+                lc[v] = c > j ? lb[c] * inv : 0.f;
+                xc[v] = c <= j ? xb[c] * inv : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+#pragma unroll
+                for (int v = 0; v < 2; v++) {
+                    s[u][v] = fmaf(-li[u], lc[v], s[u][v]);
+                    r[u][v] = fmaf(-li[u], xc[v], r[u][v]);
+                }
+            if (w == jw) {
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+#pragma unroll
+                    for (int v = 0; v < 2; v++) r[u][v] = u == ju ? xc[v] : r[u][v];
             }
         }
-        __syncthreads();
-        const int r0 = 4 * ti, c0 = 4 * tj;
-        if (r0 + 3 > j) {                                 // rows of this tile below the pivot
-            float li[4], lc[4], xc[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                li[u] = lv[r0 + u];
-                lc[u] = lv[c0 + u];
-                xc[u] = xv[c0 + u];
-            }
-            if (c0 + 3 > j && c0 <= r0 + 3) {             // S: j < c <= i
+    for (int u = 0; u < 8; u++)
 #pragma unroll
-                for (int u = 0; u < 4; u++)
-#pragma unroll
-                    for (int v = 0; v < 4; v++) {
-                        const int i = r0 + u, c = c0 + v;
-                        if (c > j && c <= i) S[i][c] = fmaf(-li[u], lc[v], S[i][c]);
-                    }
-            }
-            if (c0 <= j) {                                // R: i > j, c <= j
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-#pragma unroll
-                    for (int v = 0; v < 4; v++) {
-                        const int i = r0 + u, c = c0 + v;
-                        if (i > j && c <= j) X[i][c] = fmaf(-li[u], xc[v], X[i][c]);
-                    }
-            }
-        }
-        __syncthreads();
-    }
-    return *s_flag;
+        for (int v = 0; v < 2; v++) X[w + 8 * u][l + 32 * v] = r[u][v];
+    __syncthreads();
+    return fail;
 }
 
 // Off-diagonal 32-blocks of X = L^{-1} inside the 128-block (the diagonal
@@ -744,20 +761,49 @@ __device__ __forceinline__ float dot4_range(const float *row, const float *v, in
     return t;
 }
 
-// a . b over [0, n), computed by every CTA in the same fixed order (thread-
-// strided partial sums, a warp butterfly, then the warps in order), so that all
-// CTAs hold the same value whatever the grid size.
-__device__ __forceinline__ double dot_all(const double *a, const double *b, int n, double *red) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += PS_THREADS) s += __ldcg(a + i) * __ldcg(b + i);
-    s = warp_sum(s);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    double t = 0.0;
+// a . b and a . c over [0, n), computed by every CTA in the same fixed order (four
+// thread-strided partial sums with their loads issued together, a warp butterfly, then
+// the warps in order), so that all CTAs hold the same values whatever the grid size.
+template <bool TWO>
+__device__ __forceinline__ double2 dot_all2(const double *a, const double *b, const double *c, int n, double *red) {
+    double s[4] = {0.0, 0.0, 0.0, 0.0}, t[4] = {0.0, 0.0, 0.0, 0.0};
+    int i = threadIdx.x;
+    for (; i + 3 * PS_THREADS < n; i += 4 * PS_THREADS) {
+        double av[4], bv[4], cv[4];
 #pragma unroll
-    for (int w = 0; w < PS_THREADS / 32; w++) t += red[w];
-    return t;
+        for (int q = 0; q < 4; q++) {
+            av[q] = __ldcg(a + i + q * PS_THREADS);
+            bv[q] = __ldcg(b + i + q * PS_THREADS);
+            cv[q] = TWO ? __ldcg(c + i + q * PS_THREADS) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            s[q] += av[q] * bv[q];
+            if (TWO) t[q] += av[q] * cv[q];
+        }
+    }
+    for (; i < n; i += PS_THREADS) {
+        const double ai = __ldcg(a + i);
+        s[0] += ai * __ldcg(b + i);
+        if (TWO) t[0] += ai * __ldcg(c + i);
+    }
+    double x = warp_sum((s[0] + s[1]) + (s[2] + s[3])), y = TWO ? warp_sum((t[0] + t[1]) + (t[2] + t[3])) : 0.0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = x;
+        if (TWO) red[PS_THREADS / 32 + (threadIdx.x >> 5)] = y;
+    }
+    __syncthreads();
+    double2 r = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int w = 0; w < PS_THREADS / 32; w++) {
+        r.x += red[w];
+        if (TWO) r.y += red[PS_THREADS / 32 + w];
+    }
+    return r;
+}
+__device__ __forceinline__ double dot_all(const double *a, const double *b, int n, double *red) {
+    return dot_all2<false>(a, b, nullptr, n, red).x;
 }
 
 // ---- tensor-core trailing update.  The panel phase stores U^T split into TF32
@@ -790,21 +836,25 @@ struct TcState {
     int *err;
 };
 
-// C[i][j] -= (U^T U)[i][j] for the tile rows R0.., columns C0.. (j <= i < n), except the
-// entries with i, j < skip (the next diagonal block, updated by its owner); returns false
-// when a bounded wait gave up (err raised).
+// One 128 x 128 tile of a rank-BD update, C = A_i B_j^T over K = BD with the operands
+// rows R0 .. R0 + 127 of (ah, al) and C0 .. C0 + 127 of (bh, bl) ([row][BD] TF32 hi / lo).
+// Trailing mode (lim == 0): T[i][j] -= C for j <= i < n (row pitch n), except the entries
+// with i, j < skip (the next diagonal block, updated by its owner).  Inverse mode
+// (lim > 0): T[i][j] -= C for i < n, j < lim (row pitch ldt), where the columns j >= skip
+// take their first update (T = -C, nothing read).  Returns false when a bounded wait gave
+// up (err raised).
 template <int BD>
-__device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, float *T, int n, int R0, int C0,
-                                 int skip = 0) {
+__device__ bool trailing_tile_tc(TcState &ts, const float *ah, const float *al, const float *bh, const float *bl,
+                                 float *T, int n, int ldt, int R0, int C0, int skip, int lim) {
     constexpr int NQ = BD / 32;
     const int tid = threadIdx.x;
     const uint32_t s0 = smem_u32(ts.sm);
     auto stage = [&](int q, int b) {
         const uint32_t sb = s0 + b * TT_STAGE_BYTES;
-        stage_sw128<BD>(sb, uh, R0, q);
-        stage_sw128<BD>(sb + TT_CHUNK_BYTES, ul, R0, q);
-        stage_sw128<BD>(sb + 2 * TT_CHUNK_BYTES, uh, C0, q);
-        stage_sw128<BD>(sb + 3 * TT_CHUNK_BYTES, ul, C0, q);
+        stage_sw128<BD>(sb, ah, R0, q);
+        stage_sw128<BD>(sb + TT_CHUNK_BYTES, al, R0, q);
+        stage_sw128<BD>(sb + 2 * TT_CHUNK_BYTES, bh, C0, q);
+        stage_sw128<BD>(sb + 3 * TT_CHUNK_BYTES, bl, C0, q);
         cp_async_commit();
     };
     // M = N = 128, FP32 accumulate, TF32 operands, both K-major
@@ -861,7 +911,24 @@ __device__ bool trailing_tile_tc(TcState &ts, const float *uh, const float *ul, 
     }
     tc_fence_before();
     __syncthreads();
-    if ((n & 3) == 0) {
+    if (lim > 0) {
+        // inverse mode: ldt, lim and skip are multiples of 4, so no float4 group straddles them
+        float4 v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int e4 = tid + q * PS_THREADS, i = R0 + (e4 >> 5), j = C0 + 4 * (e4 & 31);
+            v[q] = (i < n && j < lim && j < skip) ? __ldcg((const float4 *)&T[(size_t)i * ldt + j])
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int e4 = tid + q * PS_THREADS, r = e4 >> 5, c = 4 * (e4 & 31), i = R0 + r, j = C0 + c;
+            if (i < n && j < lim) {
+                const float4 d = *(const float4 *)&ep[r * EP + c];
+                *(float4 *)&T[(size_t)i * ldt + j] = make_float4(v[q].x - d.x, v[q].y - d.y, v[q].z - d.z, v[q].w - d.w);
+            }
+        }
+    } else if ((n & 3) == 0) {
         // 16 float4 per thread, all loads before the stores
         float4 v[16];
 #pragma unroll
@@ -915,7 +982,7 @@ constexpr double CG_RTOL = 1e-10;
 
 struct FrArgs {
     float *T;           // [n][n] Gram + shift (lower) on entry; U = L^T in the upper triangle after
-    float *Li, *LiT;    // [n][ldl] L^{-1} (lower) and its transpose; pad columns are zero
+    float *Li, *LiT;    // [n][ldl] L^{-1} (lower; R while it is built) and its transpose; pad columns are zero
     int n;              // order of the system
     int ldl;            // row pitch of Li / LiT (n rounded up to 32)
     int space;          // 0: samples (n = N_s, unknown y), 1: parameters (n = N_p, unknown delta)
@@ -930,6 +997,7 @@ struct FrArgs {
     double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
     float *uh, *ul;     // [n + 128][bd] TF32 hi / lo words of the current panel U^T (K contiguous; pad rows zero)
+    float *xh, *xl;     // [n + 128][bd] TF32 hi / lo words of X^T over the current block row of X = L^{-1}
     int bd;             // diagonal block width (BD_SMALL or BD_LARGE)
     double *nrm;        // [3] |r|^2, |rhs|^2, CG iterations run
     int sweeps;         // maximum CG iterations
@@ -962,39 +1030,63 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
 #define NQS_PHASE(k)                                  \
     if (timing) {                                     \
         unsigned long long now_ = gtimer();           \
-        tacc[k] += now_ - tprev;                      \
+        if ((k) >= 0) tacc[(k) < 0 ? 0 : (k)] += now_ - tprev; \
         tprev = now_;                                 \
     }
 
     // ---------------- factor
     // Diagonal block kb: its owner CTA loads it, factors and inverts it in
     // shared memory and stores X_kk in Li / LiT (a breakdown goes to status[0]).
-    auto factor_diag = [&](int kb) {
+    // With BD = 64 and pk0 >= 0 the block is first updated by the previous step's
+    // panel rows pk0 .. pk0 + pbs - 1 of T (U = L^T): D -= U^T U, one 64 x 64 SIMT tile
+    // whose result is subtracted as the block is loaded (the block of T itself is dead
+    // after its factor, so it is not written back).
+    auto factor_diag = [&](int kb, int pk0, int pbs) {
         const int k0 = kb * BD, bs = min(BD, n - k0);
         const unsigned long long t_own = tid == 0 ? gtimer() : 0;
-        for (int e0 = 0; e0 < BD * BD; e0 += 8 * PS_THREADS) {
-            float v[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int e = e0 + tid + q * PS_THREADS, rr = e / BD, cc = e % BD;
-                const bool in = e < BD * BD && rr < bs && cc <= rr;
-                v[q] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) : (rr == cc ? 1.f : 0.f);
+        int f;
+        if (BD == 64) {
+            float acc[4][4] = {};
+            if (pk0 >= 0) {
+                const float *U = a.T + (size_t)pk0 * n;
+                gemm64<true, true>(acc, U, n, k0, k0 + bs, U, n, k0, k0 + bs, 0, pbs, TS);
             }
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int e = e0 + tid + q * PS_THREADS;
-                if (e < BD * BD) S0[e / BD][e % BD] = v[q];
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int rr = ty + 16 * u, cc = tx + 16 * v;
+                    const bool in = rr < bs && cc <= rr;
+                    S0[rr][cc] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) - acc[u][v]
+                                    : (rr == cc ? 1.f : 0.f);
+                }
+            __syncthreads();
+            f = block_chol_inv64(S0, S1, bs, tmpb);
+        } else {
+            for (int e0 = 0; e0 < BD * BD; e0 += 8 * PS_THREADS) {
+                float v[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int e = e0 + tid + q * PS_THREADS, rr = e / BD, cc = e % BD;
+                    const bool in = e < BD * BD && rr < bs && cc <= rr;
+                    v[q] = in ? __ldcg(&a.T[(size_t)(k0 + rr) * n + k0 + cc]) : (rr == cc ? 1.f : 0.f);
+                }
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int e = e0 + tid + q * PS_THREADS;
+                    if (e < BD * BD) S0[e / BD][e % BD] = v[q];
+                }
             }
+            __syncthreads();
+            f = block_chol<BD>(S0, S1, bs, &s_flag, tmpb);
+            if (f < 0) block_inv<BD>(S0, S1, tmpb);
         }
-        __syncthreads();
-        const int f = BD == 64 ? block_chol_inv64(S0, S1, bs, &s_flag, tmpb) : block_chol<BD>(S0, S1, bs, &s_flag, tmpb);
         if (f >= 0) {
             if (tid == 0) {
                 a.status[0] = k0 + f;
                 __threadfence();
             }
         } else {
-            if (BD != 64) block_inv<BD>(S0, S1, tmpb);
             for (int e = tid; e < BD * BD; e += PS_THREADS) {
                 const int rr = e / BD, q = e % BD;
                 if (rr < bs && q < bs) {
@@ -1006,24 +1098,92 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         __syncthreads();                                    // S0 / S1 are reused as GEMM staging
         if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
     };
+    // Large systems skip the explicit L^{-1} (n^3 / 3 flops) and apply the
+    // preconditioner by blocked substitution (one grid barrier per diagonal
+    // block and direction); below BLOCKED_SOLVE_MIN the inverse is cheaper than
+    // those barriers over the CG iterations.
+    const bool blocked = n >= BLOCKED_SOLVE_MIN;
+    // X = L^{-1} is built beside the factor (forward substitution of L X = I, right-looking
+    // by block columns): R = I - sum_{p < kb} L_{:,p} X_{p,:} accumulates in the lower
+    // off-diagonal blocks of Li.  In the panel phase of step kb block row kb of X is
+    // finalised, X_kb,c = X_kk R_kb,c (c < k0), written over R, transposed into LiT and split
+    // into xh / xl; in the trailing phase the rows below are updated, R_i,c -= L_i,kb X_kb,c
+    // (c < k1), by 128 x 128 tensor-core tiles beside the trailing tiles of the factor.
+    // Task t of the block row: column tile t (64 wide) of X_kb, all its rows by one CTA (the
+    // product reads the whole column tile of R before any of it is overwritten), t < k0 / 64;
+    // then (with_x) the copy of X_kk^T into xh / xl.
+    auto xrow_tasks = [&](int k0, bool with_x) { return k0 / GT + (with_x ? 1 : 0); };
+    auto xrow_tile = [&](int k0, int bs, bool with_x, int t) {
+        constexpr int NRT = BD / GT;
+        if (t < k0 / GT) {
+            const int c0 = t * GT;
+            float acc[NRT][4][4] = {};
+#pragma unroll
+            for (int rt = 0; rt < NRT; rt++)
+                if (rt * GT < bs)
+                    gemm64<false, true>(acc[rt], a.Li + (size_t)k0 * ldl + k0, ldl, rt * GT, bs, a.Li + (size_t)k0 * ldl,
+                                        ldl, c0, k0, 0, bs, TS);
+#pragma unroll
+            for (int rt = 0; rt < NRT; rt++) {
+                const int r0 = rt * GT;
+                if (r0 >= bs) break;
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int r = r0 + ty + 16 * u, c = c0 + tx + 16 * v;
+                        if (r < bs) a.Li[(size_t)(k0 + r) * ldl + c] = acc[rt][u][v];
+                        ST[ty + 16 * u][tx + 16 * v] = acc[rt][u][v];
+                    }
+                __syncthreads();
+                for (int e = tid; e < GT * GT; e += PS_THREADS) {
+                    const int cc = e / GT, rr = e % GT, r = r0 + rr, c = c0 + cc;
+                    if (r < bs) {
+                        const float x = ST[rr][cc];
+                        a.LiT[(size_t)c * ldl + k0 + r] = x;
+                        if (with_x) {
+                            const float h = tf32_rna(x);
+                            a.xh[(size_t)c * BD + r] = h;
+                            a.xl[(size_t)c * BD + r] = tf32_rna(x - h);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        } else {
+            for (int e = tid; e < BD * BD; e += PS_THREADS) {
+                const int cc = e / BD, rr = e % BD;
+                if (cc < bs) {
+                    const float x = rr < bs ? __ldcg(&a.LiT[(size_t)(k0 + cc) * ldl + k0 + rr]) : 0.f, h = tf32_rna(x);
+                    a.xh[(size_t)(k0 + cc) * BD + rr] = h;
+                    a.xl[(size_t)(k0 + cc) * BD + rr] = tf32_rna(x - h);
+                }
+            }
+        }
+    };
     // Look-ahead: the diagonal block of step kb + 1 is updated and factored by CTA 0 during
     // the trailing phase of step kb (64 x 64 SIMT tiles of U_kb^T U_kb over its lower
     // triangle, then factor_diag), while the other CTAs update the trailing tiles, the
     // first of which leaves that block's entries to CTA 0.  So each step has two grid
     // barriers (after the panel and after the trailing update) and the block's factor runs
     // beside the trailing tiles instead of in a phase of its own.
-    if (bx == 0) factor_diag(0);
+    if (bx == 0) factor_diag(0, -1, 0);
     if (!grid_barrier(a.bar, a.err, G)) return;
     if (__ldcg(a.status) >= 0) return;                      // broken factor: every CTA leaves here
     NQS_PHASE(0);
     for (int kb = 0; kb < nb; kb++) {
         const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
         if (rest <= 0) break;
-        // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1
+        // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1; block row kb of X
         {
             constexpr int NCT = (BD + GT - 1) / GT;          // column tiles of the panel
-            const int ntr = (rest + GT - 1) / GT;
-            for (int t = bx; t < NCT * ntr; t += G) {
+            const int ntr = (rest + GT - 1) / GT, npt = NCT * ntr;
+            const int ntasks = npt + (blocked ? 0 : xrow_tasks(k0, true));
+            for (int t = bx; t < ntasks; t += G) {
+                if (t >= npt) {
+                    xrow_tile(k0, bs, true, t - npt);
+                    continue;
+                }
                 const int c0 = (t % NCT) * GT, r0 = k1 + (t / NCT) * GT;
                 if (c0 >= bs) continue;
                 float acc[4][4] = {};
@@ -1052,10 +1212,13 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         NQS_PHASE(1);
-        // trailing update, with the next diagonal block updated and factored by CTA 0
+        // trailing update, with the next diagonal block updated and factored by CTA 0, and
+        // the update of R by block row kb of X
         {
             const int bs1 = min(BD, rest);                  // order of the next diagonal block
-            if (bx == 0) {
+            if (bx == 0 && BD == 64) {
+                factor_diag(kb + 1, k0, bs);                // the update fused into the block's load
+            } else if (bx == 0) {
                 // D -= U_kb^T U_kb on the lower 64 x 64 tiles of the next diagonal block, FP32
                 // from U (= L^T, the upper triangle rows k0 .. k0 + bs - 1 of T)
                 const float *U = a.T + (size_t)k0 * n;
@@ -1072,71 +1235,34 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
                             }
                         __syncthreads();
                     }
-                factor_diag(kb + 1);
+                factor_diag(kb + 1, -1, 0);
             }
             const int ntt = (rest + TT - 1) / TT, ntiles = ntt * (ntt + 1) / 2;
+            const int ncr = blocked ? 0 : (k1 + TT - 1) / TT, nall = ntiles + ntt * ncr;
             const int t0 = G > 1 ? bx - 1 : 0, dt = G > 1 ? G - 1 : 1;
-            for (int t = t0; t >= 0 && t < ntiles; t += dt) {
-                int bi, bj;
-                tri_tile(t, bi, bj);
-                if (!trailing_tile_tc<BD>(ts, a.uh, a.ul, a.T, n, k1 + bi * TT, k1 + bj * TT, t == 0 ? k1 + bs1 : 0))
-                    return;
+            for (int t = t0; t >= 0 && t < nall; t += dt) {
+                bool ok;
+                if (t < ntiles) {
+                    int bi, bj;
+                    tri_tile(t, bi, bj);
+                    ok = trailing_tile_tc<BD>(ts, a.uh, a.ul, a.uh, a.ul, a.T, n, n, k1 + bi * TT, k1 + bj * TT,
+                                              t == 0 ? k1 + bs1 : 0, 0);
+                } else {
+                    const int tr = t - ntiles;
+                    ok = trailing_tile_tc<BD>(ts, a.uh, a.ul, a.xh, a.xl, a.Li, n, ldl, k1 + (tr / ncr) * TT,
+                                              (tr % ncr) * TT, k0, k1);
+                }
+                if (!ok) return;
             }
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
         if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
         NQS_PHASE(2);
     }
-
-    // Large systems skip the explicit L^{-1} (n^3 / 3 flops) and apply the
-    // preconditioner by blocked substitution (one grid barrier per diagonal
-    // block and direction); below BLOCKED_SOLVE_MIN the inverse is cheaper than
-    // those barriers over the CG iterations.
-    const bool blocked = n >= BLOCKED_SOLVE_MIN;
-    // ---------------- L^{-1}: join halves of h blocks, h = 1, 2, 4, ...
-    for (int h = 1; h < nb && !blocked; h *= 2) {
-        // hb 64-tiles per half; a group's W / X21 have hb x hb tiles
-        const int span = 2 * h * BD, ngrp = (n + span - 1) / span, hb = h * BD / GT, per = hb * hb;
-        // W = L21 X11 (into the dead lower triangle of T)
-        for (int t = bx; t < ngrp * per; t += G) {
-            const int g = t / per, rt = (t % per) / hb, ct = t % hb;
-            const int a0 = g * span, a1 = a0 + h * BD, a2 = min(n, a0 + span);
-            const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
-            if (a1 >= a2 || r0 >= a2) continue;
-            float acc[4][4] = {};
-            gemm64<true, true>(acc, a.T, n, r0, a2, a.Li, ldl, c0, a1, c0, a1, TS);
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) {
-                    const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
-                    if (i < a2) a.T[(size_t)i * n + j] = acc[u][v];
-                }
-        }
-        if (!grid_barrier(a.bar, a.err, G)) return;
-        // X21 = -X22 W
-        for (int t = bx; t < ngrp * per; t += G) {
-            const int g = t / per, rt = (t % per) / hb, ct = t % hb;
-            const int a0 = g * span, a1 = a0 + h * BD, a2 = min(n, a0 + span);
-            const int r0 = a1 + rt * GT, c0 = a0 + ct * GT;
-            if (a1 >= a2 || r0 >= a2) continue;
-            float acc[4][4] = {};
-            gemm64<false, true>(acc, a.Li, ldl, r0, a2, a.T, n, c0, a1, a1, min(a2, r0 + GT), TS);
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) {
-                    const int i = r0 + ty + 16 * u, j = c0 + tx + 16 * v;
-                    if (i < a2) a.Li[(size_t)i * ldl + j] = -acc[u][v];
-                    ST[ty + 16 * u][tx + 16 * v] = -acc[u][v];
-                }
-            __syncthreads();
-            for (int e = tid; e < GT * GT; e += PS_THREADS) {
-                const int cc = e / GT, rr = e % GT;
-                if (r0 + rr < a2) a.LiT[(size_t)(c0 + cc) * ldl + r0 + rr] = ST[rr][cc];
-            }
-            __syncthreads();
-        }
+    // ---------------- the last block row of L^{-1}
+    if (!blocked && nb > 1) {
+        const int k0 = (nb - 1) * BD, bs = n - k0;
+        for (int t = bx; t < xrow_tasks(k0, false); t += G) xrow_tile(k0, bs, false, t);
         if (!grid_barrier(a.bar, a.err, G)) return;
     }
     NQS_PHASE(3);
@@ -1302,27 +1428,33 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         }
         return grid_barrier(a.bar, a.err, G);
     };
-    __shared__ double red[PS_THREADS / 32];
+    __shared__ double red[2 * (PS_THREADS / 32)];
     if (!precond(a.x)) return;                          // x0 = M^{-1} rhs
     NQS_PHASE(4);
+    // phase 5: the operator (and the right-hand side above); the vector updates, the dots
+    // and their barriers are left out of every slot (total minus the slots)
     if (!apply_op(a.x, a.q)) return;
+    NQS_PHASE(5);
     for (int i = gtid; i < n; i += gthreads) {
         const double ri = __ldcg(a.rhs + i) - __ldcg(a.q + i);
         a.r[i] = ri;
         a.rf[i] = (float)ri;
     }
     if (!grid_barrier(a.bar, a.err, G)) return;
-    NQS_PHASE(5);
+    NQS_PHASE(-1);
     if (!precond(a.z)) return;
     NQS_PHASE(4);
     const double bb = dot_all(a.rhs, a.rhs, n, red);
-    double rho = dot_all(a.r, a.z, n, red), rr = dot_all(a.r, a.r, n, red), beta = 0.0;
+    const double2 zr0 = dot_all2<true>(a.r, a.z, a.r, n, red);
+    double rho = zr0.x, rr = zr0.y, beta = 0.0;
     int it = 0;
     for (; it < a.sweeps && rr > CG_RTOL * CG_RTOL * bb && rho > 0.0; it++) {
         for (int i = gtid; i < n; i += gthreads)
             a.p[i] = it == 0 ? __ldcg(a.z + i) : __ldcg(a.z + i) + beta * __ldcg(a.p + i);
         if (!grid_barrier(a.bar, a.err, G)) return;
+        NQS_PHASE(-1);
         if (!apply_op(a.p, a.q)) return;
+        NQS_PHASE(5);
         const double pq = dot_all(a.p, a.q, n, red);
         if (!(pq > 0.0)) break;
         const double alpha = rho / pq;
@@ -1333,11 +1465,12 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
             a.rf[i] = (float)ri;
         }
         if (!grid_barrier(a.bar, a.err, G)) return;
-        NQS_PHASE(5);
+        NQS_PHASE(-1);
         if (!precond(a.z)) return;
         NQS_PHASE(4);
-        const double rho1 = dot_all(a.r, a.z, n, red);
-        rr = dot_all(a.r, a.r, n, red);
+        const double2 zr = dot_all2<true>(a.r, a.z, a.r, n, red);
+        const double rho1 = zr.x;
+        rr = zr.y;
         beta = rho1 / rho;
         rho = rho1;
     }
@@ -1416,7 +1549,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrA
 
 // ---------------------------------------------------------------- driver
 struct MixedWs {
-    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf, uh, ul;
+    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf, uh, ul, xh, xl;
     DevBuf<double> rhs, r, u, upart, nrm, p, q, z;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -1548,6 +1681,8 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     fa.rf = w.rf.p;
     fa.uh = w.uh.p;
     fa.ul = w.ul.p;
+    fa.xh = w.xh.p;
+    fa.xl = w.xl.p;
     fa.bd = pl.n >= BD_SWITCH ? BD_LARGE : BD_SMALL;
     fa.zf = w.zf.p;
     fa.nrm = w.nrm.p;
@@ -1605,8 +1740,8 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         *moved = true;
     }
     const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[18] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p};
+    const void *before[20] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p};
     const int ldl = (n + 31) / 32 * 32;
     // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero.
     // Sized for the wide diagonal block so a batch's autotuner can pick either width.
@@ -1614,19 +1749,22 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
         !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
+        !w.xh.ensure(nu) || !w.xl.ensure(nu) ||
         !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(3) || !w.status.ensure(2) ||
         !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
-    const void *after[18] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p};
-    for (int i = 0; i < 18; i++) *moved |= before[i] != after[i];
+    const void *after[20] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p};
+    for (int i = 0; i < 20; i++) *moved |= before[i] != after[i];
     if (*moved || w.n != n) {
         // the pad columns of L^{-1} are read (as zeros) by the vectorised solves,
-        // the pad rows of the split U^T by the tensor-core trailing tiles
+        // the pad rows of the split U^T and X^T by the tensor-core tiles
         if (!NQS_CUDA(cudaMemsetAsync(w.Li.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
             !NQS_CUDA(cudaMemsetAsync(w.LiT.p, 0, sizeof(float) * (size_t)n * ldl, st)) ||
             !NQS_CUDA(cudaMemsetAsync(w.uh.p, 0, sizeof(float) * w.uh.n, st)) ||
-            !NQS_CUDA(cudaMemsetAsync(w.ul.p, 0, sizeof(float) * w.ul.n, st)))
+            !NQS_CUDA(cudaMemsetAsync(w.ul.p, 0, sizeof(float) * w.ul.n, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.xh.p, 0, sizeof(float) * w.xh.n, st)) ||
+            !NQS_CUDA(cudaMemsetAsync(w.xl.p, 0, sizeof(float) * w.xl.n, st)))
             return false;
         w.n = n;
         *moved = true;
