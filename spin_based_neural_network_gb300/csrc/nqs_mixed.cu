@@ -210,6 +210,37 @@ static bool make_map(CUtensorMap *m, const float *ptr, long rows, long cols_pad)
     return true;
 }
 
+// ---------------------------------------------------------------- double-float arithmetic
+// The FP64 pipe of this GPU issues two FMAs per clock per SM, the FP32 pipe 128: sums that
+// need FP64 accuracy over many terms run on the FP32 pipe as unevaluated pairs hi + lo
+// (a 48-bit significand).  df_fma: s += a b with the exact product of the high words from
+// an FMA (Dekker's two-product), the cross terms a_hi b_lo + a_lo b_hi in FP32 (a_lo b_lo,
+// 2^-48 relative, is dropped), and the sum by Knuth's two-sum with its rounding error
+// carried in lo.  df_add: s += b, renormalised.  Explicit _rn intrinsics keep the compiler
+// from contracting or reordering the error terms.
+__device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float t = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    sh = t;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+__device__ __forceinline__ void df_add(float &sh, float &sl, float bh, float bl) {
+    const float t = __fadd_rn(sh, bh);
+    const float bb = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(bh, bb));
+    const float lo = __fadd_rn(err, __fadd_rn(sl, bl));
+    sh = __fadd_rn(t, lo);
+    sl = __fsub_rn(lo, __fsub_rn(sh, t));
+}
+// The parameter-space operator runs in double-float when N_p is a multiple of 4 (float4
+// rows) and at most 2048 (two four-column groups per thread).
+__host__ __device__ inline bool df_words_ok(long P) { return (P & 3) == 0 && P <= 8 * 256; }
+
 // ---------------------------------------------------------------- FP32 factor, inverse and refinement
 // One cooperative launch (one CTA per SM, all co-resident) runs everything
 // after the Gram:
@@ -275,12 +306,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
             unsigned cur;
             asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(bar) : "memory");
             if ((int)(cur - target) >= 0) break;
-            if (*((volatile int *)err)) break;
             if (++it > budget) {
                 atomicExch(err, 2);
                 break;
             }
-            if (it > 64) __nanosleep(32);
+            if ((it & 31) == 0) {                       // the error word every 32nd poll only
+                if (*((volatile int *)err)) break;
+                if (it > 256) __nanosleep(32);
+            }
         }
         asm volatile("fence.acq_rel.gpu;" ::: "memory");
         s_ok = *((volatile int *)err) == 0;
@@ -411,18 +444,21 @@ __device__ int block_chol(float (*S)[BT + 1], float (*X)[BT + 1], int bs, int *s
     return -1;
 }
 
-// The 64 x 64 diagonal block, Cholesky and X = L^{-1} in one right-looking sweep with the
-// block in registers: thread (w, l) = (tid / 32, tid % 32) holds rows i = w + 8u (u < 8)
-// and columns c = l + 32v (v < 2) of S and of R = I - L X (forward substitution of L X = I,
-// right-looking).  At step j the owners publish the pivot column S[i][j] (i >= j) and row j
-// of R into shared memory, double-buffered, so one block barrier per column; then every
-// thread forms L_jj = sqrt(S_jj), l_i = S_ij / L_jj, x_c = R_jc / L_jj and updates its
-// entries: S_ic -= l_i l_c (l_i = 0 for i <= j, l_c = 0 for c <= j; entries above the
-// diagonal take values nothing reads) and R_ic -= l_i x_c (x_c = 0 for c > j), and row j
-// of R becomes row j of X.  Shared-memory traffic is broadcasts and unit-stride rows only.
-// S (rows >= bs padded with the identity) is read once; X (zeros above the diagonal) is
-// written to X.  Returns the first non-positive pivot column below bs or -1 (the sweep
-// goes on with a unit pivot; the caller discards the block).  buf: 256 floats.
+// The 64 x 64 diagonal block, Cholesky and X = L^{-1} in one right-looking sweep over
+// four-column panels with the block in registers: thread (w, l) = (tid / 32, tid % 32)
+// holds rows i = w + 8u (u < 8) and columns c = l + 32v (v < 2) of S and of
+// R = I - L X (forward substitution of L X = I, right-looking).  At panel j0 the owners
+// publish the four pivot columns S[i][j0 .. j0+3] (i >= j0) and rows j0 .. j0+3 of R into
+// shared memory (double-buffered: one block barrier per panel); every thread factors the
+// 4 x 4 pivot block P = Lp Lp^T and inverts Lp (Ip = Lp^{-1}) itself, then
+//   l_i = Ip S[i][j0..j0+3]^T (i > j0 + 3; lane 4u + q forms component q of its warp's row
+//         w + 8u and the warp exchanges them by shuffles),
+//   l_c = Ip S[c][j0..j0+3]^T (c > j0 + 3), x_c = Ip R[j0..j0+3][c] (c <= j0 + 3),
+//   S_ic -= l_i . l_c, R_ic -= l_i . x_c, and rows j0 .. j0+3 of R become rows of X.
+// Entries above the diagonal of S take values nothing reads.  S (rows >= bs padded with
+// the identity) is read once; X (zeros above the diagonal) is written to X.  Returns the
+// first non-positive pivot column below bs or -1 (the sweep goes on with a unit pivot; the
+// caller discards the block).  buf: 1024 floats.
 __device__ int block_chol_inv64(const float (*S)[BT + 1], float (*X)[BT + 1], int bs, float *buf) {
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
     float s[8][2], r[8][2];
@@ -435,51 +471,133 @@ __device__ int block_chol_inv64(const float (*S)[BT + 1], float (*X)[BT + 1], in
             r[u][v] = i == c ? 1.f : 0.f;
         }
     int fail = -1;
+    const int lu = l >> 2, lq = l & 3;                       // this lane's (row, component) of l_i
 #pragma unroll
     for (int jv = 0; jv < 2; jv++)
-        for (int jj = 0; jj < 32; jj++) {
-            const int j = 32 * jv + jj, jw = j & 7, ju = j >> 3;
-            float *lb = buf + (j & 1) * 128, *xb = lb + 64;
-            if (l == jj) {                                   // pivot column, rows >= j
+        for (int jj0 = 0; jj0 < 32; jj0 += 4) {
+            const int j0 = 32 * jv + jj0, w0 = j0 & 7, ju = j0 >> 3;
+            float *cb = buf + ((j0 >> 2) & 1) * 512, *rb = cb + 256;   // cb[q * 64 + i], rb[a * 64 + c]
+            {
+                const int q = l - jj0;
+                if (q >= 0 && q < 4) {
 #pragma unroll
-                for (int u = 0; u < 8; u++)
-                    if (w + 8 * u >= j) lb[w + 8 * u] = s[u][jv];
-            }
-            if (w == jw) {                                   // row j of R, columns <= j
+                    for (int u = 0; u < 8; u++)
+                        if (w + 8 * u >= j0) cb[q * 64 + w + 8 * u] = s[u][jv];
+                }
+                const int a = w - w0;
+                if (a >= 0 && a < 4) {
 #pragma unroll
-                for (int v = 0; v < 2; v++) {
-                    float x = 0.f;
+                    for (int v = 0; v < 2; v++) {
+                        float x = 0.f;
 #pragma unroll
-                    for (int u = 0; u < 8; u++) x = u == ju ? r[u][v] : x;
-                    if (l + 32 * v <= j) xb[l + 32 * v] = x;
+                        for (int u = 0; u < 8; u++) x = u == ju ? r[u][v] : x;
+                        if (l + 32 * v <= j0 + 3) rb[a * 64 + l + 32 * v] = x;
+                    }
                 }
             }
             __syncthreads();
-            const float d = lb[j];
-            const bool ok = d > 0.f;
-            if (!ok && fail < 0 && j < bs) fail = j;
-            const float inv = rsqrtf(ok ? d : 1.f);
-            float li[8], lc[2], xc[2];
+            // the pivot block, its factor Lp and Ip = Lp^{-1} (every thread)
+            float P[4][4], Lp[4][4], Ip[4][4];
 #pragma unroll
-            for (int u = 0; u < 8; u++) li[u] = w + 8 * u > j ? lb[w + 8 * u] * inv : 0.f;
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b <= a; b++) P[a][b] = cb[b * 64 + j0 + a];
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                float d = P[a][a];
+#pragma unroll
+                for (int b = 0; b < a; b++) d = fmaf(-Lp[a][b], Lp[a][b], d);
+                const bool ok = d > 0.f;
+                if (!ok && fail < 0 && j0 + a < bs) fail = j0 + a;
+                const float inv = rsqrtf(ok ? d : 1.f);
+                Lp[a][a] = (ok ? d : 1.f) * inv;
+                Ip[a][a] = inv;
+#pragma unroll
+                for (int e = a + 1; e < 4; e++) {
+                    float t = P[e][a];
+#pragma unroll
+                    for (int b = 0; b < a; b++) t = fmaf(-Lp[e][b], Lp[a][b], t);
+                    Lp[e][a] = t * inv;
+                }
+            }
+#pragma unroll
+            for (int e = 1; e < 4; e++)
+#pragma unroll
+                for (int a = 0; a < e; a++) {
+                    float t = 0.f;
+#pragma unroll
+                    for (int b = a; b < e; b++) t = fmaf(Lp[e][b], Ip[b][a], t);
+                    Ip[e][a] = -Ip[e][e] * t;
+                }
+            // l_i: lane (lu, lq) forms component lq of row w + 8 lu; the warp gathers them by
+            // shuffles below, for the rows still below the panel only (a warp-uniform test)
+            float z = 0.f;
+            {
+                const int i = w + 8 * lu;
+                if (i > j0 + 3) {
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        float ip = 0.f;
+#pragma unroll
+                        for (int q = 0; q < 4; q++) ip = (q == lq && b <= q) ? Ip[q][b] : ip;
+                        z = fmaf(ip, cb[b * 64 + i], z);
+                    }
+                }
+            }
+            // l_c (columns below the panel) and x_c (columns up to it): in the first half
+            // (jv = 0) columns 32.. are all below the panel, in the second columns ..31 all
+            // above it, so those halves are known at compile time
+            float lc[2][4], xc[2][4];
 #pragma unroll
             for (int v = 0; v < 2; v++) {
                 const int c = l + 32 * v;
-                lc[v] = c > j ? lb[c] * inv : 0.f;
-                xc[v] = c <= j ? xb[c] * inv : 0.f;
+                const bool below = v > jv || (v == jv && c > j0 + 3);
+                float y[4];
+#pragma unroll
+                for (int b = 0; b < 4; b++) y[b] = below ? cb[b * 64 + c] : rb[b * 64 + c];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    float t = 0.f;
+#pragma unroll
+                    for (int b = 0; b <= q; b++) t = fmaf(Ip[q][b], y[b], t);
+                    lc[v][q] = below ? t : 0.f;
+                    xc[v][q] = below ? 0.f : t;
+                }
             }
 #pragma unroll
-            for (int u = 0; u < 8; u++)
+            for (int u = 0; u < 8; u++) {
+                if (w + 8 * u <= j0 + 3) continue;          // rows done (warp-uniform)
+                float li[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) li[q] = __shfl_sync(0xffffffffu, z, 4 * u + q);
 #pragma unroll
                 for (int v = 0; v < 2; v++) {
-                    s[u][v] = fmaf(-li[u], lc[v], s[u][v]);
-                    r[u][v] = fmaf(-li[u], xc[v], r[u][v]);
+                    if (v >= jv) {                          // S: columns that can lie below the panel
+                        float ds = 0.f;
+#pragma unroll
+                        for (int q = 0; q < 4; q++) ds = fmaf(li[q], lc[v][q], ds);
+                        s[u][v] -= ds;
+                    }
+                    if (v <= jv) {                          // R: columns that can lie up to the panel
+                        float dr = 0.f;
+#pragma unroll
+                        for (int q = 0; q < 4; q++) dr = fmaf(li[q], xc[v][q], dr);
+                        r[u][v] -= dr;
+                    }
                 }
-            if (w == jw) {
+            }
+            {
+                const int a = w - w0;                        // rows j0 .. j0+3 of R become rows of X
+                if (a >= 0 && a < 4) {
 #pragma unroll
-                for (int u = 0; u < 8; u++)
+                    for (int v = 0; v <= jv; v++) {
+                        float x = 0.f;
 #pragma unroll
-                    for (int v = 0; v < 2; v++) r[u][v] = u == ju ? xc[v] : r[u][v];
+                        for (int q = 0; q < 4; q++) x = q == a ? xc[v][q] : x;
+#pragma unroll
+                        for (int u = 0; u < 8; u++) r[u][v] = u == ju ? x : r[u][v];
+                    }
+                }
             }
         }
 #pragma unroll
@@ -993,16 +1111,17 @@ struct FrArgs {
     double shift;
     double *x;          // [n] solution
     double *rhs, *r;    // [n] right-hand side and residual
-    double *u, *upart;  // intermediate vector, partial column sums
+    double *u, *upart;  // intermediate vector, partial column sums ([N_s / 32][N_p])
     double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
     float *uh, *ul;     // [n + 128][bd] TF32 hi / lo words of the current panel U^T (K contiguous; pad rows zero)
     float *xh, *xl;     // [n + 128][bd] TF32 hi / lo words of X^T over the current block row of X = L^{-1}
+    const float *oh, *ol;  // [N_s][N_p] O_c as double-float words (FP32 hi + lo), or null
     int bd;             // diagonal block width (BD_SMALL or BD_LARGE)
     double *nrm;        // [3] |r|^2, |rhs|^2, CG iterations run
     int sweeps;         // maximum CG iterations
     int *status;        // [0] first failing column or -1
-    unsigned *bar;      // [0] arrivals, [1] generation
+    unsigned *bar;      // [0] grid barrier arrivals, [1..3] owner / worker flags (X, U, T), [4] worker barrier
     int *err;
     unsigned long long *tm;   // [8] phase nanoseconds: [0..6] CTA 0's view, [7] owners' block work
 };
@@ -1167,97 +1286,317 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     // first of which leaves that block's entries to CTA 0.  So each step has two grid
     // barriers (after the panel and after the trailing update) and the block's factor runs
     // beside the trailing tiles instead of in a phase of its own.
-    if (bx == 0) factor_diag(0, -1, 0);
-    if (!grid_barrier(a.bar, a.err, G)) return;
-    if (__ldcg(a.status) >= 0) return;                      // broken factor: every CTA leaves here
-    NQS_PHASE(0);
-    for (int kb = 0; kb < nb; kb++) {
-        const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
-        if (rest <= 0) break;
-        // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1; block row kb of X
-        {
-            constexpr int NCT = (BD + GT - 1) / GT;          // column tiles of the panel
-            const int ntr = (rest + GT - 1) / GT, npt = NCT * ntr;
-            const int ntasks = npt + (blocked ? 0 : xrow_tasks(k0, true));
-            for (int t = bx; t < ntasks; t += G) {
-                if (t >= npt) {
-                    xrow_tile(k0, bs, true, t - npt);
-                    continue;
+    // Panel tile: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m], columns c0 .. c0 + 63 of the
+    // block, rows r0 .. r0 + 63, into the upper triangle of T and split into (uhk, ulk).
+    auto panel_tile = [&](int k0, int bs, int c0, int r0, float *uhk, float *ulk) {
+        float acc[4][4] = {};
+        gemm64<false, false>(acc, a.Li + (size_t)k0 * ldl + k0, ldl, c0, bs, a.T + k0, n, r0, n, 0, min(bs, c0 + GT),
+                             TS);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int c = c0 + ty + 16 * u, r = r0 + tx + 16 * v;
+                if (c < bs && r < n) a.T[(size_t)(k0 + c) * n + r] = acc[u][v];
+                ST[ty + 16 * u][tx + 16 * v] = acc[u][v];
+            }
+        __syncthreads();
+        // U^T split into TF32 hi / lo, rows r (K = panel column contiguous)
+        for (int e = tid; e < GT * GT; e += PS_THREADS) {
+            const int rr = e / GT, cc = e % GT, r = r0 + rr, c = c0 + cc;
+            if (c < bs && r < n) {
+                const float x = ST[cc][rr], h = tf32_rna(x);
+                uhk[(size_t)r * BD + c] = h;
+                ulk[(size_t)r * BD + c] = tf32_rna(x - h);
+            }
+        }
+        __syncthreads();
+    };
+    // Flags between the owner CTA and the others (monotonic words of bar[], cleared at every
+    // launch): flag_set publishes after the whole CTA's writes (block barrier, then an
+    // acq_rel fence at GPU scope before the store); flag_wait polls with the grid barrier's
+    // bounded budget and gives up on an error or a broken factor (status set).
+    auto flag_set = [&](unsigned *f, unsigned v) {
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            atomicExch(f, v);
+        }
+    };
+    auto flag_wait = [&](const unsigned *f, unsigned target) -> bool {
+        __shared__ int s_fok;
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned budget = *(volatile unsigned *)&g_barrier_budget;
+            int ok = 1;
+            for (uint32_t it = 0;; it++) {
+                unsigned cur;
+                asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(f) : "memory");
+                if ((int)(cur - target) >= 0) break;
+                if (it + 1 > budget) {
+                    atomicExch(a.err, 2);
+                    ok = 0;
+                    break;
                 }
-                const int c0 = (t % NCT) * GT, r0 = k1 + (t / NCT) * GT;
-                if (c0 >= bs) continue;
-                float acc[4][4] = {};
-                gemm64<false, false>(acc, a.Li + (size_t)k0 * ldl + k0, ldl, c0, bs, a.T + k0, n, r0, n, 0,
-                                     min(bs, c0 + GT), TS);
+                if ((it & 31) == 31) {
+                    if (*((volatile int *)a.err)) {
+                        ok = 0;
+                        break;
+                    }
+                    if (it > 256) __nanosleep(32);
+                }
+            }
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            s_fok = ok && *((volatile int *)a.err) == 0 && *((volatile int *)a.status) < 0;
+        }
+        __syncthreads();
+        return s_fok != 0;
+    };
+    // The owner's step kb of the pipelined factor (BD = 64), with X_kk in S1 from the previous
+    // factor: the block A = T[k1 .. k1 + bs1)[k0 .. k1) is staged in shared memory (SA, the
+    // unused rows between S0 and S1) while the next diagonal block D is prefetched into
+    // registers; U = X_kk A^T (64 x bs1, both operands in shared memory) goes to the upper
+    // triangle of T and to (uhk, ulk) and stays in S0; flag U; D -= U^T U from shared memory;
+    // then D is factored and inverted into S1 (X of block kb + 1) and stored to Li / LiT.
+    float (*SA)[BT + 1] = (float (*)[BT + 1])(psm + 64 * (BT + 1));
+    auto owner_step = [&](int kb, float *uhk, float *ulk, unsigned *fl_u) -> bool {
+        const int k0 = kb * BD, k1 = k0 + BD, bs1 = min(BD, n - k1);
+        const unsigned long long t_own = tid == 0 ? gtimer() : 0;
+        float dv[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int rr = ty + 16 * u, cc = tx + 16 * v;
+                dv[u][v] = (rr < bs1 && cc <= rr) ? __ldcg(&a.T[(size_t)(k1 + rr) * n + k1 + cc]) : 0.f;
+            }
+        for (int e = tid; e < BD * BD; e += PS_THREADS) {
+            const int rr = e / BD, m = e % BD;
+            SA[rr][m] = rr < bs1 ? __ldcg(&a.T[(size_t)(k1 + rr) * n + k0 + m]) : 0.f;
+        }
+        __syncthreads();
+        {
+            // U[c][r] = sum_m X[c][m] A[r][m]: thread (ty, tx) owns c = ty + 16u, r = tx + 16v
+            float acc[4][4] = {};
+#pragma unroll 8
+            for (int m = 0; m < BD; m++) {
+                float xa[4], av[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    xa[u] = S1[ty + 16 * u][m];
+                    av[u] = SA[tx + 16 * u][m];
+                }
 #pragma unroll
                 for (int u = 0; u < 4; u++)
 #pragma unroll
-                    for (int v = 0; v < 4; v++) {
-                        const int c = c0 + ty + 16 * u, r = r0 + tx + 16 * v;
-                        if (c < bs && r < n) a.T[(size_t)(k0 + c) * n + r] = acc[u][v];
-                        ST[ty + 16 * u][tx + 16 * v] = acc[u][v];
-                    }
-                __syncthreads();
-                // U^T split into TF32 hi / lo, rows r (K = panel column contiguous)
-                for (int e = tid; e < GT * GT; e += PS_THREADS) {
-                    const int rr = e / GT, cc = e % GT, r = r0 + rr, c = c0 + cc;
-                    if (c < bs && r < n) {
-                        const float x = ST[cc][rr], h = tf32_rna(x);
-                        a.uh[(size_t)r * BD + c] = h;
-                        a.ul[(size_t)r * BD + c] = tf32_rna(x - h);
-                    }
+                    for (int v = 0; v < 4; v++) acc[u][v] = fmaf(xa[u], av[v], acc[u][v]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int c = ty + 16 * u, r = tx + 16 * v;
+                    S0[c][r] = r < bs1 ? acc[u][v] : 0.f;
+                    if (r < bs1) a.T[(size_t)(k0 + c) * n + k1 + r] = acc[u][v];
                 }
-                __syncthreads();
+        }
+        __syncthreads();
+        for (int e = tid; e < BD * BD; e += PS_THREADS) {
+            const int rr = e / BD, c = e % BD;
+            if (rr < bs1) {
+                const float x = S0[c][rr], h = tf32_rna(x);
+                uhk[(size_t)(k1 + rr) * BD + c] = h;
+                ulk[(size_t)(k1 + rr) * BD + c] = tf32_rna(x - h);
             }
         }
-        if (!grid_barrier(a.bar, a.err, G)) return;
-        NQS_PHASE(1);
-        // trailing update, with the next diagonal block updated and factored by CTA 0, and
-        // the update of R by block row kb of X
+        flag_set(fl_u, kb + 1);
         {
-            const int bs1 = min(BD, rest);                  // order of the next diagonal block
-            if (bx == 0 && BD == 64) {
-                factor_diag(kb + 1, k0, bs);                // the update fused into the block's load
-            } else if (bx == 0) {
-                // D -= U_kb^T U_kb on the lower 64 x 64 tiles of the next diagonal block, FP32
-                // from U (= L^T, the upper triangle rows k0 .. k0 + bs - 1 of T)
-                const float *U = a.T + (size_t)k0 * n;
-                for (int ti = 0; ti * GT < bs1; ti++)
-                    for (int tj = 0; tj <= ti; tj++) {
-                        float acc[4][4] = {};
-                        gemm64<true, true>(acc, U, n, k1 + ti * GT, k1 + bs1, U, n, k1 + tj * GT, k1 + bs1, 0, bs, TS);
+            // D[i][j] -= sum_c U[c][i] U[c][j] (i = ty + 16u, j = tx + 16v), lower triangle
+            float acc[4][4] = {};
+#pragma unroll 8
+            for (int c = 0; c < BD; c++) {
+                float ui[4], uj[4];
 #pragma unroll
-                        for (int u = 0; u < 4; u++)
-#pragma unroll
-                            for (int v = 0; v < 4; v++) {
-                                const int i = k1 + ti * GT + ty + 16 * u, j = k1 + tj * GT + tx + 16 * v;
-                                if (i < k1 + bs1 && j <= i) a.T[(size_t)i * n + j] -= acc[u][v];
-                            }
-                        __syncthreads();
-                    }
-                factor_diag(kb + 1, -1, 0);
-            }
-            const int ntt = (rest + TT - 1) / TT, ntiles = ntt * (ntt + 1) / 2;
-            const int ncr = blocked ? 0 : (k1 + TT - 1) / TT, nall = ntiles + ntt * ncr;
-            const int t0 = G > 1 ? bx - 1 : 0, dt = G > 1 ? G - 1 : 1;
-            for (int t = t0; t >= 0 && t < nall; t += dt) {
-                bool ok;
-                if (t < ntiles) {
-                    int bi, bj;
-                    tri_tile(t, bi, bj);
-                    ok = trailing_tile_tc<BD>(ts, a.uh, a.ul, a.uh, a.ul, a.T, n, n, k1 + bi * TT, k1 + bj * TT,
-                                              t == 0 ? k1 + bs1 : 0, 0);
-                } else {
-                    const int tr = t - ntiles;
-                    ok = trailing_tile_tc<BD>(ts, a.uh, a.ul, a.xh, a.xl, a.Li, n, ldl, k1 + (tr / ncr) * TT,
-                                              (tr % ncr) * TT, k0, k1);
+                for (int u = 0; u < 4; u++) {
+                    ui[u] = S0[c][ty + 16 * u];
+                    uj[u] = S0[c][tx + 16 * u];
                 }
-                if (!ok) return;
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] = fmaf(ui[u], uj[v], acc[u][v]);
+            }
+            __syncthreads();                                // S0 is overwritten with the updated block
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int rr = ty + 16 * u, cc = tx + 16 * v;
+                    S0[rr][cc] = (rr < bs1 && cc <= rr) ? dv[u][v] - acc[u][v] : (rr == cc ? 1.f : 0.f);
+                }
+        }
+        __syncthreads();
+        const int f = block_chol_inv64(S0, S1, bs1, tmpb);
+        if (f >= 0) {
+            if (tid == 0) {
+                a.status[0] = k1 + f;
+                __threadfence();
+            }
+        } else {
+            for (int e = tid; e < BD * BD; e += PS_THREADS) {
+                const int rr = e / BD, q = e % BD;
+                if (rr < bs1 && q < bs1) {
+                    a.Li[(size_t)(k1 + rr) * ldl + k1 + q] = S1[rr][q];
+                    a.LiT[(size_t)(k1 + rr) * ldl + k1 + q] = S1[q][rr];
+                }
             }
         }
-        if (!grid_barrier(a.bar, a.err, G)) return;
+        __syncthreads();
+        if (tid == 0 && a.tm) atomicAdd(a.tm + 7, gtimer() - t_own);
+        return f < 0;
+    };
+    // Pipelined factor (64-wide blocks, four CTAs or more): CTA 0, the owner, runs one step
+    // ahead of the others.  At step kb it waits until the trailing tile 0 of step kb - 1 is
+    // done (flag T), forms the panel tile of the rows of block kb + 1 itself (the critical
+    // one; flag U), then updates and factors the next diagonal block (flag X).  The other
+    // CTAs, the workers, wait for X_kb (flag X), form the rest of the panel and block row kb
+    // of L^{-1}, pass a barrier among themselves, wait for the critical tile (flag U) and
+    // run the trailing and inverse tiles; the worker with trailing tile 0 raises flag T.  So
+    // the chain of diagonal blocks is the owner's alone and no grid barrier lies on it.  The
+    // split U^T alternates between two buffers by step, as the owner writes step kb + 1's
+    // critical tile while the workers still read step kb's.
+    const bool piped = BD == 64 && G >= 4 && nb > 1;
+    if (piped) {
+        unsigned *fl_x = a.bar + 1, *fl_u = a.bar + 2, *fl_t = a.bar + 3, *wbar = a.bar + 4;
+        const size_t ubuf = (size_t)(n + TT) * BD;
+        if (bx == 0) {
+            factor_diag(0, -1, 0);
+            flag_set(fl_x, 1);
+            NQS_PHASE(0);
+            for (int kb = 0; kb < nb; kb++) {
+                const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
+                if (rest <= 0 || __ldcg(a.status) >= 0) break;
+                if (kb > 0 && !flag_wait(fl_t, kb)) return;
+                NQS_PHASE(1);
+                owner_step(kb, a.uh + (kb & 1) * ubuf, a.ul + (kb & 1) * ubuf, fl_u);
+                flag_set(fl_x, kb + 2);                     // also wakes the workers after a breakdown
+                NQS_PHASE(2);
+            }
+        } else {
+            const int wid = bx - 1, W = G - 1;
+            for (int kb = 0; kb < nb; kb++) {
+                const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
+                if (rest <= 0) break;
+                if (!flag_wait(fl_x, kb + 1)) return;
+                float *uhk = a.uh + (kb & 1) * ubuf, *ulk = a.ul + (kb & 1) * ubuf;
+                {
+                    const int npt = (rest + GT - 1) / GT - 1;   // panel row tiles after the critical one
+                    const int ntasks = npt + (blocked ? 0 : xrow_tasks(k0, true));
+                    for (int t = wid; t < ntasks; t += W) {
+                        if (t >= npt) xrow_tile(k0, bs, true, t - npt);
+                        else panel_tile(k0, bs, 0, k1 + (t + 1) * GT, uhk, ulk);
+                    }
+                }
+                if (!grid_barrier(wbar, a.err, W)) return;
+                if (!flag_wait(fl_u, kb + 1)) return;
+                {
+                    const int bs1 = min(BD, rest);
+                    const int ntt = (rest + TT - 1) / TT, ntiles = ntt * (ntt + 1) / 2;
+                    const int ncr = blocked ? 0 : (k1 + TT - 1) / TT, nall = ntiles + ntt * ncr;
+                    for (int t = wid; t < nall; t += W) {
+                        bool ok;
+                        if (t < ntiles) {
+                            int bi, bj;
+                            tri_tile(t, bi, bj);
+                            ok = trailing_tile_tc<BD>(ts, uhk, ulk, uhk, ulk, a.T, n, n, k1 + bi * TT, k1 + bj * TT,
+                                                      t == 0 ? k1 + bs1 : 0, 0);
+                            if (ok && t == 0) flag_set(fl_t, kb + 1);
+                        } else {
+                            const int tr = t - ntiles;
+                            ok = trailing_tile_tc<BD>(ts, uhk, ulk, a.xh, a.xl, a.Li, n, ldl, k1 + (tr / ncr) * TT,
+                                                      (tr % ncr) * TT, k0, k1);
+                        }
+                        if (!ok) return;
+                    }
+                }
+                if (!grid_barrier(wbar, a.err, W)) return;
+            }
+            if (!flag_wait(fl_x, nb)) return;               // the last diagonal block (or a breakdown)
+        }
         if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
-        NQS_PHASE(2);
+        if (!grid_barrier(a.bar, a.err, G)) return;
+    } else {
+        if (bx == 0) factor_diag(0, -1, 0);
+        if (!grid_barrier(a.bar, a.err, G)) return;
+        if (__ldcg(a.status) >= 0) return;                      // broken factor: every CTA leaves here
+        NQS_PHASE(0);
+        for (int kb = 0; kb < nb; kb++) {
+            const int k0 = kb * BD, bs = min(BD, n - k0), k1 = k0 + bs, rest = n - k1;
+            if (rest <= 0) break;
+            // panel: U[k0 + c][r] = sum_m X_kk[c][m] A[r][k0 + m] for r >= k1; block row kb of X
+            {
+                constexpr int NCT = (BD + GT - 1) / GT;          // column tiles of the panel
+                const int ntr = (rest + GT - 1) / GT, npt = NCT * ntr;
+                const int ntasks = npt + (blocked ? 0 : xrow_tasks(k0, true));
+                for (int t = bx; t < ntasks; t += G) {
+                    if (t >= npt) {
+                        xrow_tile(k0, bs, true, t - npt);
+                        continue;
+                    }
+                    const int c0 = (t % NCT) * GT, r0 = k1 + (t / NCT) * GT;
+                    if (c0 >= bs) continue;
+                    panel_tile(k0, bs, c0, r0, a.uh, a.ul);
+                }
+            }
+            if (!grid_barrier(a.bar, a.err, G)) return;
+            NQS_PHASE(1);
+            // trailing update, with the next diagonal block updated and factored by CTA 0, and
+            // the update of R by block row kb of X
+            {
+                const int bs1 = min(BD, rest);                  // order of the next diagonal block
+                if (bx == 0 && BD == 64) {
+                    factor_diag(kb + 1, k0, bs);                // the update fused into the block's load
+                } else if (bx == 0) {
+                    // D -= U_kb^T U_kb on the lower 64 x 64 tiles of the next diagonal block, FP32
+                    // from U (= L^T, the upper triangle rows k0 .. k0 + bs - 1 of T)
+                    const float *U = a.T + (size_t)k0 * n;
+                    for (int ti = 0; ti * GT < bs1; ti++)
+                        for (int tj = 0; tj <= ti; tj++) {
+                            float acc[4][4] = {};
+                            gemm64<true, true>(acc, U, n, k1 + ti * GT, k1 + bs1, U, n, k1 + tj * GT, k1 + bs1, 0, bs, TS);
+    #pragma unroll
+                            for (int u = 0; u < 4; u++)
+    #pragma unroll
+                                for (int v = 0; v < 4; v++) {
+                                    const int i = k1 + ti * GT + ty + 16 * u, j = k1 + tj * GT + tx + 16 * v;
+                                    if (i < k1 + bs1 && j <= i) a.T[(size_t)i * n + j] -= acc[u][v];
+                                }
+                            __syncthreads();
+                        }
+                    factor_diag(kb + 1, -1, 0);
+                }
+                const int ntt = (rest + TT - 1) / TT, ntiles = ntt * (ntt + 1) / 2;
+                const int ncr = blocked ? 0 : (k1 + TT - 1) / TT, nall = ntiles + ntt * ncr;
+                const int t0 = G > 1 ? bx - 1 : 0, dt = G > 1 ? G - 1 : 1;
+                for (int t = t0; t >= 0 && t < nall; t += dt) {
+                    bool ok;
+                    if (t < ntiles) {
+                        int bi, bj;
+                        tri_tile(t, bi, bj);
+                        ok = trailing_tile_tc<BD>(ts, a.uh, a.ul, a.uh, a.ul, a.T, n, n, k1 + bi * TT, k1 + bj * TT,
+                                                  t == 0 ? k1 + bs1 : 0, 0);
+                    } else {
+                        const int tr = t - ntiles;
+                        ok = trailing_tile_tc<BD>(ts, a.uh, a.ul, a.xh, a.xl, a.Li, n, ldl, k1 + (tr / ncr) * TT,
+                                                  (tr % ncr) * TT, k0, k1);
+                    }
+                    if (!ok) return;
+                }
+            }
+            if (!grid_barrier(a.bar, a.err, G)) return;
+            if (__ldcg(a.status) >= 0) return;                  // broken factor: every CTA leaves here
+            NQS_PHASE(2);
+        }
     }
     // ---------------- the last block row of L^{-1}
     if (!blocked && nb > 1) {
@@ -1267,10 +1606,151 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     }
     NQS_PHASE(3);
 
-    // ---------------- right-hand side
     const int Ns = a.Ns;
     const long P = a.P;
-    if (a.space == 1) {
+    // ---------------- the parameter-space operator in double-float arithmetic
+    // q = O_c^T (O_c v) / N_s + shift v, or the right-hand side O_c^T eps / N_s, from the
+    // double-float words of O_c (oh + ol) with v split likewise (vh + vl).  The rows of O_c
+    // are cut into chunks of DF_ROWS, dealt to the CTAs in turn: a warp forms u_i = o_i . v
+    // for one row of the chunk at a time (double-float butterfly over the lanes), then every
+    // thread accumulates sum_i u_i o_i over the chunk for its four-column groups (eight
+    // rows' loads in flight); after one grid barrier the chunks' partial column sums are
+    // summed in FP64 in chunk order (eight warps over the chunks, then the warps in order).
+    // The chunking does not depend on the grid size, so a system solved by a slice of a
+    // batch launch gets the same bits as by the whole grid.
+    constexpr int DF_ROWS = 32;
+    __shared__ double redc[PS_THREADS / 32][32];
+    const int ndc = (Ns + DF_ROWS - 1) / DF_ROWS;
+    const bool df_op = a.space == 1 && a.oh != nullptr && df_words_ok(P) && 8 * P + 8 * DF_ROWS <= PS_SMEM;
+    auto op_df = [&](const double *v, double *q, bool rhs_mode) -> bool {
+        const int warp = tid >> 5;
+        float *vh = psm, *vl = vh + P, *uh = vl + P, *ul = uh + DF_ROWS;
+        const long P4 = P >> 2;
+        if (!rhs_mode) {
+            for (long k = tid; k < P; k += PS_THREADS) {
+                const double x = __ldcg(v + k);
+                const float h = __double2float_rn(x);
+                vh[k] = h;
+                vl[k] = __double2float_rn(x - (double)h);
+            }
+        }
+        __syncthreads();
+        const float4 *oh4 = (const float4 *)a.oh, *ol4 = (const float4 *)a.ol;
+        const float4 *vh4 = (const float4 *)vh, *vl4 = (const float4 *)vl;
+        for (int ch = bx; ch < ndc; ch += G) {
+            const int i0 = ch * DF_ROWS, nr = min(Ns, i0 + DF_ROWS) - i0;
+            if (rhs_mode) {
+                for (int r = tid; r < nr; r += PS_THREADS) {
+                    const double x = __ldcg(a.eps + i0 + r);
+                    const float h = __double2float_rn(x);
+                    uh[r] = h;
+                    ul[r] = __double2float_rn(x - (double)h);
+                }
+            } else {
+                for (int r = warp; r < nr; r += PS_THREADS / 32) {
+                    const size_t rb = (size_t)(i0 + r) * P4;
+                    float sh0 = 0.f, sl0 = 0.f, sh1 = 0.f, sl1 = 0.f;
+                    for (long g0 = lane; g0 < P4; g0 += 32 * 8) {
+                        // eight groups' loads in flight per lane before their products
+                        float4 xh[8], xl[8];
+#pragma unroll
+                        for (int t = 0; t < 8; t++) {
+                            const long g = g0 + 32 * t;
+                            xh[t] = g < P4 ? __ldcg(oh4 + rb + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+                            xl[t] = g < P4 ? __ldcg(ol4 + rb + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
+#pragma unroll
+                        for (int t = 0; t < 8; t++) {
+                            const long g = g0 + 32 * t;
+                            if (g < P4) {
+                                const float4 yh = vh4[g], yl = vl4[g];
+                                df_fma(sh0, sl0, xh[t].x, xl[t].x, yh.x, yl.x);
+                                df_fma(sh1, sl1, xh[t].y, xl[t].y, yh.y, yl.y);
+                                df_fma(sh0, sl0, xh[t].z, xl[t].z, yh.z, yl.z);
+                                df_fma(sh1, sl1, xh[t].w, xl[t].w, yh.w, yl.w);
+                            }
+                        }
+                    }
+                    df_add(sh0, sl0, sh1, sl1);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+                        df_add(sh0, sl0, __shfl_xor_sync(0xffffffffu, sh0, o), __shfl_xor_sync(0xffffffffu, sl0, o));
+                    if (lane == 0) {
+                        uh[r] = sh0;
+                        ul[r] = sl0;
+                    }
+                }
+            }
+            __syncthreads();
+            for (long g = tid; g < P4; g += PS_THREADS) {
+                float chh[4] = {0.f, 0.f, 0.f, 0.f}, cll[4] = {0.f, 0.f, 0.f, 0.f};
+                int r = 0;
+                for (; r + 7 < nr; r += 8) {
+                    float4 xh[8], xl[8];
+#pragma unroll
+                    for (int t = 0; t < 8; t++) {
+                        xh[t] = __ldcg(oh4 + (size_t)(i0 + r + t) * P4 + g);
+                        xl[t] = __ldcg(ol4 + (size_t)(i0 + r + t) * P4 + g);
+                    }
+#pragma unroll
+                    for (int t = 0; t < 8; t++) {
+                        const float wh = uh[r + t], wl = ul[r + t];
+                        df_fma(chh[0], cll[0], xh[t].x, xl[t].x, wh, wl);
+                        df_fma(chh[1], cll[1], xh[t].y, xl[t].y, wh, wl);
+                        df_fma(chh[2], cll[2], xh[t].z, xl[t].z, wh, wl);
+                        df_fma(chh[3], cll[3], xh[t].w, xl[t].w, wh, wl);
+                    }
+                }
+                for (; r < nr; r++) {
+                    const float4 xh = __ldcg(oh4 + (size_t)(i0 + r) * P4 + g),
+                                 xl = __ldcg(ol4 + (size_t)(i0 + r) * P4 + g);
+                    const float wh = uh[r], wl = ul[r];
+                    df_fma(chh[0], cll[0], xh.x, xl.x, wh, wl);
+                    df_fma(chh[1], cll[1], xh.y, xl.y, wh, wl);
+                    df_fma(chh[2], cll[2], xh.z, xl.z, wh, wl);
+                    df_fma(chh[3], cll[3], xh.w, xl.w, wh, wl);
+                }
+#pragma unroll
+                for (int c = 0; c < 4; c++) a.upart[(size_t)ch * P + 4 * g + c] = (double)chh[c] + (double)cll[c];
+            }
+            __syncthreads();                                // uh / ul are refilled for the next chunk
+        }
+        if (!grid_barrier(a.bar, a.err, G)) return false;
+        const long ncg = (P + 31) / 32;
+        for (long cg = bx; cg < ncg; cg += G) {
+            const long k = cg * 32 + lane;
+            double s4[4] = {0.0, 0.0, 0.0, 0.0};
+            if (k < P) {
+                int b = warp;
+                for (; b + 24 < ndc; b += 32) {
+#pragma unroll
+                    for (int h = 0; h < 4; h++) s4[h] += __ldcg(a.upart + (size_t)(b + 8 * h) * P + k);
+                }
+                for (; b < ndc; b += 8) s4[0] += __ldcg(a.upart + (size_t)b * P + k);
+            }
+            redc[warp][lane] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+            __syncthreads();
+            if (warp == 0 && k < P) {
+                double t = 0.0;
+#pragma unroll
+                for (int w = 0; w < PS_THREADS / 32; w++) t += redc[w][lane];
+                t /= (double)Ns;
+                if (rhs_mode) {
+                    q[k] = t;
+                    a.rf[k] = (float)t;
+                } else {
+                    q[k] = t + a.shift * __ldcg(v + k);
+                }
+            }
+            __syncthreads();
+        }
+        return grid_barrier(a.bar, a.err, G);
+    };
+
+    // ---------------- right-hand side
+    if (df_op) {
+        if (!op_df(nullptr, a.rhs, true)) return;
+    } else if (a.space == 1) {
         colsum_partial(a.O, Ns, P, a.eps, a.upart, gwarp, gwarps, lane);
         if (!grid_barrier(a.bar, a.err, G)) return;
         for (long k = gwarp; k < P; k += gwarps) {
@@ -1280,13 +1760,14 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
                 a.rf[k] = (float)s;
             }
         }
+        if (!grid_barrier(a.bar, a.err, G)) return;
     } else {
         for (int i = gtid; i < n; i += gthreads) {
             a.rhs[i] = a.eps[i];
             a.rf[i] = (float)a.eps[i];
         }
+        if (!grid_barrier(a.bar, a.err, G)) return;
     }
-    if (!grid_barrier(a.bar, a.err, G)) return;
     NQS_PHASE(5);
 
     // ---------------- preconditioned conjugate gradients in FP64 on the exact
@@ -1397,6 +1878,7 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     };
     // q = A v: O_c (O_c^T v) / N_s + shift v (samples) or O_c^T (O_c v) / N_s + shift v (parameters)
     auto apply_op = [&](const double *v, double *q) -> bool {
+        if (df_op) return op_df(v, q, false);
         if (a.space == 0) {
             colsum_partial(a.O, Ns, P, v, a.upart, gwarp, gwarps, lane);
             if (!grid_barrier(a.bar, a.err, G)) return false;
@@ -1549,7 +2031,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrA
 
 // ---------------------------------------------------------------- driver
 struct MixedWs {
-    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf, uh, ul, xh, xl;
+    DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf, uh, ul, xh, xl, oh, ol;
     DevBuf<double> rhs, r, u, upart, nrm, p, q, z;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -1583,7 +2065,7 @@ static MixedPlan plan_mixed(int Ns, long P, int space_opt, int passes) {
 // Param-space operand: hi[k][i] = tf32(O_c[i][k]) (row pitch ldn), via 32 x 32
 // shared-memory transposes; O is centred in place as in k_center_split.
 __global__ void k_center_split_t(double *O, int Ns, long P, const double *__restrict__ gm, float *hi, float *lo,
-                                 long ldn) {
+                                 long ldn, float *oh, float *ol) {
     __shared__ float th[32][33], tl[32][33];
     const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
     const long tk = (P + 31) / 32, ti = (Ns + 31) / 32;
@@ -1598,6 +2080,10 @@ __global__ void k_center_split_t(double *O, int Ns, long P, const double *__rest
                 const float xf = (float)x;
                 h = tf32_rna(xf);
                 l = tf32_rna(xf - h);
+                if (oh) {                                   // the double-float words of O_c
+                    oh[i * P + k] = xf;
+                    ol[i * P + k] = (float)(x - (double)xf);
+                }
             }
             th[r][tx] = h;
             tl[r][tx] = l;
@@ -1629,7 +2115,9 @@ static void enqueue_front(MixedWs &w, const MixedPlan &pl, double *O, const doub
         k_center_split<<<ctx().sm_count * 8, 256, 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, pl.k_pad);
     } else {
         NQS_LAUNCH("center_split_t");
-        k_center_split_t<<<ctx().sm_count * 8, dim3(32, 8), 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, pl.k_pad);
+        const bool df = df_words_ok(P) && w.oh.n >= (size_t)Ns * P;
+        k_center_split_t<<<ctx().sm_count * 8, dim3(32, 8), 0, st>>>(O, Ns, P, gm, w.hi.p, w.lo.p, pl.k_pad,
+                                                                    df ? w.oh.p : nullptr, df ? w.ol.p : nullptr);
     }
     GramTcArgs g;
     g.kt_per_seg = (int)(pl.k_pad / TC_K);
@@ -1683,6 +2171,9 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     fa.ul = w.ul.p;
     fa.xh = w.xh.p;
     fa.xl = w.xl.p;
+    const bool df = pl.space == 1 && df_words_ok(P) && w.oh.n >= (size_t)Ns * P;
+    fa.oh = df ? w.oh.p : nullptr;
+    fa.ol = df ? w.ol.p : nullptr;
     fa.bd = pl.n >= BD_SWITCH ? BD_LARGE : BD_SMALL;
     fa.zf = w.zf.p;
     fa.nrm = w.nrm.p;
@@ -1696,7 +2187,7 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
 
 // Zeroed words and vectors the factor / refinement kernel expects.
 static void enqueue_fr_clear(MixedWs &w, const FrArgs &fa, cudaStream_t st) {
-    cudaMemsetAsync(w.bar.p, 0, 2 * sizeof(unsigned), st);
+    cudaMemsetAsync(w.bar.p, 0, 8 * sizeof(unsigned), st);
     cudaMemsetAsync(w.tm.p, 0, 8 * sizeof(unsigned long long), st);
     cudaMemsetAsync(w.rf.p, 0, sizeof(float) * fa.ldl, st);
     cudaMemsetAsync(w.zf.p, 0, sizeof(float) * fa.ldl, st);
@@ -1740,8 +2231,9 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         *moved = true;
     }
     const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[20] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p};
+    const void *before[22] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p,
+                              w.oh.p, w.ol.p};
     const int ldl = (n + 31) / 32 * 32;
     // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero.
     // Sized for the wide diagonal block so a batch's autotuner can pick either width.
@@ -1750,12 +2242,15 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
         !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
         !w.xh.ensure(nu) || !w.xl.ensure(nu) ||
-        !w.upart.ensure((size_t)((Ns + RCH - 1) / RCH) * P) || !w.nrm.ensure(3) || !w.status.ensure(2) ||
-        !w.bar.ensure(2) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
+        (pl.space == 1 && df_words_ok(P) && (!w.oh.ensure((size_t)Ns * P) || !w.ol.ensure((size_t)Ns * P))) ||
+        !w.upart.ensure((size_t)((Ns + 31) / 32) * P) || !w.nrm.ensure(3) ||
+        !w.status.ensure(2) ||
+        !w.bar.ensure(8) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
-    const void *after[20] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
-                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p};
-    for (int i = 0; i < 20; i++) *moved |= before[i] != after[i];
+    const void *after[22] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+                             w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p,
+                             w.oh.p, w.ol.p};
+    for (int i = 0; i < 22; i++) *moved |= before[i] != after[i];
     if (*moved || w.n != n) {
         // the pad columns of L^{-1} are read (as zeros) by the vectorised solves,
         // the pad rows of the split U^T and X^T by the tensor-core tiles

@@ -37,12 +37,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Bounded wait: gives up after ~2^24 polls with back-off (seconds), raises the
-// kernel's error flag and reports failure instead of spinning forever.
+// kernel's error flag and reports failure instead of spinning forever.  The error word
+// (global memory, an L2 round trip) is read every 32nd poll only, so a completion is
+// seen within one poll of its arrival.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
     for (uint32_t it = 0; it < (1u << 24); it++) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (*((volatile int *)err)) return false;
-        if (it > 32) __nanosleep(64);
+        if ((it & 31) == 31) {
+            if (*((volatile int *)err)) return false;
+            if (it > 256) __nanosleep(64);
+        }
     }
     atomicExch(err, 1);
     return false;
@@ -115,6 +119,7 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 
 }  // namespace nqs
 
