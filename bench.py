@@ -322,16 +322,17 @@ def exact_e0(name="heisenberg_4x4_pbc_sz0"):
 # DRAM bytes (read + write) per launch from one ncu capture of the kernel on this
 # workload (dram__bytes_read.sum + dram__bytes_write.sum), and the summary file.
 NCU_TRAFFIC = {
-    "factor_refine": (39.731456e6 + 0.294144e6, "profiles/factor_refine_heisenberg4x4_params1120_full.md"),
+    "factor_refine": (40.079360e6 + 0.204800e6, "profiles/factor_refine_heisenberg4x4_params1120_full.md"),
     "gram_tc": (37.775616e6 + 7.168e3, "profiles/gram_tc_split_params1120_ns4096_full.md"),
 }
 
 # What bounds each kernel whose roofline is reported ("bound" names the pipe the fraction is
 # taken against; these kernels do not run at that pipe's rate)
 LIMITERS = {
-    "factor_refine": "latency: a sequential chain of diagonal-block factors (one CTA) between grid "
-                     "barriers, SIMT FP32 panels and inverse, FP64 CG operator passes; the trailing "
-                     "updates alone run on the tensor cores",
+    "factor_refine": "latency: the chain of diagonal-block factors run by one CTA ahead of the others "
+                     "(FP32 SIMT, ~21 us per 64-wide block), then the CG operator passes (double-float "
+                     "on the FP32 pipe, L2-latency bound); the trailing and inverse tiles run on the "
+                     "tensor cores beside the chain",
     "gram_tc": "tensor pipe and L2 / HBM operand traffic (TF32 split, three passes)",
     "gram_fp64": "FP64 pipe (SIMT)",
     "chol_syrk": "FP64 pipe (SIMT)",
