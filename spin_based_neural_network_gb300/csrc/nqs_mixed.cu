@@ -237,6 +237,26 @@ __device__ __forceinline__ void df_add(float &sh, float &sl, float bh, float bl)
     sh = __fadd_rn(t, lo);
     sl = __fsub_rn(lo, __fsub_rn(sh, t));
 }
+// x as two FP32 words h + l, h = x truncated to 24 significant bits and l = the remainder
+// rounded to FP32 (|x - h - l| <= 2^-48 |x|), built from the bits of x on the integer and FP32
+// pipes for 2^-113 <= |x| < 2^78; other values (zero included) go through FP64 conversions.
+// The FP64 pipe of this GPU is 1/64 of the FP32 pipe, and conversions from FP64 run on it.
+__device__ __forceinline__ void split_f64_words(double x, float &h, float &l) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7FF);
+    if (E >= 910 && E <= 1100) {
+        const unsigned sg = (unsigned)(b >> 63) << 31;
+        const unsigned long long M = b & ((1ull << 52) - 1);
+        h = __uint_as_float(sg | ((unsigned)(E - 896) << 23) | (unsigned)(M >> 29));
+        const float sc = __uint_as_float((unsigned)(E - 908) << 23);          // 2^(E - 1075 + 40)
+        const float r = __fmul_rn(__fmul_rn(__uint2float_rn((unsigned)(M & 0x1FFFFFFFull)), sc), 0x1p-40f);
+        l = __uint_as_float(__float_as_uint(r) | sg);
+    } else {
+        h = __double2float_rn(x);
+        l = __double2float_rn(x - (double)h);
+    }
+}
+
 // The parameter-space operator runs in double-float when N_p is a multiple of 4 (float4
 // rows) and at most 2048 (two four-column groups per thread).
 __host__ __device__ inline bool df_words_ok(long P) { return (P & 3) == 0 && P <= 8 * 256; }
@@ -879,6 +899,30 @@ __device__ __forceinline__ float dot4_range(const float *row, const float *v, in
     return t;
 }
 
+// The same with v in shared memory.
+__device__ __forceinline__ float dot4_range_sv(const float *row, const float *v, int g0, int g1, int lane) {
+    const float4 *r4 = (const float4 *)row, *v4 = (const float4 *)v;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int g = g0 + lane;
+    for (; g + 96 < g1; g += 128) {
+        const float4 x0 = __ldcg(r4 + g), x1 = __ldcg(r4 + g + 32), x2 = __ldcg(r4 + g + 64),
+                     x3 = __ldcg(r4 + g + 96);
+        const float4 y0 = v4[g], y1 = v4[g + 32], y2 = v4[g + 64], y3 = v4[g + 96];
+        s0 += (x0.x * y0.x + x0.y * y0.y) + (x0.z * y0.z + x0.w * y0.w);
+        s1 += (x1.x * y1.x + x1.y * y1.y) + (x1.z * y1.z + x1.w * y1.w);
+        s2 += (x2.x * y2.x + x2.y * y2.y) + (x2.z * y2.z + x2.w * y2.w);
+        s3 += (x3.x * y3.x + x3.y * y3.y) + (x3.z * y3.z + x3.w * y3.w);
+    }
+    for (; g < g1; g += 32) {
+        const float4 x0 = __ldcg(r4 + g), y0 = v4[g];
+        s0 += (x0.x * y0.x + x0.y * y0.y) + (x0.z * y0.z + x0.w * y0.w);
+    }
+    float t = (s0 + s1) + (s2 + s3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
 // a . b and a . c over [0, n), computed by every CTA in the same fixed order (four
 // thread-strided partial sums with their loads issued together, a warp butterfly, then
 // the warps in order), so that all CTAs hold the same values whatever the grid size.
@@ -1111,6 +1155,7 @@ struct FrArgs {
     double shift;
     double *x;          // [n] solution
     double *rhs, *r;    // [n] right-hand side and residual
+    double *r2;         // [n] the residual's second buffer (the double-float CG alternates them)
     double *u, *upart;  // intermediate vector, partial column sums ([N_s / 32][N_p])
     double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
@@ -1622,16 +1667,24 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     __shared__ double redc[PS_THREADS / 32][32];
     const int ndc = (Ns + DF_ROWS - 1) / DF_ROWS;
     const bool df_op = a.space == 1 && a.oh != nullptr && df_words_ok(P) && 8 * P + 8 * DF_ROWS <= PS_SMEM;
-    auto op_df = [&](const double *v, double *q, bool rhs_mode) -> bool {
+    // With zs set, v is the CG direction formed on the fly by every CTA, v = zs (pold null) or
+    // zs + beta pold, and written to pnew by one CTA per 256 entries (so no grid barrier
+    // publishes it first).
+    auto op_df = [&](const double *v, double *q, bool rhs_mode, const double *zs = nullptr,
+                     const double *pold = nullptr, double beta = 0.0, double *pnew = nullptr) -> bool {
         const int warp = tid >> 5;
         float *vh = psm, *vl = vh + P, *uh = vl + P, *ul = uh + DF_ROWS;
         const long P4 = P >> 2;
         if (!rhs_mode) {
             for (long k = tid; k < P; k += PS_THREADS) {
-                const double x = __ldcg(v + k);
-                const float h = __double2float_rn(x);
-                vh[k] = h;
-                vl[k] = __double2float_rn(x - (double)h);
+                double x;
+                if (zs) {
+                    x = pold ? __fma_rn(beta, __ldcg(pold + k), __ldcg(zs + k)) : __ldcg(zs + k);
+                    if (bx == (int)((k / PS_THREADS) % G)) pnew[k] = x;
+                } else {
+                    x = __ldcg(v + k);
+                }
+                split_f64_words(x, vh[k], vl[k]);
             }
         }
         __syncthreads();
@@ -1640,12 +1693,7 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         for (int ch = bx; ch < ndc; ch += G) {
             const int i0 = ch * DF_ROWS, nr = min(Ns, i0 + DF_ROWS) - i0;
             if (rhs_mode) {
-                for (int r = tid; r < nr; r += PS_THREADS) {
-                    const double x = __ldcg(a.eps + i0 + r);
-                    const float h = __double2float_rn(x);
-                    uh[r] = h;
-                    ul[r] = __double2float_rn(x - (double)h);
-                }
+                for (int r = tid; r < nr; r += PS_THREADS) split_f64_words(__ldcg(a.eps + i0 + r), uh[r], ul[r]);
             } else {
                 for (int r = warp; r < nr; r += PS_THREADS / 32) {
                     const size_t rb = (size_t)(i0 + r) * P4;
@@ -1739,7 +1787,7 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
                     q[k] = t;
                     a.rf[k] = (float)t;
                 } else {
-                    q[k] = t + a.shift * __ldcg(v + k);
+                    q[k] = t + a.shift * __ldcg((zs ? pnew : v) + k);
                 }
             }
             __syncthreads();
@@ -1911,6 +1959,75 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         return grid_barrier(a.bar, a.err, G);
     };
     __shared__ double red[2 * (PS_THREADS / 32)];
+    // The double-float operator with L^{-1} (n < 4608): CG with two grid barriers fewer per
+    // iteration.  The direction p is formed inside the operator (op_df), and the
+    // preconditioner stages float(r - alpha q) in shared memory itself (precond_from), so
+    // the residual update needs no barrier before it; p and r alternate between two
+    // buffers, as the update of one and the reads of the other overlap.
+    auto precond_from = [&](const double *rs, const double *qs, double alpha, double *out) -> bool {
+        float *rfs = psm;
+        for (int j = tid; j < ldl; j += PS_THREADS)
+            rfs[j] = j < n ? (float)(qs ? __fma_rn(-alpha, __ldcg(qs + j), __ldcg(rs + j)) : __ldcg(rs + j)) : 0.f;
+        __syncthreads();
+        for (int i = gwarp; i < n; i += gwarps) {
+            const float t = dot4_range_sv(a.Li + (size_t)i * ldl, rfs, 0, (i >> 2) + 1, lane);
+            if (lane == 0) a.zf[i] = t;
+        }
+        if (!grid_barrier(a.bar, a.err, G)) return false;
+        for (int j = gwarp; j < n; j += gwarps) {
+            const float t = dot4_range(a.LiT + (size_t)j * ldl, a.zf, j >> 2, ldl >> 2, lane);
+            if (lane == 0) out[j] = (double)t;
+        }
+        return grid_barrier(a.bar, a.err, G);
+    };
+    if (df_op && !blocked) {
+        if (!precond_from(a.rhs, nullptr, 0.0, a.x)) return;     // x0 = M^{-1} rhs
+        NQS_PHASE(4);
+        if (!op_df(a.x, a.q, false)) return;
+        NQS_PHASE(5);
+        for (int i = gtid; i < n; i += gthreads) a.r[i] = __fma_rn(-1.0, __ldcg(a.q + i), __ldcg(a.rhs + i));
+        if (!precond_from(a.rhs, a.q, 1.0, a.z)) return;
+        NQS_PHASE(4);
+        const double bb = dot_all(a.rhs, a.rhs, n, red);
+        const double2 zr0 = dot_all2<true>(a.r, a.z, a.r, n, red);
+        double rho = zr0.x, rr = zr0.y, beta = 0.0;
+        double *rc = a.r, *rn = a.r2, *pc = a.p, *pn = a.u;
+        int it = 0;
+        for (; it < a.sweeps && rr > CG_RTOL * CG_RTOL * bb && rho > 0.0; it++) {
+            if (!op_df(nullptr, a.q, false, a.z, it == 0 ? nullptr : pc, beta, pn)) return;
+            NQS_PHASE(5);
+            const double pq = dot_all(pn, a.q, n, red);
+            if (!(pq > 0.0)) break;
+            const double alpha = rho / pq;
+            for (int i = gtid; i < n; i += gthreads) {
+                a.x[i] = __fma_rn(alpha, __ldcg(pn + i), __ldcg(a.x + i));
+                rn[i] = __fma_rn(-alpha, __ldcg(a.q + i), __ldcg(rc + i));
+            }
+            NQS_PHASE(-1);
+            if (!precond_from(rc, a.q, alpha, a.z)) return;
+            NQS_PHASE(4);
+            const double2 zr = dot_all2<true>(rn, a.z, rn, n, red);
+            beta = zr.x / rho;
+            rho = zr.x;
+            rr = zr.y;
+            double *t = rc;
+            rc = rn;
+            rn = t;
+            t = pc;
+            pc = pn;
+            pn = t;
+        }
+        if (bx == 0 && tid == 0) {
+            a.nrm[0] = rr;
+            a.nrm[1] = bb;
+            a.nrm[2] = (double)it;
+        }
+        if (timing) {
+            tacc[6] = gtimer() - tstart;
+            for (int k = 0; k < 7; k++) a.tm[k] = tacc[k];
+        }
+        return;
+    }
     if (!precond(a.x)) return;                          // x0 = M^{-1} rhs
     NQS_PHASE(4);
     // phase 5: the operator (and the right-hand side above); the vector updates, the dots
@@ -2032,7 +2149,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_factor_refine_batch(const FrA
 // ---------------------------------------------------------------- driver
 struct MixedWs {
     DevBuf<float> hi, lo, T, Tp, Li, LiT, rf, zf, uh, ul, xh, xl, oh, ol;
-    DevBuf<double> rhs, r, u, upart, nrm, p, q, z;
+    DevBuf<double> rhs, r, r2, u, upart, nrm, p, q, z;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
     DevBuf<unsigned long long> tm;
@@ -2077,12 +2194,13 @@ __global__ void k_center_split_t(double *O, int Ns, long P, const double *__rest
             if (i < Ns && k < P) {
                 const double x = O[i * P + k] - gm[k];
                 O[i * P + k] = x;
-                const float xf = (float)x;
-                h = tf32_rna(xf);
-                l = tf32_rna(xf - h);
+                float xh, xl;
+                split_f64_words(x, xh, xl);
+                h = tf32_rna(xh);
+                l = tf32_rna(xh - h);
                 if (oh) {                                   // the double-float words of O_c
-                    oh[i * P + k] = xf;
-                    ol[i * P + k] = (float)(x - (double)xf);
+                    oh[i * P + k] = xh;
+                    ol[i * P + k] = xl;
                 }
             }
             th[r][tx] = h;
@@ -2161,6 +2279,7 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     fa.x = x;
     fa.rhs = w.rhs.p;
     fa.r = w.r.p;
+    fa.r2 = w.r2.p;
     fa.u = w.u.p;
     fa.upart = w.upart.p;
     fa.p = w.p.p;
@@ -2231,15 +2350,16 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         *moved = true;
     }
     const long big = (long)Ns > P ? (long)Ns : P;
-    const void *before[22] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+    const void *before[23] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
                               w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p,
-                              w.oh.p, w.ol.p};
+                              w.oh.p, w.ol.p, w.r2.p};
     const int ldl = (n + 31) / 32 * 32;
     // split U^T: a trailing tile starting at row k1 + 128 bi reaches row n + 126 at most; pad rows read as zero.
     // Sized for the wide diagonal block so a batch's autotuner can pick either width.
     const size_t nu = (size_t)(n + TT) * BD_LARGE;
     if (!w.T.ensure((size_t)n * n) || !w.Li.ensure((size_t)n * ldl) || !w.LiT.ensure((size_t)n * ldl) ||
-        !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.u.ensure(big) ||
+        !w.rf.ensure(ldl) || !w.zf.ensure(ldl) || !w.rhs.ensure(n) || !w.r.ensure(n) || !w.r2.ensure(n) ||
+        !w.u.ensure(big) ||
         !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
         !w.xh.ensure(nu) || !w.xl.ensure(nu) ||
         (pl.space == 1 && df_words_ok(P) && (!w.oh.ensure((size_t)Ns * P) || !w.ol.ensure((size_t)Ns * P))) ||
@@ -2247,10 +2367,10 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         !w.status.ensure(2) ||
         !w.bar.ensure(8) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
-    const void *after[22] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
+    const void *after[23] = {w.T.p, w.Li.p, w.LiT.p, w.rf.p, w.zf.p, w.rhs.p, w.r.p, w.u.p, w.upart.p,
                              w.nrm.p, w.bar.p, w.tm.p, w.Tp.p, w.p.p, w.q.p, w.z.p, w.uh.p, w.ul.p, w.xh.p, w.xl.p,
-                             w.oh.p, w.ol.p};
-    for (int i = 0; i < 22; i++) *moved |= before[i] != after[i];
+                             w.oh.p, w.ol.p, w.r2.p};
+    for (int i = 0; i < 23; i++) *moved |= before[i] != after[i];
     if (*moved || w.n != n) {
         // the pad columns of L^{-1} are read (as zeros) by the vectorised solves,
         // the pad rows of the split U^T and X^T by the tensor-core tiles
