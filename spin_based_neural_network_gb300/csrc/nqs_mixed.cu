@@ -260,6 +260,8 @@ __device__ __forceinline__ void split_f64_words(double x, float &h, float &l) {
 // The parameter-space operator runs in double-float when N_p is a multiple of 4 (float4
 // rows) and at most 2048 (two four-column groups per thread).
 __host__ __device__ inline bool df_words_ok(long P) { return (P & 3) == 0 && P <= 8 * 256; }
+// Rows per chunk of the double-float operator: one chunk per SM at full grid, at least 8.
+static int df_chunk_rows(int Ns) { return std::max(8, (Ns + ctx().sm_count - 1) / ctx().sm_count); }
 
 // ---------------------------------------------------------------- FP32 factor, inverse and refinement
 // One cooperative launch (one CTA per SM, all co-resident) runs everything
@@ -1156,12 +1158,13 @@ struct FrArgs {
     double *x;          // [n] solution
     double *rhs, *r;    // [n] right-hand side and residual
     double *r2;         // [n] the residual's second buffer (the double-float CG alternates them)
-    double *u, *upart;  // intermediate vector, partial column sums ([N_s / 32][N_p])
+    double *u, *upart;  // intermediate vector, partial column sums ([chunks][N_p])
     double *p, *q, *z;  // [n] CG direction, operator times direction, preconditioned residual
     float *rf, *zf;     // [n] FP32 right-hand side and half-solve
     float *uh, *ul;     // [n + 128][bd] TF32 hi / lo words of the current panel U^T (K contiguous; pad rows zero)
     float *xh, *xl;     // [n + 128][bd] TF32 hi / lo words of X^T over the current block row of X = L^{-1}
     const float *oh, *ol;  // [N_s][N_p] O_c as double-float words (FP32 hi + lo), or null
+    int df_rows;        // rows per chunk of the double-float operator (from N_s and the SM count only)
     int bd;             // diagonal block width (BD_SMALL or BD_LARGE)
     double *nrm;        // [3] |r|^2, |rhs|^2, CG iterations run
     int sweeps;         // maximum CG iterations
@@ -1661,12 +1664,14 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     // thread accumulates sum_i u_i o_i over the chunk for its four-column groups (eight
     // rows' loads in flight); after one grid barrier the chunks' partial column sums are
     // summed in FP64 in chunk order (eight warps over the chunks, then the warps in order).
-    // The chunking does not depend on the grid size, so a system solved by a slice of a
-    // batch launch gets the same bits as by the whole grid.
-    constexpr int DF_ROWS = 32;
+    // The chunking does not depend on the grid size (a.df_rows comes from N_s and the SM
+    // count), so a system solved by a slice of a batch launch gets the same bits as by the
+    // whole grid, and at full grid every CTA has one chunk.
+    const int DF_ROWS = a.df_rows;
     __shared__ double redc[PS_THREADS / 32][32];
     const int ndc = (Ns + DF_ROWS - 1) / DF_ROWS;
-    const bool df_op = a.space == 1 && a.oh != nullptr && df_words_ok(P) && 8 * P + 8 * DF_ROWS <= PS_SMEM;
+    const bool df_op = a.space == 1 && a.oh != nullptr && df_words_ok(P) && DF_ROWS > 0 &&
+                       8 * P + 8 * (long)DF_ROWS <= PS_SMEM;
     // With zs set, v is the CG direction formed on the fly by every CTA, v = zs (pold null) or
     // zs + beta pold, and written to pnew by one CTA per 256 entries (so no grid barrier
     // publishes it first).
@@ -2293,6 +2298,7 @@ static FrArgs make_frargs(MixedWs &w, const MixedPlan &pl, double *O, const doub
     const bool df = pl.space == 1 && df_words_ok(P) && w.oh.n >= (size_t)Ns * P;
     fa.oh = df ? w.oh.p : nullptr;
     fa.ol = df ? w.ol.p : nullptr;
+    fa.df_rows = df_chunk_rows(Ns);
     fa.bd = pl.n >= BD_SWITCH ? BD_LARGE : BD_SMALL;
     fa.zf = w.zf.p;
     fa.nrm = w.nrm.p;
@@ -2363,7 +2369,8 @@ static bool prepare_ws(MixedWs &w, const MixedPlan &pl, int Ns, long P, cudaStre
         !w.p.ensure(n) || !w.q.ensure(n) || !w.z.ensure(n) || !w.uh.ensure(nu) || !w.ul.ensure(nu) ||
         !w.xh.ensure(nu) || !w.xl.ensure(nu) ||
         (pl.space == 1 && df_words_ok(P) && (!w.oh.ensure((size_t)Ns * P) || !w.ol.ensure((size_t)Ns * P))) ||
-        !w.upart.ensure((size_t)((Ns + 31) / 32) * P) || !w.nrm.ensure(3) ||
+        !w.upart.ensure((size_t)std::max((Ns + 31) / 32, (Ns + df_chunk_rows(Ns) - 1) / df_chunk_rows(Ns)) * P) ||
+        !w.nrm.ensure(3) ||
         !w.status.ensure(2) ||
         !w.bar.ensure(8) || !w.tm.ensure(8) || (pl.split && !w.Tp.ensure(3 * (size_t)n * n)))
         return false;
