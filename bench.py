@@ -932,7 +932,9 @@ def run_gpu(args):
     phases = None
     if prec == abi.PREC_MIXED:
         ph = nqs.last_step_stats().phase_us
-        phases = dict(zip(("first_diag_block", "panels", "trailing_with_next_diag_block", "triangular_inverse",
+        # the headline's factor is the pipelined one (64-wide blocks on every SM): slot 1 is CTA 0
+        # waiting for the other CTAs, slot 2 CTA 0's chain of diagonal-block steps
+        phases = dict(zip(("first_diag_block", "owner_wait_for_workers", "owner_chain", "last_inverse_block_row",
                            "preconditioner", "rhs_and_operator", "total", "diag_block_owner_work"),
                           [round(ph[i], 1) for i in range(8)]))
         phases["cg_vector_updates_and_dots"] = round(ph[6] - sum(ph[i] for i in range(6)), 1)

@@ -327,13 +327,14 @@ typedef struct {
     int    mixed_fallback;   /* 1 if the FP32 factor failed and FP64 solved the step */
     int    pad_;
     /* MIXED: microseconds spent in the phases of the cooperative factor /
-     * inverse / CG kernel (seen from CTA 0): [0] the first diagonal block, [1] panels,
-     * [2] trailing updates (each with the next diagonal block's update and factor,
-     * done by CTA 0 beside the trailing tiles), [3] triangular inverse, [4] preconditioner
-     * applications, [5] right-hand side and operator products, [6] total (the
-     * CG vector updates and dot products are the rest of it); [7] the time the
-     * owning CTAs spent on loading, updating, factoring and inverting the
-     * diagonal blocks (summed over the blocks) */
+     * inverse / CG kernel (seen from CTA 0): [0] the first diagonal block; with the
+     * pipelined factor (64-wide blocks, four CTAs or more) [1] CTA 0 waiting for the
+     * other CTAs and [2] CTA 0's own chain of diagonal-block steps, otherwise [1] panels
+     * and [2] trailing updates (each with the next diagonal block's update and factor by
+     * CTA 0 beside the trailing tiles); [3] the last block row of L^{-1} (or the whole
+     * inverse); [4] preconditioner applications, [5] right-hand side and operator
+     * products, [6] total (the CG vector updates and dot products are the rest of it);
+     * [7] the time CTA 0 spent on its diagonal-block steps (summed over the blocks) */
     double phase_us[8];
     /* MIXED with mixed_check and fp32_estimator: |<E> - <E>_fp64| / |<E>_fp64|
      * on the same samples (-1 when not measured) */

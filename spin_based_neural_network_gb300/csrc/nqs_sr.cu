@@ -133,14 +133,27 @@ __global__ void __launch_bounds__(ES_THREADS) k_energy_mb(const double *__restri
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last || t != 0) return;
+    if (!last) return;
     __threadfence();
+    // the block partials are loaded by the whole block, a tile of ES_THREADS blocks at a time,
+    // and merged by thread 0 in block order
+    __shared__ double pp[ES_THREADS][4];
     double S = 0.0, Sc = 0.0, Q = 0.0, Qc = 0.0;
-    for (int b = 0; b < (int)gridDim.x; b++) {
-        const double *p = part + (size_t)b * 4;
-        two_sum_merge(S, Sc, __ldcg(p), __ldcg(p + 1));
-        two_sum_merge(Q, Qc, __ldcg(p + 2), __ldcg(p + 3));
+    for (int b0 = 0; b0 < (int)gridDim.x; b0 += ES_THREADS) {
+        const int nb = min(ES_THREADS, (int)gridDim.x - b0);
+        if (t < nb) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) pp[t][q] = __ldcg(part + (size_t)(b0 + t) * 4 + q);
+        }
+        __syncthreads();
+        if (t == 0)
+            for (int b = 0; b < nb; b++) {
+                two_sum_merge(S, Sc, pp[b][0], pp[b][1]);
+                two_sum_merge(Q, Qc, pp[b][2], pp[b][3]);
+            }
+        __syncthreads();
     }
+    if (t != 0) return;
     scal[S_EMEAN] = (S + Sc) / (double)n;
     scal[S_ESQ] = (Q + Qc) / (double)n;
     *ticket = 0;
@@ -180,10 +193,19 @@ __global__ void __launch_bounds__(ES_THREADS) k_ess_mb(const double *__restrict_
         for (int t = 0; t <= ES_LAGS; t++)
             if (t <= T1 && e < (K - t) * C) g[t] += a * (E[e + t * C] - mean);
     }
+    // block sums of the lag products through shared memory (an FP64 butterfly per lag costs
+    // 16 cycles per warp add on this GPU's FP64 pipe): thread (lag, seg) sums 32 threads'
+    // products, then one thread per lag sums the eight segments, both in a fixed order
+    __shared__ double gs[ES_LAGS + 1][ES_THREADS + 1];
 #pragma unroll
-    for (int t = 0; t <= ES_LAGS; t++) {
-        const double v = warp_sum(g[t]);
-        if (lane == 0) red[w][t] = v;
+    for (int t = 0; t <= ES_LAGS; t++) gs[t][t0] = g[t];
+    __syncthreads();
+    if (t0 < (ES_LAGS + 1) * 8) {
+        const int lag = t0 >> 3, seg = t0 & 7;
+        double v = 0.0;
+#pragma unroll 8
+        for (int q = 0; q < 32; q++) v += gs[lag][32 * seg + q];
+        red[seg][lag] = v;
     }
     __syncthreads();
     if (t0 <= ES_LAGS) {
@@ -198,11 +220,24 @@ __global__ void __launch_bounds__(ES_THREADS) k_ess_mb(const double *__restrict_
     if (!last) return;
     __threadfence();
     // gamma(t) in block order; the window over t <= T1
+    // the block partials loaded by the whole block (a tile of blocks at a time, into gs),
+    // summed per lag in block order
     __shared__ double gam[ES_LAGS + 1];
-    if (t0 <= T1) {
+    {
+        constexpr int TB = ES_THREADS;                       // blocks per tile: gs holds [lag][block]
         double v = 0.0;
-        for (int b = 0; b < (int)gridDim.x; b++) v += __ldcg(gpart + (size_t)b * (ES_LAGS + 1) + t0);
-        gam[t0] = v / (double)((K - t0) * C);
+        for (int b0 = 0; b0 < (int)gridDim.x; b0 += TB) {
+            const int nb = min(TB, (int)gridDim.x - b0);
+            for (int e = t0; e < nb * (ES_LAGS + 1); e += ES_THREADS) {
+                const int b = e / (ES_LAGS + 1), lag = e % (ES_LAGS + 1);
+                gs[lag][b] = __ldcg(gpart + (size_t)(b0 + b) * (ES_LAGS + 1) + lag);
+            }
+            __syncthreads();
+            if (t0 <= T1)
+                for (int b = 0; b < nb; b++) v += gs[t0][b];
+            __syncthreads();
+        }
+        if (t0 <= T1) gam[t0] = v / (double)((K - t0) * C);
     }
     __syncthreads();
     __shared__ double s_tau;
@@ -288,15 +323,28 @@ __global__ void k_col_part(const double *__restrict__ O, int Ns, long P, const d
     __shared__ double a[8][33], b[8][33];
     const long k = (long)blockIdx.x * 32 + threadIdx.x;
     const int r0 = blockIdx.y * rows_per, r1 = min(Ns, r0 + rows_per);
-    double s = 0.0, se = 0.0;
-    if (k < P)
-        for (int i = r0 + threadIdx.y; i < r1; i += 8) {
-            const double g = O[(size_t)i * P + k];
-            s += g;
-            if (E) se += g * E[i];
+    // four rows' loads in flight per thread, four partial sums merged in a fixed order
+    double s[4] = {0.0, 0.0, 0.0, 0.0}, se[4] = {0.0, 0.0, 0.0, 0.0};
+    if (k < P) {
+        int i = r0 + threadIdx.y;
+        for (; i + 24 < r1; i += 32) {
+            double g[4];
+#pragma unroll
+            for (int h = 0; h < 4; h++) g[h] = O[(size_t)(i + 8 * h) * P + k];
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                s[h] += g[h];
+                if (E) se[h] += g[h] * E[i + 8 * h];
+            }
         }
-    a[threadIdx.y][threadIdx.x] = s;
-    b[threadIdx.y][threadIdx.x] = se;
+        for (; i < r1; i += 8) {
+            const double g = O[(size_t)i * P + k];
+            s[0] += g;
+            if (E) se[0] += g * E[i];
+        }
+    }
+    a[threadIdx.y][threadIdx.x] = (s[0] + s[1]) + (s[2] + s[3]);
+    b[threadIdx.y][threadIdx.x] = (se[0] + se[1]) + (se[2] + se[3]);
     __syncthreads();
     if (threadIdx.y == 0 && k < P) {
         double S = 0.0, SE = 0.0;
@@ -313,8 +361,23 @@ __global__ void k_col_fin(const double *__restrict__ part, int nchunk, int Ns, l
                           double *gm, double *F) {
     const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P) return;
+    // eight chunks' loads in flight, summed in chunk order
     double S = 0.0, SE = 0.0;
-    for (int c = 0; c < nchunk; c++) {
+    int c = 0;
+    for (; c + 7 < nchunk; c += 8) {
+        double ps[8], pe[8];
+#pragma unroll
+        for (int h = 0; h < 8; h++) {
+            ps[h] = part[(size_t)(c + h) * 2 * P + k];
+            pe[h] = part[(size_t)(c + h) * 2 * P + P + k];
+        }
+#pragma unroll
+        for (int h = 0; h < 8; h++) {
+            S += ps[h];
+            SE += pe[h];
+        }
+    }
+    for (; c < nchunk; c++) {
         S += part[(size_t)c * 2 * P + k];
         SE += part[(size_t)c * 2 * P + P + k];
     }
