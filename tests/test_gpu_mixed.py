@@ -129,3 +129,55 @@ def test_mixed_blocked_substitution_large(nqs):
     assert st.refine_residual < 1e-8
     assert 0 <= st.delta_rel_err < 1e-7
     assert st.phase_us[3] < 1.0               # no explicit triangular inverse (microseconds)
+
+
+@pytest.mark.parametrize("fp32_estimator", [0, 1])
+def test_pipelined_factor_breakdown_falls_back_to_fp64(nqs, fp32_estimator):
+    """A negative diagonal shift breaks the FP32 factor of the 1120 x 1120 parameter-space
+    system, which runs the pipelined factor (64-wide blocks on every SM): CTA 0 records the
+    failing column and raises its flag, the other CTAs leave at their next wait, and the step
+    is solved again in FP64, which breaks down as well (upstream retry semantics: update 0,
+    converged 0), as the FP64 step on the same samples does.  Nothing waits out a budget:
+    the call returns normally and the next regular step converges."""
+    from spin_based_neural_network_gb300 import abi
+    Lx = Ly = 4
+    N, M = 16, 32
+    def make(shift):
+        cfg = abi.config_defaults(ansatz=abi.ANSATZ_COMPLEX_RBM, rbm_hidden_units=M, rbm_init_scale=0.3,
+                                  hamiltonian=1, rng_seed=4242, sr_diag_shift=shift, learning_rate=0.005)
+        a = nqs.Ansatz(cfg, N)
+        return cfg, a, nqs.Marshall(a.log_amp_fn, a.user, Lx, Ly)
+    rng = np.random.default_rng(12)
+    batch = np.stack([rng.permutation(np.array([1, -1] * 8, np.int32)) for _ in range(4096)])
+    cfg, a, m = make(-2.0)
+    p0 = a.params.copy()
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=3, gram_passes=3,
+                    fp32_estimator=fp32_estimator, mixed_space=abi.SPACE_PARAMETERS)
+    try:
+        info, E, delta = nqs.sr_step_batch(cfg, Lx, Ly, a, batch, minsr=True, log_amp_fn=m.log_amp_fn,
+                                           user=m.user)
+        st = nqs.last_step_stats()
+    finally:
+        nqs.set_options()
+    assert st.mixed_fallback == 1
+    assert info.converged == 0 and info.update_norm == 0.0
+    assert np.array_equal(a.params, p0)
+    cfg2, a2, m2 = make(-2.0)
+    nqs.set_options(square_pbc=1, fp32_estimator=0)
+    try:
+        info2, E2, delta2 = nqs.sr_step_batch(cfg2, Lx, Ly, a2, batch, minsr=True, log_amp_fn=m2.log_amp_fn,
+                                              user=m2.user)
+    finally:
+        nqs.set_options()
+    assert info2.converged == 0 and info2.update_norm == 0.0
+    # the next regular step (positive shift) runs the pipelined factor normally
+    cfg3, a3, m3 = make(1e-4)
+    nqs.set_options(square_pbc=1, precision=abi.PREC_MIXED, refine_sweeps=3, gram_passes=3,
+                    fp32_estimator=fp32_estimator, mixed_space=abi.SPACE_PARAMETERS)
+    try:
+        info3, E3, delta3 = nqs.sr_step_batch(cfg3, Lx, Ly, a3, batch, minsr=True, log_amp_fn=m3.log_amp_fn,
+                                              user=m3.user)
+        st3 = nqs.last_step_stats()
+    finally:
+        nqs.set_options()
+    assert info3.converged == 1 and st3.mixed_fallback == 0 and st3.refine_residual < 1e-8
