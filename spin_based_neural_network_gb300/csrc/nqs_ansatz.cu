@@ -282,8 +282,10 @@ bool ansatz_refresh_derived(Ansatz *a) {
     }
     long work = a->kind == KIND_MLP ? (long)a->M * a->N + (long)a->M * mlp32_pitch(a->M) : (long)a->M * a->N;
     NQS_LAUNCH("derive_weights");
-    k_derive<<<(unsigned)((work + 255) / 256), 256, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
-                                                                        a->d_wti.p, a->d_f32.p, a->d_cs64.p);
+    // 64-thread blocks: the tables' FP64 cosh / sinh / sincos are FP64-pipe work (2 FMAs per
+    // clock per SM on this GPU), so the weights are spread over as many SMs as they fill
+    k_derive<<<(unsigned)((work + 63) / 64), 64, 0, ctx().stream>>>(ansatz_dev(a), a->d_wtr.p,
+                                                                     a->d_wti.p, a->d_f32.p, a->d_cs64.p);
     return NQS_CUDA(cudaGetLastError());
 }
 
