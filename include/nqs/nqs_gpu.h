@@ -281,8 +281,10 @@ int nqs_gpu_tvmc_step_batch(const nqs_config_t *cfg, double dt, int size_x, int 
  * already in place when the pool takes the remainder.  The first call on a
  * device (and the first after a cudaDeviceReset, which gives the device a new
  * context and a new copy of the array) looks up that array's device address
- * (cudaGetSymbolAddress) with the device current; make that first call before
- * any stream capture.  Every call reuses the same array and it keeps the last
+ * (cudaGetSymbolAddress) with the device current.  Every call blocks the host
+ * until its result is ready (it synchronises `stream` and copies the status and
+ * info to host memory), so it is never called on a stream that is being captured
+ * into a graph.  Every call reuses the same array and it keeps the last
  * call's contents, so calls that overlap on the GPU (other streams, other host
  * threads) race and must be serialised by the caller. */
 int nqs_gpu_minsr_solve_noalloc(const double *d_O, const double *d_E,
