@@ -271,17 +271,20 @@ static int df_chunk_rows(int Ns) { return std::max(8, (Ns + ctx().sm_count - 1) 
 //            CTA forms 64 x 64 tiles of the panel U_k = X_kk A_k^T (stored as L^T in
 //            the unused upper triangle of T), then 128 x 128 tensor-core tiles of the
 //            trailing update A -= U_k^T U_k (lower triangle), while the owner updates
-//            and factors the next diagonal block (look-ahead);
+//            and factors the next diagonal block (look-ahead); with 64-wide blocks on
+//            four CTAs or more the owner runs a whole step ahead of the others, bound to
+//            them by flags instead of grid barriers (the pipelined factor in fr_body);
 //   inverse  L^{-1} beside the factor, by block rows: in the panel phase of step k
 //            row block k of X = L^{-1} is X_kk R_k (R = I - L X over the eliminated
 //            columns, accumulated in Li), in the trailing phase the rows below take
 //            R -= L_{:,k} X_k on the tensor cores; L^{-1} is kept row-major (Li) and
 //            transposed (LiT) so both triangular solves are row GEMVs;
-//   refine   preconditioned CG on the exact operator in FP64 (two passes over O_c
-//            per product), preconditioner L^{-T} L^{-1} in FP32.
-// Phases are separated by a grid barrier on a generation word with a bounded
-// spin budget; on timeout it raises *err and every CTA leaves at its next
-// barrier.  Data written by other CTAs is read with L1-bypassing loads.
+//   refine   preconditioned CG on the exact operator (two passes over O_c per product:
+//            double-float arithmetic on the FP32 pipe in parameter space, FP64 otherwise),
+//            preconditioner L^{-T} L^{-1} in FP32.
+// Phases are separated by a grid barrier on a monotonic arrival counter with a bounded
+// spin budget; on timeout it raises *err and every CTA leaves at its next barrier.
+// Data written by other CTAs is read with L1-bypassing loads.
 constexpr int BT = 128;                              // shared-memory tile of the diagonal block
 // Diagonal block width BD (a template parameter of the factor; chosen per
 // system): 64 below BD_SWITCH, where the sequential chain of diagonal blocks
