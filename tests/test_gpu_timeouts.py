@@ -1,8 +1,9 @@
 """The bounded-wait paths of the cooperative solve kernels, exercised on purpose.
 
 Every grid-wide barrier of the mixed MinSR factor / refinement kernel and of the CG-SR
-kernel polls a bounded number of times (nqs_gpu_set_barrier_budget; 2^24 by default) and
-then raises the kernel's error word instead of waiting on.  These tests lower the budget to
+kernel, and every flag wait between the pipelined factor's first CTA and the others, polls a
+bounded number of times (nqs_gpu_set_barrier_budget; 2^24 by default) and then raises the
+kernel's error word instead of waiting on.  These tests lower the budget to
 one poll, so the CTAs that reach a barrier first give up while the others are still on
 their way: the step must return -1 with "grid barrier timed out", leave the parameters
 untouched, and the next call, with the default budget again, must succeed and give the
