@@ -46,20 +46,26 @@ __global__ void k_center_split(double *O, int Ns, long P, const double *__restri
 
 // ---------------------------------------------------------------- tensor-core Gram
 constexpr int TC_M = 128, TC_N = 128, TC_K = 32;      // tile; K per stage = 128 B of FP32
+static_assert(TC_M == TC_N, "operand tiles of both sides share one layout");
 constexpr int TC_STAGES = 3;
-constexpr int TC_STAGE_BYTES = (TC_M + TC_N) * TC_K * 4;
+constexpr int TC_TILE_BYTES = TC_M * TC_K * 4;       // one operand tile of one K stage (16 KB)
+constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;    // rows i: hi, lo; rows j: hi, lo
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
 
 struct GramTcArgs {
-    int kt_per_seg;       // K tiles per segment
-    int nseg;             // passes: 1 = hi hi^T, 3 = hi hi^T + hi lo^T + lo hi^T
+    int kt_total;         // K tiles of the whole reduction
+    int kt_per_seg;       // K tiles per CTA: kt_total, or a third of it in a split launch
+    int nseg;             // products: 1 = hi hi^T, 3 = hi hi^T + hi lo^T + lo hi^T
     float scale, shift;
     float *C;             // [n][n] lower triangle written
     int n;
     int *err;
-    int split;            // 1: blockIdx.y = pass, raw partial sums into C + pass * n * n
+    int split;            // 1: blockIdx.y = K segment, raw partial sums into C + segment * n * n
 };
 
+// One 128 x 128 lower-triangular tile of hi hi^T (+ hi lo^T + lo hi^T) per CTA.  Each K stage
+// brings the hi and lo words of both row blocks once (one pair when the tile is diagonal) and
+// all products of the stage accumulate into one FP32 TMEM accumulator.
 __global__ void __launch_bounds__(128, 1)
 k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
                GramTcArgs g) {
@@ -100,27 +106,30 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int total = g.split ? g.kt_per_seg : g.kt_per_seg * g.nseg;
+    const int kt0 = g.split ? (int)blockIdx.y * g.kt_per_seg : 0;
+    const int total = max(0, min(g.kt_total, kt0 + g.kt_per_seg) - kt0);
+    const bool three = g.nseg >= 3, diag = bi == bj;
     bool ok = true;
 
     if (warp == 0 && lane == 0) {
-        // TMA producer
+        // TMA producer: stage layout [rows i hi][rows i lo][rows j hi][rows j lo]
+        const uint32_t tx = (uint32_t)TC_TILE_BYTES * (three ? 2u : 1u) * (diag ? 1u : 2u);
         for (int it = 0; it < total && ok; it++) {
             int s = it % TC_STAGES, u = it / TC_STAGES;
             if (u > 0) ok = mbar_wait(&empty[s], (u - 1) & 1, g.err);
             if (!ok) break;
-            const int seg = g.split ? (int)blockIdx.y : it / g.kt_per_seg;
-            const int kt = g.split ? it : it - seg * g.kt_per_seg;
-            const CUtensorMap *ma = seg == 2 ? &map_lo : &map_hi;   // segments: (hi,hi) (hi,lo) (lo,hi)
-            const CUtensorMap *mb = seg == 1 ? &map_lo : &map_hi;
+            const int kc = (kt0 + it) * TC_K;
             uint8_t *sa = sm + s * TC_STAGE_BYTES;
-            uint8_t *sb = sa + TC_M * TC_K * 4;
-            mbar_expect_tx(&full[s], TC_STAGE_BYTES);
-            tma_load_2d(sa, ma, &full[s], kt * TC_K, bi * TC_M);
-            tma_load_2d(sb, mb, &full[s], kt * TC_K, bj * TC_N);
+            mbar_expect_tx(&full[s], tx);
+            tma_load_2d(sa, &map_hi, &full[s], kc, bi * TC_M);
+            if (three) tma_load_2d(sa + TC_TILE_BYTES, &map_lo, &full[s], kc, bi * TC_M);
+            if (!diag) {
+                tma_load_2d(sa + 2 * TC_TILE_BYTES, &map_hi, &full[s], kc, bj * TC_N);
+                if (three) tma_load_2d(sa + 3 * TC_TILE_BYTES, &map_lo, &full[s], kc, bj * TC_N);
+            }
         }
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer: M = N = 128, K = 8 per instruction, 4 per stage
+    } else if (warp == 1 && lane == 0 && total > 0) {
+        // MMA issuer: M = N = 128, K = 8 per instruction, 4 per stage and product
         const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
                                ((uint32_t)(TC_M >> 4) << 24);
         for (int it = 0; it < total && ok; it++) {
@@ -128,25 +137,37 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
             ok = mbar_wait(&full[s], u & 1, g.err);
             if (!ok) break;
             tc_fence_after();
-            uint32_t sa = smem_u32(sm + s * TC_STAGE_BYTES);
-            uint32_t sb = sa + TC_M * TC_K * 4;
+            const uint32_t ah = smem_u32(sm + s * TC_STAGE_BYTES), al = ah + TC_TILE_BYTES;
+            const uint32_t bh = diag ? ah : ah + 2 * TC_TILE_BYTES, bl = diag ? al : ah + 3 * TC_TILE_BYTES;
 #pragma unroll
             for (int k = 0; k < TC_K / 8; k++)
-                umma_tf32(tmem, sw128_desc(sa + k * 32), sw128_desc(sb + k * 32), idesc,
+                umma_tf32(tmem, sw128_desc(ah + k * 32), sw128_desc(bh + k * 32), idesc,
                           (it > 0 || k > 0) ? 1u : 0u);
+            if (three) {
+#pragma unroll
+                for (int k = 0; k < TC_K / 8; k++) {
+                    umma_tf32(tmem, sw128_desc(ah + k * 32), sw128_desc(bl + k * 32), idesc, 1u);
+                    umma_tf32(tmem, sw128_desc(al + k * 32), sw128_desc(bh + k * 32), idesc, 1u);
+                }
+            }
             umma_commit(&empty[s]);
         }
         umma_commit(done);
     }
     __syncwarp();
-    // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31
-    bool ready = mbar_wait(done, 0, g.err);
+    // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w+31; an empty K segment writes zeros
+    bool ready = total > 0 ? mbar_wait(done, 0, g.err) : true;
     tc_fence_after();
     if (ready) {
         const int row = bi * TC_M + warp * 32 + lane;
         for (int c = 0; c < TC_N / 32; c++) {
             float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+            if (total > 0) {
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; j++) v[j] = 0.f;
+            }
             int col0 = bj * TC_N + c * 32;
             if (row < g.n && g.split) {
                 float *dst = g.C + (size_t)blockIdx.y * g.n * g.n + (size_t)row * g.n;
@@ -173,7 +194,7 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
 }
 
 // T = scale ((P0 + P1) + P2) + shift I on the lower triangle, from the three
-// per-pass partial Grams of a split launch.
+// K-segment partial Grams of a split launch.
 __global__ void k_gram_sum(const float *__restrict__ Pp, int n, float scale, float shift, float *T) {
     const size_t nn = (size_t)n * n;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
@@ -292,6 +313,8 @@ constexpr int BT = 128;                              // shared-memory tile of th
 constexpr int BD_SMALL = 64, BD_LARGE = 128, BD_SWITCH = 4096;
 static_assert(BD_SMALL % 64 == 0 && BD_LARGE <= BT, "diagonal blocks are multiples of the 64-wide GEMM tile");
 constexpr int PS_THREADS = 256;
+constexpr int DF_G = 9;           // four-column groups per lane in flight in a row dot of the operator
+constexpr int DF_SEGS = 4;        // row segments of a chunk at most in the operator's column sums
 constexpr int PS_SMEM = 2 * BT * (BT + 1) * 4;       // two 128 x 129 float tiles
 constexpr int GT = 64, GKC = 32;                     // GEMM tile and K chunk
 constexpr int RCH = 64;                              // rows per partial column sum
@@ -1663,10 +1686,11 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     // q = O_c^T (O_c v) / N_s + shift v, or the right-hand side O_c^T eps / N_s, from the
     // double-float words of O_c (oh + ol) with v split likewise (vh + vl).  The rows of O_c
     // are cut into chunks of DF_ROWS, dealt to the CTAs in turn: a warp forms u_i = o_i . v
-    // for one row of the chunk at a time (double-float butterfly over the lanes), then every
-    // thread accumulates sum_i u_i o_i over the chunk for its four-column groups (eight
-    // rows' loads in flight); after one grid barrier the chunks' partial column sums are
-    // summed in FP64 in chunk order (eight warps over the chunks, then the warps in order).
+    // for one row of the chunk at a time (double-float butterfly over the lanes), then the
+    // threads accumulate sum_i u_i o_i over segments of the chunk's rows for four-column
+    // groups (eight rows' loads in flight) and the segments are added in double-float; after
+    // one grid barrier the chunks' partial column sums are summed in FP64 in a fixed order
+    // (eight columns per CTA, 32 slots of chunks per column, five loads in flight).
     // The chunking does not depend on the grid size (a.df_rows comes from N_s and the SM
     // count), so a system solved by a slice of a batch launch gets the same bits as by the
     // whole grid, and at full grid every CTA has one chunk.
@@ -1674,7 +1698,7 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
     __shared__ double redc[PS_THREADS / 32][32];
     const int ndc = (Ns + DF_ROWS - 1) / DF_ROWS;
     const bool df_op = a.space == 1 && a.oh != nullptr && df_words_ok(P) && DF_ROWS > 0 &&
-                       8 * P + 8 * (long)DF_ROWS <= PS_SMEM;
+                       8 * P + 8 * (long)DF_ROWS + 8 * (long)DF_SEGS * P <= PS_SMEM;
     // With zs set, v is the CG direction formed on the fly by every CTA, v = zs (pold null) or
     // zs + beta pold, and written to pnew by one CTA per 256 entries (so no grid barrier
     // publishes it first).
@@ -1698,6 +1722,7 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
         __syncthreads();
         const float4 *oh4 = (const float4 *)a.oh, *ol4 = (const float4 *)a.ol;
         const float4 *vh4 = (const float4 *)vh, *vl4 = (const float4 *)vl;
+        float2 *cs = (float2 *)(ul + DF_ROWS);          // per row segment: column sums (hi, lo)
         for (int ch = bx; ch < ndc; ch += G) {
             const int i0 = ch * DF_ROWS, nr = min(Ns, i0 + DF_ROWS) - i0;
             if (rhs_mode) {
@@ -1706,17 +1731,18 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
                 for (int r = warp; r < nr; r += PS_THREADS / 32) {
                     const size_t rb = (size_t)(i0 + r) * P4;
                     float sh0 = 0.f, sl0 = 0.f, sh1 = 0.f, sl1 = 0.f;
-                    for (long g0 = lane; g0 < P4; g0 += 32 * 8) {
-                        // eight groups' loads in flight per lane before their products
-                        float4 xh[8], xl[8];
+                    for (long g0 = lane; g0 < P4; g0 += 32 * DF_G) {
+                        // DF_G groups' loads in flight per lane before their products (a whole
+                        // row of up to 32 DF_G groups in one batch)
+                        float4 xh[DF_G], xl[DF_G];
 #pragma unroll
-                        for (int t = 0; t < 8; t++) {
+                        for (int t = 0; t < DF_G; t++) {
                             const long g = g0 + 32 * t;
                             xh[t] = g < P4 ? __ldcg(oh4 + rb + g) : make_float4(0.f, 0.f, 0.f, 0.f);
                             xl[t] = g < P4 ? __ldcg(ol4 + rb + g) : make_float4(0.f, 0.f, 0.f, 0.f);
                         }
 #pragma unroll
-                        for (int t = 0; t < 8; t++) {
+                        for (int t = 0; t < DF_G; t++) {
                             const long g = g0 + 32 * t;
                             if (g < P4) {
                                 const float4 yh = vh4[g], yl = vl4[g];
@@ -1738,64 +1764,94 @@ __device__ __forceinline__ void fr_body(const FrArgs &a, const int bx, const int
                 }
             }
             __syncthreads();
-            for (long g = tid; g < P4; g += PS_THREADS) {
+            // sum_i u_i o_i over the chunk: items (four-column group g, row segment h), with the
+            // number of segments H chosen from P and the chunk's rows only, so that the threads'
+            // rounds times each item's batches of eight rows is least (P = 1120, 27 rows: four
+            // segments of seven rows, five rounds of one batch)
+            int H = 1;
+            {
+                long best = 0;
+                for (int hh = 1; hh <= DF_SEGS; hh++) {
+                    const long cost = (P4 * hh + PS_THREADS - 1) / PS_THREADS * (((nr + hh - 1) / hh + 7) / 8);
+                    if (hh == 1 || cost < best) {
+                        best = cost;
+                        H = hh;
+                    }
+                }
+            }
+            const int seg = (nr + H - 1) / H;
+            for (long it = tid; it < P4 * H; it += PS_THREADS) {
+                const long g = it % P4;
+                const int h = (int)(it / P4), r1 = min(nr, (h + 1) * seg);
                 float chh[4] = {0.f, 0.f, 0.f, 0.f}, cll[4] = {0.f, 0.f, 0.f, 0.f};
-                int r = 0;
-                for (; r + 7 < nr; r += 8) {
+                for (int r = h * seg; r < r1; r += 8) {
+                    const int cnt = min(8, r1 - r);
                     float4 xh[8], xl[8];
 #pragma unroll
                     for (int t = 0; t < 8; t++) {
-                        xh[t] = __ldcg(oh4 + (size_t)(i0 + r + t) * P4 + g);
-                        xl[t] = __ldcg(ol4 + (size_t)(i0 + r + t) * P4 + g);
+                        xh[t] = t < cnt ? __ldcg(oh4 + (size_t)(i0 + r + t) * P4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        xl[t] = t < cnt ? __ldcg(ol4 + (size_t)(i0 + r + t) * P4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
 #pragma unroll
                     for (int t = 0; t < 8; t++) {
-                        const float wh = uh[r + t], wl = ul[r + t];
-                        df_fma(chh[0], cll[0], xh[t].x, xl[t].x, wh, wl);
-                        df_fma(chh[1], cll[1], xh[t].y, xl[t].y, wh, wl);
-                        df_fma(chh[2], cll[2], xh[t].z, xl[t].z, wh, wl);
-                        df_fma(chh[3], cll[3], xh[t].w, xl[t].w, wh, wl);
+                        if (t < cnt) {
+                            const float wh = uh[r + t], wl = ul[r + t];
+                            df_fma(chh[0], cll[0], xh[t].x, xl[t].x, wh, wl);
+                            df_fma(chh[1], cll[1], xh[t].y, xl[t].y, wh, wl);
+                            df_fma(chh[2], cll[2], xh[t].z, xl[t].z, wh, wl);
+                            df_fma(chh[3], cll[3], xh[t].w, xl[t].w, wh, wl);
+                        }
                     }
                 }
-                for (; r < nr; r++) {
-                    const float4 xh = __ldcg(oh4 + (size_t)(i0 + r) * P4 + g),
-                                 xl = __ldcg(ol4 + (size_t)(i0 + r) * P4 + g);
-                    const float wh = uh[r], wl = ul[r];
-                    df_fma(chh[0], cll[0], xh.x, xl.x, wh, wl);
-                    df_fma(chh[1], cll[1], xh.y, xl.y, wh, wl);
-                    df_fma(chh[2], cll[2], xh.z, xl.z, wh, wl);
-                    df_fma(chh[3], cll[3], xh.w, xl.w, wh, wl);
-                }
 #pragma unroll
-                for (int c = 0; c < 4; c++) a.upart[(size_t)ch * P + 4 * g + c] = (double)chh[c] + (double)cll[c];
+                for (int c = 0; c < 4; c++) cs[(size_t)h * P + 4 * g + c] = make_float2(chh[c], cll[c]);
             }
-            __syncthreads();                                // uh / ul are refilled for the next chunk
+            __syncthreads();
+            for (long k = tid; k < P; k += PS_THREADS) {
+                float sh = cs[k].x, sl = cs[k].y;
+                for (int h = 1; h < H; h++) df_add(sh, sl, cs[(size_t)h * P + k].x, cs[(size_t)h * P + k].y);
+                a.upart[(size_t)ch * P + k] = (double)sh + (double)sl;
+            }
+            __syncthreads();                                // uh / ul / cs are refilled for the next chunk
         }
         if (!grid_barrier(a.bar, a.err, G)) return false;
-        const long ncg = (P + 31) / 32;
-        for (long cg = bx; cg < ncg; cg += G) {
-            const long k = cg * 32 + lane;
-            double s4[4] = {0.0, 0.0, 0.0, 0.0};
+        // the chunks' partials, summed in FP64 for eight columns per CTA: thread (warp, lane)
+        // takes column 8 cg + (lane & 7) of chunks s, s + 32, ... (s = 4 warp + lane / 8, five
+        // loads in flight), then warp 0 adds the 32 slots of each column in a fixed order
+        const long nc8 = (P + 7) / 8;
+        for (long cg = bx; cg < nc8; cg += G) {
+            const long k = cg * 8 + (lane & 7);
+            const int s0 = warp * 4 + (lane >> 3);
+            double acc = 0.0;
             if (k < P) {
-                int b = warp;
-                for (; b + 24 < ndc; b += 32) {
+                for (int b0 = s0; b0 < ndc; b0 += 32 * 5) {
+                    double t5[5];
 #pragma unroll
-                    for (int h = 0; h < 4; h++) s4[h] += __ldcg(a.upart + (size_t)(b + 8 * h) * P + k);
+                    for (int j = 0; j < 5; j++) {
+                        const int b = b0 + 32 * j;
+                        t5[j] = b < ndc ? __ldcg(a.upart + (size_t)b * P + k) : 0.0;
+                    }
+                    acc += (t5[0] + t5[1]) + ((t5[2] + t5[3]) + t5[4]);
                 }
-                for (; b < ndc; b += 8) s4[0] += __ldcg(a.upart + (size_t)b * P + k);
             }
-            redc[warp][lane] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+            redc[warp][lane] = acc;
             __syncthreads();
-            if (warp == 0 && k < P) {
+            if (warp == 0) {
+                // lane: column lane & 7, slots 4 w + lane / 8 for w = 0..7; then across the four
                 double t = 0.0;
 #pragma unroll
                 for (int w = 0; w < PS_THREADS / 32; w++) t += redc[w][lane];
-                t /= (double)Ns;
-                if (rhs_mode) {
-                    q[k] = t;
-                    a.rf[k] = (float)t;
-                } else {
-                    q[k] = t + a.shift * __ldcg((zs ? pnew : v) + k);
+                t += __shfl_xor_sync(0xffffffffu, t, 8);
+                t += __shfl_xor_sync(0xffffffffu, t, 16);
+                const long kk = cg * 8 + lane;
+                if (lane < 8 && kk < P) {
+                    t /= (double)Ns;
+                    if (rhs_mode) {
+                        q[kk] = t;
+                        a.rf[kk] = (float)t;
+                    } else {
+                        q[kk] = t + a.shift * __ldcg((zs ? pnew : v) + kk);
+                    }
                 }
             }
             __syncthreads();
@@ -2168,7 +2224,7 @@ struct MixedWs {
 static MixedWs g_mx;
 
 struct MixedPlan {
-    bool split;       // tensor-core Gram with one CTA per (tile, pass)
+    bool split;       // tensor-core Gram with one CTA per (tile, third of K)
     int space;        // 0 samples, 1 parameters
     int n;            // order of the solved system
     long rows_pad;    // Gram operand rows (n padded to TC_M)
@@ -2183,7 +2239,7 @@ static MixedPlan plan_mixed(int Ns, long P, int space_opt, int passes) {
     p.rows_pad = (rows + TC_M - 1) / TC_M * TC_M;
     p.k_pad = (k + TC_K - 1) / TC_K * TC_K;
     const long nt = p.rows_pad / TC_M;
-    p.split = passes >= 3 && 2 * nt * (nt + 1) / 2 <= ctx().sm_count;
+    p.split = nt * (nt + 1) / 2 < ctx().sm_count;       // fewer tiles than SMs: split K in three
     return p;
 }
 
@@ -2246,7 +2302,8 @@ static void enqueue_front(MixedWs &w, const MixedPlan &pl, double *O, const doub
                                                                     df ? w.oh.p : nullptr, df ? w.ol.p : nullptr);
     }
     GramTcArgs g;
-    g.kt_per_seg = (int)(pl.k_pad / TC_K);
+    g.kt_total = (int)(pl.k_pad / TC_K);
+    g.kt_per_seg = pl.split ? (g.kt_total + 2) / 3 : g.kt_total;
     g.nseg = passes >= 3 ? 3 : 1;
     g.scale = (float)(1.0 / (double)Ns);
     g.shift = (float)shift;
@@ -2256,7 +2313,7 @@ static void enqueue_front(MixedWs &w, const MixedPlan &pl, double *O, const doub
     const int nt = (int)(pl.rows_pad / TC_M);
     g.split = pl.split ? 1 : 0;
     if (pl.split) {
-        // few lower-triangular tiles (parameter space): one CTA per tile and pass
+        // few lower-triangular tiles (parameter space): one CTA per tile and third of K
         g.C = w.Tp.p;
         {
             NQS_LAUNCH("gram_tc");
@@ -2843,7 +2900,8 @@ int nqs_gpu_gram_tc(const double *O_host, int Ns, long P, int passes, double sca
     if (!err.ensure(1)) return -1;
     NQS_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
     GramTcArgs g;
-    g.kt_per_seg = (int)(p_pad / TC_K);
+    g.kt_total = (int)(p_pad / TC_K);
+    g.kt_per_seg = g.kt_total;
     g.nseg = passes >= 3 ? 3 : 1;
     g.scale = (float)scale;
     g.shift = 0.f;
