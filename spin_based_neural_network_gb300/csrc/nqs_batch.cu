@@ -104,6 +104,13 @@ __global__ void k_batch_apply(double *params, const double *__restrict__ delta, 
     if (threadIdx.x == 0) scal[S_NORM2] = red[0];
 }
 
+bool enqueue_gated_apply(double *params, const double *delta, long P, double lr, double *scal, const int *mstatus,
+                         const int *merr, const double *mnrm) {
+    NQS_LAUNCH("apply_update");
+    k_batch_apply<<<1, 1024, 0, ctx().stream>>>(params, delta, P, lr, scal, mstatus, merr, mnrm, 0);
+    return NQS_CUDA(cudaGetLastError());
+}
+
 static bool enqueue_front(BatchInst &b, cudaStream_t st) {
     uint64_t *bits = nullptr;
     if (!ansatz_refresh_derived(b.a) || !sampler_produce_dev(b.s, b.Ns, &bits, b.move.p) ||

@@ -17,6 +17,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -234,9 +235,21 @@ constexpr double MIXED_RESID_MAX = 1e-6;
 // space, (O_c^T O_c / N_s + shift I) delta = O_c^T eps / N_s (writes delta and
 // sets *param_space); space_opt 0 picks the smaller system, 1 samples, 2
 // parameters.  *out_fail >= 0 when the FP32 factor broke down.
+// after_launch, when given, is called once the solve is enqueued and before the host waits for
+// it, with the solve's status word, error word and residual norms (device pointers) and
+// whether it solves in parameter space, so that a caller can enqueue work that depends on
+// the solve without a host round trip.
+using MixedAfterLaunch = std::function<bool(const int *status, const int *err, const double *nrm, bool param_space)>;
 bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
                        int passes, int space_opt, double *y, double *delta, bool *param_space, double *out_resid,
-                       int *out_fail);
+                       int *out_fail, const MixedAfterLaunch &after_launch = nullptr);
+
+// theta -= lr delta and ||delta||^2 into scal[S_NORM2] on the library stream, with delta
+// taken as zero when the mixed solve broke down (a non-positive FP32 pivot in status[0], or
+// |r| / |rhs| above MIXED_RESID_MAX from nrm) or its kernels raised the error word
+// (nqs_batch.cu).
+bool enqueue_gated_apply(double *params, const double *delta, long P, double lr, double *scal, const int *mstatus,
+                         const int *merr, const double *mnrm);
 
 // Device scalar block of an SR step (doubles): [0] e_mean [1] e_sq_mean
 // [2] ||delta||^2 [3] rs [4] rs0 [5] pAp [6] alpha [7] u mean [8] tau_int

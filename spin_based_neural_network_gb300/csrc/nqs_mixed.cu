@@ -194,12 +194,16 @@ k_gram_tf32_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant
 }
 
 // T = scale ((P0 + P1) + P2) + shift I on the lower triangle, from the three
-// K-segment partial Grams of a split launch.
+// K-segment partial Grams of a split launch (rows dealt to the blocks, columns c <= r to
+// the threads).
 __global__ void k_gram_sum(const float *__restrict__ Pp, int n, float scale, float shift, float *T) {
     const size_t nn = (size_t)n * n;
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
-        const int r = (int)(e / n), c = (int)(e % n);
-        if (c <= r) T[e] = ((Pp[e] + Pp[nn + e]) + Pp[2 * nn + e]) * scale + (r == c ? shift : 0.f);
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const size_t e0 = (size_t)r * n;
+        for (int c = threadIdx.x; c <= r; c += blockDim.x) {
+            const size_t e = e0 + c;
+            T[e] = ((Pp[e] + Pp[nn + e]) + Pp[2 * nn + e]) * scale + (r == c ? shift : 0.f);
+        }
     }
 }
 
@@ -2320,7 +2324,7 @@ static void enqueue_front(MixedWs &w, const MixedPlan &pl, double *O, const doub
             k_gram_tf32_tc<<<dim3(nt * (nt + 1) / 2, 3), 128, TC_SMEM, st>>>(mh, ml, g);
         }
         NQS_LAUNCH("gram_sum");
-        k_gram_sum<<<ctx().sm_count * 4, 256, 0, st>>>(w.Tp.p, pl.n, g.scale, g.shift, w.T.p);
+        k_gram_sum<<<std::min(pl.n, 65535), 256, 0, st>>>(w.Tp.p, pl.n, g.scale, g.shift, w.T.p);
     } else {
         NQS_LAUNCH("gram_tc");
         k_gram_tf32_tc<<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(mh, ml, g);
@@ -2487,7 +2491,7 @@ static MixedGraph g_mgraph;
 
 bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, long P, double shift, int sweeps,
                        int passes, int space_opt, double *y, double *delta, bool *param_space, double *out_resid,
-                       int *out_fail) {
+                       int *out_fail, const MixedAfterLaunch &after_launch) {
     Context &c = ctx();
     cudaStream_t st = c.stream;
     MixedWs &w = g_mx;
@@ -2536,6 +2540,7 @@ bool minsr_mixed_solve(double *O, const double *gm, const double *eps, int Ns, l
         if (!NQS_CUDA(cudaGraphLaunch(Gr.exec, st))) return false;
         c.launches += Gr.kernels;
     }
+    if (after_launch && !after_launch(w.status.p, err.p, w.nrm.p, pl.space == 1)) return false;
     int hs[2] = {-1, 0};
     double h[3] = {0.0, 0.0, 0.0};
     unsigned long long tns[8] = {};

@@ -317,10 +317,14 @@ __global__ void k_col_stats(const double *__restrict__ O, int Ns, long P, const 
 
 // The same statistics over a 2-D grid: partial column sums over row chunks
 // (32 columns x 8 row groups per block), then a fixed-order sum over the
-// chunks (deterministic).
+// chunks (deterministic).  With tickets (one zeroed word per column group), the
+// last block of each column group to finish (an atomic ticket; no block waits for
+// another) sums the chunks' partials itself and writes the means (and F), so that no
+// second kernel is needed; it sets the ticket back to zero.
 __global__ void k_col_part(const double *__restrict__ O, int Ns, long P, const double *__restrict__ E, int rows_per,
-                           double *part) {
+                           double *part, unsigned *tickets, const double *__restrict__ scal, double *gm, double *F) {
     __shared__ double a[8][33], b[8][33];
+    __shared__ bool last;
     const long k = (long)blockIdx.x * 32 + threadIdx.x;
     const int r0 = blockIdx.y * rows_per, r1 = min(Ns, r0 + rows_per);
     // four rows' loads in flight per thread, four partial sums merged in a fixed order
@@ -355,6 +359,36 @@ __global__ void k_col_part(const double *__restrict__ O, int Ns, long P, const d
         part[(size_t)blockIdx.y * 2 * P + k] = S;
         part[(size_t)blockIdx.y * 2 * P + P + k] = SE;
     }
+    if (!tickets) return;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) last = atomicAdd(tickets + blockIdx.x, 1u) == gridDim.y - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // thread (x, y) sums chunks y, y + 8, ... of column k; the eight sums are added in order of y
+    const int nchunk = (int)gridDim.y;
+    double S = 0.0, SE = 0.0;
+    if (k < P) {
+        for (int c = threadIdx.y; c < nchunk; c += 8) {
+            S += __ldcg(part + (size_t)c * 2 * P + k);
+            SE += __ldcg(part + (size_t)c * 2 * P + P + k);
+        }
+    }
+    a[threadIdx.y][threadIdx.x] = S;
+    b[threadIdx.y][threadIdx.x] = SE;
+    __syncthreads();
+    if (threadIdx.y == 0 && k < P) {
+        double St = 0.0, SEt = 0.0;
+        for (int y = 0; y < 8; y++) {
+            St += a[y][threadIdx.x];
+            SEt += b[y][threadIdx.x];
+        }
+        const double m = St / (double)Ns;
+        gm[k] = m;
+        if (F) F[k] = SEt / (double)Ns - m * scal[S_EMEAN];     // src/nqs/nqs_optimizer.c:213-215
+    }
+    if (threadIdx.x == 0 && threadIdx.y == 0) tickets[blockIdx.x] = 0;
 }
 
 __global__ void k_col_fin(const double *__restrict__ part, int nchunk, int Ns, long P, const double *__restrict__ scal,
@@ -787,13 +821,26 @@ static bool col_stats(const double *O, int Ns, long P, const double *E, const do
     static DevBuf<double> part;
     int rows_per;
     const int gx = (int)((P + 31) / 32), rb = col_chunks(Ns, P, &rows_per);
+    const bool own_part = part_buf == nullptr;
     if (!part_buf) {
         if (!part.ensure((size_t)rb * 2 * P)) return false;
         part_buf = part.p;
     }
     cudaStream_t st = ctx().stream;
-    k_col_part<<<dim3((unsigned)gx, (unsigned)rb), dim3(32, 8), 0, st>>>(O, Ns, P, E, rows_per, part_buf);
-    {
+    // the library's own stream finishes the sums in the partial kernel (tickets zeroed when
+    // allocated and reset by the kernel); callers with their own scratch run the two kernels
+    static DevBuf<unsigned> tickets;
+    unsigned *tk = nullptr;
+    if (own_part) {
+        const size_t n0 = tickets.p ? tickets.n : 0;
+        if (!tickets.ensure((size_t)gx)) return false;
+        if (tickets.n != n0 && !NQS_CUDA(cudaMemsetAsync(tickets.p, 0, sizeof(unsigned) * tickets.n, st)))
+            return false;
+        tk = tickets.p;
+    }
+    k_col_part<<<dim3((unsigned)gx, (unsigned)rb), dim3(32, 8), 0, st>>>(O, Ns, P, E, rows_per, part_buf, tk, scal,
+                                                                         gm, F);
+    if (!tk) {
         NQS_LAUNCH("col_sum");
         k_col_fin<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(part_buf, rb, Ns, P, scal, gm, F);
     }
@@ -1202,6 +1249,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
     NQS_CUDA(cudaMemsetAsync(w.status.p, 0xff, sizeof(int) * 16, st));   // all -1
     dim3 cb(32, 8), cg((unsigned)((P + 31) / 32));
     int converged = 0, cg_iters = 0;
+    bool applied = false;             // update and derived tables already enqueued
     if (in.minsr == 1 || hm) {
         if (!w.T.ensure((size_t)rows * rows) || !w.y.ensure(rows) || !w.z.ensure(rows)) return -1;
         {
@@ -1223,12 +1271,25 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
         ss.delta_rel_err = -1.0;
         bool solved = false, have_delta = false;
         if (mixed) {
-            // centring happens inside the split kernel of the mixed solve
+            // centring happens inside the split kernel of the mixed solve.  In parameter space
+            // the update and the derived tables are enqueued behind the solve before the host
+            // waits for it, with the update taken as zero on the device when the solve broke
+            // down (the FP64 solve below then applies its own)
             double resid = 0.0;
             int f32 = -1;
+            bool pre = false;
+            const double lr_pre = in.custom_scale ? -in.scale : cfg->learning_rate;
+            auto after = [&](const int *mst, const int *merr, const double *mnrm, bool pspace) -> bool {
+                if (in.no_apply || hm || !pspace) return true;
+                if (!enqueue_gated_apply(a->d_params.p, w.delta.p, P, lr_pre, w.scal.p, mst, merr, mnrm) ||
+                    !ansatz_refresh_derived(a))
+                    return false;
+                pre = true;
+                return true;
+            };
             if (!minsr_mixed_solve(w.O.p, w.gm.p, w.eps.p, rows, P, shift, c.opts.refine_sweeps,
                                    c.opts.gram_passes, c.opts.mixed_space, w.y.p, w.delta.p, &have_delta,
-                                   &resid, &f32))
+                                   &resid, &f32, after))
                 return -1;
             ss.refine_residual = resid;
             if (f32 < 0) {
@@ -1236,6 +1297,7 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
                 converged = 1;
                 ss.chol_fail_col = -1;
                 ss.chol_retry = 0;
+                applied = pre;
             } else {
                 ss.mixed_fallback = 1;          // FP32 factor failed: solve this step in FP64
                 have_delta = false;
@@ -1329,13 +1391,14 @@ static int sr_step_impl(const StepIn &in, nqs_sr_step_info_t *info, double *out_
             fprintf(stderr, "nqs_sr cg_solve: Krylov breakdown at iter=%d, pAp=%.3e. Returning "
                             "unconverged partial step.\n", h[I_ITERS], hs[S_PAP]);
     }
-    // 4. update: theta -= lr delta, or theta += scale delta for tVMC
+    // 4. update: theta -= lr delta, or theta += scale delta for tVMC (already enqueued behind a
+    // mixed parameter-space solve that succeeded)
     const double lr_eff = in.custom_scale ? -in.scale : cfg->learning_rate;
-    if (!in.no_apply) {
+    if (!in.no_apply && !applied) {
         NQS_LAUNCH("apply_update");
         k_apply<<<1, 1024, 0, st>>>(a->d_params.p, w.delta.p, P, lr_eff, w.scal.p, w.status.p, 0);
     }
-    if (!NQS_CUDA(cudaGetLastError()) || !ansatz_refresh_derived(a)) return -1;
+    if (!NQS_CUDA(cudaGetLastError()) || (!applied && !ansatz_refresh_derived(a))) return -1;
     double hs[16];
     if (out_E && !NQS_CUDA(cudaMemcpyAsync(out_E, w.E.p, sizeof(double) * Ns, cudaMemcpyDeviceToHost, st)))
         return -1;
