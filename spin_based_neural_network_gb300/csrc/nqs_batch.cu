@@ -84,11 +84,16 @@ __host__ __device__ inline bool mixed_broken(int status, const double *nrm) {
 }
 
 // theta -= lr delta and ||delta||^2, with delta = 0 when the instance's mixed
-// solve broke down or its kernels reported an error.
+// solve broke down or its kernels reported an error (decided by one thread: the
+// test's FP64 division and square root cost 16 cycles per warp instruction on this
+// GPU's FP64 pipe).
 __global__ void k_batch_apply(double *params, const double *__restrict__ delta, long P, double lr, double *scal,
                               const int *mstatus, const int *merr, const double *mnrm, int unconditional) {
     __shared__ double red[1024];
-    const bool zero = !unconditional && (mixed_broken(mstatus[0], mnrm) || merr[0] != 0);
+    __shared__ bool zero_s;
+    if (threadIdx.x == 0) zero_s = !unconditional && (mixed_broken(mstatus[0], mnrm) || merr[0] != 0);
+    __syncthreads();
+    const bool zero = zero_s;
     double s = 0.0;
     for (long k = threadIdx.x; k < P; k += blockDim.x) {
         const double d = zero ? 0.0 : delta[k];
