@@ -322,8 +322,8 @@ def exact_e0(name="heisenberg_4x4_pbc_sz0"):
 # DRAM bytes (read + write) per launch from one ncu capture of the kernel on this
 # workload (dram__bytes_read.sum + dram__bytes_write.sum), and the summary file.
 NCU_TRAFFIC = {
-    "factor_refine": (40.091136e6 + 0.339456e6, "profiles/factor_refine_heisenberg4x4_params1120_full.md"),
-    "gram_tc": (37.775616e6 + 7.168e3, "profiles/gram_tc_split_params1120_ns4096_full.md"),
+    "factor_refine": (40.103424e6 + 0.08704e6, "profiles/factor_refine_heisenberg4x4_params1120_full.md"),
+    "gram_tc": (37.780736e6 + 18.176e3, "profiles/gram_tc_split_params1120_ns4096_full.md"),
 }
 
 # What bounds each kernel whose roofline is reported ("bound" names the pipe the fraction is
@@ -333,7 +333,8 @@ LIMITERS = {
                      "(FP32 SIMT, ~21 us per 64-wide block), then the CG operator passes (double-float "
                      "on the FP32 pipe, L2-latency bound); the trailing and inverse tiles run on the "
                      "tensor cores beside the chain",
-    "gram_tc": "tensor pipe and L2 / HBM operand traffic (TF32 split, three passes)",
+    "gram_tc": "tensor pipe and the TMA operand stream (TF32 hi / lo words of both row blocks per K stage, "
+               "three products per stage)",
     "gram_fp64": "FP64 pipe (SIMT)",
     "chol_syrk": "FP64 pipe (SIMT)",
 }

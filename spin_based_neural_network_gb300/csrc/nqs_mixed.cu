@@ -1,21 +1,24 @@
 // Mixed-precision MinSR solve: tensor-core Gram, FP32 factor, FP64 refinement.
 //
 //   1. centre O in FP64 (in place) and split it into two TF32 words,
-//      O_c = hi + lo (hi = tf32(O_c), lo = tf32(O_c - hi));
+//      O_c = hi + lo (hi = tf32(O_c), lo = tf32(O_c - hi)), and in parameter
+//      space also into two FP32 words (double-float) for the CG operator;
 //   2. T = (hi hi^T + hi lo^T + lo hi^T) / N_s + shift I on the 5th-generation
-//      tensor cores: tcgen05.mma kind::tf32 issued by one thread, operands
-//      staged by TMA (cp.async.bulk.tensor, 128-byte swizzle) in a 3-stage
-//      mbarrier ring, FP32 accumulator in TMEM read back with tcgen05.ld;
-//      only the lower-triangular 128 x 128 tiles are computed;
-//   3. FP32 blocked Cholesky T = L L^T with 128-wide panels and the explicit
-//      inverse L^{-1}, so each triangular solve is one parallel GEMV;
-//   4. iterative refinement in FP64 against the exact operator
-//      A y = O_c (O_c^T y) / N_s + shift y (two FP64 passes over O_c):
-//      y <- y + (L L^T)^{-1} (eps - A y), the correction solved in FP32.
+//      tensor cores: tcgen05.mma kind::tf32 issued by one thread, the hi and lo
+//      words of both row blocks staged by TMA (cp.async.bulk.tensor, 128-byte
+//      swizzle) in a 3-stage mbarrier ring, the three products into one FP32
+//      accumulator in TMEM read back with tcgen05.ld; only the lower-triangular
+//      128 x 128 tiles are computed (K split in three when they are few);
+//   3. FP32 blocked Cholesky T = L L^T with 64- or 128-wide diagonal blocks
+//      (pipelined behind one CTA's chain of diagonal blocks) and the explicit
+//      inverse L^{-1} built beside it, so each triangular solve is a GEMV;
+//   4. FP64-accurate preconditioned CG with M = L L^T against the exact
+//      operator A y = O_c (O_c^T y) / N_s + shift y (FP64, or double-float
+//      words on the FP32 pipe in parameter space), to |r| / |rhs| <= 1e-10.
 // When N_p < N_s the same update is solved in parameter space instead (the
 // push-through identity O^T (O O^T / N_s + s)^{-1} = (O^T O / N_s + s)^{-1} O^T):
 // the Gram is O_c^T O_c / N_s (N_p x N_p), the right-hand side O_c^T eps / N_s,
-// and the refinement operator A d = O_c^T (O_c d) / N_s + shift d.
+// and the CG operator A d = O_c^T (O_c d) / N_s + shift d.
 // The achieved relative residual is returned.
 #include <cuda.h>
 #include <cudaTypedefs.h>
