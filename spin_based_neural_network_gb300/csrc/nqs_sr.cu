@@ -135,22 +135,33 @@ __global__ void __launch_bounds__(ES_THREADS) k_energy_mb(const double *__restri
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // the block partials are loaded by the whole block, a tile of ES_THREADS blocks at a time,
-    // and merged by thread 0 in block order
-    __shared__ double pp[ES_THREADS][4];
+    // the block partials, a tile of ES_THREADS blocks at a time, merged by a TwoSum tree over
+    // the tile (its depth, not the block count, is the chain of dependent FP64 operations),
+    // and the tiles by thread 0 in order
     double S = 0.0, Sc = 0.0, Q = 0.0, Qc = 0.0;
     for (int b0 = 0; b0 < (int)gridDim.x; b0 += ES_THREADS) {
         const int nb = min(ES_THREADS, (int)gridDim.x - b0);
-        if (t < nb) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) pp[t][q] = __ldcg(part + (size_t)(b0 + t) * 4 + q);
+        int w = 1;
+        while (w < nb) w <<= 1;
+        if (t < w) {
+            const bool in = t < nb;
+            ss[t] = in ? __ldcg(part + (size_t)(b0 + t) * 4 + 0) : 0.0;
+            sc[t] = in ? __ldcg(part + (size_t)(b0 + t) * 4 + 1) : 0.0;
+            qs[t] = in ? __ldcg(part + (size_t)(b0 + t) * 4 + 2) : 0.0;
+            qc[t] = in ? __ldcg(part + (size_t)(b0 + t) * 4 + 3) : 0.0;
         }
         __syncthreads();
-        if (t == 0)
-            for (int b = 0; b < nb; b++) {
-                two_sum_merge(S, Sc, pp[b][0], pp[b][1]);
-                two_sum_merge(Q, Qc, pp[b][2], pp[b][3]);
+        for (int o = w / 2; o > 0; o >>= 1) {
+            if (t < o) {
+                two_sum_merge(ss[t], sc[t], ss[t + o], sc[t + o]);
+                two_sum_merge(qs[t], qc[t], qs[t + o], qc[t + o]);
             }
+            __syncthreads();
+        }
+        if (t == 0) {
+            two_sum_merge(S, Sc, ss[0], sc[0]);
+            two_sum_merge(Q, Qc, qs[0], qc[0]);
+        }
         __syncthreads();
     }
     if (t != 0) return;
@@ -202,10 +213,10 @@ __global__ void __launch_bounds__(ES_THREADS) k_ess_mb(const double *__restrict_
     __syncthreads();
     if (t0 < (ES_LAGS + 1) * 8) {
         const int lag = t0 >> 3, seg = t0 & 7;
-        double v = 0.0;
-#pragma unroll 8
-        for (int q = 0; q < 32; q++) v += gs[lag][32 * seg + q];
-        red[seg][lag] = v;
+        double v4[4] = {0.0, 0.0, 0.0, 0.0};          // four chains of eight adds
+#pragma unroll
+        for (int q = 0; q < 32; q++) v4[q & 3] += gs[lag][32 * seg + q];
+        red[seg][lag] = (v4[0] + v4[1]) + (v4[2] + v4[3]);
     }
     __syncthreads();
     if (t0 <= ES_LAGS) {
@@ -233,8 +244,18 @@ __global__ void __launch_bounds__(ES_THREADS) k_ess_mb(const double *__restrict_
                 gs[lag][b] = __ldcg(gpart + (size_t)(b0 + b) * (ES_LAGS + 1) + lag);
             }
             __syncthreads();
-            if (t0 <= T1)
-                for (int b = 0; b < nb; b++) v += gs[t0][b];
+            if (t0 <= T1) {
+                double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;   // four chains, then in order
+                int b = 0;
+                for (; b + 3 < nb; b += 4) {
+                    v0 += gs[t0][b];
+                    v1 += gs[t0][b + 1];
+                    v2 += gs[t0][b + 2];
+                    v3 += gs[t0][b + 3];
+                }
+                for (; b < nb; b++) v0 += gs[t0][b];
+                v += (v0 + v1) + (v2 + v3);
+            }
             __syncthreads();
         }
         if (t0 <= T1) gam[t0] = v / (double)((K - t0) * C);
@@ -249,8 +270,9 @@ __global__ void __launch_bounds__(ES_THREADS) k_ess_mb(const double *__restrict_
         if (!(g0 > 0.0)) {
             done = 1;
         } else {
+            const double r2 = 2.0 / g0;                 // one division for the whole window
             for (int t = 1; t <= T1; t++) {
-                tau += 2.0 * gam[t] / g0;
+                tau += gam[t] * r2;
                 if ((double)t >= 5.0 * tau) {
                     done = 1;
                     break;
