@@ -241,8 +241,8 @@ def headline_config(ws):
     return {"workload": "heisenberg_4x4_pbc_crbm_alpha2_ns4096_minsr", "sites": N_SITES, "hidden": M_HIDDEN,
             "num_params": 2 * (N_SITES + M_HIDDEN + N_SITES * M_HIDDEN), "num_samples": NS, "chains": CHAINS,
             "decorrelate": DECOR, "moves": "nn-exchange, Sz=0", "shift": SHIFT, "lr": LR,
-            "l2": "working set > L2 every step (O 37 MB FP64 + split 37 MB + Gram 67 MB FP32 + factor; "
-                  "FP64 path: Gram 134 MB)",
+            "l2": "working set > L2 every step (O 37 MB FP64 + TF32 split 38 MB + double-float words 37 MB + "
+                  "Gram partials 15 MB + T, L^-1 15 MB; FP64 path: Gram 134 MB)",
             "parallelism": "replicas x%d" % ws}
 
 
